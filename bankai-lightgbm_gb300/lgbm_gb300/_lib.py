@@ -1,0 +1,66 @@
+"""Loader for the GB300 learner library (``lib/libbkgpu.so``).
+
+The library is the product: CUDA kernels for sm_103a plus the C-ABI declared in
+``include/bkgpu.h``. There is no CPU fallback; if the library is missing, ``load()`` raises.
+"""
+import ctypes
+import os
+
+PKG_DIR = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIB_PATH = os.path.join(PKG_DIR, "lib", "libbkgpu.so")
+
+_lib = None
+
+
+def load(build_if_missing: bool = False) -> ctypes.CDLL:
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIB_PATH):
+        if not build_if_missing:
+            raise RuntimeError(
+                "libbkgpu.so is not built (%s); run build_ext.build() first — there is no CPU fallback" % LIB_PATH)
+        import importlib.util
+        spec = importlib.util.spec_from_file_location("bk_build_ext", os.path.join(PKG_DIR, "build_ext.py"))
+        mod = importlib.util.module_from_spec(spec)
+        spec.loader.exec_module(mod)
+        mod.build()
+    lib = ctypes.CDLL(LIB_PATH)
+    _declare(lib)
+    _lib = lib
+    return lib
+
+
+def _declare(lib):
+    c = ctypes
+    P = c.c_void_p
+    i32, i64, u32, f64 = c.c_int32, c.c_int64, c.c_uint32, c.c_double
+    lib.bk_find_bin_numerical.restype = i32
+    lib.bk_find_bin_numerical.argtypes = [P, i64, i64, i32, i32, i32, i32, i32, i32, P, i32, P, P]
+    lib.bk_values_to_group_bins.restype = None
+    lib.bk_values_to_group_bins.argtypes = [P, i64, i64, P, i32, i32, i32, P]
+    if hasattr(lib, "bk_last_error"):
+        lib.bk_last_error.restype = c.c_char_p
+        lib.bk_last_error.argtypes = []
+    for name, res, args in _GPU_SIGNATURES:
+        if hasattr(lib, name):
+            fn = getattr(lib, name)
+            fn.restype = res
+            fn.argtypes = args
+
+
+c = ctypes
+_P, _i32, _i64, _u32, _f64 = c.c_void_p, c.c_int32, c.c_int64, c.c_uint32, c.c_double
+# (name, restype, argtypes) of the learner entry points declared in include/bkgpu.h
+_GPU_SIGNATURES = []
+
+
+def last_error() -> str:
+    lib = load()
+    msg = lib.bk_last_error()
+    return msg.decode() if msg else ""
+
+
+def check(rc: int, what: str = "") -> None:
+    if rc != 0:
+        raise RuntimeError("%s failed: %s" % (what or "bkgpu call", last_error()))

@@ -1,0 +1,173 @@
+"""Host-side dataset construction for the GB300 learner.
+
+The learner consumes a binned dataset: one stored-bin column per inner feature plus each
+feature's bin-mapper facts (num_bin, missing type, default bin, most frequent bin). In
+bankai-lightgbm the host builds this with ``Dataset::from_dense`` (crates/lgbm-core/src/io/
+dataset.rs:904-983) and keeps the bin mappers; this module does the same for dense numerical
+data so the learner can be driven without the Rust host:
+
+* row sample for bin construction — ``create_sample_indices`` (io/sample.rs:11-14) with the
+  LCG ``Random::sample`` (utils/random.rs:52-76);
+* one ``BinMapper::find_bin`` per column (io/bin.rs:342-554), done in C++ by
+  ``bk_find_bin_numerical``;
+* trivial features dropped (io/dataset.rs:389-393); every used feature is its own dense group
+  (dense data never bundles: io/dataset.rs:171-177), stored bins written by
+  ``bk_values_to_group_bins`` (io/dataset.rs:633-685).
+
+Only numerical features are supported.
+"""
+from concurrent.futures import ThreadPoolExecutor
+import ctypes
+import math
+
+import numpy as np
+
+from . import _lib
+
+K_ZERO_THRESHOLD = float(np.float32(1e-35))
+MISSING_NONE, MISSING_ZERO, MISSING_NAN = 0, 1, 2
+
+
+class _Random:
+    """utils/random.rs:7-76 — the MSVC-style LCG used by LightGBM's sampling."""
+
+    def __init__(self, seed: int):
+        self.x = seed & 0xFFFFFFFF
+
+    def _int16(self):
+        self.x = (self.x * 214013 + 2531011) & 0xFFFFFFFF
+        return (self.x >> 16) & 0x7FFF
+
+    def _int32(self):
+        self.x = (self.x * 214013 + 2531011) & 0xFFFFFFFF
+        return self.x & 0x7FFFFFFF
+
+    def next_int(self, lower, upper):
+        return self._int32() % (upper - lower) + lower
+
+    def next_float(self):
+        return np.float32(self._int16()) / np.float32(32768.0)
+
+    def sample(self, n, k):
+        if k > n or k <= 0:
+            return np.zeros(0, dtype=np.int64)
+        if k == n:
+            return np.arange(n, dtype=np.int64)
+        if k > 1 and float(k) > float(n) / math.log2(k):
+            ret = []
+            for i in range(n):
+                prob = (k - len(ret)) / float(n - i)
+                if float(self.next_float()) < prob:
+                    ret.append(i)
+            return np.asarray(ret, dtype=np.int64)
+        s = set()
+        for r in range(n - k, n):
+            v = self.next_int(0, r + 1)
+            if v in s:
+                s.add(r)
+            else:
+                s.add(v)
+        return np.asarray(sorted(s), dtype=np.int64)
+
+
+class FeatureInfo:
+    __slots__ = ("real", "num_bin", "missing_type", "default_bin", "most_freq_bin", "upper_bounds", "penalty",
+                 "min_val", "max_val", "sparse_rate")
+
+    @property
+    def offset(self):
+        return 1 if self.most_freq_bin == 0 else 0
+
+    @property
+    def group_bins(self):
+        """Stored bins of the feature's group: bin 0 holds the most-frequent-bin rows."""
+        return 1 + self.num_bin - self.offset
+
+    def bin_to_value(self, b):
+        return float(self.upper_bounds[b])
+
+
+class BinnedDataset:
+    """A dense numerical dataset in the learner's input form.
+
+    ``bins``: uint8 array ``[num_features, num_data]`` of stored group bins (column-major).
+    ``features``: per inner feature, its ``FeatureInfo``.
+    """
+
+    def __init__(self, bins, features, num_total_features):
+        self.bins = bins
+        self.features = features
+        self.num_total_features = num_total_features
+
+    @property
+    def num_data(self):
+        return self.bins.shape[1]
+
+    @property
+    def num_features(self):
+        return self.bins.shape[0]
+
+    @classmethod
+    def from_dense(cls, X, max_bin=255, min_data_in_bin=3, min_data_in_leaf=20, bin_construct_sample_cnt=200000,
+                   data_random_seed=1, use_missing=True, zero_as_missing=False, feature_pre_filter=True,
+                   threads=8):
+        if max_bin > 255:
+            raise ValueError("max_bin above 255 needs 16-bit stored bins, which this learner does not take")
+        X = np.asarray(X)
+        n, ncol = X.shape
+        lib = _lib.load()
+        rows = _Random(data_random_seed).sample(n, min(n, bin_construct_sample_cnt))
+        sample_cnt = len(rows)
+        filter_cnt = int((float(min_data_in_leaf) * sample_cnt) / float(n))
+        cap = 1024
+
+        def find(col):
+            vals = np.asarray(X[rows, col], dtype=np.float64)
+            keep = (np.abs(vals) > K_ZERO_THRESHOLD) | np.isnan(vals)
+            vals = np.ascontiguousarray(vals[keep])
+            ub = np.zeros(cap, dtype=np.float64)
+            meta = np.zeros(4, dtype=np.int32)
+            dmeta = np.zeros(3, dtype=np.float64)
+            nb = lib.bk_find_bin_numerical(vals.ctypes.data, len(vals), sample_cnt, max_bin, min_data_in_bin,
+                                           filter_cnt, int(feature_pre_filter), int(use_missing),
+                                           int(zero_as_missing), ub.ctypes.data, cap, meta.ctypes.data,
+                                           dmeta.ctypes.data)
+            if nb < 0:
+                raise RuntimeError("bin mapper capacity exceeded")
+            fi = FeatureInfo()
+            fi.real = col
+            fi.num_bin = int(nb)
+            fi.missing_type = int(meta[0])
+            fi.default_bin = int(meta[2])
+            fi.most_freq_bin = int(meta[3])
+            fi.upper_bounds = ub[:nb].copy()
+            fi.penalty = 1.0
+            fi.min_val, fi.max_val, fi.sparse_rate = float(dmeta[0]), float(dmeta[1]), float(dmeta[2])
+            return fi, bool(meta[1])
+
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            found = list(ex.map(find, range(ncol)))
+        features = [fi for fi, trivial in found if not trivial]
+        bins = np.zeros((len(features), n), dtype=np.uint8)
+
+        def fill(j):
+            fi = features[j]
+            col = np.ascontiguousarray(X[:, fi.real], dtype=np.float64)
+            lib.bk_values_to_group_bins(col.ctypes.data, n, 1, fi.upper_bounds.ctypes.data, fi.num_bin,
+                                        fi.missing_type, fi.most_freq_bin, bins[j].ctypes.data)
+
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(fill, range(len(features))))
+        return cls(bins, features, ncol)
+
+    def feature_array(self):
+        """The ``bk_feature`` records of include/bkgpu.h, as a numpy structured array."""
+        arr = np.zeros(self.num_features, dtype=FEATURE_DTYPE)
+        for j, fi in enumerate(self.features):
+            arr[j] = (fi.num_bin, fi.missing_type, fi.default_bin, fi.most_freq_bin, fi.penalty, fi.real, 0)
+        return arr
+
+
+FEATURE_DTYPE = np.dtype([("num_bin", np.int32), ("missing_type", np.int32), ("default_bin", np.int32),
+                          ("most_freq_bin", np.int32), ("penalty", np.float64), ("real_feature", np.int32),
+                          ("_pad", np.int32)], align=True)

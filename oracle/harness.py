@@ -1,0 +1,327 @@
+"""ORACLE harness — test infrastructure only.
+
+* ``OracleLearner``: ctypes wrapper over ``oracle/_build/liboracle.so`` (the C++ restatement of
+  the reference's tree learner).
+* A restatement of the reference's boosting loop around a learner
+  (crates/lgbm-core/src/boosting/train.rs:723-839): objective gradients (binary
+  objective/binary.rs:71-90, L2 objective/regression.rs:240-248, softmax
+  objective/multiclass.rs:68-90), ``boost_from_average`` (train.rs:615-640), shrinkage and the
+  score update (tree.rs:446-478, serial.rs:1974-1990).
+* A parser for the tree sections of LightGBM model text, to compare against the reference's
+  golden ``model.txt`` files.
+
+Only tests, ``__graft_entry__.smoke()`` and the CPU-baseline leg of ``bench.py`` use this module.
+"""
+import ctypes
+import math
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+sys.path.insert(0, os.path.join(ROOT, "bankai-lightgbm_gb300"))
+
+from lgbm_gb300.config import CONFIG_DTYPE, LearnerConfig  # noqa: E402
+from lgbm_gb300.dataset import FEATURE_DTYPE  # noqa: E402
+from lgbm_gb300.tree import SPLIT_DTYPE, Tree  # noqa: E402
+
+EPS = float(np.float32(1e-15))
+_olib = None
+
+
+def load():
+    global _olib
+    if _olib is None:
+        sys.path.insert(0, HERE)
+        import build as obuild  # oracle/build.py
+        path = obuild.build()
+        lib = ctypes.CDLL(path)
+        P, i32, i64, u32 = ctypes.c_void_p, ctypes.c_int32, ctypes.c_int64, ctypes.c_uint32
+        lib.orc_learner_create.restype = P
+        lib.orc_learner_create.argtypes = [P, i32, P, i64, P]
+        lib.orc_learner_destroy.argtypes = [P]
+        lib.orc_learner_train.restype = i32
+        lib.orc_learner_train.argtypes = [P, P, P, P, i64, P, P]
+        lib.orc_learner_root_output.restype = ctypes.c_double
+        lib.orc_learner_root_output.argtypes = [P]
+        lib.orc_learner_row_leaf.argtypes = [P, P]
+        lib.orc_learner_partition.argtypes = [P, P, P, P]
+        lib.orc_learner_packed.argtypes = [P, P, P]
+        lib.orc_hist_float.argtypes = [P, i64, i32, P, P, i64, P, P, i32, P]
+        lib.orc_hist_int.argtypes = [P, i64, i32, P, P, i64, P, P, P]
+        lib.orc_discretize.restype = i32
+        lib.orc_discretize.argtypes = [P, P, i64, i32, i32, i32, u32, i32, i32, i32, P, P]
+        lib.orc_mt19937.argtypes = [u32, i32, u32, i64, P]
+        lib.orc_route_table.argtypes = [P, u32, i32, P]
+        lib.orc_find_best_threshold_int.restype = i32
+        lib.orc_find_best_threshold_int.argtypes = [P, P, P, P, i64, i64, ctypes.c_double, ctypes.c_double, i32,
+                                                    ctypes.c_double, P]
+        lib.orc_find_best_threshold.restype = i32
+        lib.orc_find_best_threshold.argtypes = [P, P, P, ctypes.c_double, ctypes.c_double, i32, ctypes.c_double, P]
+        lib.orc_sizeof_split.restype = i32
+        assert lib.orc_sizeof_split() == SPLIT_DTYPE.itemsize
+        _olib = lib
+    return _olib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+class OracleLearner:
+    """The oracle counterpart of the GPU learner: same inputs, same outputs."""
+
+    def __init__(self, ds, cfg: LearnerConfig):
+        self.lib = load()
+        self.ds = ds
+        self.cfg = cfg
+        self.feats = ds.feature_array()
+        self.bins = np.ascontiguousarray(ds.bins)
+        self.rec = cfg.record()
+        self.h = self.lib.orc_learner_create(self.feats.ctypes.data, ds.num_features, self.bins.ctypes.data,
+                                             ds.num_data, self.rec.ctypes.data)
+        self.num_leaves = int(cfg.num_leaves)
+
+    def __del__(self):
+        try:
+            self.lib.orc_learner_destroy(self.h)
+        except Exception:
+            pass
+
+    def train(self, g, h, rows=None):
+        g = np.ascontiguousarray(g, dtype=np.float32)
+        h = np.ascontiguousarray(h, dtype=np.float32)
+        rows = None if rows is None else np.ascontiguousarray(rows, dtype=np.int32)
+        splits = np.zeros(max(self.num_leaves - 1, 1), dtype=SPLIT_DTYPE)
+        leaf_values = np.zeros(self.num_leaves, dtype=np.float64)
+        nl = self.lib.orc_learner_train(self.h, g.ctypes.data, h.ctypes.data, _ptr(rows),
+                                        0 if rows is None else len(rows), splits.ctypes.data,
+                                        leaf_values.ctypes.data)
+        root = self.lib.orc_learner_root_output(self.h)
+        return splits[:nl - 1].copy(), leaf_values[:nl].copy(), root
+
+    def row_leaf(self):
+        out = np.zeros(self.ds.num_data, dtype=np.int32)
+        self.lib.orc_learner_row_leaf(self.h, out.ctypes.data)
+        return out
+
+    def partition(self):
+        idx = np.zeros(self.ds.num_data, dtype=np.int32)
+        b = np.zeros(self.num_leaves, dtype=np.int64)
+        c = np.zeros(self.num_leaves, dtype=np.int64)
+        self.lib.orc_learner_partition(self.h, idx.ctypes.data, b.ctypes.data, c.ctypes.data)
+        return idx, b, c
+
+    def packed(self):
+        out = np.zeros(self.ds.num_data, dtype=np.int16)
+        sc = np.zeros(2, dtype=np.float64)
+        self.lib.orc_learner_packed(self.h, out.ctypes.data, sc.ctypes.data)
+        return out, sc
+
+
+# ------------------------------------------------------------------------------------------
+# objectives (host, f64 score -> f32 gradients), written in the reference's operation order
+# ------------------------------------------------------------------------------------------
+class L2Objective:
+    """objective/regression.rs:240-248 and :127-142."""
+    constant_hessian = True
+    num_class = 1
+
+    def __init__(self, label):
+        self.label = np.asarray(label, dtype=np.float32)
+
+    def gradients(self, score):
+        g = (score - self.label.astype(np.float64)).astype(np.float32)
+        h = np.ones_like(g)
+        return g[None, :], h[None, :]
+
+    def boost_from_score(self, k):
+        suml = 0.0
+        for v in self.label.astype(np.float64):
+            suml += v
+        return suml / len(self.label)
+
+
+class BinaryObjective:
+    """objective/binary.rs:71-115 (sigmoid 1, no weights)."""
+    constant_hessian = False
+    num_class = 1
+
+    def __init__(self, label, sigmoid=1.0):
+        self.is_pos = np.asarray(label, dtype=np.float32) > 0
+        self.s = float(sigmoid)
+
+    def gradients(self, score):
+        n = len(score)
+        g = np.empty(n, np.float32)
+        h = np.empty(n, np.float32)
+        s = self.s
+        for i in range(n):
+            label = 1.0 if self.is_pos[i] else -1.0
+            response = -label * s / (1.0 + math.exp(label * s * float(score[i])))
+            ar = abs(response)
+            g[i] = np.float32(response * 1.0)
+            h[i] = np.float32(ar * (s - ar) * 1.0)
+        return g[None, :], h[None, :]
+
+    def boost_from_score(self, k):
+        suml = 0.0
+        for p in self.is_pos:
+            suml += 1.0 if p else 0.0
+        sumw = float(len(self.is_pos))
+        pavg = min(max(suml / sumw, EPS), 1.0 - EPS)
+        pavg = max(min(suml / sumw, 1.0 - EPS), EPS)
+        return math.log(pavg / (1.0 - pavg)) / self.s
+
+
+class SoftmaxObjective:
+    """objective/multiclass.rs:20-110 (no weights)."""
+    constant_hessian = False
+
+    def __init__(self, label, num_class):
+        self.num_class = num_class
+        self.label_int = np.asarray(label, dtype=np.float32).astype(np.int64)
+        self.factor = num_class / (num_class - 1.0)
+        probs = np.zeros(num_class)
+        for v in self.label_int:
+            probs[v] += 1.0
+        self.init_probs = probs / float(len(self.label_int))
+
+    def gradients(self, score):
+        K = self.num_class
+        n = score.shape[1]
+        g = np.empty((K, n), np.float32)
+        h = np.empty((K, n), np.float32)
+        for i in range(n):
+            rec = [float(score[k, i]) for k in range(K)]
+            wmax = rec[0]
+            for v in rec[1:]:
+                wmax = max(v, wmax)
+            wsum = 0.0
+            for k in range(K):
+                rec[k] = math.exp(rec[k] - wmax)
+                wsum += rec[k]
+            for k in range(K):
+                rec[k] = rec[k] / wsum
+            for k in range(K):
+                p = rec[k]
+                gi = p - 1.0 if self.label_int[i] == k else p
+                hi = self.factor * p * (1.0 - p)
+                g[k, i] = np.float32(gi)
+                h[k, i] = np.float32(hi)
+        return g, h
+
+    def boost_from_score(self, k):
+        return math.log(max(EPS, self.init_probs[k]))
+
+    def class_need_train(self, k):
+        p = abs(self.init_probs[k])
+        return not (p <= EPS or p >= 1.0 - EPS)
+
+
+def make_objective(params, y):
+    obj = params.get("objective", "regression")
+    if obj in ("regression", "l2", "regression_l2", "mse"):
+        return L2Objective(y)
+    if obj == "binary":
+        return BinaryObjective(y, params.get("sigmoid", 1.0))
+    if obj in ("multiclass", "softmax"):
+        return SoftmaxObjective(y, int(params["num_class"]))
+    raise ValueError("objective %r is outside the learner's scope" % obj)
+
+
+def train_gbdt(learner, ds, objective, rounds, learning_rate=0.1, boost_from_average=True,
+               min_gain_to_split=0.0):
+    """train.rs:723-839 without bagging / DART / RF. Returns (trees, score)."""
+    K = getattr(objective, "num_class", 1)
+    n = ds.num_data
+    score = np.zeros((K, n), dtype=np.float64)
+    trees = []
+    for it in range(rounds):
+        init = [0.0] * K
+        for k in range(K):
+            if it == 0 and boost_from_average:
+                v = objective.boost_from_score(k)
+                if abs(v) > EPS:
+                    init[k] = v
+                    score[k] += v
+        g, h = objective.gradients(score[0] if K == 1 else score)
+        cont = False
+        for k in range(K):
+            need = objective.class_need_train(k) if hasattr(objective, "class_need_train") else True
+            if not need:
+                raise NotImplementedError("constant class trees are outside the learner's scope")
+            recs, leaf_values, root = learner.train(g[k], h[k])
+            t = Tree.from_records(learner.num_leaves, recs, leaf_values, root, ds.features, min_gain_to_split)
+            if t.num_leaves > 1:
+                cont = True
+                t.apply_shrinkage(learning_rate)
+                leaf = learner.row_leaf()
+                score[k] += t.leaf_value[leaf]
+                if abs(init[k]) > EPS:
+                    t.add_bias(init[k])
+            trees.append(t)
+        if not cont:
+            trees = trees[:-K]
+            break
+    return trees, score
+
+
+# ------------------------------------------------------------------------------------------
+# model text
+# ------------------------------------------------------------------------------------------
+def parse_model_trees(text):
+    trees = []
+    cur = None
+    for line in text.splitlines():
+        if line.startswith("Tree="):
+            cur = {}
+            trees.append(cur)
+            continue
+        if cur is None or "=" not in line:
+            if line.strip() == "end of trees":
+                break
+            continue
+        k, v = line.split("=", 1)
+        cur[k] = v
+    return trees
+
+
+def compare_tree(t: Tree, ref: dict, leaf_rtol=1e-12):
+    """Returns a list of mismatch descriptions (empty when the tree matches)."""
+    bad = []
+    nl = int(ref["num_leaves"])
+    if t.num_leaves != nl:
+        return ["num_leaves %d != %d" % (t.num_leaves, nl)]
+    ni = nl - 1
+
+    def ints(key):
+        return np.array([int(x) for x in ref[key].split()], dtype=np.int64) if ni or key.startswith("leaf") else \
+            np.zeros(0, np.int64)
+
+    def floats(key):
+        return np.array([float(x) for x in ref[key].split()], dtype=np.float64)
+
+    if ni > 0:
+        for key, mine in (("split_feature", t.split_feature[:ni]), ("decision_type", t.decision_type[:ni]),
+                          ("left_child", t.left_child[:ni]), ("right_child", t.right_child[:ni]),
+                          ("internal_count", t.internal_count[:ni])):
+            if not np.array_equal(ints(key), mine.astype(np.int64)):
+                bad.append(key)
+        if not np.array_equal(floats("threshold"), t.threshold[:ni]):
+            bad.append("threshold")
+        if not np.allclose(floats("split_gain"), t.split_gain[:ni].astype(np.float64), rtol=1e-5, atol=1e-12):
+            bad.append("split_gain")
+        if not np.allclose(floats("internal_value"), t.internal_value[:ni], rtol=1e-5, atol=1e-9):
+            bad.append("internal_value")
+        if not np.allclose(floats("internal_weight"), t.internal_weight[:ni], rtol=1e-5):
+            bad.append("internal_weight")
+    if not np.array_equal(ints("leaf_count"), t.leaf_count[:nl].astype(np.int64)):
+        bad.append("leaf_count")
+    if not np.allclose(floats("leaf_value"), t.leaf_value[:nl], rtol=leaf_rtol, atol=0):
+        bad.append("leaf_value")
+    if ni > 0 and not np.allclose(floats("leaf_weight"), t.leaf_weight[:nl], rtol=1e-12):
+        bad.append("leaf_weight")
+    return bad

@@ -1,0 +1,205 @@
+"""Pins the oracle to the reference's own golden data (no GPU).
+
+* the upstream-LightGBM models that bankai-lightgbm reproduces (tests/golden/train/*), rebuilt
+  tree by tree through the oracle learner, with both ``madd`` rounding modes;
+* the std::mt19937 / libc++ distribution vectors and the discretizer vectors;
+* the upstream stumps of quantized_gradients.json;
+* the reference's brute-force integer split search cases.
+"""
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN
+
+CASES = sorted(os.listdir(os.path.join(GOLDEN, "train")))
+
+
+def _load_case(case):
+    d = os.path.join(GOLDEN, "train", case)
+    P = json.load(open(os.path.join(d, "params.json")))
+    X = np.load(os.path.join(d, "x.npy"))
+    y = np.load(os.path.join(d, "y.npy"))
+    model = open(os.path.join(d, "model.txt")).read()
+    return P, X, y, model
+
+
+def _dataset(p, X):
+    from lgbm_gb300 import BinnedDataset
+    return BinnedDataset.from_dense(X, max_bin=p.get("max_bin", 255), min_data_in_leaf=p.get("min_data_in_leaf", 20),
+                                    zero_as_missing=p.get("zero_as_missing", False))
+
+
+@pytest.mark.parametrize("fused", [1, 0])
+@pytest.mark.parametrize("case", CASES)
+def test_oracle_reproduces_reference_models(oracle, bklib, case, fused):
+    from lgbm_gb300 import LearnerConfig
+    P, X, y, model = _load_case(case)
+    p = P["params"]
+    ds = _dataset(p, X)
+    obj = oracle.make_objective(p, y)
+    cfg = LearnerConfig(**p, fused_madd=fused, is_constant_hessian=int(obj.constant_hessian))
+    learner = oracle.OracleLearner(ds, cfg)
+    trees, _ = oracle.train_gbdt(learner, ds, obj, P["num_boost_round"], learning_rate=p.get("learning_rate", 0.1),
+                                 boost_from_average=p.get("boost_from_average", True),
+                                 min_gain_to_split=p.get("min_gain_to_split", 0.0))
+    ref = oracle.parse_model_trees(model)
+    assert len(trees) == len(ref)
+    exact = total = 0
+    for i, (t, r) in enumerate(zip(trees, ref)):
+        bad = oracle.compare_tree(t, r)
+        assert not bad, "tree %d differs in %s" % (i, bad)
+        vals = np.array([float(v) for v in r["leaf_value"].split()])
+        exact += int(np.sum(vals == t.leaf_value[:t.num_leaves]))
+        total += t.num_leaves
+    if fused:
+        # The fixtures come from an FMA build; in fused mode every leaf value is bit-identical.
+        assert exact == total, "%d of %d leaf values bit-exact" % (exact, total)
+
+
+def test_mt19937_standard_vector(oracle):
+    v = json.load(open(os.path.join(GOLDEN, "vectors.json")))
+    out = np.zeros(10000, dtype=np.uint64)
+    oracle.load().orc_mt19937(5489, 0, 0, 10000, out.ctypes.data)
+    assert int(out[-1]) == v["mt19937_default_10000th"]
+
+
+def test_libcxx_distributions(oracle):
+    v = json.load(open(os.path.join(GOLDEN, "vectors.json")))
+    u = v["uniform_real_01"]
+    out = np.zeros(len(u["bits"]), dtype=np.uint64)
+    oracle.load().orc_mt19937(u["seed"], 1, 0, len(out), out.ctypes.data)
+    assert [int(x) for x in out] == u["bits"]
+    for case in v["uniform_int_inclusive"]:
+        out = np.zeros(len(case["draws"]), dtype=np.uint64)
+        oracle.load().orc_mt19937(case["seed"], 2, case["n"], len(out), out.ctypes.data)
+        assert [int(x) for x in out] == case["draws"]
+
+
+def _discretize(oracle, g, h, bins, const_hess, stochastic=0, seed=0, threads=1, fused=0, calls=1):
+    g = np.asarray(g, np.float32)
+    h = np.asarray(h, np.float32)
+    out = np.zeros(len(g), np.int16)
+    sc = np.zeros(2, np.float64)
+    ok = oracle.load().orc_discretize(g.ctypes.data, h.ctypes.data, len(g), bins, const_hess, stochastic, seed,
+                                      threads, fused, calls, out.ctypes.data, sc.ctypes.data)
+    return ok, out, sc
+
+
+def test_discretizer_vectors(oracle):
+    v = json.load(open(os.path.join(GOLDEN, "vectors.json")))
+    assert v["nearest_bins4"]
+    for case in v["nearest_bins4"]:
+        for fused in (0, 1):
+            ok, out, sc = _discretize(oracle, case["gradients"], case["hessians"], 4, 0, fused=fused)
+            assert ok
+            assert out.tolist() == case["packed"]
+            assert sc[0] == case["gradient_scale"] and sc[1] == case["hessian_scale"]
+    c = v["nearest_const_hess_bins4"]
+    ok, out, _ = _discretize(oracle, c["gradients"], c["hessians"], 4, 1)
+    assert ok and out.tolist() == c["packed"]
+
+
+def test_discretizer_refuses_degenerate_inputs(oracle):
+    assert _discretize(oracle, [0.0, 0.0], [1.0, 1.0], 4, 0)[0] == 0
+    assert _discretize(oracle, [1.0, 1.0], [-1.0, 1.0], 4, 0)[0] == 0
+    assert _discretize(oracle, [np.nan, 1.0], [1.0, 1.0], 4, 0)[0] == 0
+
+
+def test_quantized_gradient_stumps(oracle):
+    """tests/fixtures/quantized_gradients.json: 16 upstream stumps (tolerance 1e-12 as the reference)."""
+    d = json.load(open(os.path.join(GOLDEN, "quantized_gradients.json")))
+    assert d["upstream"] == "4.7.0" and len(d["cases"]) == 16
+
+    def close(a, b):
+        assert abs(a - b) <= 1e-12 * max(abs(b), 1.0), (a, b)
+
+    for c in d["cases"]:
+        g = np.asarray(c["gradients"], np.float64).astype(np.float32)
+        h = np.asarray(c["hessians"], np.float64).astype(np.float32)
+        ok, packed, sc = _discretize(oracle, g, h, c["bins"], int(c["constant_hessian"]))
+        assert ok
+        left = np.zeros(len(g), bool)
+        left[c["left_rows"]] = True
+        gi = (packed >> 8).astype(np.int8).astype(np.int64)
+        hi = (packed & 0xFF).astype(np.int64)
+        lg, lh = gi[left].sum() * sc[0], hi[left].sum() * sc[1]
+        rg, rh = gi[~left].sum() * sc[0], hi[~left].sum() * sc[1]
+        close(lh, c["left_weight"])
+        close(rh, c["right_weight"])
+        close(-lg / lh, c["left_output"])
+        close(-rg / rh, c["right_output"])
+        gain = lg * lg / lh + rg * rg / rh - (lg + rg) ** 2 / (lh + rh)
+        close(float(np.float32(gain)), c["split_gain"])
+
+
+def _brute_force_int_split(hist, gs, hs, l2, min_data):
+    """crates/lgbm-core/tests/quantized_split_search.rs:59-135, restated."""
+    EPS = float(np.float32(1e-15))
+    tg = sum(b[0] for b in hist)
+    th = sum(b[1] for b in hist)
+    num_data = th
+    cnt_factor = num_data / float(th)
+
+    def out(g, h):
+        return -g / (h + l2)
+
+    def gain_of(g, h):
+        o = out(g, h)
+        return -(2.0 * g * o + (h + l2) * o * o)
+
+    mgs = gain_of(tg * gs, th * hs) + 0.0
+    best = dict(splittable=False, gain=-math.inf)
+    for s in range(1, len(hist)):
+        rg = sum(b[0] for b in hist[s:])
+        rh = sum(b[1] for b in hist[s:])
+        lg, lh = tg - rg, th - rh
+        rc = int(rh * cnt_factor + 0.5)
+        lc = num_data - rc
+        srh, slh = rh * hs, lh * hs
+        if rc < min_data or lc < min_data:
+            continue
+        gain = gain_of(lg * gs, slh + EPS) + gain_of(rg * gs, srh + EPS)
+        if gain <= mgs:
+            continue
+        best["splittable"] = True
+        if gain > best["gain"]:
+            best.update(gain=gain, threshold=s - 1, left_count=int(lh * cnt_factor + 0.5),
+                        right_count=int(rh * cnt_factor + 0.5), left_output=out(lg * gs, slh),
+                        right_output=out(rg * gs, srh))
+    if best["splittable"]:
+        best["gain"] -= mgs
+    return best, tg, th, num_data
+
+
+def test_int_split_search_brute_force(oracle):
+    from lgbm_gb300 import LearnerConfig, FEATURE_DTYPE
+    from lgbm_gb300.tree import SPLIT_DTYPE
+    v = json.load(open(os.path.join(GOLDEN, "vectors.json")))
+    assert v["int_split_search"]
+    for case in v["int_split_search"]:
+        hist = case["hist"]
+        for gs, hs, l2, min_data in case["checks"]:
+            want, tg, th, num_data = _brute_force_int_split(hist, gs, hs, l2, min_data)
+            f = np.zeros(1, FEATURE_DTYPE)
+            # offset 0 (the reference test's FeatureMeta): any nonzero most-frequent bin
+            f[0] = (len(hist), 0, 0, 1, 1.0, 0, 0)
+            cfg = LearnerConfig(lambda_l2=l2, min_data_in_leaf=min_data, min_sum_hessian_in_leaf=0.0).record()
+            hg = np.array([b[0] for b in hist], np.int64)
+            hh = np.array([b[1] for b in hist], np.int64)
+            out = np.zeros(1, SPLIT_DTYPE)
+            sp = oracle.load().orc_find_best_threshold_int(hg.ctypes.data, hh.ctypes.data, f.ctypes.data,
+                                                            cfg.ctypes.data, tg, th, gs, hs, num_data, 0.0,
+                                                            out.ctypes.data)
+            assert bool(sp) == want["splittable"]
+            if not want["splittable"]:
+                continue
+            o = out[0]
+            assert o["threshold"] == want["threshold"]
+            assert o["left_count"] == want["left_count"] and o["right_count"] == want["right_count"]
+            assert abs(o["gain"] - want["gain"]) <= 1e-12 * max(abs(want["gain"]), 1.0)
+            assert abs(o["left_output"] - want["left_output"]) <= 1e-12
+            assert abs(o["right_output"] - want["right_output"]) <= 1e-12
