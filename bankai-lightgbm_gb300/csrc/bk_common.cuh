@@ -1,0 +1,144 @@
+// Shared device-side definitions of the GB300 tree learner.
+//
+// Layout in HBM (one learner, `n` rows, `F` inner features, `T = ceil(F / 32)` feature tiles,
+// `B` = the largest stored-bin count of any feature, rounded up to a multiple of 8):
+//   bins_rt   uint8 [T][n][32]   row-tiled stored bins: one 32-byte sector per (tile, row), so a
+//                                gathered row of a leaf is one coalesced sector read per tile;
+//   bins_cm   uint8 [F][n]       column-major stored bins, read by the partition (one byte/row);
+//   pool      [L][T][B][32]      histogram pool, one slot per leaf (serial.rs:80-162 with a full
+//                                pool): double2 (grad, hess) on the float path, int64
+//                                (grad << 32) + hess on the quantized path;
+// and per job (one tree of the K trees grown together): gradients, packed int8 gradients,
+// two row-index buffers (ping-pong between a leaf and its children), leaf bookkeeping.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "bkgpu.h"
+
+namespace bk {
+
+constexpr int TILE = 32;
+// meta.rs:7 — kEpsilon = 1e-15f widened to double; meta.rs:4 — kZeroThreshold = 1e-35f.
+#define BK_EPS ((double)1e-15f)
+#define BK_ZERO_THRESHOLD ((double)1e-35f)
+
+struct DevFeature {
+  int32_t num_bin, missing, default_bin, mfb;
+  int32_t offset;  // 1 when the most frequent bin is 0 (its bin is not in the histogram slice)
+  int32_t gbins;   // stored bins of the feature's group: 1 + num_bin - offset
+  int32_t real;    // real (original) column index
+  int32_t len;     // searched slice length: num_bin - offset
+  double penalty;
+};
+
+// A split candidate of one (leaf, feature): SplitInfo (split_info.rs:9-31) plus its
+// splittable flag and the inner feature index.
+struct Cand {
+  double gain, left_output, right_output, lsg, lsh, rsg, rsh;
+  int64_t lint, rint;
+  int32_t feature, inner;
+  uint32_t threshold;
+  int32_t left_count, right_count, default_left, splittable, _pad;
+};
+
+// LeafSplits (serial.rs:53-76).
+struct LeafSum {
+  double sg, sh, weight;
+  int64_t int_sum;
+  int32_t num_data, _pad;
+};
+
+struct Params {
+  double l1, l2, max_delta, smooth, min_hess, min_gain;
+  int32_t min_data, fused, use_l1, use_max, use_smooth, quant;
+  int32_t const_hess, num_leaves, max_depth, F;
+  int32_t T, B, quant_bins, stochastic;
+  int32_t renew, part_grid, _p0, _p1;
+  int64_t n;
+};
+
+// Per-job control block, written and read only by kernels (the device-resident grow loop).
+struct JobState {
+  int32_t stop, do_search, tree_leaves, disc_ok;
+  int32_t smaller_leaf, larger_leaf, smaller_slot, larger_slot;
+  int32_t parent_slot, use_subtract, next_free, split_leaf;
+  int32_t split_inner, new_leaf, use_rows, _p0;
+  int64_t root_count, total_left;
+  double gscale, hscale, inv_g, inv_h;
+  double root_output;
+  uint32_t start_pos, red_maxg, red_maxh, red_flags;
+  int32_t mt_idx, _p1;
+  int64_t hist_rows_direct, hist_rows_gather, hist_builds;  // work done by the histogram kernels
+  uint32_t mt[624];
+  uint8_t route[256];
+};
+
+// Device pointers of one job.
+struct Job {
+  JobState* st;
+  const float* g;
+  const float* h;
+  int16_t* packed;
+  int32_t* idx0;
+  int32_t* idx1;
+  int64_t* leaf_begin;
+  int64_t* leaf_count;
+  int32_t* leaf_buf;
+  int32_t* leaf_depth;
+  int32_t* leaf_slot;
+  LeafSum* leaf_sum;
+  Cand* best;          // [L]
+  Cand* cand;          // [2][F]
+  uint8_t* splittable; // [L][F]
+  uint8_t* used;       // [F]
+  bk_split* records;   // [L-1]
+  double* leaf_value;  // [L]
+  void* pool;          // [L][T][B][32]
+  int64_t* part_cnt;   // [part_grid] partition block counts (scratch)
+  double* red;         // reduction partials (scratch)
+  int64_t* ired;       // integer reduction partials (scratch)
+};
+
+__device__ __forceinline__ const int32_t* leaf_idx(const Job& J, int32_t buf) { return buf ? J.idx1 : J.idx0; }
+__device__ __forceinline__ int32_t* leaf_idx_w(const Job& J, int32_t buf) { return buf ? J.idx1 : J.idx0; }
+
+__host__ __device__ __forceinline__ int64_t ceil_div64(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---- launchers (defined in the kernel translation units) ----
+struct HistLaunch {
+  int blocks_per_tile;
+  int threads;
+  size_t smem;
+  int flush_rounds;  // quantized: rounds of 32*warps rows between 16-bit -> 32-bit flushes (0: wide)
+};
+void launch_hist(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const HistLaunch& hl,
+                 cudaStream_t s);
+size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide);
+
+void launch_search(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s);
+void launch_decide(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s);
+void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm, cudaStream_t s);
+void launch_post_split(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s);
+cudaError_t hist_set_smem_attrs(size_t smem);
+
+// bk_prep.cu
+void launch_init_rows(const Job* d_jobs, int num_jobs, const Params& p, const int32_t* rows, cudaStream_t s);
+void launch_discretize(const Job* d_jobs, int num_jobs, const Params& p, const double* noise_g, const double* noise_h,
+                       cudaStream_t s);
+void launch_root_sums(const Job* d_jobs, int num_jobs, const Params& p, int exact_quant_root, cudaStream_t s);
+void launch_renew(const Job* d_jobs, int num_jobs, const Params& p, cudaStream_t s);
+void launch_add_score(const Job* d_jobs, int num_jobs, const Params& p, const double* leaf_vals, double* score,
+                      cudaStream_t s);
+void launch_row_leaf(const Job* d_jobs, int num_jobs, const Params& p, int32_t* out, cudaStream_t s);
+void launch_mt_seed(const Job* d_jobs, int num_jobs, uint32_t seed, cudaStream_t s);
+constexpr int kRootGrid = 256;
+
+// bk_objective.cu
+cudaError_t objective_gradients(int kind, const double* score, const float* label, int64_t n, int K, double sigmoid,
+                                float* g, float* h, cudaStream_t s);
+cudaError_t objective_loss(int kind, const double* score, const float* label, int64_t n, int K, double* partial,
+                           int grid, cudaStream_t s);
+void launch_tree_begin(const Job* d_jobs, int num_jobs, const Params& p, cudaStream_t s);
+
+}  // namespace bk

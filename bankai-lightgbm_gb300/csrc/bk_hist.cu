@@ -1,0 +1,270 @@
+// ConstructHistograms for the smaller leaf (serial.rs:891-1164), GB300 form.
+//
+// Grid: (blocks_per_tile, T, jobs). Each CTA owns one 32-feature tile and one contiguous chunk
+// of the leaf's rows. A warp takes 32 rows at a time: every lane fetches its row's 32-byte
+// tile sector with two 128-bit loads and stages it in shared memory; then, row by row, lane f
+// adds that row's statistics to bin[row][f] of a CTA-private shared histogram laid out
+// [bin][feature] — lane f always hits bank f, so the shared-memory atomics of a warp never
+// conflict and never collide. At the end the CTA adds its non-zero bins to the leaf's slot in
+// the histogram pool with global atomics (the pool slot is zeroed when the tree starts).
+//
+// Quantized path: the packed int8 gradient / uint8 hessian of a row is added as one 32-bit
+// value (grad << 16) + hess into a 16:16 "hot" histogram, which is folded into 32-bit
+// grad/hess "cold" counters before either half can overflow, and finally into the int64
+// (grad << 32) + hess pool slot. Integer sums are exact, so the result equals the reference's
+// sequential i64 histogram bit for bit.
+//
+// Float path: gradient and hessian each go to an fp32 (hi, lo) pair: hi is updated with
+// atomicAdd, which returns the previous value, and the exact rounding error of that addition
+// (Knuth's TwoSum on old and addend) is added to lo. hi + lo carries the sum to about 2^-48
+// relative; the pool slot receives (double)hi + (double)lo via f64 global atomics. With a
+// constant hessian the hessian slot counts rows and is scaled by hessians[0] at the flush
+// (serial.rs:980-988), which is exact.
+#include "bk_common.cuh"
+
+namespace bk {
+
+namespace {
+
+constexpr int kMinChunk = 4096;
+
+__device__ __forceinline__ float two_sum_err(float a, float b, float s) {
+  float bb = __fsub_rn(s, a);
+  float e1 = __fsub_rn(a, __fsub_rn(s, bb));
+  float e2 = __fsub_rn(b, bb);
+  return __fadd_rn(e1, e2);
+}
+
+struct Range {
+  int64_t r0, r1;
+  const int32_t* idx;
+  bool direct;
+};
+
+__device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blocks_per_tile, Range* r) {
+  const JobState* st = J.st;
+  if (st->stop || !st->do_search) return false;
+  int32_t leaf = st->smaller_leaf;
+  int64_t begin = J.leaf_begin[leaf], count = J.leaf_count[leaf];
+  int64_t chunk = ceil_div64(count, blocks_per_tile);
+  if (chunk < kMinChunk) chunk = kMinChunk;
+  chunk = (chunk + 31) / 32 * 32;
+  r->r0 = (int64_t)blockIdx.x * chunk;
+  if (r->r0 >= count) return false;
+  r->r1 = min(count, r->r0 + chunk);
+  r->idx = leaf_idx(J, J.leaf_buf[leaf]) + begin;
+  r->direct = (count == p.n);  // all rows in order: the index buffer is the identity
+  return true;
+}
+
+template <bool WIDE>
+__global__ void __launch_bounds__(1024, 1)
+    k_hist_int(const Job* __restrict__ jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile,
+               int flush_rounds) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Job& J = jobs[blockIdx.z];
+  Range R;
+  if (!cta_range(J, p, blocks_per_tile, &R)) return;
+  const int B = p.B;
+  const int tile = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
+  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + (WIDE ? 0 : B * TILE));
+  int32_t* cold_h = cold_g + B * TILE;
+  uint4* stage = reinterpret_cast<uint4*>(cold_h + B * TILE);
+  int32_t* stage_v = reinterpret_cast<int32_t*>(stage + nwarps * 64);
+  for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
+    if (!WIDE) hot[e] = 0u;
+    cold_g[e] = 0;
+    cold_h[e] = 0;
+  }
+  __syncthreads();
+  const uint8_t* tb = bins_rt + (size_t)tile * (size_t)p.n * TILE;
+  const int16_t* packed = J.packed;
+  const int64_t per_round = (int64_t)TILE * nwarps;
+  const int64_t rounds = ceil_div64(R.r1 - R.r0, per_round);
+  for (int64_t rd = 0; rd < rounds; ++rd) {
+    int64_t base = R.r0 + rd * per_round + (int64_t)warp * TILE;
+    if (base < R.r1) {
+      int64_t i = base + lane;
+      bool valid = i < R.r1;
+      uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
+      int32_t v = 0;
+      if (valid) {
+        int64_t row = R.direct ? i : (int64_t)R.idx[i];
+        const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * TILE);
+        a = __ldg(src);
+        b = __ldg(src + 1);
+        int32_t pk = packed[row];
+        int32_t gi = (int32_t)(int8_t)(pk >> 8);
+        int32_t hi = pk & 0xff;
+        v = WIDE ? ((gi & 0xffff) | (hi << 16)) : gi * 65536 + hi;
+      }
+      stage[(warp * 32 + lane) * 2] = a;
+      stage[(warp * 32 + lane) * 2 + 1] = b;
+      stage_v[warp * 32 + lane] = v;
+      __syncwarp();
+      const uint8_t* sb = reinterpret_cast<const uint8_t*>(stage + warp * 64);
+      int jn = (int)min((int64_t)32, R.r1 - base);
+      for (int j = 0; j < jn; ++j) {
+        uint32_t bin = sb[j * 32 + lane];
+        int32_t vv = stage_v[warp * 32 + j];
+        if (WIDE) {
+          atomicAdd(&cold_g[bin * TILE + lane], (int32_t)(int16_t)(vv & 0xffff));
+          atomicAdd(&cold_h[bin * TILE + lane], vv >> 16);
+        } else {
+          atomicAdd(&hot[bin * TILE + lane], (uint32_t)vv);
+        }
+      }
+      __syncwarp();
+    }
+    if (!WIDE && ((rd + 1) % flush_rounds == 0 || rd + 1 == rounds)) {
+      __syncthreads();
+      for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
+        int32_t s = (int32_t)hot[e];
+        if (s) {
+          int32_t hh = s & 0xffff;
+          int32_t gg = (s - hh) >> 16;
+          cold_g[e] += gg;
+          cold_h[e] += hh;
+          hot[e] = 0u;
+        }
+      }
+      __syncthreads();
+    }
+  }
+  if (WIDE) __syncthreads();
+  unsigned long long* slot = reinterpret_cast<unsigned long long*>(J.pool) +
+                             ((size_t)J.st->smaller_slot * p.T + tile) * (size_t)B * TILE;
+  for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
+    int32_t gg = cold_g[e], hh = cold_h[e];
+    if (gg | hh) {
+      int64_t pk = (int64_t)gg * 4294967296LL + (int64_t)hh;
+      atomicAdd(slot + e, (unsigned long long)pk);
+    }
+  }
+}
+
+template <bool CONST_HESS>
+__global__ void __launch_bounds__(1024, 1)
+    k_hist_float(const Job* __restrict__ jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const Job& J = jobs[blockIdx.z];
+  Range R;
+  if (!cta_range(J, p, blocks_per_tile, &R)) return;
+  const int B = p.B;
+  const int tile = blockIdx.y;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
+  float* ghi = reinterpret_cast<float*>(smem);
+  float* glo = ghi + B * TILE;
+  float* hhi = glo + B * TILE;  // CONST_HESS: uint32 row counts
+  float* hlo = hhi + B * TILE;  // unused with CONST_HESS
+  uint4* stage = reinterpret_cast<uint4*>(CONST_HESS ? hlo : hlo + B * TILE);
+  float2* stage_v = reinterpret_cast<float2*>(stage + nwarps * 64);
+  uint32_t* hcnt = reinterpret_cast<uint32_t*>(hhi);
+  for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
+    ghi[e] = 0.f;
+    glo[e] = 0.f;
+    if (CONST_HESS) {
+      hcnt[e] = 0u;
+    } else {
+      hhi[e] = 0.f;
+      hlo[e] = 0.f;
+    }
+  }
+  __syncthreads();
+  const uint8_t* tb = bins_rt + (size_t)tile * (size_t)p.n * TILE;
+  const float* G = J.g;
+  const float* H = J.h;
+  const int64_t per_round = (int64_t)TILE * nwarps;
+  for (int64_t base = R.r0 + (int64_t)warp * TILE; base < R.r1; base += per_round) {
+    int64_t i = base + lane;
+    bool valid = i < R.r1;
+    uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
+    float2 v = make_float2(0.f, 0.f);
+    if (valid) {
+      int64_t row = R.direct ? i : (int64_t)R.idx[i];
+      const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * TILE);
+      a = __ldg(src);
+      b = __ldg(src + 1);
+      v.x = G[row];
+      if (!CONST_HESS) v.y = H[row];
+    }
+    stage[(warp * 32 + lane) * 2] = a;
+    stage[(warp * 32 + lane) * 2 + 1] = b;
+    stage_v[warp * 32 + lane] = v;
+    __syncwarp();
+    const uint8_t* sb = reinterpret_cast<const uint8_t*>(stage + warp * 64);
+    int jn = (int)min((int64_t)32, R.r1 - base);
+    for (int j = 0; j < jn; ++j) {
+      uint32_t e = (uint32_t)sb[j * 32 + lane] * TILE + lane;
+      float2 vv = stage_v[warp * 32 + j];
+      float old = atomicAdd(&ghi[e], vv.x);
+      float err = two_sum_err(old, vv.x, __fadd_rn(old, vv.x));
+      if (err != 0.f) atomicAdd(&glo[e], err);
+      if (CONST_HESS) {
+        atomicAdd(&hcnt[e], 1u);
+      } else {
+        float oh = atomicAdd(&hhi[e], vv.y);
+        float eh = two_sum_err(oh, vv.y, __fadd_rn(oh, vv.y));
+        if (eh != 0.f) atomicAdd(&hlo[e], eh);
+      }
+    }
+    __syncwarp();
+  }
+  __syncthreads();
+  double2* slot = reinterpret_cast<double2*>(J.pool) + ((size_t)J.st->smaller_slot * p.T + tile) * (size_t)B * TILE;
+  const double h0 = CONST_HESS ? (double)H[0] : 0.0;
+  for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
+    double gs = (double)ghi[e] + (double)glo[e];
+    double hs = CONST_HESS ? (double)hcnt[e] * h0 : (double)hhi[e] + (double)hlo[e];
+    bool touched = CONST_HESS ? hcnt[e] != 0u : (ghi[e] != 0.f || glo[e] != 0.f || hhi[e] != 0.f || hlo[e] != 0.f);
+    if (touched) {
+      atomicAdd(&slot[e].x, gs);
+      atomicAdd(&slot[e].y, hs);
+    }
+  }
+}
+
+}  // namespace
+
+size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide) {
+  size_t warps = (size_t)threads / 32;
+  size_t stage = warps * 64 * sizeof(uint4);
+  size_t bins = (size_t)p.B * TILE;
+  if (quant) return (wide ? 0 : bins * 4) + bins * 8 + stage + warps * 32 * 4;
+  if (p.const_hess) return bins * 12 + stage + warps * 32 * sizeof(float2);
+  return bins * 16 + stage + warps * 32 * sizeof(float2);
+}
+
+void launch_hist(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const HistLaunch& hl,
+                 cudaStream_t s) {
+  dim3 grid(hl.blocks_per_tile, p.T, num_jobs);
+  if (p.quant) {
+    if (hl.flush_rounds > 0)
+      k_hist_int<false><<<grid, hl.threads, hl.smem, s>>>(d_jobs, p, bins_rt, hl.blocks_per_tile, hl.flush_rounds);
+    else
+      k_hist_int<true><<<grid, hl.threads, hl.smem, s>>>(d_jobs, p, bins_rt, hl.blocks_per_tile, 1);
+  } else if (p.const_hess) {
+    k_hist_float<true><<<grid, hl.threads, hl.smem, s>>>(d_jobs, p, bins_rt, hl.blocks_per_tile);
+  } else {
+    k_hist_float<false><<<grid, hl.threads, hl.smem, s>>>(d_jobs, p, bins_rt, hl.blocks_per_tile);
+  }
+}
+
+cudaError_t hist_set_smem_attrs(size_t smem) {
+  // The attribute is per kernel and process-wide: only ever raise it, so learners created
+  // earlier with larger tiles keep working.
+  static size_t current = 0;
+  if (smem <= current) return cudaSuccess;
+  cudaError_t e = cudaSuccess;
+  int v = (int)smem;
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hist_int<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hist_int<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hist_float<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hist_float<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
+  if (e == cudaSuccess) current = smem;
+  return e;
+}
+
+}  // namespace bk

@@ -1,0 +1,694 @@
+// Host side of the GB300 learner and the C ABI declared in include/bkgpu.h.
+//
+// One bk_learner owns one dataset resident in HBM and grows `num_jobs` trees per train call.
+// The grow loop (serial.rs:578-628) runs on the device: every step of an iteration —
+// histogram of the smaller leaf, split search of both children, arg-max leaf, partition,
+// bookkeeping — is a kernel that reads its operands from the per-job JobState in device memory.
+// Loop mode 0 launches the steps split by split and reads the stop flags back after each
+// arg-max (the plain form, one host round trip per split); loop mode 1 captures the whole
+// iteration (num_leaves - 1 steps) once as a CUDA graph and replays it, with the remaining steps
+// of a finished tree returning at their first instruction.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "bk_common.cuh"
+
+using namespace bk;
+
+namespace {
+
+thread_local std::string g_last_error;
+
+void set_error(const char* fmt, ...) {
+  char buf[1024];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  g_last_error = buf;
+}
+
+struct CudaError {
+  std::string msg;
+};
+
+#define CK(call)                                                                                  \
+  do {                                                                                            \
+    cudaError_t e_ = (call);                                                                      \
+    if (e_ != cudaSuccess) throw CudaError{std::string(#call) + ": " + cudaGetErrorString(e_)}; \
+  } while (0)
+
+// ---- host std::mt19937 for the per-row stochastic-rounding noise (mt19937.rs:32-101) ----
+struct HostMt {
+  uint32_t st[624];
+  int idx;
+  explicit HostMt(uint32_t seed) {
+    st[0] = seed;
+    for (int i = 1; i < 624; ++i) st[i] = 1812433253u * (st[i - 1] ^ (st[i - 1] >> 30)) + (uint32_t)i;
+    idx = 624;
+  }
+  uint32_t next() {
+    if (idx >= 624) {
+      for (int i = 0; i < 624; ++i) {
+        uint32_t y = (st[i] & 0x80000000u) | (st[(i + 1) % 624] & 0x7fffffffu);
+        uint32_t nx = st[(i + 397) % 624] ^ (y >> 1);
+        if (y & 1u) nx ^= 0x9908b0dfu;
+        st[i] = nx;
+      }
+      idx = 0;
+    }
+    uint32_t y = st[idx++];
+    y ^= y >> 11;
+    y ^= (y << 7) & 0x9d2c5680u;
+    y ^= (y << 15) & 0xefc60000u;
+    y ^= y >> 18;
+    return y;
+  }
+  double canonical() {  // libc++ generate_canonical<double, 53>
+    double g1 = (double)next();
+    double g2 = (double)next();
+    double rp = 4294967296.0;
+    double sp = g1 + g2 * rp;
+    return sp / (rp * rp);
+  }
+};
+
+__global__ void k_pack_rowtile(const uint8_t* __restrict__ cm, uint8_t* __restrict__ rt, int64_t n, int F, int T) {
+  int64_t total = n * T;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
+    int64_t tile = k / n, row = k % n;
+    uint32_t w[8];
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      uint32_t v = 0;
+#pragma unroll
+      for (int b = 0; b < 4; ++b) {
+        int f = (int)tile * TILE + q * 4 + b;
+        uint32_t x = f < F ? cm[(size_t)f * n + row] : 0u;
+        v |= x << (8 * b);
+      }
+      w[q] = v;
+    }
+    uint4* dst = reinterpret_cast<uint4*>(rt + ((size_t)tile * n + row) * TILE);
+    dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+  }
+}
+
+}  // namespace
+
+struct bk_learner {
+  int device = 0;
+  int num_sms = 152;
+  cudaStream_t stream = nullptr;
+  Params p{};
+  int K = 1;
+  int loop_mode = 1;
+  bool timing = false;
+  int exact_quant_root = 1;
+  HistLaunch hl{};
+  // dataset
+  DevFeature* d_feat = nullptr;
+  std::vector<DevFeature> h_feat;
+  uint8_t* d_bins_cm = nullptr;
+  uint8_t* d_bins_rt = nullptr;
+  double* d_noise_g = nullptr;
+  double* d_noise_h = nullptr;
+  // jobs
+  std::vector<Job> jobs;
+  Job* d_jobs = nullptr;
+  float* d_g = nullptr;
+  float* d_h = nullptr;
+  int32_t* d_rows = nullptr;
+  size_t pool_bytes_per_job = 0;
+  void* d_pool = nullptr;
+  std::vector<void*> allocs;
+  // host staging
+  bk_split* h_records = nullptr;
+  double* h_leaf_values = nullptr;
+  JobState* h_state = nullptr;
+  double* d_leaf_vals_in = nullptr;
+  // graph
+  cudaGraphExec_t graph_exec = nullptr;
+  // timing
+  cudaEvent_t ev_start = nullptr, ev_end = nullptr;
+  std::vector<cudaEvent_t> hist_events;
+  double last_total_ms = 0, last_hist_ms = 0, last_hist_bytes = 0;
+
+  template <typename T>
+  T* dalloc(size_t count) {
+    void* ptr = nullptr;
+    CK(cudaMalloc(&ptr, std::max<size_t>(count * sizeof(T), 16)));
+    allocs.push_back(ptr);
+    return reinterpret_cast<T*>(ptr);
+  }
+
+  ~bk_learner() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    for (void* a : allocs) cudaFree(a);
+    if (h_records) cudaFreeHost(h_records);
+    if (h_leaf_values) cudaFreeHost(h_leaf_values);
+    if (h_state) cudaFreeHost(h_state);
+    for (cudaEvent_t e : hist_events) cudaEventDestroy(e);
+    if (ev_start) cudaEventDestroy(ev_start);
+    if (ev_end) cudaEventDestroy(ev_end);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  void record_hist_event(int i) {
+    if (timing && (size_t)i < hist_events.size()) CK(cudaEventRecord(hist_events[i], stream));
+  }
+
+  // One grow-loop step (iteration `it`) of all jobs.
+  void step_a(int it) {
+    record_hist_event(2 * it);
+    launch_hist(d_jobs, K, p, d_bins_rt, hl, stream);
+    record_hist_event(2 * it + 1);
+    launch_search(d_jobs, K, p, d_feat, stream);
+    launch_decide(d_jobs, K, p, d_feat, stream);
+  }
+  void step_b() {
+    launch_partition(d_jobs, K, p, d_bins_cm, stream);
+    launch_post_split(d_jobs, K, p, d_feat, stream);
+  }
+
+  void tree_prologue() {
+    launch_init_rows(d_jobs, K, p, d_rows, stream);
+    if (p.quant) launch_discretize(d_jobs, K, p, d_noise_g, d_noise_h, stream);
+    launch_root_sums(d_jobs, K, p, exact_quant_root, stream);
+    CK(cudaMemsetAsync(d_pool, 0, pool_bytes_per_job * K, stream));
+    launch_tree_begin(d_jobs, K, p, stream);
+  }
+
+  void tree_epilogue() {
+    if (p.quant && p.renew) launch_renew(d_jobs, K, p, stream);
+  }
+
+  void run_graph() {
+    if (!graph_exec) {
+      cudaGraph_t g = nullptr;
+      CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      try {
+        tree_prologue();
+        for (int it = 0; it < p.num_leaves - 1; ++it) {
+          step_a(it);
+          step_b();
+        }
+        tree_epilogue();
+      } catch (...) {
+        cudaStreamEndCapture(stream, &g);
+        if (g) cudaGraphDestroy(g);
+        throw;
+      }
+      CK(cudaStreamEndCapture(stream, &g));
+      CK(cudaGraphInstantiate(&graph_exec, g, 0));
+      CK(cudaGraphDestroy(g));
+    }
+    CK(cudaGraphLaunch(graph_exec, stream));
+  }
+
+  void run_stepwise() {
+    tree_prologue();
+    for (int it = 0; it < p.num_leaves - 1; ++it) {
+      step_a(it);
+      // one host round trip per split: has every job stopped?
+      for (int j = 0; j < K; ++j)
+        CK(cudaMemcpyAsync(&h_state[j].stop, &jobs[j].st->stop, sizeof(int32_t), cudaMemcpyDeviceToHost, stream));
+      CK(cudaStreamSynchronize(stream));
+      bool all = true;
+      for (int j = 0; j < K; ++j) all = all && h_state[j].stop;
+      if (all) break;
+      step_b();
+    }
+    tree_epilogue();
+  }
+};
+
+namespace {
+
+int fail_cuda(const CudaError& e) {
+  set_error("CUDA error: %s", e.msg.c_str());
+  return -1;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char* bk_last_error(void) { return g_last_error.c_str(); }
+
+int bk_learner_create(const bk_feature* features, int32_t num_features, const uint8_t* bins, int64_t num_data,
+                      const bk_config* c, int32_t num_jobs, bk_learner** out) {
+  if (!features || !bins || !c || !out || num_features <= 0 || num_data <= 0 || num_jobs <= 0) {
+    set_error("bk_learner_create: invalid arguments");
+    return -1;
+  }
+  if (c->num_leaves < 2) {
+    set_error("num_leaves must be at least 2");
+    return -1;
+  }
+  if (num_data >= (int64_t)INT32_MAX) {
+    set_error("num_data must fit in int32 row indices");
+    return -1;
+  }
+  bool quant = c->use_quantized_grad && c->num_grad_quant_bins >= 2 && c->num_grad_quant_bins <= 127;
+  bk_learner* L = new bk_learner();
+  try {
+    CK(cudaGetDevice(&L->device));
+    CK(cudaDeviceGetAttribute(&L->num_sms, cudaDevAttrMultiProcessorCount, L->device));
+    CK(cudaStreamCreateWithFlags(&L->stream, cudaStreamNonBlocking));
+    Params& p = L->p;
+    p.l1 = c->lambda_l1;
+    p.l2 = c->lambda_l2;
+    p.max_delta = c->max_delta_step;
+    p.smooth = c->path_smooth;
+    p.min_hess = c->min_sum_hessian_in_leaf;
+    p.min_gain = c->min_gain_to_split;
+    p.min_data = c->min_data_in_leaf;
+    p.fused = c->fused_madd ? 1 : 0;
+    p.use_l1 = c->lambda_l1 > 0.0;
+    p.use_max = c->max_delta_step > 0.0;
+    p.use_smooth = c->path_smooth > BK_EPS;
+    p.quant = quant ? 1 : 0;
+    p.const_hess = c->is_constant_hessian ? 1 : 0;
+    p.num_leaves = c->num_leaves;
+    p.max_depth = c->max_depth;
+    p.F = num_features;
+    p.T = (num_features + TILE - 1) / TILE;
+    p.quant_bins = c->num_grad_quant_bins;
+    p.stochastic = c->stochastic_rounding ? 1 : 0;
+    p.renew = c->quant_train_renew_leaf ? 1 : 0;
+    p.part_grid = std::min(1024, 2 * L->num_sms);
+    p.n = num_data;
+    L->K = num_jobs;
+    int maxb = 0;
+    for (int f = 0; f < num_features; ++f) {
+      DevFeature d{};
+      d.num_bin = features[f].num_bin;
+      d.missing = features[f].missing_type;
+      d.default_bin = features[f].default_bin;
+      d.mfb = features[f].most_freq_bin;
+      d.offset = d.mfb == 0 ? 1 : 0;
+      d.gbins = 1 + d.num_bin - d.offset;
+      d.real = features[f].real_feature;
+      d.len = d.num_bin - d.offset;
+      d.penalty = features[f].penalty;
+      if (d.num_bin < 1 || d.gbins > 256 || d.missing < 0 || d.missing > 2 || d.mfb < 0 || d.mfb >= d.num_bin ||
+          d.default_bin < 0 || d.default_bin >= d.num_bin) {
+        set_error("feature %d: unsupported bin mapper (num_bin %d, missing %d, mfb %d, default %d)", f, d.num_bin,
+                  d.missing, d.mfb, d.default_bin);
+        delete L;
+        return -1;
+      }
+      maxb = std::max(maxb, d.gbins);
+      L->h_feat.push_back(d);
+    }
+    // Validate the stored bins once, as the reference's BinsCheck does (histogram.rs:50-65).
+    for (int f = 0; f < num_features; ++f) {
+      const uint8_t* col = bins + (size_t)f * (size_t)num_data;
+      int gb = L->h_feat[f].gbins;
+      for (int64_t i = 0; i < num_data; ++i)
+        if (col[i] >= gb) {
+          set_error("feature %d row %lld: stored bin %d outside [0, %d)", f, (long long)i, (int)col[i], gb);
+          delete L;
+          return -1;
+        }
+    }
+    p.B = (maxb + 7) / 8 * 8;
+    // histogram launch shape: one 1024-thread CTA per SM, split evenly over the feature tiles
+    L->hl.threads = 1024;
+    L->hl.blocks_per_tile = std::max(1, L->num_sms / p.T);
+    bool wide = false;
+    if (quant) {
+      int max_h = p.const_hess ? 1 : p.quant_bins;
+      int max_g = p.quant_bins / 2 + 1;
+      int flush_rows = std::min(65535 / max_h, 32767 / max_g);
+      int per_round = 32 * (L->hl.threads / 32);
+      L->hl.flush_rounds = flush_rows / per_round;
+      wide = L->hl.flush_rounds == 0;
+      // the f64 root sums equal the sequential ones when every partial sum is exact
+      bool pow2 = (p.quant_bins & (p.quant_bins - 1)) == 0;
+      L->exact_quant_root = (pow2 && (double)num_data * (double)p.quant_bins < 536870912.0) ? 1 : 0;
+    }
+    L->hl.smem = hist_smem_bytes(p, L->hl.threads, quant, wide);
+    if (L->hl.smem > 227 * 1024) {
+      set_error("histogram tile needs %zu bytes of shared memory", L->hl.smem);
+      delete L;
+      return -1;
+    }
+    CK(hist_set_smem_attrs(L->hl.smem));
+
+    const size_t n = (size_t)num_data;
+    L->d_feat = L->dalloc<DevFeature>(num_features);
+    CK(cudaMemcpy(L->d_feat, L->h_feat.data(), sizeof(DevFeature) * num_features, cudaMemcpyHostToDevice));
+    L->d_bins_cm = L->dalloc<uint8_t>(n * num_features);
+    CK(cudaMemcpy(L->d_bins_cm, bins, n * num_features, cudaMemcpyHostToDevice));
+    L->d_bins_rt = L->dalloc<uint8_t>(n * p.T * TILE);
+    k_pack_rowtile<<<4 * L->num_sms, 256, 0, L->stream>>>(L->d_bins_cm, L->d_bins_rt, num_data, num_features, p.T);
+    CK(cudaGetLastError());
+    if (quant && p.stochastic) {
+      // GradientDiscretizer::init_stochastic (gradient_discretizer/mod.rs:87-106)
+      std::vector<double> ng(n), nh(n);
+      size_t threads = (size_t)std::max(1, c->num_threads);
+      size_t nb = std::min(threads, (n + 511) / 512), bs = n;
+      if (nb > 1) bs = ((n + nb - 1) / nb + 31) / 32 * 32;
+      if (nb < 1) nb = 1;
+      for (size_t b = 0; b < nb; ++b) {
+        size_t s0 = b * bs, s1 = std::min(s0 + bs, n);
+        HostMt ge((uint32_t)c->seed + (uint32_t)b), he((uint32_t)c->seed + (uint32_t)b + (uint32_t)threads);
+        for (size_t i = s0; i < s1; ++i) {
+          ng[i] = ge.canonical();
+          nh[i] = he.canonical();
+        }
+      }
+      L->d_noise_g = L->dalloc<double>(n);
+      L->d_noise_h = L->dalloc<double>(n);
+      CK(cudaMemcpy(L->d_noise_g, ng.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+      CK(cudaMemcpy(L->d_noise_h, nh.data(), n * sizeof(double), cudaMemcpyHostToDevice));
+    }
+    const int Lv = p.num_leaves, F = num_features, K = num_jobs;
+    L->d_g = L->dalloc<float>(n * K);
+    L->d_h = L->dalloc<float>(n * K);
+    L->d_rows = L->dalloc<int32_t>(n);
+    L->pool_bytes_per_job = (size_t)Lv * p.T * p.B * TILE * (quant ? sizeof(int64_t) : sizeof(double2));
+    L->d_pool = L->dalloc<uint8_t>(L->pool_bytes_per_job * K);
+    JobState* d_states = L->dalloc<JobState>(K);
+    CK(cudaMemset(d_states, 0, sizeof(JobState) * K));
+    L->jobs.resize(K);
+    for (int j = 0; j < K; ++j) {
+      Job& J = L->jobs[j];
+      J.st = d_states + j;
+      J.g = L->d_g + (size_t)j * n;
+      J.h = L->d_h + (size_t)j * n;
+      J.packed = quant ? L->dalloc<int16_t>(n) : nullptr;
+      J.idx0 = L->dalloc<int32_t>(n);
+      J.idx1 = L->dalloc<int32_t>(n);
+      J.leaf_begin = L->dalloc<int64_t>(Lv);
+      J.leaf_count = L->dalloc<int64_t>(Lv);
+      J.leaf_buf = L->dalloc<int32_t>(Lv);
+      J.leaf_depth = L->dalloc<int32_t>(Lv);
+      J.leaf_slot = L->dalloc<int32_t>(Lv);
+      J.leaf_sum = L->dalloc<LeafSum>(Lv);
+      J.best = L->dalloc<Cand>(Lv);
+      J.cand = L->dalloc<Cand>(2 * (size_t)F);
+      J.splittable = L->dalloc<uint8_t>((size_t)Lv * F);
+      J.used = L->dalloc<uint8_t>(F);
+      J.records = L->dalloc<bk_split>(Lv);
+      J.leaf_value = L->dalloc<double>(Lv);
+      J.pool = reinterpret_cast<uint8_t*>(L->d_pool) + L->pool_bytes_per_job * j;
+      J.part_cnt = L->dalloc<int64_t>(p.part_grid);
+      J.red = L->dalloc<double>(2 * kRootGrid);
+      J.ired = L->dalloc<int64_t>(2 * kRootGrid);
+      CK(cudaMemset(J.records, 0, sizeof(bk_split) * Lv));
+    }
+    L->d_jobs = L->dalloc<Job>(K);
+    CK(cudaMemcpy(L->d_jobs, L->jobs.data(), sizeof(Job) * K, cudaMemcpyHostToDevice));
+    if (quant && p.stochastic) launch_mt_seed(L->d_jobs, K, (uint32_t)c->seed, L->stream);
+    CK(cudaMallocHost(&L->h_records, sizeof(bk_split) * (size_t)Lv * K));
+    CK(cudaMallocHost(&L->h_leaf_values, sizeof(double) * (size_t)Lv * K));
+    CK(cudaMallocHost(&L->h_state, sizeof(JobState) * K));
+    L->d_leaf_vals_in = L->dalloc<double>((size_t)Lv * K);
+    CK(cudaEventCreate(&L->ev_start));
+    CK(cudaEventCreate(&L->ev_end));
+    CK(cudaStreamSynchronize(L->stream));
+    CK(cudaGetLastError());
+  } catch (const CudaError& e) {
+    delete L;
+    return fail_cuda(e);
+  }
+  *out = L;
+  return 0;
+}
+
+int bk_learner_train(bk_learner* L, const float* gradients, const float* hessians, int32_t on_device,
+                     const int32_t* rows, int64_t num_rows, bk_split* splits, double* leaf_values,
+                     double* root_outputs, int32_t* num_leaves_out) {
+  if (!L || !gradients || !hessians) {
+    set_error("bk_learner_train: invalid arguments");
+    return -1;
+  }
+  const Params& p = L->p;
+  const size_t n = (size_t)p.n, K = (size_t)L->K;
+  const int Lv = p.num_leaves;
+  try {
+    CK(cudaEventRecord(L->ev_start, L->stream));
+    cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (gradients != L->d_g) CK(cudaMemcpyAsync(L->d_g, gradients, n * K * sizeof(float), kind, L->stream));
+    if (hessians != L->d_h) CK(cudaMemcpyAsync(L->d_h, hessians, n * K * sizeof(float), kind, L->stream));
+    int64_t root_count = rows ? num_rows : (int64_t)n;
+    if (rows) {
+      if (num_rows <= 0 || num_rows > (int64_t)n) {
+        set_error("bk_learner_train: num_rows out of range");
+        return -1;
+      }
+      CK(cudaMemcpyAsync(L->d_rows, rows, sizeof(int32_t) * num_rows, cudaMemcpyHostToDevice, L->stream));
+    }
+    for (size_t j = 0; j < K; ++j) {
+      L->h_state[j].use_rows = rows ? 1 : 0;
+      L->h_state[j].root_count = root_count;
+      L->h_state[j].hist_rows_direct = L->h_state[j].hist_rows_gather = L->h_state[j].hist_builds = 0;
+      JobState* st = L->jobs[j].st;
+      CK(cudaMemcpyAsync(&st->use_rows, &L->h_state[j].use_rows, sizeof(int32_t), cudaMemcpyHostToDevice,
+                         L->stream));
+      CK(cudaMemcpyAsync(&st->root_count, &L->h_state[j].root_count, sizeof(int64_t), cudaMemcpyHostToDevice,
+                         L->stream));
+      CK(cudaMemcpyAsync(&st->hist_rows_direct, &L->h_state[j].hist_rows_direct, 3 * sizeof(int64_t),
+                         cudaMemcpyHostToDevice, L->stream));
+    }
+    if (L->timing && L->hist_events.size() != (size_t)(2 * (Lv - 1))) {
+      for (cudaEvent_t e : L->hist_events) cudaEventDestroy(e);
+      L->hist_events.assign(2 * (Lv - 1), nullptr);
+      for (auto& e : L->hist_events) CK(cudaEventCreate(&e));
+      if (L->graph_exec) {
+        cudaGraphExecDestroy(L->graph_exec);
+        L->graph_exec = nullptr;
+      }
+    }
+    if (L->loop_mode == 1) L->run_graph();
+    else L->run_stepwise();
+    for (size_t j = 0; j < K; ++j) {
+      const Job& J = L->jobs[j];
+      CK(cudaMemcpyAsync(L->h_records + j * Lv, J.records, sizeof(bk_split) * (Lv - 1), cudaMemcpyDeviceToHost,
+                         L->stream));
+      CK(cudaMemcpyAsync(L->h_leaf_values + j * Lv, J.leaf_value, sizeof(double) * Lv, cudaMemcpyDeviceToHost,
+                         L->stream));
+      CK(cudaMemcpyAsync(&L->h_state[j], J.st, offsetof(JobState, mt), cudaMemcpyDeviceToHost, L->stream));
+    }
+    CK(cudaEventRecord(L->ev_end, L->stream));
+    CK(cudaStreamSynchronize(L->stream));
+    CK(cudaGetLastError());
+    float ms = 0.f;
+    CK(cudaEventElapsedTime(&ms, L->ev_start, L->ev_end));
+    L->last_total_ms = ms;
+    L->last_hist_ms = 0.0;
+    if (L->timing) {
+      // histogram launches of the steps that ran (a finished tree's remaining steps return early
+      // but are still timed: they are part of the replayed graph)
+      for (int it = 0; it < Lv - 1; ++it) {
+        float t = 0.f;
+        if (cudaEventElapsedTime(&t, L->hist_events[2 * it], L->hist_events[2 * it + 1]) == cudaSuccess)
+          L->last_hist_ms += t;
+      }
+      cudaGetLastError();
+    }
+    double bytes = 0.0;
+    for (size_t j = 0; j < K; ++j) {
+      const JobState& s = L->h_state[j];
+      double per_row = (double)p.F + (p.quant ? 2.0 : (p.const_hess ? 4.0 : 8.0));
+      bytes += (double)s.hist_rows_direct * per_row + (double)s.hist_rows_gather * (per_row + 4.0);
+      double slot_bytes = 0.0;
+      for (const DevFeature& f : L->h_feat) slot_bytes += (double)f.gbins * (p.quant ? 8.0 : 16.0);
+      bytes += (double)s.hist_builds * slot_bytes;
+    }
+    L->last_hist_bytes = bytes;
+    for (size_t j = 0; j < K; ++j) {
+      const JobState& s = L->h_state[j];
+      int nl = s.tree_leaves;
+      if (num_leaves_out) num_leaves_out[j] = nl;
+      if (root_outputs) root_outputs[j] = s.root_output;
+      if (splits) std::memcpy(splits + j * (Lv - 1), L->h_records + j * Lv, sizeof(bk_split) * (Lv - 1));
+      if (leaf_values) std::memcpy(leaf_values + j * Lv, L->h_leaf_values + j * Lv, sizeof(double) * Lv);
+    }
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
+  }
+  return 0;
+}
+
+int bk_learner_add_prediction_to_score(bk_learner* L, const double* leaf_values, double* score, int32_t on_device) {
+  if (!L || !leaf_values || !score) {
+    set_error("bk_learner_add_prediction_to_score: invalid arguments");
+    return -1;
+  }
+  const Params& p = L->p;
+  const size_t n = (size_t)p.n, K = (size_t)L->K;
+  try {
+    CK(cudaMemcpyAsync(L->d_leaf_vals_in, leaf_values, sizeof(double) * p.num_leaves * K, cudaMemcpyHostToDevice,
+                       L->stream));
+    double* d_score = score;
+    if (!on_device) {
+      d_score = nullptr;
+      CK(cudaMallocAsync((void**)&d_score, n * K * sizeof(double), L->stream));
+      CK(cudaMemcpyAsync(d_score, score, n * K * sizeof(double), cudaMemcpyHostToDevice, L->stream));
+    }
+    launch_add_score(L->d_jobs, L->K, p, L->d_leaf_vals_in, d_score, L->stream);
+    if (!on_device) {
+      CK(cudaMemcpyAsync(score, d_score, n * K * sizeof(double), cudaMemcpyDeviceToHost, L->stream));
+      CK(cudaFreeAsync(d_score, L->stream));
+    }
+    CK(cudaStreamSynchronize(L->stream));
+    CK(cudaGetLastError());
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
+  }
+  return 0;
+}
+
+int bk_learner_row_leaf(bk_learner* L, int32_t* out) {
+  if (!L || !out) {
+    set_error("bk_learner_row_leaf: invalid arguments");
+    return -1;
+  }
+  const Params& p = L->p;
+  const size_t n = (size_t)p.n, K = (size_t)L->K;
+  try {
+    int32_t* d = nullptr;
+    CK(cudaMallocAsync((void**)&d, n * K * sizeof(int32_t), L->stream));
+    CK(cudaMemsetAsync(d, 0xff, n * K * sizeof(int32_t), L->stream));
+    launch_row_leaf(L->d_jobs, L->K, p, d, L->stream);
+    CK(cudaMemcpyAsync(out, d, n * K * sizeof(int32_t), cudaMemcpyDeviceToHost, L->stream));
+    CK(cudaFreeAsync(d, L->stream));
+    CK(cudaStreamSynchronize(L->stream));
+    CK(cudaGetLastError());
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
+  }
+  return 0;
+}
+
+int bk_learner_set_loop_mode(bk_learner* L, int32_t mode) {
+  if (!L || (mode != 0 && mode != 1)) {
+    set_error("bk_learner_set_loop_mode: mode must be 0 or 1");
+    return -1;
+  }
+  L->loop_mode = mode;
+  return 0;
+}
+
+int bk_learner_set_timing(bk_learner* L, int32_t on) {
+  if (!L) {
+    set_error("bk_learner_set_timing: null learner");
+    return -1;
+  }
+  if ((on != 0) != L->timing && L->graph_exec) {
+    cudaGraphExecDestroy(L->graph_exec);
+    L->graph_exec = nullptr;
+  }
+  L->timing = on != 0;
+  return 0;
+}
+
+int bk_learner_reset_constant_hessian(bk_learner* L, int32_t value) {
+  if (!L) {
+    set_error("bk_learner_reset_constant_hessian: null learner");
+    return -1;
+  }
+  if (L->p.quant) {
+    set_error("constant-hessian changes after creation are not supported on the quantized path");
+    return -1;
+  }
+  int v = value ? 1 : 0;
+  if (v != L->p.const_hess) {
+    L->p.const_hess = v;
+    size_t smem = hist_smem_bytes(L->p, L->hl.threads, false, false);
+    L->hl.smem = smem;
+    cudaError_t e = hist_set_smem_attrs(smem);
+    if (e != cudaSuccess) {
+      set_error("CUDA error: %s", cudaGetErrorString(e));
+      return -1;
+    }
+    if (L->graph_exec) {
+      cudaGraphExecDestroy(L->graph_exec);
+      L->graph_exec = nullptr;
+    }
+  }
+  return 0;
+}
+
+int bk_learner_last_timing(bk_learner* L, double* total_ms, double* hist_ms, double* hist_bytes) {
+  if (!L) {
+    set_error("bk_learner_last_timing: null learner");
+    return -1;
+  }
+  if (total_ms) *total_ms = L->last_total_ms;
+  if (hist_ms) *hist_ms = L->last_hist_ms;
+  if (hist_bytes) *hist_bytes = L->last_hist_bytes;
+  return 0;
+}
+
+int bk_learner_gradient_buffers(bk_learner* L, float** gradients, float** hessians) {
+  if (!L) {
+    set_error("bk_learner_gradient_buffers: null learner");
+    return -1;
+  }
+  if (gradients) *gradients = L->d_g;
+  if (hessians) *hessians = L->d_h;
+  return 0;
+}
+
+int bk_learner_objective_gradients(bk_learner* L, int32_t kind, const double* score, const float* label,
+                                   double sigmoid) {
+  if (!L || !score || !label || kind < 0 || kind > 2 || (kind == 2) != (L->K > 1) || L->K > 32) {
+    set_error("bk_learner_objective_gradients: invalid arguments (kind %d, num_jobs %d)", kind, L ? L->K : 0);
+    return -1;
+  }
+  try {
+    CK(objective_gradients(kind, score, label, L->p.n, L->K, sigmoid, L->d_g, L->d_h, L->stream));
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
+  }
+  return 0;
+}
+
+int bk_learner_objective_loss(bk_learner* L, int32_t kind, const double* score, const float* label, double* out) {
+  if (!L || !score || !label || !out || kind < 0 || kind > 2) {
+    set_error("bk_learner_objective_loss: invalid arguments");
+    return -1;
+  }
+  try {
+    const int grid = 512;
+    double* d_part = L->jobs[0].red;  // 2 * kRootGrid >= grid doubles of scratch
+    CK(objective_loss(kind, score, label, L->p.n, L->K, d_part, grid, L->stream));
+    std::vector<double> part(grid);
+    CK(cudaMemcpyAsync(part.data(), d_part, sizeof(double) * grid, cudaMemcpyDeviceToHost, L->stream));
+    CK(cudaStreamSynchronize(L->stream));
+    double s = 0.0;
+    for (double v : part) s += v;
+    *out = s / (double)L->p.n;
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
+  }
+  return 0;
+}
+
+int bk_learner_stream(bk_learner* L, void** stream) {
+  if (!L || !stream) {
+    set_error("bk_learner_stream: invalid arguments");
+    return -1;
+  }
+  *stream = (void*)L->stream;
+  return 0;
+}
+
+int bk_learner_destroy(bk_learner* L) {
+  delete L;
+  return 0;
+}
+
+}  // extern "C"

@@ -1,0 +1,112 @@
+// Built-in objective gradients on the device, written into the learner's gradient buffers, and
+// the training loss, so one boosting iteration (gradients, K trees, score update) stays in HBM:
+//   L2         objective/regression.rs:240-248   g = (score - label) as f32, h = 1
+//   binary     objective/binary.rs:71-90         response = -label*s / (1 + exp(label*s*score))
+//   multiclass objective/multiclass.rs:68-90     softmax over the K class scores of a row
+// Operation order follows the reference. `exp` is CUDA's double-precision exp, which can differ
+// from the host libm's in the last bit, so binary / multiclass gradients may differ from a host
+// computation by one f32 ulp; the learner's parity is checked on given gradients.
+#include <math_constants.h>
+
+#include "bk_common.cuh"
+
+namespace bk {
+
+namespace {
+
+__global__ void k_grad_l2(const double* __restrict__ score, const float* __restrict__ label, int64_t n,
+                          float* __restrict__ g, float* __restrict__ h) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    g[i] = (float)(score[i] - (double)label[i]);
+    h[i] = 1.0f;
+  }
+}
+
+__global__ void k_grad_binary(const double* __restrict__ score, const float* __restrict__ label, int64_t n,
+                              double sigmoid, float* __restrict__ g, float* __restrict__ h) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double lab = label[i] > 0.0f ? 1.0 : -1.0;
+    double t = -lab * sigmoid;
+    double e = exp(lab * sigmoid * score[i]);
+    double response = t / (1.0 + e);
+    double ar = fabs(response);
+    g[i] = (float)(response * 1.0);
+    double q = ar * (sigmoid - ar);
+    h[i] = (float)(q * 1.0);
+  }
+}
+
+__global__ void k_grad_softmax(const double* __restrict__ score, const float* __restrict__ label, int64_t n, int K,
+                               float* __restrict__ g, float* __restrict__ h) {
+  const double factor = (double)K / ((double)K - 1.0);
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    double rec[32];
+    double wmax = score[i];
+    for (int k = 1; k < K; ++k) wmax = fmax(score[(size_t)k * n + i], wmax);
+    double wsum = 0.0;
+    for (int k = 0; k < K; ++k) {
+      rec[k] = exp(score[(size_t)k * n + i] - wmax);
+      wsum += rec[k];
+    }
+    int lab = (int)label[i];
+    for (int k = 0; k < K; ++k) {
+      double p = rec[k] / wsum;
+      double gi = lab == k ? p - 1.0 : p;
+      double hi = factor * p;
+      hi = hi * (1.0 - p);
+      g[(size_t)k * n + i] = (float)gi;
+      h[(size_t)k * n + i] = (float)hi;
+    }
+  }
+}
+
+// Per-CTA partial losses (mean squared error / log loss / multiclass log loss).
+__global__ void k_loss(int kind, const double* __restrict__ score, const float* __restrict__ label, int64_t n, int K,
+                       double* __restrict__ partial) {
+  double acc = 0.0;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    if (kind == 0) {
+      double d = score[i] - (double)label[i];
+      acc += d * d;
+    } else if (kind == 1) {
+      double p = 1.0 / (1.0 + exp(-score[i]));
+      p = fmin(fmax(p, 1e-15), 1.0 - 1e-15);
+      acc += label[i] > 0.0f ? -log(p) : -log(1.0 - p);
+    } else {
+      double wmax = score[i];
+      for (int k = 1; k < K; ++k) wmax = fmax(score[(size_t)k * n + i], wmax);
+      double wsum = 0.0;
+      for (int k = 0; k < K; ++k) wsum += exp(score[(size_t)k * n + i] - wmax);
+      int lab = (int)label[i];
+      acc += -(score[(size_t)lab * n + i] - wmax - log(wsum));
+    }
+  }
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
+  __shared__ double sh[32];
+  if ((threadIdx.x & 31) == 0) sh[threadIdx.x >> 5] = acc;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double s = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) s += sh[w];
+    partial[blockIdx.x] = s;
+  }
+}
+
+}  // namespace
+
+cudaError_t objective_gradients(int kind, const double* score, const float* label, int64_t n, int K, double sigmoid,
+                                float* g, float* h, cudaStream_t s) {
+  const int grid = 1024, threads = 256;
+  if (kind == 0) k_grad_l2<<<grid, threads, 0, s>>>(score, label, n, g, h);
+  else if (kind == 1) k_grad_binary<<<grid, threads, 0, s>>>(score, label, n, sigmoid, g, h);
+  else k_grad_softmax<<<grid, threads, 0, s>>>(score, label, n, K, g, h);
+  return cudaGetLastError();
+}
+
+cudaError_t objective_loss(int kind, const double* score, const float* label, int64_t n, int K, double* partial,
+                           int grid, cudaStream_t s) {
+  k_loss<<<grid, 256, 0, s>>>(kind, score, label, n, K, partial);
+  return cudaGetLastError();
+}
+
+}  // namespace bk

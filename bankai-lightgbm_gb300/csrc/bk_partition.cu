@@ -1,0 +1,154 @@
+// DataPartition::Split (data_partition.rs:124-174), GB300 form: a stable partition of the
+// split leaf's row-index range into the left rows (kept in leaf order) followed by the right
+// rows (kept in leaf order), written into the other index buffer.
+//
+// The reference routes each row through SplitRule::route_bin; here k_decide evaluates that rule
+// once per stored bin into a 256-entry route table, so routing a row is one byte read of the
+// split feature's column-major bins plus one shared-memory lookup. Three kernels on a fixed grid
+// (so the step can be captured in a CUDA graph while the leaf size varies): count the left rows
+// of each CTA's contiguous chunk, scan the chunk counts, scatter with a block-wide scan.
+#include "bk_common.cuh"
+
+namespace bk {
+
+namespace {
+
+constexpr int kThreads = 256;
+constexpr int kItems = 8;
+
+struct PartRange {
+  int64_t begin, count, r0, r1;
+  const int32_t* src;
+  int32_t* dst;
+  const uint8_t* col;
+};
+
+__device__ __forceinline__ void part_range(const Job& J, const Params& p, const uint8_t* bins_cm, PartRange* r) {
+  const JobState* st = J.st;
+  int32_t leaf = st->split_leaf;
+  r->begin = J.leaf_begin[leaf];
+  r->count = J.leaf_count[leaf];
+  int32_t buf = J.leaf_buf[leaf];
+  r->src = leaf_idx(J, buf) + r->begin;
+  r->dst = leaf_idx_w(J, 1 - buf) + r->begin;
+  r->col = bins_cm + (size_t)st->split_inner * (size_t)p.n;
+  int64_t chunk = ceil_div64(r->count, p.part_grid);
+  chunk = (chunk + kThreads * kItems - 1) / (kThreads * kItems) * (kThreads * kItems);
+  r->r0 = min((int64_t)blockIdx.x * chunk, r->count);
+  r->r1 = min(r->r0 + chunk, r->count);
+}
+
+template <typename T>
+__device__ __forceinline__ T block_excl_scan(T v, T* total, T* sh) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  T x = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T u = __shfl_up_sync(0xffffffffu, x, o);
+    if (lane >= o) x += u;
+  }
+  if (lane == 31) sh[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    T w = lane < (int)(blockDim.x >> 5) ? sh[lane] : (T)0;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      T u = __shfl_up_sync(0xffffffffu, w, o);
+      if (lane >= o) w += u;
+    }
+    if (lane < (int)(blockDim.x >> 5)) sh[lane] = w;
+  }
+  __syncthreads();
+  T warp_prefix = warp > 0 ? sh[warp - 1] : (T)0;
+  *total = sh[(blockDim.x >> 5) - 1];
+  T excl = warp_prefix + x - v;
+  __syncthreads();
+  return excl;
+}
+
+__global__ void __launch_bounds__(kThreads) k_part_count(const Job* __restrict__ jobs, Params p,
+                                                         const uint8_t* __restrict__ bins_cm) {
+  __shared__ uint8_t lut[256];
+  __shared__ int64_t sh[32];
+  const Job& J = jobs[blockIdx.z];
+  if (J.st->stop) return;
+  lut[threadIdx.x] = J.st->route[threadIdx.x];
+  __syncthreads();
+  PartRange R;
+  part_range(J, p, bins_cm, &R);
+  int64_t local = 0;
+  for (int64_t i = R.r0 + threadIdx.x; i < R.r1; i += kThreads) local += lut[R.col[R.src[i]]];
+  int64_t total;
+  block_excl_scan<int64_t>(local, &total, sh);
+  if (threadIdx.x == 0) J.part_cnt[blockIdx.x] = total;
+}
+
+__global__ void __launch_bounds__(1024) k_part_scan(const Job* __restrict__ jobs, Params p) {
+  __shared__ int64_t sh[32];
+  const Job& J = jobs[blockIdx.z];
+  if (J.st->stop) return;
+  int64_t v = threadIdx.x < (unsigned)p.part_grid ? J.part_cnt[threadIdx.x] : 0;
+  int64_t total;
+  int64_t ex = block_excl_scan<int64_t>(v, &total, sh);
+  if (threadIdx.x < (unsigned)p.part_grid) J.part_cnt[threadIdx.x] = ex;
+  if (threadIdx.x == 0) J.st->total_left = total;
+}
+
+__global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict__ jobs, Params p,
+                                                           const uint8_t* __restrict__ bins_cm) {
+  __shared__ uint8_t lut[256];
+  __shared__ int32_t sh[32];
+  const Job& J = jobs[blockIdx.z];
+  if (J.st->stop) return;
+  lut[threadIdx.x] = J.st->route[threadIdx.x];
+  __syncthreads();
+  PartRange R;
+  part_range(J, p, bins_cm, &R);
+  const int64_t total_left = J.st->total_left;
+  int64_t running = J.part_cnt[blockIdx.x];  // left rows before this chunk
+  for (int64_t base = R.r0; base < R.r1; base += kThreads * kItems) {
+    int64_t e0 = base + (int64_t)threadIdx.x * kItems;
+    int32_t rows[kItems];
+    uint32_t flags = 0;
+    int32_t cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+      int64_t e = e0 + k;
+      rows[k] = 0;
+      if (e < R.r1) {
+        rows[k] = R.src[e];
+        if (lut[R.col[rows[k]]]) {
+          flags |= 1u << k;
+          ++cnt;
+        }
+      }
+    }
+    int32_t tile_total;
+    int32_t pre = block_excl_scan<int32_t>(cnt, &tile_total, sh);
+    int64_t left_before = running + pre;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+      int64_t e = e0 + k;
+      if (e < R.r1) {
+        if (flags & (1u << k)) {
+          R.dst[left_before] = rows[k];
+          ++left_before;
+        } else {
+          R.dst[total_left + (e - left_before)] = rows[k];
+        }
+      }
+    }
+    running += tile_total;
+  }
+}
+
+}  // namespace
+
+void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm, cudaStream_t s) {
+  dim3 grid(p.part_grid, 1, num_jobs);
+  k_part_count<<<grid, kThreads, 0, s>>>(d_jobs, p, bins_cm);
+  k_part_scan<<<dim3(1, 1, num_jobs), 1024, 0, s>>>(d_jobs, p);
+  k_part_scatter<<<grid, kThreads, 0, s>>>(d_jobs, p, bins_cm);
+}
+
+}  // namespace bk

@@ -52,7 +52,25 @@ def _declare(lib):
 c = ctypes
 _P, _i32, _i64, _u32, _f64 = c.c_void_p, c.c_int32, c.c_int64, c.c_uint32, c.c_double
 # (name, restype, argtypes) of the learner entry points declared in include/bkgpu.h
-_GPU_SIGNATURES = []
+_GPU_SIGNATURES = [
+    ("bk_learner_create", _i32, [_P, _i32, _P, _i64, _P, _i32, _P]),
+    ("bk_learner_train", _i32, [_P, _P, _P, _i32, _P, _i64, _P, _P, _P, _P]),
+    ("bk_learner_add_prediction_to_score", _i32, [_P, _P, _P, _i32]),
+    ("bk_learner_row_leaf", _i32, [_P, _P]),
+    ("bk_learner_set_loop_mode", _i32, [_P, _i32]),
+    ("bk_learner_reset_constant_hessian", _i32, [_P, _i32]),
+    ("bk_learner_last_timing", _i32, [_P, _P, _P, _P]),
+    ("bk_learner_set_timing", _i32, [_P, _i32]),
+    ("bk_learner_gradient_buffers", _i32, [_P, _P, _P]),
+    ("bk_learner_objective_gradients", _i32, [_P, _i32, _P, _P, _f64]),
+    ("bk_learner_objective_loss", _i32, [_P, _i32, _P, _P, _P]),
+    ("bk_learner_stream", _i32, [_P, _P]),
+    ("bk_learner_destroy", _i32, [_P]),
+]
+
+# every symbol include/bkgpu.h declares
+EXPORTED = [name for name, _, _ in _GPU_SIGNATURES] + ["bk_last_error", "bk_find_bin_numerical",
+                                                        "bk_values_to_group_bins"]
 
 
 def last_error() -> str:

@@ -1,0 +1,126 @@
+"""``GpuTreeLearner`` — the host-side mirror of bankai-lightgbm's ``SerialTreeLearner``
+(crates/lgbm-core/src/treelearner/serial.rs:183-2044) over the C ABI of ``lib/libbkgpu.so``.
+
+Same constructor inputs (a binned dataset, the learner config, ``is_constant_hessian``), same
+``train(gradients, hessians, rows) -> tree`` contract, same score update. Training runs on the
+GPU; there is no CPU path.
+"""
+import ctypes
+
+import numpy as np
+
+from . import _lib
+from .config import LearnerConfig
+from .tree import SPLIT_DTYPE, Tree
+
+
+class GpuTreeLearner:
+    def __init__(self, ds, cfg: LearnerConfig, num_jobs: int = 1, loop_mode: int = 1):
+        self.lib = _lib.load()
+        self.ds = ds
+        self.cfg = cfg
+        self.num_jobs = int(num_jobs)
+        self.num_leaves = int(cfg.num_leaves)
+        self._feats = ds.feature_array()
+        self._bins = np.ascontiguousarray(ds.bins, dtype=np.uint8)
+        self._rec = cfg.record()
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.bk_learner_create(self._feats.ctypes.data, ds.num_features, self._bins.ctypes.data,
+                                              ds.num_data, self._rec.ctypes.data, self.num_jobs, ctypes.byref(h)),
+                   "bk_learner_create")
+        self.h = h
+        self.set_loop_mode(loop_mode)
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bk_learner_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_loop_mode(self, mode: int):
+        _lib.check(self.lib.bk_learner_set_loop_mode(self.h, int(mode)), "bk_learner_set_loop_mode")
+
+    def set_timing(self, on: bool):
+        _lib.check(self.lib.bk_learner_set_timing(self.h, int(bool(on))), "bk_learner_set_timing")
+
+    def last_timing(self):
+        t = (ctypes.c_double * 3)()
+        _lib.check(self.lib.bk_learner_last_timing(self.h, ctypes.byref(t, 0), ctypes.byref(t, 8),
+                                                   ctypes.byref(t, 16)), "bk_learner_last_timing")
+        return {"total_ms": t[0], "hist_ms": t[1], "hist_bytes": t[2]}
+
+    def stream(self):
+        s = ctypes.c_void_p()
+        _lib.check(self.lib.bk_learner_stream(self.h, ctypes.byref(s)), "bk_learner_stream")
+        return s.value
+
+    def objective_gradients(self, kind, score_ptr, label_ptr, sigmoid=1.0):
+        _lib.check(self.lib.bk_learner_objective_gradients(self.h, int(kind), int(score_ptr), int(label_ptr),
+                                                           float(sigmoid)), "bk_learner_objective_gradients")
+
+    def objective_loss(self, kind, score_ptr, label_ptr):
+        out = ctypes.c_double()
+        _lib.check(self.lib.bk_learner_objective_loss(self.h, int(kind), int(score_ptr), int(label_ptr),
+                                                      ctypes.byref(out)), "bk_learner_objective_loss")
+        return out.value
+
+    def gradient_buffers(self):
+        g = ctypes.c_void_p()
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.bk_learner_gradient_buffers(self.h, ctypes.byref(g), ctypes.byref(h)),
+                   "bk_learner_gradient_buffers")
+        return g.value, h.value
+
+    def train_raw(self, gradients, hessians, rows=None, on_device=False):
+        """Trains num_jobs trees. gradients/hessians: [num_jobs, num_data] float32 (numpy), or device
+        pointers (int) with on_device=True. Returns (splits, leaf_values, root_outputs, num_leaves)."""
+        K, Lv = self.num_jobs, self.num_leaves
+        if on_device:
+            gp, hp = int(gradients), int(hessians)
+        else:
+            g = np.ascontiguousarray(gradients, dtype=np.float32).reshape(K, -1)
+            hh = np.ascontiguousarray(hessians, dtype=np.float32).reshape(K, -1)
+            assert g.shape[1] == self.ds.num_data and hh.shape == g.shape
+            gp, hp = g.ctypes.data, hh.ctypes.data
+        rows_arr = None if rows is None else np.ascontiguousarray(rows, dtype=np.int32)
+        splits = np.zeros((K, max(Lv - 1, 1)), dtype=SPLIT_DTYPE)
+        leaf_values = np.zeros((K, Lv), dtype=np.float64)
+        roots = np.zeros(K, dtype=np.float64)
+        nls = np.zeros(K, dtype=np.int32)
+        _lib.check(self.lib.bk_learner_train(self.h, gp, hp, int(bool(on_device)),
+                                             None if rows_arr is None else rows_arr.ctypes.data,
+                                             0 if rows_arr is None else len(rows_arr), splits.ctypes.data,
+                                             leaf_values.ctypes.data, roots.ctypes.data, nls.ctypes.data),
+                   "bk_learner_train")
+        return splits, leaf_values, roots, nls
+
+    def train(self, gradients, hessians, rows=None):
+        """SerialTreeLearner::train for a single job: (splits, leaf_values, root_output)."""
+        assert self.num_jobs == 1
+        splits, lv, roots, nls = self.train_raw(np.asarray(gradients)[None, :], np.asarray(hessians)[None, :], rows)
+        nl = int(nls[0])
+        return splits[0, :nl - 1].copy(), lv[0, :nl].copy(), float(roots[0])
+
+    def trees(self, splits, leaf_values, roots, nls):
+        return [Tree.from_records(self.num_leaves, splits[j, :nls[j] - 1], leaf_values[j, :nls[j]], roots[j],
+                                  self.ds.features, self.cfg.min_gain_to_split) for j in range(self.num_jobs)]
+
+    def row_leaf(self):
+        out = np.zeros((self.num_jobs, self.ds.num_data), dtype=np.int32)
+        _lib.check(self.lib.bk_learner_row_leaf(self.h, out.ctypes.data), "bk_learner_row_leaf")
+        return out[0] if self.num_jobs == 1 else out
+
+    def add_prediction_to_score(self, leaf_values, score, on_device=False):
+        lv = np.ascontiguousarray(leaf_values, dtype=np.float64).reshape(self.num_jobs, self.num_leaves)
+        if on_device:
+            _lib.check(self.lib.bk_learner_add_prediction_to_score(self.h, lv.ctypes.data, int(score), 1),
+                       "bk_learner_add_prediction_to_score")
+        else:
+            assert score.dtype == np.float64 and score.flags.c_contiguous
+            _lib.check(self.lib.bk_learner_add_prediction_to_score(self.h, lv.ctypes.data, score.ctypes.data, 0),
+                       "bk_learner_add_prediction_to_score")

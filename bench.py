@@ -1,0 +1,316 @@
+#!/usr/bin/env python
+"""Benchmark: boosting iterations per second of the GB300 tree learner.
+
+Workload: L2 regression, 10,000,000 rows x 100 float32 features (70 N(0,1), 30 integer 0..15,
+10% NaN), target = sum of 20 random step functions + N(0, 0.1); max_bin 255, num_leaves 255,
+learning rate 0.1. Synthetic data of that shape (seeded) stands in for real data.
+
+A step is one boosting iteration: L2 gradients on the device, one tree (histograms, split
+search, partition, bookkeeping), and the score update. Two forms of the learner are timed:
+  * quantized+batched: int8 discretized gradients, exact integer histograms, and the whole
+    grow loop of an iteration replayed as one CUDA graph  -> the reported `value`;
+  * plain: fp32 compensated histograms with f64 gains and one host round trip per split.
+
+`e2e` is the same metric through the C ABI with host buffers: every step copies that step's
+gradients / hessians from pinned host memory to the device inside the timed region and reads
+the training loss back.
+
+`--impl reference` times the CPU learner (the oracle port of the reference's tree learner, with
+all host threads) on a bounded row sample of the same workload and scales to the full workload.
+
+Multi-GPU (`--gpus N`, torchrun): independent replicas, one per GPU (the path has no exchange
+step in this build); value = iterations of all ranks / max time over ranks.
+"""
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "bankai-lightgbm_gb300"))
+
+METRIC = "iters/s (10M x 100, 255 leaves) quantized+batched vs plain GPU; hist HBM GB/s"
+WORKLOAD = ("L2 regression 10M x 100 (70 N(0,1) + 30 int 0..15, 10% NaN), max_bin 255, 255 leaves, "
+            "lr 0.1; step = device gradients + 1 tree + score update")
+
+
+def _peaks():
+    try:
+        d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons during the timed region."""
+    FIELDS = ("clocks.sm,clocks.max.sm,clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) == 6:
+                self.samples.append(parts)
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[2 + i].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def build_dataset(rows, seed=0):
+    from lgbm_gb300 import BinnedDataset, synthetic
+    X, y = synthetic.l2_steps(n=rows, seed=seed)
+    ds = BinnedDataset.from_dense(X, max_bin=255, min_data_in_leaf=20, threads=min(32, os.cpu_count() or 8))
+    del X
+    return ds, y
+
+
+def make_cfg(quant, num_leaves=255):
+    from lgbm_gb300 import LearnerConfig
+    return LearnerConfig(num_leaves=num_leaves, min_data_in_leaf=20, use_quantized_grad=int(quant),
+                         num_grad_quant_bins=4, stochastic_rounding=1, seed=0, num_threads=16, fused_madd=1,
+                         is_constant_hessian=1)
+
+
+def run_gpu(args, rank, world):
+    import torch
+    from lgbm_gb300 import GpuTreeLearner, _lib
+    from lgbm_gb300.tree import Tree
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+    lr = 0.1
+    t0 = time.time()
+    ds, y = build_dataset(args.rows)
+    prep_s = time.time() - t0
+    n = ds.num_data
+    label = torch.from_numpy(y).cuda()
+    peak, peak_kind = _peaks()
+
+    def form(quant, loop_mode, steps, warmup, e2e=False, timing=False):
+        learner = GpuTreeLearner(ds, make_cfg(quant, args.leaves), loop_mode=loop_mode)
+        learner.set_timing(timing)
+        stream = torch.cuda.ExternalStream(learner.stream())
+        score = torch.full((n,), float(y.astype(np.float64).mean()), dtype=torch.float64, device="cuda")
+        gbuf, hbuf = learner.gradient_buffers()
+        torch.cuda.synchronize()  # score and labels are written on torch's stream
+        pin_g = torch.empty(n, dtype=torch.float32).pin_memory() if e2e else None
+        pin_h = torch.empty(n, dtype=torch.float32).pin_memory() if e2e else None
+        stats = dict(hist_ms=0.0, hist_bytes=0.0, leaves=0, loss=None)
+        total_ms = 0.0
+
+        def step(timed):
+            nonlocal total_ms
+            if e2e:
+                # this step's inputs live in pinned host memory (computed by the objective from the
+                # current score outside the timed region)
+                learner.objective_gradients(0, score.data_ptr(), label.data_ptr())
+                torch.cuda.synchronize()
+                pin_g.copy_(_device_view(gbuf, n))
+                pin_h.copy_(_device_view(hbuf, n))
+                torch.cuda.synchronize()
+            ev0 = torch.cuda.Event(enable_timing=True)
+            ev1 = torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            if e2e:
+                splits, lv, roots, nls = _host_train(learner, pin_g, pin_h)
+            else:
+                learner.objective_gradients(0, score.data_ptr(), label.data_ptr())
+                splits, lv, roots, nls = learner.train_raw(gbuf, hbuf, on_device=True)
+            t = Tree.from_records(args.leaves, splits[0, :nls[0] - 1], lv[0, :nls[0]], roots[0], ds.features)
+            t.apply_shrinkage(lr)
+            vals = np.zeros(args.leaves)
+            vals[:t.num_leaves] = t.leaf_value[:t.num_leaves]
+            learner.add_prediction_to_score(vals, score.data_ptr(), on_device=True)
+            if e2e:
+                stats["loss"] = learner.objective_loss(0, score.data_ptr(), label.data_ptr())
+            ev1.record(stream)
+            ev1.synchronize()
+            if timed:
+                total_ms += ev0.elapsed_time(ev1)
+                tm = learner.last_timing()
+                stats["hist_ms"] += tm["hist_ms"]
+                stats["hist_bytes"] += tm["hist_bytes"]
+                stats["leaves"] += int(nls[0])
+
+        for _ in range(warmup):
+            step(False)
+        torch.cuda.synchronize()
+        for _ in range(steps):
+            step(True)
+        torch.cuda.synchronize()
+        stats["ms_per_step"] = total_ms / max(steps, 1)
+        stats["loss_final"] = learner.objective_loss(0, score.data_ptr(), label.data_ptr())
+        learner.close()
+        return stats
+
+    def _host_train(learner, pg, ph):
+        """bk_learner_train on host (pinned) gradient buffers: the copy to the device is inside."""
+        K, Lv = learner.num_jobs, learner.num_leaves
+        from lgbm_gb300.tree import SPLIT_DTYPE
+        splits = np.zeros((K, Lv - 1), dtype=SPLIT_DTYPE)
+        lv = np.zeros((K, Lv))
+        roots = np.zeros(K)
+        nls = np.zeros(K, np.int32)
+        _lib.check(learner.lib.bk_learner_train(learner.h, pg.data_ptr(), ph.data_ptr(), 0, None, 0,
+                                                splits.ctypes.data, lv.ctypes.data, roots.ctypes.data,
+                                                nls.ctypes.data), "bk_learner_train")
+        return splits, lv, roots, nls
+
+    if world > 1:
+        torch.distributed.barrier()
+    clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
+    clocks.start()
+    wall0 = time.time()
+    main = form(True, 1, args.steps, args.warmup, timing=True)
+    wall = time.time() - wall0
+    clk = clocks.stop()
+    plain = form(False, 0, max(1, args.steps // 2), 1)
+    e2e = form(True, 1, args.steps, 1, e2e=True)
+    ms = main["ms_per_step"]
+    if world > 1:
+        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world * 1000.0 / ms
+    hist_gbs = main["hist_bytes"] / (main["hist_ms"] * 1e6) if main["hist_ms"] > 0 else None
+    launches_per_step = 4 + 4 + 1 + 1 + 7 * (args.leaves - 1) + 1
+    line = {
+        "metric": METRIC, "value": round(value, 4), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "int8 grad/hess, int64 histograms, f64 gains", "data": "synthetic (seeded)",
+        "config": {"workload": WORKLOAD, "rows": ds.num_data, "features": ds.num_features, "num_leaves": args.leaves,
+                   "parallelism": "replicas" if world > 1 else "single GPU",
+                   "l2_flush": "inputs larger than L2 (bins %.2f GB)" % (ds.num_data * ds.num_features / 1e9)},
+        "forms": {"quantized_graph": {"iters_per_s": round(1000.0 / main["ms_per_step"], 4),
+                                      "train_l2": main["loss_final"]},
+                  "plain_float_stepwise": {"iters_per_s": round(1000.0 / plain["ms_per_step"], 4),
+                                           "train_l2": plain["loss_final"]}},
+        "e2e": {"value": round(world * 1000.0 / e2e["ms_per_step"], 4), "unit": "iters/s",
+                "h2d_bytes_per_step": 2 * 4 * ds.num_data,
+                "d2h_bytes_per_step": 112 * (args.leaves - 1) + 8 * args.leaves + 8 + 8},
+        "roofline": {"bound": "hbm", "achieved": round(hist_gbs, 1) if hist_gbs else None, "peak": peak,
+                     "unit": "GB/s", "frac": round(hist_gbs / peak, 4) if hist_gbs else None, "traffic": None,
+                     "kernel": "k_hist_int (quantized histogram)", "peak_kind": peak_kind},
+        "gpu_launches": launches_per_step * args.steps,
+        "clocks": clk,
+        "prep_s": round(prep_s, 1),
+    }
+    if rank == 0:
+        line["cpu_baseline"] = cpu_baseline(ds, y, sample_rows=args.cpu_rows)
+    return line
+
+
+def _device_view(ptr, count):
+    """A float32 tensor view of a device buffer owned by the learner (CUDA array interface)."""
+    import torch
+
+    class _CAI:
+        __cuda_array_interface__ = {"shape": (count,), "typestr": "<f4", "data": (int(ptr), False),
+                                    "version": 3, "strides": None}
+    return torch.as_tensor(_CAI(), device="cuda")
+
+
+def cpu_baseline(ds, y, sample_rows, threads=None):
+    """The oracle (the C++ port of the reference's tree learner) on the first `sample_rows` rows
+    of the same binned data: one float-path iteration (L2 gradients, one 255-leaf tree),
+    scaled to the full row count (linear in rows)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import harness
+    from lgbm_gb300 import BinnedDataset
+    threads = threads or 1
+    m = min(sample_rows, ds.num_data)
+    sub = BinnedDataset(np.ascontiguousarray(ds.bins[:, :m]), ds.features, ds.num_total_features)
+    cfg = make_cfg(False)
+    cfg.values["num_threads"] = threads
+    orc = harness.OracleLearner(sub, cfg)
+    score = np.full(m, float(np.mean(y[:m], dtype=np.float64)))
+    g = (score - y[:m].astype(np.float64)).astype(np.float32)
+    h = np.ones(m, np.float32)
+    t0 = time.time()
+    orc.train(g, h)
+    dt = time.time() - t0
+    return {"value": round((1.0 / dt) * (m / ds.num_data), 6), "unit": "iters/s", "cores": threads, "kind": "port",
+            "sample": "oracle float path, one 255-leaf tree on the first %d of %d rows (%.1f s), scaled by rows"
+                      % (m, ds.num_data, dt)}
+
+
+def run_reference(args):
+    """CPU arm: the oracle port with all host threads, same workload, bounded sample per step."""
+    threads = os.cpu_count() or 1
+    ds, y = build_dataset(args.rows)
+    steps = []
+    for _ in range(args.warmup):
+        cpu_baseline(ds, y, args.cpu_rows, threads)
+    for _ in range(args.steps):
+        steps.append(cpu_baseline(ds, y, args.cpu_rows, threads))
+    v = float(np.median([s["value"] for s in steps]))
+    return {"metric": METRIC, "impl": "reference", "value": v, "unit": "iters/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 / v, 1) if v else None,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 grad/hess, f64 histograms",
+            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "rows": ds.num_data},
+            "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
+                             "sample": steps[-1]["sample"]},
+            "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--rows", type=int, default=10_000_000)
+    ap.add_argument("--leaves", type=int, default=255)
+    ap.add_argument("--cpu-rows", type=int, default=1_000_000)
+    args = ap.parse_args()
+    rank = int(os.environ.get("RANK", 0))
+    world = int(os.environ.get("WORLD_SIZE", 1))
+    if args.impl == "reference":
+        if rank == 0:
+            print(json.dumps(run_reference(args)))
+        return
+    if world > 1:
+        import torch
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
+        torch.distributed.init_process_group("nccl")
+    line = run_gpu(args, rank, world)
+    if rank == 0:
+        print(json.dumps(line))
+    if world > 1:
+        import torch
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,147 @@
+/* bkgpu.h — C ABI of the GB300 tree learner for bankai-lightgbm's histogram hot path.
+ *
+ * The reference has no trait for its tree learner: `Trainer` calls the concrete method set of
+ * `SerialTreeLearner` (crates/lgbm-core/src/treelearner/serial.rs:183-2044). Each entry point
+ * below replaces one of those methods (cited per function) and takes plain pointers and sizes,
+ * so a Rust `extern "C"` block can bind it directly.
+ *
+ * Conventions (mirroring the reference's c_api, crates/lgbm-capi/src/lib.rs:1-8,78):
+ *   - every function returns 0 on success and -1 on failure; bk_last_error() then holds a
+ *     message for the calling thread;
+ *   - calls on one learner must not overlap (the reference runs one tree at a time per
+ *     learner, serial.rs:569-576); all calls are synchronous unless stated;
+ *   - "host" pointers are ordinary CPU memory; "device" pointers are CUDA global memory of the
+ *     learner's device, selected by the `on_device` flags.
+ */
+#ifndef BKGPU_H
+#define BKGPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* One inner (used) feature: the BinMapper facts the learner reads (io/bin.rs:21-36) plus the
+ * real column index (io/dataset.rs:84-93 real_feature_idx) and its split penalty
+ * (feature_contri). Stored bins follow io/dataset.rs:633-685: rows whose bin equals
+ * most_freq_bin hold 0, other rows hold bin + 1 - (most_freq_bin == 0). */
+typedef struct {
+  int32_t num_bin;
+  int32_t missing_type; /* 0 none, 1 zero, 2 NaN (meta.rs:10-16) */
+  int32_t default_bin;
+  int32_t most_freq_bin;
+  double penalty;
+  int32_t real_feature;
+  int32_t _pad;
+} bk_feature;
+
+/* The Config fields the tree learner reads (config/auto.rs). `num_threads` is the reference's
+ * thread count, used only to seed stochastic-rounding noise per block exactly as the reference
+ * does (gradient_discretizer/mod.rs:87-106). `fused_madd` selects the rounding of the
+ * reference's `madd` (utils/common.rs:207-216): 1 = fused, as the aarch64 build; 0 = unfused. */
+typedef struct {
+  int32_t num_leaves, max_depth, min_data_in_leaf, _pad0;
+  double min_sum_hessian_in_leaf, lambda_l1, lambda_l2, max_delta_step, path_smooth, min_gain_to_split;
+  int32_t use_quantized_grad, num_grad_quant_bins, quant_train_renew_leaf, stochastic_rounding;
+  int32_t seed, num_threads, fused_madd, is_constant_hessian;
+} bk_config;
+
+/* One numerical split: the arguments of Tree::split_numerical (tree.rs:361-403) as computed by
+ * SerialTreeLearner::split (serial.rs:1685-1876). Counts are the partition's actual counts. */
+typedef struct {
+  int32_t leaf, right_leaf, inner_feature, real_feature;
+  uint32_t threshold; /* bin; the host maps it with BinMapper::bin_to_value */
+  int32_t default_left, missing_type, left_count, right_count;
+  double left_output, right_output, left_sum_gradient, left_sum_hessian, right_sum_gradient, right_sum_hessian;
+  double gain; /* without min_gain_to_split; the tree stores (gain + min_gain_to_split) as f32 */
+  int64_t left_int_sum, right_int_sum; /* quantized path: (grad << 32) | hess; 0 otherwise */
+} bk_split;
+
+typedef struct bk_learner bk_learner;
+
+/* Replaces SerialTreeLearner::new (serial.rs:284-565). `bins` is column-major uint8
+ * [num_features][num_data] of stored bins. `num_jobs` trees are grown per train call over the
+ * same dataset (all K class trees of one multiclass iteration, objective/multiclass.rs). */
+int bk_learner_create(const bk_feature* features, int32_t num_features, const uint8_t* bins, int64_t num_data,
+                      const bk_config* config, int32_t num_jobs, bk_learner** out);
+
+/* Replaces SerialTreeLearner::train (serial.rs:569-628) for `num_jobs` trees at once.
+ * gradients/hessians: [num_jobs][num_data] f32, host or device (on_device). rows: ascending
+ * bagged row ids (num_rows of them) or NULL for all rows, host memory.
+ * Outputs (host): splits [num_jobs][num_leaves-1], leaf_values [num_jobs][num_leaves] (the tree's
+ * leaf outputs before shrinkage, after the quantized leaf renewal), root_outputs [num_jobs],
+ * num_leaves_out [num_jobs]. */
+int bk_learner_train(bk_learner* learner, const float* gradients, const float* hessians, int32_t on_device,
+                     const int32_t* rows, int64_t num_rows, bk_split* splits, double* leaf_values,
+                     double* root_outputs, int32_t* num_leaves_out);
+
+/* Replaces SerialTreeLearner::add_prediction_to_score (serial.rs:1974-1990): for every job j
+ * and every row r of leaf l of the last tree, score[j][r] += leaf_values[j][l].
+ * score: [num_jobs][num_data] f64, host or device (on_device); leaf_values: host. */
+int bk_learner_add_prediction_to_score(bk_learner* learner, const double* leaf_values, double* score,
+                                       int32_t on_device);
+
+/* The leaf of every row after the last tree (-1 outside the bagged rows) — the partition that
+ * SerialTreeLearner keeps in `pub partition` (serial.rs:212). out: [num_jobs][num_data] host. */
+int bk_learner_row_leaf(bk_learner* learner, int32_t* out);
+
+/* Grow-loop execution: 0 = one host round trip per split (the plain form); 1 = the whole
+ * grow loop of an iteration captured once as a CUDA graph and replayed (default). */
+int bk_learner_set_loop_mode(bk_learner* learner, int32_t mode);
+
+/* Replaces SerialTreeLearner::reset_constant_hessian (serial.rs:279). */
+int bk_learner_reset_constant_hessian(bk_learner* learner, int32_t value);
+
+/* Timing of the last train call, from CUDA events on the learner's stream: total device time
+ * and the histogram kernels' time (ms), plus the algorithmic bytes the histogram kernels moved. */
+int bk_learner_last_timing(bk_learner* learner, double* total_ms, double* hist_ms, double* hist_bytes);
+
+/* Enables (1) or disables (0) CUDA-event timing of every histogram launch of a train call,
+ * reported by bk_learner_last_timing. */
+int bk_learner_set_timing(bk_learner* learner, int32_t on);
+
+/* The learner's own device gradient / hessian buffers ([num_jobs][num_data] f32). A caller that
+ * computes gradients on the device may write them here and pass these pointers to
+ * bk_learner_train with on_device = 1, which then copies nothing. */
+int bk_learner_gradient_buffers(bk_learner* learner, float** gradients, float** hessians);
+
+/* Gradients of a built-in objective on the device, written into the learner's gradient buffers
+ * (next-step work of the reference's Trainer: objective/regression.rs:240-248 (kind 0, L2),
+ * objective/binary.rs:71-90 (kind 1, binary, `sigmoid`), objective/multiclass.rs:68-90 (kind 2,
+ * softmax over num_jobs classes)). score: device [num_jobs][num_data] f64; label: device f32.
+ * Enqueued on the learner's stream, ordered before its next call. */
+int bk_learner_objective_gradients(bk_learner* learner, int32_t kind, const double* score, const float* label,
+                                   double sigmoid);
+
+/* Mean training loss (L2: squared error; binary / multiclass: log loss) of a device score,
+ * returned in *out (host). */
+int bk_learner_objective_loss(bk_learner* learner, int32_t kind, const double* score, const float* label,
+                              double* out);
+
+/* The CUDA stream (cudaStream_t) every call of this learner is ordered on, for callers that
+ * time or order their own work against the learner's. */
+int bk_learner_stream(bk_learner* learner, void** stream);
+
+int bk_learner_destroy(bk_learner* learner);
+
+/* Message of the last failed call on this thread ("" if none). */
+const char* bk_last_error(void);
+
+/* ---- host-side dataset preparation (the reference's host keeps these, io/bin.rs) ---- */
+
+/* BinMapper::find_bin for a numerical feature (io/bin.rs:342-554). */
+int32_t bk_find_bin_numerical(double* values, int64_t num_values, int64_t total_sample_cnt, int32_t max_bin,
+                              int32_t min_data_in_bin, int32_t min_split_data, int32_t pre_filter,
+                              int32_t use_missing, int32_t zero_as_missing, double* upper_bounds, int32_t cap,
+                              int32_t* meta_out, double* dmeta_out);
+
+/* Stored group bins of one column (io/dataset.rs:633-685 with BinMapper::value_to_bin). */
+void bk_values_to_group_bins(const double* col, int64_t n, int64_t stride, const double* upper_bounds,
+                             int32_t num_bin, int32_t missing_type, int32_t most_freq_bin, uint8_t* out);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BKGPU_H */
