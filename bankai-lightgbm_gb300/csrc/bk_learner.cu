@@ -161,8 +161,12 @@ struct bk_learner {
     if (stream) cudaStreamDestroy(stream);
   }
 
+  bool capturing = false;
   void record_hist_event(int i) {
-    if (timing && (size_t)i < hist_events.size()) CK(cudaEventRecord(hist_events[i], stream));
+    if (!timing || (size_t)i >= hist_events.size()) return;
+    // inside stream capture only an external record becomes a timed event node of the graph
+    if (capturing) CK(cudaEventRecordWithFlags(hist_events[i], stream, cudaEventRecordExternal));
+    else CK(cudaEventRecord(hist_events[i], stream));
   }
 
   // One grow-loop step (iteration `it`) of all jobs.
@@ -194,6 +198,7 @@ struct bk_learner {
     if (!graph_exec) {
       cudaGraph_t g = nullptr;
       CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+      capturing = true;
       try {
         tree_prologue();
         for (int it = 0; it < p.num_leaves - 1; ++it) {
@@ -202,10 +207,12 @@ struct bk_learner {
         }
         tree_epilogue();
       } catch (...) {
+        capturing = false;
         cudaStreamEndCapture(stream, &g);
         if (g) cudaGraphDestroy(g);
         throw;
       }
+      capturing = false;
       CK(cudaStreamEndCapture(stream, &g));
       CK(cudaGraphInstantiate(&graph_exec, g, 0));
       CK(cudaGraphDestroy(g));

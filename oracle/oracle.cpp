@@ -16,10 +16,15 @@
 // linear trees / categorical features.
 
 #include <algorithm>
+#include <atomic>
 #include <cmath>
+#include <condition_variable>
 #include <cstdint>
 #include <cstring>
+#include <functional>
 #include <limits>
+#include <mutex>
+#include <thread>
 #include <vector>
 
 namespace orc {
@@ -631,6 +636,75 @@ static void route_table(const FeatureMeta& m, uint32_t threshold, bool default_l
 }
 
 // ---------------------------------------------------------------------------------------------
+// A persistent worker pool: the reference runs its per-feature histogram and search tasks on
+// rayon (serial.rs:1022-1038, :1481-1489). Every task owns its feature's slices and the results
+// are folded in feature order afterwards, so any thread count gives the same tree.
+// ---------------------------------------------------------------------------------------------
+struct Pool {
+  std::vector<std::thread> workers;
+  std::mutex m;
+  std::condition_variable cv, done_cv;
+  std::function<void(int)> job;
+  int njobs = 0, active = 0;
+  std::atomic<int> next{0};
+  uint64_t gen = 0;
+  bool quit = false;
+
+  explicit Pool(int threads) {
+    for (int t = 1; t < threads; ++t) workers.emplace_back([this] { loop(); });
+  }
+  ~Pool() {
+    {
+      std::lock_guard<std::mutex> g(m);
+      quit = true;
+    }
+    cv.notify_all();
+    for (auto& w : workers) w.join();
+  }
+  void work() {
+    for (;;) {
+      int i = next.fetch_add(1);
+      if (i >= njobs) break;
+      job(i);
+    }
+  }
+  void loop() {
+    uint64_t seen = 0;
+    for (;;) {
+      {
+        std::unique_lock<std::mutex> lk(m);
+        cv.wait(lk, [&] { return quit || gen != seen; });
+        if (quit) return;
+        seen = gen;
+      }
+      work();
+      {
+        std::lock_guard<std::mutex> g(m);
+        if (--active == 0) done_cv.notify_all();
+      }
+    }
+  }
+  void run(int n, const std::function<void(int)>& f) {
+    if (workers.empty() || n < 2) {
+      for (int i = 0; i < n; ++i) f(i);
+      return;
+    }
+    {
+      std::lock_guard<std::mutex> g(m);
+      job = f;
+      njobs = n;
+      next = 0;
+      active = (int)workers.size();
+      ++gen;
+    }
+    cv.notify_all();
+    work();
+    std::unique_lock<std::mutex> lk(m);
+    done_cv.wait(lk, [&] { return active == 0; });
+  }
+};
+
+// ---------------------------------------------------------------------------------------------
 // Learner (treelearner/serial.rs)
 // ---------------------------------------------------------------------------------------------
 struct SplitRecord {  // one numerical split, the arguments of tree.split_numerical
@@ -681,6 +755,8 @@ struct Learner {
   int32_t tree_leaves = 1;
   double root_output = 0.0;
   std::vector<float> og, oh;
+  Pool* workers = nullptr;
+  ~Learner() { delete workers; }
 
   int32_t pool_get(int32_t leaf, bool* had) {  // serial.rs:117-141 (full pool)
     if (leaf_slot[leaf] >= 0) {
@@ -745,8 +821,8 @@ struct Learner {
       ph = const_hess ? h : oh.data();
     }
     std::vector<double>& hist = slots[slot];
-    for (int f = 0; f < nf; ++f) {
-      if (!used[f]) continue;
+    workers->run(nf, [&](int f) {
+      if (!used[f]) return;
       double* out = hist.data() + 2 * gstart[f];
       std::fill(out, out + 2 * gbins[f], 0.0);
       const uint8_t* col = cols[f];
@@ -760,7 +836,7 @@ struct Learner {
         double h0 = (double)h[0];
         for (int b = 0; b < gbins[f]; ++b) out[2 * b + 1] *= h0;
       }
-    }
+    });
   }
 
   // serial.rs:1074-1164 — integer histograms of one leaf.
@@ -768,8 +844,8 @@ struct Learner {
     int64_t cnt = leaf_count[leaf];
     const int32_t* ix = cnt < n ? leaf_rows(leaf) : nullptr;
     const int16_t* pk = disc.packed.data();
-    for (int f = 0; f < nf; ++f) {
-      if (!used[f]) continue;
+    workers->run(nf, [&](int f) {
+      if (!used[f]) return;
       int64_t* og_ = islots_g[slot].data() + gstart[f];
       int64_t* oh_ = islots_h[slot].data() + gstart[f];
       std::fill(og_, og_ + gbins[f], 0);
@@ -782,7 +858,7 @@ struct Learner {
         og_[b] += (int64_t)(int8_t)(pv >> 8);
         oh_[b] += (int64_t)(uint8_t)(pv & 0xff);
       }
-    }
+    });
   }
 
   // serial.rs:2205-2238 — FixHistogram on one feature slice (feature-local bins).
@@ -815,9 +891,10 @@ struct Learner {
   void find_best_splits_from_histograms(const std::vector<uint8_t>& used, bool use_subtract, double sp_out,
                                         double lp_out) {
     int32_t lslot = larger.leaf >= 0 ? larger_slot : -1;
-    SplitInfo sbest, lbest;
-    for (int f = 0; f < nf; ++f) {
-      if (!used[f]) continue;
+    std::vector<SplitInfo> cs_all(nf), cl_all(nf);
+    std::vector<uint8_t> ss_all(nf, 0), sl_all(nf, 0);
+    workers->run(nf, [&](int f) {
+      if (!used[f]) return;
       const FeatureMeta& m = metas[f];
       int64_t start = gstart[f] + 1;  // feature_hist_offsets: group start + bin_offsets[0]
       int len = m.num_bin - m.offset;
@@ -865,12 +942,21 @@ struct Learner {
         }
       }
       cs.feature = m.real;
-      splittable[smaller_slot][f] = ss;
-      if (cs.better_than(sbest)) sbest = cs;
+      cl.feature = m.real;
+      cs_all[f] = cs;
+      cl_all[f] = cl;
+      ss_all[f] = ss;
+      sl_all[f] = sl;
+    });
+    // serial.rs:1523-1558 — fold in feature order
+    SplitInfo sbest, lbest;
+    for (int f = 0; f < nf; ++f) {
+      if (!used[f]) continue;
+      splittable[smaller_slot][f] = ss_all[f];
+      if (cs_all[f].better_than(sbest)) sbest = cs_all[f];
       if (lslot >= 0) {
-        cl.feature = m.real;
-        splittable[lslot][f] = sl;
-        if (cl.better_than(lbest)) lbest = cl;
+        splittable[lslot][f] = sl_all[f];
+        if (cl_all[f].better_than(lbest)) lbest = cl_all[f];
       }
     }
     best[smaller.leaf] = sbest;
@@ -1153,6 +1239,7 @@ void* orc_learner_create(const orc_feature* feats, int32_t nf, const uint8_t* bi
   L->renew_leaf = c->quant_train_renew_leaf != 0;
   L->stoch = c->stochastic_rounding != 0;
   L->setup();
+  L->workers = new Pool(c->num_threads > 0 ? c->num_threads : 1);
   if (L->quant) {
     L->disc.init((size_t)n, c->num_grad_quant_bins, L->const_hess, L->p.fused);
     if (L->stoch) L->disc.init_stochastic((uint32_t)c->seed, (size_t)(c->num_threads > 0 ? c->num_threads : 1));
