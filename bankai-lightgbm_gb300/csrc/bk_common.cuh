@@ -70,6 +70,7 @@ struct JobState {
   uint32_t start_pos, red_maxg, red_maxh, red_flags;
   int32_t mt_idx, _p1;
   int64_t hist_rows_direct, hist_rows_gather, hist_builds;  // work done by the histogram kernels
+  uint32_t search_done, part_done;  // CTAs finished in the current search / scatter launch
   uint32_t mt[624];
   uint8_t route[256];
 };
@@ -89,7 +90,11 @@ struct Job {
   int32_t* leaf_slot;
   LeafSum* leaf_sum;
   Cand* best;          // [L]
+  double* bgain;       // [L]   gain of best[] (compact copy for the arg-max)
+  int32_t* bfeat;      // [L]   real feature of best[]
   Cand* cand;          // [2][F]
+  double* cgain;       // [2][F] gain of cand[] (compact copy for the fold)
+  uint8_t* csplit;     // [2][F] splittable flag of cand[]
   uint8_t* splittable; // [L][F]
   uint8_t* used;       // [F]
   bk_split* records;   // [L-1]
@@ -117,9 +122,9 @@ void launch_hist(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t
 size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide);
 
 void launch_search(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s);
-void launch_decide(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s);
-void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm, cudaStream_t s);
-void launch_post_split(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s);
+void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
+                      const DevFeature* feats, cudaStream_t s);
+
 cudaError_t hist_set_smem_attrs(size_t smem);
 
 // bk_prep.cu

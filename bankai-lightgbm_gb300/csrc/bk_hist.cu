@@ -81,6 +81,7 @@ __global__ void __launch_bounds__(1024, 1)
   __syncthreads();
   const uint8_t* tb = bins_rt + (size_t)tile * (size_t)p.n * TILE;
   const int16_t* packed = J.packed;
+  const bool feat_lane = tile * TILE + lane < p.F;
   const int64_t per_round = (int64_t)TILE * nwarps;
   const int64_t rounds = ceil_div64(R.r1 - R.r0, per_round);
   for (int64_t rd = 0; rd < rounds; ++rd) {
@@ -105,7 +106,8 @@ __global__ void __launch_bounds__(1024, 1)
       stage_v[warp * 32 + lane] = v;
       __syncwarp();
       const uint8_t* sb = reinterpret_cast<const uint8_t*>(stage + warp * 64);
-      int jn = (int)min((int64_t)32, R.r1 - base);
+      // lanes past the last feature of the last tile (padding bytes) add nothing
+      int jn = feat_lane ? (int)min((int64_t)32, R.r1 - base) : 0;
       for (int j = 0; j < jn; ++j) {
         uint32_t bin = sb[j * 32 + lane];
         int32_t vv = stage_v[warp * 32 + j];
@@ -174,6 +176,7 @@ __global__ void __launch_bounds__(1024, 1)
   }
   __syncthreads();
   const uint8_t* tb = bins_rt + (size_t)tile * (size_t)p.n * TILE;
+  const bool feat_lane = tile * TILE + lane < p.F;
   const float* G = J.g;
   const float* H = J.h;
   const int64_t per_round = (int64_t)TILE * nwarps;
@@ -195,7 +198,7 @@ __global__ void __launch_bounds__(1024, 1)
     stage_v[warp * 32 + lane] = v;
     __syncwarp();
     const uint8_t* sb = reinterpret_cast<const uint8_t*>(stage + warp * 64);
-    int jn = (int)min((int64_t)32, R.r1 - base);
+    int jn = feat_lane ? (int)min((int64_t)32, R.r1 - base) : 0;
     for (int j = 0; j < jn; ++j) {
       uint32_t e = (uint32_t)sb[j * 32 + lane] * TILE + lane;
       float2 vv = stage_v[warp * 32 + j];

@@ -174,12 +174,10 @@ struct bk_learner {
     record_hist_event(2 * it);
     launch_hist(d_jobs, K, p, d_bins_rt, hl, stream);
     record_hist_event(2 * it + 1);
-    launch_search(d_jobs, K, p, d_feat, stream);
-    launch_decide(d_jobs, K, p, d_feat, stream);
+    launch_search(d_jobs, K, p, d_feat, stream);  // its last CTA also picks the split
   }
   void step_b() {
-    launch_partition(d_jobs, K, p, d_bins_cm, stream);
-    launch_post_split(d_jobs, K, p, d_feat, stream);
+    launch_partition(d_jobs, K, p, d_bins_cm, d_feat, stream);  // its last CTA also records the split
   }
 
   void tree_prologue() {
@@ -403,7 +401,11 @@ int bk_learner_create(const bk_feature* features, int32_t num_features, const ui
       J.leaf_slot = L->dalloc<int32_t>(Lv);
       J.leaf_sum = L->dalloc<LeafSum>(Lv);
       J.best = L->dalloc<Cand>(Lv);
+      J.bgain = L->dalloc<double>(Lv);
+      J.bfeat = L->dalloc<int32_t>(Lv);
       J.cand = L->dalloc<Cand>(2 * (size_t)F);
+      J.cgain = L->dalloc<double>(2 * (size_t)F);
+      J.csplit = L->dalloc<uint8_t>(2 * (size_t)F);
       J.splittable = L->dalloc<uint8_t>((size_t)Lv * F);
       J.used = L->dalloc<uint8_t>(F);
       J.records = L->dalloc<bk_split>(Lv);

@@ -4,10 +4,11 @@
 //
 // The reference routes each row through SplitRule::route_bin; here k_decide evaluates that rule
 // once per stored bin into a 256-entry route table, so routing a row is one byte read of the
-// split feature's column-major bins plus one shared-memory lookup. Three kernels on a fixed grid
+// split feature's column-major bins plus one shared-memory lookup. Two kernels on a fixed grid
 // (so the step can be captured in a CUDA graph while the leaf size varies): count the left rows
-// of each CTA's contiguous chunk, scan the chunk counts, scatter with a block-wide scan.
-#include "bk_common.cuh"
+// of each CTA's contiguous chunk; then scatter, each CTA summing the counts of the chunks before
+// its own (at most a few hundred) and ordering its rows with block-wide scans.
+#include "bk_grow.cuh"
 
 namespace bk {
 
@@ -83,29 +84,29 @@ __global__ void __launch_bounds__(kThreads) k_part_count(const Job* __restrict__
   if (threadIdx.x == 0) J.part_cnt[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(1024) k_part_scan(const Job* __restrict__ jobs, Params p) {
-  __shared__ int64_t sh[32];
-  const Job& J = jobs[blockIdx.z];
-  if (J.st->stop) return;
-  int64_t v = threadIdx.x < (unsigned)p.part_grid ? J.part_cnt[threadIdx.x] : 0;
-  int64_t total;
-  int64_t ex = block_excl_scan<int64_t>(v, &total, sh);
-  if (threadIdx.x < (unsigned)p.part_grid) J.part_cnt[threadIdx.x] = ex;
-  if (threadIdx.x == 0) J.st->total_left = total;
-}
-
 __global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict__ jobs, Params p,
-                                                           const uint8_t* __restrict__ bins_cm) {
+                                                           const uint8_t* __restrict__ bins_cm,
+                                                           const DevFeature* __restrict__ feats) {
   __shared__ uint8_t lut[256];
   __shared__ int32_t sh[32];
   const Job& J = jobs[blockIdx.z];
   if (J.st->stop) return;
   lut[threadIdx.x] = J.st->route[threadIdx.x];
   __syncthreads();
+  __shared__ int64_t sh64[32];
   PartRange R;
   part_range(J, p, bins_cm, &R);
-  const int64_t total_left = J.st->total_left;
-  int64_t running = J.part_cnt[blockIdx.x];  // left rows before this chunk
+  // left rows before this chunk, and in total
+  int64_t before = 0, all = 0;
+  for (int i = threadIdx.x; i < p.part_grid; i += kThreads) {
+    int64_t c = J.part_cnt[i];
+    all += c;
+    if (i < (int)blockIdx.x) before += c;
+  }
+  int64_t total_left, running;
+  block_excl_scan<int64_t>(all, &total_left, sh64);
+  block_excl_scan<int64_t>(before, &running, sh64);
+  if (blockIdx.x == 0 && threadIdx.x == 0) J.st->total_left = total_left;
   for (int64_t base = R.r0; base < R.r1; base += kThreads * kItems) {
     int64_t e0 = base + (int64_t)threadIdx.x * kItems;
     int32_t rows[kItems];
@@ -140,15 +141,28 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict
     }
     running += tile_total;
   }
+  // the last CTA of the launch applies the split to the leaf records (bk_grow.cuh)
+  __shared__ int last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned t = atomicAdd(&J.st->part_done, 1u);
+    last = t == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x < 32) post_split_body(J, p, feats);
+  if (threadIdx.x == 0) J.st->part_done = 0u;
 }
 
 }  // namespace
 
-void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm, cudaStream_t s) {
+void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
+                      const DevFeature* feats, cudaStream_t s) {
   dim3 grid(p.part_grid, 1, num_jobs);
   k_part_count<<<grid, kThreads, 0, s>>>(d_jobs, p, bins_cm);
-  k_part_scan<<<dim3(1, 1, num_jobs), 1024, 0, s>>>(d_jobs, p);
-  k_part_scatter<<<grid, kThreads, 0, s>>>(d_jobs, p, bins_cm);
+  k_part_scatter<<<grid, kThreads, 0, s>>>(d_jobs, p, bins_cm, feats);
 }
 
 }  // namespace bk

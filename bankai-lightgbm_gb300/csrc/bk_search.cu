@@ -1,7 +1,7 @@
 // FindBestSplitsFromHistograms (serial.rs:1322-1566, int: :1212-1300) and the grow-loop
 // bookkeeping kernels (serial.rs:578-628, :779-825, :1685-1876), GB300 form.
 //
-// k_search: one warp per feature. It fixes the smaller leaf's most-frequent bin
+// k_search: one warp per (leaf, feature). It fixes the smaller leaf's most-frequent bin
 // (FixHistogram, serial.rs:2205-2238), derives the larger leaf by parent-minus-smaller
 // subtraction in place, then runs the reference's directional threshold scans
 // (FindBestThresholdSequentially[Int], feature_histogram.rs:363-663 / 839-1142) as warp-parallel
@@ -12,13 +12,13 @@
 // prefix sums are exact integers, so its candidates are bit-identical to the reference's; the
 // float path's f64 prefix sums are associated differently (≈1e-16 relative).
 //
-// k_decide: folds the per-feature candidates of each searched leaf in feature order with
-// `better_than`, takes the arg-max leaf (split_info.rs:88-96), stops the tree when its gain is
-// <= 0, and builds the route table of the chosen split (data_partition.rs:299-410).
-// k_post_split: applies the partition result to the leaf records and prepares the next
-// iteration (BeforeFindBestSplit), all on the device.
+// The last CTA of k_search folds the per-feature candidates of each searched leaf in feature
+// order with `better_than`, takes the arg-max leaf (split_info.rs:88-96), stops the tree when its
+// gain is <= 0, and builds the route table of the chosen split (data_partition.rs:299-410). The
+// post-split bookkeeping (bk_grow.cuh) runs in the last CTA of the partition scatter.
 #include <math_constants.h>
 
+#include "bk_grow.cuh"
 #include "bk_math.cuh"
 
 namespace bk {
@@ -82,8 +82,57 @@ __device__ __forceinline__ int warp_best_lane(bool better, double gain, int lane
   return bl;
 }
 
+// ---- fp32 prefilter of the plain split gain (no L1 / max_delta_step / path_smooth) ----
+// The reference evaluates gl^2/(hl+l2) + gr^2/(hr+l2) in f64 for every threshold; GB300 runs f64 at
+// a small fraction of its fp32 rate. Each candidate is first evaluated in fp32 together with a
+// rigorous bound E on |fp32 - f64| (the inputs' conversion, the squares, the sums and the division
+// add up to about 14 units of 2^-24 relative to the non-negative result, the fp32 comparisons
+// against E one more; E uses 48). Only the
+// candidates that can still be the best (fp32 + E >= the best lower bound so far) or whose
+// pass/fail against min_gain_shift is uncertain are evaluated in f64, so the chosen split, its
+// gain and the splittable flag are exactly the reference's.
+constexpr float kPrefilterRel = 48.0f * 5.9604645e-08f;
+
+struct Approx {
+  float g, e;
+  bool uncertain;
+};
+
+__device__ __forceinline__ Approx approx_from(float xl, float yl, float xr, float yr) {
+  Approx a;
+  float tl = __fdiv_rn(__fmul_rn(xl, xl), yl);
+  float tr = __fdiv_rn(__fmul_rn(xr, xr), yr);
+  a.g = __fadd_rn(tl, tr);
+  a.e = __fadd_rn(__fmul_rn(kPrefilterRel, a.g), 1e-30f);
+  // non-finite values, tiny denominators (where the reference's +kEpsilon matters) and huge
+  // numerators go to f64
+  a.uncertain = !(yl >= 1e-6f) || !(yr >= 1e-6f) || !(a.g < 1e30f) || isnan(a.g);
+  return a;
+}
+
+// Smallest x in [0, hi) with pred(x) (monotone false -> true), or hi; one warp, 32-ary search.
+template <typename Pred>
+__device__ int64_t warp_first_true(int64_t hi, int lane, Pred pred) {
+  int64_t lo = 0;
+  while (lo < hi) {
+    int64_t step = (hi - lo + 31) / 32;
+    int64_t x = lo + (int64_t)lane * step;
+    bool t = x < hi && pred(x);
+    unsigned m = __ballot_sync(FULL, t);
+    if (m == 0) {
+      int64_t nlo = lo + 31 * step + 1;
+      lo = nlo < hi ? nlo : hi;
+    } else {
+      int k = __ffs(m) - 1;
+      hi = lo + (int64_t)k * step;
+      if (k > 0) lo = lo + (int64_t)(k - 1) * step + 1;
+    }
+  }
+  return lo;
+}
+
 // FindBestThresholdSequentially (float), feature_histogram.rs:363-663.
-template <bool REV>
+template <bool REV, bool PLAIN>
 __device__ DirBest scan_float(const Params& p, const DevFeature& m, const FloatHist& H, bool SKIP, bool NA,
                               double sum_g, double sum_h, int32_t num_data, double mgs, double parent, int lane) {
   DirBest r;
@@ -96,6 +145,8 @@ __device__ DirBest scan_float(const Params& p, const DevFeature& m, const FloatH
   r.lg = r.lh = 0;
   const double cnt_factor = (double)num_data / sum_h;
   const int off = m.offset;
+  const float l2f = (float)p.l2;
+  const float mgs_up = __double2float_ru(mgs), mgs_dn = __double2float_rd(mgs);
   double cg, ch;
   int32_t cc;
   int t_first, P;
@@ -109,7 +160,7 @@ __device__ DirBest scan_float(const Params& p, const DevFeature& m, const FloatH
   } else {
     int t_end = m.num_bin - 2 - off;
     if (NA && off == 1) {
-      // left starts as everything outside the slice (the most-frequent bin 0 and nothing else)
+      // left starts as everything outside the slice (the most-frequent bin 0)
       double pg = 0.0, ph = 0.0;
       int32_t pc = 0;
       for (int i = lane; i < m.num_bin - off; i += 32) {
@@ -152,7 +203,6 @@ __device__ DirBest scan_float(const Params& p, const DevFeature& m, const FloatH
     cg = __shfl_sync(FULL, pg, 31);
     ch = __shfl_sync(FULL, ph, 31);
     cc = __shfl_sync(FULL, pc, 31);
-    // REV: p* are the right side; FWD: the left side.
     bool first, brk;
     double slg, slh, srg, srh;
     int32_t lc, rc;
@@ -178,11 +228,27 @@ __device__ DirBest scan_float(const Params& p, const DevFeature& m, const FloatH
     unsigned bm = __ballot_sync(FULL, brk);
     int stop_lane = bm ? __ffs(bm) - 1 : 32;
     bool valid = first && !brk && lane < stop_lane;
-    double gain = valid ? split_gains(p, slg, slh, srg, srh, lc, rc, parent) : -CUDART_INF;
-    bool pass = valid && !(gain <= mgs);
-    if (__any_sync(FULL, pass)) r.splittable = 1;
+    bool exact = valid, cpass = false;
+    if (PLAIN) {
+      Approx a{0.f, 0.f, true};
+      if (valid) a = approx_from((float)slg, __fadd_rn((float)slh, l2f), (float)srg, __fadd_rn((float)srh, l2f));
+      float e2 = a.e;
+      cpass = valid && !a.uncertain && __fsub_rn(a.g, e2) > mgs_up;
+      bool mpass = valid && (a.uncertain || __fadd_rn(a.g, e2) > mgs_dn);
+      float lower = cpass ? __fsub_rn(a.g, e2) : -CUDART_INF_F;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) lower = fmaxf(lower, __shfl_xor_sync(FULL, lower, o));
+      float thr = fmaxf(lower, __double2float_rd(r.gain));
+      bool contender = mpass && (a.uncertain || __fadd_rn(a.g, e2) >= thr);
+      bool any_cpass = __any_sync(FULL, cpass);
+      bool unsure = mpass && !cpass && !any_cpass && !r.splittable;
+      exact = contender || unsure;
+    }
+    double gain = exact ? split_gains(p, slg, slh, srg, srh, lc, rc, parent) : -CUDART_INF;
+    bool pass = exact ? !(gain <= mgs) : cpass;
+    if (__any_sync(FULL, valid && pass)) r.splittable = 1;
     double bg;
-    int bl = warp_best_lane(pass && gain > r.gain, gain, lane, &bg);
+    int bl = warp_best_lane(exact && pass && gain > r.gain, gain, lane, &bg);
     if (bl < 32) {
       r.gain = bg;
       r.th = __shfl_sync(FULL, REV ? (t - 1 + off) : (t + off), bl);
@@ -195,10 +261,33 @@ __device__ DirBest scan_float(const Params& p, const DevFeature& m, const FloatH
   return r;
 }
 
+// Integer thresholds of a leaf (feature-independent): for an accumulated side with integer hessian
+// x, the reference's `count >= min_data && hess >= min_hessian` test (counts estimated as
+// round_int(x * cnt_factor), feature_histogram.rs:927-940) is monotone in x, so it is x >= first_x;
+// and the `break` test on the other side is x >= brk_x.
+struct IntThresholds {
+  int64_t first_x, brk_x;
+};
+
+__device__ IntThresholds int_thresholds(const Params& p, int64_t th, double hs, int32_t num_data, int lane) {
+  const double cf = (double)num_data / (double)th;
+  const int64_t hi = th + 1;
+  int64_t cnt_ok = warp_first_true(hi, lane, [&](int64_t x) { return round_int((double)x * cf) >= p.min_data; });
+  int64_t hess_ok = warp_first_true(hi, lane, [&](int64_t x) { return (double)x * hs >= p.min_hess; });
+  int64_t cnt_brk =
+      warp_first_true(hi, lane, [&](int64_t x) { return round_int((double)x * cf) > num_data - p.min_data; });
+  IntThresholds r;
+  r.first_x = cnt_ok > hess_ok ? cnt_ok : hess_ok;
+  int64_t hess_brk = th - hess_ok + 1;  // (th - x) * hs < min_hess  <=>  th - x < hess_ok
+  r.brk_x = cnt_brk < hess_brk ? cnt_brk : hess_brk;
+  return r;
+}
+
 // FindBestThresholdSequentiallyInt, feature_histogram.rs:839-1142.
-template <bool REV>
+template <bool REV, bool PLAIN>
 __device__ DirBest scan_int(const Params& p, const DevFeature& m, const IntHist& H, bool SKIP, bool NA, int64_t tg,
-                            int64_t th, double gs, double hs, int32_t num_data, double mgs, double parent, int lane) {
+                            int64_t th, double gs, double hs, int32_t num_data, double mgs, double parent,
+                            const IntThresholds& X, int lane) {
   DirBest r;
   r.splittable = 0;
   r.gain = -CUDART_INF;
@@ -208,6 +297,8 @@ __device__ DirBest scan_int(const Params& p, const DevFeature& m, const IntHist&
   r.lg = r.lh = 0;
   const double cnt_factor = (double)num_data / (double)th;
   const int off = m.offset;
+  const float gsf = (float)gs, hsf = (float)hs, l2f = (float)p.l2;
+  const float mgs_up = __double2float_ru(mgs), mgs_dn = __double2float_rd(mgs);
   int64_t cg, ch;
   int t_first, P;
   if (REV) {
@@ -247,46 +338,44 @@ __device__ DirBest scan_int(const Params& p, const DevFeature& m, const IntHist&
     int64_t ph = warp_incl_scan(h, lane) + ch;
     cg = __shfl_sync(FULL, pg, 31);
     ch = __shfl_sync(FULL, ph, 31);
-    bool first, brk;
-    int64_t lg, lh, rg, rh;
-    int32_t lc, rc;
-    double slh, srh;
-    if (REV) {
-      rg = pg;
-      rh = ph;
-      rc = round_int((double)rh * cnt_factor);
-      srh = (double)rh * hs;
-      first = cand && !(rc < p.min_data || srh < p.min_hess);
-      lc = num_data - rc;
-      lh = th - rh;
-      slh = (double)lh * hs;
-      brk = first && (lc < p.min_data || slh < p.min_hess);
-      lg = tg - rg;
-    } else {
-      lg = pg;
-      lh = ph;
-      lc = round_int((double)lh * cnt_factor);
-      slh = (double)lh * hs;
-      first = cand && !(lc < p.min_data || slh < p.min_hess);
-      rc = num_data - lc;
-      rh = th - lh;
-      srh = (double)rh * hs;
-      brk = first && (rc < p.min_data || srh < p.min_hess);
-      rg = tg - lg;
-    }
+    // REV accumulates the right side, FWD the left side
+    int64_t lg = REV ? tg - pg : pg;
+    int64_t lh = REV ? th - ph : ph;
+    int64_t rg = tg - lg, rh = th - lh;
+    bool first = cand && ph >= X.first_x;
+    bool brk = first && ph >= X.brk_x;
     unsigned bm = __ballot_sync(FULL, brk);
     int stop_lane = bm ? __ffs(bm) - 1 : 32;
     bool valid = first && !brk && lane < stop_lane;
-    double gain = -CUDART_INF;
-    if (valid) {
-      double slg = (double)lg * gs;
-      double srg = (double)rg * gs;
-      gain = split_gains(p, slg, slh + BK_EPS, srg, srh + BK_EPS, lc, rc, parent);
+    bool exact = valid, cpass = false;
+    if (PLAIN) {
+      Approx a{0.f, 0.f, true};
+      if (valid)
+        a = approx_from(__fmul_rn((float)lg, gsf), __fadd_rn(__fmul_rn((float)lh, hsf), l2f), __fmul_rn((float)rg, gsf),
+                        __fadd_rn(__fmul_rn((float)rh, hsf), l2f));
+      float e2 = a.e;
+      cpass = valid && !a.uncertain && __fsub_rn(a.g, e2) > mgs_up;
+      bool mpass = valid && (a.uncertain || __fadd_rn(a.g, e2) > mgs_dn);
+      float lower = cpass ? __fsub_rn(a.g, e2) : -CUDART_INF_F;
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) lower = fmaxf(lower, __shfl_xor_sync(FULL, lower, o));
+      float thr = fmaxf(lower, __double2float_rd(r.gain));
+      bool contender = mpass && (a.uncertain || __fadd_rn(a.g, e2) >= thr);
+      bool any_cpass = __any_sync(FULL, cpass);
+      bool unsure = mpass && !cpass && !any_cpass && !r.splittable;
+      exact = contender || unsure;
     }
-    bool pass = valid && !(gain <= mgs);
-    if (__any_sync(FULL, pass)) r.splittable = 1;
+    double gain = -CUDART_INF;
+    if (exact) {
+      double slh = (double)lh * hs, srh = (double)rh * hs;
+      int32_t lc = PLAIN ? 0 : round_int((double)lh * cnt_factor);
+      int32_t rc = PLAIN ? 0 : round_int((double)rh * cnt_factor);
+      gain = split_gains(p, (double)lg * gs, slh + BK_EPS, (double)rg * gs, srh + BK_EPS, lc, rc, parent);
+    }
+    bool pass = exact ? !(gain <= mgs) : cpass;
+    if (__any_sync(FULL, valid && pass)) r.splittable = 1;
     double bg;
-    int bl = warp_best_lane(pass && gain > r.gain, gain, lane, &bg);
+    int bl = warp_best_lane(exact && pass && gain > r.gain, gain, lane, &bg);
     if (bl < 32) {
       r.gain = bg;
       r.th = __shfl_sync(FULL, REV ? (t - 1 + off) : (t + off), bl);
@@ -312,8 +401,10 @@ __device__ void cand_reset(Cand* c, int32_t real, int32_t inner) {
 }
 
 // FindBestThreshold (float) for one leaf: feature_histogram.rs:219-357.
+template <bool PLAIN>
 __device__ void search_leaf_float(const Params& p, const DevFeature& m, const FloatHist& H, const LeafSum& ls,
-                                  double parent, int lane, Cand* out, int32_t f) {
+                                  double parent, int lane, Cand* out, double* out_gain, uint8_t* out_split,
+                                  int32_t f) {
   const double sum_g = ls.sg;
   const double sum_h = ls.sh + 2.0 * BK_EPS;
   const int32_t num_data = ls.num_data;
@@ -321,18 +412,15 @@ __device__ void search_leaf_float(const Params& p, const DevFeature& m, const Fl
   double mgs = gain_shift + p.min_gain;
   DirBest d[2];
   int nd;
-  bool rev_of[2];
   if (m.num_bin > 2 && m.missing != 0) {
     bool skip = m.missing == 1, na = m.missing == 2;
-    d[0] = scan_float<true>(p, m, H, skip, na, sum_g, sum_h, num_data, mgs, parent, lane);
-    d[1] = scan_float<false>(p, m, H, skip, na, sum_g, sum_h, num_data, mgs, parent, lane);
+    d[0] = scan_float<true, PLAIN>(p, m, H, skip, na, sum_g, sum_h, num_data, mgs, parent, lane);
+    d[1] = scan_float<false, PLAIN>(p, m, H, skip, na, sum_g, sum_h, num_data, mgs, parent, lane);
     nd = 2;
   } else {
-    d[0] = scan_float<true>(p, m, H, false, false, sum_g, sum_h, num_data, mgs, parent, lane);
+    d[0] = scan_float<true, PLAIN>(p, m, H, false, false, sum_g, sum_h, num_data, mgs, parent, lane);
     nd = 1;
   }
-  rev_of[0] = true;
-  rev_of[1] = false;
   if (lane != 0) return;
   Cand c;
   cand_reset(&c, m.real, f);
@@ -351,18 +439,22 @@ __device__ void search_leaf_float(const Params& p, const DevFeature& m, const Fl
       c.rsg = sum_g - r.slg;
       c.rsh = (sum_h - r.slh) - BK_EPS;
       c.gain = r.gain - mgs;
-      c.default_left = rev_of[i] ? 1 : 0;
+      c.default_left = i == 0 ? 1 : 0;
     }
   }
   if (nd == 1 && m.missing == 2) c.default_left = 0;
   c.gain *= m.penalty;
   c.splittable = sp;
   *out = c;
+  *out_gain = c.gain;
+  *out_split = (uint8_t)sp;
 }
 
 // FindBestThresholdInt for one leaf: feature_histogram.rs:673-830.
+template <bool PLAIN>
 __device__ void search_leaf_int(const Params& p, const DevFeature& m, const IntHist& H, const LeafSum& ls,
-                                double gs, double hs, double parent, int lane, Cand* out, int32_t f) {
+                                double gs, double hs, double parent, int lane, Cand* out, double* out_gain,
+                                uint8_t* out_split, int32_t f) {
   const int64_t tg = ls.int_sum >> 32;
   const int64_t th = ls.int_sum & 0xffffffffLL;
   const int32_t num_data = ls.num_data;
@@ -370,15 +462,16 @@ __device__ void search_leaf_int(const Params& p, const DevFeature& m, const IntH
   const double sum_h = (double)th * hs;
   double gain_shift = leaf_gain(p, sum_g, sum_h, num_data, parent);
   double mgs = gain_shift + p.min_gain;
+  const IntThresholds X = int_thresholds(p, th, hs, num_data, lane);
   DirBest d[2];
   int nd;
   if (m.num_bin > 2 && m.missing != 0) {
     bool skip = m.missing == 1, na = m.missing == 2;
-    d[0] = scan_int<true>(p, m, H, skip, na, tg, th, gs, hs, num_data, mgs, parent, lane);
-    d[1] = scan_int<false>(p, m, H, skip, na, tg, th, gs, hs, num_data, mgs, parent, lane);
+    d[0] = scan_int<true, PLAIN>(p, m, H, skip, na, tg, th, gs, hs, num_data, mgs, parent, X, lane);
+    d[1] = scan_int<false, PLAIN>(p, m, H, skip, na, tg, th, gs, hs, num_data, mgs, parent, X, lane);
     nd = 2;
   } else {
-    d[0] = scan_int<true>(p, m, H, false, false, tg, th, gs, hs, num_data, mgs, parent, lane);
+    d[0] = scan_int<true, PLAIN>(p, m, H, false, false, tg, th, gs, hs, num_data, mgs, parent, X, lane);
     nd = 1;
   }
   if (lane != 0) return;
@@ -414,6 +507,8 @@ __device__ void search_leaf_int(const Params& p, const DevFeature& m, const IntH
   c.gain *= m.penalty;
   c.splittable = sp;
   *out = c;
+  *out_gain = c.gain;
+  *out_split = (uint8_t)sp;
 }
 
 __device__ __forceinline__ double parent_output_of(const Params& p, const JobState* st, const LeafSum& ls) {
@@ -422,81 +517,105 @@ __device__ __forceinline__ double parent_output_of(const Params& p, const JobSta
   return ls.weight;
 }
 
-__global__ void __launch_bounds__(128) k_search(const Job* __restrict__ jobs, Params p,
-                                                const DevFeature* __restrict__ feats) {
+__device__ void decide_body(const Job& J, const Params& p, const DevFeature* feats);
+
+// One warp per (leaf side, feature): side 0 = the smaller leaf, side 1 = the larger leaf.
+// Side 0 fixes the smaller leaf's most-frequent bin (FixHistogram, serial.rs:2205-2238); side 1
+// derives the larger leaf as parent minus the fixed smaller histogram (serial.rs:1407-1437,
+// :1218-1242) — it recomputes the fixed most-frequent bin itself with the same reduction, so the
+// two warps never wait for each other. The last CTA to finish runs the fold / arg-max (k_decide).
+template <bool PLAIN>
+__global__ void __launch_bounds__(64) k_search(const Job* __restrict__ jobs, Params p,
+                                               const DevFeature* __restrict__ feats) {
   const Job& J = jobs[blockIdx.z];
-  const JobState* st = J.st;
-  if (st->stop || !st->do_search) return;
+  JobState* st = J.st;
+  if (st->stop) return;  // uniform over the grid
   const int lane = threadIdx.x & 31;
-  const int f = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  if (f >= p.F) return;
-  if (!J.used[f]) return;
-  const DevFeature m = feats[f];
-  const int tile = f / TILE, fl = f % TILE;
-  const size_t slot_stride = (size_t)p.T * p.B * TILE;
-  const size_t feat_off = (size_t)tile * p.B * TILE + fl;
-  const int32_t sl = st->smaller_leaf, ll = st->larger_leaf;
-  const LeafSum S = J.leaf_sum[sl];
-  const double sp_out = parent_output_of(p, st, S);
-  if (p.quant) {
-    int64_t* pool = reinterpret_cast<int64_t*>(J.pool);
-    IntHist HS{pool + (size_t)st->smaller_slot * slot_stride + feat_off};
-    // FixHistogram on the smaller leaf (exact integers)
-    if (m.mfb > 0) {
-      int64_t acc = 0;
-      for (int i = lane; i < m.num_bin; i += 32)
-        if (i != m.mfb) acc += HS.get(i);
-      acc = warp_sum(acc);
-      // the packed leaf total (grad << 32) | hess equals grad * 2^32 + hess, so packed
-      // arithmetic is exact componentwise
-      if (lane == 0) HS.base[(size_t)(m.mfb + 1) * TILE] = S.int_sum - acc;
-      __syncwarp();
-    }
-    if (ll >= 0) {
-      IntHist HL{pool + (size_t)st->larger_slot * slot_stride + feat_off};
-      for (int i = lane; i < m.len; i += 32) HL.base[(size_t)(i + 1) * TILE] -= HS.get(i);
-      __syncwarp();
-    }
-    const double gs = st->gscale, hs = st->hscale;
-    search_leaf_int(p, m, HS, S, gs, hs, sp_out, lane, &J.cand[f], f);
-    if (ll >= 0) {
-      IntHist HL{pool + (size_t)st->larger_slot * slot_stride + feat_off};
-      const LeafSum Lg = J.leaf_sum[ll];
-      double lp_out = parent_output_of(p, st, Lg);
-      search_leaf_int(p, m, HL, Lg, gs, hs, lp_out, lane, &J.cand[p.F + f], f);
-    }
-  } else {
-    double2* pool = reinterpret_cast<double2*>(J.pool);
-    FloatHist HS{pool + (size_t)st->smaller_slot * slot_stride + feat_off};
-    if (m.mfb > 0) {
-      double ag = 0.0, ah = 0.0;
-      for (int i = lane; i < m.num_bin; i += 32)
-        if (i != m.mfb) {
-          double2 v = HS.get(i);
-          ag += v.x;
-          ah += v.y;
-        }
-      ag = warp_sum(ag);
-      ah = warp_sum(ah);
-      if (lane == 0) HS.base[(size_t)(m.mfb + 1) * TILE] = make_double2(S.sg - ag, S.sh - ah);
-      __syncwarp();
-    }
-    if (ll >= 0) {
-      FloatHist HL{pool + (size_t)st->larger_slot * slot_stride + feat_off};
-      for (int i = lane; i < m.len; i += 32) {
-        double2 a = HL.get(i), b = HS.get(i);
-        HL.base[(size_t)(i + 1) * TILE] = make_double2(a.x - b.x, a.y - b.y);
+  const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int side = w >= p.F ? 1 : 0;
+  const int f = w - side * p.F;
+  const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
+  if (st->do_search && f < p.F && J.used[f] && leaf >= 0) {
+    const DevFeature m = feats[f];
+    const size_t slot_stride = (size_t)p.T * p.B * TILE;
+    const size_t feat_off = (size_t)(f / TILE) * p.B * TILE + (f % TILE);
+    const LeafSum S = J.leaf_sum[st->smaller_leaf];
+    const LeafSum ls = side ? J.leaf_sum[leaf] : S;
+    const double parent = parent_output_of(p, st, ls);
+    if (p.quant) {
+      int64_t* pool = reinterpret_cast<int64_t*>(J.pool);
+      IntHist HS{pool + (size_t)st->smaller_slot * slot_stride + feat_off};
+      int64_t fixed = 0;
+      if (m.mfb > 0) {
+        int64_t acc = 0;
+        for (int i = lane; i < m.num_bin; i += 32)
+          if (i != m.mfb) acc += HS.get(i);
+        acc = warp_sum(acc);
+        // the packed leaf total (grad << 32) | hess equals grad * 2^32 + hess, so packed
+        // arithmetic is exact componentwise
+        fixed = S.int_sum - acc;
       }
-      __syncwarp();
-    }
-    search_leaf_float(p, m, HS, S, sp_out, lane, &J.cand[f], f);
-    if (ll >= 0) {
-      FloatHist HL{pool + (size_t)st->larger_slot * slot_stride + feat_off};
-      const LeafSum Lg = J.leaf_sum[ll];
-      double lp_out = parent_output_of(p, st, Lg);
-      search_leaf_float(p, m, HL, Lg, lp_out, lane, &J.cand[p.F + f], f);
+      if (side == 0) {
+        if (m.mfb > 0 && lane == 0) HS.base[(size_t)(m.mfb + 1) * TILE] = fixed;
+        __syncwarp();
+        search_leaf_int<PLAIN>(p, m, HS, ls, st->gscale, st->hscale, parent, lane, &J.cand[f], &J.cgain[f],
+                               &J.csplit[f], f);
+      } else {
+        IntHist HL{pool + (size_t)st->larger_slot * slot_stride + feat_off};
+        for (int i = lane; i < m.len; i += 32) {
+          int64_t sv = (m.mfb > 0 && i == m.mfb) ? fixed : HS.get(i);
+          HL.base[(size_t)(i + 1) * TILE] -= sv;
+        }
+        __syncwarp();
+        search_leaf_int<PLAIN>(p, m, HL, ls, st->gscale, st->hscale, parent, lane, &J.cand[p.F + f],
+                               &J.cgain[p.F + f], &J.csplit[p.F + f], f);
+      }
+    } else {
+      double2* pool = reinterpret_cast<double2*>(J.pool);
+      FloatHist HS{pool + (size_t)st->smaller_slot * slot_stride + feat_off};
+      double2 fixed = make_double2(0.0, 0.0);
+      if (m.mfb > 0) {
+        double ag = 0.0, ah = 0.0;
+        for (int i = lane; i < m.num_bin; i += 32)
+          if (i != m.mfb) {
+            double2 v = HS.get(i);
+            ag += v.x;
+            ah += v.y;
+          }
+        ag = warp_sum(ag);
+        ah = warp_sum(ah);
+        fixed = make_double2(S.sg - ag, S.sh - ah);
+      }
+      if (side == 0) {
+        if (m.mfb > 0 && lane == 0) HS.base[(size_t)(m.mfb + 1) * TILE] = fixed;
+        __syncwarp();
+        search_leaf_float<PLAIN>(p, m, HS, ls, parent, lane, &J.cand[f], &J.cgain[f], &J.csplit[f], f);
+      } else {
+        FloatHist HL{pool + (size_t)st->larger_slot * slot_stride + feat_off};
+        for (int i = lane; i < m.len; i += 32) {
+          double2 a = HL.get(i);
+          double2 b = (m.mfb > 0 && i == m.mfb) ? fixed : HS.get(i);
+          HL.base[(size_t)(i + 1) * TILE] = make_double2(a.x - b.x, a.y - b.y);
+        }
+        __syncwarp();
+        search_leaf_float<PLAIN>(p, m, HL, ls, parent, lane, &J.cand[p.F + f], &J.cgain[p.F + f],
+                                 &J.csplit[p.F + f], f);
+      }
     }
   }
+  // the last CTA of this launch runs the fold and the leaf arg-max
+  __shared__ int last;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned t = atomicAdd(&st->search_done, 1u);
+    last = t == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  decide_body(J, p, feats);
+  if (threadIdx.x == 0) st->search_done = 0u;
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -547,58 +666,91 @@ __device__ uint8_t route_bin(const DevFeature& m, uint32_t threshold, bool defau
   return left ? 1 : 0;
 }
 
-__device__ __forceinline__ bool cand_better(const Cand& a, const Cand& b) {
-  return better_than(a.gain, a.feature, b.gain, b.feature);
+// Combine two (index, gain, real feature) candidates of a fold or an arg-max. `a` is the one
+// that comes first in the sequential order; `b` replaces it only when strictly better
+// (split_info.rs:104-121); NaN gains never win (the sequential fold never adopts them).
+__device__ __forceinline__ void pick(int& ai, double& ag, int& af, int bi, double bg, int bf) {
+  if (bi < 0 || isnan(bg)) return;
+  if (ai < 0 || better_than(bg, bf, ag, af) || (!better_than(ag, af, bg, bf) && bi < ai)) {
+    ai = bi;
+    ag = bg;
+    af = bf;
+  }
 }
 
-__global__ void __launch_bounds__(64) k_decide(const Job* __restrict__ jobs, Params p,
-                                               const DevFeature* __restrict__ feats) {
-  const Job& J = jobs[blockIdx.z];
+// Cand is 8-byte aligned and its size a multiple of 8 (not of 16): copy it in 8-byte words.
+static_assert(sizeof(Cand) % 8 == 0 && alignof(Cand) == 8, "Cand is copied in 8-byte words");
+__device__ __forceinline__ Cand load_cand_cg(const Cand* c) {
+  Cand r;
+  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(c);
+  unsigned long long* dst = reinterpret_cast<unsigned long long*>(&r);
+#pragma unroll
+  for (int i = 0; i < (int)(sizeof(Cand) / 8); ++i) dst[i] = __ldcg(src + i);
+  return r;
+}
+
+// The fold of the searched leaves' candidates and the leaf arg-max (64 threads). Everything
+// written by other CTAs of the search launch is read through L2 (__ldcg).
+__device__ void decide_body(const Job& J, const Params& p, const DevFeature* feats) {
   JobState* st = J.st;
-  if (st->stop) return;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   if (st->do_search) {
     // serial.rs:1523-1558 — fold the candidates of each searched leaf in feature order.
     const int32_t leaf = warp == 0 ? st->smaller_leaf : st->larger_leaf;
     const int32_t slot = warp == 0 ? st->smaller_slot : st->larger_slot;
     if (leaf >= 0) {
-      int bf = -1;  // best feature index among this lane's features (NaN gains never win)
+      int bi = -1, bf = 0x7fffffff;
+      double bg = -CUDART_INF;
       for (int f = lane; f < p.F; f += 32) {
         if (!J.used[f]) continue;
-        const Cand& c = J.cand[warp * p.F + f];
-        J.splittable[(size_t)slot * p.F + f] = (uint8_t)c.splittable;
-        if (isnan(c.gain)) continue;
-        if (bf < 0 || cand_better(c, J.cand[warp * p.F + bf])) bf = f;
+        J.splittable[(size_t)slot * p.F + f] = __ldcg(&J.csplit[warp * p.F + f]);
+        pick(bi, bg, bf, f, __ldcg(&J.cgain[warp * p.F + f]), feats[f].real);
       }
 #pragma unroll
       for (int o = 16; o > 0; o >>= 1) {
+        int oi = __shfl_xor_sync(FULL, bi, o);
+        double og = __shfl_xor_sync(FULL, bg, o);
         int of = __shfl_xor_sync(FULL, bf, o);
-        if (of >= 0 && (bf < 0 || cand_better(J.cand[warp * p.F + of], J.cand[warp * p.F + bf]))) bf = of;
+        pick(bi, bg, bf, oi, og, of);
       }
       if (lane == 0) {
+        // the fold starts from SplitInfo::default (gain -inf, feature -1) and replaces it only
+        // with a better candidate
         Cand best;
         cand_reset(&best, -1, -1);
-        // The reference starts from SplitInfo::default (gain -inf, feature -1) and replaces it
-        // only with a better candidate.
-        if (bf >= 0 && cand_better(J.cand[warp * p.F + bf], best)) best = J.cand[warp * p.F + bf];
+        if (bi >= 0 && better_than(bg, bf, best.gain, best.feature)) best = load_cand_cg(&J.cand[warp * p.F + bi]);
         J.best[leaf] = best;
+        J.bgain[leaf] = best.gain;
+        J.bfeat[leaf] = best.feature;
       }
     }
   }
   __syncthreads();
   if (warp != 0) return;
+  __threadfence_block();
   // split_info.rs:125-133 — first arg-max leaf under better_than.
-  int bl = -1;
+  int bl = -1, bf = 0;
+  double bg = 0.0;
   for (int i = lane; i < p.num_leaves; i += 32) {
-    if (bl < 0 || cand_better(J.best[i], J.best[bl])) bl = i;
+    double g = J.bgain[i];
+    int32_t fe = J.bfeat[i];
+    if (bl < 0 || better_than(g, fe, bg, bf)) {
+      bl = i;
+      bg = g;
+      bf = fe;
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) {
-    int ob = __shfl_xor_sync(FULL, bl, o);
-    if (ob >= 0) {
-      if (bl < 0) bl = ob;
-      else if (cand_better(J.best[ob], J.best[bl])) bl = ob;
-      else if (!cand_better(J.best[bl], J.best[ob]) && ob < bl) bl = ob;
+    int oi = __shfl_xor_sync(FULL, bl, o);
+    double og = __shfl_xor_sync(FULL, bg, o);
+    int of = __shfl_xor_sync(FULL, bf, o);
+    if (oi >= 0) {
+      if (bl < 0 || better_than(og, of, bg, bf) || (!better_than(bg, bf, og, of) && oi < bl)) {
+        bl = oi;
+        bg = og;
+        bf = of;
+      }
     }
   }
   const Cand info = J.best[bl];
@@ -616,129 +768,6 @@ __global__ void __launch_bounds__(64) k_decide(const Job* __restrict__ jobs, Par
   }
 }
 
-// ---------------------------------------------------------------------------------------------
-// k_post_split: serial.rs:1685-1876 after the partition, then :779-825 for the next iteration.
-// ---------------------------------------------------------------------------------------------
-__device__ void before_find_best_split(const Job& J, const Params& p, JobState* st, int32_t left, int32_t right,
-                                       int lane) {
-  bool go = true;
-  if (p.max_depth > 0 && J.leaf_depth[left] >= p.max_depth) go = false;
-  int32_t nl = (int32_t)J.leaf_count[left];
-  int32_t nr = right >= 0 ? (int32_t)J.leaf_count[right] : 0;
-  if (go && nr < p.min_data * 2 && nl < p.min_data * 2) go = false;
-  if (!go) {
-    if (lane == 0) {
-      J.best[left].gain = -CUDART_INF;
-      if (right >= 0) J.best[right].gain = -CUDART_INF;
-      st->do_search = 0;
-    }
-    return;
-  }
-  int32_t smaller_slot, parent_slot;
-  if (right < 0) {
-    smaller_slot = st->next_free;
-    parent_slot = -1;
-    if (lane == 0) {
-      st->next_free += 1;
-      J.leaf_slot[left] = smaller_slot;
-      st->smaller_leaf = left;
-      st->larger_leaf = -1;
-      st->smaller_slot = smaller_slot;
-      st->larger_slot = -1;
-      st->parent_slot = -1;
-      st->use_subtract = 0;
-    }
-  } else {
-    parent_slot = J.leaf_slot[left];
-    smaller_slot = st->next_free;
-    if (lane == 0) {
-      st->next_free += 1;
-      if (nl < nr) {  // the left child is smaller: the right child inherits the parent's slot
-        J.leaf_slot[right] = parent_slot;
-        J.leaf_slot[left] = smaller_slot;
-        st->smaller_leaf = left;
-        st->larger_leaf = right;
-      } else {
-        J.leaf_slot[right] = smaller_slot;
-        st->smaller_leaf = right;
-        st->larger_leaf = left;
-      }
-      st->smaller_slot = smaller_slot;
-      st->larger_slot = parent_slot;
-      st->parent_slot = parent_slot;
-      st->use_subtract = 1;
-    }
-  }
-  if (lane == 0) {
-    int32_t sl = right < 0 ? left : (nl < nr ? left : right);
-    int64_t rows = J.leaf_count[sl];
-    if (rows == p.n) st->hist_rows_direct += rows;
-    else st->hist_rows_gather += rows;
-    st->hist_builds += 1;
-  }
-  // serial.rs:840-854 — features the parent could not split are skipped for both children.
-  for (int f = lane; f < p.F; f += 32) {
-    uint8_t u = parent_slot < 0 ? 1 : J.splittable[(size_t)parent_slot * p.F + f];
-    J.used[f] = u;
-    if (!u) J.splittable[(size_t)smaller_slot * p.F + f] = 0;
-  }
-  if (lane == 0) st->do_search = 1;
-}
-
-__global__ void __launch_bounds__(32) k_post_split(const Job* __restrict__ jobs, Params p,
-                                                   const DevFeature* __restrict__ feats) {
-  const Job& J = jobs[blockIdx.z];
-  JobState* st = J.st;
-  if (st->stop) return;
-  const int lane = threadIdx.x;
-  const int32_t bl = st->split_leaf, nl = st->new_leaf;
-  const int64_t L = st->total_left;
-  const int64_t b = J.leaf_begin[bl], c = J.leaf_count[bl];
-  const int32_t buf = J.leaf_buf[bl];
-  Cand info = J.best[bl];
-  __syncwarp();
-  if (lane == 0) {
-    J.leaf_count[bl] = L;
-    J.leaf_begin[nl] = b + L;
-    J.leaf_count[nl] = c - L;
-    J.leaf_buf[bl] = 1 - buf;
-    J.leaf_buf[nl] = 1 - buf;
-    info.left_count = (int32_t)L;
-    info.right_count = (int32_t)(c - L);
-    bk_split& r = J.records[st->tree_leaves - 1];
-    r.leaf = bl;
-    r.right_leaf = nl;
-    r.inner_feature = info.inner;
-    r.real_feature = info.feature;
-    r.threshold = info.threshold;
-    r.default_left = info.default_left;
-    r.missing_type = feats[info.inner].missing;
-    r.left_count = info.left_count;
-    r.right_count = info.right_count;
-    r.left_output = info.left_output;
-    r.right_output = info.right_output;
-    r.left_sum_gradient = info.lsg;
-    r.left_sum_hessian = info.lsh;
-    r.right_sum_gradient = info.rsg;
-    r.right_sum_hessian = info.rsh;
-    r.gain = info.gain;
-    r.left_int_sum = info.lint;
-    r.right_int_sum = info.rint;
-    J.leaf_value[bl] = isnan(info.left_output) ? 0.0 : info.left_output;
-    J.leaf_value[nl] = isnan(info.right_output) ? 0.0 : info.right_output;
-    J.leaf_depth[nl] = J.leaf_depth[bl] + 1;
-    J.leaf_depth[bl] += 1;
-    LeafSum ls{info.lsg, info.lsh, info.left_output, info.lint, info.left_count, 0};
-    LeafSum rs{info.rsg, info.rsh, info.right_output, info.rint, info.right_count, 0};
-    J.leaf_sum[bl] = ls;
-    J.leaf_sum[nl] = rs;
-    J.best[bl] = info;
-    st->tree_leaves += 1;
-  }
-  __syncwarp();
-  before_find_best_split(J, p, st, bl, nl, lane);
-}
-
 // Root of a tree (serial.rs:658-776 after the root sums, then :580-586 and the first
 // BeforeFindBestSplit). leaf_sum[0] and root_count are already set.
 __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs, Params p) {
@@ -754,6 +783,8 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
     Cand c;
     cand_reset(&c, -1, -1);
     J.best[i] = c;
+    J.bgain[i] = c.gain;
+    J.bfeat[i] = -1;
   }
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -775,17 +806,13 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
 }  // namespace
 
 void launch_search(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s) {
-  dim3 grid((unsigned)ceil_div64(p.F, 4), 1, num_jobs);
-  k_search<<<grid, 128, 0, s>>>(d_jobs, p, feats);
+  dim3 grid((unsigned)ceil_div64(2 * p.F, 2), 1, num_jobs);
+  if (!p.use_l1 && !p.use_max && !p.use_smooth)
+    k_search<true><<<grid, 64, 0, s>>>(d_jobs, p, feats);
+  else
+    k_search<false><<<grid, 64, 0, s>>>(d_jobs, p, feats);
 }
 
-void launch_decide(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s) {
-  k_decide<<<dim3(1, 1, num_jobs), 64, 0, s>>>(d_jobs, p, feats);
-}
-
-void launch_post_split(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s) {
-  k_post_split<<<dim3(1, 1, num_jobs), 32, 0, s>>>(d_jobs, p, feats);
-}
 
 void launch_tree_begin(const Job* d_jobs, int num_jobs, const Params& p, cudaStream_t s) {
   k_tree_begin<<<dim3(1, 1, num_jobs), 256, 0, s>>>(d_jobs, p);

@@ -197,12 +197,7 @@ def run_gpu(args, rank, world):
     clk = clocks.stop()
     plain = form(False, 0, max(1, args.steps // 2), 1)
     e2e = form(True, 1, args.steps, 1, e2e=True)
-    ms = main["ms_per_step"]
-    if world > 1:
-        t = torch.tensor([ms], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world * 1000.0 / ms
+    ms, value = aggregate_ranks(main["ms_per_step"], world)
     hist_gbs = main["hist_bytes"] / (main["hist_ms"] * 1e6) if main["hist_ms"] > 0 else None
     launches_per_step = 4 + 4 + 1 + 1 + 7 * (args.leaves - 1) + 1
     line = {
@@ -229,6 +224,19 @@ def run_gpu(args, rank, world):
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(ds, y, sample_rows=args.cpu_rows)
     return line
+
+
+def aggregate_ranks(ms_per_step, world):
+    """Replicas: the slowest rank's time per step, and the iterations of all ranks per second."""
+    ms = float(ms_per_step)
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+        t = torch.tensor([ms], dtype=torch.float64, device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    return ms, world * 1000.0 / ms
 
 
 def _device_view(ptr, count):
