@@ -80,32 +80,46 @@ __device__ __forceinline__ void before_find_best_split(const Job& J, const Param
   if (lane == 0) st->do_search = 1;
 }
 
-// Runs on the first warp of the last CTA of the partition scatter.
+// Runs on the first warp of the last CTA of the partition scatter: SerialTreeLearner::split's
+// bookkeeping after DataPartition::split, then BeforeFindBestSplit(left, right) of the next
+// iteration. Every value is loaded first (independent loads in flight together), then every
+// store is issued, so the serial tail of a split costs about one memory round trip.
 __device__ __forceinline__ void post_split_body(const Job& J, const Params& p, const DevFeature* feats) {
   JobState* st = J.st;
   const int lane = threadIdx.x;
-  const int32_t bl = st->split_leaf, nl = st->new_leaf;
+  // ---- loads ----
+  const int32_t bl = st->split_leaf, nl = st->new_leaf, tl = st->tree_leaves, nf = st->next_free;
   const int64_t L = __ldcg(&st->total_left);  // written by another CTA of the scatter
+  const int64_t hdir = st->hist_rows_direct, hgat = st->hist_rows_gather, hbld = st->hist_builds;
   const int64_t b = J.leaf_begin[bl], c = J.leaf_count[bl];
-  const int32_t buf = J.leaf_buf[bl];
+  const int32_t buf = J.leaf_buf[bl], depth = J.leaf_depth[bl], pslot = J.leaf_slot[bl];
   Cand info = J.best[bl];
-  __syncwarp();
+  const int32_t miss = feats[info.inner].missing;
+  // ---- the split (serial.rs:1685-1876) ----
+  const int64_t R = c - L;
+  info.left_count = (int32_t)L;
+  info.right_count = (int32_t)R;
+  const int32_t nd = depth + 1;  // tree.leaf_depth of both children
+  // ---- BeforeFindBestSplit(bl, nl) (serial.rs:779-825) ----
+  bool go = !(p.max_depth > 0 && nd >= p.max_depth);
+  const int32_t nleft = (int32_t)L, nright = (int32_t)R;
+  if (go && nright < p.min_data * 2 && nleft < p.min_data * 2) go = false;
+  const bool left_smaller = nleft < nright;
+  const int32_t sslot = nf;  // the smaller child gets a new slot; the larger keeps the parent's
   if (lane == 0) {
     J.leaf_count[bl] = L;
     J.leaf_begin[nl] = b + L;
-    J.leaf_count[nl] = c - L;
+    J.leaf_count[nl] = R;
     J.leaf_buf[bl] = 1 - buf;
     J.leaf_buf[nl] = 1 - buf;
-    info.left_count = (int32_t)L;
-    info.right_count = (int32_t)(c - L);
-    bk_split& r = J.records[st->tree_leaves - 1];
+    bk_split& r = J.records[tl - 1];
     r.leaf = bl;
     r.right_leaf = nl;
     r.inner_feature = info.inner;
     r.real_feature = info.feature;
     r.threshold = info.threshold;
     r.default_left = info.default_left;
-    r.missing_type = feats[info.inner].missing;
+    r.missing_type = miss;
     r.left_count = info.left_count;
     r.right_count = info.right_count;
     r.left_output = info.left_output;
@@ -119,20 +133,44 @@ __device__ __forceinline__ void post_split_body(const Job& J, const Params& p, c
     r.right_int_sum = info.rint;
     J.leaf_value[bl] = isnan(info.left_output) ? 0.0 : info.left_output;
     J.leaf_value[nl] = isnan(info.right_output) ? 0.0 : info.right_output;
-    J.leaf_depth[nl] = J.leaf_depth[bl] + 1;
-    J.leaf_depth[bl] += 1;
-    LeafSum ls{info.lsg, info.lsh, info.left_output, info.lint, info.left_count, 0};
-    LeafSum rs{info.rsg, info.rsh, info.right_output, info.rint, info.right_count, 0};
-    J.leaf_sum[bl] = ls;
-    J.leaf_sum[nl] = rs;
+    J.leaf_depth[nl] = nd;
+    J.leaf_depth[bl] = nd;
+    J.leaf_sum[bl] = LeafSum{info.lsg, info.lsh, info.left_output, info.lint, info.left_count, 0};
+    J.leaf_sum[nl] = LeafSum{info.rsg, info.rsh, info.right_output, info.rint, info.right_count, 0};
+    if (!go) info.gain = -CUDART_INF;  // no search for the children: both leaves drop out
     J.best[bl] = info;
     J.bgain[bl] = info.gain;
     J.bfeat[bl] = info.feature;
-    st->tree_leaves += 1;
+    st->tree_leaves = tl + 1;
+    if (!go) {
+      J.best[nl].gain = -CUDART_INF;
+      J.bgain[nl] = -CUDART_INF;
+      st->do_search = 0;
+    } else {
+      st->next_free = nf + 1;
+      J.leaf_slot[left_smaller ? nl : bl] = pslot;
+      J.leaf_slot[left_smaller ? bl : nl] = sslot;
+      st->smaller_leaf = left_smaller ? bl : nl;
+      st->larger_leaf = left_smaller ? nl : bl;
+      st->smaller_slot = sslot;
+      st->larger_slot = pslot;
+      st->parent_slot = pslot;
+      st->use_subtract = 1;
+      const int64_t rows = left_smaller ? L : R;
+      if (rows == p.n) st->hist_rows_direct = hdir + rows;
+      else st->hist_rows_gather = hgat + rows;
+      st->hist_builds = hbld + 1;
+      st->do_search = 1;
+    }
   }
-  __syncwarp();
-  before_find_best_split(J, p, st, bl, nl, lane);
+  if (go) {
+    // serial.rs:840-854 — features the parent could not split are skipped for both children
+    for (int f = lane; f < p.F; f += 32) {
+      uint8_t u = J.splittable[(size_t)pslot * p.F + f];
+      J.used[f] = u;
+      if (!u) J.splittable[(size_t)sslot * p.F + f] = 0;
+    }
+  }
 }
-
 
 }  // namespace bk

@@ -57,6 +57,43 @@ __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blo
   return true;
 }
 
+// One warp's rows of a round: global loads of the 32-byte tile sectors and the packed values.
+struct RoundLoad {
+  uint4 a, b;
+  int32_t v;
+};
+
+__device__ __forceinline__ RoundLoad load_round_int(const Range& R, const uint8_t* tb, const int16_t* packed,
+                                                    int64_t base, int lane, bool wide) {
+  RoundLoad L;
+  L.a = make_uint4(0, 0, 0, 0);
+  L.b = make_uint4(0, 0, 0, 0);
+  L.v = 0;
+  int64_t i = base + lane;
+  if (i < R.r1) {
+    int64_t row = R.direct ? i : (int64_t)R.idx[i];
+    const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * TILE);
+    L.a = __ldg(src);
+    L.b = __ldg(src + 1);
+    int32_t pk = packed[row];
+    int32_t gi = (int32_t)(int8_t)(pk >> 8);
+    int32_t hi = pk & 0xff;
+    L.v = wide ? ((gi & 0xffff) | (hi << 16)) : gi * 65536 + hi;
+  }
+  return L;
+}
+
+template <bool WIDE>
+__device__ __forceinline__ void add_row(uint32_t* hot, int32_t* cold_g, int32_t* cold_h, uint32_t bin, int32_t v,
+                                        int lane) {
+  if (WIDE) {
+    atomicAdd(&cold_g[bin * TILE + lane], (int32_t)(int16_t)(v & 0xffff));
+    atomicAdd(&cold_h[bin * TILE + lane], v >> 16);
+  } else {
+    atomicAdd(&hot[bin * TILE + lane], (uint32_t)v);
+  }
+}
+
 template <bool WIDE>
 __global__ void __launch_bounds__(1024, 1)
     k_hist_int(const Job* __restrict__ jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile,
@@ -81,45 +118,47 @@ __global__ void __launch_bounds__(1024, 1)
   __syncthreads();
   const uint8_t* tb = bins_rt + (size_t)tile * (size_t)p.n * TILE;
   const int16_t* packed = J.packed;
+  // lanes past the last feature of the last tile (padding bytes) add nothing
   const bool feat_lane = tile * TILE + lane < p.F;
   const int64_t per_round = (int64_t)TILE * nwarps;
   const int64_t rounds = ceil_div64(R.r1 - R.r0, per_round);
+  uint4* my_stage = stage + warp * 64;
+  const uint8_t* sb = reinterpret_cast<const uint8_t*>(my_stage);
+  int32_t* my_v = stage_v + warp * 32;
+  // software pipeline: the next round's rows are in flight while this round is added up
+  RoundLoad cur = load_round_int(R, tb, packed, R.r0 + (int64_t)warp * TILE, lane, WIDE);
   for (int64_t rd = 0; rd < rounds; ++rd) {
-    int64_t base = R.r0 + rd * per_round + (int64_t)warp * TILE;
+    const int64_t base = R.r0 + rd * per_round + (int64_t)warp * TILE;
+    RoundLoad nxt = load_round_int(R, tb, packed, base + per_round, lane, WIDE);
     if (base < R.r1) {
-      int64_t i = base + lane;
-      bool valid = i < R.r1;
-      uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
-      int32_t v = 0;
-      if (valid) {
-        int64_t row = R.direct ? i : (int64_t)R.idx[i];
-        const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * TILE);
-        a = __ldg(src);
-        b = __ldg(src + 1);
-        int32_t pk = packed[row];
-        int32_t gi = (int32_t)(int8_t)(pk >> 8);
-        int32_t hi = pk & 0xff;
-        v = WIDE ? ((gi & 0xffff) | (hi << 16)) : gi * 65536 + hi;
-      }
-      stage[(warp * 32 + lane) * 2] = a;
-      stage[(warp * 32 + lane) * 2 + 1] = b;
-      stage_v[warp * 32 + lane] = v;
+      my_stage[lane * 2] = cur.a;
+      my_stage[lane * 2 + 1] = cur.b;
+      my_v[lane] = cur.v;
       __syncwarp();
-      const uint8_t* sb = reinterpret_cast<const uint8_t*>(stage + warp * 64);
-      // lanes past the last feature of the last tile (padding bytes) add nothing
-      int jn = feat_lane ? (int)min((int64_t)32, R.r1 - base) : 0;
-      for (int j = 0; j < jn; ++j) {
-        uint32_t bin = sb[j * 32 + lane];
-        int32_t vv = stage_v[warp * 32 + j];
-        if (WIDE) {
-          atomicAdd(&cold_g[bin * TILE + lane], (int32_t)(int16_t)(vv & 0xffff));
-          atomicAdd(&cold_h[bin * TILE + lane], vv >> 16);
-        } else {
-          atomicAdd(&hot[bin * TILE + lane], (uint32_t)vv);
+      const int jn = (int)min((int64_t)32, R.r1 - base);  // warp-uniform
+      if (jn == 32) {
+#pragma unroll 2
+        for (int j = 0; j < 32; j += 4) {
+          const int4 v4 = *reinterpret_cast<const int4*>(my_v + j);
+          const uint32_t b0 = sb[(j + 0) * 32 + lane], b1 = sb[(j + 1) * 32 + lane];
+          const uint32_t b2 = sb[(j + 2) * 32 + lane], b3 = sb[(j + 3) * 32 + lane];
+          if (feat_lane) {
+            add_row<WIDE>(hot, cold_g, cold_h, b0, v4.x, lane);
+            add_row<WIDE>(hot, cold_g, cold_h, b1, v4.y, lane);
+            add_row<WIDE>(hot, cold_g, cold_h, b2, v4.z, lane);
+            add_row<WIDE>(hot, cold_g, cold_h, b3, v4.w, lane);
+          }
+        }
+      } else {
+        for (int j = 0; j < jn; ++j) {
+          const uint32_t b0 = sb[j * 32 + lane];
+          const int32_t v0 = my_v[j];
+          if (feat_lane) add_row<WIDE>(hot, cold_g, cold_h, b0, v0, lane);
         }
       }
       __syncwarp();
     }
+    cur = nxt;
     if (!WIDE && ((rd + 1) % flush_rounds == 0 || rd + 1 == rounds)) {
       __syncthreads();
       for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
@@ -198,19 +237,22 @@ __global__ void __launch_bounds__(1024, 1)
     stage_v[warp * 32 + lane] = v;
     __syncwarp();
     const uint8_t* sb = reinterpret_cast<const uint8_t*>(stage + warp * 64);
-    int jn = feat_lane ? (int)min((int64_t)32, R.r1 - base) : 0;
+    const int jn = (int)min((int64_t)32, R.r1 - base);  // warp-uniform; padding lanes add nothing
+#pragma unroll 4
     for (int j = 0; j < jn; ++j) {
       uint32_t e = (uint32_t)sb[j * 32 + lane] * TILE + lane;
       float2 vv = stage_v[warp * 32 + j];
-      float old = atomicAdd(&ghi[e], vv.x);
-      float err = two_sum_err(old, vv.x, __fadd_rn(old, vv.x));
-      if (err != 0.f) atomicAdd(&glo[e], err);
-      if (CONST_HESS) {
-        atomicAdd(&hcnt[e], 1u);
-      } else {
-        float oh = atomicAdd(&hhi[e], vv.y);
-        float eh = two_sum_err(oh, vv.y, __fadd_rn(oh, vv.y));
-        if (eh != 0.f) atomicAdd(&hlo[e], eh);
+      if (feat_lane) {
+        float old = atomicAdd(&ghi[e], vv.x);
+        float err = two_sum_err(old, vv.x, __fadd_rn(old, vv.x));
+        if (err != 0.f) atomicAdd(&glo[e], err);
+        if (CONST_HESS) {
+          atomicAdd(&hcnt[e], 1u);
+        } else {
+          float oh = atomicAdd(&hhi[e], vv.y);
+          float eh = two_sum_err(oh, vv.y, __fadd_rn(oh, vv.y));
+          if (eh != 0.f) atomicAdd(&hlo[e], eh);
+        }
       }
     }
     __syncwarp();
