@@ -16,6 +16,9 @@
 
 #include "bkgpu.h"
 
+// Sets the calling thread's message for bk_last_error() (defined in bk_learner.cu).
+void bk_set_last_error(const char* msg);
+
 namespace bk {
 
 constexpr int TILE = 32;

@@ -25,6 +25,13 @@ namespace {
 
 thread_local std::string g_last_error;
 
+}  // namespace
+
+// Shared with the other translation units of the library (bk_common.cuh).
+void bk_set_last_error(const char* msg) { g_last_error = msg; }
+
+namespace {
+
 void set_error(const char* fmt, ...) {
   char buf[1024];
   va_list ap;

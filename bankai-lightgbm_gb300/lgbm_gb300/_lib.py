@@ -66,6 +66,7 @@ _GPU_SIGNATURES = [
     ("bk_learner_objective_loss", _i32, [_P, _i32, _P, _P, _P]),
     ("bk_learner_stream", _i32, [_P, _P]),
     ("bk_learner_destroy", _i32, [_P]),
+    ("bk_partition_split_noalloc", _i32, [_P, _i64, _P, _i64, _P, _P, _P, _P]),
 ]
 
 # every symbol include/bkgpu.h declares

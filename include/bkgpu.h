@@ -125,6 +125,20 @@ int bk_learner_stream(bk_learner* learner, void** stream);
 
 int bk_learner_destroy(bk_learner* learner);
 
+/* Stable partition of one row range, for callers that cannot allocate device memory (a host
+ * whose GPU memory belongs to its own caching allocator, or a latency-critical path that cannot
+ * take cudaMalloc's implicit synchronization). No counterpart in the reference: it is the
+ * learner's DataPartition::Split kernel pair made callable on its own, with no allocation.
+ * rows_in: device int32 row ids [num_rows]; bins: device uint8 stored bins indexed by row id
+ * (bins_len entries); route: host uint8[256], route[b] != 0 sends stored bin b left; rows_out:
+ * device int32 [num_rows], not aliasing rows_in, receives the left rows then the right rows, each
+ * in input order; *num_left (host) receives the left count. stream: a cudaStream_t or NULL.
+ * Synchronous. Its only scratch is a fixed 8 KiB device array inside the library (at most 2^30
+ * rows; larger inputs are rejected), set up on the first call on each device — make that first
+ * call before any stream capture. Calls that overlap on the GPU share that array and race. */
+int bk_partition_split_noalloc(const int32_t* rows_in, int64_t num_rows, const uint8_t* bins, int64_t bins_len,
+                               const uint8_t* route, int32_t* rows_out, int64_t* num_left, void* stream);
+
 /* Message of the last failed call on this thread ("" if none). */
 const char* bk_last_error(void);
 
