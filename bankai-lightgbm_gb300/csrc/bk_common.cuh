@@ -142,6 +142,10 @@ void launch_row_leaf(const Job* d_jobs, int num_jobs, const Params& p, int32_t* 
 void launch_mt_seed(const Job* d_jobs, int num_jobs, uint32_t seed, cudaStream_t s);
 constexpr int kRootGrid = 256;
 
+// bk_predict.cu
+cudaError_t predict_tree(const DevFeature* feats, int32_t num_leaves, const int32_t* d_tree, const double* d_leaf_value,
+                         const uint8_t* bins, int64_t m, double* score, cudaStream_t s);
+
 // bk_objective.cu
 cudaError_t objective_gradients(int kind, const double* score, const float* label, int64_t n, int K, double sigmoid,
                                 float* g, float* h, cudaStream_t s);

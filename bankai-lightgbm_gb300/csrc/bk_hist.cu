@@ -127,6 +127,7 @@ __global__ void __launch_bounds__(1024, 1)
   int32_t* my_v = stage_v + warp * 32;
   // software pipeline: the next round's rows are in flight while this round is added up
   RoundLoad cur = load_round_int(R, tb, packed, R.r0 + (int64_t)warp * TILE, lane, WIDE);
+  int until_flush = flush_rounds;
   for (int64_t rd = 0; rd < rounds; ++rd) {
     const int64_t base = R.r0 + rd * per_round + (int64_t)warp * TILE;
     RoundLoad nxt = load_round_int(R, tb, packed, base + per_round, lane, WIDE);
@@ -159,7 +160,8 @@ __global__ void __launch_bounds__(1024, 1)
       __syncwarp();
     }
     cur = nxt;
-    if (!WIDE && ((rd + 1) % flush_rounds == 0 || rd + 1 == rounds)) {
+    if (!WIDE && (--until_flush == 0 || rd + 1 == rounds)) {
+      until_flush = flush_rounds;
       __syncthreads();
       for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
         int32_t s = (int32_t)hot[e];

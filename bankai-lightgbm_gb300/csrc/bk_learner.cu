@@ -141,12 +141,15 @@ struct bk_learner {
   double* h_leaf_values = nullptr;
   JobState* h_state = nullptr;
   double* d_leaf_vals_in = nullptr;
+  int32_t* d_tree = nullptr;     // one tree's node arrays for prediction (5 x (num_leaves - 1))
+  double* d_tree_values = nullptr;
+  std::vector<int32_t> h_tree;
   // graph
   cudaGraphExec_t graph_exec = nullptr;
   // timing
   cudaEvent_t ev_start = nullptr, ev_end = nullptr;
   std::vector<cudaEvent_t> hist_events;
-  double last_total_ms = 0, last_hist_ms = 0, last_hist_bytes = 0;
+  double last_total_ms = 0, last_hist_ms = 0, last_hist_bytes = 0, last_search_ms = 0, last_part_ms = 0;
 
   template <typename T>
   T* dalloc(size_t count) {
@@ -176,15 +179,18 @@ struct bk_learner {
     else CK(cudaEventRecord(hist_events[i], stream));
   }
 
-  // One grow-loop step (iteration `it`) of all jobs.
+  // One grow-loop step (iteration `it`) of all jobs; with timing on, events split the step into
+  // histogram / search / partition phases.
   void step_a(int it) {
-    record_hist_event(2 * it);
+    record_hist_event(4 * it);
     launch_hist(d_jobs, K, p, d_bins_rt, hl, stream);
-    record_hist_event(2 * it + 1);
+    record_hist_event(4 * it + 1);
     launch_search(d_jobs, K, p, d_feat, stream);  // its last CTA also picks the split
+    record_hist_event(4 * it + 2);
   }
-  void step_b() {
+  void step_b(int it) {
     launch_partition(d_jobs, K, p, d_bins_cm, d_feat, stream);  // its last CTA also records the split
+    record_hist_event(4 * it + 3);
   }
 
   void tree_prologue() {
@@ -208,7 +214,7 @@ struct bk_learner {
         tree_prologue();
         for (int it = 0; it < p.num_leaves - 1; ++it) {
           step_a(it);
-          step_b();
+          step_b(it);
         }
         tree_epilogue();
       } catch (...) {
@@ -236,7 +242,7 @@ struct bk_learner {
       bool all = true;
       for (int j = 0; j < K; ++j) all = all && h_state[j].stop;
       if (all) break;
-      step_b();
+      step_b(it);
     }
     tree_epilogue();
   }
@@ -430,6 +436,8 @@ int bk_learner_create(const bk_feature* features, int32_t num_features, const ui
     CK(cudaMallocHost(&L->h_leaf_values, sizeof(double) * (size_t)Lv * K));
     CK(cudaMallocHost(&L->h_state, sizeof(JobState) * K));
     L->d_leaf_vals_in = L->dalloc<double>((size_t)Lv * K);
+    L->d_tree = L->dalloc<int32_t>(5 * (size_t)Lv);
+    L->d_tree_values = L->dalloc<double>(Lv);
     CK(cudaEventCreate(&L->ev_start));
     CK(cudaEventCreate(&L->ev_end));
     CK(cudaStreamSynchronize(L->stream));
@@ -477,9 +485,9 @@ int bk_learner_train(bk_learner* L, const float* gradients, const float* hessian
       CK(cudaMemcpyAsync(&st->hist_rows_direct, &L->h_state[j].hist_rows_direct, 3 * sizeof(int64_t),
                          cudaMemcpyHostToDevice, L->stream));
     }
-    if (L->timing && L->hist_events.size() != (size_t)(2 * (Lv - 1))) {
+    if (L->timing && L->hist_events.size() != (size_t)(4 * (Lv - 1))) {
       for (cudaEvent_t e : L->hist_events) cudaEventDestroy(e);
-      L->hist_events.assign(2 * (Lv - 1), nullptr);
+      L->hist_events.assign(4 * (Lv - 1), nullptr);
       for (auto& e : L->hist_events) CK(cudaEventCreate(&e));
       if (L->graph_exec) {
         cudaGraphExecDestroy(L->graph_exec);
@@ -502,14 +510,19 @@ int bk_learner_train(bk_learner* L, const float* gradients, const float* hessian
     float ms = 0.f;
     CK(cudaEventElapsedTime(&ms, L->ev_start, L->ev_end));
     L->last_total_ms = ms;
-    L->last_hist_ms = 0.0;
+    L->last_hist_ms = L->last_search_ms = L->last_part_ms = 0.0;
     if (L->timing) {
-      // histogram launches of the steps that ran (a finished tree's remaining steps return early
-      // but are still timed: they are part of the replayed graph)
+      // the phases of the steps that ran (a finished tree's remaining steps return early but are
+      // still timed: they are part of the replayed graph); a stepwise loop that stopped early
+      // leaves later events unrecorded, which the elapsed-time calls report and skip
       for (int it = 0; it < Lv - 1; ++it) {
         float t = 0.f;
-        if (cudaEventElapsedTime(&t, L->hist_events[2 * it], L->hist_events[2 * it + 1]) == cudaSuccess)
+        if (cudaEventElapsedTime(&t, L->hist_events[4 * it], L->hist_events[4 * it + 1]) == cudaSuccess)
           L->last_hist_ms += t;
+        if (cudaEventElapsedTime(&t, L->hist_events[4 * it + 1], L->hist_events[4 * it + 2]) == cudaSuccess)
+          L->last_search_ms += t;
+        if (cudaEventElapsedTime(&t, L->hist_events[4 * it + 2], L->hist_events[4 * it + 3]) == cudaSuccess)
+          L->last_part_ms += t;
       }
       cudaGetLastError();
     }
@@ -648,6 +661,16 @@ int bk_learner_last_timing(bk_learner* L, double* total_ms, double* hist_ms, dou
   return 0;
 }
 
+int bk_learner_last_phase_timing(bk_learner* L, double* search_ms, double* partition_ms) {
+  if (!L) {
+    set_error("bk_learner_last_phase_timing: null learner");
+    return -1;
+  }
+  if (search_ms) *search_ms = L->last_search_ms;
+  if (partition_ms) *partition_ms = L->last_part_ms;
+  return 0;
+}
+
 int bk_learner_gradient_buffers(bk_learner* L, float** gradients, float** hessians) {
   if (!L) {
     set_error("bk_learner_gradient_buffers: null learner");
@@ -687,6 +710,52 @@ int bk_learner_objective_loss(bk_learner* L, int32_t kind, const double* score, 
     double s = 0.0;
     for (double v : part) s += v;
     *out = s / (double)L->p.n;
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
+  }
+  return 0;
+}
+
+int bk_learner_predict_add(bk_learner* L, int32_t num_leaves, const int32_t* left_child, const int32_t* right_child,
+                           const int32_t* split_feature_inner, const uint32_t* threshold_in_bin,
+                           const int8_t* decision_type, const double* leaf_value, const uint8_t* bins,
+                           int64_t num_rows, double* score) {
+  if (!L || !leaf_value || !bins || !score || num_rows < 0 || num_leaves < 1 || num_leaves > L->p.num_leaves ||
+      (num_leaves > 1 && (!left_child || !right_child || !split_feature_inner || !threshold_in_bin ||
+                          !decision_type))) {
+    set_error("bk_learner_predict_add: invalid arguments");
+    return -1;
+  }
+  const int ni = num_leaves - 1;
+  // validate the node arrays so the device walk stays inside them
+  for (int i = 0; i < ni; ++i) {
+    for (int32_t ch : {left_child[i], right_child[i]}) {
+      if (ch >= ni || (ch < 0 && ~ch >= num_leaves)) {
+        set_error("bk_learner_predict_add: node %d has child %d outside the tree", i, ch);
+        return -1;
+      }
+    }
+    if (split_feature_inner[i] < 0 || split_feature_inner[i] >= L->p.F ||
+        threshold_in_bin[i] >= (uint32_t)L->h_feat[split_feature_inner[i]].num_bin) {
+      set_error("bk_learner_predict_add: node %d splits an unknown feature or bin", i);
+      return -1;
+    }
+  }
+  L->h_tree.assign(5 * (size_t)std::max(ni, 1), 0);
+  for (int i = 0; i < ni; ++i) {
+    L->h_tree[i] = left_child[i];
+    L->h_tree[ni + i] = right_child[i];
+    L->h_tree[2 * ni + i] = split_feature_inner[i];
+    L->h_tree[3 * ni + i] = (int32_t)threshold_in_bin[i];
+    L->h_tree[4 * ni + i] = decision_type[i];
+  }
+  try {
+    CK(cudaMemcpyAsync(L->d_tree, L->h_tree.data(), sizeof(int32_t) * L->h_tree.size(), cudaMemcpyHostToDevice,
+                       L->stream));
+    CK(cudaMemcpyAsync(L->d_tree_values, leaf_value, sizeof(double) * num_leaves, cudaMemcpyHostToDevice, L->stream));
+    if (num_rows > 0)
+      CK(predict_tree(L->d_feat, num_leaves, L->d_tree, L->d_tree_values, bins, num_rows, score, L->stream));
+    CK(cudaStreamSynchronize(L->stream));
   } catch (const CudaError& e) {
     return fail_cuda(e);
   }

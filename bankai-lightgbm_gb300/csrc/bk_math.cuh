@@ -109,4 +109,48 @@ __device__ __forceinline__ bool better_than(double ga, int32_t fa, double gb, in
   return a < b;
 }
 
+// The route of one stored bin for a numerical split of a single-feature dense group
+// (data_partition.rs:299-410 with group_view :25-40: min_bin 1, max_bin gbins - 1,
+// use_min_bin false). 1 = left.
+__device__ __forceinline__ uint8_t route_bin(const DevFeature& m, uint32_t threshold, bool default_left, uint32_t bin) {
+  const uint32_t min_bin = 1, max_bin = (uint32_t)m.gbins - 1;
+  const uint32_t default_bin = (uint32_t)m.default_bin, mfb = (uint32_t)m.mfb;
+  bool miss_zero = false, miss_na = false, mfb_zero = false, mfb_na = false;
+  if (m.missing == 1) {
+    miss_zero = true;
+    mfb_zero = default_bin == mfb;
+  } else if (m.missing == 2) {
+    miss_na = true;
+    mfb_na = (max_bin == mfb + 1) && mfb > 0;
+  }
+  uint32_t th = threshold + min_bin;
+  uint32_t t_zero_bin = min_bin + default_bin;
+  if (mfb == 0) {
+    th -= 1;
+    t_zero_bin -= 1;
+  }
+  const bool default_route_left = mfb <= threshold;
+  const bool missing_default_left = (miss_zero || miss_na) && default_left;
+  const bool max_bin_left = max_bin <= th;
+  const bool either_mfb = (miss_na && mfb_na) || (miss_zero && mfb_zero);
+  bool left;
+  if (min_bin < max_bin) {
+    if ((miss_zero && !mfb_zero && bin == t_zero_bin) || (miss_na && !mfb_na && bin == max_bin))
+      left = missing_default_left;
+    else if (bin == 0)
+      left = either_mfb ? missing_default_left : default_route_left;
+    else
+      left = !(bin > th);
+  } else if (miss_zero && !mfb_zero && bin == t_zero_bin) {
+    left = missing_default_left;
+  } else if (bin != max_bin) {
+    left = either_mfb ? missing_default_left : default_route_left;
+  } else if (miss_na && !mfb_na) {
+    left = missing_default_left;
+  } else {
+    left = max_bin_left;
+  }
+  return left ? 1 : 0;
+}
+
 }  // namespace bk

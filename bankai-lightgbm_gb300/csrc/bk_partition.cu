@@ -19,6 +19,7 @@ constexpr int kItems = 8;
 
 struct PartRange {
   int64_t begin, count, r0, r1;
+  int active;  // CTAs with rows: ceil(count / chunk)
   const int32_t* src;
   int32_t* dst;
   const uint8_t* col;
@@ -35,8 +36,10 @@ __device__ __forceinline__ void part_range(const Job& J, const Params& p, const 
   r->col = bins_cm + (size_t)st->split_inner * (size_t)p.n;
   int64_t chunk = ceil_div64(r->count, p.part_grid);
   chunk = (chunk + kThreads * kItems - 1) / (kThreads * kItems) * (kThreads * kItems);
+  if (chunk < kThreads * kItems) chunk = kThreads * kItems;
   r->r0 = min((int64_t)blockIdx.x * chunk, r->count);
   r->r1 = min(r->r0 + chunk, r->count);
+  r->active = (int)ceil_div64(r->count, chunk);
 }
 
 template <typename T>
@@ -77,6 +80,7 @@ __global__ void __launch_bounds__(kThreads) k_part_count(const Job* __restrict__
   __syncthreads();
   PartRange R;
   part_range(J, p, bins_cm, &R);
+  if ((int)blockIdx.x >= R.active) return;  // no rows: the scatter reads only active CTAs' counts
   int64_t local = 0;
   for (int64_t i = R.r0 + threadIdx.x; i < R.r1; i += kThreads) local += lut[R.col[R.src[i]]];
   int64_t total;
@@ -98,15 +102,18 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict
   part_range(J, p, bins_cm, &R);
   // left rows before this chunk, and in total
   int64_t before = 0, all = 0;
-  for (int i = threadIdx.x; i < p.part_grid; i += kThreads) {
+  const bool active = (int)blockIdx.x < R.active;
+  for (int i = threadIdx.x; active && i < R.active; i += kThreads) {
     int64_t c = J.part_cnt[i];
     all += c;
     if (i < (int)blockIdx.x) before += c;
   }
-  int64_t total_left, running;
-  block_excl_scan<int64_t>(all, &total_left, sh64);
-  block_excl_scan<int64_t>(before, &running, sh64);
-  if (blockIdx.x == 0 && threadIdx.x == 0) J.st->total_left = total_left;
+  int64_t total_left = 0, running = 0;
+  if (active) {
+    block_excl_scan<int64_t>(all, &total_left, sh64);
+    block_excl_scan<int64_t>(before, &running, sh64);
+    if (blockIdx.x == 0 && threadIdx.x == 0) J.st->total_left = total_left;
+  }
   for (int64_t base = R.r0; base < R.r1; base += kThreads * kItems) {
     int64_t e0 = base + (int64_t)threadIdx.x * kItems;
     int32_t rows[kItems];

@@ -261,6 +261,19 @@ __device__ DirBest scan_float(const Params& p, const DevFeature& m, const FloatH
   return r;
 }
 
+// As warp_first_true, trying first the 32 values around `guess` (one warp-wide evaluation) and
+// falling back to the full search when the answer lies outside that window.
+template <typename Pred>
+__device__ int64_t warp_first_true_near(int64_t hi, int64_t guess, int lane, Pred pred) {
+  guess = guess < 0 ? 0 : (guess > hi ? hi : guess);
+  const int64_t x = guess - 15 + lane;
+  const bool t = x >= hi ? true : (x < 0 ? false : pred(x));
+  const unsigned m = __ballot_sync(FULL, t);
+  if (m != 0u && (m & 1u) == 0u) return guess - 15 + (__ffs(m) - 1);  // false -> true inside
+  if (m != 0u && guess - 15 <= 0) return 0;  // everything from 0 on is true
+  return warp_first_true(hi, lane, pred);
+}
+
 // Integer thresholds of a leaf (feature-independent): for an accumulated side with integer hessian
 // x, the reference's `count >= min_data && hess >= min_hessian` test (counts estimated as
 // round_int(x * cnt_factor), feature_histogram.rs:927-940) is monotone in x, so it is x >= first_x;
@@ -272,10 +285,17 @@ struct IntThresholds {
 __device__ IntThresholds int_thresholds(const Params& p, int64_t th, double hs, int32_t num_data, int lane) {
   const double cf = (double)num_data / (double)th;
   const int64_t hi = th + 1;
-  int64_t cnt_ok = warp_first_true(hi, lane, [&](int64_t x) { return round_int((double)x * cf) >= p.min_data; });
-  int64_t hess_ok = warp_first_true(hi, lane, [&](int64_t x) { return (double)x * hs >= p.min_hess; });
-  int64_t cnt_brk =
-      warp_first_true(hi, lane, [&](int64_t x) { return round_int((double)x * cf) > num_data - p.min_data; });
+  // fp32 guesses of the transitions; the exact f64 predicates decide
+  const float fth = (float)th, fnd = (float)num_data;
+  const int64_t g_cnt = (int64_t)((float)((double)p.min_data - 0.5) * fth / fnd);
+  const int64_t g_brk = (int64_t)((float)((double)(num_data - p.min_data) + 0.5) * fth / fnd);
+  const float fh = (float)hs;
+  const int64_t g_hess = fh > 0.f ? (int64_t)fminf((float)p.min_hess / fh, 4.0e18f) : hi;
+  int64_t cnt_ok = warp_first_true_near(hi, g_cnt, lane,
+                                        [&](int64_t x) { return round_int((double)x * cf) >= p.min_data; });
+  int64_t hess_ok = warp_first_true_near(hi, g_hess, lane, [&](int64_t x) { return (double)x * hs >= p.min_hess; });
+  int64_t cnt_brk = warp_first_true_near(
+      hi, g_brk, lane, [&](int64_t x) { return round_int((double)x * cf) > num_data - p.min_data; });
   IntThresholds r;
   r.first_x = cnt_ok > hess_ok ? cnt_ok : hess_ok;
   int64_t hess_brk = th - hess_ok + 1;  // (th - x) * hs < min_hess  <=>  th - x < hess_ok
@@ -283,7 +303,11 @@ __device__ IntThresholds int_thresholds(const Params& p, int64_t th, double hs, 
   return r;
 }
 
-// FindBestThresholdSequentiallyInt, feature_histogram.rs:839-1142.
+// FindBestThresholdSequentiallyInt, feature_histogram.rs:839-1142. With PLAIN gains the scan
+// runs twice over the (cheap, exact) integer prefix sums: pass 1 evaluates every threshold in
+// fp32 and finds the best certified lower bound M; pass 2 evaluates in f64 only the thresholds
+// whose upper bound reaches M (plus, while the splittable flag is still undecided, those whose
+// pass / fail is uncertain), so most 32-threshold chunks take no f64 instruction at all.
 template <bool REV, bool PLAIN>
 __device__ DirBest scan_int(const Params& p, const DevFeature& m, const IntHist& H, bool SKIP, bool NA, int64_t tg,
                             int64_t th, double gs, double hs, int32_t num_data, double mgs, double parent,
@@ -299,12 +323,12 @@ __device__ DirBest scan_int(const Params& p, const DevFeature& m, const IntHist&
   const int off = m.offset;
   const float gsf = (float)gs, hsf = (float)hs, l2f = (float)p.l2;
   const float mgs_up = __double2float_ru(mgs), mgs_dn = __double2float_rd(mgs);
-  int64_t cg, ch;
+  int64_t cg0, ch0;
   int t_first, P;
   if (REV) {
     t_first = m.num_bin - 1 - off - (NA ? 1 : 0);
     P = t_first - (1 - off) + 1;
-    cg = ch = 0;
+    cg0 = ch0 = 0;
   } else {
     int t_end = m.num_bin - 2 - off;
     if (NA && off == 1) {
@@ -314,75 +338,90 @@ __device__ DirBest scan_int(const Params& p, const DevFeature& m, const IntHist&
         pg += unpack_g(v);
         ph += unpack_h(v);
       }
-      cg = tg - warp_sum(pg);
-      ch = th - warp_sum(ph);
+      cg0 = tg - warp_sum(pg);
+      ch0 = th - warp_sum(ph);
       t_first = -1;
     } else {
-      cg = ch = 0;
+      cg0 = ch0 = 0;
       t_first = 0;
     }
     P = t_end - t_first + 1;
   }
-  for (int c0 = 0; c0 < P; c0 += 32) {
-    int k = c0 + lane;
-    int t = REV ? t_first - k : t_first + k;
-    bool act = k < P;
-    bool cand = act && !(SKIP && (t + off) == m.default_bin);
-    int64_t g = 0, h = 0;
-    if (cand && t >= 0) {
-      int64_t v = H.get(t);
-      g = unpack_g(v);
-      h = unpack_h(v);
-    }
-    int64_t pg = warp_incl_scan(g, lane) + cg;
-    int64_t ph = warp_incl_scan(h, lane) + ch;
-    cg = __shfl_sync(FULL, pg, 31);
-    ch = __shfl_sync(FULL, ph, 31);
-    // REV accumulates the right side, FWD the left side
-    int64_t lg = REV ? tg - pg : pg;
-    int64_t lh = REV ? th - ph : ph;
-    int64_t rg = tg - lg, rh = th - lh;
-    bool first = cand && ph >= X.first_x;
-    bool brk = first && ph >= X.brk_x;
-    unsigned bm = __ballot_sync(FULL, brk);
-    int stop_lane = bm ? __ffs(bm) - 1 : 32;
-    bool valid = first && !brk && lane < stop_lane;
-    bool exact = valid, cpass = false;
-    if (PLAIN) {
-      Approx a{0.f, 0.f, true};
-      if (valid)
-        a = approx_from(__fmul_rn((float)lg, gsf), __fadd_rn(__fmul_rn((float)lh, hsf), l2f), __fmul_rn((float)rg, gsf),
-                        __fadd_rn(__fmul_rn((float)rh, hsf), l2f));
-      float e2 = a.e;
-      cpass = valid && !a.uncertain && __fsub_rn(a.g, e2) > mgs_up;
-      bool mpass = valid && (a.uncertain || __fadd_rn(a.g, e2) > mgs_dn);
-      float lower = cpass ? __fsub_rn(a.g, e2) : -CUDART_INF_F;
+  // pass 1 (PLAIN only): the best certified lower bound, and whether some threshold certainly passes
+  float M = -CUDART_INF_F;
+  bool certain_split = false;
+  const int passes = PLAIN ? 2 : 1;
+  for (int pass = 0; pass < passes; ++pass) {
+    const bool exact_pass = pass == passes - 1;
+    int64_t cg = cg0, ch = ch0;
+    for (int c0 = 0; c0 < P; c0 += 32) {
+      int k = c0 + lane;
+      int t = REV ? t_first - k : t_first + k;
+      bool act = k < P;
+      bool cand = act && !(SKIP && (t + off) == m.default_bin);
+      int64_t g = 0, h = 0;
+      if (cand && t >= 0) {
+        int64_t v = H.get(t);
+        g = unpack_g(v);
+        h = unpack_h(v);
+      }
+      int64_t pg = warp_incl_scan(g, lane) + cg;
+      int64_t ph = warp_incl_scan(h, lane) + ch;
+      cg = __shfl_sync(FULL, pg, 31);
+      ch = __shfl_sync(FULL, ph, 31);
+      // REV accumulates the right side, FWD the left side
+      int64_t lg = REV ? tg - pg : pg;
+      int64_t lh = REV ? th - ph : ph;
+      int64_t rg = tg - lg, rh = th - lh;
+      bool first = cand && ph >= X.first_x;
+      bool brk = first && ph >= X.brk_x;
+      unsigned bm = __ballot_sync(FULL, brk);
+      int stop_lane = bm ? __ffs(bm) - 1 : 32;
+      bool valid = first && !brk && lane < stop_lane;
+      bool exact = valid;
+      bool cpass = false;
+      if (PLAIN) {
+        Approx a{0.f, 0.f, true};
+        if (valid)
+          a = approx_from(__fmul_rn((float)lg, gsf), __fadd_rn(__fmul_rn((float)lh, hsf), l2f),
+                          __fmul_rn((float)rg, gsf), __fadd_rn(__fmul_rn((float)rh, hsf), l2f));
+        cpass = valid && !a.uncertain && __fsub_rn(a.g, a.e) > mgs_up;
+        bool mpass = valid && (a.uncertain || __fadd_rn(a.g, a.e) > mgs_dn);
+        if (!exact_pass) {
+          float lower = cpass ? __fsub_rn(a.g, a.e) : -CUDART_INF_F;
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) lower = fmaxf(lower, __shfl_xor_sync(FULL, lower, o));
-      float thr = fmaxf(lower, __double2float_rd(r.gain));
-      bool contender = mpass && (a.uncertain || __fadd_rn(a.g, e2) >= thr);
-      bool any_cpass = __any_sync(FULL, cpass);
-      bool unsure = mpass && !cpass && !any_cpass && !r.splittable;
-      exact = contender || unsure;
+          for (int o = 16; o > 0; o >>= 1) lower = fmaxf(lower, __shfl_xor_sync(FULL, lower, o));
+          M = fmaxf(M, lower);
+          if (__any_sync(FULL, cpass)) certain_split = true;
+          if (bm) break;
+          continue;
+        }
+        bool contender = mpass && (a.uncertain || __fadd_rn(a.g, a.e) >= M);
+        bool unsure = mpass && !cpass && !certain_split && !r.splittable;
+        exact = contender || unsure;
+        if (certain_split) r.splittable = 1;
+      }
+      double gain = -CUDART_INF;
+      if (__any_sync(FULL, exact)) {
+        if (exact) {
+          double slh = (double)lh * hs, srh = (double)rh * hs;
+          int32_t lc = PLAIN ? 0 : round_int((double)lh * cnt_factor);
+          int32_t rc = PLAIN ? 0 : round_int((double)rh * cnt_factor);
+          gain = split_gains(p, (double)lg * gs, slh + BK_EPS, (double)rg * gs, srh + BK_EPS, lc, rc, parent);
+        }
+      }
+      bool passed = exact ? !(gain <= mgs) : cpass;
+      if (__any_sync(FULL, valid && passed)) r.splittable = 1;
+      double bg;
+      int bl = warp_best_lane(exact && passed && gain > r.gain, gain, lane, &bg);
+      if (bl < 32) {
+        r.gain = bg;
+        r.th = __shfl_sync(FULL, REV ? (t - 1 + off) : (t + off), bl);
+        r.lg = __shfl_sync(FULL, lg, bl);
+        r.lh = __shfl_sync(FULL, lh, bl);
+      }
+      if (bm) break;
     }
-    double gain = -CUDART_INF;
-    if (exact) {
-      double slh = (double)lh * hs, srh = (double)rh * hs;
-      int32_t lc = PLAIN ? 0 : round_int((double)lh * cnt_factor);
-      int32_t rc = PLAIN ? 0 : round_int((double)rh * cnt_factor);
-      gain = split_gains(p, (double)lg * gs, slh + BK_EPS, (double)rg * gs, srh + BK_EPS, lc, rc, parent);
-    }
-    bool pass = exact ? !(gain <= mgs) : cpass;
-    if (__any_sync(FULL, valid && pass)) r.splittable = 1;
-    double bg;
-    int bl = warp_best_lane(exact && pass && gain > r.gain, gain, lane, &bg);
-    if (bl < 32) {
-      r.gain = bg;
-      r.th = __shfl_sync(FULL, REV ? (t - 1 + off) : (t + off), bl);
-      r.lg = __shfl_sync(FULL, lg, bl);
-      r.lh = __shfl_sync(FULL, lh, bl);
-    }
-    if (bm) break;
   }
   return r;
 }
@@ -524,7 +563,7 @@ __device__ void decide_body(const Job& J, const Params& p, const DevFeature* fea
 // derives the larger leaf as parent minus the fixed smaller histogram (serial.rs:1407-1437,
 // :1218-1242) — it recomputes the fixed most-frequent bin itself with the same reduction, so the
 // two warps never wait for each other. The last CTA to finish runs the fold / arg-max (k_decide).
-template <bool PLAIN>
+template <bool PLAIN, bool QUANT>
 __global__ void __launch_bounds__(64) k_search(const Job* __restrict__ jobs, Params p,
                                                const DevFeature* __restrict__ feats) {
   const Job& J = jobs[blockIdx.z];
@@ -542,7 +581,7 @@ __global__ void __launch_bounds__(64) k_search(const Job* __restrict__ jobs, Par
     const LeafSum S = J.leaf_sum[st->smaller_leaf];
     const LeafSum ls = side ? J.leaf_sum[leaf] : S;
     const double parent = parent_output_of(p, st, ls);
-    if (p.quant) {
+    if (QUANT) {
       int64_t* pool = reinterpret_cast<int64_t*>(J.pool);
       IntHist HS{pool + (size_t)st->smaller_slot * slot_stride + feat_off};
       int64_t fixed = 0;
@@ -621,50 +660,6 @@ __global__ void __launch_bounds__(64) k_search(const Job* __restrict__ jobs, Par
 // ---------------------------------------------------------------------------------------------
 // k_decide
 // ---------------------------------------------------------------------------------------------
-
-// The route of one stored bin for a numerical split of a single-feature dense group
-// (data_partition.rs:299-410 with group_view :25-40: min_bin 1, max_bin gbins - 1,
-// use_min_bin false). 1 = left.
-__device__ uint8_t route_bin(const DevFeature& m, uint32_t threshold, bool default_left, uint32_t bin) {
-  const uint32_t min_bin = 1, max_bin = (uint32_t)m.gbins - 1;
-  const uint32_t default_bin = (uint32_t)m.default_bin, mfb = (uint32_t)m.mfb;
-  bool miss_zero = false, miss_na = false, mfb_zero = false, mfb_na = false;
-  if (m.missing == 1) {
-    miss_zero = true;
-    mfb_zero = default_bin == mfb;
-  } else if (m.missing == 2) {
-    miss_na = true;
-    mfb_na = (max_bin == mfb + 1) && mfb > 0;
-  }
-  uint32_t th = threshold + min_bin;
-  uint32_t t_zero_bin = min_bin + default_bin;
-  if (mfb == 0) {
-    th -= 1;
-    t_zero_bin -= 1;
-  }
-  const bool default_route_left = mfb <= threshold;
-  const bool missing_default_left = (miss_zero || miss_na) && default_left;
-  const bool max_bin_left = max_bin <= th;
-  const bool either_mfb = (miss_na && mfb_na) || (miss_zero && mfb_zero);
-  bool left;
-  if (min_bin < max_bin) {
-    if ((miss_zero && !mfb_zero && bin == t_zero_bin) || (miss_na && !mfb_na && bin == max_bin))
-      left = missing_default_left;
-    else if (bin == 0)
-      left = either_mfb ? missing_default_left : default_route_left;
-    else
-      left = !(bin > th);
-  } else if (miss_zero && !mfb_zero && bin == t_zero_bin) {
-    left = missing_default_left;
-  } else if (bin != max_bin) {
-    left = either_mfb ? missing_default_left : default_route_left;
-  } else if (miss_na && !mfb_na) {
-    left = missing_default_left;
-  } else {
-    left = max_bin_left;
-  }
-  return left ? 1 : 0;
-}
 
 // Combine two (index, gain, real feature) candidates of a fold or an arg-max. `a` is the one
 // that comes first in the sequential order; `b` replaces it only when strictly better
@@ -807,10 +802,14 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
 
 void launch_search(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s) {
   dim3 grid((unsigned)ceil_div64(2 * p.F, 2), 1, num_jobs);
-  if (!p.use_l1 && !p.use_max && !p.use_smooth)
-    k_search<true><<<grid, 64, 0, s>>>(d_jobs, p, feats);
-  else
-    k_search<false><<<grid, 64, 0, s>>>(d_jobs, p, feats);
+  const bool plain = !p.use_l1 && !p.use_max && !p.use_smooth;
+  if (p.quant) {
+    if (plain) k_search<true, true><<<grid, 64, 0, s>>>(d_jobs, p, feats);
+    else k_search<false, true><<<grid, 64, 0, s>>>(d_jobs, p, feats);
+  } else {
+    if (plain) k_search<true, false><<<grid, 64, 0, s>>>(d_jobs, p, feats);
+    else k_search<false, false><<<grid, 64, 0, s>>>(d_jobs, p, feats);
+  }
 }
 
 

@@ -160,6 +160,24 @@ class BinnedDataset:
             list(ex.map(fill, range(len(features))))
         return cls(bins, features, ncol)
 
+    def bin_like(self, X, threads=8):
+        """Stored bins of new rows with this dataset's bin mappers (held-out / validation data,
+        io/dataset.rs:987-1003 from_dense_reference)."""
+        X = np.asarray(X)
+        lib = _lib.load()
+        n = X.shape[0]
+        bins = np.zeros((self.num_features, n), dtype=np.uint8)
+
+        def fill(j):
+            fi = self.features[j]
+            col = np.ascontiguousarray(X[:, fi.real], dtype=np.float64)
+            lib.bk_values_to_group_bins(col.ctypes.data, n, 1, fi.upper_bounds.ctypes.data, fi.num_bin,
+                                        fi.missing_type, fi.most_freq_bin, bins[j].ctypes.data)
+
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(fill, range(self.num_features)))
+        return bins
+
     def feature_array(self):
         """The ``bk_feature`` records of include/bkgpu.h, as a numpy structured array."""
         arr = np.zeros(self.num_features, dtype=FEATURE_DTYPE)

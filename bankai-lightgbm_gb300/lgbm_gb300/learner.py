@@ -52,7 +52,10 @@ class GpuTreeLearner:
         t = (ctypes.c_double * 3)()
         _lib.check(self.lib.bk_learner_last_timing(self.h, ctypes.byref(t, 0), ctypes.byref(t, 8),
                                                    ctypes.byref(t, 16)), "bk_learner_last_timing")
-        return {"total_ms": t[0], "hist_ms": t[1], "hist_bytes": t[2]}
+        ph = (ctypes.c_double * 2)()
+        _lib.check(self.lib.bk_learner_last_phase_timing(self.h, ctypes.byref(ph, 0), ctypes.byref(ph, 8)),
+                   "bk_learner_last_phase_timing")
+        return {"total_ms": t[0], "hist_ms": t[1], "hist_bytes": t[2], "search_ms": ph[0], "partition_ms": ph[1]}
 
     def stream(self):
         s = ctypes.c_void_p()
@@ -68,6 +71,22 @@ class GpuTreeLearner:
         _lib.check(self.lib.bk_learner_objective_loss(self.h, int(kind), int(score_ptr), int(label_ptr),
                                                       ctypes.byref(out)), "bk_learner_objective_loss")
         return out.value
+
+    def predict_add(self, tree, bins_ptr, num_rows, score_ptr):
+        """Adds `tree`'s output to a device score for device-resident binned rows
+        ([num_features][num_rows] uint8 stored bins made with this dataset's bin mappers)."""
+        import numpy as np
+        ni = max(tree.num_leaves - 1, 0)
+        lc = np.ascontiguousarray(tree.left_child[:ni], np.int32)
+        rc = np.ascontiguousarray(tree.right_child[:ni], np.int32)
+        sf = np.ascontiguousarray(tree.split_feature_inner[:ni], np.int32)
+        th = np.ascontiguousarray(tree.threshold_in_bin[:ni], np.uint32)
+        dt = np.ascontiguousarray(tree.decision_type[:ni], np.int8)
+        lv = np.ascontiguousarray(tree.leaf_value[:tree.num_leaves], np.float64)
+        _lib.check(self.lib.bk_learner_predict_add(self.h, tree.num_leaves, lc.ctypes.data, rc.ctypes.data,
+                                                   sf.ctypes.data, th.ctypes.data, dt.ctypes.data, lv.ctypes.data,
+                                                   int(bins_ptr), int(num_rows), int(score_ptr)),
+                   "bk_learner_predict_add")
 
     def gradient_buffers(self):
         g = ctypes.c_void_p()

