@@ -61,6 +61,16 @@ struct Params {
   int64_t n;
 };
 
+// Per-leaf constants of one searched leaf (FindBestThreshold's preamble, feature_histogram.rs:
+// 219-240 / 673-700): computed once per search, before it, by one CTA of the histogram launch.
+struct LeafConst {
+  double sum_g, sum_h, parent, mgs, cnt_factor;  // mgs = min_gain_shift
+  int64_t first_x, brk_x;  // quantized path: validity thresholds on the accumulated hessian
+  float mgs_up, mgs_dn;    // min_gain_shift rounded up / down to fp32
+  float gsf, hsf, l2f;     // fp32 copies of the gradient / hessian scales and lambda_l2
+  float _pad;
+};
+
 // Per-job control block, written and read only by kernels (the device-resident grow loop).
 struct JobState {
   int32_t stop, do_search, tree_leaves, disc_ok;
@@ -98,6 +108,7 @@ struct Job {
   Cand* cand;          // [2][F]
   double* cgain;       // [2][F] gain of cand[] (compact copy for the fold)
   uint8_t* csplit;     // [2][F] splittable flag of cand[]
+  LeafConst* lconst;   // [2]   constants of the smaller / larger leaf of the current search
   uint8_t* splittable; // [L][F]
   uint8_t* used;       // [F]
   bk_split* records;   // [L-1]

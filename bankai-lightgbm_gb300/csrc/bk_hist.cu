@@ -20,7 +20,10 @@
 // relative; the pool slot receives (double)hi + (double)lo via f64 global atomics. With a
 // constant hessian the hessian slot counts rows and is scaled by hessians[0] at the flush
 // (serial.rs:980-988), which is exact.
-#include "bk_common.cuh"
+//
+// The last CTA of tile 0 also computes the per-leaf constants of the search that follows
+// (bk_leaf.cuh) before its own rows.
+#include "bk_leaf.cuh"
 
 namespace bk {
 
@@ -57,21 +60,25 @@ __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blo
   return true;
 }
 
-// One warp's rows of a round: global loads of the 32-byte tile sectors and the packed values.
+// The rows of a warp's round are fetched in two stages, each one round ahead of its use: the row
+// index (a coalesced load of the leaf's index range, two rounds ahead) and then the row's 32-byte
+// tile sector and packed value (one round ahead), so no gather waits on an index load.
+__device__ __forceinline__ int32_t round_row(const Range& R, int64_t i) {
+  if (i >= R.r1) return -1;
+  return R.direct ? (int32_t)i : __ldg(R.idx + i);
+}
+
 struct RoundLoad {
   uint4 a, b;
   int32_t v;
 };
 
-__device__ __forceinline__ RoundLoad load_round_int(const Range& R, const uint8_t* tb, const int16_t* packed,
-                                                    int64_t base, int lane, bool wide) {
+__device__ __forceinline__ RoundLoad load_round_int(const uint8_t* tb, const int16_t* packed, int32_t row, bool wide) {
   RoundLoad L;
   L.a = make_uint4(0, 0, 0, 0);
   L.b = make_uint4(0, 0, 0, 0);
   L.v = 0;
-  int64_t i = base + lane;
-  if (i < R.r1) {
-    int64_t row = R.direct ? i : (int64_t)R.idx[i];
+  if (row >= 0) {
     const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * TILE);
     L.a = __ldg(src);
     L.b = __ldg(src + 1);
@@ -100,6 +107,7 @@ __global__ void __launch_bounds__(1024, 1)
                int flush_rounds) {
   extern __shared__ __align__(16) unsigned char smem[];
   const Job& J = jobs[blockIdx.z];
+  hist_leaf_constants(J, p);
   Range R;
   if (!cta_range(J, p, blocks_per_tile, &R)) return;
   const int B = p.B;
@@ -125,12 +133,17 @@ __global__ void __launch_bounds__(1024, 1)
   uint4* my_stage = stage + warp * 64;
   const uint8_t* sb = reinterpret_cast<const uint8_t*>(my_stage);
   int32_t* my_v = stage_v + warp * 32;
-  // software pipeline: the next round's rows are in flight while this round is added up
-  RoundLoad cur = load_round_int(R, tb, packed, R.r0 + (int64_t)warp * TILE, lane, WIDE);
+  // software pipeline: the next round's sectors and the round after's row indices are in flight
+  // while this round is added up
+  const int64_t first = R.r0 + (int64_t)warp * TILE + lane;
+  RoundLoad cur = load_round_int(tb, packed, round_row(R, first), WIDE);
+  int32_t row_nxt = round_row(R, first + per_round);
   int until_flush = flush_rounds;
   for (int64_t rd = 0; rd < rounds; ++rd) {
     const int64_t base = R.r0 + rd * per_round + (int64_t)warp * TILE;
-    RoundLoad nxt = load_round_int(R, tb, packed, base + per_round, lane, WIDE);
+    const int32_t row_nn = round_row(R, base + 2 * per_round + lane);
+    RoundLoad nxt = load_round_int(tb, packed, row_nxt, WIDE);
+    row_nxt = row_nn;
     if (base < R.r1) {
       my_stage[lane * 2] = cur.a;
       my_stage[lane * 2 + 1] = cur.b;
@@ -193,6 +206,7 @@ __global__ void __launch_bounds__(1024, 1)
     k_hist_float(const Job* __restrict__ jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile) {
   extern __shared__ __align__(16) unsigned char smem[];
   const Job& J = jobs[blockIdx.z];
+  hist_leaf_constants(J, p);
   Range R;
   if (!cta_range(J, p, blocks_per_tile, &R)) return;
   const int B = p.B;
@@ -221,22 +235,36 @@ __global__ void __launch_bounds__(1024, 1)
   const float* G = J.g;
   const float* H = J.h;
   const int64_t per_round = (int64_t)TILE * nwarps;
-  for (int64_t base = R.r0 + (int64_t)warp * TILE; base < R.r1; base += per_round) {
-    int64_t i = base + lane;
-    bool valid = i < R.r1;
-    uint4 a = make_uint4(0, 0, 0, 0), b = make_uint4(0, 0, 0, 0);
-    float2 v = make_float2(0.f, 0.f);
-    if (valid) {
-      int64_t row = R.direct ? i : (int64_t)R.idx[i];
+  // the same two-stage software pipeline as the integer kernel
+  auto load = [&](int32_t row, uint4& a, uint4& b, float2& v) {
+    a = make_uint4(0, 0, 0, 0);
+    b = make_uint4(0, 0, 0, 0);
+    v = make_float2(0.f, 0.f);
+    if (row >= 0) {
       const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * TILE);
       a = __ldg(src);
       b = __ldg(src + 1);
       v.x = G[row];
       if (!CONST_HESS) v.y = H[row];
     }
-    stage[(warp * 32 + lane) * 2] = a;
-    stage[(warp * 32 + lane) * 2 + 1] = b;
-    stage_v[warp * 32 + lane] = v;
+  };
+  const int64_t first = R.r0 + (int64_t)warp * TILE + lane;
+  uint4 ca, cb;
+  float2 cv;
+  load(round_row(R, first), ca, cb, cv);
+  int32_t row_nxt = round_row(R, first + per_round);
+  for (int64_t base = R.r0 + (int64_t)warp * TILE; base < R.r1; base += per_round) {
+    const int32_t row_nn = round_row(R, base + 2 * per_round + lane);
+    uint4 na, nb;
+    float2 nv;
+    load(row_nxt, na, nb, nv);
+    row_nxt = row_nn;
+    stage[(warp * 32 + lane) * 2] = ca;
+    stage[(warp * 32 + lane) * 2 + 1] = cb;
+    stage_v[warp * 32 + lane] = cv;
+    ca = na;
+    cb = nb;
+    cv = nv;
     __syncwarp();
     const uint8_t* sb = reinterpret_cast<const uint8_t*>(stage + warp * 64);
     const int jn = (int)min((int64_t)32, R.r1 - base);  // warp-uniform; padding lanes add nothing

@@ -1,0 +1,115 @@
+// Per-leaf constants of a split search: the preamble of FindBestThreshold / FindBestThresholdInt
+// (feature_histogram.rs:219-240, :673-700) that every feature of a leaf shares — the leaf's sums,
+// its parent output (serial.rs:1924-1935), min_gain_shift, the count factor and, on the quantized
+// path, the integer validity thresholds of the threshold scans. They are computed once per search
+// by one CTA of the histogram launch that precedes it, so the search warps start from them.
+#pragma once
+#include "bk_common.cuh"
+#include "bk_math.cuh"
+
+namespace bk {
+
+// Smallest x in [0, hi) with pred(x) (monotone false -> true), or hi; one warp, 32-ary search.
+template <typename Pred>
+__device__ int64_t warp_first_true(int64_t hi, int lane, Pred pred) {
+  int64_t lo = 0;
+  while (lo < hi) {
+    int64_t step = (hi - lo + 31) >> 5;  // hi > lo: a shift, not an int64 division
+    int64_t x = lo + (int64_t)lane * step;
+    bool t = x < hi && pred(x);
+    unsigned m = __ballot_sync(0xffffffffu, t);
+    if (m == 0) {
+      int64_t nlo = lo + 31 * step + 1;
+      lo = nlo < hi ? nlo : hi;
+    } else {
+      int k = __ffs(m) - 1;
+      hi = lo + (int64_t)k * step;
+      if (k > 0) lo = lo + (int64_t)(k - 1) * step + 1;
+    }
+  }
+  return lo;
+}
+
+// As warp_first_true, trying first the 32 values around `guess` (one warp-wide evaluation) and
+// falling back to the full search when the answer lies outside that window.
+template <typename Pred>
+__device__ int64_t warp_first_true_near(int64_t hi, int64_t guess, int lane, Pred pred) {
+  guess = guess < 0 ? 0 : (guess > hi ? hi : guess);
+  const int64_t x = guess - 15 + lane;
+  const bool t = x >= hi ? true : (x < 0 ? false : pred(x));
+  const unsigned m = __ballot_sync(0xffffffffu, t);
+  if (m != 0u && (m & 1u) == 0u) return guess - 15 + (__ffs(m) - 1);  // false -> true inside
+  if (m != 0u && guess - 15 <= 0) return 0;  // everything from 0 on is true
+  return warp_first_true(hi, lane, pred);
+}
+
+// Integer thresholds of a leaf (feature-independent): for an accumulated side with integer hessian
+// x, the reference's `count >= min_data && hess >= min_hessian` test (counts estimated as
+// round_int(x * cnt_factor), feature_histogram.rs:927-940) is monotone in x, so it is x >= first_x;
+// and the `break` test on the other side is x >= brk_x.
+__device__ __forceinline__ void int_thresholds(const Params& p, int64_t th, double hs, int32_t num_data, int lane,
+                                               int64_t* first_x, int64_t* brk_x) {
+  const double cf = (double)num_data / (double)th;
+  const int64_t hi = th + 1;
+  // fp32 guesses of the transitions; the exact f64 predicates decide
+  const float fth = (float)th, fnd = (float)num_data;
+  const int64_t g_cnt = (int64_t)((float)((double)p.min_data - 0.5) * fth / fnd);
+  const int64_t g_brk = (int64_t)((float)((double)(num_data - p.min_data) + 0.5) * fth / fnd);
+  const float fh = (float)hs;
+  const int64_t g_hess = fh > 0.f ? (int64_t)fminf((float)p.min_hess / fh, 4.0e18f) : hi;
+  int64_t cnt_ok = warp_first_true_near(hi, g_cnt, lane,
+                                        [&](int64_t x) { return round_int((double)x * cf) >= p.min_data; });
+  int64_t hess_ok = warp_first_true_near(hi, g_hess, lane, [&](int64_t x) { return (double)x * hs >= p.min_hess; });
+  int64_t cnt_brk = warp_first_true_near(
+      hi, g_brk, lane, [&](int64_t x) { return round_int((double)x * cf) > num_data - p.min_data; });
+  *first_x = cnt_ok > hess_ok ? cnt_ok : hess_ok;
+  int64_t hess_brk = th - hess_ok + 1;  // (th - x) * hs < min_hess  <=>  th - x < hess_ok
+  *brk_x = cnt_brk < hess_brk ? cnt_brk : hess_brk;
+}
+
+__device__ __forceinline__ double parent_output_of(const Params& p, const JobState* st, const LeafSum& ls) {
+  // serial.rs:1924-1935 (GetParentOutput)
+  if (st->tree_leaves == 1) return leaf_output_root(p, ls.sg, ls.sh, ls.num_data);
+  return ls.weight;
+}
+
+// One warp: the constants of side `side` (0 = smaller leaf, 1 = larger leaf) of the coming search.
+__device__ __forceinline__ void compute_leaf_const(const Job& J, const Params& p, const JobState* st, int side,
+                                                   int lane) {
+  const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
+  if (leaf < 0) return;
+  const LeafSum ls = J.leaf_sum[leaf];
+  LeafConst c;
+  c.first_x = c.brk_x = 0;
+  if (p.quant) {
+    const int64_t tg = ls.int_sum >> 32, th = ls.int_sum & 0xffffffffLL;
+    c.sum_g = (double)tg * st->gscale;
+    c.sum_h = (double)th * st->hscale;
+    c.cnt_factor = (double)ls.num_data / (double)th;
+    int_thresholds(p, th, st->hscale, ls.num_data, lane, &c.first_x, &c.brk_x);
+  } else {
+    c.sum_g = ls.sg;
+    c.sum_h = ls.sh + 2.0 * BK_EPS;
+    c.cnt_factor = (double)ls.num_data / c.sum_h;
+  }
+  c.parent = parent_output_of(p, st, ls);
+  c.mgs = leaf_gain(p, c.sum_g, c.sum_h, ls.num_data, c.parent) + p.min_gain;
+  c.mgs_up = __double2float_ru(c.mgs);
+  c.mgs_dn = __double2float_rd(c.mgs);
+  c.gsf = (float)st->gscale;
+  c.hsf = (float)st->hscale;
+  c.l2f = (float)p.l2;
+  c._pad = 0.f;
+  if (lane == 0) J.lconst[side] = c;
+}
+
+// Called by every thread of a histogram CTA before its row loop: the last CTA of tile 0 (idle for
+// leaves that do not need the whole grid) computes both sides' constants with its first two warps.
+__device__ __forceinline__ void hist_leaf_constants(const Job& J, const Params& p) {
+  if (blockIdx.x != gridDim.x - 1 || blockIdx.y != 0 || threadIdx.x >= 64) return;
+  const JobState* st = J.st;
+  if (st->stop || !st->do_search) return;
+  compute_leaf_const(J, p, st, (int)(threadIdx.x >> 5), (int)(threadIdx.x & 31));
+}
+
+}  // namespace bk

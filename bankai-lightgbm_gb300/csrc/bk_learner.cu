@@ -276,6 +276,17 @@ int bk_learner_create(const bk_feature* features, int32_t num_features, const ui
     return -1;
   }
   bool quant = c->use_quantized_grad && c->num_grad_quant_bins >= 2 && c->num_grad_quant_bins <= 127;
+  if (quant) {
+    // the device's integer histograms and prefix sums hold (grad << 32) + hess: every partial sum
+    // of a leaf's gradients must fit in 32 signed bits and of its hessians in 32 unsigned bits
+    const double max_g = c->num_grad_quant_bins / 2 + 1;
+    const double max_h = c->is_constant_hessian ? 1 : c->num_grad_quant_bins;
+    if ((double)num_data * max_g >= 2147483648.0 || (double)num_data * max_h >= 4294967296.0) {
+      set_error("quantized histograms of %lld rows with %d gradient bins overflow 32-bit sums",
+                (long long)num_data, c->num_grad_quant_bins);
+      return -1;
+    }
+  }
   bk_learner* L = new bk_learner();
   try {
     CK(cudaGetDevice(&L->device));
@@ -419,6 +430,7 @@ int bk_learner_create(const bk_feature* features, int32_t num_features, const ui
       J.cand = L->dalloc<Cand>(2 * (size_t)F);
       J.cgain = L->dalloc<double>(2 * (size_t)F);
       J.csplit = L->dalloc<uint8_t>(2 * (size_t)F);
+      J.lconst = L->dalloc<LeafConst>(2);
       J.splittable = L->dalloc<uint8_t>((size_t)Lv * F);
       J.used = L->dalloc<uint8_t>(F);
       J.records = L->dalloc<bk_split>(Lv);

@@ -1,24 +1,33 @@
 // FindBestSplitsFromHistograms (serial.rs:1322-1566, int: :1212-1300) and the grow-loop
 // bookkeeping kernels (serial.rs:578-628, :779-825, :1685-1876), GB300 form.
 //
-// k_search: one warp per (leaf, feature). It fixes the smaller leaf's most-frequent bin
-// (FixHistogram, serial.rs:2205-2238), derives the larger leaf by parent-minus-smaller
-// subtraction in place, then runs the reference's directional threshold scans
-// (FindBestThresholdSequentially[Int], feature_histogram.rs:363-663 / 839-1142) as warp-parallel
-// prefix scans over 32 thresholds at a time. The sequential scan's `break` (the first threshold
-// whose other side falls under min_data / min_hessian ends the scan) becomes "the first such
-// position in scan order and everything after it is excluded"; `current_gain > best_gain` becomes
-// a warp argmax with ties going to the earliest position in scan order. The quantized path's
-// prefix sums are exact integers, so its candidates are bit-identical to the reference's; the
-// float path's f64 prefix sums are associated differently (≈1e-16 relative).
+// k_search: one 256-thread CTA per (leaf side, feature), thread t owning local bin t (a feature
+// slice holds at most 255 bins). The CTA fixes the smaller leaf's most-frequent bin (FixHistogram,
+// serial.rs:2205-2238), derives the larger leaf's slice as parent minus the fixed smaller slice in
+// place (serial.rs:1407-1437, :1218-1242), and evaluates both directional threshold scans of the
+// reference (FindBestThresholdSequentially[Int], feature_histogram.rs:363-663 / 839-1142) at once,
+// thread t holding the reverse scan's position t and the forward scan's position t. The sequential
+// scan's `break` (the first threshold whose other side falls under min_data / min_hessian ends the
+// scan) becomes "the first such position in scan order and everything after it is excluded";
+// `current_gain > best_gain` becomes an arg-max with ties going to the earliest position in scan
+// order. Every reduction is a warp reduction plus one barrier.
 //
-// The last CTA of k_search folds the per-feature candidates of each searched leaf in feature
-// order with `better_than`, takes the arg-max leaf (split_info.rs:88-96), stops the tree when its
-// gain is <= 0, and builds the route table of the chosen split (data_partition.rs:299-410). The
-// post-split bookkeeping (bk_grow.cuh) runs in the last CTA of the partition scatter.
+// The quantized path scans the packed (grad << 32) + hess sums with one block prefix scan; the
+// reverse scan's sums are the total minus the prefix, exact in integers, so its candidates are
+// bit-identical to the reference's. The float path scans f64 prefix and suffix sums (associated
+// differently from the sequential scan, about 1e-16 relative).
+//
+// f64 is slow on this part, so it stays off the common path: the leaf constants the scans share
+// come precomputed from the histogram launch (bk_leaf.cuh), plain gains are filtered in fp32 with
+// a rigorous error bound, and every comparison of the fold and the arg-max runs on integer keys.
+// The last CTA of k_search folds the per-feature candidates of each searched leaf in feature order
+// with `better_than`, takes the arg-max leaf (split_info.rs:88-96), stops the tree when its gain is
+// <= 0, and builds the route table of the chosen split (data_partition.rs:299-410). The post-split
+// bookkeeping (bk_grow.cuh) runs in the last CTA of the partition scatter.
 #include <math_constants.h>
 
 #include "bk_grow.cuh"
+#include "bk_leaf.cuh"
 #include "bk_math.cuh"
 
 namespace bk {
@@ -26,6 +35,9 @@ namespace bk {
 namespace {
 
 constexpr unsigned FULL = 0xffffffffu;
+constexpr int kSearchThreads = 256;  // one thread per local bin
+constexpr int kSearchWarps = kSearchThreads / 32;
+constexpr long long kNoKey = (long long)0x8000000000000000ULL;
 
 template <typename T>
 __device__ __forceinline__ T warp_incl_scan(T v, int lane) {
@@ -37,6 +49,17 @@ __device__ __forceinline__ T warp_incl_scan(T v, int lane) {
   return v;
 }
 
+// Inclusive scan towards lower lanes: lane l gets the sum over lanes l .. 31.
+template <typename T>
+__device__ __forceinline__ T warp_incl_scan_down(T v, int lane) {
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    T u = __shfl_down_sync(FULL, v, o);
+    if (lane + o < 32) v += u;
+  }
+  return v;
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T v) {
 #pragma unroll
@@ -44,53 +67,44 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-struct DirBest {
-  int splittable;
-  double gain;      // best gain of this direction (-inf when none)
-  int32_t th, lc;
-  double slg, slh;  // float path
-  int64_t lg, lh;   // int path
-};
-
-// Accessors of one feature's slice in a pool slot: local bin t lives at group bin t + 1.
-struct FloatHist {
-  double2* base;  // entry of group bin 0 of this feature
-  __device__ double2 get(int t) const { return base[(size_t)(t + 1) * TILE]; }
-};
-struct IntHist {
-  int64_t* base;
-  __device__ int64_t get(int t) const { return base[(size_t)(t + 1) * TILE]; }
-};
+__device__ __forceinline__ long long warp_max64(long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long y = __shfl_xor_sync(FULL, x, o);
+    x = y > x ? y : x;
+  }
+  return x;
+}
 
 __device__ __forceinline__ int64_t unpack_g(int64_t pk) { return pk >> 32; }
 __device__ __forceinline__ int64_t unpack_h(int64_t pk) { return pk & 0xffffffffLL; }
 
-// Warp arg-max over lanes whose candidate beats `cur`; ties go to the lowest lane.
-__device__ __forceinline__ int warp_best_lane(bool better, double gain, int lane, double* out_gain) {
-  double bg = better ? gain : -CUDART_INF;
-  int bl = better ? lane : 32;
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    double og = __shfl_xor_sync(FULL, bg, o);
-    int ol = __shfl_xor_sync(FULL, bl, o);
-    if (og > bg || (og == bg && ol < bl)) {
-      bg = og;
-      bl = ol;
-    }
-  }
-  *out_gain = bg;
-  return bl;
+// Order-preserving integer keys of non-NaN floats and doubles (negative zero counts as zero),
+// computed with integer operations only.
+__device__ __forceinline__ int32_t float_key(float x) {
+  int32_t b = __float_as_int(x);
+  if (b == (int32_t)0x80000000) b = 0;
+  return b ^ ((b >> 31) & 0x7fffffff);
+}
+__device__ __forceinline__ long long dkey(double x) {
+  long long b = __double_as_longlong(x);
+  if (b == kNoKey) b = 0;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool dnan(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL;
 }
 
 // ---- fp32 prefilter of the plain split gain (no L1 / max_delta_step / path_smooth) ----
-// The reference evaluates gl^2/(hl+l2) + gr^2/(hr+l2) in f64 for every threshold; GB300 runs f64 at
-// a small fraction of its fp32 rate. Each candidate is first evaluated in fp32 together with a
-// rigorous bound E on |fp32 - f64| (the inputs' conversion, the squares, the sums and the division
-// add up to about 14 units of 2^-24 relative to the non-negative result, the fp32 comparisons
-// against E one more; E uses 48). Only the
-// candidates that can still be the best (fp32 + E >= the best lower bound so far) or whose
-// pass/fail against min_gain_shift is uncertain are evaluated in f64, so the chosen split, its
-// gain and the splittable flag are exactly the reference's.
+// The reference evaluates gl^2/(hl+l2) + gr^2/(hr+l2) in f64 for every threshold. Each candidate is
+// first evaluated in fp32 together with a rigorous bound E on |fp32 - f64|: the inputs'
+// conversions (about 2 units of 2^-24 each), the squares, the divisions (__fdividef: at most 2 ulp
+// for divisors in [2^-126, 2^126]) and the sum add up to about 9 units of 2^-24 relative to the
+// non-negative result, the fp32 comparisons against E one more; E uses 48. Only the candidates
+// that can still be the best (fp32 + E >= the best certified lower bound of their direction) or,
+// while no candidate certainly passes, whose pass / fail against min_gain_shift is uncertain are
+// evaluated in f64, so the chosen split, its gain and the splittable flag are exactly the
+// reference's.
 constexpr float kPrefilterRel = 48.0f * 5.9604645e-08f;
 
 struct Approx {
@@ -100,330 +114,37 @@ struct Approx {
 
 __device__ __forceinline__ Approx approx_from(float xl, float yl, float xr, float yr) {
   Approx a;
-  float tl = __fdiv_rn(__fmul_rn(xl, xl), yl);
-  float tr = __fdiv_rn(__fmul_rn(xr, xr), yr);
+  float tl = __fdividef(__fmul_rn(xl, xl), yl);
+  float tr = __fdividef(__fmul_rn(xr, xr), yr);
   a.g = __fadd_rn(tl, tr);
   a.e = __fadd_rn(__fmul_rn(kPrefilterRel, a.g), 1e-30f);
-  // non-finite values, tiny denominators (where the reference's +kEpsilon matters) and huge
-  // numerators go to f64
-  a.uncertain = !(yl >= 1e-6f) || !(yr >= 1e-6f) || !(a.g < 1e30f) || isnan(a.g);
+  // non-finite values, denominators outside [1e-6, 1e30] (where the reference's +kEpsilon matters
+  // or the fast division leaves its accuracy range) and huge results go to f64
+  a.uncertain = !(yl >= 1e-6f) || !(yr >= 1e-6f) || !(yl <= 1e30f) || !(yr <= 1e30f) || !(a.g < 1e30f) ||
+                isnan(a.g);
   return a;
 }
 
-// Smallest x in [0, hi) with pred(x) (monotone false -> true), or hi; one warp, 32-ary search.
-template <typename Pred>
-__device__ int64_t warp_first_true(int64_t hi, int lane, Pred pred) {
-  int64_t lo = 0;
-  while (lo < hi) {
-    int64_t step = (hi - lo + 31) / 32;
-    int64_t x = lo + (int64_t)lane * step;
-    bool t = x < hi && pred(x);
-    unsigned m = __ballot_sync(FULL, t);
-    if (m == 0) {
-      int64_t nlo = lo + 31 * step + 1;
-      lo = nlo < hi ? nlo : hi;
-    } else {
-      int k = __ffs(m) - 1;
-      hi = lo + (int64_t)k * step;
-      if (k > 0) lo = lo + (int64_t)(k - 1) * step + 1;
-    }
-  }
-  return lo;
+// The quantized sums fit in 32 bits (signed gradients, unsigned hessians), so the conversions are
+// single 32-bit ones.
+__device__ __forceinline__ Approx approx_int(int64_t lg, int64_t lh, int64_t tg, int64_t th, float gsf, float hsf,
+                                             float l2f) {
+  const int64_t rg = tg - lg, rh = th - lh;
+  return approx_from(__fmul_rn((float)(int32_t)lg, gsf), __fadd_rn(__fmul_rn((float)(uint32_t)lh, hsf), l2f),
+                     __fmul_rn((float)(int32_t)rg, gsf), __fadd_rn(__fmul_rn((float)(uint32_t)rh, hsf), l2f));
 }
 
-// FindBestThresholdSequentially (float), feature_histogram.rs:363-663.
-template <bool REV, bool PLAIN>
-__device__ DirBest scan_float(const Params& p, const DevFeature& m, const FloatHist& H, bool SKIP, bool NA,
-                              double sum_g, double sum_h, int32_t num_data, double mgs, double parent, int lane) {
-  DirBest r;
-  r.splittable = 0;
-  r.gain = -CUDART_INF;
-  r.th = m.num_bin;
-  r.lc = 0;
-  r.slg = CUDART_NAN;
-  r.slh = CUDART_NAN;
-  r.lg = r.lh = 0;
-  const double cnt_factor = (double)num_data / sum_h;
-  const int off = m.offset;
-  const float l2f = (float)p.l2;
-  const float mgs_up = __double2float_ru(mgs), mgs_dn = __double2float_rd(mgs);
-  double cg, ch;
-  int32_t cc;
-  int t_first, P;
-  if (REV) {
-    t_first = m.num_bin - 1 - off - (NA ? 1 : 0);
-    int t_end = 1 - off;
-    P = t_first - t_end + 1;
-    cg = 0.0;
-    ch = BK_EPS;
-    cc = 0;
-  } else {
-    int t_end = m.num_bin - 2 - off;
-    if (NA && off == 1) {
-      // left starts as everything outside the slice (the most-frequent bin 0)
-      double pg = 0.0, ph = 0.0;
-      int32_t pc = 0;
-      for (int i = lane; i < m.num_bin - off; i += 32) {
-        double2 v = H.get(i);
-        pg += v.x;
-        ph += v.y;
-        pc += round_int(v.y * cnt_factor);
-      }
-      pg = warp_sum(pg);
-      ph = warp_sum(ph);
-      pc = warp_sum(pc);
-      cg = sum_g - pg;
-      ch = (sum_h - BK_EPS) - ph;
-      cc = num_data - pc;
-      t_first = -1;
-    } else {
-      cg = 0.0;
-      ch = BK_EPS;
-      cc = 0;
-      t_first = 0;
-    }
-    P = t_end - t_first + 1;
-  }
-  for (int c0 = 0; c0 < P; c0 += 32) {
-    int k = c0 + lane;
-    int t = REV ? t_first - k : t_first + k;
-    bool act = k < P;
-    bool cand = act && !(SKIP && (t + off) == m.default_bin);
-    double g = 0.0, h = 0.0;
-    int32_t c = 0;
-    if (cand && t >= 0) {
-      double2 v = H.get(t);
-      g = v.x;
-      h = v.y;
-      c = round_int(h * cnt_factor);
-    }
-    double pg = warp_incl_scan(g, lane) + cg;
-    double ph = warp_incl_scan(h, lane) + ch;
-    int32_t pc = warp_incl_scan(c, lane) + cc;
-    cg = __shfl_sync(FULL, pg, 31);
-    ch = __shfl_sync(FULL, ph, 31);
-    cc = __shfl_sync(FULL, pc, 31);
-    bool first, brk;
-    double slg, slh, srg, srh;
-    int32_t lc, rc;
-    if (REV) {
-      srg = pg;
-      srh = ph;
-      rc = pc;
-      first = cand && !(rc < p.min_data || srh < p.min_hess);
-      lc = num_data - rc;
-      slh = sum_h - srh;
-      brk = first && (lc < p.min_data || slh < p.min_hess);
-      slg = sum_g - srg;
-    } else {
-      slg = pg;
-      slh = ph;
-      lc = pc;
-      first = cand && !(lc < p.min_data || slh < p.min_hess);
-      rc = num_data - lc;
-      srh = sum_h - slh;
-      brk = first && (rc < p.min_data || srh < p.min_hess);
-      srg = sum_g - slg;
-    }
-    unsigned bm = __ballot_sync(FULL, brk);
-    int stop_lane = bm ? __ffs(bm) - 1 : 32;
-    bool valid = first && !brk && lane < stop_lane;
-    bool exact = valid, cpass = false;
-    if (PLAIN) {
-      Approx a{0.f, 0.f, true};
-      if (valid) a = approx_from((float)slg, __fadd_rn((float)slh, l2f), (float)srg, __fadd_rn((float)srh, l2f));
-      float e2 = a.e;
-      cpass = valid && !a.uncertain && __fsub_rn(a.g, e2) > mgs_up;
-      bool mpass = valid && (a.uncertain || __fadd_rn(a.g, e2) > mgs_dn);
-      float lower = cpass ? __fsub_rn(a.g, e2) : -CUDART_INF_F;
-#pragma unroll
-      for (int o = 16; o > 0; o >>= 1) lower = fmaxf(lower, __shfl_xor_sync(FULL, lower, o));
-      float thr = fmaxf(lower, __double2float_rd(r.gain));
-      bool contender = mpass && (a.uncertain || __fadd_rn(a.g, e2) >= thr);
-      bool any_cpass = __any_sync(FULL, cpass);
-      bool unsure = mpass && !cpass && !any_cpass && !r.splittable;
-      exact = contender || unsure;
-    }
-    double gain = exact ? split_gains(p, slg, slh, srg, srh, lc, rc, parent) : -CUDART_INF;
-    bool pass = exact ? !(gain <= mgs) : cpass;
-    if (__any_sync(FULL, valid && pass)) r.splittable = 1;
-    double bg;
-    int bl = warp_best_lane(exact && pass && gain > r.gain, gain, lane, &bg);
-    if (bl < 32) {
-      r.gain = bg;
-      r.th = __shfl_sync(FULL, REV ? (t - 1 + off) : (t + off), bl);
-      r.lc = __shfl_sync(FULL, lc, bl);
-      r.slg = __shfl_sync(FULL, slg, bl);
-      r.slh = __shfl_sync(FULL, slh, bl);
-    }
-    if (bm) break;
-  }
-  return r;
-}
-
-// As warp_first_true, trying first the 32 values around `guess` (one warp-wide evaluation) and
-// falling back to the full search when the answer lies outside that window.
-template <typename Pred>
-__device__ int64_t warp_first_true_near(int64_t hi, int64_t guess, int lane, Pred pred) {
-  guess = guess < 0 ? 0 : (guess > hi ? hi : guess);
-  const int64_t x = guess - 15 + lane;
-  const bool t = x >= hi ? true : (x < 0 ? false : pred(x));
-  const unsigned m = __ballot_sync(FULL, t);
-  if (m != 0u && (m & 1u) == 0u) return guess - 15 + (__ffs(m) - 1);  // false -> true inside
-  if (m != 0u && guess - 15 <= 0) return 0;  // everything from 0 on is true
-  return warp_first_true(hi, lane, pred);
-}
-
-// Integer thresholds of a leaf (feature-independent): for an accumulated side with integer hessian
-// x, the reference's `count >= min_data && hess >= min_hessian` test (counts estimated as
-// round_int(x * cnt_factor), feature_histogram.rs:927-940) is monotone in x, so it is x >= first_x;
-// and the `break` test on the other side is x >= brk_x.
-struct IntThresholds {
-  int64_t first_x, brk_x;
-};
-
-__device__ IntThresholds int_thresholds(const Params& p, int64_t th, double hs, int32_t num_data, int lane) {
-  const double cf = (double)num_data / (double)th;
-  const int64_t hi = th + 1;
-  // fp32 guesses of the transitions; the exact f64 predicates decide
-  const float fth = (float)th, fnd = (float)num_data;
-  const int64_t g_cnt = (int64_t)((float)((double)p.min_data - 0.5) * fth / fnd);
-  const int64_t g_brk = (int64_t)((float)((double)(num_data - p.min_data) + 0.5) * fth / fnd);
-  const float fh = (float)hs;
-  const int64_t g_hess = fh > 0.f ? (int64_t)fminf((float)p.min_hess / fh, 4.0e18f) : hi;
-  int64_t cnt_ok = warp_first_true_near(hi, g_cnt, lane,
-                                        [&](int64_t x) { return round_int((double)x * cf) >= p.min_data; });
-  int64_t hess_ok = warp_first_true_near(hi, g_hess, lane, [&](int64_t x) { return (double)x * hs >= p.min_hess; });
-  int64_t cnt_brk = warp_first_true_near(
-      hi, g_brk, lane, [&](int64_t x) { return round_int((double)x * cf) > num_data - p.min_data; });
-  IntThresholds r;
-  r.first_x = cnt_ok > hess_ok ? cnt_ok : hess_ok;
-  int64_t hess_brk = th - hess_ok + 1;  // (th - x) * hs < min_hess  <=>  th - x < hess_ok
-  r.brk_x = cnt_brk < hess_brk ? cnt_brk : hess_brk;
-  return r;
-}
-
-// FindBestThresholdSequentiallyInt, feature_histogram.rs:839-1142. With PLAIN gains the scan
-// runs twice over the (cheap, exact) integer prefix sums: pass 1 evaluates every threshold in
-// fp32 and finds the best certified lower bound M; pass 2 evaluates in f64 only the thresholds
-// whose upper bound reaches M (plus, while the splittable flag is still undecided, those whose
-// pass / fail is uncertain), so most 32-threshold chunks take no f64 instruction at all.
-template <bool REV, bool PLAIN>
-__device__ DirBest scan_int(const Params& p, const DevFeature& m, const IntHist& H, bool SKIP, bool NA, int64_t tg,
-                            int64_t th, double gs, double hs, int32_t num_data, double mgs, double parent,
-                            const IntThresholds& X, int lane) {
-  DirBest r;
-  r.splittable = 0;
-  r.gain = -CUDART_INF;
-  r.th = m.num_bin;
-  r.lc = 0;
-  r.slg = r.slh = 0.0;
-  r.lg = r.lh = 0;
-  const double cnt_factor = (double)num_data / (double)th;
-  const int off = m.offset;
-  const float gsf = (float)gs, hsf = (float)hs, l2f = (float)p.l2;
-  const float mgs_up = __double2float_ru(mgs), mgs_dn = __double2float_rd(mgs);
-  int64_t cg0, ch0;
-  int t_first, P;
-  if (REV) {
-    t_first = m.num_bin - 1 - off - (NA ? 1 : 0);
-    P = t_first - (1 - off) + 1;
-    cg0 = ch0 = 0;
-  } else {
-    int t_end = m.num_bin - 2 - off;
-    if (NA && off == 1) {
-      int64_t pg = 0, ph = 0;
-      for (int i = lane; i < m.num_bin - off; i += 32) {
-        int64_t v = H.get(i);
-        pg += unpack_g(v);
-        ph += unpack_h(v);
-      }
-      cg0 = tg - warp_sum(pg);
-      ch0 = th - warp_sum(ph);
-      t_first = -1;
-    } else {
-      cg0 = ch0 = 0;
-      t_first = 0;
-    }
-    P = t_end - t_first + 1;
-  }
-  // pass 1 (PLAIN only): the best certified lower bound, and whether some threshold certainly passes
-  float M = -CUDART_INF_F;
-  bool certain_split = false;
-  const int passes = PLAIN ? 2 : 1;
-  for (int pass = 0; pass < passes; ++pass) {
-    const bool exact_pass = pass == passes - 1;
-    int64_t cg = cg0, ch = ch0;
-    for (int c0 = 0; c0 < P; c0 += 32) {
-      int k = c0 + lane;
-      int t = REV ? t_first - k : t_first + k;
-      bool act = k < P;
-      bool cand = act && !(SKIP && (t + off) == m.default_bin);
-      int64_t g = 0, h = 0;
-      if (cand && t >= 0) {
-        int64_t v = H.get(t);
-        g = unpack_g(v);
-        h = unpack_h(v);
-      }
-      int64_t pg = warp_incl_scan(g, lane) + cg;
-      int64_t ph = warp_incl_scan(h, lane) + ch;
-      cg = __shfl_sync(FULL, pg, 31);
-      ch = __shfl_sync(FULL, ph, 31);
-      // REV accumulates the right side, FWD the left side
-      int64_t lg = REV ? tg - pg : pg;
-      int64_t lh = REV ? th - ph : ph;
-      int64_t rg = tg - lg, rh = th - lh;
-      bool first = cand && ph >= X.first_x;
-      bool brk = first && ph >= X.brk_x;
-      unsigned bm = __ballot_sync(FULL, brk);
-      int stop_lane = bm ? __ffs(bm) - 1 : 32;
-      bool valid = first && !brk && lane < stop_lane;
-      bool exact = valid;
-      bool cpass = false;
-      if (PLAIN) {
-        Approx a{0.f, 0.f, true};
-        if (valid)
-          a = approx_from(__fmul_rn((float)lg, gsf), __fadd_rn(__fmul_rn((float)lh, hsf), l2f),
-                          __fmul_rn((float)rg, gsf), __fadd_rn(__fmul_rn((float)rh, hsf), l2f));
-        cpass = valid && !a.uncertain && __fsub_rn(a.g, a.e) > mgs_up;
-        bool mpass = valid && (a.uncertain || __fadd_rn(a.g, a.e) > mgs_dn);
-        if (!exact_pass) {
-          float lower = cpass ? __fsub_rn(a.g, a.e) : -CUDART_INF_F;
-#pragma unroll
-          for (int o = 16; o > 0; o >>= 1) lower = fmaxf(lower, __shfl_xor_sync(FULL, lower, o));
-          M = fmaxf(M, lower);
-          if (__any_sync(FULL, cpass)) certain_split = true;
-          if (bm) break;
-          continue;
-        }
-        bool contender = mpass && (a.uncertain || __fadd_rn(a.g, a.e) >= M);
-        bool unsure = mpass && !cpass && !certain_split && !r.splittable;
-        exact = contender || unsure;
-        if (certain_split) r.splittable = 1;
-      }
-      double gain = -CUDART_INF;
-      if (__any_sync(FULL, exact)) {
-        if (exact) {
-          double slh = (double)lh * hs, srh = (double)rh * hs;
-          int32_t lc = PLAIN ? 0 : round_int((double)lh * cnt_factor);
-          int32_t rc = PLAIN ? 0 : round_int((double)rh * cnt_factor);
-          gain = split_gains(p, (double)lg * gs, slh + BK_EPS, (double)rg * gs, srh + BK_EPS, lc, rc, parent);
-        }
-      }
-      bool passed = exact ? !(gain <= mgs) : cpass;
-      if (__any_sync(FULL, valid && passed)) r.splittable = 1;
-      double bg;
-      int bl = warp_best_lane(exact && passed && gain > r.gain, gain, lane, &bg);
-      if (bl < 32) {
-        r.gain = bg;
-        r.th = __shfl_sync(FULL, REV ? (t - 1 + off) : (t + off), bl);
-        r.lg = __shfl_sync(FULL, lg, bl);
-        r.lh = __shfl_sync(FULL, lh, bl);
-      }
-      if (bm) break;
-    }
-  }
-  return r;
+// GetSplitGains of one integer threshold (feature_histogram.rs:878-925: the hessians get
+// kEpsilon added, counts are round_int(hess * cnt_factor)).
+__device__ __forceinline__ double int_split_gain(const Params& p, int64_t lg, int64_t lh, int64_t tg, int64_t th,
+                                                 double gs, double hs, double cnt_factor, double parent, bool plain) {
+  // the sums fit in 32 bits (signed gradients, unsigned hessians): 32-bit conversions, exact
+  const int64_t rg = tg - lg, rh = th - lh;
+  const double slh = (double)(uint32_t)lh * hs, srh = (double)(uint32_t)rh * hs;
+  const int32_t lc = plain ? 0 : round_int((double)(uint32_t)lh * cnt_factor);
+  const int32_t rc = plain ? 0 : round_int((double)(uint32_t)rh * cnt_factor);
+  return split_gains(p, (double)(int32_t)lg * gs, slh + BK_EPS, (double)(int32_t)rg * gs, srh + BK_EPS, lc, rc,
+                     parent);
 }
 
 __device__ void cand_reset(Cand* c, int32_t real, int32_t inner) {
@@ -439,239 +160,741 @@ __device__ void cand_reset(Cand* c, int32_t real, int32_t inner) {
   c->splittable = 0;
 }
 
-// FindBestThreshold (float) for one leaf: feature_histogram.rs:219-357.
-template <bool PLAIN>
-__device__ void search_leaf_float(const Params& p, const DevFeature& m, const FloatHist& H, const LeafSum& ls,
-                                  double parent, int lane, Cand* out, double* out_gain, uint8_t* out_split,
-                                  int32_t f) {
-  const double sum_g = ls.sg;
-  const double sum_h = ls.sh + 2.0 * BK_EPS;
-  const int32_t num_data = ls.num_data;
-  double gain_shift = leaf_gain(p, sum_g, sum_h, num_data, parent);
-  double mgs = gain_shift + p.min_gain;
-  DirBest d[2];
-  int nd;
-  if (m.num_bin > 2 && m.missing != 0) {
-    bool skip = m.missing == 1, na = m.missing == 2;
-    d[0] = scan_float<true, PLAIN>(p, m, H, skip, na, sum_g, sum_h, num_data, mgs, parent, lane);
-    d[1] = scan_float<false, PLAIN>(p, m, H, skip, na, sum_g, sum_h, num_data, mgs, parent, lane);
-    nd = 2;
-  } else {
-    d[0] = scan_float<true, PLAIN>(p, m, H, false, false, sum_g, sum_h, num_data, mgs, parent, lane);
-    nd = 1;
+// Direction geometry of FindBestThreshold[Int] (feature_histogram.rs:219-357, :673-830): direction
+// 0 is the reverse scan (right side accumulates, default left, positions t = tf_r down to 1 - off),
+// direction 1 the forward scan (left side accumulates, positions t = -1 or 0 up to t_end).
+struct ScanGeom {
+  bool two, skip, fwd_rest;
+  int off, tf_r, t_end;
+};
+
+__device__ __forceinline__ ScanGeom scan_geom(const DevFeature& m) {
+  ScanGeom G;
+  G.two = m.num_bin > 2 && m.missing != 0;
+  G.skip = G.two && m.missing == 1;
+  const bool na = G.two && m.missing == 2;
+  G.off = m.offset;
+  G.tf_r = m.num_bin - 1 - G.off - (na ? 1 : 0);
+  G.t_end = m.num_bin - 2 - G.off;
+  // with NaN missing and the most-frequent bin 0, the forward scan's left side starts as
+  // everything outside the slice, at position t = -1 (held by the last thread)
+  G.fwd_rest = na && G.off == 1;
+  return G;
+}
+
+// Scan order: the reverse scan visits higher bins first, the forward scan lower bins first.
+__device__ __forceinline__ bool earlier(int d, int ta, int tb) { return d == 0 ? ta > tb : ta < tb; }
+
+// The best position of one direction within a warp (and, combined, within the CTA).
+struct DirBest {
+  long long key;  // dkey of the gain; kNoKey when no position qualified
+  double gain;    // -inf when none
+  int64_t a, b;   // int: left (grad, hess) sums; float: bit patterns of the accumulated (grad, hess)
+  int32_t t, c;   // position; float: accumulated count
+};
+
+// One direction's stop / prefilter summary of a warp (published before one barrier).
+struct WarpFilt {
+  int32_t lb;      // the warp's first `break` position in scan order (kNoneLo / kNoneHi: none)
+  int32_t mb, ma;  // best certified fp32 lower-bound key of positions before lb / of all positions
+  int32_t cb, ca;  // some position before lb / some position certainly passes min_gain_shift
+};
+
+constexpr int kNoneLo = -0x7fffffff, kNoneHi = 0x7fffffff;
+
+// A position queued for its f64 gain (PLAIN gains): evaluated by warp 0.
+struct QEnt {
+  int64_t a, b;  // int: left (grad, hess) sums; float: bit patterns of the accumulated (grad, hess)
+  int32_t c;     // float: accumulated count
+  int16_t t, d;  // position, direction
+};
+
+constexpr int kQueueCap = 2 * kSearchThreads;  // every position of both directions
+
+struct SearchSmem {
+  QEnt q[kQueueCap];
+  int32_t qn;
+  int64_t wi[2][kSearchWarps];
+  double wd[10][kSearchWarps];
+  int32_t wc[3][kSearchWarps];
+  WarpFilt wf[2][kSearchWarps];
+  WarpFilt xf;  // the forward scan's position -1 (last thread)
+  int32_t spl[2][kSearchWarps];
+  DirBest wb[2][kSearchWarps];
+};
+
+// This warp's arg-max of direction d (highest key, then the earliest position in scan order) into w.
+__device__ __forceinline__ void warp_best(int d, bool elig, double gain, int t, int64_t a, int64_t b, int32_t c,
+                                          int lane, DirBest* w) {
+  const long long key = elig ? dkey(gain) : kNoKey;
+  const long long km = warp_max64(key);
+  if (km == kNoKey) {
+    if (lane == 0) {
+      w->key = kNoKey;
+      w->gain = -CUDART_INF;
+      w->t = 0;
+    }
+    return;
   }
-  if (lane != 0) return;
+  const bool at = elig && key == km;
+  const int tb = d == 0 ? __reduce_max_sync(FULL, at ? t : kNoneLo) : __reduce_min_sync(FULL, at ? t : kNoneHi);
+  if (at && t == tb) *w = DirBest{km, gain, a, b, t, c};
+}
+
+// Warp 0 after the barrier: the CTA's best of each direction (lane 0: direction 0, lane 8:
+// direction 1), broadcast to every lane of the warp.
+__device__ __forceinline__ void combine_best(const SearchSmem& sm, int lane, DirBest (&r)[2], int (&split)[2]) {
+  const int d = (lane >> 3) & 1;
+  DirBest e;
+  e.key = kNoKey;
+  e.gain = -CUDART_INF;
+  e.a = e.b = 0;
+  e.t = e.c = 0;
+  int sp = 0;
+  if (lane < 16) {
+    e = sm.wb[d][lane & 7];
+    if (e.key == kNoKey) e.gain = -CUDART_INF;
+    sp = sm.spl[d][lane & 7];
+  }
+#pragma unroll
+  for (int o = 1; o < 8; o <<= 1) {
+    DirBest x;
+    x.key = __shfl_xor_sync(FULL, e.key, o);
+    x.gain = __shfl_xor_sync(FULL, e.gain, o);
+    x.a = __shfl_xor_sync(FULL, e.a, o);
+    x.b = __shfl_xor_sync(FULL, e.b, o);
+    x.t = __shfl_xor_sync(FULL, e.t, o);
+    x.c = __shfl_xor_sync(FULL, e.c, o);
+    sp |= __shfl_xor_sync(FULL, sp, o);
+    if (x.key > e.key || (x.key == e.key && x.key != kNoKey && earlier(d, x.t, e.t))) e = x;
+  }
+#pragma unroll
+  for (int k = 0; k < 2; ++k) {
+    const int src = 8 * k;
+    r[k].key = __shfl_sync(FULL, e.key, src);
+    r[k].gain = __shfl_sync(FULL, e.gain, src);
+    r[k].a = __shfl_sync(FULL, e.a, src);
+    r[k].b = __shfl_sync(FULL, e.b, src);
+    r[k].t = __shfl_sync(FULL, e.t, src);
+    r[k].c = __shfl_sync(FULL, e.c, src);
+    split[k] |= __shfl_sync(FULL, sp, src);
+  }
+}
+
+// The fp32 view of one position: certainly passes (cp) with certified lower-bound key lo, maybe
+// passes (mp), and its upper-bound key up.
+struct Filt {
+  bool cp, mp, unc;
+  int32_t lo, up;
+};
+
+__device__ __forceinline__ Filt filt_of(bool cand, const Approx& a, const LeafConst& C) {
+  Filt f;
+  f.unc = a.uncertain;
+  f.cp = cand && !a.uncertain && __fsub_rn(a.g, a.e) > C.mgs_up;
+  f.mp = cand && (a.uncertain || __fadd_rn(a.g, a.e) > C.mgs_dn);
+  f.lo = f.cp ? float_key(__fsub_rn(a.g, a.e)) : float_key(-CUDART_INF_F);
+  f.up = a.uncertain ? 0 : float_key(__fadd_rn(a.g, a.e));
+  return f;
+}
+
+// Before the barrier: the warp's summary of direction d for positions `pos` (thread order = t).
+template <bool PLAIN>
+__device__ __forceinline__ void publish_dir(SearchSmem& sm, int d, bool brk, int pos, const Filt& f, int lane,
+                                            int warp) {
+  const int lb = d == 0 ? __reduce_max_sync(FULL, brk ? pos : kNoneLo) : __reduce_min_sync(FULL, brk ? pos : kNoneHi);
+  WarpFilt w;
+  w.lb = lb;
+  w.mb = w.ma = float_key(-CUDART_INF_F);
+  w.cb = w.ca = 0;
+  if (PLAIN) {
+    const bool none = d == 0 ? lb == kNoneLo : lb == kNoneHi;
+    const bool before = none || (d == 0 ? pos > lb : pos < lb);
+    w.ma = __reduce_max_sync(FULL, f.lo);
+    w.mb = __reduce_max_sync(FULL, before ? f.lo : float_key(-CUDART_INF_F));
+    w.ca = __any_sync(FULL, f.cp);
+    w.cb = __any_sync(FULL, f.cp && before);
+  }
+  if (lane == 0) sm.wf[d][warp] = w;
+}
+
+// After the barrier: direction d's stop S (the first `break` in scan order; positions from it on
+// are invalid), and over the valid positions the best certified lower bound M and whether one
+// certainly passes. Warp w holds positions 32w .. 32w + 31; the forward scan's position -1 (when
+// `has_x`) comes first in its scan order.
+template <bool PLAIN>
+__device__ __forceinline__ void resolve_dir(const SearchSmem& sm, int d, bool has_x, int* S, int32_t* M,
+                                            int* certain) {
+  int s = d == 0 ? kNoneLo : kNoneHi;
+#pragma unroll
+  for (int w = 0; w < kSearchWarps; ++w) s = d == 0 ? max(s, sm.wf[d][w].lb) : min(s, sm.wf[d][w].lb);
+  if (d == 1 && has_x && sm.xf.lb == -1) s = -1;
+  *S = s;
+  int32_t m = float_key(-CUDART_INF_F);
+  int c = 0;
+  if (PLAIN) {
+    const bool none = d == 0 ? s == kNoneLo : s == kNoneHi;
+    if (d == 1 && has_x && s != -1) {
+      m = sm.xf.ma;
+      c = sm.xf.ca;
+    }
+#pragma unroll
+    for (int w = 0; w < kSearchWarps; ++w) {
+      const WarpFilt& f = sm.wf[d][w];
+      const bool contains = !none && f.lb == s;
+      const bool all_before = none || (d == 0 ? 32 * w > s : 32 * w + 31 < s);
+      if (contains) {
+        m = max(m, f.mb);
+        c |= f.cb;
+      } else if (all_before) {
+        m = max(m, f.ma);
+        c |= f.ca;
+      }
+    }
+  }
+  *M = m;
+  *certain = c;
+}
+
+// !(gain <= mgs) without an f64 comparison.
+__device__ __forceinline__ bool gain_passes(double gain, double mgs) {
+  return dnan(gain) || dnan(mgs) || dkey(gain) > dkey(mgs);
+}
+__device__ __forceinline__ bool is_neg_inf(double x) {
+  return (unsigned long long)__double_as_longlong(x) == 0xfff0000000000000ULL;
+}
+
+// Appends this thread's entry (when `push`) to the CTA's queue, one shared atomic per warp.
+__device__ __forceinline__ void queue_push(SearchSmem& sm, bool push, const QEnt& e, int lane) {
+  const unsigned bal = __ballot_sync(FULL, push);
+  int base = 0;
+  if (lane == 0 && bal) base = atomicAdd(&sm.qn, __popc(bal));
+  base = __shfl_sync(FULL, base, 0);
+  if (push) sm.q[base + __popc(bal & ((1u << lane) - 1u))] = e;
+}
+
+// Warp 0: the f64 gains of the queued positions, 32 at a time; per direction the arg-max (highest
+// gain, ties to the earliest position in scan order) and whether any queued position passed.
+template <typename Gain>
+__device__ __forceinline__ void eval_queue(const SearchSmem& sm, int lane, double mgs, DirBest (&r)[2],
+                                           int (&split)[2], Gain gain_of) {
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    r[d].key = kNoKey;
+    r[d].gain = -CUDART_INF;
+    r[d].a = r[d].b = 0;
+    r[d].t = d == 0 ? kNoneLo : kNoneHi;
+    r[d].c = 0;
+  }
+  const int n = sm.qn;
+  for (int b0 = 0; b0 < n; b0 += 32) {
+    const bool have = b0 + lane < n;
+    QEnt e;
+    e.a = e.b = 0;
+    e.c = 0;
+    e.t = 0;
+    e.d = -1;
+    if (have) e = sm.q[b0 + lane];
+    const double g = have ? gain_of(e) : -CUDART_INF;
+    const bool passed = have && gain_passes(g, mgs);
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      const bool mine = have && e.d == d;
+      if (__any_sync(FULL, mine && passed)) split[d] = 1;
+      const bool elig = mine && passed && !dnan(g) && !is_neg_inf(g);  // NaN never wins
+      const long long k = warp_max64(elig ? dkey(g) : kNoKey);
+      if (k == kNoKey) continue;
+      const bool at = elig && dkey(g) == k;
+      const int tb = d == 0 ? __reduce_max_sync(FULL, at ? (int)e.t : kNoneLo)
+                            : __reduce_min_sync(FULL, at ? (int)e.t : kNoneHi);
+      const int wl = __ffs(__ballot_sync(FULL, at && (int)e.t == tb)) - 1;
+      if (k > r[d].key || (k == r[d].key && earlier(d, tb, r[d].t))) {
+        r[d].key = k;
+        r[d].t = tb;
+        r[d].gain = __shfl_sync(FULL, g, wl);
+        r[d].a = __shfl_sync(FULL, e.a, wl);
+        r[d].b = __shfl_sync(FULL, e.b, wl);
+        r[d].c = __shfl_sync(FULL, e.c, wl);
+      }
+    }
+  }
+}
+
+__device__ __forceinline__ void store_cand(const Job& J, const Params& p, int side, int32_t f, const Cand& c) {
+  J.cand[side * p.F + f] = c;
+  J.cgain[side * p.F + f] = c.gain;
+  J.csplit[side * p.F + f] = (uint8_t)c.splittable;
+}
+
+// FindBestThresholdInt for one (leaf, feature): feature_histogram.rs:673-830, scans :839-1142.
+// Three barriers: the prefix scan (with the most-frequent-bin fix and the forward scan's start
+// folded in), the stop / prefilter summaries, and the arg-max.
+template <bool PLAIN>
+__device__ void search_int(const Job& J, const Params& p, const JobState* st, const DevFeature& m, int side,
+                           int32_t f, int32_t leaf, SearchSmem& sm) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const LeafConst C = J.lconst[side];
+  const int64_t s_int = J.leaf_sum[st->smaller_leaf].int_sum;
+  const int64_t l_int = side ? J.leaf_sum[leaf].int_sum : s_int;
+  const size_t slot_stride = (size_t)p.T * p.B * TILE;
+  const size_t feat_off = (size_t)(f / TILE) * p.B * TILE + (f % TILE);
+  int64_t* pool = reinterpret_cast<int64_t*>(J.pool);
+  int64_t* hs = pool + (size_t)st->smaller_slot * slot_stride + feat_off;  // group bin 0 of the feature
+  int64_t* hl = pool + (size_t)(side ? st->larger_slot : st->smaller_slot) * slot_stride + feat_off;
+  const bool fix = m.mfb > 0;  // offset 0: the slice holds every bin and the most frequent one is empty
+  const bool in = t < m.len;
+  // the smaller leaf's most-frequent entry is rewritten by its side-0 CTA; side 1 never reads it
+  const int64_t sv = (in && !(fix && t == m.mfb)) ? hs[(size_t)(t + 1) * TILE] : 0;
+  const int64_t lv = (side && in) ? hl[(size_t)(t + 1) * TILE] : 0;
+  const ScanGeom G = scan_geom(m);
+  if (t == 0) sm.qn = 0;
+  const bool skip_t = G.skip && t + G.off == m.default_bin;
+  const bool acc_t = !skip_t && t <= G.tf_r;  // bin t is accumulated by the scans
+  const int64_t v0 = side ? lv - sv : sv;     // before the most-frequent bin's fix
+  // barrier 1: the packed prefix sums of the accumulated bins, plus the sum that fixes the
+  // most-frequent bin (fix) or starts the forward scan outside the slice (fwd_rest; never both:
+  // fix needs offset 0, fwd_rest offset 1). Packed arithmetic is exact componentwise.
+  int64_t w = acc_t ? v0 : 0;
+  int64_t P = warp_incl_scan(w, lane);
+  const int64_t aux = warp_sum(fix ? sv : v0);
+  if (lane == 31) sm.wi[0][warp] = P;
+  if (lane == 0) sm.wi[1][warp] = aux;
+  __syncthreads();
+  int64_t T = 0, AUX = 0;
+#pragma unroll
+  for (int i = 0; i < kSearchWarps; ++i) {
+    const int64_t y = sm.wi[0][i];
+    if (i < warp) P += y;
+    T += y;
+    AUX += sm.wi[1][i];
+  }
+  int64_t v = v0;
+  if (fix) {
+    const int64_t fixed = s_int - AUX;  // FixHistogram: the leaf total minus every other bin
+    const int64_t delta = side ? -fixed : fixed;
+    if (t == m.mfb) {
+      v = v0 + delta;
+      if (side == 0) hs[(size_t)(t + 1) * TILE] = fixed;
+    }
+    if (m.mfb <= G.tf_r && !(G.skip && m.mfb + G.off == m.default_bin)) {
+      T += delta;
+      if (t >= m.mfb) P += delta;
+      if (t == m.mfb) w += delta;
+    }
+  }
+  if (side && in) hl[(size_t)(t + 1) * TILE] = v;
+  const int64_t base_f = G.fwd_rest ? l_int - AUX : 0;
+  const int64_t tg = unpack_g(l_int), th = unpack_h(l_int);
+  // reverse position t: right side = bins t .. tf_r; forward position t: left side = base_f plus
+  // bins 0 .. t; the last thread also holds forward position -1 (left side = base_f)
+  const int64_t right = T - (P - w);
+  const int64_t left = base_f + P;
+  const bool xpos = G.fwd_rest && t == kSearchThreads - 1;
+  const bool first0 = t >= 1 - G.off && acc_t && unpack_h(right) >= C.first_x;
+  const bool brk0 = first0 && unpack_h(right) >= C.brk_x;
+  const bool first1 = G.two && t <= G.t_end && !skip_t && unpack_h(left) >= C.first_x;
+  const bool brk1 = first1 && unpack_h(left) >= C.brk_x;
+  const bool firstx = xpos && unpack_h(base_f) >= C.first_x;
+  const bool brkx = firstx && unpack_h(base_f) >= C.brk_x;
+  const int64_t lg[2] = {tg - unpack_g(right), xpos ? unpack_g(base_f) : unpack_g(left)};
+  const int64_t lh[2] = {th - unpack_h(right), xpos ? unpack_h(base_f) : unpack_h(left)};
+  // barrier 2: stops and prefilter summaries
+  Filt fl[2];
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    const bool cand = d == 0 ? first0 : (first1 || firstx);
+    Approx a{0.f, 0.f, true};
+    if (PLAIN && cand) a = approx_int(lg[d], lh[d], tg, th, C.gsf, C.hsf, C.l2f);
+    fl[d] = filt_of(cand, a, C);
+  }
+  publish_dir<PLAIN>(sm, 0, brk0, t, fl[0], lane, warp);
+  {
+    Filt nat = fl[1];
+    if (xpos) nat.cp = false;  // the natural position 255 is never a candidate
+    publish_dir<PLAIN>(sm, 1, brk1, t, nat, lane, warp);
+  }
+  if (xpos) {
+    WarpFilt x;
+    x.lb = brkx ? -1 : kNoneHi;
+    x.ma = x.mb = fl[1].lo;
+    x.ca = x.cb = fl[1].cp;
+    sm.xf = x;
+  }
+  __syncthreads();
+  int S[2], certain[2];
+  int32_t M[2];
+  resolve_dir<PLAIN>(sm, 0, false, &S[0], &M[0], &certain[0]);
+  resolve_dir<PLAIN>(sm, 1, G.fwd_rest, &S[1], &M[1], &certain[1]);
+  const bool valid[2] = {first0 && t > S[0], xpos ? (firstx && S[1] != -1) : (first1 && t < S[1])};
+  DirBest r[2];
+  int rs[2] = {PLAIN ? certain[0] : 0, PLAIN ? certain[1] : 0};
+  if (PLAIN) {
+    // barrier 3: the few positions that need their f64 gain, evaluated together by warp 0
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      const bool exact = valid[d] && fl[d].mp && (fl[d].unc || fl[d].up >= M[d]);
+      queue_push(sm, exact, QEnt{lg[d], lh[d], 0, (int16_t)(d == 0 || !xpos ? t : -1), (int16_t)d}, lane);
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    const double gs = st->gscale, hsc = st->hscale;
+    eval_queue(sm, lane, C.mgs, r, rs, [&](const QEnt& e) {
+      return int_split_gain(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, true);
+    });
+  } else {
+    // every valid position evaluates its own f64 gain; barrier 3: the arg-max
+    double gain[2];
+    bool split[2], elig[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      gain[d] = -CUDART_INF;
+      if (valid[d])
+        gain[d] = int_split_gain(p, lg[d], lh[d], tg, th, st->gscale, st->hscale, C.cnt_factor, C.parent, false);
+      const bool passed = valid[d] && gain_passes(gain[d], C.mgs);
+      split[d] = passed;
+      elig[d] = passed && !dnan(gain[d]) && !is_neg_inf(gain[d]);  // NaN never wins
+    }
+    warp_best(0, elig[0], gain[0], t, lg[0], lh[0], 0, lane, &sm.wb[0][warp]);
+    warp_best(1, elig[1], gain[1], xpos ? -1 : t, lg[1], lh[1], 0, lane, &sm.wb[1][warp]);
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      const int ws = __any_sync(FULL, split[d]);
+      if (lane == 0) sm.spl[d][warp] = ws;
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    combine_best(sm, lane, r, rs);
+  }
+  // FindBestThresholdInt's combination of the directions (feature_histogram.rs:700-830): the
+  // reverse scan first, the forward scan replaces it only with a strictly larger gain
+  const double mgs = C.mgs, gs = st->gscale, hsc = st->hscale;
+  const int nd = G.two ? 2 : 1;
+  int sp = 0, ch = -1;
+  double cgain = -CUDART_INF;
+  for (int i = 0; i < nd; ++i) {
+    sp |= rs[i];
+    if (rs[i] && r[i].gain > cgain + mgs) {
+      ch = i;
+      cgain = r[i].gain - mgs;
+    }
+  }
   Cand c;
   cand_reset(&c, m.real, f);
-  int sp = 0;
-  for (int i = 0; i < nd; ++i) {
-    const DirBest& r = d[i];
-    sp |= r.splittable;
-    if (r.splittable && r.gain > c.gain + mgs) {
-      c.threshold = (uint32_t)r.th;
-      c.left_output = split_output(p, r.slg, r.slh, r.lc, parent);
-      c.left_count = r.lc;
-      c.lsg = r.slg;
-      c.lsh = r.slh - BK_EPS;
-      c.right_output = split_output(p, sum_g - r.slg, sum_h - r.slh, num_data - r.lc, parent);
-      c.right_count = num_data - r.lc;
-      c.rsg = sum_g - r.slg;
-      c.rsh = (sum_h - r.slh) - BK_EPS;
-      c.gain = r.gain - mgs;
-      c.default_left = i == 0 ? 1 : 0;
-    }
+  if (ch >= 0) {
+    const DirBest& b = ch == 0 ? r[0] : r[1];
+    const int64_t rg = tg - b.a, rh = th - b.b;
+    // lane 0 computes the left output, lane 1 the right one
+    const double sg1 = (double)(int32_t)(lane == 0 ? b.a : rg) * gs;
+    const double sh1 = (double)(uint32_t)(lane == 0 ? b.b : rh) * hsc;
+    const int32_t n1 = round_int((double)(uint32_t)(lane == 0 ? b.b : rh) * C.cnt_factor);
+    const double out = lane < 2 ? split_output(p, sg1, sh1, n1, C.parent) : 0.0;
+    c.threshold = (uint32_t)(ch == 0 ? b.t - 1 + G.off : b.t + G.off);
+    c.left_output = out;
+    c.left_count = n1;
+    c.lsg = sg1;
+    c.lsh = sh1;
+    c.right_output = __shfl_sync(FULL, out, 1);
+    c.right_count = __shfl_sync(FULL, n1, 1);
+    c.rsg = __shfl_sync(FULL, sg1, 1);
+    c.rsh = __shfl_sync(FULL, sh1, 1);
+    c.lint = (int64_t)(((uint64_t)b.a << 32) | ((uint64_t)b.b & 0xffffffffull));
+    c.rint = (int64_t)(((uint64_t)rg << 32) | ((uint64_t)rh & 0xffffffffull));
+    c.gain = cgain;
+    c.default_left = ch == 0 ? 1 : 0;
   }
   if (nd == 1 && m.missing == 2) c.default_left = 0;
   c.gain *= m.penalty;
   c.splittable = sp;
-  *out = c;
-  *out_gain = c.gain;
-  *out_split = (uint8_t)sp;
+  if (lane == 0) store_cand(J, p, side, f, c);
 }
 
-// FindBestThresholdInt for one leaf: feature_histogram.rs:673-830.
+// FindBestThreshold (float) for one (leaf, feature): feature_histogram.rs:219-357, scans
+// :363-663. f64 (grad, hess) sums and row counts estimated per bin as round_int(hess *
+// cnt_factor); the forward scan uses prefix sums, the reverse scan suffix sums (accumulated from
+// the top bin down, not derived by subtraction).
 template <bool PLAIN>
-__device__ void search_leaf_int(const Params& p, const DevFeature& m, const IntHist& H, const LeafSum& ls,
-                                double gs, double hs, double parent, int lane, Cand* out, double* out_gain,
-                                uint8_t* out_split, int32_t f) {
-  const int64_t tg = ls.int_sum >> 32;
-  const int64_t th = ls.int_sum & 0xffffffffLL;
-  const int32_t num_data = ls.num_data;
-  const double sum_g = (double)tg * gs;
-  const double sum_h = (double)th * hs;
-  double gain_shift = leaf_gain(p, sum_g, sum_h, num_data, parent);
-  double mgs = gain_shift + p.min_gain;
-  const IntThresholds X = int_thresholds(p, th, hs, num_data, lane);
-  DirBest d[2];
-  int nd;
-  if (m.num_bin > 2 && m.missing != 0) {
-    bool skip = m.missing == 1, na = m.missing == 2;
-    d[0] = scan_int<true, PLAIN>(p, m, H, skip, na, tg, th, gs, hs, num_data, mgs, parent, X, lane);
-    d[1] = scan_int<false, PLAIN>(p, m, H, skip, na, tg, th, gs, hs, num_data, mgs, parent, X, lane);
-    nd = 2;
-  } else {
-    d[0] = scan_int<true, PLAIN>(p, m, H, false, false, tg, th, gs, hs, num_data, mgs, parent, X, lane);
-    nd = 1;
+__device__ void search_float(const Job& J, const Params& p, const JobState* st, const DevFeature& m, int side,
+                             int32_t f, int32_t leaf, SearchSmem& sm) {
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const LeafConst C = J.lconst[side];
+  const LeafSum S0 = J.leaf_sum[st->smaller_leaf];
+  const int32_t num_data = side ? J.leaf_sum[leaf].num_data : S0.num_data;
+  const size_t slot_stride = (size_t)p.T * p.B * TILE;
+  const size_t feat_off = (size_t)(f / TILE) * p.B * TILE + (f % TILE);
+  double2* pool = reinterpret_cast<double2*>(J.pool);
+  double2* hs = pool + (size_t)st->smaller_slot * slot_stride + feat_off;
+  double2* hl = pool + (size_t)(side ? st->larger_slot : st->smaller_slot) * slot_stride + feat_off;
+  const double2 zero = make_double2(0.0, 0.0);
+  const bool fix = m.mfb > 0;
+  const bool in = t < m.len;
+  double2 sv = (in && !(fix && t == m.mfb)) ? hs[(size_t)(t + 1) * TILE] : zero;
+  const double2 lv = (side && in) ? hl[(size_t)(t + 1) * TILE] : zero;
+  const ScanGeom G = scan_geom(m);
+  if (t == 0) sm.qn = 0;
+  const double sum_g = C.sum_g, sum_h = C.sum_h;
+  if (fix) {  // one barrier for both sums
+    const double ag = warp_sum(sv.x), ah = warp_sum(sv.y);
+    if (lane == 0) {
+      sm.wd[0][warp] = ag;
+      sm.wd[1][warp] = ah;
+    }
+    __syncthreads();
+    double tg = 0.0, th = 0.0;
+#pragma unroll
+    for (int i = 0; i < kSearchWarps; ++i) {
+      tg += sm.wd[0][i];
+      th += sm.wd[1][i];
+    }
+    if (t == m.mfb) {
+      sv = make_double2(S0.sg - tg, S0.sh - th);
+      if (side == 0) hs[(size_t)(t + 1) * TILE] = sv;
+    }
   }
-  if (lane != 0) return;
+  const double2 v = side ? make_double2(lv.x - sv.x, lv.y - sv.y) : sv;
+  if (side && in) hl[(size_t)(t + 1) * TILE] = v;
+  const int32_t cn = in ? round_int(v.y * C.cnt_factor) : 0;
+  // barrier: prefix sums (forward), suffix sums over bins <= tf_r (reverse) and, when the forward
+  // scan starts outside the slice, the slice totals
+  const bool skip_t = G.skip && t + G.off == m.default_bin;
+  const double wg = skip_t ? 0.0 : v.x, wh = skip_t ? 0.0 : v.y;
+  const int32_t wc = skip_t ? 0 : cn;
+  const bool rin = t <= G.tf_r;
+  double pg = warp_incl_scan(wg, lane), ph = warp_incl_scan(wh, lane);
+  int32_t pc = warp_incl_scan(wc, lane);
+  double rg = warp_incl_scan_down(rin ? wg : 0.0, lane), rh = warp_incl_scan_down(rin ? wh : 0.0, lane);
+  int32_t rc = warp_incl_scan_down(rin ? wc : 0, lane);
+  if (lane == 31) {
+    sm.wd[2][warp] = pg;
+    sm.wd[3][warp] = ph;
+    sm.wc[0][warp] = pc;
+  }
+  if (lane == 0) {
+    sm.wd[4][warp] = rg;
+    sm.wd[5][warp] = rh;
+    sm.wc[1][warp] = rc;
+  }
+  if (G.fwd_rest) {
+    const double ug = warp_sum(v.x), uh = warp_sum(v.y);
+    const int32_t uc = warp_sum(cn);
+    if (lane == 0) {
+      sm.wd[6][warp] = ug;
+      sm.wd[7][warp] = uh;
+      sm.wc[2][warp] = uc;
+    }
+  }
+  __syncthreads();
+  // forward scan start: nothing (with kEpsilon hessian) or everything outside the slice
+  double bg = 0.0, bh = BK_EPS;
+  int32_t bc = 0;
+  {
+    double og = 0.0, oh = 0.0, sg_ = 0.0, sh_ = 0.0, ug = 0.0, uh = 0.0;
+    int32_t oc = 0, sc = 0, uc = 0;
+#pragma unroll
+    for (int i = 0; i < kSearchWarps; ++i) {
+      if (i < warp) {
+        og += sm.wd[2][i];
+        oh += sm.wd[3][i];
+        oc += sm.wc[0][i];
+      }
+    }
+#pragma unroll
+    for (int i = kSearchWarps - 1; i >= 0; --i) {
+      if (i > warp) {
+        sg_ += sm.wd[4][i];
+        sh_ += sm.wd[5][i];
+        sc += sm.wc[1][i];
+      }
+    }
+    if (G.fwd_rest) {
+#pragma unroll
+      for (int i = 0; i < kSearchWarps; ++i) {
+        ug += sm.wd[6][i];
+        uh += sm.wd[7][i];
+        uc += sm.wc[2][i];
+      }
+      bg = sum_g - ug;
+      bh = (sum_h - BK_EPS) - uh;
+      bc = num_data - uc;
+    }
+    pg = bg + (pg + og);
+    ph = bh + (ph + oh);
+    pc = bc + (pc + oc);
+    rg = rg + sg_;
+    rh = BK_EPS + (rh + sh_);
+    rc = rc + sc;
+  }
+  // reverse position t: right side (rg, rh, rc); forward position t: left side (pg, ph, pc); the
+  // last thread holds forward position -1 when the scan starts outside the slice
+  const bool xpos = G.fwd_rest && t == kSearchThreads - 1;
+  const bool first0 = t >= 1 - G.off && rin && !skip_t && !(rc < p.min_data || rh < p.min_hess);
+  const bool brk0 = first0 && (num_data - rc < p.min_data || sum_h - rh < p.min_hess);
+  const bool first1 = G.two && t <= G.t_end && !skip_t && !(pc < p.min_data || ph < p.min_hess);
+  const bool brk1 = first1 && (num_data - pc < p.min_data || sum_h - ph < p.min_hess);
+  const bool firstx = xpos && !(bc < p.min_data || bh < p.min_hess);
+  const bool brkx = firstx && (num_data - bc < p.min_data || sum_h - bh < p.min_hess);
+  const double fg = xpos ? bg : pg, fh = xpos ? bh : ph;
+  const int32_t fc = xpos ? bc : pc;
+  // left / right sums of both positions
+  const double slg[2] = {sum_g - rg, fg}, slh[2] = {sum_h - rh, fh};
+  const double srg[2] = {rg, sum_g - fg}, srh[2] = {rh, sum_h - fh};
+  const int32_t lc[2] = {num_data - rc, fc}, rcn[2] = {rc, num_data - fc};
+  Filt fl[2];
+#pragma unroll
+  for (int d = 0; d < 2; ++d) {
+    const bool cand = d == 0 ? first0 : (first1 || firstx);
+    Approx a{0.f, 0.f, true};
+    if (PLAIN && cand)
+      a = approx_from((float)slg[d], __fadd_rn((float)slh[d], C.l2f), (float)srg[d], __fadd_rn((float)srh[d], C.l2f));
+    fl[d] = filt_of(cand, a, C);
+  }
+  publish_dir<PLAIN>(sm, 0, brk0, t, fl[0], lane, warp);
+  {
+    Filt nat = fl[1];
+    if (xpos) nat.cp = false;
+    publish_dir<PLAIN>(sm, 1, brk1, t, nat, lane, warp);
+  }
+  if (xpos) {
+    WarpFilt x;
+    x.lb = brkx ? -1 : kNoneHi;
+    x.ma = x.mb = fl[1].lo;
+    x.ca = x.cb = fl[1].cp;
+    sm.xf = x;
+  }
+  __syncthreads();
+  int S[2], certain[2];
+  int32_t M[2];
+  resolve_dir<PLAIN>(sm, 0, false, &S[0], &M[0], &certain[0]);
+  resolve_dir<PLAIN>(sm, 1, G.fwd_rest, &S[1], &M[1], &certain[1]);
+  const bool valid[2] = {first0 && t > S[0], xpos ? (firstx && S[1] != -1) : (first1 && t < S[1])};
+  DirBest r[2];
+  int rs[2] = {PLAIN ? certain[0] : 0, PLAIN ? certain[1] : 0};
+  // carried per position: the accumulated side's sums (reverse: right, forward: left)
+  const int64_t ca[2] = {__double_as_longlong(rg), __double_as_longlong(fg)};
+  const int64_t cb[2] = {__double_as_longlong(rh), __double_as_longlong(fh)};
+  const int32_t cc[2] = {rc, fc};
+  auto gain_of = [&](const QEnt& e) {
+    const double ag = __longlong_as_double(e.a), ah = __longlong_as_double(e.b);
+    if (e.d == 0)  // reverse: (ag, ah, c) is the right side
+      return split_gains(p, sum_g - ag, sum_h - ah, ag, ah, num_data - e.c, e.c, C.parent);
+    return split_gains(p, ag, ah, sum_g - ag, sum_h - ah, e.c, num_data - e.c, C.parent);
+  };
+  if (PLAIN) {
+    // barrier 3: the few positions that need their f64 gain, evaluated together by warp 0
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      const bool exact = valid[d] && fl[d].mp && (fl[d].unc || fl[d].up >= M[d]);
+      queue_push(sm, exact, QEnt{ca[d], cb[d], cc[d], (int16_t)(d == 0 || !xpos ? t : -1), (int16_t)d}, lane);
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    eval_queue(sm, lane, C.mgs, r, rs, gain_of);
+  } else {
+    double gain[2];
+    bool split[2], elig[2];
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      gain[d] = -CUDART_INF;
+      if (valid[d]) gain[d] = split_gains(p, slg[d], slh[d], srg[d], srh[d], lc[d], rcn[d], C.parent);
+      const bool passed = valid[d] && gain_passes(gain[d], C.mgs);
+      split[d] = passed;
+      elig[d] = passed && !dnan(gain[d]) && !is_neg_inf(gain[d]);
+    }
+    warp_best(0, elig[0], gain[0], t, ca[0], cb[0], cc[0], lane, &sm.wb[0][warp]);
+    warp_best(1, elig[1], gain[1], xpos ? -1 : t, ca[1], cb[1], cc[1], lane, &sm.wb[1][warp]);
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      const int ws = __any_sync(FULL, split[d]);
+      if (lane == 0) sm.spl[d][warp] = ws;
+    }
+    __syncthreads();
+    if (warp != 0) return;
+    combine_best(sm, lane, r, rs);
+  }
+  // FindBestThreshold's combination of the directions (feature_histogram.rs:240-357)
+  const double mgs = C.mgs;
+  const int nd = G.two ? 2 : 1;
+  int sp = 0, ch = -1;
+  double cgain = -CUDART_INF;
+  for (int i = 0; i < nd; ++i) {
+    sp |= rs[i];
+    if (rs[i] && r[i].gain > cgain + mgs) {
+      ch = i;
+      cgain = r[i].gain - mgs;
+    }
+  }
   Cand c;
   cand_reset(&c, m.real, f);
-  const double cnt_factor = (double)num_data / (double)th;
-  int sp = 0;
-  for (int i = 0; i < nd; ++i) {
-    const DirBest& r = d[i];
-    sp |= r.splittable;
-    if (r.splittable && r.gain > c.gain + mgs) {
-      int64_t rg = tg - r.lg, rh = th - r.lh;
-      double slg = (double)r.lg * gs, slh = (double)r.lh * hs;
-      double srg = (double)rg * gs, srh = (double)rh * hs;
-      int32_t lc = round_int((double)r.lh * cnt_factor);
-      int32_t rc = round_int((double)rh * cnt_factor);
-      c.threshold = (uint32_t)r.th;
-      c.left_output = split_output(p, slg, slh, lc, parent);
-      c.left_count = lc;
-      c.lsg = slg;
-      c.lsh = slh;
-      c.right_output = split_output(p, srg, srh, rc, parent);
-      c.right_count = rc;
-      c.rsg = srg;
-      c.rsh = srh;
-      c.lint = (int64_t)(((uint64_t)r.lg << 32) | ((uint64_t)r.lh & 0xffffffffull));
-      c.rint = (int64_t)(((uint64_t)rg << 32) | ((uint64_t)rh & 0xffffffffull));
-      c.gain = r.gain - mgs;
-      c.default_left = i == 0 ? 1 : 0;
-    }
+  if (ch >= 0) {
+    const DirBest& b = ch == 0 ? r[0] : r[1];
+    const double ag = __longlong_as_double(b.a), ah = __longlong_as_double(b.b);
+    const double bslg = ch == 0 ? sum_g - ag : ag, bslh = ch == 0 ? sum_h - ah : ah;
+    const int32_t blc = ch == 0 ? num_data - b.c : b.c;
+    // lane 0 computes the left output, lane 1 the right one
+    const double sg1 = lane == 0 ? bslg : sum_g - bslg;
+    const double sh1 = lane == 0 ? bslh : sum_h - bslh;
+    const int32_t n1 = lane == 0 ? blc : num_data - blc;
+    const double out = lane < 2 ? split_output(p, sg1, sh1, n1, C.parent) : 0.0;
+    c.threshold = (uint32_t)(ch == 0 ? b.t - 1 + G.off : b.t + G.off);
+    c.left_output = out;
+    c.left_count = blc;
+    c.lsg = bslg;
+    c.lsh = bslh - BK_EPS;
+    c.right_output = __shfl_sync(FULL, out, 1);
+    c.right_count = num_data - blc;
+    c.rsg = sum_g - bslg;
+    c.rsh = (sum_h - bslh) - BK_EPS;
+    c.gain = cgain;
+    c.default_left = ch == 0 ? 1 : 0;
   }
   if (nd == 1 && m.missing == 2) c.default_left = 0;
   c.gain *= m.penalty;
   c.splittable = sp;
-  *out = c;
-  *out_gain = c.gain;
-  *out_split = (uint8_t)sp;
+  if (lane == 0) store_cand(J, p, side, f, c);
 }
 
-__device__ __forceinline__ double parent_output_of(const Params& p, const JobState* st, const LeafSum& ls) {
-  // serial.rs:1924-1935 (GetParentOutput)
-  if (st->tree_leaves == 1) return leaf_output_root(p, ls.sg, ls.sh, ls.num_data);
-  return ls.weight;
+// ---- the fold and the leaf arg-max on integer keys ----
+
+// split_info.rs:104-121 (better_than) on keys: the higher gain, then the smaller real feature
+// (-1 counts as largest); with a NaN gain on either side neither is better.
+__device__ __forceinline__ bool better_k(long long ka, bool na, int fa, long long kb, bool nb, int fb) {
+  if (na || nb) return false;
+  if (ka != kb) return ka > kb;
+  const int a = fa == -1 ? 0x7fffffff : fa;
+  const int b = fb == -1 ? 0x7fffffff : fb;
+  return a < b;
 }
 
-__device__ void decide_body(const Job& J, const Params& p, const DevFeature* feats);
+struct Pick {
+  int i, f;  // index (-1: none), real feature
+  long long k;
+  bool nan;
+};
 
-// One warp per (leaf side, feature): side 0 = the smaller leaf, side 1 = the larger leaf.
-// Side 0 fixes the smaller leaf's most-frequent bin (FixHistogram, serial.rs:2205-2238); side 1
-// derives the larger leaf as parent minus the fixed smaller histogram (serial.rs:1407-1437,
-// :1218-1242) — it recomputes the fixed most-frequent bin itself with the same reduction, so the
-// two warps never wait for each other. The last CTA to finish runs the fold / arg-max (k_decide).
-template <bool PLAIN, bool QUANT>
-__global__ void __launch_bounds__(64) k_search(const Job* __restrict__ jobs, Params p,
-                                               const DevFeature* __restrict__ feats) {
-  const Job& J = jobs[blockIdx.z];
-  JobState* st = J.st;
-  if (st->stop) return;  // uniform over the grid
-  const int lane = threadIdx.x & 31;
-  const int w = blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
-  const int side = w >= p.F ? 1 : 0;
-  const int f = w - side * p.F;
-  const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
-  if (st->do_search && f < p.F && J.used[f] && leaf >= 0) {
-    const DevFeature m = feats[f];
-    const size_t slot_stride = (size_t)p.T * p.B * TILE;
-    const size_t feat_off = (size_t)(f / TILE) * p.B * TILE + (f % TILE);
-    const LeafSum S = J.leaf_sum[st->smaller_leaf];
-    const LeafSum ls = side ? J.leaf_sum[leaf] : S;
-    const double parent = parent_output_of(p, st, ls);
-    if (QUANT) {
-      int64_t* pool = reinterpret_cast<int64_t*>(J.pool);
-      IntHist HS{pool + (size_t)st->smaller_slot * slot_stride + feat_off};
-      int64_t fixed = 0;
-      if (m.mfb > 0) {
-        int64_t acc = 0;
-        for (int i = lane; i < m.num_bin; i += 32)
-          if (i != m.mfb) acc += HS.get(i);
-        acc = warp_sum(acc);
-        // the packed leaf total (grad << 32) | hess equals grad * 2^32 + hess, so packed
-        // arithmetic is exact componentwise
-        fixed = S.int_sum - acc;
-      }
-      if (side == 0) {
-        if (m.mfb > 0 && lane == 0) HS.base[(size_t)(m.mfb + 1) * TILE] = fixed;
-        __syncwarp();
-        search_leaf_int<PLAIN>(p, m, HS, ls, st->gscale, st->hscale, parent, lane, &J.cand[f], &J.cgain[f],
-                               &J.csplit[f], f);
-      } else {
-        IntHist HL{pool + (size_t)st->larger_slot * slot_stride + feat_off};
-        for (int i = lane; i < m.len; i += 32) {
-          int64_t sv = (m.mfb > 0 && i == m.mfb) ? fixed : HS.get(i);
-          HL.base[(size_t)(i + 1) * TILE] -= sv;
-        }
-        __syncwarp();
-        search_leaf_int<PLAIN>(p, m, HL, ls, st->gscale, st->hscale, parent, lane, &J.cand[p.F + f],
-                               &J.cgain[p.F + f], &J.csplit[p.F + f], f);
-      }
-    } else {
-      double2* pool = reinterpret_cast<double2*>(J.pool);
-      FloatHist HS{pool + (size_t)st->smaller_slot * slot_stride + feat_off};
-      double2 fixed = make_double2(0.0, 0.0);
-      if (m.mfb > 0) {
-        double ag = 0.0, ah = 0.0;
-        for (int i = lane; i < m.num_bin; i += 32)
-          if (i != m.mfb) {
-            double2 v = HS.get(i);
-            ag += v.x;
-            ah += v.y;
-          }
-        ag = warp_sum(ag);
-        ah = warp_sum(ah);
-        fixed = make_double2(S.sg - ag, S.sh - ah);
-      }
-      if (side == 0) {
-        if (m.mfb > 0 && lane == 0) HS.base[(size_t)(m.mfb + 1) * TILE] = fixed;
-        __syncwarp();
-        search_leaf_float<PLAIN>(p, m, HS, ls, parent, lane, &J.cand[f], &J.cgain[f], &J.csplit[f], f);
-      } else {
-        FloatHist HL{pool + (size_t)st->larger_slot * slot_stride + feat_off};
-        for (int i = lane; i < m.len; i += 32) {
-          double2 a = HL.get(i);
-          double2 b = (m.mfb > 0 && i == m.mfb) ? fixed : HS.get(i);
-          HL.base[(size_t)(i + 1) * TILE] = make_double2(a.x - b.x, a.y - b.y);
-        }
-        __syncwarp();
-        search_leaf_float<PLAIN>(p, m, HL, ls, parent, lane, &J.cand[p.F + f], &J.cgain[p.F + f],
-                                 &J.csplit[p.F + f], f);
-      }
-    }
-  }
-  // the last CTA of this launch runs the fold and the leaf arg-max
-  __shared__ int last;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    unsigned t = atomicAdd(&st->search_done, 1u);
-    last = t == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  decide_body(J, p, feats);
-  if (threadIdx.x == 0) st->search_done = 0u;
+// Fold step: `a` comes first in the sequential order; `b` replaces it only when strictly better;
+// NaN gains never win (the sequential fold never adopts them).
+__device__ __forceinline__ void pick(Pick& a, const Pick& b) {
+  if (b.i < 0 || b.nan) return;
+  if (a.i < 0 || better_k(b.k, false, b.f, a.k, a.nan, a.f) || (!better_k(a.k, a.nan, a.f, b.k, false, b.f) && b.i < a.i))
+    a = b;
 }
 
-// ---------------------------------------------------------------------------------------------
-// k_decide
-// ---------------------------------------------------------------------------------------------
-
-// Combine two (index, gain, real feature) candidates of a fold or an arg-max. `a` is the one
-// that comes first in the sequential order; `b` replaces it only when strictly better
-// (split_info.rs:104-121); NaN gains never win (the sequential fold never adopts them).
-__device__ __forceinline__ void pick(int& ai, double& ag, int& af, int bi, double bg, int bf) {
-  if (bi < 0 || isnan(bg)) return;
-  if (ai < 0 || better_than(bg, bf, ag, af) || (!better_than(ag, af, bg, bf) && bi < ai)) {
-    ai = bi;
-    ag = bg;
-    af = bf;
-  }
+// Arg-max step over leaves: the first arg-max under better_than, ties to the smaller index.
+__device__ __forceinline__ void leaf_pick(Pick& a, const Pick& b) {
+  if (b.i < 0) return;
+  if (a.i < 0 || better_k(b.k, b.nan, b.f, a.k, a.nan, a.f) || (!better_k(a.k, a.nan, a.f, b.k, b.nan, b.f) && b.i < a.i))
+    a = b;
 }
+
+__device__ __forceinline__ Pick shfl_pick(const Pick& a, int o) {
+  Pick b;
+  b.i = __shfl_xor_sync(FULL, a.i, o);
+  b.f = __shfl_xor_sync(FULL, a.f, o);
+  b.k = __shfl_xor_sync(FULL, a.k, o);
+  b.nan = __shfl_xor_sync(FULL, (int)a.nan, o) != 0;
+  return b;
+}
+
+__device__ __forceinline__ Pick make_pick(int i, double g, int f) { return Pick{i, f, dkey(g), dnan(g)}; }
 
 // Cand is 8-byte aligned and its size a multiple of 8 (not of 16): copy it in 8-byte words.
 static_assert(sizeof(Cand) % 8 == 0 && alignof(Cand) == 8, "Cand is copied in 8-byte words");
@@ -684,83 +907,116 @@ __device__ __forceinline__ Cand load_cand_cg(const Cand* c) {
   return r;
 }
 
-// The fold of the searched leaves' candidates and the leaf arg-max (64 threads). Everything
-// written by other CTAs of the search launch is read through L2 (__ldcg).
+// The fold of the searched leaves' candidates and the leaf arg-max, run by the last CTA of the
+// search launch. Everything written by other CTAs of the launch is read through L2 (__ldcg).
 __device__ void decide_body(const Job& J, const Params& p, const DevFeature* feats) {
+  __shared__ Pick s_p[kSearchWarps];
   JobState* st = J.st;
-  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  if (st->do_search) {
-    // serial.rs:1523-1558 — fold the candidates of each searched leaf in feature order.
-    const int32_t leaf = warp == 0 ? st->smaller_leaf : st->larger_leaf;
-    const int32_t slot = warp == 0 ? st->smaller_slot : st->larger_slot;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  constexpr int kHalf = kSearchThreads / 2;
+  const bool searched = st->do_search != 0;
+  if (searched) {
+    // serial.rs:1523-1558 — fold the candidates of each searched leaf in feature order: the first
+    // half of the CTA folds the smaller leaf, the second half the larger one
+    const int side = t / kHalf;
+    const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
+    const int32_t slot = side ? st->larger_slot : st->smaller_slot;
+    Pick a{-1, 0x7fffffff, 0, false};
     if (leaf >= 0) {
-      int bi = -1, bf = 0x7fffffff;
-      double bg = -CUDART_INF;
-      for (int f = lane; f < p.F; f += 32) {
-        if (!J.used[f]) continue;
-        J.splittable[(size_t)slot * p.F + f] = __ldcg(&J.csplit[warp * p.F + f]);
-        pick(bi, bg, bf, f, __ldcg(&J.cgain[warp * p.F + f]), feats[f].real);
+      for (int f = t % kHalf; f < p.F; f += kHalf) {
+        const uint8_t u = J.used[f];
+        const uint8_t cs = __ldcg(&J.csplit[side * p.F + f]);
+        const double g = __ldcg(&J.cgain[side * p.F + f]);
+        const int real = feats[f].real;
+        if (!u) continue;
+        J.splittable[(size_t)slot * p.F + f] = cs;
+        pick(a, make_pick(f, g, real));
       }
+    }
 #pragma unroll
-      for (int o = 16; o > 0; o >>= 1) {
-        int oi = __shfl_xor_sync(FULL, bi, o);
-        double og = __shfl_xor_sync(FULL, bg, o);
-        int of = __shfl_xor_sync(FULL, bf, o);
-        pick(bi, bg, bf, oi, og, of);
-      }
-      if (lane == 0) {
-        // the fold starts from SplitInfo::default (gain -inf, feature -1) and replaces it only
-        // with a better candidate
-        Cand best;
-        cand_reset(&best, -1, -1);
-        if (bi >= 0 && better_than(bg, bf, best.gain, best.feature)) best = load_cand_cg(&J.cand[warp * p.F + bi]);
-        J.best[leaf] = best;
-        J.bgain[leaf] = best.gain;
-        J.bfeat[leaf] = best.feature;
-      }
+    for (int o = 16; o > 0; o >>= 1) pick(a, shfl_pick(a, o));
+    if (lane == 0) s_p[warp] = a;
+  }
+  __syncthreads();
+  if (searched && t % kHalf == 0) {
+    const int side = t / kHalf;
+    const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
+    if (leaf >= 0) {
+      Pick a{-1, 0x7fffffff, 0, false};
+      for (int w = side * (kSearchWarps / 2); w < (side + 1) * (kSearchWarps / 2); ++w) pick(a, s_p[w]);
+      // the fold starts from SplitInfo::default (gain -inf, feature -1) and replaces it only
+      // with a better candidate
+      Cand best;
+      cand_reset(&best, -1, -1);
+      if (a.i >= 0 && better_k(a.k, a.nan, a.f, dkey(-CUDART_INF), false, -1))
+        best = load_cand_cg(&J.cand[side * p.F + a.i]);
+      J.best[leaf] = best;
+      J.bgain[leaf] = best.gain;
+      J.bfeat[leaf] = best.feature;
     }
   }
   __syncthreads();
-  if (warp != 0) return;
-  __threadfence_block();
   // split_info.rs:125-133 — first arg-max leaf under better_than.
-  int bl = -1, bf = 0;
-  double bg = 0.0;
-  for (int i = lane; i < p.num_leaves; i += 32) {
-    double g = J.bgain[i];
-    int32_t fe = J.bfeat[i];
-    if (bl < 0 || better_than(g, fe, bg, bf)) {
-      bl = i;
-      bg = g;
-      bf = fe;
-    }
-  }
+  Pick b{-1, 0, 0, false};
+  for (int i = t; i < p.num_leaves; i += kSearchThreads) leaf_pick(b, make_pick(i, J.bgain[i], J.bfeat[i]));
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    int oi = __shfl_xor_sync(FULL, bl, o);
-    double og = __shfl_xor_sync(FULL, bg, o);
-    int of = __shfl_xor_sync(FULL, bf, o);
-    if (oi >= 0) {
-      if (bl < 0 || better_than(og, of, bg, bf) || (!better_than(bg, bf, og, of) && oi < bl)) {
-        bl = oi;
-        bg = og;
-        bf = of;
-      }
-    }
-  }
-  const Cand info = J.best[bl];
-  if ((!(info.gain > 0.0) && !isnan(info.gain)) || info.inner < 0) {  // serial.rs:611 — gain <= 0 stops
+  for (int o = 16; o > 0; o >>= 1) leaf_pick(b, shfl_pick(b, o));
+  if (lane == 0) s_p[warp] = b;
+  __syncthreads();
+  if (warp != 0) return;
+  Pick w = lane < kSearchWarps ? s_p[lane] : Pick{-1, 0, 0, false};
+#pragma unroll
+  for (int o = 4; o > 0; o >>= 1) leaf_pick(w, shfl_pick(w, o));
+  const int32_t win = __shfl_sync(FULL, w.i, 0);
+  const double gain = win >= 0 ? J.best[win].gain : 0.0;
+  const int32_t inner = win >= 0 ? J.best[win].inner : -1;
+  if ((!(gain > 0.0) && !isnan(gain)) || inner < 0) {  // serial.rs:611 — gain <= 0 stops
     if (lane == 0) st->stop = 1;
     return;
   }
-  const DevFeature m = feats[info.inner];
-  for (int b = lane; b < 256; b += 32)
-    st->route[b] = b < m.gbins ? route_bin(m, info.threshold, info.default_left != 0, (uint32_t)b) : 0;
+  const DevFeature m = feats[inner];
+  const uint32_t threshold = J.best[win].threshold;
+  const bool default_left = J.best[win].default_left != 0;
+  for (int bb = lane; bb < 256; bb += 32)
+    st->route[bb] = bb < m.gbins ? route_bin(m, threshold, default_left, (uint32_t)bb) : 0;
   if (lane == 0) {
-    st->split_leaf = bl;
-    st->split_inner = info.inner;
+    st->split_leaf = win;
+    st->split_inner = inner;
     st->new_leaf = st->tree_leaves;
   }
+}
+
+// One CTA per (feature, side): blockIdx.x = 2 * feature + side (0 = smaller leaf). The last CTA to
+// finish runs the fold / arg-max.
+template <bool PLAIN, bool QUANT>
+__global__ void __launch_bounds__(kSearchThreads) k_search(const Job* __restrict__ jobs, Params p,
+                                                           const DevFeature* __restrict__ feats) {
+  __shared__ SearchSmem sm;
+  __shared__ int last;
+  const Job& J = jobs[blockIdx.z];
+  JobState* st = J.st;
+  if (st->stop) return;  // uniform over the grid
+  const int side = (int)(blockIdx.x & 1u);
+  const int f = (int)(blockIdx.x >> 1);
+  const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
+  if (st->do_search && J.used[f] && leaf >= 0) {  // uniform over the CTA
+    const DevFeature m = feats[f];
+    if (QUANT)
+      search_int<PLAIN>(J, p, st, m, side, f, leaf, sm);
+    else
+      search_float<PLAIN>(J, p, st, m, side, f, leaf, sm);
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned c = atomicAdd(&st->search_done, 1u);
+    last = c == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  decide_body(J, p, feats);
+  if (threadIdx.x == 0) st->search_done = 0u;
 }
 
 // Root of a tree (serial.rs:658-776 after the root sums, then :580-586 and the first
@@ -801,17 +1057,16 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
 }  // namespace
 
 void launch_search(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s) {
-  dim3 grid((unsigned)ceil_div64(2 * p.F, 2), 1, num_jobs);
+  dim3 grid((unsigned)(2 * p.F), 1, num_jobs);
   const bool plain = !p.use_l1 && !p.use_max && !p.use_smooth;
   if (p.quant) {
-    if (plain) k_search<true, true><<<grid, 64, 0, s>>>(d_jobs, p, feats);
-    else k_search<false, true><<<grid, 64, 0, s>>>(d_jobs, p, feats);
+    if (plain) k_search<true, true><<<grid, kSearchThreads, 0, s>>>(d_jobs, p, feats);
+    else k_search<false, true><<<grid, kSearchThreads, 0, s>>>(d_jobs, p, feats);
   } else {
-    if (plain) k_search<true, false><<<grid, 64, 0, s>>>(d_jobs, p, feats);
-    else k_search<false, false><<<grid, 64, 0, s>>>(d_jobs, p, feats);
+    if (plain) k_search<true, false><<<grid, kSearchThreads, 0, s>>>(d_jobs, p, feats);
+    else k_search<false, false><<<grid, kSearchThreads, 0, s>>>(d_jobs, p, feats);
   }
 }
-
 
 void launch_tree_begin(const Job* d_jobs, int num_jobs, const Params& p, cudaStream_t s) {
   k_tree_begin<<<dim3(1, 1, num_jobs), 256, 0, s>>>(d_jobs, p);
