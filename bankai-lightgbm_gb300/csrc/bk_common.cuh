@@ -42,7 +42,7 @@ struct Cand {
   int64_t lint, rint;
   int32_t feature, inner;
   uint32_t threshold;
-  int32_t left_count, right_count, default_left, splittable, _pad;
+  int32_t left_count, right_count, default_left, splittable, missing;  // missing: the feature's missing type
 };
 
 // LeafSplits (serial.rs:53-76).
@@ -57,7 +57,7 @@ struct Params {
   int32_t min_data, fused, use_l1, use_max, use_smooth, quant;
   int32_t const_hess, num_leaves, max_depth, F;
   int32_t T, B, quant_bins, stochastic;
-  int32_t renew, part_grid, _p0, _p1;
+  int32_t renew, part_grid, pdl, _p1;  // pdl: launch the grow-loop kernels with programmatic dependence
   int64_t n;
 };
 
@@ -76,7 +76,8 @@ struct JobState {
   int32_t stop, do_search, tree_leaves, disc_ok;
   int32_t smaller_leaf, larger_leaf, smaller_slot, larger_slot;
   int32_t parent_slot, use_subtract, next_free, split_leaf;
-  int32_t split_inner, new_leaf, use_rows, _p0;
+  int32_t split_inner, new_leaf, use_rows;
+  uint32_t split_thr;  // threshold of the chosen split | default_left << 31
   int64_t root_count, total_left;
   double gscale, hscale, inv_g, inv_h;
   double root_output;
@@ -85,7 +86,6 @@ struct JobState {
   int64_t hist_rows_direct, hist_rows_gather, hist_builds;  // work done by the histogram kernels
   uint32_t search_done, part_done;  // CTAs finished in the current search / scatter launch
   uint32_t mt[624];
-  uint8_t route[256];
 };
 
 // Device pointers of one job.
@@ -102,12 +102,14 @@ struct Job {
   int32_t* leaf_depth;
   int32_t* leaf_slot;
   LeafSum* leaf_sum;
-  Cand* best;          // [L]
-  double* bgain;       // [L]   gain of best[] (compact copy for the arg-max)
-  int32_t* bfeat;      // [L]   real feature of best[]
-  Cand* cand;          // [2][F]
-  double* cgain;       // [2][F] gain of cand[] (compact copy for the fold)
-  uint8_t* csplit;     // [2][F] splittable flag of cand[]
+  double* bgain;       // [L]   gain of each leaf's best split (the arg-max reads these)
+  int32_t* bfeat;      // [L]   real feature of each leaf's best split
+  Cand* cand;          // [L][F] the candidate of every searched (leaf, feature); a leaf's best split is
+                       //        cand[leaf][inner feature of bsplit[leaf]]
+  double* cgain;       // [2][F] gains of the current search's candidates (compact copy for the fold)
+  uint8_t* csplit;     // [2][F] splittable flags of the current search's candidates
+  uint32_t* cthr;      // [2][F] threshold | default_left << 31 of cand[]
+  int64_t* bsplit;     // [L]   inner feature << 32 | threshold | default_left << 31 of each leaf's best split
   LeafConst* lconst;   // [2]   constants of the smaller / larger leaf of the current search
   uint8_t* splittable; // [L][F]
   uint8_t* used;       // [F]

@@ -19,12 +19,8 @@ __device__ __forceinline__ void before_find_best_split(const Job& J, const Param
   if (go && nr < p.min_data * 2 && nl < p.min_data * 2) go = false;
   if (!go) {
     if (lane == 0) {
-      J.best[left].gain = -CUDART_INF;
       J.bgain[left] = -CUDART_INF;
-      if (right >= 0) {
-        J.best[right].gain = -CUDART_INF;
-        J.bgain[right] = -CUDART_INF;
-      }
+      if (right >= 0) J.bgain[right] = -CUDART_INF;
       st->do_search = 0;
     }
     return;
@@ -93,8 +89,8 @@ __device__ __forceinline__ void post_split_body(const Job& J, const Params& p, c
   const int64_t hdir = st->hist_rows_direct, hgat = st->hist_rows_gather, hbld = st->hist_builds;
   const int64_t b = J.leaf_begin[bl], c = J.leaf_count[bl];
   const int32_t buf = J.leaf_buf[bl], depth = J.leaf_depth[bl], pslot = J.leaf_slot[bl];
-  Cand info = J.best[bl];
-  const int32_t miss = feats[info.inner].missing;
+  Cand info = J.cand[(size_t)bl * p.F + st->split_inner];  // the chosen leaf's best split
+  const int32_t miss = info.missing;
   // ---- the split (serial.rs:1685-1876) ----
   const int64_t R = c - L;
   info.left_count = (int32_t)L;
@@ -137,13 +133,11 @@ __device__ __forceinline__ void post_split_body(const Job& J, const Params& p, c
     J.leaf_depth[bl] = nd;
     J.leaf_sum[bl] = LeafSum{info.lsg, info.lsh, info.left_output, info.lint, info.left_count, 0};
     J.leaf_sum[nl] = LeafSum{info.rsg, info.rsh, info.right_output, info.rint, info.right_count, 0};
-    if (!go) info.gain = -CUDART_INF;  // no search for the children: both leaves drop out
-    J.best[bl] = info;
-    J.bgain[bl] = info.gain;
+    // the children's bests come from their search; without one both leaves drop out
+    J.bgain[bl] = -CUDART_INF;
     J.bfeat[bl] = info.feature;
     st->tree_leaves = tl + 1;
     if (!go) {
-      J.best[nl].gain = -CUDART_INF;
       J.bgain[nl] = -CUDART_INF;
       st->do_search = 0;
     } else {

@@ -23,13 +23,16 @@
 //
 // The last CTA of tile 0 also computes the per-leaf constants of the search that follows
 // (bk_leaf.cuh) before its own rows.
+#include "bk_launch.cuh"
 #include "bk_leaf.cuh"
 
 namespace bk {
 
 namespace {
 
-constexpr int kMinChunk = 4096;
+// At least one round (32 warps x 32 rows) per CTA: small leaves spread over as many SMs as they
+// can fill, since a round costs the SM's shared-atomic throughput, not its DRAM share.
+constexpr int kMinChunk = 1024;
 
 __device__ __forceinline__ float two_sum_err(float a, float b, float s) {
   float bb = __fsub_rn(s, a);
@@ -90,6 +93,9 @@ __device__ __forceinline__ RoundLoad load_round_int(const uint8_t* tb, const int
   return L;
 }
 
+// The gradient half of a 16:16 hot counter (grad * 65536 + hess, hess in [0, 65536)).
+__device__ __forceinline__ int32_t hot_g(uint32_t s) { return ((int32_t)s - (int32_t)(s & 0xffffu)) >> 16; }
+
 template <bool WIDE>
 __device__ __forceinline__ void add_row(uint32_t* hot, int32_t* cold_g, int32_t* cold_h, uint32_t bin, int32_t v,
                                         int lane) {
@@ -106,11 +112,18 @@ __global__ void __launch_bounds__(1024, 1)
     k_hist_int(const Job* __restrict__ jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile,
                int flush_rounds) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const int B = p.B;
+  // the shared histogram is zeroed while the previous kernel of the grow loop finishes
+  {
+    uint4* z = reinterpret_cast<uint4*>(smem);
+    const int n16 = (WIDE ? 2 : 3) * B * TILE / 4;
+    for (int e = threadIdx.x; e < n16; e += blockDim.x) z[e] = make_uint4(0, 0, 0, 0);
+  }
+  griddep_wait();
   const Job& J = jobs[blockIdx.z];
   hist_leaf_constants(J, p);
   Range R;
   if (!cta_range(J, p, blocks_per_tile, &R)) return;
-  const int B = p.B;
   const int tile = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
@@ -118,11 +131,6 @@ __global__ void __launch_bounds__(1024, 1)
   int32_t* cold_h = cold_g + B * TILE;
   uint4* stage = reinterpret_cast<uint4*>(cold_h + B * TILE);
   int32_t* stage_v = reinterpret_cast<int32_t*>(stage + nwarps * 64);
-  for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
-    if (!WIDE) hot[e] = 0u;
-    cold_g[e] = 0;
-    cold_h[e] = 0;
-  }
   __syncthreads();
   const uint8_t* tb = bins_rt + (size_t)tile * (size_t)p.n * TILE;
   const int16_t* packed = J.packed;
@@ -173,27 +181,45 @@ __global__ void __launch_bounds__(1024, 1)
       __syncwarp();
     }
     cur = nxt;
-    if (!WIDE && (--until_flush == 0 || rd + 1 == rounds)) {
+    // fold the 16:16 counters into the 32-bit ones before either half can overflow (the last
+    // round's counters are folded by the final flush below)
+    if (!WIDE && --until_flush == 0 && rd + 1 < rounds) {
       until_flush = flush_rounds;
       __syncthreads();
-      for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
-        int32_t s = (int32_t)hot[e];
-        if (s) {
-          int32_t hh = s & 0xffff;
-          int32_t gg = (s - hh) >> 16;
-          cold_g[e] += gg;
-          cold_h[e] += hh;
-          hot[e] = 0u;
+      uint4* hot4 = reinterpret_cast<uint4*>(hot);
+      int4* g4 = reinterpret_cast<int4*>(cold_g);
+      int4* h4 = reinterpret_cast<int4*>(cold_h);
+      for (int e = threadIdx.x; e < B * TILE / 4; e += blockDim.x) {
+        const uint4 s = hot4[e];
+        if (s.x | s.y | s.z | s.w) {
+          int4 g = g4[e], h = h4[e];
+          g.x += hot_g(s.x);
+          g.y += hot_g(s.y);
+          g.z += hot_g(s.z);
+          g.w += hot_g(s.w);
+          h.x += (int32_t)(s.x & 0xffffu);
+          h.y += (int32_t)(s.y & 0xffffu);
+          h.z += (int32_t)(s.z & 0xffffu);
+          h.w += (int32_t)(s.w & 0xffffu);
+          g4[e] = g;
+          h4[e] = h;
+          hot4[e] = make_uint4(0, 0, 0, 0);
         }
       }
       __syncthreads();
     }
   }
-  if (WIDE) __syncthreads();
+  griddep_launch();  // only the flush is left: the next kernel may be scheduled
+  __syncthreads();
   unsigned long long* slot = reinterpret_cast<unsigned long long*>(J.pool) +
                              ((size_t)J.st->smaller_slot * p.T + tile) * (size_t)B * TILE;
   for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
     int32_t gg = cold_g[e], hh = cold_h[e];
+    if (!WIDE) {
+      const uint32_t s = hot[e];
+      gg += hot_g(s);
+      hh += (int32_t)(s & 0xffffu);
+    }
     if (gg | hh) {
       int64_t pk = (int64_t)gg * 4294967296LL + (int64_t)hh;
       atomicAdd(slot + e, (unsigned long long)pk);
@@ -205,11 +231,17 @@ template <bool CONST_HESS>
 __global__ void __launch_bounds__(1024, 1)
     k_hist_float(const Job* __restrict__ jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile) {
   extern __shared__ __align__(16) unsigned char smem[];
+  const int B = p.B;
+  {
+    uint4* z = reinterpret_cast<uint4*>(smem);
+    const int n16 = (CONST_HESS ? 3 : 4) * B * TILE / 4;
+    for (int e = threadIdx.x; e < n16; e += blockDim.x) z[e] = make_uint4(0, 0, 0, 0);
+  }
+  griddep_wait();
   const Job& J = jobs[blockIdx.z];
   hist_leaf_constants(J, p);
   Range R;
   if (!cta_range(J, p, blocks_per_tile, &R)) return;
-  const int B = p.B;
   const int tile = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   float* ghi = reinterpret_cast<float*>(smem);
@@ -219,16 +251,6 @@ __global__ void __launch_bounds__(1024, 1)
   uint4* stage = reinterpret_cast<uint4*>(CONST_HESS ? hlo : hlo + B * TILE);
   float2* stage_v = reinterpret_cast<float2*>(stage + nwarps * 64);
   uint32_t* hcnt = reinterpret_cast<uint32_t*>(hhi);
-  for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
-    ghi[e] = 0.f;
-    glo[e] = 0.f;
-    if (CONST_HESS) {
-      hcnt[e] = 0u;
-    } else {
-      hhi[e] = 0.f;
-      hlo[e] = 0.f;
-    }
-  }
   __syncthreads();
   const uint8_t* tb = bins_rt + (size_t)tile * (size_t)p.n * TILE;
   const bool feat_lane = tile * TILE + lane < p.F;
@@ -287,6 +309,7 @@ __global__ void __launch_bounds__(1024, 1)
     }
     __syncwarp();
   }
+  griddep_launch();
   __syncthreads();
   double2* slot = reinterpret_cast<double2*>(J.pool) + ((size_t)J.st->smaller_slot * p.T + tile) * (size_t)B * TILE;
   const double h0 = CONST_HESS ? (double)H[0] : 0.0;
@@ -317,13 +340,17 @@ void launch_hist(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t
   dim3 grid(hl.blocks_per_tile, p.T, num_jobs);
   if (p.quant) {
     if (hl.flush_rounds > 0)
-      k_hist_int<false><<<grid, hl.threads, hl.smem, s>>>(d_jobs, p, bins_rt, hl.blocks_per_tile, hl.flush_rounds);
+      (void)launch_kernel(k_hist_int<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, d_jobs, p, bins_rt,
+                        hl.blocks_per_tile, hl.flush_rounds);
     else
-      k_hist_int<true><<<grid, hl.threads, hl.smem, s>>>(d_jobs, p, bins_rt, hl.blocks_per_tile, 1);
+      (void)launch_kernel(k_hist_int<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, d_jobs, p, bins_rt,
+                        hl.blocks_per_tile, 1);
   } else if (p.const_hess) {
-    k_hist_float<true><<<grid, hl.threads, hl.smem, s>>>(d_jobs, p, bins_rt, hl.blocks_per_tile);
+    (void)launch_kernel(k_hist_float<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, d_jobs, p, bins_rt,
+                      hl.blocks_per_tile);
   } else {
-    k_hist_float<false><<<grid, hl.threads, hl.smem, s>>>(d_jobs, p, bins_rt, hl.blocks_per_tile);
+    (void)launch_kernel(k_hist_float<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, d_jobs, p, bins_rt,
+                      hl.blocks_per_tile);
   }
 }
 

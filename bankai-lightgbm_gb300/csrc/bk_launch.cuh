@@ -1,0 +1,33 @@
+// Kernel launches of the grow loop with programmatic dependent launch: each grow-loop kernel is
+// launched with programmatic stream serialization, so it is scheduled while the kernel before it
+// finishes. It runs its independent prologue (shared-memory setup), then waits in griddep_wait()
+// until the previous grid has completed and its writes are visible. Each kernel calls
+// griddep_launch() when only its serial tail is left (the histogram's flush, the search's and the
+// scatter's last-CTA bookkeeping), which lets the next kernel be scheduled then. Without the
+// launch attribute (or when the previous stream operation is not a kernel) both are no-ops.
+#pragma once
+#include <cuda_runtime.h>
+
+namespace bk {
+
+__device__ __forceinline__ void griddep_wait() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+__device__ __forceinline__ void griddep_launch() { asm volatile("griddepcontrol.launch_dependents;" ::: "memory"); }
+
+// cudaLaunchKernelEx with (pdl != 0) the programmatic-stream-serialization attribute.
+template <typename... KArgs, typename... Args>
+inline cudaError_t launch_kernel(void (*kern)(KArgs...), dim3 grid, dim3 block, size_t smem, cudaStream_t s, int pdl,
+                                 Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute attr[1];
+  attr[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  attr[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = pdl ? attr : nullptr;
+  cfg.numAttrs = pdl ? 1 : 0;
+  return cudaLaunchKernelEx(&cfg, kern, static_cast<KArgs>(args)...);
+}
+
+}  // namespace bk

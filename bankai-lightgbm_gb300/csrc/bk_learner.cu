@@ -305,6 +305,7 @@ int bk_learner_create(const bk_feature* features, int32_t num_features, const ui
     p.use_max = c->max_delta_step > 0.0;
     p.use_smooth = c->path_smooth > BK_EPS;
     p.quant = quant ? 1 : 0;
+    p.pdl = 1;
     p.const_hess = c->is_constant_hessian ? 1 : 0;
     p.num_leaves = c->num_leaves;
     p.max_depth = c->max_depth;
@@ -424,12 +425,13 @@ int bk_learner_create(const bk_feature* features, int32_t num_features, const ui
       J.leaf_depth = L->dalloc<int32_t>(Lv);
       J.leaf_slot = L->dalloc<int32_t>(Lv);
       J.leaf_sum = L->dalloc<LeafSum>(Lv);
-      J.best = L->dalloc<Cand>(Lv);
       J.bgain = L->dalloc<double>(Lv);
       J.bfeat = L->dalloc<int32_t>(Lv);
-      J.cand = L->dalloc<Cand>(2 * (size_t)F);
+      J.cand = L->dalloc<Cand>((size_t)Lv * F);
       J.cgain = L->dalloc<double>(2 * (size_t)F);
       J.csplit = L->dalloc<uint8_t>(2 * (size_t)F);
+      J.cthr = L->dalloc<uint32_t>(2 * (size_t)F);
+      J.bsplit = L->dalloc<int64_t>(Lv);
       J.lconst = L->dalloc<LeafConst>(2);
       J.splittable = L->dalloc<uint8_t>((size_t)Lv * F);
       J.used = L->dalloc<uint8_t>(F);
@@ -619,6 +621,19 @@ int bk_learner_set_loop_mode(bk_learner* L, int32_t mode) {
     return -1;
   }
   L->loop_mode = mode;
+  return 0;
+}
+
+int bk_learner_set_launch_overlap(bk_learner* L, int32_t on) {
+  if (!L) {
+    set_error("bk_learner_set_launch_overlap: null learner");
+    return -1;
+  }
+  if ((on != 0) != (L->p.pdl != 0) && L->graph_exec) {
+    cudaGraphExecDestroy(L->graph_exec);
+    L->graph_exec = nullptr;
+  }
+  L->p.pdl = on != 0;
   return 0;
 }
 

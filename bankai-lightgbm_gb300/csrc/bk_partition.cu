@@ -2,13 +2,14 @@
 // split leaf's row-index range into the left rows (kept in leaf order) followed by the right
 // rows (kept in leaf order), written into the other index buffer.
 //
-// The reference routes each row through SplitRule::route_bin; here k_decide evaluates that rule
-// once per stored bin into a 256-entry route table, so routing a row is one byte read of the
-// split feature's column-major bins plus one shared-memory lookup. Two kernels on a fixed grid
+// The reference routes each row through SplitRule::route_bin; here every CTA evaluates that rule
+// once per stored bin into a 256-entry shared route table, so routing a row is one byte read of
+// the split feature's column-major bins plus one shared-memory lookup. Two kernels on a fixed grid
 // (so the step can be captured in a CUDA graph while the leaf size varies): count the left rows
 // of each CTA's contiguous chunk; then scatter, each CTA summing the counts of the chunks before
 // its own (at most a few hundred) and ordering its rows with block-wide scans.
 #include "bk_grow.cuh"
+#include "bk_launch.cuh"
 
 namespace bk {
 
@@ -70,19 +71,44 @@ __device__ __forceinline__ T block_excl_scan(T v, T* total, T* sh) {
   return excl;
 }
 
+// The route of every stored bin of the chosen split (data_partition.rs:299-410), one per thread.
+__device__ __forceinline__ void build_route(const JobState* st, const DevFeature* feats, uint8_t* lut) {
+  const DevFeature m = feats[st->split_inner];
+  const uint32_t th = st->split_thr;
+  const uint32_t b = threadIdx.x;
+  lut[b] = (int)b < m.gbins ? route_bin(m, th & 0x7fffffffu, (th >> 31) != 0, b) : 0;
+}
+
 __global__ void __launch_bounds__(kThreads) k_part_count(const Job* __restrict__ jobs, Params p,
-                                                         const uint8_t* __restrict__ bins_cm) {
+                                                         const uint8_t* __restrict__ bins_cm,
+                                                         const DevFeature* __restrict__ feats) {
   __shared__ uint8_t lut[256];
   __shared__ int64_t sh[32];
+  griddep_wait();
   const Job& J = jobs[blockIdx.z];
   if (J.st->stop) return;
-  lut[threadIdx.x] = J.st->route[threadIdx.x];
-  __syncthreads();
   PartRange R;
-  part_range(J, p, bins_cm, &R);
-  if ((int)blockIdx.x >= R.active) return;  // no rows: the scatter reads only active CTAs' counts
+  part_range(J, p, bins_cm, &R);  // its loads are in flight with the route table's
+  build_route(J.st, feats, lut);
+  __syncthreads();
+  if ((int)blockIdx.x >= R.active) {  // no rows: the scatter reads only active CTAs' counts
+    griddep_launch();
+    return;
+  }
+  // per tile: every row index first, then every bin byte, so a tile costs two memory round trips
   int64_t local = 0;
-  for (int64_t i = R.r0 + threadIdx.x; i < R.r1; i += kThreads) local += lut[R.col[R.src[i]]];
+  for (int64_t base = R.r0; base < R.r1; base += kThreads * kItems) {
+    int32_t rows[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+      const int64_t e = base + (int64_t)k * kThreads + threadIdx.x;
+      rows[k] = e < R.r1 ? __ldg(R.src + e) : -1;
+    }
+#pragma unroll
+    for (int k = 0; k < kItems; ++k)
+      if (rows[k] >= 0) local += lut[__ldg(R.col + rows[k])];
+  }
+  griddep_launch();
   int64_t total;
   block_excl_scan<int64_t>(local, &total, sh);
   if (threadIdx.x == 0) J.part_cnt[blockIdx.x] = total;
@@ -93,13 +119,14 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict
                                                            const DevFeature* __restrict__ feats) {
   __shared__ uint8_t lut[256];
   __shared__ int32_t sh[32];
+  griddep_wait();
   const Job& J = jobs[blockIdx.z];
   if (J.st->stop) return;
-  lut[threadIdx.x] = J.st->route[threadIdx.x];
-  __syncthreads();
   __shared__ int64_t sh64[32];
   PartRange R;
-  part_range(J, p, bins_cm, &R);
+  part_range(J, p, bins_cm, &R);  // its loads are in flight with the route table's
+  build_route(J.st, feats, lut);
+  __syncthreads();
   // left rows before this chunk, and in total
   int64_t before = 0, all = 0;
   const bool active = (int)blockIdx.x < R.active;
@@ -120,17 +147,13 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict
     uint32_t flags = 0;
     int32_t cnt = 0;
 #pragma unroll
-    for (int k = 0; k < kItems; ++k) {
-      int64_t e = e0 + k;
-      rows[k] = 0;
-      if (e < R.r1) {
-        rows[k] = R.src[e];
-        if (lut[R.col[rows[k]]]) {
-          flags |= 1u << k;
-          ++cnt;
-        }
+    for (int k = 0; k < kItems; ++k) rows[k] = e0 + k < R.r1 ? __ldg(R.src + e0 + k) : -1;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k)
+      if (rows[k] >= 0 && lut[__ldg(R.col + rows[k])]) {
+        flags |= 1u << k;
+        ++cnt;
       }
-    }
     int32_t tile_total;
     int32_t pre = block_excl_scan<int32_t>(cnt, &tile_total, sh);
     int64_t left_before = running + pre;
@@ -148,6 +171,7 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict
     }
     running += tile_total;
   }
+  griddep_launch();  // only the last CTA's bookkeeping is left: the next histogram may be scheduled
   // the last CTA of the launch applies the split to the leaf records (bk_grow.cuh)
   __shared__ int last;
   __syncthreads();
@@ -168,8 +192,8 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict
 void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
                       const DevFeature* feats, cudaStream_t s) {
   dim3 grid(p.part_grid, 1, num_jobs);
-  k_part_count<<<grid, kThreads, 0, s>>>(d_jobs, p, bins_cm);
-  k_part_scatter<<<grid, kThreads, 0, s>>>(d_jobs, p, bins_cm, feats);
+  (void)launch_kernel(k_part_count, grid, dim3(kThreads), 0, s, p.pdl, d_jobs, p, bins_cm, feats);
+  (void)launch_kernel(k_part_scatter, grid, dim3(kThreads), 0, s, p.pdl, d_jobs, p, bins_cm, feats);
 }
 
 }  // namespace bk

@@ -27,6 +27,7 @@
 #include <math_constants.h>
 
 #include "bk_grow.cuh"
+#include "bk_launch.cuh"
 #include "bk_leaf.cuh"
 #include "bk_math.cuh"
 
@@ -100,11 +101,12 @@ __device__ __forceinline__ bool dnan(double x) {
 // first evaluated in fp32 together with a rigorous bound E on |fp32 - f64|: the inputs'
 // conversions (about 2 units of 2^-24 each), the squares, the divisions (__fdividef: at most 2 ulp
 // for divisors in [2^-126, 2^126]) and the sum add up to about 9 units of 2^-24 relative to the
-// non-negative result, the fp32 comparisons against E one more; E uses 48. Only the candidates
-// that can still be the best (fp32 + E >= the best certified lower bound of their direction) or,
-// while no candidate certainly passes, whose pass / fail against min_gain_shift is uncertain are
-// evaluated in f64, so the chosen split, its gain and the splittable flag are exactly the
-// reference's.
+// non-negative result, the fp32 comparisons against E one more; E uses 48. The largest gain G* of
+// a direction is at least the best certified lower bound M over its valid thresholds, so only the
+// thresholds whose upper bound reaches M (and exceeds min_gain_shift) can hold it, and the
+// direction is splittable exactly when G* passes min_gain_shift. Those few thresholds (and any
+// whose fp32 evaluation is uncertain) are evaluated in f64, so the chosen split, its gain and the
+// splittable flag are exactly the reference's.
 constexpr float kPrefilterRel = 48.0f * 5.9604645e-08f;
 
 struct Approx {
@@ -186,18 +188,75 @@ __device__ __forceinline__ ScanGeom scan_geom(const DevFeature& m) {
 __device__ __forceinline__ bool earlier(int d, int ta, int tb) { return d == 0 ? ta > tb : ta < tb; }
 
 // The best position of one direction within a warp (and, combined, within the CTA).
+// Everything a candidate threshold contributes to its SplitInfo: the gain, the left / right sums,
+// counts and outputs.
+struct Eval {
+  double gain, lsg, lsh, rsg, rsh, lo, ro;
+  int32_t lc, rc;
+  int64_t lint, rint;
+};
+
 struct DirBest {
   long long key;  // dkey of the gain; kNoKey when no position qualified
-  double gain;    // -inf when none
   int64_t a, b;   // int: left (grad, hess) sums; float: bit patterns of the accumulated (grad, hess)
   int32_t t, c;   // position; float: accumulated count
+  Eval ev;        // ev.gain: -inf when none
 };
+
+
+// The chosen threshold's SplitInfo: lane 0 evaluates the left side, lane 1 the right side, in one
+// instruction stream (FindBestThresholdInt's output assembly, feature_histogram.rs:700-830: 32-bit
+// conversions of the packed sums, exact since they fit in 32 bits).
+__device__ __forceinline__ Eval eval_int(const Params& p, int64_t lg, int64_t lh, int64_t tg, int64_t th, double gs,
+                                         double hs, double cnt_factor, double parent, double gain, int lane) {
+  const int64_t rg = tg - lg, rh = th - lh;
+  const int64_t sg = lane == 0 ? lg : rg, sh = lane == 0 ? lh : rh;
+  const double dg = (double)(int32_t)sg * gs, dh = (double)(uint32_t)sh * hs;
+  const int32_t n = round_int((double)(uint32_t)sh * cnt_factor);
+  const double out = lane < 2 ? split_output(p, dg, dh, n, parent) : 0.0;
+  Eval v;
+  v.gain = gain;
+  v.lsg = dg;
+  v.lsh = dh;
+  v.lc = n;
+  v.lo = out;
+  v.rsg = __shfl_sync(FULL, dg, 1);
+  v.rsh = __shfl_sync(FULL, dh, 1);
+  v.rc = __shfl_sync(FULL, n, 1);
+  v.ro = __shfl_sync(FULL, out, 1);
+  v.lint = (int64_t)(((uint64_t)lg << 32) | ((uint64_t)lh & 0xffffffffull));
+  v.rint = (int64_t)(((uint64_t)rg << 32) | ((uint64_t)rh & 0xffffffffull));
+  return v;
+}
+
+// FindBestThreshold's output assembly (feature_histogram.rs:240-357): (ag, ah, c) is the
+// accumulated side of direction d (0: right, 1: left); the right side of the outputs derives from
+// the left sums. Lane 0 evaluates the left output, lane 1 the right one.
+__device__ __forceinline__ Eval eval_float(const Params& p, int d, double ag, double ah, int32_t c, double sum_g,
+                                           double sum_h, int32_t num_data, double parent, double gain, int lane) {
+  const double slg = d == 0 ? sum_g - ag : ag, slh = d == 0 ? sum_h - ah : ah;
+  const int32_t lc = d == 0 ? num_data - c : c;
+  const double sg = lane == 0 ? slg : sum_g - slg, sh = lane == 0 ? slh : sum_h - slh;
+  const int32_t n = lane == 0 ? lc : num_data - lc;
+  const double out = lane < 2 ? split_output(p, sg, sh, n, parent) : 0.0;
+  Eval v;
+  v.gain = gain;
+  v.lsg = slg;
+  v.lsh = slh - BK_EPS;
+  v.lc = lc;
+  v.lo = out;
+  v.rsg = sum_g - slg;
+  v.rsh = (sum_h - slh) - BK_EPS;
+  v.rc = num_data - lc;
+  v.ro = __shfl_sync(FULL, out, 1);
+  v.lint = v.rint = 0;
+  return v;
+}
 
 // One direction's stop / prefilter summary of a warp (published before one barrier).
 struct WarpFilt {
   int32_t lb;      // the warp's first `break` position in scan order (kNoneLo / kNoneHi: none)
   int32_t mb, ma;  // best certified fp32 lower-bound key of positions before lb / of all positions
-  int32_t cb, ca;  // some position before lb / some position certainly passes min_gain_shift
 };
 
 constexpr int kNoneLo = -0x7fffffff, kNoneHi = 0x7fffffff;
@@ -209,11 +268,12 @@ struct QEnt {
   int16_t t, d;  // position, direction
 };
 
-constexpr int kQueueCap = 2 * kSearchThreads;  // every position of both directions
-
 struct SearchSmem {
-  QEnt q[kQueueCap];
-  int32_t qn;
+  QEnt q[2][kSearchThreads];  // per direction: every position at most once
+  int32_t qn[2];
+  DirBest pres[2];            // per direction: the arg-max of the queued positions
+  int32_t psplit[2];
+  Eval pev[2];                // per direction: the outputs of its only queued position
   int64_t wi[2][kSearchWarps];
   double wd[10][kSearchWarps];
   int32_t wc[3][kSearchWarps];
@@ -231,69 +291,85 @@ __device__ __forceinline__ void warp_best(int d, bool elig, double gain, int t, 
   if (km == kNoKey) {
     if (lane == 0) {
       w->key = kNoKey;
-      w->gain = -CUDART_INF;
+      w->ev.gain = -CUDART_INF;
       w->t = 0;
     }
     return;
   }
   const bool at = elig && key == km;
   const int tb = d == 0 ? __reduce_max_sync(FULL, at ? t : kNoneLo) : __reduce_min_sync(FULL, at ? t : kNoneHi);
-  if (at && t == tb) *w = DirBest{km, gain, a, b, t, c};
+  if (at && t == tb) {
+    w->key = km;
+    w->a = a;
+    w->b = b;
+    w->t = t;
+    w->c = c;
+    w->ev.gain = gain;
+  }
 }
 
 // Warp 0 after the barrier: the CTA's best of each direction (lane 0: direction 0, lane 8:
 // direction 1), broadcast to every lane of the warp.
 __device__ __forceinline__ void combine_best(const SearchSmem& sm, int lane, DirBest (&r)[2], int (&split)[2]) {
   const int d = (lane >> 3) & 1;
-  DirBest e;
-  e.key = kNoKey;
-  e.gain = -CUDART_INF;
-  e.a = e.b = 0;
-  e.t = e.c = 0;
+  long long key = kNoKey;
+  double gain = -CUDART_INF;
+  int64_t a = 0, b = 0;
+  int32_t t = 0, c = 0;
   int sp = 0;
   if (lane < 16) {
-    e = sm.wb[d][lane & 7];
-    if (e.key == kNoKey) e.gain = -CUDART_INF;
+    const DirBest& e = sm.wb[d][lane & 7];
+    key = e.key;
+    if (key != kNoKey) {
+      gain = e.ev.gain;
+      a = e.a;
+      b = e.b;
+      t = e.t;
+      c = e.c;
+    }
     sp = sm.spl[d][lane & 7];
   }
 #pragma unroll
   for (int o = 1; o < 8; o <<= 1) {
-    DirBest x;
-    x.key = __shfl_xor_sync(FULL, e.key, o);
-    x.gain = __shfl_xor_sync(FULL, e.gain, o);
-    x.a = __shfl_xor_sync(FULL, e.a, o);
-    x.b = __shfl_xor_sync(FULL, e.b, o);
-    x.t = __shfl_xor_sync(FULL, e.t, o);
-    x.c = __shfl_xor_sync(FULL, e.c, o);
+    const long long xk = __shfl_xor_sync(FULL, key, o);
+    const double xg = __shfl_xor_sync(FULL, gain, o);
+    const int64_t xa = __shfl_xor_sync(FULL, a, o), xb = __shfl_xor_sync(FULL, b, o);
+    const int32_t xt = __shfl_xor_sync(FULL, t, o), xc = __shfl_xor_sync(FULL, c, o);
     sp |= __shfl_xor_sync(FULL, sp, o);
-    if (x.key > e.key || (x.key == e.key && x.key != kNoKey && earlier(d, x.t, e.t))) e = x;
+    if (xk > key || (xk == key && xk != kNoKey && earlier(d, xt, t))) {
+      key = xk;
+      gain = xg;
+      a = xa;
+      b = xb;
+      t = xt;
+      c = xc;
+    }
   }
 #pragma unroll
   for (int k = 0; k < 2; ++k) {
     const int src = 8 * k;
-    r[k].key = __shfl_sync(FULL, e.key, src);
-    r[k].gain = __shfl_sync(FULL, e.gain, src);
-    r[k].a = __shfl_sync(FULL, e.a, src);
-    r[k].b = __shfl_sync(FULL, e.b, src);
-    r[k].t = __shfl_sync(FULL, e.t, src);
-    r[k].c = __shfl_sync(FULL, e.c, src);
+    r[k].key = __shfl_sync(FULL, key, src);
+    r[k].ev.gain = __shfl_sync(FULL, gain, src);
+    r[k].a = __shfl_sync(FULL, a, src);
+    r[k].b = __shfl_sync(FULL, b, src);
+    r[k].t = __shfl_sync(FULL, t, src);
+    r[k].c = __shfl_sync(FULL, c, src);
     split[k] |= __shfl_sync(FULL, sp, src);
   }
 }
 
-// The fp32 view of one position: certainly passes (cp) with certified lower-bound key lo, maybe
-// passes (mp), and its upper-bound key up.
+// The fp32 view of one position: certified lower-bound key lo, upper-bound key up, and whether it
+// may pass min_gain_shift (mp).
 struct Filt {
-  bool cp, mp, unc;
+  bool mp, unc;
   int32_t lo, up;
 };
 
 __device__ __forceinline__ Filt filt_of(bool cand, const Approx& a, const LeafConst& C) {
   Filt f;
   f.unc = a.uncertain;
-  f.cp = cand && !a.uncertain && __fsub_rn(a.g, a.e) > C.mgs_up;
   f.mp = cand && (a.uncertain || __fadd_rn(a.g, a.e) > C.mgs_dn);
-  f.lo = f.cp ? float_key(__fsub_rn(a.g, a.e)) : float_key(-CUDART_INF_F);
+  f.lo = (cand && !a.uncertain) ? float_key(__fsub_rn(a.g, a.e)) : float_key(-CUDART_INF_F);
   f.up = a.uncertain ? 0 : float_key(__fadd_rn(a.g, a.e));
   return f;
 }
@@ -306,54 +382,43 @@ __device__ __forceinline__ void publish_dir(SearchSmem& sm, int d, bool brk, int
   WarpFilt w;
   w.lb = lb;
   w.mb = w.ma = float_key(-CUDART_INF_F);
-  w.cb = w.ca = 0;
   if (PLAIN) {
     const bool none = d == 0 ? lb == kNoneLo : lb == kNoneHi;
     const bool before = none || (d == 0 ? pos > lb : pos < lb);
     w.ma = __reduce_max_sync(FULL, f.lo);
     w.mb = __reduce_max_sync(FULL, before ? f.lo : float_key(-CUDART_INF_F));
-    w.ca = __any_sync(FULL, f.cp);
-    w.cb = __any_sync(FULL, f.cp && before);
   }
   if (lane == 0) sm.wf[d][warp] = w;
 }
 
 // After the barrier: direction d's stop S (the first `break` in scan order; positions from it on
-// are invalid), and over the valid positions the best certified lower bound M and whether one
-// certainly passes. Warp w holds positions 32w .. 32w + 31; the forward scan's position -1 (when
-// `has_x`) comes first in its scan order.
+// are invalid) and the best certified lower bound M over the valid positions. Warp w holds
+// positions 32w .. 32w + 31; the forward scan's position -1 (when `has_x`) comes first in its
+// scan order. The maximal gain G* of the direction is at least M, so only positions whose upper
+// bound reaches M can hold it; and any position passes min_gain_shift exactly when G* does.
 template <bool PLAIN>
-__device__ __forceinline__ void resolve_dir(const SearchSmem& sm, int d, bool has_x, int* S, int32_t* M,
-                                            int* certain) {
+__device__ __forceinline__ void resolve_dir(const SearchSmem& sm, int d, bool has_x, int* S, int32_t* M) {
   int s = d == 0 ? kNoneLo : kNoneHi;
 #pragma unroll
   for (int w = 0; w < kSearchWarps; ++w) s = d == 0 ? max(s, sm.wf[d][w].lb) : min(s, sm.wf[d][w].lb);
   if (d == 1 && has_x && sm.xf.lb == -1) s = -1;
   *S = s;
   int32_t m = float_key(-CUDART_INF_F);
-  int c = 0;
   if (PLAIN) {
     const bool none = d == 0 ? s == kNoneLo : s == kNoneHi;
-    if (d == 1 && has_x && s != -1) {
-      m = sm.xf.ma;
-      c = sm.xf.ca;
-    }
+    if (d == 1 && has_x && s != -1) m = sm.xf.ma;
 #pragma unroll
     for (int w = 0; w < kSearchWarps; ++w) {
       const WarpFilt& f = sm.wf[d][w];
       const bool contains = !none && f.lb == s;
       const bool all_before = none || (d == 0 ? 32 * w > s : 32 * w + 31 < s);
-      if (contains) {
+      if (contains)
         m = max(m, f.mb);
-        c |= f.cb;
-      } else if (all_before) {
+      else if (all_before)
         m = max(m, f.ma);
-        c |= f.ca;
-      }
     }
   }
   *M = m;
-  *certain = c;
 }
 
 // !(gain <= mgs) without an f64 comparison.
@@ -364,66 +429,138 @@ __device__ __forceinline__ bool is_neg_inf(double x) {
   return (unsigned long long)__double_as_longlong(x) == 0xfff0000000000000ULL;
 }
 
-// Appends this thread's entry (when `push`) to the CTA's queue, one shared atomic per warp.
-__device__ __forceinline__ void queue_push(SearchSmem& sm, bool push, const QEnt& e, int lane) {
+// Appends this thread's entry (when `push`) to direction d's queue, one shared atomic per warp.
+__device__ __forceinline__ void queue_push(SearchSmem& sm, int d, bool push, const QEnt& e, int lane) {
   const unsigned bal = __ballot_sync(FULL, push);
   int base = 0;
-  if (lane == 0 && bal) base = atomicAdd(&sm.qn, __popc(bal));
+  if (lane == 0 && bal) base = atomicAdd(&sm.qn[d], __popc(bal));
   base = __shfl_sync(FULL, base, 0);
-  if (push) sm.q[base + __popc(bal & ((1u << lane) - 1u))] = e;
+  if (push) sm.q[d][base + __popc(bal & ((1u << lane) - 1u))] = e;
 }
 
-// Warp 0: the f64 gains of the queued positions, 32 at a time; per direction the arg-max (highest
-// gain, ties to the earliest position in scan order) and whether any queued position passed.
+// One warp: the f64 gains of direction d's queued positions, 32 at a time; their arg-max (highest
+// gain, ties to the earliest position in scan order) and whether any passed, into sm.pres[d] /
+// sm.psplit[d]. The two directions run on two warps (two schedulers): f64 issue throughput is
+// the bottleneck on this part.
 template <typename Gain>
-__device__ __forceinline__ void eval_queue(const SearchSmem& sm, int lane, double mgs, DirBest (&r)[2],
-                                           int (&split)[2], Gain gain_of) {
-#pragma unroll
-  for (int d = 0; d < 2; ++d) {
-    r[d].key = kNoKey;
-    r[d].gain = -CUDART_INF;
-    r[d].a = r[d].b = 0;
-    r[d].t = d == 0 ? kNoneLo : kNoneHi;
-    r[d].c = 0;
-  }
-  const int n = sm.qn;
+__device__ __forceinline__ void eval_dir(SearchSmem& sm, int d, int lane, double mgs, Gain gain_of) {
+  DirBest r;
+  r.key = kNoKey;
+  r.ev.gain = -CUDART_INF;
+  r.a = r.b = 0;
+  r.t = d == 0 ? kNoneLo : kNoneHi;
+  r.c = 0;
+  int split = 0;
+  const int n = sm.qn[d];
   for (int b0 = 0; b0 < n; b0 += 32) {
     const bool have = b0 + lane < n;
     QEnt e;
     e.a = e.b = 0;
     e.c = 0;
     e.t = 0;
-    e.d = -1;
-    if (have) e = sm.q[b0 + lane];
+    e.d = (int16_t)d;
+    if (have) e = sm.q[d][b0 + lane];
     const double g = have ? gain_of(e) : -CUDART_INF;
     const bool passed = have && gain_passes(g, mgs);
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      const bool mine = have && e.d == d;
-      if (__any_sync(FULL, mine && passed)) split[d] = 1;
-      const bool elig = mine && passed && !dnan(g) && !is_neg_inf(g);  // NaN never wins
-      const long long k = warp_max64(elig ? dkey(g) : kNoKey);
-      if (k == kNoKey) continue;
-      const bool at = elig && dkey(g) == k;
-      const int tb = d == 0 ? __reduce_max_sync(FULL, at ? (int)e.t : kNoneLo)
-                            : __reduce_min_sync(FULL, at ? (int)e.t : kNoneHi);
-      const int wl = __ffs(__ballot_sync(FULL, at && (int)e.t == tb)) - 1;
-      if (k > r[d].key || (k == r[d].key && earlier(d, tb, r[d].t))) {
-        r[d].key = k;
-        r[d].t = tb;
-        r[d].gain = __shfl_sync(FULL, g, wl);
-        r[d].a = __shfl_sync(FULL, e.a, wl);
-        r[d].b = __shfl_sync(FULL, e.b, wl);
-        r[d].c = __shfl_sync(FULL, e.c, wl);
-      }
+    if (__any_sync(FULL, passed)) split = 1;
+    const bool elig = passed && !dnan(g) && !is_neg_inf(g);  // NaN never wins
+    const long long k = warp_max64(elig ? dkey(g) : kNoKey);
+    if (k == kNoKey) continue;
+    const bool at = elig && dkey(g) == k;
+    const int tb = d == 0 ? __reduce_max_sync(FULL, at ? (int)e.t : kNoneLo)
+                          : __reduce_min_sync(FULL, at ? (int)e.t : kNoneHi);
+    const int wl = __ffs(__ballot_sync(FULL, at && (int)e.t == tb)) - 1;
+    if (k > r.key || (k == r.key && earlier(d, tb, r.t))) {
+      r.key = k;
+      r.t = tb;
+      r.ev.gain = __shfl_sync(FULL, g, wl);
+      r.a = __shfl_sync(FULL, e.a, wl);
+      r.b = __shfl_sync(FULL, e.b, wl);
+      r.c = __shfl_sync(FULL, e.c, wl);
     }
+  }
+  if (lane == 0) {
+    sm.pres[d] = r;
+    sm.psplit[d] = split;
   }
 }
 
-__device__ __forceinline__ void store_cand(const Job& J, const Params& p, int side, int32_t f, const Cand& c) {
-  J.cand[side * p.F + f] = c;
+// After the queues are filled (barrier 3): warps 0 / 1 evaluate the two directions' gains; warps
+// 2 / 3 evaluate, for a direction with a single queued position, that position's outputs (it is
+// the direction's only possible choice). Barrier 4, then warp 0 holds every result.
+template <typename Gain, typename Side>
+__device__ __forceinline__ void eval_queues(SearchSmem& sm, int warp, int lane, double mgs, Gain gain_of,
+                                            Side side_of) {
+  if (warp < 2) {
+    eval_dir(sm, warp, lane, mgs, gain_of);
+  } else if (warp < 4) {
+    const int d = warp - 2;
+    if (sm.qn[d] == 1) {
+      const Eval v = side_of(sm.q[d][0]);
+      if (lane == 0) sm.pev[d] = v;
+    }
+  }
+  __syncthreads();
+}
+
+__device__ __forceinline__ void store_cand(const Job& J, const Params& p, int side, int32_t leaf, int32_t f,
+                                           const Cand& c) {
+  J.cand[(size_t)leaf * p.F + f] = c;
   J.cgain[side * p.F + f] = c.gain;
   J.csplit[side * p.F + f] = (uint8_t)c.splittable;
+  J.cthr[side * p.F + f] = c.threshold | ((uint32_t)(c.default_left != 0) << 31);
+}
+
+// The combination of the directions (feature_histogram.rs:240-357, :700-830): the reverse scan
+// first, the forward scan replaces it only with a strictly larger gain; then the chosen threshold's
+// SplitInfo (`eval_of(best, direction)`), the penalty and the feature's candidate record. Warp 0,
+// every lane with the same values.
+template <typename EvalOf>
+__device__ __forceinline__ void finish_cand(const Job& J, const Params& p, const DevFeature& m, int side, int32_t leaf,
+                                            int32_t f, const ScanGeom& G, double mgs, const DirBest (&r)[2],
+                                            const int (&rs)[2], int lane, EvalOf eval_of) {
+  const int nd = G.two ? 2 : 1;
+  int sp = 0, ch = -1;
+  double cgain = -CUDART_INF;
+  for (int i = 0; i < nd; ++i) {
+    sp |= rs[i];
+    if (rs[i] && r[i].ev.gain > cgain + mgs) {
+      ch = i;
+      cgain = r[i].ev.gain - mgs;
+    }
+  }
+  Cand c;
+  cand_reset(&c, m.real, f);
+  if (ch >= 0) {
+    // field-wise selects keep the chosen direction in registers
+    DirBest b;
+    b.key = ch == 0 ? r[0].key : r[1].key;
+    b.a = ch == 0 ? r[0].a : r[1].a;
+    b.b = ch == 0 ? r[0].b : r[1].b;
+    b.c = ch == 0 ? r[0].c : r[1].c;
+    b.t = ch == 0 ? r[0].t : r[1].t;
+    b.ev.gain = ch == 0 ? r[0].ev.gain : r[1].ev.gain;
+    const Eval e = eval_of(b, ch);
+    const int32_t t = b.t;
+    c.threshold = (uint32_t)(ch == 0 ? t - 1 + G.off : t + G.off);
+    c.left_output = e.lo;
+    c.left_count = e.lc;
+    c.lsg = e.lsg;
+    c.lsh = e.lsh;
+    c.right_output = e.ro;
+    c.right_count = e.rc;
+    c.rsg = e.rsg;
+    c.rsh = e.rsh;
+    c.lint = e.lint;
+    c.rint = e.rint;
+    c.gain = cgain;
+    c.default_left = ch == 0 ? 1 : 0;
+  }
+  if (nd == 1 && m.missing == 2) c.default_left = 0;
+  c.gain *= m.penalty;
+  c.splittable = sp;
+  c.missing = m.missing;
+  if (lane == 0) store_cand(J, p, side, leaf, f, c);
 }
 
 // FindBestThresholdInt for one (leaf, feature): feature_histogram.rs:673-830, scans :839-1142.
@@ -447,7 +584,7 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
   const int64_t sv = (in && !(fix && t == m.mfb)) ? hs[(size_t)(t + 1) * TILE] : 0;
   const int64_t lv = (side && in) ? hl[(size_t)(t + 1) * TILE] : 0;
   const ScanGeom G = scan_geom(m);
-  if (t == 0) sm.qn = 0;
+  if (t < 2) sm.qn[t] = 0;
   const bool skip_t = G.skip && t + G.off == m.default_bin;
   const bool acc_t = !skip_t && t <= G.tf_r;  // bin t is accumulated by the scans
   const int64_t v0 = side ? lv - sv : sv;     // before the most-frequent bin's fix
@@ -510,37 +647,42 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
   publish_dir<PLAIN>(sm, 0, brk0, t, fl[0], lane, warp);
   {
     Filt nat = fl[1];
-    if (xpos) nat.cp = false;  // the natural position 255 is never a candidate
+    if (xpos) nat.lo = float_key(-CUDART_INF_F);  // the natural position 255 is never a candidate
     publish_dir<PLAIN>(sm, 1, brk1, t, nat, lane, warp);
   }
   if (xpos) {
     WarpFilt x;
     x.lb = brkx ? -1 : kNoneHi;
     x.ma = x.mb = fl[1].lo;
-    x.ca = x.cb = fl[1].cp;
     sm.xf = x;
   }
   __syncthreads();
-  int S[2], certain[2];
+  int S[2];
   int32_t M[2];
-  resolve_dir<PLAIN>(sm, 0, false, &S[0], &M[0], &certain[0]);
-  resolve_dir<PLAIN>(sm, 1, G.fwd_rest, &S[1], &M[1], &certain[1]);
+  resolve_dir<PLAIN>(sm, 0, false, &S[0], &M[0]);
+  resolve_dir<PLAIN>(sm, 1, G.fwd_rest, &S[1], &M[1]);
   const bool valid[2] = {first0 && t > S[0], xpos ? (firstx && S[1] != -1) : (first1 && t < S[1])};
   DirBest r[2];
-  int rs[2] = {PLAIN ? certain[0] : 0, PLAIN ? certain[1] : 0};
+  int rs[2] = {0, 0};
   if (PLAIN) {
-    // barrier 3: the few positions that need their f64 gain, evaluated together by warp 0
+    // barrier 3: the few positions that need their f64 gain; barrier 4: evaluated on four warps
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
-      const bool exact = valid[d] && fl[d].mp && (fl[d].unc || fl[d].up >= M[d]);
-      queue_push(sm, exact, QEnt{lg[d], lh[d], 0, (int16_t)(d == 0 || !xpos ? t : -1), (int16_t)d}, lane);
+      const bool exact = valid[d] && (fl[d].unc || (fl[d].mp && fl[d].up >= M[d]));
+      queue_push(sm, d, exact, QEnt{lg[d], lh[d], 0, (int16_t)(d == 0 || !xpos ? t : -1), (int16_t)d}, lane);
     }
     __syncthreads();
-    if (warp != 0) return;
     const double gs = st->gscale, hsc = st->hscale;
-    eval_queue(sm, lane, C.mgs, r, rs, [&](const QEnt& e) {
-      return int_split_gain(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, true);
-    });
+    eval_queues(
+        sm, warp, lane, C.mgs,
+        [&](const QEnt& e) { return int_split_gain(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, true); },
+        [&](const QEnt& e) { return eval_int(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, 0.0, lane); });
+    if (warp != 0) return;
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      r[d] = sm.pres[d];
+      rs[d] = sm.psplit[d];
+    }
   } else {
     // every valid position evaluates its own f64 gain; barrier 3: the arg-max
     double gain[2];
@@ -565,47 +707,15 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
     if (warp != 0) return;
     combine_best(sm, lane, r, rs);
   }
-  // FindBestThresholdInt's combination of the directions (feature_histogram.rs:700-830): the
-  // reverse scan first, the forward scan replaces it only with a strictly larger gain
-  const double mgs = C.mgs, gs = st->gscale, hsc = st->hscale;
-  const int nd = G.two ? 2 : 1;
-  int sp = 0, ch = -1;
-  double cgain = -CUDART_INF;
-  for (int i = 0; i < nd; ++i) {
-    sp |= rs[i];
-    if (rs[i] && r[i].gain > cgain + mgs) {
-      ch = i;
-      cgain = r[i].gain - mgs;
+  // FindBestThresholdInt's combination of the directions (feature_histogram.rs:700-830)
+  finish_cand(J, p, m, side, leaf, f, G, C.mgs, r, rs, lane, [&](const DirBest& b, int d) {
+    if (PLAIN && sm.qn[d] == 1) {  // evaluated by warp 2 + d
+      Eval v = sm.pev[d];
+      v.gain = b.ev.gain;
+      return v;
     }
-  }
-  Cand c;
-  cand_reset(&c, m.real, f);
-  if (ch >= 0) {
-    const DirBest& b = ch == 0 ? r[0] : r[1];
-    const int64_t rg = tg - b.a, rh = th - b.b;
-    // lane 0 computes the left output, lane 1 the right one
-    const double sg1 = (double)(int32_t)(lane == 0 ? b.a : rg) * gs;
-    const double sh1 = (double)(uint32_t)(lane == 0 ? b.b : rh) * hsc;
-    const int32_t n1 = round_int((double)(uint32_t)(lane == 0 ? b.b : rh) * C.cnt_factor);
-    const double out = lane < 2 ? split_output(p, sg1, sh1, n1, C.parent) : 0.0;
-    c.threshold = (uint32_t)(ch == 0 ? b.t - 1 + G.off : b.t + G.off);
-    c.left_output = out;
-    c.left_count = n1;
-    c.lsg = sg1;
-    c.lsh = sh1;
-    c.right_output = __shfl_sync(FULL, out, 1);
-    c.right_count = __shfl_sync(FULL, n1, 1);
-    c.rsg = __shfl_sync(FULL, sg1, 1);
-    c.rsh = __shfl_sync(FULL, sh1, 1);
-    c.lint = (int64_t)(((uint64_t)b.a << 32) | ((uint64_t)b.b & 0xffffffffull));
-    c.rint = (int64_t)(((uint64_t)rg << 32) | ((uint64_t)rh & 0xffffffffull));
-    c.gain = cgain;
-    c.default_left = ch == 0 ? 1 : 0;
-  }
-  if (nd == 1 && m.missing == 2) c.default_left = 0;
-  c.gain *= m.penalty;
-  c.splittable = sp;
-  if (lane == 0) store_cand(J, p, side, f, c);
+    return eval_int(p, b.a, b.b, tg, th, st->gscale, st->hscale, C.cnt_factor, C.parent, b.ev.gain, lane);
+  });
 }
 
 // FindBestThreshold (float) for one (leaf, feature): feature_histogram.rs:219-357, scans
@@ -630,7 +740,7 @@ __device__ void search_float(const Job& J, const Params& p, const JobState* st, 
   double2 sv = (in && !(fix && t == m.mfb)) ? hs[(size_t)(t + 1) * TILE] : zero;
   const double2 lv = (side && in) ? hl[(size_t)(t + 1) * TILE] : zero;
   const ScanGeom G = scan_geom(m);
-  if (t == 0) sm.qn = 0;
+  if (t < 2) sm.qn[t] = 0;
   const double sum_g = C.sum_g, sum_h = C.sum_h;
   if (fix) {  // one barrier for both sums
     const double ag = warp_sum(sv.x), ah = warp_sum(sv.y);
@@ -750,24 +860,23 @@ __device__ void search_float(const Job& J, const Params& p, const JobState* st, 
   publish_dir<PLAIN>(sm, 0, brk0, t, fl[0], lane, warp);
   {
     Filt nat = fl[1];
-    if (xpos) nat.cp = false;
+    if (xpos) nat.lo = float_key(-CUDART_INF_F);
     publish_dir<PLAIN>(sm, 1, brk1, t, nat, lane, warp);
   }
   if (xpos) {
     WarpFilt x;
     x.lb = brkx ? -1 : kNoneHi;
     x.ma = x.mb = fl[1].lo;
-    x.ca = x.cb = fl[1].cp;
     sm.xf = x;
   }
   __syncthreads();
-  int S[2], certain[2];
+  int S[2];
   int32_t M[2];
-  resolve_dir<PLAIN>(sm, 0, false, &S[0], &M[0], &certain[0]);
-  resolve_dir<PLAIN>(sm, 1, G.fwd_rest, &S[1], &M[1], &certain[1]);
+  resolve_dir<PLAIN>(sm, 0, false, &S[0], &M[0]);
+  resolve_dir<PLAIN>(sm, 1, G.fwd_rest, &S[1], &M[1]);
   const bool valid[2] = {first0 && t > S[0], xpos ? (firstx && S[1] != -1) : (first1 && t < S[1])};
   DirBest r[2];
-  int rs[2] = {PLAIN ? certain[0] : 0, PLAIN ? certain[1] : 0};
+  int rs[2] = {0, 0};
   // carried per position: the accumulated side's sums (reverse: right, forward: left)
   const int64_t ca[2] = {__double_as_longlong(rg), __double_as_longlong(fg)};
   const int64_t cb[2] = {__double_as_longlong(rh), __double_as_longlong(fh)};
@@ -779,15 +888,23 @@ __device__ void search_float(const Job& J, const Params& p, const JobState* st, 
     return split_gains(p, ag, ah, sum_g - ag, sum_h - ah, e.c, num_data - e.c, C.parent);
   };
   if (PLAIN) {
-    // barrier 3: the few positions that need their f64 gain, evaluated together by warp 0
+    // barrier 3: the few positions that need their f64 gain; barrier 4: evaluated on four warps
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
-      const bool exact = valid[d] && fl[d].mp && (fl[d].unc || fl[d].up >= M[d]);
-      queue_push(sm, exact, QEnt{ca[d], cb[d], cc[d], (int16_t)(d == 0 || !xpos ? t : -1), (int16_t)d}, lane);
+      const bool exact = valid[d] && (fl[d].unc || (fl[d].mp && fl[d].up >= M[d]));
+      queue_push(sm, d, exact, QEnt{ca[d], cb[d], cc[d], (int16_t)(d == 0 || !xpos ? t : -1), (int16_t)d}, lane);
     }
     __syncthreads();
+    eval_queues(sm, warp, lane, C.mgs, gain_of, [&](const QEnt& e) {
+      return eval_float(p, e.d, __longlong_as_double(e.a), __longlong_as_double(e.b), e.c, sum_g, sum_h, num_data,
+                        C.parent, 0.0, lane);
+    });
     if (warp != 0) return;
-    eval_queue(sm, lane, C.mgs, r, rs, gain_of);
+#pragma unroll
+    for (int d = 0; d < 2; ++d) {
+      r[d] = sm.pres[d];
+      rs[d] = sm.psplit[d];
+    }
   } else {
     double gain[2];
     bool split[2], elig[2];
@@ -811,45 +928,15 @@ __device__ void search_float(const Job& J, const Params& p, const JobState* st, 
     combine_best(sm, lane, r, rs);
   }
   // FindBestThreshold's combination of the directions (feature_histogram.rs:240-357)
-  const double mgs = C.mgs;
-  const int nd = G.two ? 2 : 1;
-  int sp = 0, ch = -1;
-  double cgain = -CUDART_INF;
-  for (int i = 0; i < nd; ++i) {
-    sp |= rs[i];
-    if (rs[i] && r[i].gain > cgain + mgs) {
-      ch = i;
-      cgain = r[i].gain - mgs;
+  finish_cand(J, p, m, side, leaf, f, G, C.mgs, r, rs, lane, [&](const DirBest& b, int d) {
+    if (PLAIN && sm.qn[d] == 1) {  // evaluated by warp 2 + d
+      Eval v = sm.pev[d];
+      v.gain = b.ev.gain;
+      return v;
     }
-  }
-  Cand c;
-  cand_reset(&c, m.real, f);
-  if (ch >= 0) {
-    const DirBest& b = ch == 0 ? r[0] : r[1];
-    const double ag = __longlong_as_double(b.a), ah = __longlong_as_double(b.b);
-    const double bslg = ch == 0 ? sum_g - ag : ag, bslh = ch == 0 ? sum_h - ah : ah;
-    const int32_t blc = ch == 0 ? num_data - b.c : b.c;
-    // lane 0 computes the left output, lane 1 the right one
-    const double sg1 = lane == 0 ? bslg : sum_g - bslg;
-    const double sh1 = lane == 0 ? bslh : sum_h - bslh;
-    const int32_t n1 = lane == 0 ? blc : num_data - blc;
-    const double out = lane < 2 ? split_output(p, sg1, sh1, n1, C.parent) : 0.0;
-    c.threshold = (uint32_t)(ch == 0 ? b.t - 1 + G.off : b.t + G.off);
-    c.left_output = out;
-    c.left_count = blc;
-    c.lsg = bslg;
-    c.lsh = bslh - BK_EPS;
-    c.right_output = __shfl_sync(FULL, out, 1);
-    c.right_count = num_data - blc;
-    c.rsg = sum_g - bslg;
-    c.rsh = (sum_h - bslh) - BK_EPS;
-    c.gain = cgain;
-    c.default_left = ch == 0 ? 1 : 0;
-  }
-  if (nd == 1 && m.missing == 2) c.default_left = 0;
-  c.gain *= m.penalty;
-  c.splittable = sp;
-  if (lane == 0) store_cand(J, p, side, f, c);
+    return eval_float(p, d, __longlong_as_double(b.a), __longlong_as_double(b.b), b.c, sum_g, sum_h, num_data,
+                      C.parent, b.ev.gain, lane);
+  });
 }
 
 // ---- the fold and the leaf arg-max on integer keys ----
@@ -865,9 +952,11 @@ __device__ __forceinline__ bool better_k(long long ka, bool na, int fa, long lon
 }
 
 struct Pick {
-  int i, f;  // index (-1: none), real feature
-  long long k;
+  int i, f;     // index (-1: none), real feature
+  long long k;  // dkey of the gain
   bool nan;
+  double g;     // the gain
+  long long pay;  // fold: threshold | default_left << 31; leaf arg-max: the split descriptor
 };
 
 // Fold step: `a` comes first in the sequential order; `b` replaces it only when strictly better;
@@ -885,103 +974,115 @@ __device__ __forceinline__ void leaf_pick(Pick& a, const Pick& b) {
     a = b;
 }
 
-__device__ __forceinline__ Pick shfl_pick(const Pick& a, int o) {
+__device__ __forceinline__ Pick shfl_pick(const Pick& a, int src_or_mask, bool xor_mode) {
   Pick b;
-  b.i = __shfl_xor_sync(FULL, a.i, o);
-  b.f = __shfl_xor_sync(FULL, a.f, o);
-  b.k = __shfl_xor_sync(FULL, a.k, o);
-  b.nan = __shfl_xor_sync(FULL, (int)a.nan, o) != 0;
+  if (xor_mode) {
+    b.i = __shfl_xor_sync(FULL, a.i, src_or_mask);
+    b.f = __shfl_xor_sync(FULL, a.f, src_or_mask);
+    b.k = __shfl_xor_sync(FULL, a.k, src_or_mask);
+    b.nan = __shfl_xor_sync(FULL, (int)a.nan, src_or_mask) != 0;
+    b.g = __shfl_xor_sync(FULL, a.g, src_or_mask);
+    b.pay = __shfl_xor_sync(FULL, a.pay, src_or_mask);
+  } else {
+    b.i = __shfl_sync(FULL, a.i, src_or_mask);
+    b.f = __shfl_sync(FULL, a.f, src_or_mask);
+    b.k = __shfl_sync(FULL, a.k, src_or_mask);
+    b.nan = __shfl_sync(FULL, (int)a.nan, src_or_mask) != 0;
+    b.g = __shfl_sync(FULL, a.g, src_or_mask);
+    b.pay = __shfl_sync(FULL, a.pay, src_or_mask);
+  }
   return b;
 }
 
-__device__ __forceinline__ Pick make_pick(int i, double g, int f) { return Pick{i, f, dkey(g), dnan(g)}; }
-
-// Cand is 8-byte aligned and its size a multiple of 8 (not of 16): copy it in 8-byte words.
-static_assert(sizeof(Cand) % 8 == 0 && alignof(Cand) == 8, "Cand is copied in 8-byte words");
-__device__ __forceinline__ Cand load_cand_cg(const Cand* c) {
-  Cand r;
-  const unsigned long long* src = reinterpret_cast<const unsigned long long*>(c);
-  unsigned long long* dst = reinterpret_cast<unsigned long long*>(&r);
-#pragma unroll
-  for (int i = 0; i < (int)(sizeof(Cand) / 8); ++i) dst[i] = __ldcg(src + i);
-  return r;
+__device__ __forceinline__ Pick make_pick(int i, double g, int f, long long pay) {
+  return Pick{i, f, dkey(g), dnan(g), g, pay};
 }
 
 // The fold of the searched leaves' candidates and the leaf arg-max, run by the last CTA of the
-// search launch. Everything written by other CTAs of the launch is read through L2 (__ldcg).
+// search launch. Every load is issued up front (the candidates of both searched leaves and every
+// other leaf's best), then one barrier; warp 0 finishes. Everything written by other CTAs of the
+// launch is read through L2 (__ldcg). A leaf's best split stays in cand[leaf][feature]; the
+// partition builds the route table of the chosen split from (split_inner, split_thr).
 __device__ void decide_body(const Job& J, const Params& p, const DevFeature* feats) {
-  __shared__ Pick s_p[kSearchWarps];
+  __shared__ Pick s_f[kSearchWarps], s_l[kSearchWarps];
   JobState* st = J.st;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   constexpr int kHalf = kSearchThreads / 2;
   const bool searched = st->do_search != 0;
+  const int32_t leaf0 = st->smaller_leaf, leaf1 = st->larger_leaf;
+  const Pick none{-1, 0x7fffffff, 0, false, 0.0, 0};
+  // serial.rs:1523-1558 — fold the candidates of each searched leaf in feature order: the first
+  // half of the CTA folds the smaller leaf, the second half the larger one
+  Pick a = none;
   if (searched) {
-    // serial.rs:1523-1558 — fold the candidates of each searched leaf in feature order: the first
-    // half of the CTA folds the smaller leaf, the second half the larger one
     const int side = t / kHalf;
-    const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
+    const int32_t leaf = side ? leaf1 : leaf0;
     const int32_t slot = side ? st->larger_slot : st->smaller_slot;
-    Pick a{-1, 0x7fffffff, 0, false};
     if (leaf >= 0) {
       for (int f = t % kHalf; f < p.F; f += kHalf) {
         const uint8_t u = J.used[f];
         const uint8_t cs = __ldcg(&J.csplit[side * p.F + f]);
         const double g = __ldcg(&J.cgain[side * p.F + f]);
+        const uint32_t th = __ldcg(&J.cthr[side * p.F + f]);
         const int real = feats[f].real;
         if (!u) continue;
         J.splittable[(size_t)slot * p.F + f] = cs;
-        pick(a, make_pick(f, g, real));
+        pick(a, make_pick(f, g, real, th));
       }
     }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) pick(a, shfl_pick(a, o));
-    if (lane == 0) s_p[warp] = a;
   }
-  __syncthreads();
-  if (searched && t % kHalf == 0) {
-    const int side = t / kHalf;
-    const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
-    if (leaf >= 0) {
-      Pick a{-1, 0x7fffffff, 0, false};
-      for (int w = side * (kSearchWarps / 2); w < (side + 1) * (kSearchWarps / 2); ++w) pick(a, s_p[w]);
-      // the fold starts from SplitInfo::default (gain -inf, feature -1) and replaces it only
-      // with a better candidate
-      Cand best;
-      cand_reset(&best, -1, -1);
-      if (a.i >= 0 && better_k(a.k, a.nan, a.f, dkey(-CUDART_INF), false, -1))
-        best = load_cand_cg(&J.cand[side * p.F + a.i]);
-      J.best[leaf] = best;
-      J.bgain[leaf] = best.gain;
-      J.bfeat[leaf] = best.feature;
-    }
+  // split_info.rs:125-133 — first arg-max leaf under better_than; the searched leaves' new bests
+  // join from the fold
+  Pick b = none;
+  b.f = 0;
+  for (int i = t; i < p.num_leaves; i += kSearchThreads) {
+    if (searched && (i == leaf0 || i == leaf1)) continue;
+    leaf_pick(b, make_pick(i, J.bgain[i], J.bfeat[i], J.bsplit[i]));
   }
-  __syncthreads();
-  // split_info.rs:125-133 — first arg-max leaf under better_than.
-  Pick b{-1, 0, 0, false};
-  for (int i = t; i < p.num_leaves; i += kSearchThreads) leaf_pick(b, make_pick(i, J.bgain[i], J.bfeat[i]));
+  if (searched) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) leaf_pick(b, shfl_pick(b, o));
-  if (lane == 0) s_p[warp] = b;
+    for (int o = 16; o > 0; o >>= 1) pick(a, shfl_pick(a, o, true));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) leaf_pick(b, shfl_pick(b, o, true));
+  if (lane == 0) {
+    s_f[warp] = a;
+    s_l[warp] = b;
+  }
   __syncthreads();
   if (warp != 0) return;
-  Pick w = lane < kSearchWarps ? s_p[lane] : Pick{-1, 0, 0, false};
+  // lanes 0 / 1: the new best of the smaller / larger leaf
+  Pick nb = none;
+  const int32_t my_leaf = lane == 0 ? leaf0 : leaf1;
+  if (searched && lane < 2 && my_leaf >= 0) {
+    Pick fa = none;
+    for (int w = lane * (kSearchWarps / 2); w < (lane + 1) * (kSearchWarps / 2); ++w) pick(fa, s_f[w]);
+    // the fold starts from SplitInfo::default (gain -inf, feature -1) and replaces it only with a
+    // better candidate
+    const bool take = fa.i >= 0 && better_k(fa.k, fa.nan, fa.f, dkey(-CUDART_INF), false, -1);
+    if (take)
+      nb = Pick{my_leaf, fa.f, fa.k, fa.nan, fa.g, (long long)fa.i * 4294967296LL + (long long)(uint32_t)fa.pay};
+    else
+      nb = make_pick(my_leaf, -CUDART_INF, -1, (long long)-1 * 4294967296LL);
+    J.bgain[my_leaf] = nb.g;
+    J.bfeat[my_leaf] = nb.f;
+    J.bsplit[my_leaf] = nb.pay;
+  }
+  // the leaf arg-max over the 8 warp partials (lanes 0..7) and the searched leaves (lanes 8, 9)
+  const Pick moved = shfl_pick(nb, lane & 1, false);
+  Pick w = lane < kSearchWarps ? s_l[lane] : ((lane == 8 || lane == 9) ? moved : none);
 #pragma unroll
-  for (int o = 4; o > 0; o >>= 1) leaf_pick(w, shfl_pick(w, o));
-  const int32_t win = __shfl_sync(FULL, w.i, 0);
-  const double gain = win >= 0 ? J.best[win].gain : 0.0;
-  const int32_t inner = win >= 0 ? J.best[win].inner : -1;
-  if ((!(gain > 0.0) && !isnan(gain)) || inner < 0) {  // serial.rs:611 — gain <= 0 stops
+  for (int o = 16; o > 0; o >>= 1) leaf_pick(w, shfl_pick(w, o, true));
+  const int32_t inner = w.i >= 0 ? (int32_t)(w.pay >> 32) : -1;
+  // serial.rs:611 — a best gain <= 0 stops the tree
+  if ((!w.nan && w.k <= 0) || inner < 0) {
     if (lane == 0) st->stop = 1;
     return;
   }
-  const DevFeature m = feats[inner];
-  const uint32_t threshold = J.best[win].threshold;
-  const bool default_left = J.best[win].default_left != 0;
-  for (int bb = lane; bb < 256; bb += 32)
-    st->route[bb] = bb < m.gbins ? route_bin(m, threshold, default_left, (uint32_t)bb) : 0;
   if (lane == 0) {
-    st->split_leaf = win;
+    st->split_leaf = w.i;
     st->split_inner = inner;
+    st->split_thr = (uint32_t)(w.pay & 0xffffffffLL);
     st->new_leaf = st->tree_leaves;
   }
 }
@@ -993,6 +1094,7 @@ __global__ void __launch_bounds__(kSearchThreads) k_search(const Job* __restrict
                                                            const DevFeature* __restrict__ feats) {
   __shared__ SearchSmem sm;
   __shared__ int last;
+  griddep_wait();
   const Job& J = jobs[blockIdx.z];
   JobState* st = J.st;
   if (st->stop) return;  // uniform over the grid
@@ -1006,6 +1108,7 @@ __global__ void __launch_bounds__(kSearchThreads) k_search(const Job* __restrict
     else
       search_float<PLAIN>(J, p, st, m, side, f, leaf, sm);
   }
+  griddep_launch();  // only the last CTA's fold is left: the partition may be scheduled
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -1031,11 +1134,9 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
     J.leaf_depth[i] = 0;
     J.leaf_slot[i] = -1;
     J.leaf_value[i] = 0.0;
-    Cand c;
-    cand_reset(&c, -1, -1);
-    J.best[i] = c;
-    J.bgain[i] = c.gain;
+    J.bgain[i] = -CUDART_INF;
     J.bfeat[i] = -1;
+    J.bsplit[i] = (int64_t)-1 * 4294967296LL;
   }
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -1059,12 +1160,13 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
 void launch_search(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s) {
   dim3 grid((unsigned)(2 * p.F), 1, num_jobs);
   const bool plain = !p.use_l1 && !p.use_max && !p.use_smooth;
+  const dim3 block(kSearchThreads);
   if (p.quant) {
-    if (plain) k_search<true, true><<<grid, kSearchThreads, 0, s>>>(d_jobs, p, feats);
-    else k_search<false, true><<<grid, kSearchThreads, 0, s>>>(d_jobs, p, feats);
+    if (plain) (void)launch_kernel(k_search<true, true>, grid, block, 0, s, p.pdl, d_jobs, p, feats);
+    else (void)launch_kernel(k_search<false, true>, grid, block, 0, s, p.pdl, d_jobs, p, feats);
   } else {
-    if (plain) k_search<true, false><<<grid, kSearchThreads, 0, s>>>(d_jobs, p, feats);
-    else k_search<false, false><<<grid, kSearchThreads, 0, s>>>(d_jobs, p, feats);
+    if (plain) (void)launch_kernel(k_search<true, false>, grid, block, 0, s, p.pdl, d_jobs, p, feats);
+    else (void)launch_kernel(k_search<false, false>, grid, block, 0, s, p.pdl, d_jobs, p, feats);
   }
 }
 

@@ -45,6 +45,10 @@ class GpuTreeLearner:
     def set_loop_mode(self, mode: int):
         _lib.check(self.lib.bk_learner_set_loop_mode(self.h, int(mode)), "bk_learner_set_loop_mode")
 
+    def set_launch_overlap(self, on: bool):
+        """Programmatic dependent launch of the grow-loop kernels (default on)."""
+        _lib.check(self.lib.bk_learner_set_launch_overlap(self.h, int(bool(on))), "bk_learner_set_launch_overlap")
+
     def set_timing(self, on: bool):
         _lib.check(self.lib.bk_learner_set_timing(self.h, int(bool(on))), "bk_learner_set_timing")
 

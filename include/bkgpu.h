@@ -90,6 +90,10 @@ int bk_learner_row_leaf(bk_learner* learner, int32_t* out);
  * grow loop of an iteration captured once as a CUDA graph and replayed (default). */
 int bk_learner_set_loop_mode(bk_learner* learner, int32_t mode);
 
+/* Grow-loop kernel launches: 1 (default) = each kernel is launched with programmatic dependent
+ * launch, so it is scheduled while the previous kernel finishes; 0 = plain stream order. */
+int bk_learner_set_launch_overlap(bk_learner* learner, int32_t on);
+
 /* Replaces SerialTreeLearner::reset_constant_hessian (serial.rs:279). */
 int bk_learner_reset_constant_hessian(bk_learner* learner, int32_t value);
 
