@@ -98,16 +98,19 @@ __device__ __forceinline__ bool dnan(double x) {
 
 // ---- fp32 prefilter of the plain split gain (no L1 / max_delta_step / path_smooth) ----
 // The reference evaluates gl^2/(hl+l2) + gr^2/(hr+l2) in f64 for every threshold. Each candidate is
-// first evaluated in fp32 together with a rigorous bound E on |fp32 - f64|: the inputs'
-// conversions (about 2 units of 2^-24 each), the squares, the divisions (__fdividef: at most 2 ulp
-// for divisors in [2^-126, 2^126]) and the sum add up to about 9 units of 2^-24 relative to the
-// non-negative result, the fp32 comparisons against E one more; E uses 48. The largest gain G* of
-// a direction is at least the best certified lower bound M over its valid thresholds, so only the
-// thresholds whose upper bound reaches M (and exceeds min_gain_shift) can hold it, and the
-// direction is splittable exactly when G* passes min_gain_shift. Those few thresholds (and any
-// whose fp32 evaluation is uncertain) are evaluated in f64, so the chosen split, its gain and the
-// splittable flag are exactly the reference's.
-constexpr float kPrefilterRel = 48.0f * 5.9604645e-08f;
+// first evaluated in fp32 together with a rigorous bound E on |fp32 - f64| (u = 2^-24): the
+// numerators' conversions and scaling (3u), the denominators' (4u, plus kEpsilon, below 0.02u for
+// denominators >= 1e-6), the square (u), the division (__fdividef: at most 2 ulp = 4u for divisors
+// in [2^-126, 2^126]) and the sum (u) add up to at most 16.1u relative to the non-negative result;
+// the fp32 bound computations round once more. E uses 24u. The largest gain G* of a direction is
+// at least the best certified lower bound M over its valid thresholds, so only the thresholds
+// whose upper bound reaches M (and exceeds min_gain_shift) can hold it, and the direction is
+// splittable exactly when G* passes min_gain_shift. Those few thresholds (and any whose fp32
+// evaluation is uncertain) are evaluated in f64, so the chosen split, its gain and the splittable
+// flag are exactly the reference's. A threshold whose accumulated side gained nothing since its
+// predecessor in scan order (an empty bin between them) has that predecessor's gain exactly and
+// comes after it, so it is never queued.
+constexpr float kPrefilterRel = 24.0f * 5.9604645e-08f;
 
 struct Approx {
   float g, e;
@@ -665,10 +668,14 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
   DirBest r[2];
   int rs[2] = {0, 0};
   if (PLAIN) {
+    // a position whose bin adds nothing repeats its scan predecessor (t + 1 reverse, t - 1 forward)
+    const bool rep[2] = {w == 0 && t + 1 <= G.tf_r && !(G.skip && t + 1 + G.off == m.default_bin),
+                         !xpos && w == 0 && ((t >= 1 && !(G.skip && t - 1 + G.off == m.default_bin)) ||
+                                             (t == 0 && G.fwd_rest))};
     // barrier 3: the few positions that need their f64 gain; barrier 4: evaluated on four warps
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
-      const bool exact = valid[d] && (fl[d].unc || (fl[d].mp && fl[d].up >= M[d]));
+      const bool exact = valid[d] && !rep[d] && (fl[d].unc || (fl[d].mp && fl[d].up >= M[d]));
       queue_push(sm, d, exact, QEnt{lg[d], lh[d], 0, (int16_t)(d == 0 || !xpos ? t : -1), (int16_t)d}, lane);
     }
     __syncthreads();
@@ -888,10 +895,15 @@ __device__ void search_float(const Job& J, const Params& p, const JobState* st, 
     return split_gains(p, ag, ah, sum_g - ag, sum_h - ah, e.c, num_data - e.c, C.parent);
   };
   if (PLAIN) {
+    // a position whose bin adds nothing repeats its scan predecessor (t + 1 reverse, t - 1 forward)
+    const bool empty = wg == 0.0 && wh == 0.0 && wc == 0;
+    const bool rep[2] = {empty && t + 1 <= G.tf_r && !(G.skip && t + 1 + G.off == m.default_bin),
+                         !xpos && empty && ((t >= 1 && !(G.skip && t - 1 + G.off == m.default_bin)) ||
+                                            (t == 0 && G.fwd_rest))};
     // barrier 3: the few positions that need their f64 gain; barrier 4: evaluated on four warps
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
-      const bool exact = valid[d] && (fl[d].unc || (fl[d].mp && fl[d].up >= M[d]));
+      const bool exact = valid[d] && !rep[d] && (fl[d].unc || (fl[d].mp && fl[d].up >= M[d]));
       queue_push(sm, d, exact, QEnt{ca[d], cb[d], cc[d], (int16_t)(d == 0 || !xpos ? t : -1), (int16_t)d}, lane);
     }
     __syncthreads();
