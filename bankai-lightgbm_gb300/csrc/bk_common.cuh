@@ -79,6 +79,7 @@ struct JobState {
   int32_t split_inner, new_leaf, use_rows;
   uint32_t split_thr;  // threshold of the chosen split | default_left << 31
   int64_t root_count, total_left;
+  int64_t part_left, part_right;  // single-pass partition: rows placed from the front / back
   double gscale, hscale, inv_g, inv_h;
   double root_output;
   uint32_t start_pos, red_maxg, red_maxh, red_flags;
@@ -139,7 +140,7 @@ size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide);
 
 void launch_search(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s);
 void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
-                      const DevFeature* feats, cudaStream_t s);
+                      const DevFeature* feats, bool stable, cudaStream_t s);
 
 cudaError_t hist_set_smem_attrs(size_t smem);
 

@@ -189,7 +189,10 @@ struct bk_learner {
     record_hist_event(4 * it + 2);
   }
   void step_b(int it) {
-    launch_partition(d_jobs, K, p, d_bins_cm, d_feat, stream);  // its last CTA also records the split
+    // the plain form keeps the reference's stable compaction; so does leaf renewal, whose f64 sums
+    // run in leaf row order
+    const bool stable = loop_mode == 0 || (p.quant && p.renew);
+    launch_partition(d_jobs, K, p, d_bins_cm, d_feat, stable, stream);  // its last CTA also records the split
     record_hist_event(4 * it + 3);
   }
 

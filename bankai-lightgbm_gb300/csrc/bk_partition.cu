@@ -1,6 +1,8 @@
 // DataPartition::Split (data_partition.rs:124-174), GB300 form: a stable partition of the
 // split leaf's row-index range into the left rows (kept in leaf order) followed by the right
-// rows (kept in leaf order), written into the other index buffer.
+// rows (kept in leaf order), written into the other index buffer. When the rows' order inside a
+// child cannot change any result (no leaf renewal), the batched grow loop uses a single-pass
+// form instead (k_part_onepass, below).
 //
 // The reference routes each row through SplitRule::route_bin; here every CTA evaluates that rule
 // once per stored bin into a 256-entry shared route table, so routing a row is one byte read of
@@ -187,13 +189,95 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict
   if (threadIdx.x == 0) J.st->part_done = 0u;
 }
 
+// Single-pass partition, for when the order of a child's rows inside its range cannot change any
+// result (no leaf renewal: integer histograms, the score update and the row -> leaf map do not
+// depend on it). Each 2048-row tile claims the slots of its left rows from the front of the
+// range and those of its right rows from the back, one atomic each; inside a tile the rows keep
+// their leaf order. No count pass: the last CTA reads the left total and runs the post-split
+// bookkeeping.
+__global__ void __launch_bounds__(kThreads) k_part_onepass(const Job* __restrict__ jobs, Params p,
+                                                           const uint8_t* __restrict__ bins_cm,
+                                                           const DevFeature* __restrict__ feats) {
+  __shared__ uint8_t lut[256];
+  __shared__ int32_t sh[32];
+  __shared__ int64_t s_off[2];
+  __shared__ int last;
+  griddep_wait();
+  const Job& J = jobs[blockIdx.z];
+  JobState* st = J.st;
+  if (st->stop) return;
+  PartRange R;
+  part_range(J, p, bins_cm, &R);  // its loads are in flight with the route table's
+  build_route(st, feats, lut);
+  __syncthreads();
+  for (int64_t base = R.r0; base < R.r1; base += kThreads * kItems) {
+    const int64_t e0 = base + (int64_t)threadIdx.x * kItems;
+    int32_t rows[kItems];
+    uint32_t flags = 0;
+    int32_t cnt = 0;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) rows[k] = e0 + k < R.r1 ? __ldg(R.src + e0 + k) : -1;
+#pragma unroll
+    for (int k = 0; k < kItems; ++k)
+      if (rows[k] >= 0 && lut[__ldg(R.col + rows[k])]) {
+        flags |= 1u << k;
+        ++cnt;
+      }
+    int32_t tile_left;
+    const int32_t pre = block_excl_scan<int32_t>(cnt, &tile_left, sh);
+    const int32_t n = (int32_t)min((int64_t)kThreads * kItems, R.r1 - base);
+    if (threadIdx.x == 0) {
+      s_off[0] = (int64_t)atomicAdd(reinterpret_cast<unsigned long long*>(&st->part_left), (unsigned long long)tile_left);
+      s_off[1] = (int64_t)atomicAdd(reinterpret_cast<unsigned long long*>(&st->part_right),
+                                    (unsigned long long)(n - tile_left));
+    }
+    __syncthreads();
+    // left rows fill [lo, lo + tile_left); right rows fill the tile's slots ending at count - ro
+    int64_t lslot = s_off[0] + pre;
+    int64_t rslot = R.count - s_off[1] - (n - tile_left) + ((int64_t)threadIdx.x * kItems - pre);
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+      if (e0 + k < R.r1) {
+        if (flags & (1u << k))
+          R.dst[lslot++] = rows[k];
+        else
+          R.dst[rslot++] = rows[k];
+      }
+    }
+    __syncthreads();  // s_off is rewritten by the next tile
+  }
+  griddep_launch();  // only the last CTA's bookkeeping is left: the next histogram may be scheduled
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    unsigned t = atomicAdd(&st->part_done, 1u);
+    last = t == gridDim.x - 1;
+  }
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
+  if (threadIdx.x == 0) {
+    st->total_left = __ldcg(&st->part_left);
+    st->part_left = 0;
+    st->part_right = 0;
+    __threadfence();
+  }
+  __syncthreads();
+  if (threadIdx.x < 32) post_split_body(J, p, feats);
+  if (threadIdx.x == 0) st->part_done = 0u;
+}
+
 }  // namespace
 
 void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
-                      const DevFeature* feats, cudaStream_t s) {
+                      const DevFeature* feats, bool stable, cudaStream_t s) {
   dim3 grid(p.part_grid, 1, num_jobs);
-  (void)launch_kernel(k_part_count, grid, dim3(kThreads), 0, s, p.pdl, d_jobs, p, bins_cm, feats);
-  (void)launch_kernel(k_part_scatter, grid, dim3(kThreads), 0, s, p.pdl, d_jobs, p, bins_cm, feats);
+  if (stable) {
+    (void)launch_kernel(k_part_count, grid, dim3(kThreads), 0, s, p.pdl, d_jobs, p, bins_cm, feats);
+    (void)launch_kernel(k_part_scatter, grid, dim3(kThreads), 0, s, p.pdl, d_jobs, p, bins_cm, feats);
+  } else {
+    (void)launch_kernel(k_part_onepass, grid, dim3(kThreads), 0, s, p.pdl, d_jobs, p, bins_cm, feats);
+  }
 }
 
 }  // namespace bk

@@ -259,6 +259,28 @@ def run_gpu(args, rank, world):
     return line
 
 
+def run_hist_traffic(args):
+    """One quantized tree (graph form) on the synthetic workload, for a DRAM-traffic capture of the
+    histogram kernel: prints its algorithmic bytes and launch count, the denominator of
+    HIST_TRAFFIC_PER_BYTE (run under ncu with the dram__bytes_{read,write}.sum metrics and
+    -k regex:k_hist_int, the capture's totals divided by these bytes)."""
+    import torch
+    from lgbm_gb300 import GpuTreeLearner
+    ds, y, _ = build_dataset(args.rows)
+    n = ds.num_data
+    label = torch.from_numpy(y).cuda()
+    learner = GpuTreeLearner(ds, make_cfg(True, args.leaves), loop_mode=1)
+    score = torch.full((n,), float(y.astype(np.float64).mean()), dtype=torch.float64, device="cuda")
+    gbuf, hbuf = learner.gradient_buffers()
+    torch.cuda.synchronize()
+    learner.objective_gradients(0, score.data_ptr(), label.data_ptr())
+    learner.train_raw(gbuf, hbuf, on_device=True)
+    torch.cuda.synchronize()
+    tm = learner.last_timing()
+    learner.close()
+    return {"rows": n, "hist_launches": args.leaves - 1, "hist_alg_bytes": tm["hist_bytes"]}
+
+
 def aggregate_ranks(ms_per_step, world):
     """Replicas: the slowest rank's time per step, and the iterations of all ranks per second."""
     ms = float(ms_per_step)
@@ -334,7 +356,12 @@ def main():
     ap.add_argument("--rows", type=int, default=10_000_000)
     ap.add_argument("--leaves", type=int, default=255)
     ap.add_argument("--cpu-rows", type=int, default=1_000_000)
+    ap.add_argument("--hist-traffic", action="store_true",
+                    help="train one tree and print the histogram kernel's algorithmic bytes (for an ncu capture)")
     args = ap.parse_args()
+    if args.hist_traffic:
+        print(json.dumps(run_hist_traffic(args)))
+        return
     rank = int(os.environ.get("RANK", 0))
     world = int(os.environ.get("WORLD_SIZE", 1))
     if args.impl == "reference":
