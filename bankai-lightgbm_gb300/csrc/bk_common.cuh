@@ -69,6 +69,7 @@ struct LeafConst {
   float mgs_up, mgs_dn;    // min_gain_shift rounded up / down to fp32
   float gsf, hsf, l2f;     // fp32 copies of the gradient / hessian scales and lambda_l2
   float _pad;
+  double gs, hs;           // quantized path: the gradient / hessian scales
 };
 
 // Per-job control block, written and read only by kernels (the device-resident grow loop).
@@ -80,6 +81,9 @@ struct JobState {
   uint32_t split_thr;  // threshold of the chosen split | default_left << 31
   int64_t root_count, total_left;
   int64_t part_left, part_right;  // single-pass partition: rows placed from the front / back
+  int64_t hist_begin, hist_count;  // the smaller leaf's row range and index buffer, for the histogram
+  int32_t hist_buf, split_buf;
+  int64_t split_begin, split_count;  // the chosen leaf's row range and index buffer, for the partition
   double gscale, hscale, inv_g, inv_h;
   double root_output;
   uint32_t start_pos, red_maxg, red_maxh, red_flags;
@@ -122,6 +126,25 @@ struct Job {
   int64_t* ired;       // integer reduction partials (scratch)
 };
 
+// The jobs of one grow-loop launch, passed by value: the kernel parameters sit in the constant
+// bank, so a kernel reaches its job's buffers without a global-memory round trip after it starts.
+// A learner with more jobs launches each grow-loop kernel once per group.
+constexpr int kJobsPerLaunch = 4;
+struct JobTable {
+  Job job[kJobsPerLaunch];
+};
+
+// Calls f(table, jobs in it) for each group of up to kJobsPerLaunch consecutive host-side jobs.
+template <typename F>
+inline void for_job_groups(const Job* h_jobs, int num_jobs, F f) {
+  for (int z0 = 0; z0 < num_jobs; z0 += kJobsPerLaunch) {
+    JobTable t = {};
+    const int nz = num_jobs - z0 < kJobsPerLaunch ? num_jobs - z0 : kJobsPerLaunch;
+    for (int i = 0; i < nz; ++i) t.job[i] = h_jobs[z0 + i];
+    f(t, nz);
+  }
+}
+
 __device__ __forceinline__ const int32_t* leaf_idx(const Job& J, int32_t buf) { return buf ? J.idx1 : J.idx0; }
 __device__ __forceinline__ int32_t* leaf_idx_w(const Job& J, int32_t buf) { return buf ? J.idx1 : J.idx0; }
 
@@ -134,12 +157,12 @@ struct HistLaunch {
   size_t smem;
   int flush_rounds;  // quantized: rounds of 32*warps rows between 16-bit -> 32-bit flushes (0: wide)
 };
-void launch_hist(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const HistLaunch& hl,
+void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const HistLaunch& hl,
                  cudaStream_t s);
 size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide);
 
-void launch_search(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s);
-void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
+void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s);
+void launch_partition(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
                       const DevFeature* feats, bool stable, cudaStream_t s);
 
 cudaError_t hist_set_smem_attrs(size_t smem);

@@ -63,6 +63,9 @@ __device__ __forceinline__ void before_find_best_split(const Job& J, const Param
   if (lane == 0) {
     int32_t sl = right < 0 ? left : (nl < nr ? left : right);
     int64_t rows = J.leaf_count[sl];
+    st->hist_begin = J.leaf_begin[sl];
+    st->hist_count = rows;
+    st->hist_buf = J.leaf_buf[sl];
     if (rows == p.n) st->hist_rows_direct += rows;
     else st->hist_rows_gather += rows;
     st->hist_builds += 1;
@@ -87,8 +90,8 @@ __device__ __forceinline__ void post_split_body(const Job& J, const Params& p, c
   const int32_t bl = st->split_leaf, nl = st->new_leaf, tl = st->tree_leaves, nf = st->next_free;
   const int64_t L = __ldcg(&st->total_left);  // written by another CTA of the scatter
   const int64_t hdir = st->hist_rows_direct, hgat = st->hist_rows_gather, hbld = st->hist_builds;
-  const int64_t b = J.leaf_begin[bl], c = J.leaf_count[bl];
-  const int32_t buf = J.leaf_buf[bl], depth = J.leaf_depth[bl], pslot = J.leaf_slot[bl];
+  const int64_t b = st->split_begin, c = st->split_count;
+  const int32_t buf = st->split_buf, depth = J.leaf_depth[bl], pslot = J.leaf_slot[bl];
   Cand info = J.cand[(size_t)bl * p.F + st->split_inner];  // the chosen leaf's best split
   const int32_t miss = info.missing;
   // ---- the split (serial.rs:1685-1876) ----
@@ -151,6 +154,9 @@ __device__ __forceinline__ void post_split_body(const Job& J, const Params& p, c
       st->parent_slot = pslot;
       st->use_subtract = 1;
       const int64_t rows = left_smaller ? L : R;
+      st->hist_begin = left_smaller ? b : b + L;
+      st->hist_count = rows;
+      st->hist_buf = 1 - buf;
       if (rows == p.n) st->hist_rows_direct = hdir + rows;
       else st->hist_rows_gather = hgat + rows;
       st->hist_builds = hbld + 1;

@@ -50,15 +50,14 @@ struct Range {
 __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blocks_per_tile, Range* r) {
   const JobState* st = J.st;
   if (st->stop || !st->do_search) return false;
-  int32_t leaf = st->smaller_leaf;
-  int64_t begin = J.leaf_begin[leaf], count = J.leaf_count[leaf];
+  const int64_t begin = st->hist_begin, count = st->hist_count;
   int64_t chunk = ceil_div64(count, blocks_per_tile);
   if (chunk < kMinChunk) chunk = kMinChunk;
   chunk = (chunk + 31) / 32 * 32;
   r->r0 = (int64_t)blockIdx.x * chunk;
   if (r->r0 >= count) return false;
   r->r1 = min(count, r->r0 + chunk);
-  r->idx = leaf_idx(J, J.leaf_buf[leaf]) + begin;
+  r->idx = leaf_idx(J, st->hist_buf) + begin;
   r->direct = (count == p.n);  // all rows in order: the index buffer is the identity
   return true;
 }
@@ -109,7 +108,7 @@ __device__ __forceinline__ void add_row(uint32_t* hot, int32_t* cold_g, int32_t*
 
 template <bool WIDE>
 __global__ void __launch_bounds__(1024, 1)
-    k_hist_int(const Job* __restrict__ jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile,
+    k_hist_int(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile,
                int flush_rounds) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int B = p.B;
@@ -120,7 +119,7 @@ __global__ void __launch_bounds__(1024, 1)
     for (int e = threadIdx.x; e < n16; e += blockDim.x) z[e] = make_uint4(0, 0, 0, 0);
   }
   griddep_wait();
-  const Job& J = jobs[blockIdx.z];
+  const Job& J = jobs.job[blockIdx.z];
   hist_leaf_constants(J, p);
   Range R;
   if (!cta_range(J, p, blocks_per_tile, &R)) return;
@@ -229,7 +228,7 @@ __global__ void __launch_bounds__(1024, 1)
 
 template <bool CONST_HESS>
 __global__ void __launch_bounds__(1024, 1)
-    k_hist_float(const Job* __restrict__ jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile) {
+    k_hist_float(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int B = p.B;
   {
@@ -238,7 +237,7 @@ __global__ void __launch_bounds__(1024, 1)
     for (int e = threadIdx.x; e < n16; e += blockDim.x) z[e] = make_uint4(0, 0, 0, 0);
   }
   griddep_wait();
-  const Job& J = jobs[blockIdx.z];
+  const Job& J = jobs.job[blockIdx.z];
   hist_leaf_constants(J, p);
   Range R;
   if (!cta_range(J, p, blocks_per_tile, &R)) return;
@@ -335,23 +334,25 @@ size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide) {
   return bins * 16 + stage + warps * 32 * sizeof(float2);
 }
 
-void launch_hist(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const HistLaunch& hl,
+void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const HistLaunch& hl,
                  cudaStream_t s) {
-  dim3 grid(hl.blocks_per_tile, p.T, num_jobs);
-  if (p.quant) {
-    if (hl.flush_rounds > 0)
-      (void)launch_kernel(k_hist_int<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, d_jobs, p, bins_rt,
-                        hl.blocks_per_tile, hl.flush_rounds);
-    else
-      (void)launch_kernel(k_hist_int<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, d_jobs, p, bins_rt,
-                        hl.blocks_per_tile, 1);
-  } else if (p.const_hess) {
-    (void)launch_kernel(k_hist_float<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, d_jobs, p, bins_rt,
-                      hl.blocks_per_tile);
-  } else {
-    (void)launch_kernel(k_hist_float<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, d_jobs, p, bins_rt,
-                      hl.blocks_per_tile);
-  }
+  for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
+    dim3 grid(hl.blocks_per_tile, p.T, nz);
+    if (p.quant) {
+      if (hl.flush_rounds > 0)
+        (void)launch_kernel(k_hist_int<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt,
+                            hl.blocks_per_tile, hl.flush_rounds);
+      else
+        (void)launch_kernel(k_hist_int<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt,
+                            hl.blocks_per_tile, 1);
+    } else if (p.const_hess) {
+      (void)launch_kernel(k_hist_float<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt,
+                          hl.blocks_per_tile);
+    } else {
+      (void)launch_kernel(k_hist_float<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt,
+                          hl.blocks_per_tile);
+    }
+  });
 }
 
 cudaError_t hist_set_smem_attrs(size_t smem) {

@@ -100,6 +100,8 @@ __device__ __forceinline__ void compute_leaf_const(const Job& J, const Params& p
   c.hsf = (float)st->hscale;
   c.l2f = (float)p.l2;
   c._pad = 0.f;
+  c.gs = st->gscale;
+  c.hs = st->hscale;
   if (lane == 0) J.lconst[side] = c;
 }
 

@@ -183,16 +183,16 @@ struct bk_learner {
   // histogram / search / partition phases.
   void step_a(int it) {
     record_hist_event(4 * it);
-    launch_hist(d_jobs, K, p, d_bins_rt, hl, stream);
+    launch_hist(jobs.data(), K, p, d_bins_rt, hl, stream);
     record_hist_event(4 * it + 1);
-    launch_search(d_jobs, K, p, d_feat, stream);  // its last CTA also picks the split
+    launch_search(jobs.data(), K, p, d_feat, stream);  // its last CTA also picks the split
     record_hist_event(4 * it + 2);
   }
   void step_b(int it) {
     // the plain form keeps the reference's stable compaction; so does leaf renewal, whose f64 sums
     // run in leaf row order
     const bool stable = loop_mode == 0 || (p.quant && p.renew);
-    launch_partition(d_jobs, K, p, d_bins_cm, d_feat, stable, stream);  // its last CTA also records the split
+    launch_partition(jobs.data(), K, p, d_bins_cm, d_feat, stable, stream);  // its last CTA also records the split
     record_hist_event(4 * it + 3);
   }
 

@@ -30,10 +30,9 @@ struct PartRange {
 
 __device__ __forceinline__ void part_range(const Job& J, const Params& p, const uint8_t* bins_cm, PartRange* r) {
   const JobState* st = J.st;
-  int32_t leaf = st->split_leaf;
-  r->begin = J.leaf_begin[leaf];
-  r->count = J.leaf_count[leaf];
-  int32_t buf = J.leaf_buf[leaf];
+  r->begin = st->split_begin;
+  r->count = st->split_count;
+  const int32_t buf = st->split_buf;
   r->src = leaf_idx(J, buf) + r->begin;
   r->dst = leaf_idx_w(J, 1 - buf) + r->begin;
   r->col = bins_cm + (size_t)st->split_inner * (size_t)p.n;
@@ -81,13 +80,13 @@ __device__ __forceinline__ void build_route(const JobState* st, const DevFeature
   lut[b] = (int)b < m.gbins ? route_bin(m, th & 0x7fffffffu, (th >> 31) != 0, b) : 0;
 }
 
-__global__ void __launch_bounds__(kThreads) k_part_count(const Job* __restrict__ jobs, Params p,
+__global__ void __launch_bounds__(kThreads) k_part_count(const JobTable jobs, Params p,
                                                          const uint8_t* __restrict__ bins_cm,
                                                          const DevFeature* __restrict__ feats) {
   __shared__ uint8_t lut[256];
   __shared__ int64_t sh[32];
   griddep_wait();
-  const Job& J = jobs[blockIdx.z];
+  const Job& J = jobs.job[blockIdx.z];
   if (J.st->stop) return;
   PartRange R;
   part_range(J, p, bins_cm, &R);  // its loads are in flight with the route table's
@@ -116,13 +115,13 @@ __global__ void __launch_bounds__(kThreads) k_part_count(const Job* __restrict__
   if (threadIdx.x == 0) J.part_cnt[blockIdx.x] = total;
 }
 
-__global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict__ jobs, Params p,
+__global__ void __launch_bounds__(kThreads) k_part_scatter(const JobTable jobs, Params p,
                                                            const uint8_t* __restrict__ bins_cm,
                                                            const DevFeature* __restrict__ feats) {
   __shared__ uint8_t lut[256];
   __shared__ int32_t sh[32];
   griddep_wait();
-  const Job& J = jobs[blockIdx.z];
+  const Job& J = jobs.job[blockIdx.z];
   if (J.st->stop) return;
   __shared__ int64_t sh64[32];
   PartRange R;
@@ -195,7 +194,7 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const Job* __restrict
 // range and those of its right rows from the back, one atomic each; inside a tile the rows keep
 // their leaf order. No count pass: the last CTA reads the left total and runs the post-split
 // bookkeeping.
-__global__ void __launch_bounds__(kThreads) k_part_onepass(const Job* __restrict__ jobs, Params p,
+__global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, Params p,
                                                            const uint8_t* __restrict__ bins_cm,
                                                            const DevFeature* __restrict__ feats) {
   __shared__ uint8_t lut[256];
@@ -203,7 +202,7 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const Job* __restrict
   __shared__ int64_t s_off[2];
   __shared__ int last;
   griddep_wait();
-  const Job& J = jobs[blockIdx.z];
+  const Job& J = jobs.job[blockIdx.z];
   JobState* st = J.st;
   if (st->stop) return;
   PartRange R;
@@ -269,15 +268,17 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const Job* __restrict
 
 }  // namespace
 
-void launch_partition(const Job* d_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
+void launch_partition(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
                       const DevFeature* feats, bool stable, cudaStream_t s) {
-  dim3 grid(p.part_grid, 1, num_jobs);
-  if (stable) {
-    (void)launch_kernel(k_part_count, grid, dim3(kThreads), 0, s, p.pdl, d_jobs, p, bins_cm, feats);
-    (void)launch_kernel(k_part_scatter, grid, dim3(kThreads), 0, s, p.pdl, d_jobs, p, bins_cm, feats);
-  } else {
-    (void)launch_kernel(k_part_onepass, grid, dim3(kThreads), 0, s, p.pdl, d_jobs, p, bins_cm, feats);
-  }
+  for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
+    dim3 grid(p.part_grid, 1, nz);
+    if (stable) {
+      (void)launch_kernel(k_part_count, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats);
+      (void)launch_kernel(k_part_scatter, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats);
+    } else {
+      (void)launch_kernel(k_part_onepass, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats);
+    }
+  });
 }
 
 }  // namespace bk

@@ -679,7 +679,7 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
       queue_push(sm, d, exact, QEnt{lg[d], lh[d], 0, (int16_t)(d == 0 || !xpos ? t : -1), (int16_t)d}, lane);
     }
     __syncthreads();
-    const double gs = st->gscale, hsc = st->hscale;
+    const double gs = C.gs, hsc = C.hs;
     eval_queues(
         sm, warp, lane, C.mgs,
         [&](const QEnt& e) { return int_split_gain(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, true); },
@@ -698,7 +698,7 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
     for (int d = 0; d < 2; ++d) {
       gain[d] = -CUDART_INF;
       if (valid[d])
-        gain[d] = int_split_gain(p, lg[d], lh[d], tg, th, st->gscale, st->hscale, C.cnt_factor, C.parent, false);
+        gain[d] = int_split_gain(p, lg[d], lh[d], tg, th, C.gs, C.hs, C.cnt_factor, C.parent, false);
       const bool passed = valid[d] && gain_passes(gain[d], C.mgs);
       split[d] = passed;
       elig[d] = passed && !dnan(gain[d]) && !is_neg_inf(gain[d]);  // NaN never wins
@@ -721,7 +721,7 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
       v.gain = b.ev.gain;
       return v;
     }
-    return eval_int(p, b.a, b.b, tg, th, st->gscale, st->hscale, C.cnt_factor, C.parent, b.ev.gain, lane);
+    return eval_int(p, b.a, b.b, tg, th, C.gs, C.hs, C.cnt_factor, C.parent, b.ev.gain, lane);
   });
 }
 
@@ -1017,6 +1017,10 @@ __device__ __forceinline__ Pick make_pick(int i, double g, int f, long long pay)
 // partition builds the route table of the chosen split from (split_inner, split_thr).
 __device__ void decide_body(const Job& J, const Params& p, const DevFeature* feats) {
   __shared__ Pick s_f[kSearchWarps], s_l[kSearchWarps];
+  // the row range of the first kSearchThreads leaves, so the chosen leaf's is at hand for the
+  // partition that follows
+  __shared__ int64_t s_lb[kSearchThreads], s_lc[kSearchThreads];
+  __shared__ int32_t s_lbuf[kSearchThreads];
   JobState* st = J.st;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   constexpr int kHalf = kSearchThreads / 2;
@@ -1048,6 +1052,11 @@ __device__ void decide_body(const Job& J, const Params& p, const DevFeature* fea
   Pick b = none;
   b.f = 0;
   for (int i = t; i < p.num_leaves; i += kSearchThreads) {
+    if (i < kSearchThreads) {
+      s_lb[i] = J.leaf_begin[i];
+      s_lc[i] = J.leaf_count[i];
+      s_lbuf[i] = J.leaf_buf[i];
+    }
     if (searched && (i == leaf0 || i == leaf1)) continue;
     leaf_pick(b, make_pick(i, J.bgain[i], J.bfeat[i], J.bsplit[i]));
   }
@@ -1092,6 +1101,10 @@ __device__ void decide_body(const Job& J, const Params& p, const DevFeature* fea
     return;
   }
   if (lane == 0) {
+    const bool near = w.i < kSearchThreads;
+    st->split_begin = near ? s_lb[w.i] : J.leaf_begin[w.i];
+    st->split_count = near ? s_lc[w.i] : J.leaf_count[w.i];
+    st->split_buf = near ? s_lbuf[w.i] : J.leaf_buf[w.i];
     st->split_leaf = w.i;
     st->split_inner = inner;
     st->split_thr = (uint32_t)(w.pay & 0xffffffffLL);
@@ -1102,19 +1115,19 @@ __device__ void decide_body(const Job& J, const Params& p, const DevFeature* fea
 // One CTA per (feature, side): blockIdx.x = 2 * feature + side (0 = smaller leaf). The last CTA to
 // finish runs the fold / arg-max.
 template <bool PLAIN, bool QUANT>
-__global__ void __launch_bounds__(kSearchThreads) k_search(const Job* __restrict__ jobs, Params p,
+__global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, Params p,
                                                            const DevFeature* __restrict__ feats) {
   __shared__ SearchSmem sm;
   __shared__ int last;
-  griddep_wait();
-  const Job& J = jobs[blockIdx.z];
-  JobState* st = J.st;
-  if (st->stop) return;  // uniform over the grid
   const int side = (int)(blockIdx.x & 1u);
   const int f = (int)(blockIdx.x >> 1);
+  const DevFeature m = feats[f];  // static: loaded while the histogram launch finishes
+  griddep_wait();
+  const Job& J = jobs.job[blockIdx.z];
+  JobState* st = J.st;
+  if (st->stop) return;  // uniform over the grid
   const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
   if (st->do_search && J.used[f] && leaf >= 0) {  // uniform over the CTA
-    const DevFeature m = feats[f];
     if (QUANT)
       search_int<PLAIN>(J, p, st, m, side, f, leaf, sm);
     else
@@ -1169,17 +1182,19 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
 
 }  // namespace
 
-void launch_search(const Job* d_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s) {
-  dim3 grid((unsigned)(2 * p.F), 1, num_jobs);
+void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s) {
   const bool plain = !p.use_l1 && !p.use_max && !p.use_smooth;
   const dim3 block(kSearchThreads);
-  if (p.quant) {
-    if (plain) (void)launch_kernel(k_search<true, true>, grid, block, 0, s, p.pdl, d_jobs, p, feats);
-    else (void)launch_kernel(k_search<false, true>, grid, block, 0, s, p.pdl, d_jobs, p, feats);
-  } else {
-    if (plain) (void)launch_kernel(k_search<true, false>, grid, block, 0, s, p.pdl, d_jobs, p, feats);
-    else (void)launch_kernel(k_search<false, false>, grid, block, 0, s, p.pdl, d_jobs, p, feats);
-  }
+  for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
+    dim3 grid((unsigned)(2 * p.F), 1, nz);
+    if (p.quant) {
+      if (plain) (void)launch_kernel(k_search<true, true>, grid, block, 0, s, p.pdl, t, p, feats);
+      else (void)launch_kernel(k_search<false, true>, grid, block, 0, s, p.pdl, t, p, feats);
+    } else {
+      if (plain) (void)launch_kernel(k_search<true, false>, grid, block, 0, s, p.pdl, t, p, feats);
+      else (void)launch_kernel(k_search<false, false>, grid, block, 0, s, p.pdl, t, p, feats);
+    }
+  });
 }
 
 void launch_tree_begin(const Job* d_jobs, int num_jobs, const Params& p, cudaStream_t s) {
