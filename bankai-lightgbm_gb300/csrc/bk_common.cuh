@@ -2,14 +2,21 @@
 //
 // Layout in HBM (one learner, `n` rows, `F` inner features, `T = ceil(F / 32)` feature tiles,
 // `B` = the largest stored-bin count of any feature, rounded up to a multiple of 8):
-//   bins_rt   uint8 [T][n][32]   row-tiled stored bins: one 32-byte sector per (tile, row), so a
-//                                gathered row of a leaf is one coalesced sector read per tile;
+//   bins_rt   uint8 [n][T][32]   row-tiled stored bins: one 32-byte sector per (row, tile), so a
+//                                gathered row of a sparse leaf is one sector read per tile, and
+//                                the T histogram CTAs of a row chunk, which run side by side,
+//                                read neighbouring sectors of the same lines;
+//   bins_tm   uint8 [T][n][32]   the same sectors tile-major: the root and dense leaves (a
+//                                quarter of the rows or more) stream each tile contiguously;
 //   bins_cm   uint8 [F][n]       column-major stored bins, read by the partition (one byte/row);
 //   pool      [L][T][B][32]      histogram pool, one slot per leaf (serial.rs:80-162 with a full
 //                                pool): double2 (grad, hess) on the float path, int64
 //                                (grad << 32) + hess on the quantized path;
 // and per job (one tree of the K trees grown together): gradients, packed int8 gradients,
-// two row-index buffers (ping-pong between a leaf and its children), leaf bookkeeping.
+// two row-index buffers (ping-pong between a leaf and its children) and, on the quantized path,
+// the packed values in the same leaf order beside them (the partition moves them with the row
+// indices, so a histogram reads them contiguously instead of gathering one per row), leaf
+// bookkeeping.
 #pragma once
 #include <cuda_runtime.h>
 #include <stdint.h>
@@ -101,6 +108,8 @@ struct Job {
   int16_t* packed;
   int32_t* idx0;
   int32_t* idx1;
+  int16_t* pk0;  // quantized path: packed values in the leaf order of idx0 / idx1 (not the root's)
+  int16_t* pk1;
   int64_t* leaf_begin;
   int64_t* leaf_count;
   int32_t* leaf_buf;
@@ -147,6 +156,7 @@ inline void for_job_groups(const Job* h_jobs, int num_jobs, F f) {
 
 __device__ __forceinline__ const int32_t* leaf_idx(const Job& J, int32_t buf) { return buf ? J.idx1 : J.idx0; }
 __device__ __forceinline__ int32_t* leaf_idx_w(const Job& J, int32_t buf) { return buf ? J.idx1 : J.idx0; }
+__device__ __forceinline__ int16_t* leaf_pk(const Job& J, int32_t buf) { return buf ? J.pk1 : J.pk0; }
 
 __host__ __device__ __forceinline__ int64_t ceil_div64(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
@@ -157,7 +167,12 @@ struct HistLaunch {
   size_t smem;
   int flush_rounds;  // quantized: rounds of 32*warps rows between 16-bit -> 32-bit flushes (0: wide)
 };
-void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const HistLaunch& hl,
+// BinsCheck over device columns: the smallest flat index (feature * n + row) of a stored bin
+// outside its feature's range, or INT64_MAX (bk_binning.cu). Synchronizes `s`.
+cudaError_t check_bins_device(const uint8_t* bins, int64_t n, int32_t F, const DevFeature* d_feat,
+                              int64_t* first_bad, cudaStream_t s);
+void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const uint8_t* bins_tm,
+                 const HistLaunch& hl,
                  cudaStream_t s);
 size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide);
 

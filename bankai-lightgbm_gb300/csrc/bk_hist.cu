@@ -42,9 +42,10 @@ __device__ __forceinline__ float two_sum_err(float a, float b, float s) {
 }
 
 struct Range {
-  int64_t r0, r1;
+  int64_t r0, r1, count;
   const int32_t* idx;
-  bool direct;
+  const int16_t* pk;  // packed values: by row for the root, else in leaf order
+  bool direct, pk_row;
 };
 
 __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blocks_per_tile, Range* r) {
@@ -57,8 +58,11 @@ __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blo
   r->r0 = (int64_t)blockIdx.x * chunk;
   if (r->r0 >= count) return false;
   r->r1 = min(count, r->r0 + chunk);
+  r->count = count;
   r->idx = leaf_idx(J, st->hist_buf) + begin;
   r->direct = (count == p.n);  // all rows in order: the index buffer is the identity
+  r->pk_row = st->tree_leaves == 1;  // the root: no leaf-ordered copy yet
+  r->pk = r->pk_row ? J.packed : (J.pk0 ? leaf_pk(J, st->hist_buf) + begin : nullptr);
   return true;
 }
 
@@ -75,16 +79,17 @@ struct RoundLoad {
   int32_t v;
 };
 
-__device__ __forceinline__ RoundLoad load_round_int(const uint8_t* tb, const int16_t* packed, int32_t row, bool wide) {
+__device__ __forceinline__ RoundLoad load_round_int(const uint8_t* tb, size_t rs, const Range& R, int64_t i, int32_t row,
+                                                    bool wide) {
   RoundLoad L;
   L.a = make_uint4(0, 0, 0, 0);
   L.b = make_uint4(0, 0, 0, 0);
   L.v = 0;
   if (row >= 0) {
-    const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * TILE);
+    const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * rs);
     L.a = __ldg(src);
     L.b = __ldg(src + 1);
-    int32_t pk = packed[row];
+    int32_t pk = R.pk_row ? R.pk[row] : R.pk[i];
     int32_t gi = (int32_t)(int8_t)(pk >> 8);
     int32_t hi = pk & 0xff;
     L.v = wide ? ((gi & 0xffff) | (hi << 16)) : gi * 65536 + hi;
@@ -108,7 +113,8 @@ __device__ __forceinline__ void add_row(uint32_t* hot, int32_t* cold_g, int32_t*
 
 template <bool WIDE>
 __global__ void __launch_bounds__(1024, 1)
-    k_hist_int(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile,
+    k_hist_int(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
+               int blocks_per_tile,
                int flush_rounds) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int B = p.B;
@@ -131,8 +137,10 @@ __global__ void __launch_bounds__(1024, 1)
   uint4* stage = reinterpret_cast<uint4*>(cold_h + B * TILE);
   int32_t* stage_v = reinterpret_cast<int32_t*>(stage + nwarps * 64);
   __syncthreads();
-  const uint8_t* tb = bins_rt + (size_t)tile * (size_t)p.n * TILE;
-  const int16_t* packed = J.packed;
+  // the tile's sector of row 0 and the row stride, in the copy that suits the leaf's density
+  const bool dense = R.count * 4 >= p.n;
+  const uint8_t* tb = dense ? bins_tm + (size_t)tile * (size_t)p.n * TILE : bins_rt + (size_t)tile * TILE;
+  const size_t rs = dense ? (size_t)TILE : (size_t)p.T * TILE;
   // lanes past the last feature of the last tile (padding bytes) add nothing
   const bool feat_lane = tile * TILE + lane < p.F;
   const int64_t per_round = (int64_t)TILE * nwarps;
@@ -143,13 +151,13 @@ __global__ void __launch_bounds__(1024, 1)
   // software pipeline: the next round's sectors and the round after's row indices are in flight
   // while this round is added up
   const int64_t first = R.r0 + (int64_t)warp * TILE + lane;
-  RoundLoad cur = load_round_int(tb, packed, round_row(R, first), WIDE);
+  RoundLoad cur = load_round_int(tb, rs, R, first, round_row(R, first), WIDE);
   int32_t row_nxt = round_row(R, first + per_round);
   int until_flush = flush_rounds;
   for (int64_t rd = 0; rd < rounds; ++rd) {
     const int64_t base = R.r0 + rd * per_round + (int64_t)warp * TILE;
     const int32_t row_nn = round_row(R, base + 2 * per_round + lane);
-    RoundLoad nxt = load_round_int(tb, packed, row_nxt, WIDE);
+    RoundLoad nxt = load_round_int(tb, rs, R, base + per_round + lane, row_nxt, WIDE);
     row_nxt = row_nn;
     if (base < R.r1) {
       my_stage[lane * 2] = cur.a;
@@ -228,7 +236,8 @@ __global__ void __launch_bounds__(1024, 1)
 
 template <bool CONST_HESS>
 __global__ void __launch_bounds__(1024, 1)
-    k_hist_float(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, int blocks_per_tile) {
+    k_hist_float(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
+                 int blocks_per_tile) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int B = p.B;
   {
@@ -251,7 +260,10 @@ __global__ void __launch_bounds__(1024, 1)
   float2* stage_v = reinterpret_cast<float2*>(stage + nwarps * 64);
   uint32_t* hcnt = reinterpret_cast<uint32_t*>(hhi);
   __syncthreads();
-  const uint8_t* tb = bins_rt + (size_t)tile * (size_t)p.n * TILE;
+  // the tile's sector of row 0 and the row stride, in the copy that suits the leaf's density
+  const bool dense = R.count * 4 >= p.n;
+  const uint8_t* tb = dense ? bins_tm + (size_t)tile * (size_t)p.n * TILE : bins_rt + (size_t)tile * TILE;
+  const size_t rs = dense ? (size_t)TILE : (size_t)p.T * TILE;
   const bool feat_lane = tile * TILE + lane < p.F;
   const float* G = J.g;
   const float* H = J.h;
@@ -262,7 +274,7 @@ __global__ void __launch_bounds__(1024, 1)
     b = make_uint4(0, 0, 0, 0);
     v = make_float2(0.f, 0.f);
     if (row >= 0) {
-      const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * TILE);
+      const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * rs);
       a = __ldg(src);
       b = __ldg(src + 1);
       v.x = G[row];
@@ -334,22 +346,22 @@ size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide) {
   return bins * 16 + stage + warps * 32 * sizeof(float2);
 }
 
-void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const HistLaunch& hl,
-                 cudaStream_t s) {
+void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const uint8_t* bins_tm,
+                 const HistLaunch& hl, cudaStream_t s) {
   for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
     dim3 grid(hl.blocks_per_tile, p.T, nz);
     if (p.quant) {
       if (hl.flush_rounds > 0)
-        (void)launch_kernel(k_hist_int<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt,
+        (void)launch_kernel(k_hist_int<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
                             hl.blocks_per_tile, hl.flush_rounds);
       else
-        (void)launch_kernel(k_hist_int<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt,
+        (void)launch_kernel(k_hist_int<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
                             hl.blocks_per_tile, 1);
     } else if (p.const_hess) {
-      (void)launch_kernel(k_hist_float<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt,
+      (void)launch_kernel(k_hist_float<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
                           hl.blocks_per_tile);
     } else {
-      (void)launch_kernel(k_hist_float<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt,
+      (void)launch_kernel(k_hist_float<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
                           hl.blocks_per_tile);
     }
   });

@@ -86,7 +86,9 @@ struct HostMt {
   }
 };
 
-__global__ void k_pack_rowtile(const uint8_t* __restrict__ cm, uint8_t* __restrict__ rt, int64_t n, int F, int T) {
+// The two row-tiled copies of the column-major bins: rt [n][T][32] and tm [T][n][32].
+__global__ void k_pack_rowtile(const uint8_t* __restrict__ cm, uint8_t* __restrict__ rt, uint8_t* __restrict__ tm,
+                               int64_t n, int F, int T) {
   int64_t total = n * T;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
     int64_t tile = k / n, row = k % n;
@@ -102,9 +104,12 @@ __global__ void k_pack_rowtile(const uint8_t* __restrict__ cm, uint8_t* __restri
       }
       w[q] = v;
     }
-    uint4* dst = reinterpret_cast<uint4*>(rt + ((size_t)tile * n + row) * TILE);
+    uint4* dst = reinterpret_cast<uint4*>(rt + ((size_t)row * T + tile) * TILE);
     dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
     dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    uint4* dtm = reinterpret_cast<uint4*>(tm + ((size_t)tile * n + row) * TILE);
+    dtm[0] = make_uint4(w[0], w[1], w[2], w[3]);
+    dtm[1] = make_uint4(w[4], w[5], w[6], w[7]);
   }
 }
 
@@ -124,7 +129,8 @@ struct bk_learner {
   DevFeature* d_feat = nullptr;
   std::vector<DevFeature> h_feat;
   uint8_t* d_bins_cm = nullptr;
-  uint8_t* d_bins_rt = nullptr;
+  uint8_t* d_bins_rt = nullptr;  // [n][T][32]: gathered leaves
+  uint8_t* d_bins_tm = nullptr;  // [T][n][32]: the root and dense leaves
   double* d_noise_g = nullptr;
   double* d_noise_h = nullptr;
   // jobs
@@ -183,7 +189,7 @@ struct bk_learner {
   // histogram / search / partition phases.
   void step_a(int it) {
     record_hist_event(4 * it);
-    launch_hist(jobs.data(), K, p, d_bins_rt, hl, stream);
+    launch_hist(jobs.data(), K, p, d_bins_rt, d_bins_tm, hl, stream);
     record_hist_event(4 * it + 1);
     launch_search(jobs.data(), K, p, d_feat, stream);  // its last CTA also picks the split
     record_hist_event(4 * it + 2);
@@ -264,8 +270,12 @@ extern "C" {
 
 const char* bk_last_error(void) { return g_last_error.c_str(); }
 
-int bk_learner_create(const bk_feature* features, int32_t num_features, const uint8_t* bins, int64_t num_data,
-                      const bk_config* c, int32_t num_jobs, bk_learner** out) {
+}  // extern "C"
+
+namespace {
+
+int learner_create(const bk_feature* features, int32_t num_features, const uint8_t* bins, int64_t num_data,
+                   const bk_config* c, int32_t num_jobs, bk_learner** out, bool device_bins) {
   if (!features || !bins || !c || !out || num_features <= 0 || num_data <= 0 || num_jobs <= 0) {
     set_error("bk_learner_create: invalid arguments");
     return -1;
@@ -342,8 +352,9 @@ int bk_learner_create(const bk_feature* features, int32_t num_features, const ui
       maxb = std::max(maxb, d.gbins);
       L->h_feat.push_back(d);
     }
-    // Validate the stored bins once, as the reference's BinsCheck does (histogram.rs:50-65).
-    for (int f = 0; f < num_features; ++f) {
+    // Validate the stored bins once, as the reference's BinsCheck does (histogram.rs:50-65);
+    // device-resident bins are checked on the device after the copy below.
+    for (int f = 0; !device_bins && f < num_features; ++f) {
       const uint8_t* col = bins + (size_t)f * (size_t)num_data;
       int gb = L->h_feat[f].gbins;
       for (int64_t i = 0; i < num_data; ++i)
@@ -381,9 +392,24 @@ int bk_learner_create(const bk_feature* features, int32_t num_features, const ui
     L->d_feat = L->dalloc<DevFeature>(num_features);
     CK(cudaMemcpy(L->d_feat, L->h_feat.data(), sizeof(DevFeature) * num_features, cudaMemcpyHostToDevice));
     L->d_bins_cm = L->dalloc<uint8_t>(n * num_features);
-    CK(cudaMemcpy(L->d_bins_cm, bins, n * num_features, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(L->d_bins_cm, bins, n * num_features, device_bins ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice));
+    if (device_bins) {
+      int64_t bad = INT64_MAX;
+      CK(check_bins_device(L->d_bins_cm, num_data, num_features, L->d_feat, &bad, L->stream));
+      if (bad != INT64_MAX) {
+        uint8_t v = 0;
+        CK(cudaMemcpy(&v, L->d_bins_cm + bad, 1, cudaMemcpyDeviceToHost));
+        const int f = (int)(bad / num_data);
+        set_error("feature %d row %lld: stored bin %d outside [0, %d)", f, (long long)(bad % num_data), (int)v,
+                  L->h_feat[f].gbins);
+        delete L;
+        return -1;
+      }
+    }
     L->d_bins_rt = L->dalloc<uint8_t>(n * p.T * TILE);
-    k_pack_rowtile<<<4 * L->num_sms, 256, 0, L->stream>>>(L->d_bins_cm, L->d_bins_rt, num_data, num_features, p.T);
+    L->d_bins_tm = L->dalloc<uint8_t>(n * p.T * TILE);
+    k_pack_rowtile<<<4 * L->num_sms, 256, 0, L->stream>>>(L->d_bins_cm, L->d_bins_rt, L->d_bins_tm, num_data,
+                                                          num_features, p.T);
     CK(cudaGetLastError());
     if (quant && p.stochastic) {
       // GradientDiscretizer::init_stochastic (gradient_discretizer/mod.rs:87-106)
@@ -422,6 +448,8 @@ int bk_learner_create(const bk_feature* features, int32_t num_features, const ui
       J.packed = quant ? L->dalloc<int16_t>(n) : nullptr;
       J.idx0 = L->dalloc<int32_t>(n);
       J.idx1 = L->dalloc<int32_t>(n);
+      J.pk0 = quant ? L->dalloc<int16_t>(n) : nullptr;
+      J.pk1 = quant ? L->dalloc<int16_t>(n) : nullptr;
       J.leaf_begin = L->dalloc<int64_t>(Lv);
       J.leaf_count = L->dalloc<int64_t>(Lv);
       J.leaf_buf = L->dalloc<int32_t>(Lv);
@@ -465,6 +493,20 @@ int bk_learner_create(const bk_feature* features, int32_t num_features, const ui
   }
   *out = L;
   return 0;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bk_learner_create(const bk_feature* features, int32_t num_features, const uint8_t* bins, int64_t num_data,
+                      const bk_config* c, int32_t num_jobs, bk_learner** out) {
+  return learner_create(features, num_features, bins, num_data, c, num_jobs, out, false);
+}
+
+int bk_learner_create_device_bins(const bk_feature* features, int32_t num_features, const uint8_t* bins,
+                                  int64_t num_data, const bk_config* c, int32_t num_jobs, bk_learner** out) {
+  return learner_create(features, num_features, bins, num_data, c, num_jobs, out, true);
 }
 
 int bk_learner_train(bk_learner* L, const float* gradients, const float* hessians, int32_t on_device,

@@ -26,7 +26,15 @@ struct PartRange {
   const int32_t* src;
   int32_t* dst;
   const uint8_t* col;
+  // quantized path: the packed values move with the row indices; the root's are read by row
+  const int16_t* pk_src;
+  int16_t* pk_dst;
+  bool pk_row;
 };
+
+__device__ __forceinline__ int32_t part_pk(const PartRange& R, int64_t e, int32_t row) {
+  return R.pk_row ? R.pk_src[row] : R.pk_src[e];
+}
 
 __device__ __forceinline__ void part_range(const Job& J, const Params& p, const uint8_t* bins_cm, PartRange* r) {
   const JobState* st = J.st;
@@ -36,6 +44,9 @@ __device__ __forceinline__ void part_range(const Job& J, const Params& p, const 
   r->src = leaf_idx(J, buf) + r->begin;
   r->dst = leaf_idx_w(J, 1 - buf) + r->begin;
   r->col = bins_cm + (size_t)st->split_inner * (size_t)p.n;
+  r->pk_row = st->tree_leaves == 1;  // the root: no leaf-ordered copy yet
+  r->pk_src = p.quant ? (r->pk_row ? J.packed : leaf_pk(J, buf) + r->begin) : nullptr;
+  r->pk_dst = p.quant ? leaf_pk(J, 1 - buf) + r->begin : nullptr;
   int64_t chunk = ceil_div64(r->count, p.part_grid);
   chunk = (chunk + kThreads * kItems - 1) / (kThreads * kItems) * (kThreads * kItems);
   if (chunk < kThreads * kItems) chunk = kThreads * kItems;
@@ -158,16 +169,16 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const JobTable jobs, 
     int32_t tile_total;
     int32_t pre = block_excl_scan<int32_t>(cnt, &tile_total, sh);
     int64_t left_before = running + pre;
+    int32_t pkv[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) pkv[k] = (p.quant && rows[k] >= 0) ? part_pk(R, e0 + k, rows[k]) : 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
       int64_t e = e0 + k;
       if (e < R.r1) {
-        if (flags & (1u << k)) {
-          R.dst[left_before] = rows[k];
-          ++left_before;
-        } else {
-          R.dst[total_left + (e - left_before)] = rows[k];
-        }
+        const int64_t slot = (flags & (1u << k)) ? left_before++ : total_left + (e - left_before);
+        R.dst[slot] = rows[k];
+        if (p.quant) R.pk_dst[slot] = (int16_t)pkv[k];
       }
     }
     running += tile_total;
@@ -234,13 +245,15 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
     // left rows fill [lo, lo + tile_left); right rows fill the tile's slots ending at count - ro
     int64_t lslot = s_off[0] + pre;
     int64_t rslot = R.count - s_off[1] - (n - tile_left) + ((int64_t)threadIdx.x * kItems - pre);
+    int32_t pkv[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) pkv[k] = (p.quant && rows[k] >= 0) ? part_pk(R, e0 + k, rows[k]) : 0;
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
       if (e0 + k < R.r1) {
-        if (flags & (1u << k))
-          R.dst[lslot++] = rows[k];
-        else
-          R.dst[rslot++] = rows[k];
+        const int64_t slot = (flags & (1u << k)) ? lslot++ : rslot++;
+        R.dst[slot] = rows[k];
+        if (p.quant) R.pk_dst[slot] = (int16_t)pkv[k];
       }
     }
     __syncthreads();  // s_off is rewritten by the next tile

@@ -54,6 +54,8 @@ _P, _i32, _i64, _u32, _f64 = c.c_void_p, c.c_int32, c.c_int64, c.c_uint32, c.c_d
 # (name, restype, argtypes) of the learner entry points declared in include/bkgpu.h
 _GPU_SIGNATURES = [
     ("bk_learner_create", _i32, [_P, _i32, _P, _i64, _P, _i32, _P]),
+    ("bk_learner_create_device_bins", _i32, [_P, _i32, _P, _i64, _P, _i32, _P]),
+    ("bk_bin_dense_device", _i32, [_P, _i32, _i64, _i32, _P, _i32, _P, _P, _P, _P]),
     ("bk_learner_train", _i32, [_P, _P, _P, _i32, _P, _i64, _P, _P, _P, _P]),
     ("bk_learner_add_prediction_to_score", _i32, [_P, _P, _P, _i32]),
     ("bk_learner_row_leaf", _i32, [_P, _P]),

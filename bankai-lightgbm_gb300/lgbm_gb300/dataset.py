@@ -100,12 +100,17 @@ class BinnedDataset:
         self.num_total_features = num_total_features
 
     @property
+    def on_device(self):
+        """True when ``bins`` is a CUDA tensor (``from_dense_device``)."""
+        return bool(getattr(self.bins, "is_cuda", False))
+
+    @property
     def num_data(self):
         return self.bins.shape[1]
 
     @property
     def num_features(self):
-        return self.bins.shape[0]
+        return len(self.features)
 
     @classmethod
     def from_dense(cls, X, max_bin=255, min_data_in_bin=3, min_data_in_leaf=20, bin_construct_sample_cnt=200000,
@@ -117,37 +122,9 @@ class BinnedDataset:
         n, ncol = X.shape
         lib = _lib.load()
         rows = _Random(data_random_seed).sample(n, min(n, bin_construct_sample_cnt))
-        sample_cnt = len(rows)
-        filter_cnt = int((float(min_data_in_leaf) * sample_cnt) / float(n))
-        cap = 1024
-
-        def find(col):
-            vals = np.asarray(X[rows, col], dtype=np.float64)
-            keep = (np.abs(vals) > K_ZERO_THRESHOLD) | np.isnan(vals)
-            vals = np.ascontiguousarray(vals[keep])
-            ub = np.zeros(cap, dtype=np.float64)
-            meta = np.zeros(4, dtype=np.int32)
-            dmeta = np.zeros(3, dtype=np.float64)
-            nb = lib.bk_find_bin_numerical(vals.ctypes.data, len(vals), sample_cnt, max_bin, min_data_in_bin,
-                                           filter_cnt, int(feature_pre_filter), int(use_missing),
-                                           int(zero_as_missing), ub.ctypes.data, cap, meta.ctypes.data,
-                                           dmeta.ctypes.data)
-            if nb < 0:
-                raise RuntimeError("bin mapper capacity exceeded")
-            fi = FeatureInfo()
-            fi.real = col
-            fi.num_bin = int(nb)
-            fi.missing_type = int(meta[0])
-            fi.default_bin = int(meta[2])
-            fi.most_freq_bin = int(meta[3])
-            fi.upper_bounds = ub[:nb].copy()
-            fi.penalty = 1.0
-            fi.min_val, fi.max_val, fi.sparse_rate = float(dmeta[0]), float(dmeta[1]), float(dmeta[2])
-            return fi, bool(meta[1])
-
-        with ThreadPoolExecutor(max_workers=threads) as ex:
-            found = list(ex.map(find, range(ncol)))
-        features = [fi for fi, trivial in found if not trivial]
+        features = _find_mappers(lambda col: np.asarray(X[rows, col], dtype=np.float64), ncol, n, len(rows),
+                                 max_bin, min_data_in_bin, min_data_in_leaf, use_missing, zero_as_missing,
+                                 feature_pre_filter, threads)
         bins = np.zeros((len(features), n), dtype=np.uint8)
 
         def fill(j):
@@ -178,12 +155,95 @@ class BinnedDataset:
             list(ex.map(fill, range(self.num_features)))
         return bins
 
+    @classmethod
+    def from_dense_device(cls, X, max_bin=255, min_data_in_bin=3, min_data_in_leaf=20, bin_construct_sample_cnt=200000,
+                          data_random_seed=1, use_missing=True, zero_as_missing=False, feature_pre_filter=True,
+                          threads=8):
+        """As ``from_dense`` for a row-major CUDA tensor ``X`` ([num_data, num_columns], float32 or
+        float64): the bin mappers come from the same row sample (copied to the host), the stored
+        bins are written on the device by ``bk_bin_dense_device``; ``bins`` is a uint8 CUDA tensor
+        [num_features, num_data]."""
+        import torch
+        if max_bin > 255:
+            raise ValueError("max_bin above 255 needs 16-bit stored bins, which this learner does not take")
+        if not (X.is_cuda and X.dim() == 2 and X.dtype in (torch.float32, torch.float64)):
+            raise ValueError("X must be a 2-D float32 / float64 CUDA tensor")
+        X = X.contiguous()
+        n, ncol = X.shape
+        rows = _Random(data_random_seed).sample(n, min(n, bin_construct_sample_cnt))
+        sample = X[torch.as_tensor(rows, device=X.device)].double().cpu().numpy()
+        features = _find_mappers(lambda col: sample[:, col], ncol, n, len(rows), max_bin, min_data_in_bin,
+                                 min_data_in_leaf, use_missing, zero_as_missing, feature_pre_filter, threads)
+        ds = cls(None, features, ncol)
+        ds.bins = ds.bin_like_device(X)
+        return ds
+
+    def bin_like_device(self, X):
+        """Stored bins of the rows of a row-major CUDA tensor ``X`` with this dataset's bin mappers,
+        on the device (uint8 CUDA tensor [num_features, rows])."""
+        import torch
+        X = X.contiguous()
+        n, ncol = X.shape
+        out = torch.empty((len(self.features), n), dtype=torch.uint8, device=X.device)
+        if not self.features:
+            return out
+        lib = _lib.load()
+        feats = self.feature_array()
+        offs = np.zeros(len(self.features) + 1, dtype=np.int32)
+        for j, fi in enumerate(self.features):
+            offs[j + 1] = offs[j] + fi.num_bin
+        ub = np.concatenate([fi.upper_bounds for fi in self.features]).astype(np.float64)
+        vt = 0 if X.dtype == torch.float64 else 1
+        stream = torch.cuda.current_stream(X.device).cuda_stream
+        _lib.check(lib.bk_bin_dense_device(X.data_ptr(), vt, n, ncol, feats.ctypes.data, len(self.features),
+                                           ub.ctypes.data, offs.ctypes.data, out.data_ptr(), stream),
+                   "bk_bin_dense_device")
+        return out
+
     def feature_array(self):
         """The ``bk_feature`` records of include/bkgpu.h, as a numpy structured array."""
         arr = np.zeros(self.num_features, dtype=FEATURE_DTYPE)
         for j, fi in enumerate(self.features):
             arr[j] = (fi.num_bin, fi.missing_type, fi.default_bin, fi.most_freq_bin, fi.penalty, fi.real, 0)
         return arr
+
+
+def _find_mappers(sample_col, ncol, n, sample_cnt, max_bin, min_data_in_bin, min_data_in_leaf, use_missing,
+                  zero_as_missing, feature_pre_filter, threads):
+    """``BinMapper::find_bin`` (io/bin.rs:342-554) for every column over the sampled rows
+    (``sample_col(col)``: the column's sampled values, f64), dropping trivial features
+    (io/dataset.rs:389-393)."""
+    lib = _lib.load()
+    filter_cnt = int((float(min_data_in_leaf) * sample_cnt) / float(n))
+    cap = 1024
+
+    def find(col):
+        vals = np.asarray(sample_col(col), dtype=np.float64)
+        keep = (np.abs(vals) > K_ZERO_THRESHOLD) | np.isnan(vals)
+        vals = np.ascontiguousarray(vals[keep])
+        ub = np.zeros(cap, dtype=np.float64)
+        meta = np.zeros(4, dtype=np.int32)
+        dmeta = np.zeros(3, dtype=np.float64)
+        nb = lib.bk_find_bin_numerical(vals.ctypes.data, len(vals), sample_cnt, max_bin, min_data_in_bin,
+                                       filter_cnt, int(feature_pre_filter), int(use_missing),
+                                       int(zero_as_missing), ub.ctypes.data, cap, meta.ctypes.data,
+                                       dmeta.ctypes.data)
+        if nb < 0:
+            raise RuntimeError("bin mapper capacity exceeded")
+        fi = FeatureInfo()
+        fi.real = col
+        fi.num_bin = int(nb)
+        fi.missing_type = int(meta[0])
+        fi.default_bin = int(meta[2])
+        fi.most_freq_bin = int(meta[3])
+        fi.upper_bounds = ub[:nb].copy()
+        fi.penalty = 1.0
+        fi.min_val, fi.max_val, fi.sparse_rate = float(dmeta[0]), float(dmeta[1]), float(dmeta[2])
+        return fi, bool(meta[1])
+
+    with ThreadPoolExecutor(max_workers=threads) as ex:
+        found = list(ex.map(find, range(ncol)))
+    return [fi for fi, trivial in found if not trivial]
 
 
 FEATURE_DTYPE = np.dtype([("num_bin", np.int32), ("missing_type", np.int32), ("default_bin", np.int32),

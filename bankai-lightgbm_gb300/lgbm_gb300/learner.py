@@ -22,12 +22,19 @@ class GpuTreeLearner:
         self.num_jobs = int(num_jobs)
         self.num_leaves = int(cfg.num_leaves)
         self._feats = ds.feature_array()
-        self._bins = np.ascontiguousarray(ds.bins, dtype=np.uint8)
         self._rec = cfg.record()
         h = ctypes.c_void_p()
-        _lib.check(self.lib.bk_learner_create(self._feats.ctypes.data, ds.num_features, self._bins.ctypes.data,
-                                              ds.num_data, self._rec.ctypes.data, self.num_jobs, ctypes.byref(h)),
-                   "bk_learner_create")
+        if ds.on_device:
+            # stored bins already in device memory (BinnedDataset.from_dense_device)
+            _lib.check(self.lib.bk_learner_create_device_bins(self._feats.ctypes.data, ds.num_features,
+                                                              ds.bins.data_ptr(), ds.num_data, self._rec.ctypes.data,
+                                                              self.num_jobs, ctypes.byref(h)),
+                       "bk_learner_create_device_bins")
+        else:
+            self._bins = np.ascontiguousarray(ds.bins, dtype=np.uint8)
+            _lib.check(self.lib.bk_learner_create(self._feats.ctypes.data, ds.num_features, self._bins.ctypes.data,
+                                                  ds.num_data, self._rec.ctypes.data, self.num_jobs, ctypes.byref(h)),
+                       "bk_learner_create")
         self.h = h
         self.set_loop_mode(loop_mode)
 

@@ -90,17 +90,56 @@ class ClockSampler:
                 "reasons": reasons, "samples": len(self.samples)}
 
 
-def build_dataset(rows, seed=0, heldout=False):
+def build_dataset(rows, seed=0, heldout=False, device_binning=False):
     """Training rows, plus (heldout=True) a 20% held-out split from the same generator, binned
-    with the training bin mappers."""
+    with the training bin mappers. device_binning=True also bins the training rows on the device
+    (BinnedDataset.from_dense_device) and returns its timings and whether its bins equal the
+    host's."""
     from lgbm_gb300 import BinnedDataset, synthetic
     total = rows + (rows // 4 if heldout else 0)
     X, y = synthetic.l2_steps(n=total, seed=seed)
     threads = min(32, os.cpu_count() or 8)
+    t0 = time.time()
     ds = BinnedDataset.from_dense(X[:rows], max_bin=255, min_data_in_leaf=20, threads=threads)
+    host_s = time.time() - t0
+    binning = _device_binning(X[:rows], ds, threads, host_s) if device_binning else None
     ho = (ds.bin_like(X[rows:], threads=threads), y[rows:]) if heldout else None
     del X
+    if device_binning:
+        return ds, y[:rows], ho, binning
     return ds, y[:rows], ho
+
+
+def _device_binning(X, ds, threads, host_s):
+    """Device bin construction of the same rows: the whole from_dense_device (host bin mappers
+    from the row sample + device binning) and the device binning call alone (CUDA events, median
+    of 3), against the host's from_dense time; value bytes read + stored bytes written per second."""
+    import torch
+    from lgbm_gb300 import BinnedDataset
+    Xd = torch.from_numpy(np.ascontiguousarray(X)).cuda()
+    torch.cuda.synchronize()
+    t0 = time.time()
+    dev = BinnedDataset.from_dense_device(Xd, max_bin=255, min_data_in_leaf=20, threads=threads)
+    torch.cuda.synchronize()
+    full_s = time.time() - t0
+    match = bool(np.array_equal(dev.bins.cpu().numpy(), ds.bins))
+    times = []
+    for _ in range(3):
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = dev.bin_like_device(Xd)
+        e1.record()
+        e1.synchronize()
+        times.append(e0.elapsed_time(e1))
+        del out
+    ms = float(np.median(times))
+    n, ncol = Xd.shape
+    nbytes = n * ncol * Xd.element_size() + n * dev.num_features
+    del Xd, dev
+    torch.cuda.empty_cache()
+    return {"host_from_dense_s": round(host_s, 2), "device_from_dense_s": round(full_s, 2),
+            "device_bin_ms": round(ms, 3), "device_bin_gbs": round(nbytes / (ms * 1e6), 1), "bins_equal": match,
+            "values": "f32 [%d x %d] row-major" % (n, ncol)}
 
 
 def make_cfg(quant, num_leaves=255):
@@ -117,7 +156,7 @@ def run_gpu(args, rank, world):
     torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", 0)))
     lr = 0.1
     t0 = time.time()
-    ds, y, (ho_bins_np, ho_y) = build_dataset(args.rows, heldout=True)
+    ds, y, (ho_bins_np, ho_y), binning = build_dataset(args.rows, heldout=True, device_binning=True)
     prep_s = time.time() - t0
     n = ds.num_data
     label = torch.from_numpy(y).cuda()
@@ -253,6 +292,7 @@ def run_gpu(args, rank, world):
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk,
         "prep_s": round(prep_s, 1),
+        "binning": binning,
     }
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(ds, y, sample_rows=args.cpu_rows)

@@ -66,6 +66,24 @@ typedef struct bk_learner bk_learner;
 int bk_learner_create(const bk_feature* features, int32_t num_features, const uint8_t* bins, int64_t num_data,
                       const bk_config* config, int32_t num_jobs, bk_learner** out);
 
+/* As bk_learner_create, with `bins` in device memory ([num_features][num_data] stored bins,
+ * e.g. written by bk_bin_dense_device); the learner copies them and checks them on the device. */
+int bk_learner_create_device_bins(const bk_feature* features, int32_t num_features, const uint8_t* bins,
+                                  int64_t num_data, const bk_config* config, int32_t num_jobs, bk_learner** out);
+
+/* Dense bin construction on the device: Dataset::from_dense's fill_dense (io/dataset.rs:633-685)
+ * with BinMapper::value_to_bin (io/bin.rs:558-589) for every value, for bin mappers found on the
+ * host (BinMapper::find_bin over a row sample, io/bin.rs:342-554; the held-out form is
+ * from_dense_reference, io/dataset.rs:987-1003). values: device memory, row-major
+ * [num_data][num_columns], value_type 0 = f64, 1 = f32. features: the used features' bin mappers
+ * (real_feature = their column); upper_bounds: host, feature f's num_bin bounds at
+ * upper_bounds[bound_offsets[f]], bound_offsets[num_features] in total. out: device
+ * [num_features][num_data] stored bins (the most frequent bin stored as 0). Runs on `stream`
+ * (a cudaStream_t, NULL for the default stream) and returns when the bins are written. */
+int bk_bin_dense_device(const void* values, int32_t value_type, int64_t num_data, int32_t num_columns,
+                        const bk_feature* features, int32_t num_features, const double* upper_bounds,
+                        const int32_t* bound_offsets, uint8_t* out, void* stream);
+
 /* Replaces SerialTreeLearner::train (serial.rs:569-628) for `num_jobs` trees at once.
  * gradients/hessians: [num_jobs][num_data] f32, host or device (on_device). rows: ascending
  * bagged row ids (num_rows of them) or NULL for all rows, host memory.
