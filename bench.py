@@ -40,6 +40,15 @@ WORKLOAD = ("L2 regression 10M x 100 (70 N(0,1) + 30 int 0..15, 10% NaN), max_bi
             "lr 0.1; step = device gradients + 1 tree + score update")
 
 
+# DRAM bytes (read + write) per algorithmic byte of the quantized histogram kernel, from one ncu
+# capture of every k_hist_int launch of one 255-leaf tree on this workload (10M rows):
+#   python bench.py --hist-traffic --rows 10000000 &&
+#   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none \
+#       -k regex:k_hist_int --csv --log-file ht10.csv python bench.py --hist-traffic --rows 10000000
+# 6.353 GB of DRAM traffic for 4.078 GB of algorithmic bytes over the 254 launches.
+HIST_TRAFFIC_PER_BYTE = 6.353 / 4.078
+
+
 def _peaks():
     try:
         d = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
@@ -264,7 +273,10 @@ def run_gpu(args, rank, world):
     e2e = form(True, 1, args.steps, 1, e2e=True)
     ms, value = aggregate_ranks(main["ms_per_step"], world)
     hist_gbs = roof["hist_bytes"] / (roof["hist_ms"] * 1e6) if roof["hist_ms"] > 0 else None
-    launches_per_step = 4 + 4 + 1 + 1 + 7 * (args.leaves - 1) + 1
+    hist_launches = (args.leaves - 1) * args.steps  # one histogram launch per split step of a tree
+    # per step: objective gradients, row init, discretization (4), root sums (2), tree begin, three
+    # kernels per split (histogram, search, partition), score update
+    launches_per_step = 1 + 1 + 4 + 2 + 1 + 3 * (args.leaves - 1) + 1
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
@@ -287,7 +299,11 @@ def run_gpu(args, rank, world):
                 "h2d_bytes_per_step": 2 * 4 * ds.num_data,
                 "d2h_bytes_per_step": 112 * (args.leaves - 1) + 8 * args.leaves + 8 + 8},
         "roofline": {"bound": "hbm", "achieved": round(hist_gbs, 1) if hist_gbs else None, "peak": peak,
-                     "unit": "GB/s", "frac": round(hist_gbs / peak, 4) if hist_gbs else None, "traffic": None,
+                     "unit": "GB/s", "frac": round(hist_gbs / peak, 4) if hist_gbs else None,
+                     "traffic": round(HIST_TRAFFIC_PER_BYTE * roof["hist_bytes"] / hist_launches, 0),
+                     "algorithmic_bytes_per_launch": round(roof["hist_bytes"] / hist_launches, 0),
+                     "traffic_source": "ncu capture of one tree's launches (DRAM bytes per algorithmic byte x this "
+                                       "run's algorithmic bytes per launch)",
                      "kernel": "k_hist_int (quantized histogram)", "peak_kind": peak_kind},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk,
