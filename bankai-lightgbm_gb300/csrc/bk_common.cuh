@@ -87,10 +87,11 @@ struct JobState {
   int32_t split_inner, new_leaf, use_rows;
   uint32_t split_thr;  // threshold of the chosen split | default_left << 31
   int64_t root_count, total_left;
-  int64_t part_left, part_right;  // single-pass partition: rows placed from the front / back
+  int64_t pcnt[2][2];  // single-pass partition: rows placed from the front / back, per split parity
   int64_t hist_begin, hist_count;  // the smaller leaf's row range and index buffer, for the histogram
   int32_t hist_buf, split_buf;
   int64_t split_begin, split_count;  // the chosen leaf's row range and index buffer, for the partition
+  int32_t split_depth, split_sslot;  // the chosen leaf's depth and the pool slot its smaller child gets
   double gscale, hscale, inv_g, inv_h;
   double root_output;
   uint32_t start_pos, red_maxg, red_maxh, red_flags;
@@ -171,14 +172,22 @@ struct HistLaunch {
 // outside its feature's range, or INT64_MAX (bk_binning.cu). Synchronizes `s`.
 cudaError_t check_bins_device(const uint8_t* bins, int64_t n, int32_t F, const DevFeature* d_feat,
                               int64_t* first_bad, cudaStream_t s);
+// post: the previous split came from the single-pass partition, whose counter pair `par` holds
+// its left total; the launch applies that split's bookkeeping.
 void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const uint8_t* bins_tm,
-                 const HistLaunch& hl,
-                 cudaStream_t s);
+                 const HistLaunch& hl, int post, int par, cudaStream_t s);
 size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide);
 
-void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s);
+// The bookkeeping of the last split of a tree partitioned in one pass (counter pair `par`).
+void launch_apply_split(const Job* h_jobs, int num_jobs, const Params& p, int par, cudaStream_t s);
+// clear_par >= 0: the launch zeroes that single-pass partition counter pair first.
+void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, int clear_par,
+                   cudaStream_t s);
+// stable: the two-kernel compaction whose last CTA applies the split's bookkeeping; otherwise the
+// single-pass partition, counting into the counter pair `par` (the split index's parity), whose
+// bookkeeping the next histogram launch applies.
 void launch_partition(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
-                      const DevFeature* feats, bool stable, cudaStream_t s);
+                      const DevFeature* feats, bool stable, int par, cudaStream_t s);
 
 cudaError_t hist_set_smem_attrs(size_t smem);
 

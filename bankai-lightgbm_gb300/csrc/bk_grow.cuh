@@ -79,39 +79,70 @@ __device__ __forceinline__ void before_find_best_split(const Job& J, const Param
   if (lane == 0) st->do_search = 1;
 }
 
-// Runs on the first warp of the last CTA of the partition scatter: SerialTreeLearner::split's
-// bookkeeping after DataPartition::split, then BeforeFindBestSplit(left, right) of the next
-// iteration. Every value is loaded first (independent loads in flight together), then every
-// store is issued, so the serial tail of a split costs about one memory round trip.
-__device__ __forceinline__ void post_split_body(const Job& J, const Params& p, const DevFeature* feats) {
+// What a split does to the leaf records once its left row count L is known
+// (SerialTreeLearner::split, serial.rs:1685-1876, then BeforeFindBestSplit(left, right) of the
+// next iteration, serial.rs:779-825): every value comes from the job state the decision wrote
+// (split leaf, its row range, depth, the next free pool slot) and L, so any CTA can derive the
+// children's row ranges without waiting for the bookkeeping below.
+struct SplitOutcome {
+  int32_t bl, nl, tl;   // the split leaf (keeps the left child), the new right leaf, leaves before the split
+  int32_t sslot;        // the pool slot of the smaller child (the larger keeps the parent's)
+  int32_t depth;        // depth of both children
+  int32_t nbuf;         // index buffer of both children
+  int64_t b, L, R;      // the parent's range start, the children's row counts
+  bool go, left_smaller;
+  __device__ int64_t hist_begin() const { return left_smaller ? b : b + L; }
+  __device__ int64_t hist_count() const { return left_smaller ? L : R; }
+};
+
+__device__ __forceinline__ SplitOutcome split_outcome(const Params& p, const JobState* st, int64_t L) {
+  SplitOutcome o;
+  o.bl = st->split_leaf;
+  o.nl = st->new_leaf;
+  o.tl = st->new_leaf;  // the decision records the leaf count as the new leaf's index
+  o.sslot = st->split_sslot;
+  o.depth = st->split_depth + 1;
+  o.nbuf = 1 - st->split_buf;
+  o.b = st->split_begin;
+  o.L = L;
+  o.R = st->split_count - L;
+  o.go = !(p.max_depth > 0 && o.depth >= p.max_depth);
+  if (o.go && (int32_t)o.R < p.min_data * 2 && (int32_t)o.L < p.min_data * 2) o.go = false;
+  o.left_smaller = (int32_t)o.L < (int32_t)o.R;
+  return o;
+}
+
+// The children's sums and outputs from the split's candidate record: what the bookkeeping writes
+// into leaf_sum (the smaller child first).
+__device__ __forceinline__ void split_children(const Cand& info, const SplitOutcome& o, LeafSum* smaller,
+                                               LeafSum* larger) {
+  const LeafSum left{info.lsg, info.lsh, info.left_output, info.lint, (int32_t)o.L, 0};
+  const LeafSum right{info.rsg, info.rsh, info.right_output, info.rint, (int32_t)o.R, 0};
+  *smaller = o.left_smaller ? left : right;
+  *larger = o.left_smaller ? right : left;
+}
+
+// One warp: the bookkeeping of a split (records, leaf arrays, pool slots, the next smaller /
+// larger leaf and its row range, the skipped features). Every value is loaded first (independent
+// loads in flight together), then every store is issued. It writes no job-state field that a
+// split_outcome() reads, so CTAs of the same launch can still derive the outcome.
+__device__ __forceinline__ void post_split_writes(const Job& J, const Params& p, const SplitOutcome& o, int lane) {
   JobState* st = J.st;
-  const int lane = threadIdx.x;
   // ---- loads ----
-  const int32_t bl = st->split_leaf, nl = st->new_leaf, tl = st->tree_leaves, nf = st->next_free;
-  const int64_t L = __ldcg(&st->total_left);  // written by another CTA of the scatter
   const int64_t hdir = st->hist_rows_direct, hgat = st->hist_rows_gather, hbld = st->hist_builds;
-  const int64_t b = st->split_begin, c = st->split_count;
-  const int32_t buf = st->split_buf, depth = J.leaf_depth[bl], pslot = J.leaf_slot[bl];
-  Cand info = J.cand[(size_t)bl * p.F + st->split_inner];  // the chosen leaf's best split
+  const int32_t pslot = J.leaf_slot[o.bl];
+  Cand info = J.cand[(size_t)o.bl * p.F + st->split_inner];  // the chosen leaf's best split
   const int32_t miss = info.missing;
-  // ---- the split (serial.rs:1685-1876) ----
-  const int64_t R = c - L;
-  info.left_count = (int32_t)L;
-  info.right_count = (int32_t)R;
-  const int32_t nd = depth + 1;  // tree.leaf_depth of both children
-  // ---- BeforeFindBestSplit(bl, nl) (serial.rs:779-825) ----
-  bool go = !(p.max_depth > 0 && nd >= p.max_depth);
-  const int32_t nleft = (int32_t)L, nright = (int32_t)R;
-  if (go && nright < p.min_data * 2 && nleft < p.min_data * 2) go = false;
-  const bool left_smaller = nleft < nright;
-  const int32_t sslot = nf;  // the smaller child gets a new slot; the larger keeps the parent's
+  info.left_count = (int32_t)o.L;
+  info.right_count = (int32_t)o.R;
+  const int32_t bl = o.bl, nl = o.nl;
   if (lane == 0) {
-    J.leaf_count[bl] = L;
-    J.leaf_begin[nl] = b + L;
-    J.leaf_count[nl] = R;
-    J.leaf_buf[bl] = 1 - buf;
-    J.leaf_buf[nl] = 1 - buf;
-    bk_split& r = J.records[tl - 1];
+    J.leaf_count[bl] = o.L;
+    J.leaf_begin[nl] = o.b + o.L;
+    J.leaf_count[nl] = o.R;
+    J.leaf_buf[bl] = o.nbuf;
+    J.leaf_buf[nl] = o.nbuf;
+    bk_split& r = J.records[o.tl - 1];
     r.leaf = bl;
     r.right_leaf = nl;
     r.inner_feature = info.inner;
@@ -132,45 +163,53 @@ __device__ __forceinline__ void post_split_body(const Job& J, const Params& p, c
     r.right_int_sum = info.rint;
     J.leaf_value[bl] = isnan(info.left_output) ? 0.0 : info.left_output;
     J.leaf_value[nl] = isnan(info.right_output) ? 0.0 : info.right_output;
-    J.leaf_depth[nl] = nd;
-    J.leaf_depth[bl] = nd;
+    J.leaf_depth[nl] = o.depth;
+    J.leaf_depth[bl] = o.depth;
     J.leaf_sum[bl] = LeafSum{info.lsg, info.lsh, info.left_output, info.lint, info.left_count, 0};
     J.leaf_sum[nl] = LeafSum{info.rsg, info.rsh, info.right_output, info.rint, info.right_count, 0};
     // the children's bests come from their search; without one both leaves drop out
     J.bgain[bl] = -CUDART_INF;
     J.bfeat[bl] = info.feature;
-    st->tree_leaves = tl + 1;
-    if (!go) {
+    st->tree_leaves = o.tl + 1;
+    if (!o.go) {
       J.bgain[nl] = -CUDART_INF;
       st->do_search = 0;
     } else {
-      st->next_free = nf + 1;
-      J.leaf_slot[left_smaller ? nl : bl] = pslot;
-      J.leaf_slot[left_smaller ? bl : nl] = sslot;
-      st->smaller_leaf = left_smaller ? bl : nl;
-      st->larger_leaf = left_smaller ? nl : bl;
-      st->smaller_slot = sslot;
+      st->next_free = o.sslot + 1;
+      J.leaf_slot[o.left_smaller ? nl : bl] = pslot;
+      J.leaf_slot[o.left_smaller ? bl : nl] = o.sslot;
+      st->smaller_leaf = o.left_smaller ? bl : nl;
+      st->larger_leaf = o.left_smaller ? nl : bl;
+      st->smaller_slot = o.sslot;
       st->larger_slot = pslot;
       st->parent_slot = pslot;
       st->use_subtract = 1;
-      const int64_t rows = left_smaller ? L : R;
-      st->hist_begin = left_smaller ? b : b + L;
+      const int64_t rows = o.hist_count();
+      st->hist_begin = o.hist_begin();
       st->hist_count = rows;
-      st->hist_buf = 1 - buf;
+      st->hist_buf = o.nbuf;
       if (rows == p.n) st->hist_rows_direct = hdir + rows;
       else st->hist_rows_gather = hgat + rows;
       st->hist_builds = hbld + 1;
       st->do_search = 1;
     }
   }
-  if (go) {
+  if (o.go) {
     // serial.rs:840-854 — features the parent could not split are skipped for both children
     for (int f = lane; f < p.F; f += 32) {
       uint8_t u = J.splittable[(size_t)pslot * p.F + f];
       J.used[f] = u;
-      if (!u) J.splittable[(size_t)sslot * p.F + f] = 0;
+      if (!u) J.splittable[(size_t)o.sslot * p.F + f] = 0;
     }
   }
+}
+
+// Runs on the first warp of the last CTA of the stable partition: the split's bookkeeping with L
+// from the partition's count.
+__device__ __forceinline__ void post_split_body(const Job& J, const Params& p, const DevFeature* feats) {
+  (void)feats;
+  const SplitOutcome o = split_outcome(p, J.st, __ldcg(&J.st->total_left));
+  post_split_writes(J, p, o, (int)threadIdx.x);
 }
 
 }  // namespace bk

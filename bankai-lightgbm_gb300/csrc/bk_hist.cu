@@ -45,13 +45,38 @@ struct Range {
   int64_t r0, r1, count;
   const int32_t* idx;
   const int16_t* pk;  // packed values: by row for the root, else in leaf order
+  int32_t slot;       // the pool slot the histogram goes to
   bool direct, pk_row;
 };
 
-__device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blocks_per_tile, Range* r) {
+// The smaller leaf's rows for this CTA (false: none). With `post`, the previous split's
+// single-pass partition left its bookkeeping to this launch: the range comes from the split's
+// outcome (bk_grow.cuh), and the side CTA writes the bookkeeping and the leaf constants.
+// Otherwise it comes from the job state and the side CTA computes the constants.
+__device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blocks_per_tile, int post, int par,
+                                          Range* r) {
   const JobState* st = J.st;
-  if (st->stop || !st->do_search) return false;
-  const int64_t begin = st->hist_begin, count = st->hist_count;
+  if (st->stop) return false;
+  int64_t begin, count;
+  int32_t buf;
+  if (post) {
+    const SplitOutcome o = split_outcome(p, st, __ldcg(&st->pcnt[par][0]));
+    hist_apply_split(J, p, o);
+    if (!o.go) return false;
+    begin = o.hist_begin();
+    count = o.hist_count();
+    buf = o.nbuf;
+    r->slot = o.sslot;
+    r->pk_row = false;
+  } else {
+    hist_leaf_constants(J, p);
+    if (!st->do_search) return false;
+    begin = st->hist_begin;
+    count = st->hist_count;
+    buf = st->hist_buf;
+    r->slot = st->smaller_slot;
+    r->pk_row = st->tree_leaves == 1;  // the root: no leaf-ordered copy yet
+  }
   int64_t chunk = ceil_div64(count, blocks_per_tile);
   if (chunk < kMinChunk) chunk = kMinChunk;
   chunk = (chunk + 31) / 32 * 32;
@@ -59,10 +84,9 @@ __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blo
   if (r->r0 >= count) return false;
   r->r1 = min(count, r->r0 + chunk);
   r->count = count;
-  r->idx = leaf_idx(J, st->hist_buf) + begin;
+  r->idx = leaf_idx(J, buf) + begin;
   r->direct = (count == p.n);  // all rows in order: the index buffer is the identity
-  r->pk_row = st->tree_leaves == 1;  // the root: no leaf-ordered copy yet
-  r->pk = r->pk_row ? J.packed : (J.pk0 ? leaf_pk(J, st->hist_buf) + begin : nullptr);
+  r->pk = r->pk_row ? J.packed : (J.pk0 ? leaf_pk(J, buf) + begin : nullptr);
   return true;
 }
 
@@ -114,8 +138,7 @@ __device__ __forceinline__ void add_row(uint32_t* hot, int32_t* cold_g, int32_t*
 template <bool WIDE>
 __global__ void __launch_bounds__(1024, 1)
     k_hist_int(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
-               int blocks_per_tile,
-               int flush_rounds) {
+               int blocks_per_tile, int flush_rounds, int post, int par) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int B = p.B;
   // the shared histogram is zeroed while the previous kernel of the grow loop finishes
@@ -126,9 +149,8 @@ __global__ void __launch_bounds__(1024, 1)
   }
   griddep_wait();
   const Job& J = jobs.job[blockIdx.z];
-  hist_leaf_constants(J, p);
   Range R;
-  if (!cta_range(J, p, blocks_per_tile, &R)) return;
+  if (!cta_range(J, p, blocks_per_tile, post, par, &R)) return;
   const int tile = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
@@ -219,7 +241,7 @@ __global__ void __launch_bounds__(1024, 1)
   griddep_launch();  // only the flush is left: the next kernel may be scheduled
   __syncthreads();
   unsigned long long* slot = reinterpret_cast<unsigned long long*>(J.pool) +
-                             ((size_t)J.st->smaller_slot * p.T + tile) * (size_t)B * TILE;
+                             ((size_t)R.slot * p.T + tile) * (size_t)B * TILE;
   for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
     int32_t gg = cold_g[e], hh = cold_h[e];
     if (!WIDE) {
@@ -237,7 +259,7 @@ __global__ void __launch_bounds__(1024, 1)
 template <bool CONST_HESS>
 __global__ void __launch_bounds__(1024, 1)
     k_hist_float(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
-                 int blocks_per_tile) {
+                 int blocks_per_tile, int post, int par) {
   extern __shared__ __align__(16) unsigned char smem[];
   const int B = p.B;
   {
@@ -247,9 +269,8 @@ __global__ void __launch_bounds__(1024, 1)
   }
   griddep_wait();
   const Job& J = jobs.job[blockIdx.z];
-  hist_leaf_constants(J, p);
   Range R;
-  if (!cta_range(J, p, blocks_per_tile, &R)) return;
+  if (!cta_range(J, p, blocks_per_tile, post, par, &R)) return;
   const int tile = blockIdx.y;
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   float* ghi = reinterpret_cast<float*>(smem);
@@ -322,7 +343,7 @@ __global__ void __launch_bounds__(1024, 1)
   }
   griddep_launch();
   __syncthreads();
-  double2* slot = reinterpret_cast<double2*>(J.pool) + ((size_t)J.st->smaller_slot * p.T + tile) * (size_t)B * TILE;
+  double2* slot = reinterpret_cast<double2*>(J.pool) + ((size_t)R.slot * p.T + tile) * (size_t)B * TILE;
   const double h0 = CONST_HESS ? (double)H[0] : 0.0;
   for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
     double gs = (double)ghi[e] + (double)glo[e];
@@ -347,22 +368,22 @@ size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide) {
 }
 
 void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const uint8_t* bins_tm,
-                 const HistLaunch& hl, cudaStream_t s) {
+                 const HistLaunch& hl, int post, int par, cudaStream_t s) {
   for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
     dim3 grid(hl.blocks_per_tile, p.T, nz);
     if (p.quant) {
       if (hl.flush_rounds > 0)
         (void)launch_kernel(k_hist_int<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
-                            hl.blocks_per_tile, hl.flush_rounds);
+                            hl.blocks_per_tile, hl.flush_rounds, post, par);
       else
         (void)launch_kernel(k_hist_int<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
-                            hl.blocks_per_tile, 1);
+                            hl.blocks_per_tile, 1, post, par);
     } else if (p.const_hess) {
       (void)launch_kernel(k_hist_float<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
-                          hl.blocks_per_tile);
+                          hl.blocks_per_tile, post, par);
     } else {
       (void)launch_kernel(k_hist_float<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
-                          hl.blocks_per_tile);
+                          hl.blocks_per_tile, post, par);
     }
   });
 }

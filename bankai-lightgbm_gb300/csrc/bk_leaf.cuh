@@ -5,6 +5,7 @@
 // by one CTA of the histogram launch that precedes it, so the search warps start from them.
 #pragma once
 #include "bk_common.cuh"
+#include "bk_grow.cuh"
 #include "bk_math.cuh"
 
 namespace bk {
@@ -67,18 +68,16 @@ __device__ __forceinline__ void int_thresholds(const Params& p, int64_t th, doub
   *brk_x = cnt_brk < hess_brk ? cnt_brk : hess_brk;
 }
 
-__device__ __forceinline__ double parent_output_of(const Params& p, const JobState* st, const LeafSum& ls) {
+__device__ __forceinline__ double parent_output_of(const Params& p, bool root, const LeafSum& ls) {
   // serial.rs:1924-1935 (GetParentOutput)
-  if (st->tree_leaves == 1) return leaf_output_root(p, ls.sg, ls.sh, ls.num_data);
+  if (root) return leaf_output_root(p, ls.sg, ls.sh, ls.num_data);
   return ls.weight;
 }
 
-// One warp: the constants of side `side` (0 = smaller leaf, 1 = larger leaf) of the coming search.
-__device__ __forceinline__ void compute_leaf_const(const Job& J, const Params& p, const JobState* st, int side,
-                                                   int lane) {
-  const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
-  if (leaf < 0) return;
-  const LeafSum ls = J.leaf_sum[leaf];
+// One warp: the constants of side `side` (0 = smaller leaf, 1 = larger leaf) of the coming search,
+// for a leaf with sums `ls` (`root`: the tree's only leaf).
+__device__ __forceinline__ void compute_leaf_const_ls(const Job& J, const Params& p, const JobState* st, int side,
+                                                      const LeafSum& ls, bool root, int lane) {
   LeafConst c;
   c.first_x = c.brk_x = 0;
   if (p.quant) {
@@ -92,7 +91,7 @@ __device__ __forceinline__ void compute_leaf_const(const Job& J, const Params& p
     c.sum_h = ls.sh + 2.0 * BK_EPS;
     c.cnt_factor = (double)ls.num_data / c.sum_h;
   }
-  c.parent = parent_output_of(p, st, ls);
+  c.parent = parent_output_of(p, root, ls);
   c.mgs = leaf_gain(p, c.sum_g, c.sum_h, ls.num_data, c.parent) + p.min_gain;
   c.mgs_up = __double2float_ru(c.mgs);
   c.mgs_dn = __double2float_rd(c.mgs);
@@ -105,13 +104,42 @@ __device__ __forceinline__ void compute_leaf_const(const Job& J, const Params& p
   if (lane == 0) J.lconst[side] = c;
 }
 
-// Called by every thread of a histogram CTA before its row loop: the last CTA of tile 0 (idle for
-// leaves that do not need the whole grid) computes both sides' constants with its first two warps.
+__device__ __forceinline__ void compute_leaf_const(const Job& J, const Params& p, const JobState* st, int side,
+                                                   int lane) {
+  const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
+  if (leaf < 0) return;
+  compute_leaf_const_ls(J, p, st, side, J.leaf_sum[leaf], st->tree_leaves == 1, lane);
+}
+
+// The histogram CTA that does the serial side work of its launch: the last CTA of tile 0, idle for
+// leaves that do not need the whole grid.
+__device__ __forceinline__ bool hist_side_cta() { return blockIdx.x == gridDim.x - 1 && blockIdx.y == 0; }
+
+// Called by every thread of a histogram CTA before its row loop: the side CTA computes both sides'
+// constants with its first two warps, from the leaf records.
 __device__ __forceinline__ void hist_leaf_constants(const Job& J, const Params& p) {
-  if (blockIdx.x != gridDim.x - 1 || blockIdx.y != 0 || threadIdx.x >= 64) return;
+  if (!hist_side_cta() || threadIdx.x >= 64) return;
   const JobState* st = J.st;
   if (st->stop || !st->do_search) return;
   compute_leaf_const(J, p, st, (int)(threadIdx.x >> 5), (int)(threadIdx.x & 31));
+}
+
+// The same when the launch also applies the previous split (the single-pass partition leaves it
+// to the histogram launch): the side CTA's warps 0 / 1 compute the constants from the split's
+// candidate record and row counts, warp 2 writes the split's bookkeeping.
+__device__ __forceinline__ void hist_apply_split(const Job& J, const Params& p, const SplitOutcome& o) {
+  if (!hist_side_cta() || threadIdx.x >= 96) return;
+  const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
+  if (warp == 2) {
+    post_split_writes(J, p, o, lane);
+    return;
+  }
+  if (!o.go) return;
+  const JobState* st = J.st;
+  const Cand& info = J.cand[(size_t)o.bl * p.F + st->split_inner];
+  LeafSum small, large;
+  split_children(info, o, &small, &large);
+  compute_leaf_const_ls(J, p, st, warp, warp ? large : small, false, lane);
 }
 
 }  // namespace bk

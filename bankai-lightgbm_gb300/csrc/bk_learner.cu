@@ -187,18 +187,22 @@ struct bk_learner {
 
   // One grow-loop step (iteration `it`) of all jobs; with timing on, events split the step into
   // histogram / search / partition phases.
+  // The plain form keeps the reference's stable compaction; so does leaf renewal, whose f64 sums
+  // run in leaf row order. Otherwise split `it` is partitioned in one pass, counting into the
+  // counter pair it & 1, and the histogram launch of step it + 1 applies its bookkeeping.
+  bool stable_partition() const { return loop_mode == 0 || (p.quant && p.renew); }
   void step_a(int it) {
+    const bool stable = stable_partition();
     record_hist_event(4 * it);
-    launch_hist(jobs.data(), K, p, d_bins_rt, d_bins_tm, hl, stream);
+    launch_hist(jobs.data(), K, p, d_bins_rt, d_bins_tm, hl, !stable && it > 0, (it + 1) & 1, stream);
     record_hist_event(4 * it + 1);
-    launch_search(jobs.data(), K, p, d_feat, stream);  // its last CTA also picks the split
+    // its last CTA also picks the split; it clears the counter pair that split it + 1 uses
+    launch_search(jobs.data(), K, p, d_feat, stable ? -1 : (it + 1) & 1, stream);
     record_hist_event(4 * it + 2);
   }
   void step_b(int it) {
-    // the plain form keeps the reference's stable compaction; so does leaf renewal, whose f64 sums
-    // run in leaf row order
-    const bool stable = loop_mode == 0 || (p.quant && p.renew);
-    launch_partition(jobs.data(), K, p, d_bins_cm, d_feat, stable, stream);  // its last CTA also records the split
+    const bool stable = stable_partition();
+    launch_partition(jobs.data(), K, p, d_bins_cm, d_feat, stable, it & 1, stream);
     record_hist_event(4 * it + 3);
   }
 
@@ -211,6 +215,7 @@ struct bk_learner {
   }
 
   void tree_epilogue() {
+    if (!stable_partition()) launch_apply_split(jobs.data(), K, p, (p.num_leaves - 2) & 1, stream);
     if (p.quant && p.renew) launch_renew(d_jobs, K, p, stream);
   }
 

@@ -202,24 +202,30 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const JobTable jobs, 
 // Single-pass partition, for when the order of a child's rows inside its range cannot change any
 // result (no leaf renewal: integer histograms, the score update and the row -> leaf map do not
 // depend on it). Each 2048-row tile claims the slots of its left rows from the front of the
-// range and those of its right rows from the back, one atomic each; inside a tile the rows keep
-// their leaf order. No count pass: the last CTA reads the left total and runs the post-split
-// bookkeeping.
+// range and those of its right rows from the back, one atomic each on the counter pair of this
+// split's parity; inside a tile the rows keep their leaf order. No count pass and no serial tail:
+// the histogram launch that follows reads the left total and applies the split's bookkeeping
+// (bk_grow.cuh), and the search after it clears the counter pair for the split after next.
 __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, Params p,
                                                            const uint8_t* __restrict__ bins_cm,
-                                                           const DevFeature* __restrict__ feats) {
+                                                           const DevFeature* __restrict__ feats, int par) {
   __shared__ uint8_t lut[256];
   __shared__ int32_t sh[32];
   __shared__ int64_t s_off[2];
-  __shared__ int last;
   griddep_wait();
   const Job& J = jobs.job[blockIdx.z];
   JobState* st = J.st;
   if (st->stop) return;
   PartRange R;
-  part_range(J, p, bins_cm, &R);  // its loads are in flight with the route table's
+  part_range(J, p, bins_cm, &R);
+  if ((int)blockIdx.x >= R.active) {  // CTAs past the leaf's rows leave at once
+    griddep_launch();
+    return;
+  }
   build_route(st, feats, lut);
   __syncthreads();
+  unsigned long long* cnt_left = reinterpret_cast<unsigned long long*>(&st->pcnt[par][0]);
+  unsigned long long* cnt_right = reinterpret_cast<unsigned long long*>(&st->pcnt[par][1]);
   for (int64_t base = R.r0; base < R.r1; base += kThreads * kItems) {
     const int64_t e0 = base + (int64_t)threadIdx.x * kItems;
     int32_t rows[kItems];
@@ -237,9 +243,8 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
     const int32_t pre = block_excl_scan<int32_t>(cnt, &tile_left, sh);
     const int32_t n = (int32_t)min((int64_t)kThreads * kItems, R.r1 - base);
     if (threadIdx.x == 0) {
-      s_off[0] = (int64_t)atomicAdd(reinterpret_cast<unsigned long long*>(&st->part_left), (unsigned long long)tile_left);
-      s_off[1] = (int64_t)atomicAdd(reinterpret_cast<unsigned long long*>(&st->part_right),
-                                    (unsigned long long)(n - tile_left));
+      s_off[0] = (int64_t)atomicAdd(cnt_left, (unsigned long long)tile_left);
+      s_off[1] = (int64_t)atomicAdd(cnt_right, (unsigned long long)(n - tile_left));
     }
     __syncthreads();
     // left rows fill [lo, lo + tile_left); right rows fill the tile's slots ending at count - ro
@@ -258,38 +263,20 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
     }
     __syncthreads();  // s_off is rewritten by the next tile
   }
-  griddep_launch();  // only the last CTA's bookkeeping is left: the next histogram may be scheduled
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    __threadfence();
-    unsigned t = atomicAdd(&st->part_done, 1u);
-    last = t == gridDim.x - 1;
-  }
-  __syncthreads();
-  if (!last) return;
-  __threadfence();
-  if (threadIdx.x == 0) {
-    st->total_left = __ldcg(&st->part_left);
-    st->part_left = 0;
-    st->part_right = 0;
-    __threadfence();
-  }
-  __syncthreads();
-  if (threadIdx.x < 32) post_split_body(J, p, feats);
-  if (threadIdx.x == 0) st->part_done = 0u;
+  griddep_launch();
 }
 
 }  // namespace
 
 void launch_partition(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
-                      const DevFeature* feats, bool stable, cudaStream_t s) {
+                      const DevFeature* feats, bool stable, int par, cudaStream_t s) {
   for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
     dim3 grid(p.part_grid, 1, nz);
     if (stable) {
       (void)launch_kernel(k_part_count, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats);
       (void)launch_kernel(k_part_scatter, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats);
     } else {
-      (void)launch_kernel(k_part_onepass, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats);
+      (void)launch_kernel(k_part_onepass, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats, par);
     }
   });
 }

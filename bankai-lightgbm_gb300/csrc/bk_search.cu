@@ -274,8 +274,8 @@ struct QEnt {
 struct SearchSmem {
   QEnt q[2][kSearchThreads];  // per direction: every position at most once
   int32_t qn[2];
-  DirBest pres[2];            // per direction: the arg-max of the queued positions
-  int32_t psplit[2];
+  DirBest pres[2][4];         // per direction and batch lane (below): the arg-max of its batches
+  int32_t psplit[2][4];
   Eval pev[2];                // per direction: the outputs of its only queued position
   int64_t wi[2][kSearchWarps];
   double wd[10][kSearchWarps];
@@ -441,12 +441,13 @@ __device__ __forceinline__ void queue_push(SearchSmem& sm, int d, bool push, con
   if (push) sm.q[d][base + __popc(bal & ((1u << lane) - 1u))] = e;
 }
 
-// One warp: the f64 gains of direction d's queued positions, 32 at a time; their arg-max (highest
-// gain, ties to the earliest position in scan order) and whether any passed, into sm.pres[d] /
-// sm.psplit[d]. The two directions run on two warps (two schedulers): f64 issue throughput is
-// the bottleneck on this part.
+// Queue batches of 32 positions: batch k of direction d runs on warp d + 2 (k mod 4), so the
+// first batches of the two directions run on two schedulers and longer queues spread over all
+// four (f64 issue throughput is the bottleneck of this part). One warp: the f64 gains of its
+// batches k0, k0 + 4, ...; their arg-max (highest gain, ties to the earliest position in scan
+// order) and whether any passed, into sm.pres[d][k0] / sm.psplit[d][k0].
 template <typename Gain>
-__device__ __forceinline__ void eval_dir(SearchSmem& sm, int d, int lane, double mgs, Gain gain_of) {
+__device__ __forceinline__ void eval_batches(SearchSmem& sm, int d, int k0, int lane, double mgs, Gain gain_of) {
   DirBest r;
   r.key = kNoKey;
   r.ev.gain = -CUDART_INF;
@@ -455,15 +456,14 @@ __device__ __forceinline__ void eval_dir(SearchSmem& sm, int d, int lane, double
   r.c = 0;
   int split = 0;
   const int n = sm.qn[d];
-  for (int b0 = 0; b0 < n; b0 += 32) {
+  for (int b0 = 32 * k0; b0 < n; b0 += 128) {
+    // lanes past the queue's end evaluate its last entry and discard the result: an all-zero
+    // entry would send the whole warp through the f64 division's slow path (zero dividend, tiny
+    // divisor), which costs more than the gain itself on this part
     const bool have = b0 + lane < n;
-    QEnt e;
-    e.a = e.b = 0;
-    e.c = 0;
-    e.t = 0;
-    e.d = (int16_t)d;
-    if (have) e = sm.q[d][b0 + lane];
-    const double g = have ? gain_of(e) : -CUDART_INF;
+    const QEnt e = sm.q[d][have ? b0 + lane : n - 1];
+    double g = gain_of(e);
+    if (!have) g = -CUDART_INF;
     const bool passed = have && gain_passes(g, mgs);
     if (__any_sync(FULL, passed)) split = 1;
     const bool elig = passed && !dnan(g) && !is_neg_inf(g);  // NaN never wins
@@ -483,27 +483,38 @@ __device__ __forceinline__ void eval_dir(SearchSmem& sm, int d, int lane, double
     }
   }
   if (lane == 0) {
-    sm.pres[d] = r;
-    sm.psplit[d] = split;
+    sm.pres[d][k0] = r;
+    sm.psplit[d][k0] = split;
   }
 }
 
-// After the queues are filled (barrier 3): warps 0 / 1 evaluate the two directions' gains; warps
-// 2 / 3 evaluate, for a direction with a single queued position, that position's outputs (it is
-// the direction's only possible choice). Barrier 4, then warp 0 holds every result.
+// After the queues are filled (barrier 3): warps 0-7 evaluate the queue batches (warp w takes
+// direction w & 1, batches w >> 1, (w >> 1) + 4, ...); warps 2 / 3, whose direction has a
+// single queued position (so no batch of theirs), evaluate that position's outputs (it is the
+// direction's only possible choice). Barrier 4; then warp 0 combines the batch results of each
+// direction into r / rs.
 template <typename Gain, typename Side>
 __device__ __forceinline__ void eval_queues(SearchSmem& sm, int warp, int lane, double mgs, Gain gain_of,
-                                            Side side_of) {
-  if (warp < 2) {
-    eval_dir(sm, warp, lane, mgs, gain_of);
-  } else if (warp < 4) {
-    const int d = warp - 2;
-    if (sm.qn[d] == 1) {
-      const Eval v = side_of(sm.q[d][0]);
-      if (lane == 0) sm.pev[d] = v;
-    }
+                                            Side side_of, DirBest (&r)[2], int (&rs)[2]) {
+  const int d = warp & 1, k0 = warp >> 1;
+  if (k0 < 4) eval_batches(sm, d, k0, lane, mgs, gain_of);
+  if ((warp == 2 || warp == 3) && sm.qn[d] == 1) {
+    const Eval v = side_of(sm.q[d][0]);
+    if (lane == 0) sm.pev[d] = v;
   }
   __syncthreads();
+  if (warp != 0) return;
+#pragma unroll
+  for (int dd = 0; dd < 2; ++dd) {
+    r[dd] = sm.pres[dd][0];
+    rs[dd] = sm.psplit[dd][0];
+#pragma unroll
+    for (int k = 1; k < 4; ++k) {
+      const DirBest& x = sm.pres[dd][k];
+      rs[dd] |= sm.psplit[dd][k];
+      if (x.key != kNoKey && (x.key > r[dd].key || (x.key == r[dd].key && earlier(dd, x.t, r[dd].t)))) r[dd] = x;
+    }
+  }
 }
 
 __device__ __forceinline__ void store_cand(const Job& J, const Params& p, int side, int32_t leaf, int32_t f,
@@ -672,7 +683,7 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
     const bool rep[2] = {w == 0 && t + 1 <= G.tf_r && !(G.skip && t + 1 + G.off == m.default_bin),
                          !xpos && w == 0 && ((t >= 1 && !(G.skip && t - 1 + G.off == m.default_bin)) ||
                                              (t == 0 && G.fwd_rest))};
-    // barrier 3: the few positions that need their f64 gain; barrier 4: evaluated on four warps
+    // barrier 3: the few positions that need their f64 gain; barrier 4: evaluated on the eight warps
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
       const bool exact = valid[d] && !rep[d] && (fl[d].unc || (fl[d].mp && fl[d].up >= M[d]));
@@ -683,13 +694,9 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
     eval_queues(
         sm, warp, lane, C.mgs,
         [&](const QEnt& e) { return int_split_gain(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, true); },
-        [&](const QEnt& e) { return eval_int(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, 0.0, lane); });
+        [&](const QEnt& e) { return eval_int(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, 0.0, lane); }, r,
+        rs);
     if (warp != 0) return;
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      r[d] = sm.pres[d];
-      rs[d] = sm.psplit[d];
-    }
   } else {
     // every valid position evaluates its own f64 gain; barrier 3: the arg-max
     double gain[2];
@@ -900,23 +907,21 @@ __device__ void search_float(const Job& J, const Params& p, const JobState* st, 
     const bool rep[2] = {empty && t + 1 <= G.tf_r && !(G.skip && t + 1 + G.off == m.default_bin),
                          !xpos && empty && ((t >= 1 && !(G.skip && t - 1 + G.off == m.default_bin)) ||
                                             (t == 0 && G.fwd_rest))};
-    // barrier 3: the few positions that need their f64 gain; barrier 4: evaluated on four warps
+    // barrier 3: the few positions that need their f64 gain; barrier 4: evaluated on the eight warps
 #pragma unroll
     for (int d = 0; d < 2; ++d) {
       const bool exact = valid[d] && !rep[d] && (fl[d].unc || (fl[d].mp && fl[d].up >= M[d]));
       queue_push(sm, d, exact, QEnt{ca[d], cb[d], cc[d], (int16_t)(d == 0 || !xpos ? t : -1), (int16_t)d}, lane);
     }
     __syncthreads();
-    eval_queues(sm, warp, lane, C.mgs, gain_of, [&](const QEnt& e) {
-      return eval_float(p, e.d, __longlong_as_double(e.a), __longlong_as_double(e.b), e.c, sum_g, sum_h, num_data,
-                        C.parent, 0.0, lane);
-    });
+    eval_queues(
+        sm, warp, lane, C.mgs, gain_of,
+        [&](const QEnt& e) {
+          return eval_float(p, e.d, __longlong_as_double(e.a), __longlong_as_double(e.b), e.c, sum_g, sum_h,
+                            num_data, C.parent, 0.0, lane);
+        },
+        r, rs);
     if (warp != 0) return;
-#pragma unroll
-    for (int d = 0; d < 2; ++d) {
-      r[d] = sm.pres[d];
-      rs[d] = sm.psplit[d];
-    }
   } else {
     double gain[2];
     bool split[2], elig[2];
@@ -1020,7 +1025,7 @@ __device__ void decide_body(const Job& J, const Params& p, const DevFeature* fea
   // the row range of the first kSearchThreads leaves, so the chosen leaf's is at hand for the
   // partition that follows
   __shared__ int64_t s_lb[kSearchThreads], s_lc[kSearchThreads];
-  __shared__ int32_t s_lbuf[kSearchThreads];
+  __shared__ int32_t s_lbuf[kSearchThreads], s_ld[kSearchThreads];
   JobState* st = J.st;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   constexpr int kHalf = kSearchThreads / 2;
@@ -1029,22 +1034,22 @@ __device__ void decide_body(const Job& J, const Params& p, const DevFeature* fea
   const Pick none{-1, 0x7fffffff, 0, false, 0.0, 0};
   // serial.rs:1523-1558 — fold the candidates of each searched leaf in feature order: the first
   // half of the CTA folds the smaller leaf, the second half the larger one
+  // the candidate and leaf loads do not depend on the state: issued together with its loads, so
+  // the fold and the arg-max wait for one memory round trip
   Pick a = none;
-  if (searched) {
+  {
     const int side = t / kHalf;
     const int32_t leaf = side ? leaf1 : leaf0;
     const int32_t slot = side ? st->larger_slot : st->smaller_slot;
-    if (leaf >= 0) {
-      for (int f = t % kHalf; f < p.F; f += kHalf) {
-        const uint8_t u = J.used[f];
-        const uint8_t cs = __ldcg(&J.csplit[side * p.F + f]);
-        const double g = __ldcg(&J.cgain[side * p.F + f]);
-        const uint32_t th = __ldcg(&J.cthr[side * p.F + f]);
-        const int real = feats[f].real;
-        if (!u) continue;
-        J.splittable[(size_t)slot * p.F + f] = cs;
-        pick(a, make_pick(f, g, real, th));
-      }
+    for (int f = t % kHalf; f < p.F; f += kHalf) {
+      const uint8_t u = J.used[f];
+      const uint8_t cs = __ldcg(&J.csplit[side * p.F + f]);
+      const double g = __ldcg(&J.cgain[side * p.F + f]);
+      const uint32_t th = __ldcg(&J.cthr[side * p.F + f]);
+      const int real = feats[f].real;
+      if (!searched || leaf < 0 || !u) continue;
+      J.splittable[(size_t)slot * p.F + f] = cs;
+      pick(a, make_pick(f, g, real, th));
     }
   }
   // split_info.rs:125-133 — first arg-max leaf under better_than; the searched leaves' new bests
@@ -1056,9 +1061,13 @@ __device__ void decide_body(const Job& J, const Params& p, const DevFeature* fea
       s_lb[i] = J.leaf_begin[i];
       s_lc[i] = J.leaf_count[i];
       s_lbuf[i] = J.leaf_buf[i];
+      s_ld[i] = J.leaf_depth[i];
     }
+    const double bg = J.bgain[i];
+    const int32_t bf = J.bfeat[i];
+    const int64_t bs = J.bsplit[i];
     if (searched && (i == leaf0 || i == leaf1)) continue;
-    leaf_pick(b, make_pick(i, J.bgain[i], J.bfeat[i], J.bsplit[i]));
+    leaf_pick(b, make_pick(i, bg, bf, bs));
   }
   if (searched) {
 #pragma unroll
@@ -1105,6 +1114,8 @@ __device__ void decide_body(const Job& J, const Params& p, const DevFeature* fea
     st->split_begin = near ? s_lb[w.i] : J.leaf_begin[w.i];
     st->split_count = near ? s_lc[w.i] : J.leaf_count[w.i];
     st->split_buf = near ? s_lbuf[w.i] : J.leaf_buf[w.i];
+    st->split_depth = near ? s_ld[w.i] : J.leaf_depth[w.i];
+    st->split_sslot = st->next_free;
     st->split_leaf = w.i;
     st->split_inner = inner;
     st->split_thr = (uint32_t)(w.pay & 0xffffffffLL);
@@ -1116,7 +1127,7 @@ __device__ void decide_body(const Job& J, const Params& p, const DevFeature* fea
 // finish runs the fold / arg-max.
 template <bool PLAIN, bool QUANT>
 __global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, Params p,
-                                                           const DevFeature* __restrict__ feats) {
+                                                           const DevFeature* __restrict__ feats, int clear_par) {
   __shared__ SearchSmem sm;
   __shared__ int last;
   const int side = (int)(blockIdx.x & 1u);
@@ -1125,6 +1136,11 @@ __global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, 
   griddep_wait();
   const Job& J = jobs.job[blockIdx.z];
   JobState* st = J.st;
+  if (clear_par >= 0 && blockIdx.x == 0 && threadIdx.x < 2) {
+    // the single-pass partition counter pair of the split after next: its last reader, the
+    // histogram launch before this one, has finished
+    st->pcnt[clear_par][threadIdx.x] = 0;
+  }
   if (st->stop) return;  // uniform over the grid
   const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
   if (st->do_search && J.used[f] && leaf >= 0) {  // uniform over the CTA
@@ -1145,6 +1161,16 @@ __global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, 
   __threadfence();
   decide_body(J, p, feats);
   if (threadIdx.x == 0) st->search_done = 0u;
+}
+
+// The bookkeeping of a tree's last split when it was partitioned in one pass (no histogram launch
+// follows it to apply it).
+__global__ void __launch_bounds__(32) k_apply_split(const JobTable jobs, Params p, int par) {
+  const Job& J = jobs.job[blockIdx.z];
+  JobState* st = J.st;
+  if (st->stop) return;
+  const SplitOutcome o = split_outcome(p, st, __ldcg(&st->pcnt[par][0]));
+  post_split_writes(J, p, o, (int)threadIdx.x);
 }
 
 // Root of a tree (serial.rs:658-776 after the root sums, then :580-586 and the first
@@ -1170,6 +1196,7 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
       st->stop = 0;
       st->tree_leaves = 1;
       st->next_free = 0;
+      st->pcnt[0][0] = st->pcnt[0][1] = st->pcnt[1][0] = st->pcnt[1][1] = 0;
       const LeafSum r = J.leaf_sum[0];
       double root = leaf_output_root(p, r.sg, r.sh, r.num_data);
       st->root_output = round_to_zero(root);
@@ -1182,18 +1209,25 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
 
 }  // namespace
 
-void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, cudaStream_t s) {
+void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, int clear_par,
+                   cudaStream_t s) {
   const bool plain = !p.use_l1 && !p.use_max && !p.use_smooth;
   const dim3 block(kSearchThreads);
   for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
     dim3 grid((unsigned)(2 * p.F), 1, nz);
     if (p.quant) {
-      if (plain) (void)launch_kernel(k_search<true, true>, grid, block, 0, s, p.pdl, t, p, feats);
-      else (void)launch_kernel(k_search<false, true>, grid, block, 0, s, p.pdl, t, p, feats);
+      if (plain) (void)launch_kernel(k_search<true, true>, grid, block, 0, s, p.pdl, t, p, feats, clear_par);
+      else (void)launch_kernel(k_search<false, true>, grid, block, 0, s, p.pdl, t, p, feats, clear_par);
     } else {
-      if (plain) (void)launch_kernel(k_search<true, false>, grid, block, 0, s, p.pdl, t, p, feats);
-      else (void)launch_kernel(k_search<false, false>, grid, block, 0, s, p.pdl, t, p, feats);
+      if (plain) (void)launch_kernel(k_search<true, false>, grid, block, 0, s, p.pdl, t, p, feats, clear_par);
+      else (void)launch_kernel(k_search<false, false>, grid, block, 0, s, p.pdl, t, p, feats, clear_par);
     }
+  });
+}
+
+void launch_apply_split(const Job* h_jobs, int num_jobs, const Params& p, int par, cudaStream_t s) {
+  for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
+    k_apply_split<<<dim3(1, 1, nz), 32, 0, s>>>(t, p, par);
   });
 }
 
