@@ -180,14 +180,16 @@ size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide);
 
 // The bookkeeping of the last split of a tree partitioned in one pass (counter pair `par`).
 void launch_apply_split(const Job* h_jobs, int num_jobs, const Params& p, int par, cudaStream_t s);
-// clear_par >= 0: the launch zeroes that single-pass partition counter pair first.
+// clear_par >= 0: the launch zeroes that single-pass partition counter pair first. decide: its
+// last CTA decides and records the split (else the single-pass partition decides it).
 void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, int clear_par,
-                   cudaStream_t s);
+                   bool decide, cudaStream_t s);
 // stable: the two-kernel compaction whose last CTA applies the split's bookkeeping; otherwise the
 // single-pass partition, counting into the counter pair `par` (the split index's parity), whose
 // bookkeeping the next histogram launch applies.
+// decide (single-pass only): every CTA decides the split from the search's records first.
 void launch_partition(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
-                      const DevFeature* feats, bool stable, int par, cudaStream_t s);
+                      const DevFeature* feats, bool stable, int par, bool decide, cudaStream_t s);
 
 cudaError_t hist_set_smem_attrs(size_t smem);
 

@@ -1,0 +1,230 @@
+// The split decision after a search (serial.rs:1523-1558 fold of each searched leaf's candidates
+// in feature order, split_info.rs:67-133 better_than / argmax over the leaves, serial.rs:611 stop
+// on a gain <= 0): shared by the search launch (its last CTA decides) and the single-pass
+// partition (every CTA decides the same split from the same records, CTA 0 records it).
+#pragma once
+#include <math_constants.h>
+
+#include "bk_common.cuh"
+
+namespace bk {
+
+namespace {
+
+constexpr unsigned FULL = 0xffffffffu;
+constexpr int kDecideThreads = 256;  // the decision runs on one 256-thread CTA
+constexpr int kDecideWarps = kDecideThreads / 32;
+constexpr long long kNoKey = (long long)0x8000000000000000ULL;
+
+// Order-preserving integer key of an f64 gain (the fold and arg-max compare keys, not doubles:
+// f64 comparisons are slow on this part).
+__device__ __forceinline__ long long dkey(double x) {
+  long long b = __double_as_longlong(x);
+  if (b == kNoKey) b = 0;
+  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
+}
+__device__ __forceinline__ bool dnan(double x) {
+  return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL;
+}
+
+
+// split_info.rs:104-121 (better_than) on keys: the higher gain, then the smaller real feature
+// (-1 counts as largest); with a NaN gain on either side neither is better.
+__device__ __forceinline__ bool better_k(long long ka, bool na, int fa, long long kb, bool nb, int fb) {
+  if (na || nb) return false;
+  if (ka != kb) return ka > kb;
+  const int a = fa == -1 ? 0x7fffffff : fa;
+  const int b = fb == -1 ? 0x7fffffff : fb;
+  return a < b;
+}
+
+struct Pick {
+  int i, f;     // index (-1: none), real feature
+  long long k;  // dkey of the gain
+  bool nan;
+  double g;     // the gain
+  long long pay;  // fold: threshold | default_left << 31; leaf arg-max: the split descriptor
+};
+
+// Fold step: `a` comes first in the sequential order; `b` replaces it only when strictly better;
+// NaN gains never win (the sequential fold never adopts them).
+__device__ __forceinline__ void pick(Pick& a, const Pick& b) {
+  if (b.i < 0 || b.nan) return;
+  if (a.i < 0 || better_k(b.k, false, b.f, a.k, a.nan, a.f) || (!better_k(a.k, a.nan, a.f, b.k, false, b.f) && b.i < a.i))
+    a = b;
+}
+
+// Arg-max step over leaves: the first arg-max under better_than, ties to the smaller index.
+__device__ __forceinline__ void leaf_pick(Pick& a, const Pick& b) {
+  if (b.i < 0) return;
+  if (a.i < 0 || better_k(b.k, b.nan, b.f, a.k, a.nan, a.f) || (!better_k(a.k, a.nan, a.f, b.k, b.nan, b.f) && b.i < a.i))
+    a = b;
+}
+
+__device__ __forceinline__ Pick shfl_pick(const Pick& a, int src_or_mask, bool xor_mode) {
+  Pick b;
+  if (xor_mode) {
+    b.i = __shfl_xor_sync(FULL, a.i, src_or_mask);
+    b.f = __shfl_xor_sync(FULL, a.f, src_or_mask);
+    b.k = __shfl_xor_sync(FULL, a.k, src_or_mask);
+    b.nan = __shfl_xor_sync(FULL, (int)a.nan, src_or_mask) != 0;
+    b.g = __shfl_xor_sync(FULL, a.g, src_or_mask);
+    b.pay = __shfl_xor_sync(FULL, a.pay, src_or_mask);
+  } else {
+    b.i = __shfl_sync(FULL, a.i, src_or_mask);
+    b.f = __shfl_sync(FULL, a.f, src_or_mask);
+    b.k = __shfl_sync(FULL, a.k, src_or_mask);
+    b.nan = __shfl_sync(FULL, (int)a.nan, src_or_mask) != 0;
+    b.g = __shfl_sync(FULL, a.g, src_or_mask);
+    b.pay = __shfl_sync(FULL, a.pay, src_or_mask);
+  }
+  return b;
+}
+
+__device__ __forceinline__ Pick make_pick(int i, double g, int f, long long pay) {
+  return Pick{i, f, dkey(g), dnan(g), g, pay};
+}
+
+// The chosen split, as every CTA that decides it sees it.
+struct Decision {
+  int32_t stop, leaf, inner, buf, depth, sslot, new_leaf;
+  uint32_t thr;  // threshold | default_left << 31
+  int64_t begin, count;
+};
+
+// The fold of the searched leaves' candidates and the leaf arg-max on one CTA of kDecideThreads
+// threads. Every thread gets the chosen split through `out` (written by thread 0: the caller
+// synchronizes before reading it). With `record`, the decision's effects are written to the job:
+// the searched leaves' new bests and splittable flags, the chosen split (the row range, depth and
+// new pool slot the partition and the next histogram launch use) or the stop flag; without it
+// nothing is written, so several CTAs can decide the same split from the same records. Every load
+// is issued up front (the candidates of both searched leaves and every other leaf's best), then
+// one barrier; warp 0 finishes. Candidates written by other CTAs are read through L2 (__ldcg). A
+// leaf's best split stays in cand[leaf][feature]; the partition builds the route table of the
+// chosen split from (inner, thr).
+__device__ void decide_split(const Job& J, const Params& p, const DevFeature* feats, bool record, Decision* out) {
+  __shared__ Pick s_f[kDecideWarps], s_l[kDecideWarps];
+  // the row range of the first kDecideThreads leaves, so the chosen leaf's is at hand for the
+  // partition that follows
+  __shared__ int64_t s_lb[kDecideThreads], s_lc[kDecideThreads];
+  __shared__ int32_t s_lbuf[kDecideThreads], s_ld[kDecideThreads];
+  JobState* st = J.st;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  constexpr int kHalf = kDecideThreads / 2;
+  const bool searched = st->do_search != 0;
+  const int32_t leaf0 = st->smaller_leaf, leaf1 = st->larger_leaf;
+  const Pick none{-1, 0x7fffffff, 0, false, 0.0, 0};
+  // serial.rs:1523-1558 — fold the candidates of each searched leaf in feature order: the first
+  // half of the CTA folds the smaller leaf, the second half the larger one
+  // the candidate and leaf loads do not depend on the state: issued together with its loads, so
+  // the fold and the arg-max wait for one memory round trip
+  Pick a = none;
+  {
+    const int side = t / kHalf;
+    const int32_t leaf = side ? leaf1 : leaf0;
+    const int32_t slot = side ? st->larger_slot : st->smaller_slot;
+    for (int f = t % kHalf; f < p.F; f += kHalf) {
+      const uint8_t u = J.used[f];
+      const uint8_t cs = __ldcg(&J.csplit[side * p.F + f]);
+      const double g = __ldcg(&J.cgain[side * p.F + f]);
+      const uint32_t th = __ldcg(&J.cthr[side * p.F + f]);
+      const int real = feats[f].real;
+      if (!searched || leaf < 0 || !u) continue;
+      if (record) J.splittable[(size_t)slot * p.F + f] = cs;
+      pick(a, make_pick(f, g, real, th));
+    }
+  }
+  // split_info.rs:125-133 — first arg-max leaf under better_than; the searched leaves' new bests
+  // join from the fold
+  Pick b = none;
+  b.f = 0;
+  for (int i = t; i < p.num_leaves; i += kDecideThreads) {
+    if (i < kDecideThreads) {
+      s_lb[i] = J.leaf_begin[i];
+      s_lc[i] = J.leaf_count[i];
+      s_lbuf[i] = J.leaf_buf[i];
+      s_ld[i] = J.leaf_depth[i];
+    }
+    const double bg = J.bgain[i];
+    const int32_t bf = J.bfeat[i];
+    const int64_t bs = J.bsplit[i];
+    if (searched && (i == leaf0 || i == leaf1)) continue;
+    leaf_pick(b, make_pick(i, bg, bf, bs));
+  }
+  if (searched) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) pick(a, shfl_pick(a, o, true));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) leaf_pick(b, shfl_pick(b, o, true));
+  if (lane == 0) {
+    s_f[warp] = a;
+    s_l[warp] = b;
+  }
+  __syncthreads();
+  if (warp != 0) return;
+  // lanes 0 / 1: the new best of the smaller / larger leaf
+  Pick nb = none;
+  const int32_t my_leaf = lane == 0 ? leaf0 : leaf1;
+  if (searched && lane < 2 && my_leaf >= 0) {
+    Pick fa = none;
+    for (int w = lane * (kDecideWarps / 2); w < (lane + 1) * (kDecideWarps / 2); ++w) pick(fa, s_f[w]);
+    // the fold starts from SplitInfo::default (gain -inf, feature -1) and replaces it only with a
+    // better candidate
+    const bool take = fa.i >= 0 && better_k(fa.k, fa.nan, fa.f, dkey(-CUDART_INF), false, -1);
+    if (take)
+      nb = Pick{my_leaf, fa.f, fa.k, fa.nan, fa.g, (long long)fa.i * 4294967296LL + (long long)(uint32_t)fa.pay};
+    else
+      nb = make_pick(my_leaf, -CUDART_INF, -1, (long long)-1 * 4294967296LL);
+    if (record) {
+      J.bgain[my_leaf] = nb.g;
+      J.bfeat[my_leaf] = nb.f;
+      J.bsplit[my_leaf] = nb.pay;
+    }
+  }
+  // the leaf arg-max over the 8 warp partials (lanes 0..7) and the searched leaves (lanes 8, 9)
+  const Pick moved = shfl_pick(nb, lane & 1, false);
+  Pick w = lane < kDecideWarps ? s_l[lane] : ((lane == 8 || lane == 9) ? moved : none);
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) leaf_pick(w, shfl_pick(w, o, true));
+  const int32_t inner = w.i >= 0 ? (int32_t)(w.pay >> 32) : -1;
+  // serial.rs:611 — a best gain <= 0 stops the tree
+  if ((!w.nan && w.k <= 0) || inner < 0) {
+    if (lane == 0) {
+      out->stop = 1;
+      if (record) st->stop = 1;
+    }
+    return;
+  }
+  if (lane == 0) {
+    const bool near = w.i < kDecideThreads;
+    Decision d;
+    d.stop = 0;
+    d.leaf = w.i;
+    d.inner = inner;
+    d.thr = (uint32_t)(w.pay & 0xffffffffLL);
+    d.begin = near ? s_lb[w.i] : J.leaf_begin[w.i];
+    d.count = near ? s_lc[w.i] : J.leaf_count[w.i];
+    d.buf = near ? s_lbuf[w.i] : J.leaf_buf[w.i];
+    d.depth = near ? s_ld[w.i] : J.leaf_depth[w.i];
+    d.sslot = st->next_free;
+    d.new_leaf = st->tree_leaves;
+    *out = d;
+    if (record) {
+      st->split_begin = d.begin;
+      st->split_count = d.count;
+      st->split_buf = d.buf;
+      st->split_depth = d.depth;
+      st->split_sslot = d.sslot;
+      st->split_leaf = d.leaf;
+      st->split_inner = d.inner;
+      st->split_thr = d.thr;
+      st->new_leaf = d.new_leaf;
+    }
+  }
+}
+
+
+}  // namespace
+
+}  // namespace bk

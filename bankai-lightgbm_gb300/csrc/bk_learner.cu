@@ -196,13 +196,14 @@ struct bk_learner {
     record_hist_event(4 * it);
     launch_hist(jobs.data(), K, p, d_bins_rt, d_bins_tm, hl, !stable && it > 0, (it + 1) & 1, stream);
     record_hist_event(4 * it + 1);
-    // its last CTA also picks the split; it clears the counter pair that split it + 1 uses
-    launch_search(jobs.data(), K, p, d_feat, stable ? -1 : (it + 1) & 1, stream);
+    // it clears the counter pair that split it + 1 uses; on the stable path its last CTA also
+    // decides the split, otherwise the partition does
+    launch_search(jobs.data(), K, p, d_feat, stable ? -1 : (it + 1) & 1, stable, stream);
     record_hist_event(4 * it + 2);
   }
   void step_b(int it) {
     const bool stable = stable_partition();
-    launch_partition(jobs.data(), K, p, d_bins_cm, d_feat, stable, it & 1, stream);
+    launch_partition(jobs.data(), K, p, d_bins_cm, d_feat, stable, it & 1, !stable, stream);
     record_hist_event(4 * it + 3);
   }
 

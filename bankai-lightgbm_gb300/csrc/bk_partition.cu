@@ -10,6 +10,7 @@
 // (so the step can be captured in a CUDA graph while the leaf size varies): count the left rows
 // of each CTA's contiguous chunk; then scatter, each CTA summing the counts of the chunks before
 // its own (at most a few hundred) and ordering its rows with block-wide scans.
+#include "bk_decide.cuh"
 #include "bk_grow.cuh"
 #include "bk_launch.cuh"
 
@@ -36,14 +37,31 @@ __device__ __forceinline__ int32_t part_pk(const PartRange& R, int64_t e, int32_
   return R.pk_row ? R.pk_src[row] : R.pk_src[e];
 }
 
-__device__ __forceinline__ void part_range(const Job& J, const Params& p, const uint8_t* bins_cm, PartRange* r) {
+// The split recorded in the job state (the search launch decided it).
+__device__ __forceinline__ Decision recorded_decision(const JobState* st) {
+  Decision d;
+  d.stop = st->stop;
+  d.leaf = st->split_leaf;
+  d.inner = st->split_inner;
+  d.thr = st->split_thr;
+  d.begin = st->split_begin;
+  d.count = st->split_count;
+  d.buf = st->split_buf;
+  d.depth = st->split_depth;
+  d.sslot = st->split_sslot;
+  d.new_leaf = st->new_leaf;
+  return d;
+}
+
+__device__ __forceinline__ void part_range(const Job& J, const Params& p, const uint8_t* bins_cm, const Decision& d,
+                                           PartRange* r) {
   const JobState* st = J.st;
-  r->begin = st->split_begin;
-  r->count = st->split_count;
-  const int32_t buf = st->split_buf;
+  r->begin = d.begin;
+  r->count = d.count;
+  const int32_t buf = d.buf;
   r->src = leaf_idx(J, buf) + r->begin;
   r->dst = leaf_idx_w(J, 1 - buf) + r->begin;
-  r->col = bins_cm + (size_t)st->split_inner * (size_t)p.n;
+  r->col = bins_cm + (size_t)d.inner * (size_t)p.n;
   r->pk_row = st->tree_leaves == 1;  // the root: no leaf-ordered copy yet
   r->pk_src = p.quant ? (r->pk_row ? J.packed : leaf_pk(J, buf) + r->begin) : nullptr;
   r->pk_dst = p.quant ? leaf_pk(J, 1 - buf) + r->begin : nullptr;
@@ -84,9 +102,9 @@ __device__ __forceinline__ T block_excl_scan(T v, T* total, T* sh) {
 }
 
 // The route of every stored bin of the chosen split (data_partition.rs:299-410), one per thread.
-__device__ __forceinline__ void build_route(const JobState* st, const DevFeature* feats, uint8_t* lut) {
-  const DevFeature m = feats[st->split_inner];
-  const uint32_t th = st->split_thr;
+__device__ __forceinline__ void build_route(const Decision& d, const DevFeature* feats, uint8_t* lut) {
+  const DevFeature m = feats[d.inner];
+  const uint32_t th = d.thr;
   const uint32_t b = threadIdx.x;
   lut[b] = (int)b < m.gbins ? route_bin(m, th & 0x7fffffffu, (th >> 31) != 0, b) : 0;
 }
@@ -99,9 +117,10 @@ __global__ void __launch_bounds__(kThreads) k_part_count(const JobTable jobs, Pa
   griddep_wait();
   const Job& J = jobs.job[blockIdx.z];
   if (J.st->stop) return;
+  const Decision dec = recorded_decision(J.st);
   PartRange R;
-  part_range(J, p, bins_cm, &R);  // its loads are in flight with the route table's
-  build_route(J.st, feats, lut);
+  part_range(J, p, bins_cm, dec, &R);  // its loads are in flight with the route table's
+  build_route(dec, feats, lut);
   __syncthreads();
   if ((int)blockIdx.x >= R.active) {  // no rows: the scatter reads only active CTAs' counts
     griddep_launch();
@@ -135,9 +154,10 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const JobTable jobs, 
   const Job& J = jobs.job[blockIdx.z];
   if (J.st->stop) return;
   __shared__ int64_t sh64[32];
+  const Decision dec = recorded_decision(J.st);
   PartRange R;
-  part_range(J, p, bins_cm, &R);  // its loads are in flight with the route table's
-  build_route(J.st, feats, lut);
+  part_range(J, p, bins_cm, dec, &R);  // its loads are in flight with the route table's
+  build_route(dec, feats, lut);
   __syncthreads();
   // left rows before this chunk, and in total
   int64_t before = 0, all = 0;
@@ -208,21 +228,32 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const JobTable jobs, 
 // (bk_grow.cuh), and the search after it clears the counter pair for the split after next.
 __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, Params p,
                                                            const uint8_t* __restrict__ bins_cm,
-                                                           const DevFeature* __restrict__ feats, int par) {
+                                                           const DevFeature* __restrict__ feats, int par,
+                                                           int decide) {
+  static_assert(kThreads == kDecideThreads, "the partition CTA runs the split decision");
   __shared__ uint8_t lut[256];
   __shared__ int32_t sh[32];
   __shared__ int64_t s_off[2];
+  __shared__ Decision dec;
   griddep_wait();
   const Job& J = jobs.job[blockIdx.z];
   JobState* st = J.st;
   if (st->stop) return;
+  if (decide) {
+    // every CTA decides the split from the search's records; CTA 0 records it
+    decide_split(J, p, feats, blockIdx.x == 0, &dec);
+  } else if (threadIdx.x == 0) {
+    dec = recorded_decision(st);
+  }
+  __syncthreads();
+  if (dec.stop) return;
   PartRange R;
-  part_range(J, p, bins_cm, &R);
+  part_range(J, p, bins_cm, dec, &R);
   if ((int)blockIdx.x >= R.active) {  // CTAs past the leaf's rows leave at once
     griddep_launch();
     return;
   }
-  build_route(st, feats, lut);
+  build_route(dec, feats, lut);
   __syncthreads();
   unsigned long long* cnt_left = reinterpret_cast<unsigned long long*>(&st->pcnt[par][0]);
   unsigned long long* cnt_right = reinterpret_cast<unsigned long long*>(&st->pcnt[par][1]);
@@ -269,14 +300,15 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
 }  // namespace
 
 void launch_partition(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_cm,
-                      const DevFeature* feats, bool stable, int par, cudaStream_t s) {
+                      const DevFeature* feats, bool stable, int par, bool decide, cudaStream_t s) {
   for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
     dim3 grid(p.part_grid, 1, nz);
     if (stable) {
       (void)launch_kernel(k_part_count, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats);
       (void)launch_kernel(k_part_scatter, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats);
     } else {
-      (void)launch_kernel(k_part_onepass, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats, par);
+      (void)launch_kernel(k_part_onepass, grid, dim3(kThreads), 0, s, p.pdl, t, p, bins_cm, feats, par,
+                          decide ? 1 : 0);
     }
   });
 }

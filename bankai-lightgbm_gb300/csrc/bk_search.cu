@@ -26,6 +26,7 @@
 // bookkeeping (bk_grow.cuh) runs in the last CTA of the partition scatter.
 #include <math_constants.h>
 
+#include "bk_decide.cuh"
 #include "bk_grow.cuh"
 #include "bk_launch.cuh"
 #include "bk_leaf.cuh"
@@ -35,10 +36,8 @@ namespace bk {
 
 namespace {
 
-constexpr unsigned FULL = 0xffffffffu;
-constexpr int kSearchThreads = 256;  // one thread per local bin
+constexpr int kSearchThreads = kDecideThreads;  // one thread per local bin
 constexpr int kSearchWarps = kSearchThreads / 32;
-constexpr long long kNoKey = (long long)0x8000000000000000ULL;
 
 template <typename T>
 __device__ __forceinline__ T warp_incl_scan(T v, int lane) {
@@ -87,15 +86,6 @@ __device__ __forceinline__ int32_t float_key(float x) {
   if (b == (int32_t)0x80000000) b = 0;
   return b ^ ((b >> 31) & 0x7fffffff);
 }
-__device__ __forceinline__ long long dkey(double x) {
-  long long b = __double_as_longlong(x);
-  if (b == kNoKey) b = 0;
-  return b ^ ((b >> 63) & 0x7fffffffffffffffLL);
-}
-__device__ __forceinline__ bool dnan(double x) {
-  return ((unsigned long long)__double_as_longlong(x) & 0x7fffffffffffffffULL) > 0x7ff0000000000000ULL;
-}
-
 // ---- fp32 prefilter of the plain split gain (no L1 / max_delta_step / path_smooth) ----
 // The reference evaluates gl^2/(hl+l2) + gr^2/(hr+l2) in f64 for every threshold. Each candidate is
 // first evaluated in fp32 together with a rigorous bound E on |fp32 - f64| (u = 2^-24): the
@@ -956,180 +946,16 @@ __device__ void search_float(const Job& J, const Params& p, const JobState* st, 
   });
 }
 
-// ---- the fold and the leaf arg-max on integer keys ----
-
-// split_info.rs:104-121 (better_than) on keys: the higher gain, then the smaller real feature
-// (-1 counts as largest); with a NaN gain on either side neither is better.
-__device__ __forceinline__ bool better_k(long long ka, bool na, int fa, long long kb, bool nb, int fb) {
-  if (na || nb) return false;
-  if (ka != kb) return ka > kb;
-  const int a = fa == -1 ? 0x7fffffff : fa;
-  const int b = fb == -1 ? 0x7fffffff : fb;
-  return a < b;
-}
-
-struct Pick {
-  int i, f;     // index (-1: none), real feature
-  long long k;  // dkey of the gain
-  bool nan;
-  double g;     // the gain
-  long long pay;  // fold: threshold | default_left << 31; leaf arg-max: the split descriptor
-};
-
-// Fold step: `a` comes first in the sequential order; `b` replaces it only when strictly better;
-// NaN gains never win (the sequential fold never adopts them).
-__device__ __forceinline__ void pick(Pick& a, const Pick& b) {
-  if (b.i < 0 || b.nan) return;
-  if (a.i < 0 || better_k(b.k, false, b.f, a.k, a.nan, a.f) || (!better_k(a.k, a.nan, a.f, b.k, false, b.f) && b.i < a.i))
-    a = b;
-}
-
-// Arg-max step over leaves: the first arg-max under better_than, ties to the smaller index.
-__device__ __forceinline__ void leaf_pick(Pick& a, const Pick& b) {
-  if (b.i < 0) return;
-  if (a.i < 0 || better_k(b.k, b.nan, b.f, a.k, a.nan, a.f) || (!better_k(a.k, a.nan, a.f, b.k, b.nan, b.f) && b.i < a.i))
-    a = b;
-}
-
-__device__ __forceinline__ Pick shfl_pick(const Pick& a, int src_or_mask, bool xor_mode) {
-  Pick b;
-  if (xor_mode) {
-    b.i = __shfl_xor_sync(FULL, a.i, src_or_mask);
-    b.f = __shfl_xor_sync(FULL, a.f, src_or_mask);
-    b.k = __shfl_xor_sync(FULL, a.k, src_or_mask);
-    b.nan = __shfl_xor_sync(FULL, (int)a.nan, src_or_mask) != 0;
-    b.g = __shfl_xor_sync(FULL, a.g, src_or_mask);
-    b.pay = __shfl_xor_sync(FULL, a.pay, src_or_mask);
-  } else {
-    b.i = __shfl_sync(FULL, a.i, src_or_mask);
-    b.f = __shfl_sync(FULL, a.f, src_or_mask);
-    b.k = __shfl_sync(FULL, a.k, src_or_mask);
-    b.nan = __shfl_sync(FULL, (int)a.nan, src_or_mask) != 0;
-    b.g = __shfl_sync(FULL, a.g, src_or_mask);
-    b.pay = __shfl_sync(FULL, a.pay, src_or_mask);
-  }
-  return b;
-}
-
-__device__ __forceinline__ Pick make_pick(int i, double g, int f, long long pay) {
-  return Pick{i, f, dkey(g), dnan(g), g, pay};
-}
-
-// The fold of the searched leaves' candidates and the leaf arg-max, run by the last CTA of the
-// search launch. Every load is issued up front (the candidates of both searched leaves and every
-// other leaf's best), then one barrier; warp 0 finishes. Everything written by other CTAs of the
-// launch is read through L2 (__ldcg). A leaf's best split stays in cand[leaf][feature]; the
-// partition builds the route table of the chosen split from (split_inner, split_thr).
-__device__ void decide_body(const Job& J, const Params& p, const DevFeature* feats) {
-  __shared__ Pick s_f[kSearchWarps], s_l[kSearchWarps];
-  // the row range of the first kSearchThreads leaves, so the chosen leaf's is at hand for the
-  // partition that follows
-  __shared__ int64_t s_lb[kSearchThreads], s_lc[kSearchThreads];
-  __shared__ int32_t s_lbuf[kSearchThreads], s_ld[kSearchThreads];
-  JobState* st = J.st;
-  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  constexpr int kHalf = kSearchThreads / 2;
-  const bool searched = st->do_search != 0;
-  const int32_t leaf0 = st->smaller_leaf, leaf1 = st->larger_leaf;
-  const Pick none{-1, 0x7fffffff, 0, false, 0.0, 0};
-  // serial.rs:1523-1558 — fold the candidates of each searched leaf in feature order: the first
-  // half of the CTA folds the smaller leaf, the second half the larger one
-  // the candidate and leaf loads do not depend on the state: issued together with its loads, so
-  // the fold and the arg-max wait for one memory round trip
-  Pick a = none;
-  {
-    const int side = t / kHalf;
-    const int32_t leaf = side ? leaf1 : leaf0;
-    const int32_t slot = side ? st->larger_slot : st->smaller_slot;
-    for (int f = t % kHalf; f < p.F; f += kHalf) {
-      const uint8_t u = J.used[f];
-      const uint8_t cs = __ldcg(&J.csplit[side * p.F + f]);
-      const double g = __ldcg(&J.cgain[side * p.F + f]);
-      const uint32_t th = __ldcg(&J.cthr[side * p.F + f]);
-      const int real = feats[f].real;
-      if (!searched || leaf < 0 || !u) continue;
-      J.splittable[(size_t)slot * p.F + f] = cs;
-      pick(a, make_pick(f, g, real, th));
-    }
-  }
-  // split_info.rs:125-133 — first arg-max leaf under better_than; the searched leaves' new bests
-  // join from the fold
-  Pick b = none;
-  b.f = 0;
-  for (int i = t; i < p.num_leaves; i += kSearchThreads) {
-    if (i < kSearchThreads) {
-      s_lb[i] = J.leaf_begin[i];
-      s_lc[i] = J.leaf_count[i];
-      s_lbuf[i] = J.leaf_buf[i];
-      s_ld[i] = J.leaf_depth[i];
-    }
-    const double bg = J.bgain[i];
-    const int32_t bf = J.bfeat[i];
-    const int64_t bs = J.bsplit[i];
-    if (searched && (i == leaf0 || i == leaf1)) continue;
-    leaf_pick(b, make_pick(i, bg, bf, bs));
-  }
-  if (searched) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) pick(a, shfl_pick(a, o, true));
-  }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) leaf_pick(b, shfl_pick(b, o, true));
-  if (lane == 0) {
-    s_f[warp] = a;
-    s_l[warp] = b;
-  }
-  __syncthreads();
-  if (warp != 0) return;
-  // lanes 0 / 1: the new best of the smaller / larger leaf
-  Pick nb = none;
-  const int32_t my_leaf = lane == 0 ? leaf0 : leaf1;
-  if (searched && lane < 2 && my_leaf >= 0) {
-    Pick fa = none;
-    for (int w = lane * (kSearchWarps / 2); w < (lane + 1) * (kSearchWarps / 2); ++w) pick(fa, s_f[w]);
-    // the fold starts from SplitInfo::default (gain -inf, feature -1) and replaces it only with a
-    // better candidate
-    const bool take = fa.i >= 0 && better_k(fa.k, fa.nan, fa.f, dkey(-CUDART_INF), false, -1);
-    if (take)
-      nb = Pick{my_leaf, fa.f, fa.k, fa.nan, fa.g, (long long)fa.i * 4294967296LL + (long long)(uint32_t)fa.pay};
-    else
-      nb = make_pick(my_leaf, -CUDART_INF, -1, (long long)-1 * 4294967296LL);
-    J.bgain[my_leaf] = nb.g;
-    J.bfeat[my_leaf] = nb.f;
-    J.bsplit[my_leaf] = nb.pay;
-  }
-  // the leaf arg-max over the 8 warp partials (lanes 0..7) and the searched leaves (lanes 8, 9)
-  const Pick moved = shfl_pick(nb, lane & 1, false);
-  Pick w = lane < kSearchWarps ? s_l[lane] : ((lane == 8 || lane == 9) ? moved : none);
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) leaf_pick(w, shfl_pick(w, o, true));
-  const int32_t inner = w.i >= 0 ? (int32_t)(w.pay >> 32) : -1;
-  // serial.rs:611 — a best gain <= 0 stops the tree
-  if ((!w.nan && w.k <= 0) || inner < 0) {
-    if (lane == 0) st->stop = 1;
-    return;
-  }
-  if (lane == 0) {
-    const bool near = w.i < kSearchThreads;
-    st->split_begin = near ? s_lb[w.i] : J.leaf_begin[w.i];
-    st->split_count = near ? s_lc[w.i] : J.leaf_count[w.i];
-    st->split_buf = near ? s_lbuf[w.i] : J.leaf_buf[w.i];
-    st->split_depth = near ? s_ld[w.i] : J.leaf_depth[w.i];
-    st->split_sslot = st->next_free;
-    st->split_leaf = w.i;
-    st->split_inner = inner;
-    st->split_thr = (uint32_t)(w.pay & 0xffffffffLL);
-    st->new_leaf = st->tree_leaves;
-  }
-}
-
-// One CTA per (feature, side): blockIdx.x = 2 * feature + side (0 = smaller leaf). The last CTA to
-// finish runs the fold / arg-max.
+// One CTA per (feature, side): blockIdx.x = 2 * feature + side (0 = smaller leaf). With `decide`,
+// the last CTA to finish runs the fold / arg-max and records the split; otherwise the single-pass
+// partition that follows decides it.
 template <bool PLAIN, bool QUANT>
 __global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, Params p,
-                                                           const DevFeature* __restrict__ feats, int clear_par) {
+                                                           const DevFeature* __restrict__ feats, int clear_par,
+                                                           int decide) {
   __shared__ SearchSmem sm;
   __shared__ int last;
+  __shared__ Decision dec;
   const int side = (int)(blockIdx.x & 1u);
   const int f = (int)(blockIdx.x >> 1);
   const DevFeature m = feats[f];  // static: loaded while the histogram launch finishes
@@ -1149,7 +975,8 @@ __global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, 
     else
       search_float<PLAIN>(J, p, st, m, side, f, leaf, sm);
   }
-  griddep_launch();  // only the last CTA's fold is left: the partition may be scheduled
+  griddep_launch();  // only the last CTA's fold (if any) is left: the partition may be scheduled
+  if (!decide) return;
   __syncthreads();
   if (threadIdx.x == 0) {
     __threadfence();
@@ -1159,7 +986,7 @@ __global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, 
   __syncthreads();
   if (!last) return;
   __threadfence();
-  decide_body(J, p, feats);
+  decide_split(J, p, feats, true, &dec);
   if (threadIdx.x == 0) st->search_done = 0u;
 }
 
@@ -1210,17 +1037,17 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
 }  // namespace
 
 void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, int clear_par,
-                   cudaStream_t s) {
+                   bool decide, cudaStream_t s) {
   const bool plain = !p.use_l1 && !p.use_max && !p.use_smooth;
   const dim3 block(kSearchThreads);
   for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
     dim3 grid((unsigned)(2 * p.F), 1, nz);
     if (p.quant) {
-      if (plain) (void)launch_kernel(k_search<true, true>, grid, block, 0, s, p.pdl, t, p, feats, clear_par);
-      else (void)launch_kernel(k_search<false, true>, grid, block, 0, s, p.pdl, t, p, feats, clear_par);
+      if (plain) (void)launch_kernel(k_search<true, true>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, decide ? 1 : 0);
+      else (void)launch_kernel(k_search<false, true>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, decide ? 1 : 0);
     } else {
-      if (plain) (void)launch_kernel(k_search<true, false>, grid, block, 0, s, p.pdl, t, p, feats, clear_par);
-      else (void)launch_kernel(k_search<false, false>, grid, block, 0, s, p.pdl, t, p, feats, clear_par);
+      if (plain) (void)launch_kernel(k_search<true, false>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, decide ? 1 : 0);
+      else (void)launch_kernel(k_search<false, false>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, decide ? 1 : 0);
     }
   });
 }
