@@ -81,6 +81,36 @@ __device__ __forceinline__ Pick shfl_pick(const Pick& a, int src_or_mask, bool x
   return b;
 }
 
+__device__ __forceinline__ long long warp_max64(long long x) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const long long y = __shfl_xor_sync(FULL, x, o);
+    x = y > x ? y : x;
+  }
+  return x;
+}
+
+// The warp's arg-max under pick / leaf_pick when no valid lane holds a NaN gain: the order is then
+// total (higher key, then the smaller real feature with -1 last, then the smaller index), so a
+// 64-bit max and two 32-bit min reductions replace the record-by-record tree of shuffles. Every
+// lane gets the winner (index -1: no valid lane).
+__device__ __forceinline__ Pick warp_argmax(const Pick& x, bool valid, int lane) {
+  const long long km = warp_max64(valid ? x.k : kNoKey);
+  if (km == kNoKey) {
+    Pick n = x;
+    n.i = -1;
+    return n;
+  }
+  const bool at = valid && x.k == km;
+  const int fa = x.f == -1 ? 0x7fffffff : x.f;
+  const int fm = __reduce_min_sync(FULL, at ? fa : 0x7fffffff);
+  const bool at2 = at && fa == fm;
+  const int im = __reduce_min_sync(FULL, at2 ? x.i : 0x7fffffff);
+  const int wl = __ffs(__ballot_sync(FULL, at2 && x.i == im)) - 1;
+  (void)lane;
+  return shfl_pick(x, wl, false);
+}
+
 __device__ __forceinline__ Pick make_pick(int i, double g, int f, long long pay) {
   return Pick{i, f, dkey(g), dnan(g), g, pay};
 }
@@ -151,12 +181,14 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
     if (searched && (i == leaf0 || i == leaf1)) continue;
     leaf_pick(b, make_pick(i, bg, bf, bs));
   }
-  if (searched) {
+  // the fold never adopts a NaN gain, so its order is total
+  if (searched) a = warp_argmax(a, a.i >= 0, lane);
+  if (__any_sync(FULL, b.i >= 0 && b.nan)) {
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) pick(a, shfl_pick(a, o, true));
+    for (int o = 16; o > 0; o >>= 1) leaf_pick(b, shfl_pick(b, o, true));
+  } else {
+    b = warp_argmax(b, b.i >= 0, lane);
   }
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) leaf_pick(b, shfl_pick(b, o, true));
   if (lane == 0) {
     s_f[warp] = a;
     s_l[warp] = b;
@@ -185,8 +217,12 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
   // the leaf arg-max over the 8 warp partials (lanes 0..7) and the searched leaves (lanes 8, 9)
   const Pick moved = shfl_pick(nb, lane & 1, false);
   Pick w = lane < kDecideWarps ? s_l[lane] : ((lane == 8 || lane == 9) ? moved : none);
+  if (__any_sync(FULL, w.i >= 0 && w.nan)) {
 #pragma unroll
-  for (int o = 16; o > 0; o >>= 1) leaf_pick(w, shfl_pick(w, o, true));
+    for (int o = 16; o > 0; o >>= 1) leaf_pick(w, shfl_pick(w, o, true));
+  } else {
+    w = warp_argmax(w, w.i >= 0, lane);
+  }
   const int32_t inner = w.i >= 0 ? (int32_t)(w.pay >> 32) : -1;
   // serial.rs:611 — a best gain <= 0 stops the tree
   if ((!w.nan && w.k <= 0) || inner < 0) {

@@ -67,14 +67,6 @@ __device__ __forceinline__ T warp_sum(T v) {
   return v;
 }
 
-__device__ __forceinline__ long long warp_max64(long long x) {
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) {
-    const long long y = __shfl_xor_sync(FULL, x, o);
-    x = y > x ? y : x;
-  }
-  return x;
-}
 
 __device__ __forceinline__ int64_t unpack_g(int64_t pk) { return pk >> 32; }
 __device__ __forceinline__ int64_t unpack_h(int64_t pk) { return pk & 0xffffffffLL; }
