@@ -257,21 +257,59 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
   __syncthreads();
   unsigned long long* cnt_left = reinterpret_cast<unsigned long long*>(&st->pcnt[par][0]);
   unsigned long long* cnt_right = reinterpret_cast<unsigned long long*>(&st->pcnt[par][1]);
+  __shared__ int32_t s_pre[kItems][kThreads / 32];  // left rows before each (item, warp) group
+  __shared__ int32_t s_tile_left;
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const unsigned lanes_below = (1u << lane) - 1u;
+  // A tile's element j = k * kThreads + threadIdx.x (item k of this thread): every load and store
+  // instruction covers 32 consecutive elements. Rows keep the tile's element order on both sides.
   for (int64_t base = R.r0; base < R.r1; base += kThreads * kItems) {
-    const int64_t e0 = base + (int64_t)threadIdx.x * kItems;
     int32_t rows[kItems];
     uint32_t flags = 0;
-    int32_t cnt = 0;
 #pragma unroll
-    for (int k = 0; k < kItems; ++k) rows[k] = e0 + k < R.r1 ? __ldg(R.src + e0 + k) : -1;
+    for (int k = 0; k < kItems; ++k) {
+      const int64_t e = base + k * kThreads + threadIdx.x;
+      rows[k] = e < R.r1 ? __ldg(R.src + e) : -1;
+    }
+    int32_t pkv[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+      const int64_t e = base + k * kThreads + threadIdx.x;
+      pkv[k] = (p.quant && rows[k] >= 0) ? part_pk(R, e, rows[k]) : 0;
+    }
 #pragma unroll
     for (int k = 0; k < kItems; ++k)
-      if (rows[k] >= 0 && lut[__ldg(R.col + rows[k])]) {
-        flags |= 1u << k;
-        ++cnt;
+      if (rows[k] >= 0 && lut[__ldg(R.col + rows[k])]) flags |= 1u << k;
+    // left rows before each element of the tile, in element order: within the warp's 32 elements
+    // of item k by ballot, across (item, warp) groups by one scan of kItems * warps counts
+    int32_t in_warp[kItems];
+#pragma unroll
+    for (int k = 0; k < kItems; ++k) {
+      const unsigned b = __ballot_sync(FULL, (flags >> k) & 1u);
+      in_warp[k] = __popc(b & lanes_below);
+      if (lane == 0) s_pre[k][warp] = __popc(b);
+    }
+    __syncthreads();
+    if (warp == 0) {
+      // kItems * warps = 64 group counts in element order (item-major), two per lane
+      constexpr int kGroups = kItems * (kThreads / 32);
+      static_assert(kGroups == 64, "two groups per lane");
+      int32_t* flat = &s_pre[0][0];
+      const int32_t c0 = flat[2 * lane], c1 = flat[2 * lane + 1];
+      int32_t x = c0 + c1;
+#pragma unroll
+      for (int o = 1; o < 32; o <<= 1) {
+        const int32_t y = __shfl_up_sync(FULL, x, o);
+        if (lane >= o) x += y;
       }
-    int32_t tile_left;
-    const int32_t pre = block_excl_scan<int32_t>(cnt, &tile_left, sh);
+      const int32_t excl = x - (c0 + c1);
+      __syncwarp();
+      flat[2 * lane] = excl;
+      flat[2 * lane + 1] = excl + c0;
+      if (lane == 31) s_tile_left = x;
+    }
+    __syncthreads();
+    const int32_t tile_left = s_tile_left;
     const int32_t n = (int32_t)min((int64_t)kThreads * kItems, R.r1 - base);
     if (threadIdx.x == 0) {
       s_off[0] = (int64_t)atomicAdd(cnt_left, (unsigned long long)tile_left);
@@ -279,20 +317,19 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
     }
     __syncthreads();
     // left rows fill [lo, lo + tile_left); right rows fill the tile's slots ending at count - ro
-    int64_t lslot = s_off[0] + pre;
-    int64_t rslot = R.count - s_off[1] - (n - tile_left) + ((int64_t)threadIdx.x * kItems - pre);
-    int32_t pkv[kItems];
-#pragma unroll
-    for (int k = 0; k < kItems; ++k) pkv[k] = (p.quant && rows[k] >= 0) ? part_pk(R, e0 + k, rows[k]) : 0;
+    const int64_t lo = s_off[0];
+    const int64_t ro = R.count - s_off[1] - (n - tile_left);
 #pragma unroll
     for (int k = 0; k < kItems; ++k) {
-      if (e0 + k < R.r1) {
-        const int64_t slot = (flags & (1u << k)) ? lslot++ : rslot++;
+      const int32_t j = k * kThreads + (int32_t)threadIdx.x;
+      if (j < n) {
+        const int32_t left_before = s_pre[k][warp] + in_warp[k];
+        const int64_t slot = ((flags >> k) & 1u) ? lo + left_before : ro + (j - left_before);
         R.dst[slot] = rows[k];
         if (p.quant) R.pk_dst[slot] = (int16_t)pkv[k];
       }
     }
-    __syncthreads();  // s_off is rewritten by the next tile
+    __syncthreads();  // s_pre and s_off are rewritten by the next tile
   }
   griddep_launch();
 }
