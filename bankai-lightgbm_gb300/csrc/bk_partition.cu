@@ -65,9 +65,11 @@ __device__ __forceinline__ void part_range(const Job& J, const Params& p, const 
   r->pk_row = st->tree_leaves == 1;  // the root: no leaf-ordered copy yet
   r->pk_src = p.quant ? (r->pk_row ? J.packed : leaf_pk(J, buf) + r->begin) : nullptr;
   r->pk_dst = p.quant ? leaf_pk(J, 1 - buf) + r->begin : nullptr;
+  // rows per CTA in multiples of one row per thread: a small leaf spreads over as many CTAs as
+  // it fills, so each CTA's gather of the split column is short
   int64_t chunk = ceil_div64(r->count, p.part_grid);
-  chunk = (chunk + kThreads * kItems - 1) / (kThreads * kItems) * (kThreads * kItems);
-  if (chunk < kThreads * kItems) chunk = kThreads * kItems;
+  chunk = (chunk + kThreads - 1) / kThreads * kThreads;
+  if (chunk < kThreads) chunk = kThreads;
   r->r0 = min((int64_t)blockIdx.x * chunk, r->count);
   r->r1 = min(r->r0 + chunk, r->count);
   r->active = (int)ceil_div64(r->count, chunk);
