@@ -30,9 +30,9 @@ namespace bk {
 
 namespace {
 
-// At least one round (32 warps x 32 rows) per CTA: small leaves spread over as many SMs as they
-// can fill, since a round costs the SM's shared-atomic throughput, not its DRAM share.
-constexpr int kMinChunk = 1024;
+// At least 256 rows (eight warps' worth) per CTA: small leaves spread over as many SMs as they can
+// fill, since a CTA's rows cost its SM's load and shared-atomic pipes, not a DRAM share.
+constexpr int kMinChunk = 256;
 
 __device__ __forceinline__ float two_sum_err(float a, float b, float s) {
   float bb = __fsub_rn(s, a);
