@@ -127,7 +127,8 @@ struct Job {
   int64_t* bsplit;     // [L]   inner feature << 32 | threshold | default_left << 31 of each leaf's best split
   LeafConst* lconst;   // [2]   constants of the smaller / larger leaf of the current search
   uint8_t* splittable; // [L][F]
-  uint8_t* used;       // [F]
+  uint8_t* used;       // [F]   features searched in the current step
+  uint8_t* tree_mask;  // [F]   features the tree may split on (by-tree column sample), 1 by default
   bk_split* records;   // [L-1]
   double* leaf_value;  // [L]
   void* pool;          // [L][T][B][32]

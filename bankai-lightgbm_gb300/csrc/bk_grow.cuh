@@ -70,10 +70,11 @@ __device__ __forceinline__ void before_find_best_split(const Job& J, const Param
     else st->hist_rows_gather += rows;
     st->hist_builds += 1;
   }
-  // serial.rs:840-854 — features the parent could not split are skipped for both children.
+  // serial.rs:840-854 — features outside the tree's column sample are not searched; features the
+  // parent could not split are skipped for both children.
   for (int f = lane; f < p.F; f += 32) {
     uint8_t u = parent_slot < 0 ? 1 : J.splittable[(size_t)parent_slot * p.F + f];
-    J.used[f] = u;
+    J.used[f] = u & J.tree_mask[f];
     if (!u) J.splittable[(size_t)smaller_slot * p.F + f] = 0;
   }
   if (lane == 0) st->do_search = 1;
@@ -195,10 +196,11 @@ __device__ __forceinline__ void post_split_writes(const Job& J, const Params& p,
     }
   }
   if (o.go) {
-    // serial.rs:840-854 — features the parent could not split are skipped for both children
+    // serial.rs:840-854 — features outside the tree's column sample are not searched; features
+    // the parent could not split are skipped for both children
     for (int f = lane; f < p.F; f += 32) {
       uint8_t u = J.splittable[(size_t)pslot * p.F + f];
-      J.used[f] = u;
+      J.used[f] = u & J.tree_mask[f];
       if (!u) J.splittable[(size_t)o.sslot * p.F + f] = 0;
     }
   }

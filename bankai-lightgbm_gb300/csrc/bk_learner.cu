@@ -472,6 +472,8 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
       J.lconst = L->dalloc<LeafConst>(2);
       J.splittable = L->dalloc<uint8_t>((size_t)Lv * F);
       J.used = L->dalloc<uint8_t>(F);
+      J.tree_mask = L->dalloc<uint8_t>(F);
+      CK(cudaMemset(J.tree_mask, 1, F));
       J.records = L->dalloc<bk_split>(Lv);
       J.leaf_value = L->dalloc<double>(Lv);
       J.pool = reinterpret_cast<uint8_t*>(L->d_pool) + L->pool_bytes_per_job * j;
@@ -724,6 +726,28 @@ int bk_learner_reset_constant_hessian(bk_learner* L, int32_t value) {
       cudaGraphExecDestroy(L->graph_exec);
       L->graph_exec = nullptr;
     }
+  }
+  return 0;
+}
+
+int bk_learner_set_feature_mask(bk_learner* L, const uint8_t* mask) {
+  if (!L) {
+    set_error("bk_learner_set_feature_mask: null learner");
+    return -1;
+  }
+  const size_t F = (size_t)L->p.F;
+  try {
+    for (int j = 0; j < L->K; ++j) {
+      if (mask) {
+        CK(cudaMemcpyAsync(L->jobs[j].tree_mask, mask + (size_t)j * F, F, cudaMemcpyHostToDevice, L->stream));
+      } else {
+        CK(cudaMemsetAsync(L->jobs[j].tree_mask, 1, F, L->stream));
+      }
+    }
+    // the host mask may be freed or reused as soon as this call returns
+    CK(cudaStreamSynchronize(L->stream));
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
   }
   return 0;
 }

@@ -56,6 +56,17 @@ class GpuTreeLearner:
         """Programmatic dependent launch of the grow-loop kernels (default on)."""
         _lib.check(self.lib.bk_learner_set_launch_overlap(self.h, int(bool(on))), "bk_learner_set_launch_overlap")
 
+    def set_feature_mask(self, mask=None):
+        """The by-tree column sample of the following trees (ColSampler::reset_by_tree,
+        treelearner/col_sampler.rs:87-103): mask [num_jobs, num_features] (or [num_features] for
+        one job) of inner features the trees may split on; None = every feature."""
+        if mask is None:
+            _lib.check(self.lib.bk_learner_set_feature_mask(self.h, None), "bk_learner_set_feature_mask")
+            return
+        m = np.ascontiguousarray(np.asarray(mask, dtype=bool).reshape(self.num_jobs, self.ds.num_features),
+                                 dtype=np.uint8)
+        _lib.check(self.lib.bk_learner_set_feature_mask(self.h, m.ctypes.data), "bk_learner_set_feature_mask")
+
     def set_timing(self, on: bool):
         _lib.check(self.lib.bk_learner_set_timing(self.h, int(bool(on))), "bk_learner_set_timing")
 

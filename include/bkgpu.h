@@ -112,6 +112,13 @@ int bk_learner_set_loop_mode(bk_learner* learner, int32_t mode);
  * launch, so it is scheduled while the previous kernel finishes; 0 = plain stream order. */
 int bk_learner_set_launch_overlap(bk_learner* learner, int32_t on);
 
+/* The by-tree column sample of the following train calls: the `is_feature_used_bytree` mask that
+ * ColSampler::reset_by_tree draws before each tree (treelearner/col_sampler.rs:87-103) and
+ * find_best_splits applies (serial.rs:839-854): features with mask 0 are neither searched nor
+ * split on. mask: host uint8 [num_jobs][num_features] over inner features (one mask per class
+ * tree, as the reference draws one per train call), or NULL for "every feature". */
+int bk_learner_set_feature_mask(bk_learner* learner, const uint8_t* mask);
+
 /* Replaces SerialTreeLearner::reset_constant_hessian (serial.rs:279). */
 int bk_learner_reset_constant_hessian(bk_learner* learner, int32_t value);
 

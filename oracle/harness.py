@@ -25,6 +25,7 @@ sys.path.insert(0, os.path.join(ROOT, "bankai-lightgbm_gb300"))
 
 from lgbm_gb300.config import CONFIG_DTYPE, LearnerConfig  # noqa: E402
 from lgbm_gb300.dataset import FEATURE_DTYPE  # noqa: E402
+from lgbm_gb300.dataset import _Random as LcgRandom  # noqa: E402  (utils/random.rs, the bin sampler's LCG)
 from lgbm_gb300.tree import SPLIT_DTYPE, Tree  # noqa: E402
 
 EPS = float(np.float32(1e-15))
@@ -42,6 +43,7 @@ def load():
         lib.orc_learner_create.restype = P
         lib.orc_learner_create.argtypes = [P, i32, P, i64, P]
         lib.orc_learner_destroy.argtypes = [P]
+        lib.orc_learner_set_feature_mask.argtypes = [P, P]
         lib.orc_learner_train.restype = i32
         lib.orc_learner_train.argtypes = [P, P, P, P, i64, P, P]
         lib.orc_learner_root_output.restype = ctypes.c_double
@@ -101,6 +103,15 @@ class OracleLearner:
                                         leaf_values.ctypes.data)
         root = self.lib.orc_learner_root_output(self.h)
         return splits[:nl - 1].copy(), leaf_values[:nl].copy(), root
+
+    def set_feature_mask(self, mask=None):
+        """By-tree column sample of the following trees (None = every feature)."""
+        if mask is None:
+            self._mask = None
+        else:
+            self._mask = np.ascontiguousarray(np.asarray(mask, dtype=bool).reshape(-1), dtype=np.uint8)
+            assert len(self._mask) == self.ds.num_features
+        self.lib.orc_learner_set_feature_mask(self.h, _ptr(self._mask))
 
     def row_leaf(self):
         out = np.zeros(self.ds.num_data, dtype=np.int32)
@@ -232,9 +243,108 @@ def make_objective(params, y):
     raise ValueError("objective %r is outside the learner's scope" % obj)
 
 
+# ------------------------------------------------------------------------------------------
+# row and column sampling (the Trainer's side of the learner's `rows` / feature-mask inputs)
+# ------------------------------------------------------------------------------------------
+class TreeColumnSampler:
+    """The by-tree part of ColSampler (treelearner/col_sampler.rs:9-108): one draw when the learner
+    is built, then one per tree (serial.rs:678). Features are the learner's inner features, which
+    follow the real-index order of the used features."""
+
+    def __init__(self, num_features, fraction, seed):
+        self.nf = num_features
+        self.rand = LcgRandom(seed)
+        self.active = fraction < 1.0
+        self.cnt = max(min(1, num_features), int(num_features * fraction + 0.5)) if self.active else num_features
+        self.mask = np.ones(num_features, dtype=bool)
+        self.reset_by_tree()
+
+    def reset_by_tree(self):
+        if self.active:
+            self.mask = np.zeros(self.nf, dtype=bool)
+            self.mask[np.asarray(self.rand.sample(self.nf, self.cnt), dtype=np.int64)] = True
+        return self.mask.copy()
+
+
+class RowBagging:
+    """Plain bagging (boosting/sample.rs:16-240 without the balanced / by-query / GOSS forms): one
+    LCG per 1024-row block seeded bagging_seed + block, one draw per row in row order, redrawn
+    every bagging_freq iterations. sample(iter) returns the ascending bag or None (all rows)."""
+    BLOCK = 1024
+
+    def __init__(self, n, fraction, freq, seed):
+        self.n = n
+        self.fraction = float(fraction)
+        self.freq = int(freq)
+        self.active = self.fraction < 1.0 and self.freq > 0
+        self.rands = [LcgRandom((int(seed) + b) & 0xFFFFFFFF) for b in range((n + self.BLOCK - 1) // self.BLOCK)]
+        self.bag = None
+        self.need = True
+
+    def sample(self, it):
+        if not self.active:
+            return None
+        if self.need or (len(self.bag) < self.n and it % self.freq == 0):
+            self.need = False
+            self.bag = np.array([i for i in range(self.n)
+                                 if float(self.rands[i // self.BLOCK].next_float()) < self.fraction], dtype=np.int32)
+        return self.bag if len(self.bag) < self.n else None
+
+
+def resolved_params(model_text):
+    """The resolved config a model file records in its parameters section (`[name: value]`
+    lines), e.g. the seeds upstream derives from `seed`."""
+    out = {}
+    for line in model_text.splitlines():
+        if line.startswith("[") and line.endswith("]") and ": " in line:
+            k, v = line[1:-1].split(": ", 1)
+            out[k] = v
+    return out
+
+
+def samplers_from_params(resolved, ds):
+    """(TreeColumnSampler or None, RowBagging or None) for a resolved config; by-node sampling is
+    outside the learner's interface."""
+    if float(resolved.get("feature_fraction_bynode", 1)) < 1.0:
+        raise NotImplementedError("feature_fraction_bynode draws per node inside the grow loop")
+    ff = float(resolved.get("feature_fraction", 1))
+    cols = TreeColumnSampler(ds.num_features, ff, int(resolved.get("feature_fraction_seed", 2))) if ff < 1 else None
+    bag = RowBagging(ds.num_data, float(resolved.get("bagging_fraction", 1)), int(resolved.get("bagging_freq", 0)),
+                     int(resolved.get("bagging_seed", 3)))
+    return cols, (bag if bag.active else None)
+
+
+def replay_leaves(tree, ds, rows):
+    """Leaf of each of `rows` under `tree`, routed on the stored bins with the training routing
+    (serial.rs:2009-2041 add_prediction_for_rows; data_partition.rs:299-410 per split)."""
+    lib = load()
+    feats = ds.feature_array()
+    ni = tree.num_leaves - 1
+    luts = np.zeros((max(ni, 1), 256), dtype=np.uint8)
+    for node in range(ni):
+        f = int(tree.split_feature_inner[node])
+        lib.orc_route_table(feats[f:f + 1].ctypes.data, int(tree.threshold_in_bin[node]),
+                            int((int(tree.decision_type[node]) >> 1) & 1), luts[node].ctypes.data)
+    rows = np.asarray(rows, dtype=np.int64)
+    node = np.zeros(len(rows), dtype=np.int64)
+    leaf = np.full(len(rows), -1 if ni > 0 else 0, dtype=np.int64)
+    live = np.arange(len(rows)) if ni > 0 else np.zeros(0, np.int64)
+    while len(live):
+        nd = node[live]
+        b = ds.bins[tree.split_feature_inner[nd], rows[live]]
+        nxt = np.where(luts[nd, b] != 0, tree.left_child[nd], tree.right_child[nd]).astype(np.int64)
+        done = nxt < 0
+        leaf[live[done]] = ~nxt[done]
+        node[live[~done]] = nxt[~done]
+        live = live[~done]
+    return leaf
+
+
 def train_gbdt(learner, ds, objective, rounds, learning_rate=0.1, boost_from_average=True,
-               min_gain_to_split=0.0):
-    """train.rs:723-839 without bagging / DART / RF. Returns (trees, score)."""
+               min_gain_to_split=0.0, col_sampler=None, bagging=None):
+    """train.rs:723-839 with optional plain bagging (rows passed to the learner, out-of-bag rows
+    scored by replaying the tree, serial.rs:1995-2000) and a by-tree column sample (a mask set
+    before each tree); no DART / RF / GOSS. Returns (trees, score)."""
     K = getattr(objective, "num_class", 1)
     n = ds.num_data
     score = np.zeros((K, n), dtype=np.float64)
@@ -248,18 +358,25 @@ def train_gbdt(learner, ds, objective, rounds, learning_rate=0.1, boost_from_ave
                     init[k] = v
                     score[k] += v
         g, h = objective.gradients(score[0] if K == 1 else score)
+        rows = bagging.sample(it) if bagging is not None else None
+        oob = None if rows is None else np.setdiff1d(np.arange(n, dtype=np.int32), rows)
         cont = False
         for k in range(K):
             need = objective.class_need_train(k) if hasattr(objective, "class_need_train") else True
             if not need:
                 raise NotImplementedError("constant class trees are outside the learner's scope")
-            recs, leaf_values, root = learner.train(g[k], h[k])
+            if col_sampler is not None:
+                learner.set_feature_mask(col_sampler.reset_by_tree())
+            recs, leaf_values, root = learner.train(g[k], h[k], rows)
             t = Tree.from_records(learner.num_leaves, recs, leaf_values, root, ds.features, min_gain_to_split)
             if t.num_leaves > 1:
                 cont = True
                 t.apply_shrinkage(learning_rate)
                 leaf = learner.row_leaf()
-                score[k] += t.leaf_value[leaf]
+                inbag = leaf >= 0
+                score[k][inbag] += t.leaf_value[leaf[inbag]]
+                if oob is not None and len(oob):
+                    score[k][oob] += t.leaf_value[replay_leaves(t, ds, oob)]
                 if abs(init[k]) > EPS:
                     t.add_bias(init[k])
             trees.append(t)

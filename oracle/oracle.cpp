@@ -755,6 +755,7 @@ struct Learner {
   int32_t tree_leaves = 1;
   double root_output = 0.0;
   std::vector<float> og, oh;
+  std::vector<uint8_t> tree_mask;  // empty: every feature is used by the tree
   Pool* workers = nullptr;
   ~Learner() { delete workers; }
 
@@ -997,10 +998,12 @@ struct Learner {
     return true;
   }
 
-  // serial.rs:830-887
+  // serial.rs:830-887; the by-tree feature mask (ColSampler::is_feature_used_bytree,
+  // col_sampler.rs:87-108) skips a feature before the splittable propagation (serial.rs:841-846)
   void find_best_splits(const float* g, const float* h) {
     std::vector<uint8_t> used(nf, 0);
     for (int f = 0; f < nf; ++f) {
+      if (!tree_mask.empty() && !tree_mask[f]) continue;
       if (parent_slot >= 0 && !splittable[parent_slot][f]) {
         splittable[smaller_slot][f] = 0;
         continue;
@@ -1248,6 +1251,14 @@ void* orc_learner_create(const orc_feature* feats, int32_t nf, const uint8_t* bi
 }
 
 void orc_learner_destroy(void* h) { delete (Learner*)h; }
+
+// The features the following trees may split on (ColSampler::reset_by_tree, col_sampler.rs:87-103):
+// mask[f] != 0 for every used inner feature f; NULL restores "all features".
+void orc_learner_set_feature_mask(void* h, const uint8_t* mask) {
+  Learner* L = (Learner*)h;
+  if (mask) L->tree_mask.assign(mask, mask + L->nf);
+  else L->tree_mask.clear();
+}
 
 // Trains one tree. Returns the number of leaves; fills `splits` (num_leaves-1 capacity) and
 // `leaf_value` (num_leaves capacity, the tree's leaf outputs before shrinkage).

@@ -154,6 +154,51 @@ def test_multiclass_jobs_batched_match_sequential_oracle():
         G = (G * 0.9).astype(np.float32)
 
 
+@pytest.mark.parametrize("quant", [1, 0])
+def test_feature_mask_per_job(quant):
+    """bk_learner_set_feature_mask: one by-tree column sample per class tree (serial.rs:839-854);
+    the quantized trees equal the oracle's bit for bit, the float trees within tolerance."""
+    K = 3
+    cfg = dict(num_leaves=31, use_quantized_grad=quant, stochastic_rounding=1, seed=5, num_threads=2)
+    ds, z = _dataset(20000, 24, seed=8)
+    rng = np.random.default_rng(3)
+    G = rng.normal(0, 1, (K, ds.num_data)).astype(np.float32)
+    H = rng.uniform(0.05, 0.25, (K, ds.num_data)).astype(np.float32)
+    orc, gpu, _ = _learners(ds, False, num_jobs=K, **cfg)
+    divergences = []
+    for it in range(3):
+        mask = rng.random((K, ds.num_features)) < 0.5
+        mask[:, it] = True  # at least one feature per tree
+        gpu.set_feature_mask(mask)
+        splits, lv, roots, nls = gpu.train_raw(G, H)
+        rl = gpu.row_leaf()
+        for k in range(K):
+            used = set(np.flatnonzero(mask[k]).tolist())
+            assert set(splits[k, :nls[k] - 1]["inner_feature"].tolist()) <= used
+            orc.set_feature_mask(mask[k])
+            ro = orc.train(G[k], H[k])
+            if quant:
+                _assert_records_equal(ro[0], splits[k, :nls[k] - 1])
+                assert np.array_equal(ro[1], lv[k, :nls[k]])
+                assert np.array_equal(orc.row_leaf(), rl[k])
+            else:
+                rg = (splits[k, :nls[k] - 1], lv[k, :nls[k]], roots[k])
+                d = _float_compare(ro, rg)
+                if d >= 0:
+                    divergences.append((it, k, d))
+    # float near-tie split choices are allowed but must be rare
+    print("float near-tie divergences (call, job, split):", divergences)
+    assert len(divergences) <= 1
+    # the mask stays until it is replaced; None restores every feature
+    gpu.set_feature_mask(None)
+    orc.set_feature_mask(None)
+    splits, lv, roots, nls = gpu.train_raw(G, H)
+    ro = orc.train(G[0], H[0])
+    if quant:
+        _assert_records_equal(ro[0], splits[0, :nls[0] - 1])
+    gpu.close()
+
+
 def _float_compare(ro, rg):
     """Structure equal, gains within 1e-6 relative; returns the index of the first near-tie
     divergence (or -1)."""
@@ -209,10 +254,12 @@ def test_gpu_reproduces_reference_models(oracle, case):
     obj = oracle.make_objective(p, y)
     cfg = LearnerConfig(**p, fused_madd=1, is_constant_hessian=int(obj.constant_hessian))
     learner = GpuTreeLearner(ds, cfg)
+    model = open(os.path.join(d, "model.txt")).read()
+    cols, bag = oracle.samplers_from_params(oracle.resolved_params(model), ds)
     trees, _ = oracle.train_gbdt(learner, ds, obj, P["num_boost_round"], learning_rate=p.get("learning_rate", 0.1),
                                  boost_from_average=p.get("boost_from_average", True),
-                                 min_gain_to_split=p.get("min_gain_to_split", 0.0))
-    ref = oracle.parse_model_trees(open(os.path.join(d, "model.txt")).read())
+                                 min_gain_to_split=p.get("min_gain_to_split", 0.0), col_sampler=cols, bagging=bag)
+    ref = oracle.parse_model_trees(model)
     assert len(trees) == len(ref)
     for i, (t, r) in enumerate(zip(trees, ref)):
         bad = oracle.compare_tree(t, r, leaf_rtol=1e-9)

@@ -1,7 +1,9 @@
 """Pins the oracle to the reference's own golden data (no GPU).
 
 * the upstream-LightGBM models that bankai-lightgbm reproduces (tests/golden/train/*), rebuilt
-  tree by tree through the oracle learner, with both ``madd`` rounding modes;
+  tree by tree through the oracle learner, with both ``madd`` rounding modes (bagged cases pass
+  their rows, feature-fraction cases a by-tree feature mask, drawn as the reference's Trainer
+  draws them);
 * the std::mt19937 / libc++ distribution vectors and the discretizer vectors;
 * the upstream stumps of quantized_gradients.json;
 * the reference's brute-force integer split search cases.
@@ -43,9 +45,10 @@ def test_oracle_reproduces_reference_models(oracle, bklib, case, fused):
     obj = oracle.make_objective(p, y)
     cfg = LearnerConfig(**p, fused_madd=fused, is_constant_hessian=int(obj.constant_hessian))
     learner = oracle.OracleLearner(ds, cfg)
+    cols, bag = oracle.samplers_from_params(oracle.resolved_params(model), ds)
     trees, _ = oracle.train_gbdt(learner, ds, obj, P["num_boost_round"], learning_rate=p.get("learning_rate", 0.1),
                                  boost_from_average=p.get("boost_from_average", True),
-                                 min_gain_to_split=p.get("min_gain_to_split", 0.0))
+                                 min_gain_to_split=p.get("min_gain_to_split", 0.0), col_sampler=cols, bagging=bag)
     ref = oracle.parse_model_trees(model)
     assert len(trees) == len(ref)
     exact = total = 0
