@@ -271,6 +271,7 @@ def run_gpu(args, rank, world):
     roof = form(True, 1, args.steps, 1, timing=True)
     plain = form(False, 0, args.steps, args.warmup)
     e2e = form(True, 1, args.steps, 1, e2e=True)
+    multiclass = run_multiclass(args) if args.multiclass_rows > 0 else None
     ms, value = aggregate_ranks(main["ms_per_step"], world)
     hist_gbs = roof["hist_bytes"] / (roof["hist_ms"] * 1e6) if roof["hist_ms"] > 0 else None
     hist_launches = (args.leaves - 1) * args.steps  # one histogram launch per split step of a tree
@@ -294,7 +295,8 @@ def run_gpu(args, rank, world):
                   "plain_float_stepwise": {"iters_per_s": round(1000.0 / plain["ms_per_step"], 4),
                                            "train_l2": plain["loss_final"], "heldout_l2": plain["heldout_l2"],
                                            "iterations": plain["iterations"]},
-                  "heldout_l2_delta": main["heldout_l2"] - plain["heldout_l2"], "heldout_rows": m_ho},
+                  "heldout_l2_delta": main["heldout_l2"] - plain["heldout_l2"], "heldout_rows": m_ho,
+                  "multiclass_k10": multiclass},
         "e2e": {"value": round(world * 1000.0 / e2e["ms_per_step"], 4), "unit": "iters/s",
                 "h2d_bytes_per_step": 2 * 4 * ds.num_data,
                 "d2h_bytes_per_step": 112 * (args.leaves - 1) + 8 * args.leaves + 8 + 8},
@@ -313,6 +315,73 @@ def run_gpu(args, rank, world):
     if rank == 0:
         line["cpu_baseline"] = cpu_baseline(ds, y, sample_rows=args.cpu_rows)
     return line
+
+
+def run_multiclass(args):
+    """Multiclass softmax, K=10 class trees per iteration grown in one call (each grow-loop kernel
+    launched for groups of class trees): 2M x 64 Gaussian-mixture rows (10 components, means
+    spread 2.0), max_bin 63, 63 leaves. Quantized + graph form against the plain float form with
+    one host round trip per split; iterations per second, training and held-out (20%) multi-class
+    log loss."""
+    import torch
+    from lgbm_gb300 import BinnedDataset, GpuTreeLearner, LearnerConfig, synthetic
+    from lgbm_gb300.tree import Tree
+    K, leaves, lr = 10, 63, 0.1
+    rows = args.multiclass_rows
+    X, y = synthetic.gaussian_mixture(n=rows + rows // 4, F=64, K=K, seed=0)
+    threads = min(32, os.cpu_count() or 8)
+    ds = BinnedDataset.from_dense(X[:rows], max_bin=63, min_data_in_leaf=20, threads=threads)
+    ho_bins = torch.from_numpy(ds.bin_like(X[rows:], threads=threads)).cuda()
+    del X
+    n, m = ds.num_data, ho_bins.shape[1]
+    label = torch.from_numpy(y[:rows]).cuda()
+    ho_y = torch.from_numpy(y[rows:].astype(np.int64)).cuda()
+    prior = np.bincount(y[:rows].astype(np.int64), minlength=K) / float(rows)
+    init = torch.tensor(np.log(np.maximum(prior, 1e-15)), dtype=torch.float64, device="cuda")[:, None]
+
+    def form(quant, loop_mode, steps, warmup):
+        cfg = LearnerConfig(num_leaves=leaves, min_data_in_leaf=20, use_quantized_grad=int(quant),
+                            num_grad_quant_bins=4, stochastic_rounding=1, seed=0, num_threads=16, fused_madd=1)
+        learner = GpuTreeLearner(ds, cfg, num_jobs=K, loop_mode=loop_mode)
+        stream = torch.cuda.ExternalStream(learner.stream())
+        score = (init.expand(K, n)).contiguous()
+        gbuf, hbuf = learner.gradient_buffers()
+        torch.cuda.synchronize()
+        trees, total_ms = [], 0.0
+        for it in range(warmup + steps):
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            learner.objective_gradients(2, score.data_ptr(), label.data_ptr())
+            splits, lv, roots, nls = learner.train_raw(gbuf, hbuf, on_device=True)
+            vals = lv * lr
+            vals[np.abs(vals) <= K_ZERO_THRESHOLD] = 0.0
+            learner.add_prediction_to_score(vals, score.data_ptr(), on_device=True)
+            ev1.record(stream)
+            ev1.synchronize()
+            if it >= warmup:
+                total_ms += ev0.elapsed_time(ev1)
+            trees.append([(splits[k, :nls[k] - 1].copy(), lv[k, :nls[k]].copy(), float(roots[k])) for k in range(K)])
+        train_loss = learner.objective_loss(2, score.data_ptr(), label.data_ptr())
+        ho = (init.expand(K, m)).contiguous()
+        torch.cuda.synchronize()
+        for per_class in trees:
+            for k, (sp, lvals, root) in enumerate(per_class):
+                t = Tree.from_records(leaves, sp, lvals, root, ds.features)
+                t.apply_shrinkage(lr)
+                learner.predict_add(t, ho_bins.data_ptr(), m, ho[k].data_ptr())
+        torch.cuda.synchronize()
+        ho_loss = float((torch.logsumexp(ho, 0) - ho.gather(0, ho_y[None, :])[0]).mean().item())
+        learner.close()
+        return {"iters_per_s": round(1000.0 * steps / total_ms, 3), "ms_per_iter": round(total_ms / steps, 3),
+                "train_logloss": round(train_loss, 6), "heldout_logloss": round(ho_loss, 6),
+                "iterations": len(trees)}
+
+    q = form(True, 1, args.steps, args.warmup)
+    p = form(False, 0, args.steps, args.warmup)
+    return {"workload": "multiclass softmax K=10, %d x 64 Gaussian mixture, max_bin 63, 63 leaves; step = device "
+                        "gradients + 10 class trees in one call + score update" % n,
+            "quantized_graph": q, "plain_float_stepwise": p,
+            "heldout_logloss_delta": round(q["heldout_logloss"] - p["heldout_logloss"], 6)}
 
 
 def run_hist_traffic(args):
@@ -412,6 +481,8 @@ def main():
     ap.add_argument("--rows", type=int, default=10_000_000)
     ap.add_argument("--leaves", type=int, default=255)
     ap.add_argument("--cpu-rows", type=int, default=1_000_000)
+    ap.add_argument("--multiclass-rows", type=int, default=2_000_000,
+                    help="rows of the K=10 multiclass form reported beside the headline (0: skip it)")
     ap.add_argument("--hist-traffic", action="store_true",
                     help="train one tree and print the histogram kernel's algorithmic bytes (for an ncu capture)")
     args = ap.parse_args()
