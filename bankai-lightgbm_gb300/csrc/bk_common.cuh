@@ -202,6 +202,8 @@ void launch_root_sums(const Job* d_jobs, int num_jobs, const Params& p, int exac
 void launch_renew(const Job* d_jobs, int num_jobs, const Params& p, cudaStream_t s);
 void launch_add_score(const Job* d_jobs, int num_jobs, const Params& p, const double* leaf_vals, double* score,
                       cudaStream_t s);
+void launch_add_score_own(const Job* d_jobs, int num_jobs, const Params& p, double rate, double* score,
+                          cudaStream_t s);
 void launch_row_leaf(const Job* d_jobs, int num_jobs, const Params& p, int32_t* out, cudaStream_t s);
 void launch_mt_seed(const Job* d_jobs, int num_jobs, uint32_t seed, cudaStream_t s);
 constexpr int kRootGrid = 256;

@@ -517,6 +517,115 @@ int bk_learner_create_device_bins(const bk_feature* features, int32_t num_featur
   return learner_create(features, num_features, bins, num_data, c, num_jobs, out, true);
 }
 
+namespace {
+
+// The asynchronous half of a train call, all on the learner's stream: the gradient and row copies,
+// the grow loop of every job, optionally the score update with the new trees (shrunk on the
+// device), and the copies of the split records, leaf values and job states into pinned host
+// buffers. Returns false with the error set on invalid arguments; CUDA errors throw.
+bool train_enqueue(bk_learner* L, const float* gradients, const float* hessians, int32_t on_device,
+                   const int32_t* rows, int64_t num_rows, double shrinkage, double* score) {
+  const Params& p = L->p;
+  const size_t n = (size_t)p.n, K = (size_t)L->K;
+  const int Lv = p.num_leaves;
+  if (rows && (num_rows <= 0 || num_rows > (int64_t)n)) {
+    set_error("bk_learner_train: num_rows out of range");
+    return false;
+  }
+  CK(cudaEventRecord(L->ev_start, L->stream));
+  cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+  if (gradients != L->d_g) CK(cudaMemcpyAsync(L->d_g, gradients, n * K * sizeof(float), kind, L->stream));
+  if (hessians != L->d_h) CK(cudaMemcpyAsync(L->d_h, hessians, n * K * sizeof(float), kind, L->stream));
+  int64_t root_count = rows ? num_rows : (int64_t)n;
+  if (rows) CK(cudaMemcpyAsync(L->d_rows, rows, sizeof(int32_t) * num_rows, cudaMemcpyHostToDevice, L->stream));
+  for (size_t j = 0; j < K; ++j) {
+    L->h_state[j].use_rows = rows ? 1 : 0;
+    L->h_state[j].root_count = root_count;
+    L->h_state[j].hist_rows_direct = L->h_state[j].hist_rows_gather = L->h_state[j].hist_builds = 0;
+    JobState* st = L->jobs[j].st;
+    CK(cudaMemcpyAsync(&st->use_rows, &L->h_state[j].use_rows, sizeof(int32_t), cudaMemcpyHostToDevice,
+                       L->stream));
+    CK(cudaMemcpyAsync(&st->root_count, &L->h_state[j].root_count, sizeof(int64_t), cudaMemcpyHostToDevice,
+                       L->stream));
+    CK(cudaMemcpyAsync(&st->hist_rows_direct, &L->h_state[j].hist_rows_direct, 3 * sizeof(int64_t),
+                       cudaMemcpyHostToDevice, L->stream));
+  }
+  if (L->timing && L->hist_events.size() != (size_t)(4 * (Lv - 1))) {
+    for (cudaEvent_t e : L->hist_events) cudaEventDestroy(e);
+    L->hist_events.assign(4 * (Lv - 1), nullptr);
+    for (auto& e : L->hist_events) CK(cudaEventCreate(&e));
+    if (L->graph_exec) {
+      cudaGraphExecDestroy(L->graph_exec);
+      L->graph_exec = nullptr;
+    }
+  }
+  if (L->loop_mode == 1) L->run_graph();
+  else L->run_stepwise();
+  if (score) {
+    launch_add_score_own(L->d_jobs, L->K, p, shrinkage, score, L->stream);
+    CK(cudaGetLastError());
+  }
+  for (size_t j = 0; j < K; ++j) {
+    const Job& J = L->jobs[j];
+    CK(cudaMemcpyAsync(L->h_records + j * Lv, J.records, sizeof(bk_split) * (Lv - 1), cudaMemcpyDeviceToHost,
+                       L->stream));
+    CK(cudaMemcpyAsync(L->h_leaf_values + j * Lv, J.leaf_value, sizeof(double) * Lv, cudaMemcpyDeviceToHost,
+                       L->stream));
+    CK(cudaMemcpyAsync(&L->h_state[j], J.st, offsetof(JobState, mt), cudaMemcpyDeviceToHost, L->stream));
+  }
+  CK(cudaEventRecord(L->ev_end, L->stream));
+  return true;
+}
+
+// The synchronous half: waits for the learner's stream, reads the timings and fills the outputs.
+void train_finish(bk_learner* L, bk_split* splits, double* leaf_values, double* root_outputs,
+                  int32_t* num_leaves_out) {
+  const Params& p = L->p;
+  const size_t K = (size_t)L->K;
+  const int Lv = p.num_leaves;
+  CK(cudaStreamSynchronize(L->stream));
+  CK(cudaGetLastError());
+  float ms = 0.f;
+  CK(cudaEventElapsedTime(&ms, L->ev_start, L->ev_end));
+  L->last_total_ms = ms;
+  L->last_hist_ms = L->last_search_ms = L->last_part_ms = 0.0;
+  if (L->timing) {
+    // the phases of the steps that ran (a finished tree's remaining steps return early but are
+    // still timed: they are part of the replayed graph); a stepwise loop that stopped early
+    // leaves later events unrecorded, which the elapsed-time calls report and skip
+    for (int it = 0; it < Lv - 1; ++it) {
+      float t = 0.f;
+      if (cudaEventElapsedTime(&t, L->hist_events[4 * it], L->hist_events[4 * it + 1]) == cudaSuccess)
+        L->last_hist_ms += t;
+      if (cudaEventElapsedTime(&t, L->hist_events[4 * it + 1], L->hist_events[4 * it + 2]) == cudaSuccess)
+        L->last_search_ms += t;
+      if (cudaEventElapsedTime(&t, L->hist_events[4 * it + 2], L->hist_events[4 * it + 3]) == cudaSuccess)
+        L->last_part_ms += t;
+    }
+    cudaGetLastError();
+  }
+  double bytes = 0.0;
+  for (size_t j = 0; j < K; ++j) {
+    const JobState& s = L->h_state[j];
+    double per_row = (double)p.F + (p.quant ? 2.0 : (p.const_hess ? 4.0 : 8.0));
+    bytes += (double)s.hist_rows_direct * per_row + (double)s.hist_rows_gather * (per_row + 4.0);
+    double slot_bytes = 0.0;
+    for (const DevFeature& f : L->h_feat) slot_bytes += (double)f.gbins * (p.quant ? 8.0 : 16.0);
+    bytes += (double)s.hist_builds * slot_bytes;
+  }
+  L->last_hist_bytes = bytes;
+  for (size_t j = 0; j < K; ++j) {
+    const JobState& s = L->h_state[j];
+    int nl = s.tree_leaves;
+    if (num_leaves_out) num_leaves_out[j] = nl;
+    if (root_outputs) root_outputs[j] = s.root_output;
+    if (splits) std::memcpy(splits + j * (Lv - 1), L->h_records + j * Lv, sizeof(bk_split) * (Lv - 1));
+    if (leaf_values) std::memcpy(leaf_values + j * Lv, L->h_leaf_values + j * Lv, sizeof(double) * Lv);
+  }
+}
+
+}  // namespace
+
 int bk_learner_train(bk_learner* L, const float* gradients, const float* hessians, int32_t on_device,
                      const int32_t* rows, int64_t num_rows, bk_split* splits, double* leaf_values,
                      double* root_outputs, int32_t* num_leaves_out) {
@@ -524,95 +633,53 @@ int bk_learner_train(bk_learner* L, const float* gradients, const float* hessian
     set_error("bk_learner_train: invalid arguments");
     return -1;
   }
-  const Params& p = L->p;
-  const size_t n = (size_t)p.n, K = (size_t)L->K;
-  const int Lv = p.num_leaves;
   try {
-    CK(cudaEventRecord(L->ev_start, L->stream));
-    cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
-    if (gradients != L->d_g) CK(cudaMemcpyAsync(L->d_g, gradients, n * K * sizeof(float), kind, L->stream));
-    if (hessians != L->d_h) CK(cudaMemcpyAsync(L->d_h, hessians, n * K * sizeof(float), kind, L->stream));
-    int64_t root_count = rows ? num_rows : (int64_t)n;
-    if (rows) {
-      if (num_rows <= 0 || num_rows > (int64_t)n) {
-        set_error("bk_learner_train: num_rows out of range");
-        return -1;
-      }
-      CK(cudaMemcpyAsync(L->d_rows, rows, sizeof(int32_t) * num_rows, cudaMemcpyHostToDevice, L->stream));
-    }
-    for (size_t j = 0; j < K; ++j) {
-      L->h_state[j].use_rows = rows ? 1 : 0;
-      L->h_state[j].root_count = root_count;
-      L->h_state[j].hist_rows_direct = L->h_state[j].hist_rows_gather = L->h_state[j].hist_builds = 0;
-      JobState* st = L->jobs[j].st;
-      CK(cudaMemcpyAsync(&st->use_rows, &L->h_state[j].use_rows, sizeof(int32_t), cudaMemcpyHostToDevice,
-                         L->stream));
-      CK(cudaMemcpyAsync(&st->root_count, &L->h_state[j].root_count, sizeof(int64_t), cudaMemcpyHostToDevice,
-                         L->stream));
-      CK(cudaMemcpyAsync(&st->hist_rows_direct, &L->h_state[j].hist_rows_direct, 3 * sizeof(int64_t),
-                         cudaMemcpyHostToDevice, L->stream));
-    }
-    if (L->timing && L->hist_events.size() != (size_t)(4 * (Lv - 1))) {
-      for (cudaEvent_t e : L->hist_events) cudaEventDestroy(e);
-      L->hist_events.assign(4 * (Lv - 1), nullptr);
-      for (auto& e : L->hist_events) CK(cudaEventCreate(&e));
-      if (L->graph_exec) {
-        cudaGraphExecDestroy(L->graph_exec);
-        L->graph_exec = nullptr;
-      }
-    }
-    if (L->loop_mode == 1) L->run_graph();
-    else L->run_stepwise();
-    for (size_t j = 0; j < K; ++j) {
-      const Job& J = L->jobs[j];
-      CK(cudaMemcpyAsync(L->h_records + j * Lv, J.records, sizeof(bk_split) * (Lv - 1), cudaMemcpyDeviceToHost,
-                         L->stream));
-      CK(cudaMemcpyAsync(L->h_leaf_values + j * Lv, J.leaf_value, sizeof(double) * Lv, cudaMemcpyDeviceToHost,
-                         L->stream));
-      CK(cudaMemcpyAsync(&L->h_state[j], J.st, offsetof(JobState, mt), cudaMemcpyDeviceToHost, L->stream));
-    }
-    CK(cudaEventRecord(L->ev_end, L->stream));
-    CK(cudaStreamSynchronize(L->stream));
-    CK(cudaGetLastError());
-    float ms = 0.f;
-    CK(cudaEventElapsedTime(&ms, L->ev_start, L->ev_end));
-    L->last_total_ms = ms;
-    L->last_hist_ms = L->last_search_ms = L->last_part_ms = 0.0;
-    if (L->timing) {
-      // the phases of the steps that ran (a finished tree's remaining steps return early but are
-      // still timed: they are part of the replayed graph); a stepwise loop that stopped early
-      // leaves later events unrecorded, which the elapsed-time calls report and skip
-      for (int it = 0; it < Lv - 1; ++it) {
-        float t = 0.f;
-        if (cudaEventElapsedTime(&t, L->hist_events[4 * it], L->hist_events[4 * it + 1]) == cudaSuccess)
-          L->last_hist_ms += t;
-        if (cudaEventElapsedTime(&t, L->hist_events[4 * it + 1], L->hist_events[4 * it + 2]) == cudaSuccess)
-          L->last_search_ms += t;
-        if (cudaEventElapsedTime(&t, L->hist_events[4 * it + 2], L->hist_events[4 * it + 3]) == cudaSuccess)
-          L->last_part_ms += t;
-      }
-      cudaGetLastError();
-    }
-    double bytes = 0.0;
-    for (size_t j = 0; j < K; ++j) {
-      const JobState& s = L->h_state[j];
-      double per_row = (double)p.F + (p.quant ? 2.0 : (p.const_hess ? 4.0 : 8.0));
-      bytes += (double)s.hist_rows_direct * per_row + (double)s.hist_rows_gather * (per_row + 4.0);
-      double slot_bytes = 0.0;
-      for (const DevFeature& f : L->h_feat) slot_bytes += (double)f.gbins * (p.quant ? 8.0 : 16.0);
-      bytes += (double)s.hist_builds * slot_bytes;
-    }
-    L->last_hist_bytes = bytes;
-    for (size_t j = 0; j < K; ++j) {
-      const JobState& s = L->h_state[j];
-      int nl = s.tree_leaves;
-      if (num_leaves_out) num_leaves_out[j] = nl;
-      if (root_outputs) root_outputs[j] = s.root_output;
-      if (splits) std::memcpy(splits + j * (Lv - 1), L->h_records + j * Lv, sizeof(bk_split) * (Lv - 1));
-      if (leaf_values) std::memcpy(leaf_values + j * Lv, L->h_leaf_values + j * Lv, sizeof(double) * Lv);
-    }
+    if (!train_enqueue(L, gradients, hessians, on_device, rows, num_rows, 0.0, nullptr)) return -1;
+    train_finish(L, splits, leaf_values, root_outputs, num_leaves_out);
   } catch (const CudaError& e) {
     return fail_cuda(e);
+  }
+  return 0;
+}
+
+int bk_learners_train_batch(bk_learner* const* learners, int32_t count, const float* const* gradients,
+                            const float* const* hessians, int32_t on_device, double shrinkage,
+                            double* const* scores, bk_split* const* splits, double* const* leaf_values,
+                            double* const* root_outputs, int32_t* const* num_leaves_out) {
+  if (!learners || count <= 0 || !gradients || !hessians) {
+    set_error("bk_learners_train_batch: invalid arguments");
+    return -1;
+  }
+  for (int32_t i = 0; i < count; ++i) {
+    if (!learners[i] || !gradients[i] || !hessians[i]) {
+      set_error("bk_learners_train_batch: learner %d: invalid arguments", i);
+      return -1;
+    }
+    for (int32_t k = 0; k < i; ++k)
+      if (learners[k] == learners[i]) {
+        set_error("bk_learners_train_batch: learner %d appears twice", i);
+        return -1;
+      }
+  }
+  int32_t i = 0;
+  try {
+    // every learner's iteration is queued on its own stream before any is waited for, so the
+    // devices's schedulers interleave the independent grow loops
+    for (i = 0; i < count; ++i)
+      if (!train_enqueue(learners[i], gradients[i], hessians[i], on_device, nullptr, 0, shrinkage,
+                         scores ? scores[i] : nullptr)) {
+        std::string msg = "learner " + std::to_string(i) + ": " + g_last_error;
+        for (int32_t k = 0; k < i; ++k) cudaStreamSynchronize(learners[k]->stream);
+        set_error("bk_learners_train_batch: %s", msg.c_str());
+        return -1;
+      }
+    for (i = 0; i < count; ++i)
+      train_finish(learners[i], splits ? splits[i] : nullptr, leaf_values ? leaf_values[i] : nullptr,
+                   root_outputs ? root_outputs[i] : nullptr, num_leaves_out ? num_leaves_out[i] : nullptr);
+  } catch (const CudaError& e) {
+    for (int32_t k = 0; k < count; ++k) cudaStreamSynchronize(learners[k]->stream);
+    set_error("bk_learners_train_batch: learner %d: CUDA error: %s", i, e.msg.c_str());
+    return -1;
   }
   return 0;
 }

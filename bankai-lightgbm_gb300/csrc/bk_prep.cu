@@ -306,6 +306,22 @@ __global__ void k_add_score(const Job* __restrict__ jobs, Params p, const double
     sc[idx[k]] += v;
 }
 
+// The same update with the tree's own leaf outputs from the device, shrunk as Tree::apply_shrinkage
+// does (tree.rs:446-463): score += round_to_zero(leaf_value * rate). A one-leaf tree adds nothing
+// (train.rs:776-795 turns it into a constant tree instead).
+__global__ void k_add_score_own(const Job* __restrict__ jobs, Params p, double rate, double* __restrict__ score) {
+  const Job& J = jobs[blockIdx.z];
+  const int32_t leaf = blockIdx.y;
+  if (leaf >= J.st->tree_leaves || J.st->tree_leaves <= 1) return;
+  double v = __dmul_rn(J.leaf_value[leaf], rate);
+  if (v >= -BK_ZERO_THRESHOLD && v <= BK_ZERO_THRESHOLD) v = 0.0;
+  const int64_t begin = J.leaf_begin[leaf], cnt = J.leaf_count[leaf];
+  const int32_t* idx = leaf_idx(J, J.leaf_buf[leaf]) + begin;
+  double* sc = score + (size_t)blockIdx.z * p.n;
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < cnt; k += (int64_t)gridDim.x * blockDim.x)
+    sc[idx[k]] += v;
+}
+
 __global__ void k_row_leaf(const Job* __restrict__ jobs, Params p, int32_t* __restrict__ out) {
   const Job& J = jobs[blockIdx.z];
   const int32_t leaf = blockIdx.y;
@@ -348,6 +364,11 @@ void launch_renew(const Job* d_jobs, int num_jobs, const Params& p, cudaStream_t
 void launch_add_score(const Job* d_jobs, int num_jobs, const Params& p, const double* leaf_vals, double* score,
                       cudaStream_t s) {
   k_add_score<<<dim3(8, p.num_leaves, num_jobs), 256, 0, s>>>(d_jobs, p, leaf_vals, score);
+}
+
+void launch_add_score_own(const Job* d_jobs, int num_jobs, const Params& p, double rate, double* score,
+                          cudaStream_t s) {
+  k_add_score_own<<<dim3(8, p.num_leaves, num_jobs), 256, 0, s>>>(d_jobs, p, rate, score);
 }
 
 void launch_row_leaf(const Job* d_jobs, int num_jobs, const Params& p, int32_t* out, cudaStream_t s) {

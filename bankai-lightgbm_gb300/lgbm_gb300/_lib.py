@@ -57,6 +57,7 @@ _GPU_SIGNATURES = [
     ("bk_learner_create_device_bins", _i32, [_P, _i32, _P, _i64, _P, _i32, _P]),
     ("bk_bin_dense_device", _i32, [_P, _i32, _i64, _i32, _P, _i32, _P, _P, _P, _P]),
     ("bk_learner_train", _i32, [_P, _P, _P, _i32, _P, _i64, _P, _P, _P, _P]),
+    ("bk_learners_train_batch", _i32, [_P, _i32, _P, _P, _i32, _f64, _P, _P, _P, _P, _P]),
     ("bk_learner_add_prediction_to_score", _i32, [_P, _P, _P, _i32]),
     ("bk_learner_row_leaf", _i32, [_P, _P]),
     ("bk_learner_set_loop_mode", _i32, [_P, _i32]),

@@ -165,3 +165,49 @@ class GpuTreeLearner:
             assert score.dtype == np.float64 and score.flags.c_contiguous
             _lib.check(self.lib.bk_learner_add_prediction_to_score(self.h, lv.ctypes.data, score.ctypes.data, 0),
                        "bk_learner_add_prediction_to_score")
+
+
+def train_batch(learners, gradients, hessians, on_device=False, shrinkage=None, scores=None):
+    """One tree per learner for many independent learners at once (``bk_learners_train_batch``):
+    every learner's grow loop is queued on its own stream before any is waited for.
+
+    gradients / hessians: per learner, a [num_jobs, num_data] float32 array, or a device pointer
+    (int) with on_device=True. scores: None, or per learner a device pointer to its
+    [num_jobs, num_data] f64 score, which then receives the new trees' leaf outputs times
+    ``shrinkage``. Returns per learner (splits, leaf_values, root_outputs, num_leaves) as
+    ``GpuTreeLearner.train_raw`` does."""
+    count = len(learners)
+    assert count > 0 and len(gradients) == count and len(hessians) == count
+    lib = learners[0].lib
+    keep = []
+    gp = (ctypes.c_void_p * count)()
+    hp = (ctypes.c_void_p * count)()
+    for i, L in enumerate(learners):
+        if on_device:
+            gp[i], hp[i] = int(gradients[i]), int(hessians[i])
+        else:
+            g = np.ascontiguousarray(gradients[i], dtype=np.float32).reshape(L.num_jobs, -1)
+            hh = np.ascontiguousarray(hessians[i], dtype=np.float32).reshape(L.num_jobs, -1)
+            assert g.shape[1] == L.ds.num_data and hh.shape == g.shape
+            keep += [g, hh]
+            gp[i], hp[i] = g.ctypes.data, hh.ctypes.data
+    outs = []
+    sp = (ctypes.c_void_p * count)()
+    lp = (ctypes.c_void_p * count)()
+    rp = (ctypes.c_void_p * count)()
+    np_ = (ctypes.c_void_p * count)()
+    for i, L in enumerate(learners):
+        K, Lv = L.num_jobs, L.num_leaves
+        o = (np.zeros((K, max(Lv - 1, 1)), dtype=SPLIT_DTYPE), np.zeros((K, Lv), dtype=np.float64),
+             np.zeros(K, dtype=np.float64), np.zeros(K, dtype=np.int32))
+        outs.append(o)
+        sp[i], lp[i], rp[i], np_[i] = (a.ctypes.data for a in o)
+    hs = (ctypes.c_void_p * count)(*[L.h.value for L in learners])
+    sc = None
+    if scores is not None:
+        assert shrinkage is not None and len(scores) == count
+        sc = (ctypes.c_void_p * count)(*[int(s) for s in scores])
+    _lib.check(lib.bk_learners_train_batch(hs, count, gp, hp, int(bool(on_device)),
+                                           float(shrinkage if shrinkage is not None else 0.0), sc, sp, lp, rp, np_),
+               "bk_learners_train_batch")
+    return outs

@@ -272,6 +272,7 @@ def run_gpu(args, rank, world):
     plain = form(False, 0, args.steps, args.warmup)
     e2e = form(True, 1, args.steps, 1, e2e=True)
     multiclass = run_multiclass(args) if args.multiclass_rows > 0 else None
+    batched_jobs = run_batched_jobs(args) if args.batch_jobs > 0 else None
     ms, value = aggregate_ranks(main["ms_per_step"], world)
     hist_gbs = roof["hist_bytes"] / (roof["hist_ms"] * 1e6) if roof["hist_ms"] > 0 else None
     hist_launches = (args.leaves - 1) * args.steps  # one histogram launch per split step of a tree
@@ -296,7 +297,7 @@ def run_gpu(args, rank, world):
                                            "train_l2": plain["loss_final"], "heldout_l2": plain["heldout_l2"],
                                            "iterations": plain["iterations"]},
                   "heldout_l2_delta": main["heldout_l2"] - plain["heldout_l2"], "heldout_rows": m_ho,
-                  "multiclass_k10": multiclass},
+                  "multiclass_k10": multiclass, "batched_jobs": batched_jobs},
         "e2e": {"value": round(world * 1000.0 / e2e["ms_per_step"], 4), "unit": "iters/s",
                 "h2d_bytes_per_step": 2 * 4 * ds.num_data,
                 "d2h_bytes_per_step": 112 * (args.leaves - 1) + 8 * args.leaves + 8 + 8},
@@ -382,6 +383,89 @@ def run_multiclass(args):
                         "gradients + 10 class trees in one call + score update" % n,
             "quantized_graph": q, "plain_float_stepwise": p,
             "heldout_logloss_delta": round(q["heldout_logloss"] - p["heldout_logloss"], 6)}
+
+
+def run_batched_jobs(args):
+    """Independent binary-classification jobs: rows log-uniform in [5,000, 500,000], features
+    uniform in [20, 300] (N(0,1), 1% NaN), logistic labels from per-job random linear models,
+    max_bin drawn from {15, 63, 255}, 31 leaves, quantized gradients. Every job has its own
+    learner, dataset and stream. One iteration = device binary gradients + one tree + device score
+    update for every job; timed for the jobs one after another (bk_learner_train per job) and for
+    all jobs in one bk_learners_train_batch call per iteration. Host wall clock around each
+    iteration loop, bracketed by device synchronization (the work spans many streams)."""
+    import torch
+    from lgbm_gb300 import BinnedDataset, GpuTreeLearner, LearnerConfig, train_batch
+    rng = np.random.default_rng(7)
+    threads = min(32, os.cpu_count() or 8)
+    jobs = []
+    t0 = time.time()
+    for i in range(args.batch_jobs):
+        n = int(round(np.exp(rng.uniform(np.log(5_000), np.log(500_000)))))
+        F = int(rng.integers(20, 301))
+        mb = int(rng.choice([15, 63, 255]))
+        X = rng.standard_normal((n, F), dtype=np.float32)
+        w = (rng.standard_normal(F) * (rng.random(F) < 0.2)).astype(np.float32)
+        z = X @ w
+        X[rng.random((n, F), dtype=np.float32) < 0.01] = np.nan
+        y = (rng.random(n) < 1.0 / (1.0 + np.exp(-z))).astype(np.float32)
+        ds = BinnedDataset.from_dense(X, max_bin=mb, min_data_in_leaf=20, threads=threads)
+        jobs.append((ds, torch.from_numpy(y).cuda(), mb))
+        del X
+    prep_s = time.time() - t0
+    rows = [ds.num_data for ds, _, _ in jobs]
+    feats = [ds.num_features for ds, _, _ in jobs]
+
+    def make():
+        out = []
+        for i, (ds, label, mb) in enumerate(jobs):
+            cfg = LearnerConfig(num_leaves=31, min_data_in_leaf=20, use_quantized_grad=1, num_grad_quant_bins=4,
+                                stochastic_rounding=1, seed=i, num_threads=16, fused_madd=1)
+            L = GpuTreeLearner(ds, cfg)
+            score = torch.zeros(ds.num_data, dtype=torch.float64, device="cuda")
+            out.append((L, score, label, L.gradient_buffers()))
+        torch.cuda.synchronize()
+        return out
+
+    def run(learners, batched, iters):
+        for L, score, label, _ in learners:
+            score.zero_()
+        torch.cuda.synchronize()
+        t = time.perf_counter()
+        for _ in range(iters):
+            if batched:
+                for L, score, label, _ in learners:
+                    L.objective_gradients(1, score.data_ptr(), label.data_ptr())
+                train_batch([x[0] for x in learners], [x[3][0] for x in learners], [x[3][1] for x in learners],
+                            on_device=True, shrinkage=0.1, scores=[x[1].data_ptr() for x in learners])
+            else:
+                for L, score, label, (gb, hb) in learners:
+                    L.objective_gradients(1, score.data_ptr(), label.data_ptr())
+                    _, lv, _, nls = L.train_raw(gb, hb, on_device=True)
+                    if nls[0] > 1:
+                        vals = lv * 0.1
+                        vals[np.abs(vals) <= K_ZERO_THRESHOLD] = 0.0
+                        L.add_prediction_to_score(vals, score.data_ptr(), on_device=True)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t
+        loss = float(np.mean([L.objective_loss(1, score.data_ptr(), label.data_ptr()) for L, score, label, _ in learners]))
+        return dt, loss
+
+    learners = make()
+    run(learners, True, 1)  # warm-up: graph capture of every learner
+    run(learners, False, 1)
+    seq_s, seq_loss = run(learners, False, args.batch_iters)
+    bat_s, bat_loss = run(learners, True, args.batch_iters)
+    for L, _, _, _ in learners:
+        L.close()
+    J, it = len(jobs), args.batch_iters
+    return {"workload": "%d independent binary jobs, rows log-uniform 5k-500k (total %d), features 20-300 (mean %.0f), "
+                        "max_bin in {15, 63, 255}, 31 leaves, quantized; %d iterations each"
+                        % (J, sum(rows), float(np.mean(feats)), it),
+            "one_by_one": {"job_iters_per_s": round(J * it / seq_s, 2), "s": round(seq_s, 3),
+                           "mean_train_logloss": round(seq_loss, 6)},
+            "batched": {"job_iters_per_s": round(J * it / bat_s, 2), "s": round(bat_s, 3),
+                        "mean_train_logloss": round(bat_loss, 6)},
+            "speedup": round(seq_s / bat_s, 3), "prep_s": round(prep_s, 1)}
 
 
 def run_hist_traffic(args):
@@ -473,6 +557,9 @@ def run_reference(args):
 
 
 def main():
+    # the batched-jobs form runs one stream per job: give the device more hardware queues than the
+    # default 8 so that independent streams do not serialise behind each other
+    os.environ.setdefault("CUDA_DEVICE_MAX_CONNECTIONS", "32")
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=10)
@@ -481,6 +568,9 @@ def main():
     ap.add_argument("--rows", type=int, default=10_000_000)
     ap.add_argument("--leaves", type=int, default=255)
     ap.add_argument("--cpu-rows", type=int, default=1_000_000)
+    ap.add_argument("--batch-jobs", type=int, default=32,
+                    help="independent jobs of the batched-jobs form (256 for the full set; 0: skip it)")
+    ap.add_argument("--batch-iters", type=int, default=10, help="iterations per job of the batched-jobs form")
     ap.add_argument("--multiclass-rows", type=int, default=2_000_000,
                     help="rows of the K=10 multiclass form reported beside the headline (0: skip it)")
     ap.add_argument("--hist-traffic", action="store_true",

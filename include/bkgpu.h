@@ -94,6 +94,23 @@ int bk_learner_train(bk_learner* learner, const float* gradients, const float* h
                      const int32_t* rows, int64_t num_rows, bk_split* splits, double* leaf_values,
                      double* root_outputs, int32_t* num_leaves_out);
 
+/* Many independent boosting jobs at once: one bk_learner_train call (all rows, no bagging) for
+ * each of `count` distinct learners — each with its own dataset, shape and config — queued on
+ * the learners' own streams before any is waited for, so their grow loops run concurrently on
+ * the device; then, if `scores` is not NULL, each learner's score update with its new trees
+ * (train.rs:776-785: leaf outputs times `shrinkage`, values within kZeroThreshold of 0 set to 0
+ * as Tree::apply_shrinkage does, tree.rs:446-463; a one-leaf tree adds nothing).
+ * Per learner i: gradients[i] / hessians[i] as in bk_learner_train (host or device, on_device);
+ * scores[i]: device f64 [num_jobs][num_data]; splits[i], leaf_values[i], root_outputs[i],
+ * num_leaves_out[i]: host outputs as in bk_learner_train (each array of pointers may be NULL).
+ * Replaces the per-job calls of SerialTreeLearner::train (serial.rs:569-628) and
+ * add_prediction_to_score (serial.rs:1974-1990) that a host running many Boosters would make
+ * one after another. Returns after every learner has finished. */
+int bk_learners_train_batch(bk_learner* const* learners, int32_t count, const float* const* gradients,
+                            const float* const* hessians, int32_t on_device, double shrinkage, double* const* scores,
+                            bk_split* const* splits, double* const* leaf_values, double* const* root_outputs,
+                            int32_t* const* num_leaves_out);
+
 /* Replaces SerialTreeLearner::add_prediction_to_score (serial.rs:1974-1990): for every job j
  * and every row r of leaf l of the last tree, score[j][r] += leaf_values[j][l].
  * score: [num_jobs][num_data] f64, host or device (on_device); leaf_values: host. */
