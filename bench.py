@@ -575,7 +575,14 @@ def main():
                     help="rows of the K=10 multiclass form reported beside the headline (0: skip it)")
     ap.add_argument("--hist-traffic", action="store_true",
                     help="train one tree and print the histogram kernel's algorithmic bytes (for an ncu capture)")
+    ap.add_argument("--only", choices=["multiclass", "batched"],
+                    help="run only that side form and print its result (not a bench line)")
     args = ap.parse_args()
+    if args.only:
+        import torch
+        torch.cuda.set_device(0)
+        print(json.dumps(run_multiclass(args) if args.only == "multiclass" else run_batched_jobs(args)))
+        return
     if args.hist_traffic:
         print(json.dumps(run_hist_traffic(args)))
         return
