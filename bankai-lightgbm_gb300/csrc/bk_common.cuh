@@ -64,7 +64,8 @@ struct Params {
   int32_t min_data, fused, use_l1, use_max, use_smooth, quant;
   int32_t const_hess, num_leaves, max_depth, F;
   int32_t T, B, quant_bins, stochastic;
-  int32_t renew, part_grid, pdl, _p1;  // pdl: launch the grow-loop kernels with programmatic dependence
+  int32_t renew, part_grid, pdl;  // pdl: launch the grow-loop kernels with programmatic dependence
+  int32_t hist_min_rows;          // fewest rows a histogram CTA takes (launch shape, autotuned)
   int64_t n;
 };
 
@@ -163,6 +164,8 @@ __device__ __forceinline__ int16_t* leaf_pk(const Job& J, int32_t buf) { return 
 __host__ __device__ __forceinline__ int64_t ceil_div64(int64_t a, int64_t b) { return (a + b - 1) / b; }
 
 // ---- launchers (defined in the kernel translation units) ----
+constexpr int kMaxPartGrid = 1024;  // most partition CTAs per launch (the per-CTA count scratch)
+
 struct HistLaunch {
   int blocks_per_tile;
   int threads;

@@ -30,10 +30,6 @@ namespace bk {
 
 namespace {
 
-// At least 256 rows (eight warps' worth) per CTA: small leaves spread over as many SMs as they can
-// fill, since a CTA's rows cost its SM's load and shared-atomic pipes, not a DRAM share.
-constexpr int kMinChunk = 256;
-
 __device__ __forceinline__ float two_sum_err(float a, float b, float s) {
   float bb = __fsub_rn(s, a);
   float e1 = __fsub_rn(a, __fsub_rn(s, bb));
@@ -77,8 +73,11 @@ __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blo
     r->slot = st->smaller_slot;
     r->pk_row = st->tree_leaves == 1;  // the root: no leaf-ordered copy yet
   }
+  // at least p.hist_min_rows rows per CTA (256 by default, eight warps' worth): small leaves spread
+  // over as many SMs as they can fill, since a CTA's rows cost its SM's load and shared-atomic
+  // pipes, not a DRAM share
   int64_t chunk = ceil_div64(count, blocks_per_tile);
-  if (chunk < kMinChunk) chunk = kMinChunk;
+  if (chunk < p.hist_min_rows) chunk = p.hist_min_rows;
   chunk = (chunk + 31) / 32 * 32;
   r->r0 = (int64_t)blockIdx.x * chunk;
   if (r->r0 >= count) return false;

@@ -11,9 +11,12 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <array>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -177,6 +180,22 @@ struct bk_learner {
     if (stream) cudaStreamDestroy(stream);
   }
 
+  // The launch shape of the grow-loop kernels, clamped to what the dataset's rows can fill: a
+  // leaf never has more rows than the dataset, so CTAs past n / min_rows would never get rows.
+  // Results do not depend on it (integer histograms are exact; the float path changes only its
+  // rounding order; the partitions it feeds are the same). The graph is captured anew.
+  void set_launch_shape(int hist_min_rows, int hist_ctas_per_tile, int part_grid) {
+    const int64_t n = p.n;
+    p.hist_min_rows = std::max(32, hist_min_rows / 32 * 32);
+    hl.blocks_per_tile = (int)std::max<int64_t>(
+        1, std::min<int64_t>(hist_ctas_per_tile, (n + p.hist_min_rows - 1) / p.hist_min_rows));
+    p.part_grid = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(part_grid, kMaxPartGrid), (n + 255) / 256));
+    if (graph_exec) {
+      cudaGraphExecDestroy(graph_exec);
+      graph_exec = nullptr;
+    }
+  }
+
   bool capturing = false;
   void record_hist_event(int i) {
     if (!timing || (size_t)i >= hist_events.size()) return;
@@ -333,7 +352,6 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
     p.quant_bins = c->num_grad_quant_bins;
     p.stochastic = c->stochastic_rounding ? 1 : 0;
     p.renew = c->quant_train_renew_leaf ? 1 : 0;
-    p.part_grid = std::min(1024, 2 * L->num_sms);
     p.n = num_data;
     L->K = num_jobs;
     int maxb = 0;
@@ -371,9 +389,11 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
         }
     }
     p.B = (maxb + 7) / 8 * 8;
-    // histogram launch shape: one 1024-thread CTA per SM, split evenly over the feature tiles
+    // launch shapes: histogram CTAs of 1024 threads, one per SM, split evenly over the feature
+    // tiles, each taking at least 256 rows; two partition CTAs per SM; no more CTAs than the
+    // dataset's rows can fill (bk_learner_autotune may change all three)
     L->hl.threads = 1024;
-    L->hl.blocks_per_tile = std::max(1, L->num_sms / p.T);
+    L->set_launch_shape(256, L->num_sms / p.T, 2 * L->num_sms);
     bool wide = false;
     if (quant) {
       int max_h = p.const_hess ? 1 : p.quant_bins;
@@ -477,7 +497,7 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
       J.records = L->dalloc<bk_split>(Lv);
       J.leaf_value = L->dalloc<double>(Lv);
       J.pool = reinterpret_cast<uint8_t*>(L->d_pool) + L->pool_bytes_per_job * j;
-      J.part_cnt = L->dalloc<int64_t>(p.part_grid);
+      J.part_cnt = L->dalloc<int64_t>(kMaxPartGrid);
       J.red = L->dalloc<double>(2 * kRootGrid);
       J.ired = L->dalloc<int64_t>(2 * kRootGrid);
       CK(cudaMemset(J.records, 0, sizeof(bk_split) * Lv));
@@ -639,6 +659,135 @@ int bk_learner_train(bk_learner* L, const float* gradients, const float* hessian
   } catch (const CudaError& e) {
     return fail_cuda(e);
   }
+  return 0;
+}
+
+namespace {
+
+// Autotuned launch shapes by dataset shape class: (log2 rows, feature tiles, bins per feature
+// slot, quantized, num_leaves) -> (hist_min_rows, hist CTAs per tile, partition CTAs).
+std::mutex g_tune_mutex;
+std::map<std::array<int, 5>, std::array<int, 3>> g_tune_cache;
+
+std::array<int, 5> tune_key(const bk_learner* L) {
+  int lg = 0;
+  while ((int64_t(1) << (lg + 1)) <= L->p.n) ++lg;
+  return {lg, L->p.T, L->p.B, L->p.quant, L->p.num_leaves};
+}
+
+}  // namespace
+
+int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hessians, int32_t on_device,
+                        int32_t trials, int32_t* shape_out) {
+  if (!L || !gradients || !hessians || trials < 1) {
+    set_error("bk_learner_autotune: invalid arguments");
+    return -1;
+  }
+  const auto key = tune_key(L);
+  {
+    std::lock_guard<std::mutex> g(g_tune_mutex);
+    auto it = g_tune_cache.find(key);
+    if (it != g_tune_cache.end()) {
+      L->set_launch_shape(it->second[0], it->second[1], it->second[2]);
+      if (shape_out) {
+        shape_out[0] = L->p.hist_min_rows;
+        shape_out[1] = L->hl.blocks_per_tile;
+        shape_out[2] = L->p.part_grid;
+      }
+      return 0;
+    }
+  }
+  const int sms = L->num_sms, T = L->p.T;
+  const int saved_mode = L->loop_mode;
+  JobState* saved = nullptr;
+  const size_t state_bytes = sizeof(JobState) * (size_t)L->K;
+  try {
+    // the trial trees must not advance the learner's state across trees (the stochastic-rounding
+    // engine): the job states are saved here and put back afterwards
+    CK(cudaMallocAsync((void**)&saved, state_bytes, L->stream));
+    CK(cudaMemcpyAsync(saved, L->jobs[0].st, state_bytes, cudaMemcpyDeviceToDevice, L->stream));
+    const size_t n = (size_t)L->p.n * (size_t)L->K;
+    cudaMemcpyKind kind = on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice;
+    if (gradients != L->d_g) CK(cudaMemcpyAsync(L->d_g, gradients, n * sizeof(float), kind, L->stream));
+    if (hessians != L->d_h) CK(cudaMemcpyAsync(L->d_h, hessians, n * sizeof(float), kind, L->stream));
+    L->loop_mode = 1;
+    std::map<std::array<int, 3>, double> seen;
+    // one tree per trial (graph form) after one untimed tree of each shape; the median device time
+    auto measure = [&](int min_rows, int ctas, int grid) -> std::pair<std::array<int, 3>, double> {
+      L->set_launch_shape(min_rows, ctas, grid);
+      std::array<int, 3> s = {L->p.hist_min_rows, L->hl.blocks_per_tile, L->p.part_grid};
+      auto f = seen.find(s);
+      if (f != seen.end()) return {s, f->second};
+      std::vector<double> t;
+      for (int r = 0; r <= trials; ++r) {
+        CK(cudaMemcpyAsync(L->jobs[0].st, saved, state_bytes, cudaMemcpyDeviceToDevice, L->stream));
+        if (!train_enqueue(L, L->d_g, L->d_h, 1, nullptr, 0, 0.0, nullptr)) throw CudaError{g_last_error};
+        train_finish(L, nullptr, nullptr, nullptr, nullptr);
+        if (r > 0) t.push_back(L->last_total_ms);
+      }
+      std::sort(t.begin(), t.end());
+      seen[s] = t[t.size() / 2];
+      return {s, t[t.size() / 2]};
+    };
+    // coordinate descent from the default shape: rows per histogram CTA, histogram CTAs per
+    // feature tile, partition CTAs
+    std::array<int, 3> best = {256, sms / T, 2 * sms};
+    double best_ms = measure(best[0], best[1], best[2]).second;
+    auto consider = [&](std::array<int, 3> c) {
+      auto r = measure(c[0], c[1], c[2]);
+      if (r.second < best_ms) {
+        best_ms = r.second;
+        best = c;
+      }
+    };
+    for (int mr : {64, 128, 512, 1024}) consider({mr, best[1], best[2]});
+    consider({best[0], 2 * sms / T, best[2]});
+    for (int pg : {sms, 4 * sms}) consider({best[0], best[1], pg});
+    CK(cudaMemcpyAsync(L->jobs[0].st, saved, state_bytes, cudaMemcpyDeviceToDevice, L->stream));
+    CK(cudaFreeAsync(saved, L->stream));
+    saved = nullptr;
+    CK(cudaStreamSynchronize(L->stream));
+    L->loop_mode = saved_mode;
+    L->set_launch_shape(best[0], best[1], best[2]);
+    {
+      std::lock_guard<std::mutex> g(g_tune_mutex);
+      g_tune_cache[key] = best;
+    }
+    if (shape_out) {
+      shape_out[0] = L->p.hist_min_rows;
+      shape_out[1] = L->hl.blocks_per_tile;
+      shape_out[2] = L->p.part_grid;
+    }
+  } catch (const CudaError& e) {
+    if (saved) {
+      cudaMemcpyAsync(L->jobs[0].st, saved, state_bytes, cudaMemcpyDeviceToDevice, L->stream);
+      cudaFreeAsync(saved, L->stream);
+      cudaStreamSynchronize(L->stream);
+    }
+    L->loop_mode = saved_mode;
+    set_error("bk_learner_autotune: %s", e.msg.c_str());
+    return -1;
+  }
+  return 0;
+}
+
+int bk_learner_set_launch_shape(bk_learner* L, const int32_t* shape) {
+  if (!L || !shape || shape[0] < 32 || shape[1] < 1 || shape[2] < 1) {
+    set_error("bk_learner_set_launch_shape: invalid arguments");
+    return -1;
+  }
+  L->set_launch_shape(shape[0], shape[1], shape[2]);
+  return 0;
+}
+
+int bk_learner_launch_shape(bk_learner* L, int32_t* shape_out) {
+  if (!L || !shape_out) {
+    set_error("bk_learner_launch_shape: invalid arguments");
+    return -1;
+  }
+  shape_out[0] = L->p.hist_min_rows;
+  shape_out[1] = L->hl.blocks_per_tile;
+  shape_out[2] = L->p.part_grid;
   return 0;
 }
 

@@ -67,6 +67,33 @@ class GpuTreeLearner:
                                  dtype=np.uint8)
         _lib.check(self.lib.bk_learner_set_feature_mask(self.h, m.ctypes.data), "bk_learner_set_feature_mask")
 
+    def autotune(self, gradients, hessians, on_device=False, trials=2):
+        """Picks the grow-loop launch shape by timing whole trees grown from these gradients
+        (bk_learner_autotune; cached per dataset shape class). Returns the chosen shape
+        (rows per histogram CTA, histogram CTAs per feature tile, partition CTAs)."""
+        K = self.num_jobs
+        if on_device:
+            gp, hp = int(gradients), int(hessians)
+        else:
+            g = np.ascontiguousarray(gradients, dtype=np.float32).reshape(K, -1)
+            hh = np.ascontiguousarray(hessians, dtype=np.float32).reshape(K, -1)
+            assert g.shape[1] == self.ds.num_data and hh.shape == g.shape
+            gp, hp = g.ctypes.data, hh.ctypes.data
+        out = np.zeros(3, np.int32)
+        _lib.check(self.lib.bk_learner_autotune(self.h, gp, hp, int(bool(on_device)), int(trials), out.ctypes.data),
+                   "bk_learner_autotune")
+        return tuple(int(x) for x in out)
+
+    def launch_shape(self):
+        out = np.zeros(3, np.int32)
+        _lib.check(self.lib.bk_learner_launch_shape(self.h, out.ctypes.data), "bk_learner_launch_shape")
+        return tuple(int(x) for x in out)
+
+    def set_launch_shape(self, shape):
+        arr = np.ascontiguousarray(shape, dtype=np.int32)
+        assert arr.shape == (3,)
+        _lib.check(self.lib.bk_learner_set_launch_shape(self.h, arr.ctypes.data), "bk_learner_set_launch_shape")
+
     def set_timing(self, on: bool):
         _lib.check(self.lib.bk_learner_set_timing(self.h, int(bool(on))), "bk_learner_set_timing")
 

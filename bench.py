@@ -174,6 +174,8 @@ def run_gpu(args, rank, world):
     m_ho = ho_bins.shape[1]
     peak, peak_kind = _peaks()
 
+    shapes = {}
+
     def form(quant, loop_mode, steps, warmup, e2e=False, timing=False):
         learner = GpuTreeLearner(ds, make_cfg(quant, args.leaves), loop_mode=loop_mode)
         learner.set_timing(timing)
@@ -181,6 +183,12 @@ def run_gpu(args, rank, world):
         score = torch.full((n,), float(y.astype(np.float64).mean()), dtype=torch.float64, device="cuda")
         gbuf, hbuf = learner.gradient_buffers()
         torch.cuda.synchronize()  # score and labels are written on torch's stream
+        if args.autotune:
+            # launch shape from trial trees on the first iteration's gradients (cached per shape
+            # class, so only the first learner of each form kind pays for the trials)
+            learner.objective_gradients(0, score.data_ptr(), label.data_ptr())
+            learner.autotune(gbuf, hbuf, on_device=True, trials=2)
+        shapes[(quant, loop_mode)] = learner.launch_shape()
         pin_g = torch.empty(n, dtype=torch.float32).pin_memory() if e2e else None
         pin_h = torch.empty(n, dtype=torch.float32).pin_memory() if e2e else None
         stats = dict(hist_ms=0.0, hist_bytes=0.0, train_ms=0.0, search_ms=0.0, part_ms=0.0, leaves=0, loss=None)
@@ -292,10 +300,12 @@ def run_gpu(args, rank, world):
                                       "search_ms": round(roof["search_ms"] / max(args.steps, 1), 3),
                                       "partition_ms": round(roof["part_ms"] / max(args.steps, 1), 3),
                                       "train_l2": main["loss_final"], "heldout_l2": main["heldout_l2"],
-                                      "iterations": main["iterations"]},
+                                      "iterations": main["iterations"],
+                                      "launch_shape": _shape_dict(shapes.get((True, 1)), args.autotune)},
                   "plain_float_stepwise": {"iters_per_s": round(1000.0 / plain["ms_per_step"], 4),
                                            "train_l2": plain["loss_final"], "heldout_l2": plain["heldout_l2"],
-                                           "iterations": plain["iterations"]},
+                                           "iterations": plain["iterations"],
+                                           "launch_shape": _shape_dict(shapes.get((False, 0)), args.autotune)},
                   "heldout_l2_delta": main["heldout_l2"] - plain["heldout_l2"], "heldout_rows": m_ho,
                   "multiclass_k10": multiclass, "batched_jobs": batched_jobs},
         "e2e": {"value": round(world * 1000.0 / e2e["ms_per_step"], 4), "unit": "iters/s",
@@ -422,7 +432,12 @@ def run_batched_jobs(args):
                                 stochastic_rounding=1, seed=i, num_threads=16, fused_madd=1)
             L = GpuTreeLearner(ds, cfg)
             score = torch.zeros(ds.num_data, dtype=torch.float64, device="cuda")
-            out.append((L, score, label, L.gradient_buffers()))
+            gb, hb = L.gradient_buffers()
+            if args.autotune:
+                torch.cuda.synchronize()
+                L.objective_gradients(1, score.data_ptr(), label.data_ptr())
+                L.autotune(gb, hb, on_device=True, trials=1)
+            out.append((L, score, label, (gb, hb)))
         torch.cuda.synchronize()
         return out
 
@@ -450,7 +465,9 @@ def run_batched_jobs(args):
         loss = float(np.mean([L.objective_loss(1, score.data_ptr(), label.data_ptr()) for L, score, label, _ in learners]))
         return dt, loss
 
+    t0 = time.time()
     learners = make()
+    setup_s = time.time() - t0
     run(learners, True, 1)  # warm-up: graph capture of every learner
     run(learners, False, 1)
     seq_s, seq_loss = run(learners, False, args.batch_iters)
@@ -465,7 +482,8 @@ def run_batched_jobs(args):
                            "mean_train_logloss": round(seq_loss, 6)},
             "batched": {"job_iters_per_s": round(J * it / bat_s, 2), "s": round(bat_s, 3),
                         "mean_train_logloss": round(bat_loss, 6)},
-            "speedup": round(seq_s / bat_s, 3), "prep_s": round(prep_s, 1)}
+            "speedup": round(seq_s / bat_s, 3), "prep_s": round(prep_s, 1),
+            "learner_setup_s": round(setup_s, 2), "autotuned": bool(args.autotune)}
 
 
 def run_hist_traffic(args):
@@ -488,6 +506,13 @@ def run_hist_traffic(args):
     tm = learner.last_timing()
     learner.close()
     return {"rows": n, "hist_launches": args.leaves - 1, "hist_alg_bytes": tm["hist_bytes"]}
+
+
+def _shape_dict(shape, tuned):
+    if shape is None:
+        return None
+    return {"hist_min_rows_per_cta": shape[0], "hist_ctas_per_feature_tile": shape[1], "partition_ctas": shape[2],
+            "source": "bk_learner_autotune" if tuned else "default"}
 
 
 def aggregate_ranks(ms_per_step, world):
@@ -575,6 +600,7 @@ def main():
                     help="rows of the K=10 multiclass form reported beside the headline (0: skip it)")
     ap.add_argument("--hist-traffic", action="store_true",
                     help="train one tree and print the histogram kernel's algorithmic bytes (for an ncu capture)")
+    ap.add_argument("--autotune", type=int, default=1, help="1: autotune each form's launch shape first")
     ap.add_argument("--only", choices=["multiclass", "batched"],
                     help="run only that side form and print its result (not a bench line)")
     args = ap.parse_args()

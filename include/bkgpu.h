@@ -136,6 +136,28 @@ int bk_learner_set_launch_overlap(bk_learner* learner, int32_t on);
  * tree, as the reference draws one per train call), or NULL for "every feature". */
 int bk_learner_set_feature_mask(bk_learner* learner, const uint8_t* mask);
 
+/* Launch-shape autotuner (GB300-only, no reference counterpart; results never depend on it).
+ * Times whole trees (graph form, median of `trials` after one untimed tree per shape) grown from
+ * the given gradients (as bk_learner_train takes them, all rows) over a coordinate descent of
+ * three launch parameters — the fewest rows a histogram CTA takes, histogram CTAs per 32-feature
+ * tile, partition CTAs — and keeps the fastest. Choices are cached per dataset shape class
+ * (log2 rows, feature tiles, bins per feature, quantized, num_leaves): a later learner of the same
+ * class takes the cached shape without timing. The learner's state across trees (the
+ * stochastic-rounding engine) is restored afterwards; the trial trees replace the "last tree"
+ * outputs (bk_learner_row_leaf), so call it before the first bk_learner_train. shape_out (host,
+ * 3 ints, may be NULL) receives the chosen shape. */
+int bk_learner_autotune(bk_learner* learner, const float* gradients, const float* hessians, int32_t on_device,
+                        int32_t trials, int32_t* shape_out);
+
+/* The current launch shape: {rows per histogram CTA (minimum), histogram CTAs per feature tile,
+ * partition CTAs}. */
+int bk_learner_launch_shape(bk_learner* learner, int32_t* shape_out);
+
+/* Sets the launch shape (e.g. one found by bk_learner_autotune earlier), clamped to what the
+ * dataset's rows can fill: shape[0] >= 32 rows (rounded down to a multiple of 32), shape[1] >= 1,
+ * shape[2] >= 1 (at most 1024). */
+int bk_learner_set_launch_shape(bk_learner* learner, const int32_t* shape);
+
 /* Replaces SerialTreeLearner::reset_constant_hessian (serial.rs:279). */
 int bk_learner_reset_constant_hessian(bk_learner* learner, int32_t value);
 

@@ -296,3 +296,46 @@ def test_device_prediction_replays_the_partition():
         got = score.cpu().numpy()
         assert np.array_equal(got, t.leaf_value[row_leaf])
         gpu.close()
+
+
+@pytest.mark.parametrize("shape", [(32, 1, 1), (64, 3, 7), (1024, 200, 1024), (256, 38, 304)])
+def test_launch_shapes_do_not_change_results(shape):
+    """Every launch shape grows the oracle's trees: quantized bit-exact, both partition forms."""
+    cfg = dict(num_leaves=31, use_quantized_grad=1, stochastic_rounding=1, seed=2, num_threads=2)
+    ds, z = _dataset(25000, 40, seed=21)
+    g, h, const = _grads(z, "binary", seed=22)
+    for loop_mode in (1, 0):
+        orc, gpu, _ = _learners(ds, const, loop_mode=loop_mode, **cfg)
+        gpu.set_launch_shape(shape)
+        got = gpu.launch_shape()
+        assert got[0] == max(32, shape[0] // 32 * 32) and 1 <= got[1] <= shape[1] and 1 <= got[2] <= shape[2]
+        for it in range(2):
+            ro, rg = orc.train(g, h), gpu.train(g, h)
+            _assert_records_equal(ro[0], rg[0])
+            assert np.array_equal(ro[1], rg[1])
+            assert np.array_equal(orc.row_leaf(), gpu.row_leaf())
+            g = (g * 0.9).astype(np.float32)
+        gpu.close()
+
+
+def test_autotune_keeps_parity_and_caches_by_shape():
+    """bk_learner_autotune times trial trees and restores the learner's state: the trees after it
+    equal the oracle's (which never grew the trial trees); a second learner of the same shape
+    class takes the cached shape."""
+    cfg = dict(num_leaves=31, use_quantized_grad=1, stochastic_rounding=1, seed=4, num_threads=2)
+    ds, z = _dataset(30000, 36, seed=23)
+    g, h, const = _grads(z, "l2", seed=24)
+    orc, gpu, c = _learners(ds, const, **cfg)
+    shape = gpu.autotune(g, h, trials=1)
+    assert shape == gpu.launch_shape()
+    for it in range(2):
+        ro, rg = orc.train(g, h), gpu.train(g, h)
+        _assert_records_equal(ro[0], rg[0])
+        assert np.array_equal(ro[1], rg[1])
+        assert np.array_equal(orc.row_leaf(), gpu.row_leaf())
+        g = (g * 0.9).astype(np.float32)
+    from lgbm_gb300 import GpuTreeLearner
+    other = GpuTreeLearner(ds, c)
+    assert other.autotune(g, h, trials=1) == shape
+    gpu.close()
+    other.close()
