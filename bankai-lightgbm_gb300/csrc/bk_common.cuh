@@ -140,11 +140,14 @@ struct Job {
 
 // The jobs of one grow-loop launch, passed by value: the kernel parameters sit in the constant
 // bank, so a kernel reaches its job's buffers without a global-memory round trip after it starts.
-// A learner with more jobs launches each grow-loop kernel once per group.
-constexpr int kJobsPerLaunch = 4;
+// Sixteen jobs (about 4 KB of parameters) cover every class tree of a multiclass iteration of up
+// to 16 classes in one launch per kernel; a learner with more jobs launches each grow-loop kernel
+// once per group of sixteen.
+constexpr int kJobsPerLaunch = 16;
 struct JobTable {
   Job job[kJobsPerLaunch];
 };
+static_assert(sizeof(JobTable) <= 4096, "the job table of a grow-loop launch stays within 4 KB of parameters");
 
 // Calls f(table, jobs in it) for each group of up to kJobsPerLaunch consecutive host-side jobs.
 template <typename F>
