@@ -358,6 +358,10 @@ def run_multiclass(args):
         score = (init.expand(K, n)).contiguous()
         gbuf, hbuf = learner.gradient_buffers()
         torch.cuda.synchronize()
+        if args.autotune:
+            learner.objective_gradients(2, score.data_ptr(), label.data_ptr())
+            learner.autotune(gbuf, hbuf, on_device=True, trials=2)
+        shape = learner.launch_shape()
         trees, total_ms = [], 0.0
         for it in range(warmup + steps):
             ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -385,7 +389,7 @@ def run_multiclass(args):
         learner.close()
         return {"iters_per_s": round(1000.0 * steps / total_ms, 3), "ms_per_iter": round(total_ms / steps, 3),
                 "train_logloss": round(train_loss, 6), "heldout_logloss": round(ho_loss, 6),
-                "iterations": len(trees)}
+                "iterations": len(trees), "launch_shape": _shape_dict(shape, args.autotune)}
 
     q = form(True, 1, args.steps, args.warmup)
     p = form(False, 0, args.steps, args.warmup)
