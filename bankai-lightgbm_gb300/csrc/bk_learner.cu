@@ -366,6 +366,11 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
       d.real = features[f].real_feature;
       d.len = d.num_bin - d.offset;
       d.penalty = features[f].penalty;
+      if (features[f].bin_type != 0) {
+        set_error("feature %d: categorical features are not supported by this learner yet", f);
+        delete L;
+        return -1;
+      }
       if (d.num_bin < 1 || d.gbins > 256 || d.missing < 0 || d.missing > 2 || d.mfb < 0 || d.mfb >= d.num_bin ||
           d.default_bin < 0 || d.default_bin >= d.num_bin) {
         set_error("feature %d: unsupported bin mapper (num_bin %d, missing %d, mfb %d, default %d)", f, d.num_bin,

@@ -39,6 +39,10 @@ def _declare(lib):
     lib.bk_find_bin_numerical.argtypes = [P, i64, i64, i32, i32, i32, i32, i32, i32, P, i32, P, P]
     lib.bk_values_to_group_bins.restype = None
     lib.bk_values_to_group_bins.argtypes = [P, i64, i64, P, i32, i32, i32, P]
+    lib.bk_find_bin_categorical.restype = i32
+    lib.bk_find_bin_categorical.argtypes = [P, i64, i64, i32, i32, i32, i32, i32, i32, P, i32, P, P]
+    lib.bk_values_to_group_bins_categorical.restype = None
+    lib.bk_values_to_group_bins_categorical.argtypes = [P, i64, i64, P, i32, i32, P]
     if hasattr(lib, "bk_last_error"):
         lib.bk_last_error.restype = c.c_char_p
         lib.bk_last_error.argtypes = []
@@ -81,7 +85,8 @@ _GPU_SIGNATURES = [
 
 # every symbol include/bkgpu.h declares
 EXPORTED = [name for name, _, _ in _GPU_SIGNATURES] + ["bk_last_error", "bk_find_bin_numerical",
-                                                        "bk_values_to_group_bins"]
+                                                        "bk_values_to_group_bins", "bk_find_bin_categorical",
+                                                        "bk_values_to_group_bins_categorical"]
 
 
 def last_error() -> str:

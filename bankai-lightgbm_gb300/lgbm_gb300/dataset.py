@@ -14,7 +14,7 @@ data so the learner can be driven without the Rust host:
   (dense data never bundles: io/dataset.rs:171-177), stored bins written by
   ``bk_values_to_group_bins`` (io/dataset.rs:633-685).
 
-Only numerical features are supported.
+Numerical and categorical features (``categorical=`` column list) are supported.
 """
 from concurrent.futures import ThreadPoolExecutor
 import ctypes
@@ -26,6 +26,7 @@ from . import _lib
 
 K_ZERO_THRESHOLD = float(np.float32(1e-35))
 MISSING_NONE, MISSING_ZERO, MISSING_NAN = 0, 1, 2
+BIN_NUMERICAL, BIN_CATEGORICAL = 0, 1
 
 
 class _Random:
@@ -72,7 +73,11 @@ class _Random:
 
 class FeatureInfo:
     __slots__ = ("real", "num_bin", "missing_type", "default_bin", "most_freq_bin", "upper_bounds", "penalty",
-                 "min_val", "max_val", "sparse_rate")
+                 "min_val", "max_val", "sparse_rate", "bin_type", "bin_to_category")
+
+    def __init__(self):
+        self.bin_type = BIN_NUMERICAL
+        self.bin_to_category = None
 
     @property
     def offset(self):
@@ -83,12 +88,20 @@ class FeatureInfo:
         """Stored bins of the feature's group: bin 0 holds the most-frequent-bin rows."""
         return 1 + self.num_bin - self.offset
 
+    @property
+    def categorical(self):
+        return self.bin_type == BIN_CATEGORICAL
+
     def bin_to_value(self, b):
+        """BinMapper::bin_to_value (io/bin.rs:593-599): the bound of a numerical bin, the category
+        code of a categorical one."""
+        if self.categorical:
+            return float(self.bin_to_category[b])
         return float(self.upper_bounds[b])
 
 
 class BinnedDataset:
-    """A dense numerical dataset in the learner's input form.
+    """A dense dataset in the learner's input form.
 
     ``bins``: uint8 array ``[num_features, num_data]`` of stored group bins (column-major).
     ``features``: per inner feature, its ``FeatureInfo``.
@@ -115,27 +128,20 @@ class BinnedDataset:
     @classmethod
     def from_dense(cls, X, max_bin=255, min_data_in_bin=3, min_data_in_leaf=20, bin_construct_sample_cnt=200000,
                    data_random_seed=1, use_missing=True, zero_as_missing=False, feature_pre_filter=True,
-                   threads=8):
+                   threads=8, categorical=()):
+        """``categorical``: the column indices binned as categories (io/dataset.rs from_dense's
+        categorical list); the others are numerical."""
         if max_bin > 255:
             raise ValueError("max_bin above 255 needs 16-bit stored bins, which this learner does not take")
         X = np.asarray(X)
         n, ncol = X.shape
-        lib = _lib.load()
         rows = _Random(data_random_seed).sample(n, min(n, bin_construct_sample_cnt))
         features = _find_mappers(lambda col: np.asarray(X[rows, col], dtype=np.float64), ncol, n, len(rows),
                                  max_bin, min_data_in_bin, min_data_in_leaf, use_missing, zero_as_missing,
-                                 feature_pre_filter, threads)
-        bins = np.zeros((len(features), n), dtype=np.uint8)
-
-        def fill(j):
-            fi = features[j]
-            col = np.ascontiguousarray(X[:, fi.real], dtype=np.float64)
-            lib.bk_values_to_group_bins(col.ctypes.data, n, 1, fi.upper_bounds.ctypes.data, fi.num_bin,
-                                        fi.missing_type, fi.most_freq_bin, bins[j].ctypes.data)
-
-        with ThreadPoolExecutor(max_workers=threads) as ex:
-            list(ex.map(fill, range(len(features))))
-        return cls(bins, features, ncol)
+                                 feature_pre_filter, threads, categorical)
+        ds = cls(None, features, ncol)
+        ds.bins = ds.bin_like(X, threads=threads)
+        return ds
 
     def bin_like(self, X, threads=8):
         """Stored bins of new rows with this dataset's bin mappers (held-out / validation data,
@@ -148,8 +154,12 @@ class BinnedDataset:
         def fill(j):
             fi = self.features[j]
             col = np.ascontiguousarray(X[:, fi.real], dtype=np.float64)
-            lib.bk_values_to_group_bins(col.ctypes.data, n, 1, fi.upper_bounds.ctypes.data, fi.num_bin,
-                                        fi.missing_type, fi.most_freq_bin, bins[j].ctypes.data)
+            if fi.categorical:
+                lib.bk_values_to_group_bins_categorical(col.ctypes.data, n, 1, fi.bin_to_category.ctypes.data,
+                                                        fi.num_bin, fi.most_freq_bin, bins[j].ctypes.data)
+            else:
+                lib.bk_values_to_group_bins(col.ctypes.data, n, 1, fi.upper_bounds.ctypes.data, fi.num_bin,
+                                            fi.missing_type, fi.most_freq_bin, bins[j].ctypes.data)
 
         with ThreadPoolExecutor(max_workers=threads) as ex:
             list(ex.map(fill, range(self.num_features)))
@@ -173,7 +183,7 @@ class BinnedDataset:
         rows = _Random(data_random_seed).sample(n, min(n, bin_construct_sample_cnt))
         sample = X[torch.as_tensor(rows, device=X.device)].double().cpu().numpy()
         features = _find_mappers(lambda col: sample[:, col], ncol, n, len(rows), max_bin, min_data_in_bin,
-                                 min_data_in_leaf, use_missing, zero_as_missing, feature_pre_filter, threads)
+                                 min_data_in_leaf, use_missing, zero_as_missing, feature_pre_filter, threads, ())
         ds = cls(None, features, ncol)
         ds.bins = ds.bin_like_device(X)
         return ds
@@ -184,6 +194,8 @@ class BinnedDataset:
         import torch
         X = X.contiguous()
         n, ncol = X.shape
+        if any(fi.categorical for fi in self.features):
+            raise ValueError("device binning takes numerical features only; bin categorical data with bin_like")
         out = torch.empty((len(self.features), n), dtype=torch.uint8, device=X.device)
         if not self.features:
             return out
@@ -204,33 +216,46 @@ class BinnedDataset:
         """The ``bk_feature`` records of include/bkgpu.h, as a numpy structured array."""
         arr = np.zeros(self.num_features, dtype=FEATURE_DTYPE)
         for j, fi in enumerate(self.features):
-            arr[j] = (fi.num_bin, fi.missing_type, fi.default_bin, fi.most_freq_bin, fi.penalty, fi.real, 0)
+            arr[j] = (fi.num_bin, fi.missing_type, fi.default_bin, fi.most_freq_bin, fi.penalty, fi.real, fi.bin_type)
         return arr
 
 
 def _find_mappers(sample_col, ncol, n, sample_cnt, max_bin, min_data_in_bin, min_data_in_leaf, use_missing,
-                  zero_as_missing, feature_pre_filter, threads):
+                  zero_as_missing, feature_pre_filter, threads, categorical=()):
     """``BinMapper::find_bin`` (io/bin.rs:342-554) for every column over the sampled rows
-    (``sample_col(col)``: the column's sampled values, f64), dropping trivial features
-    (io/dataset.rs:389-393)."""
+    (``sample_col(col)``: the column's sampled values, f64), categorical for the columns in
+    ``categorical``, dropping trivial features (io/dataset.rs:389-393)."""
     lib = _lib.load()
     filter_cnt = int((float(min_data_in_leaf) * sample_cnt) / float(n))
     cap = 1024
+    cat_cols = set(int(c) for c in categorical)
 
     def find(col):
         vals = np.asarray(sample_col(col), dtype=np.float64)
         keep = (np.abs(vals) > K_ZERO_THRESHOLD) | np.isnan(vals)
         vals = np.ascontiguousarray(vals[keep])
-        ub = np.zeros(cap, dtype=np.float64)
         meta = np.zeros(4, dtype=np.int32)
         dmeta = np.zeros(3, dtype=np.float64)
-        nb = lib.bk_find_bin_numerical(vals.ctypes.data, len(vals), sample_cnt, max_bin, min_data_in_bin,
-                                       filter_cnt, int(feature_pre_filter), int(use_missing),
-                                       int(zero_as_missing), ub.ctypes.data, cap, meta.ctypes.data,
-                                       dmeta.ctypes.data)
-        if nb < 0:
-            raise RuntimeError("bin mapper capacity exceeded")
         fi = FeatureInfo()
+        if col in cat_cols:
+            b2c = np.zeros(cap, dtype=np.int32)
+            nb = lib.bk_find_bin_categorical(vals.ctypes.data, len(vals), sample_cnt, max_bin, min_data_in_bin,
+                                             filter_cnt, int(feature_pre_filter), int(use_missing),
+                                             int(zero_as_missing), b2c.ctypes.data, cap, meta.ctypes.data,
+                                             dmeta.ctypes.data)
+            if nb < 0:
+                raise RuntimeError("bin mapper capacity exceeded")
+            fi.bin_type = BIN_CATEGORICAL
+            fi.bin_to_category = b2c[:nb].copy()
+            ub = np.zeros(0)
+        else:
+            ub = np.zeros(cap, dtype=np.float64)
+            nb = lib.bk_find_bin_numerical(vals.ctypes.data, len(vals), sample_cnt, max_bin, min_data_in_bin,
+                                           filter_cnt, int(feature_pre_filter), int(use_missing),
+                                           int(zero_as_missing), ub.ctypes.data, cap, meta.ctypes.data,
+                                           dmeta.ctypes.data)
+            if nb < 0:
+                raise RuntimeError("bin mapper capacity exceeded")
         fi.real = col
         fi.num_bin = int(nb)
         fi.missing_type = int(meta[0])
@@ -248,4 +273,4 @@ def _find_mappers(sample_col, ncol, n, sample_cnt, max_bin, min_data_in_bin, min
 
 FEATURE_DTYPE = np.dtype([("num_bin", np.int32), ("missing_type", np.int32), ("default_bin", np.int32),
                           ("most_freq_bin", np.int32), ("penalty", np.float64), ("real_feature", np.int32),
-                          ("_pad", np.int32)], align=True)
+                          ("bin_type", np.int32)], align=True)

@@ -1,13 +1,32 @@
 """Host-side tree assembly from the learner's split records.
 
 The learner returns, per split, the arguments of ``Tree::split_numerical``
-(crates/lgbm-core/src/tree.rs:361-403); this module applies them exactly like the reference's
-``Tree`` (``split_common`` tree.rs:310-357, ``apply_shrinkage`` :446-463, ``add_bias`` :465-478)
-so the result can be compared with, or written as, a LightGBM model tree.
+(crates/lgbm-core/src/tree.rs:361-403) or ``Tree::split_categorical`` (:405-443); this module
+applies them exactly like the reference's ``Tree`` (``split_common`` tree.rs:310-357,
+``apply_shrinkage`` :446-463, ``add_bias`` :465-478) so the result can be compared with, or
+written as, a LightGBM model tree.
 """
 import numpy as np
 
 K_ZERO_THRESHOLD = float(np.float32(1e-35))
+K_CATEGORICAL_MASK = 1  # tree.rs decision_type bit 0
+
+
+def construct_bitset(vals):
+    """utils/common.rs:221-231: bit v of word v / 32 for every value; as many words as the largest
+    value needs."""
+    words = []
+    for v in vals:
+        i1 = v // 32
+        if len(words) < i1 + 1:
+            words.extend([0] * (i1 + 1 - len(words)))
+        words[i1] |= 1 << (v % 32)
+    return words
+
+
+def bits_to_bins(bits):
+    """The set bits of an 8-word bin bitset, ascending."""
+    return [b for b in range(256) if (int(bits[b // 32]) >> (b % 32)) & 1]
 
 SPLIT_DTYPE = np.dtype([
     ("leaf", np.int32), ("right_leaf", np.int32), ("inner_feature", np.int32), ("real_feature", np.int32),
@@ -15,7 +34,7 @@ SPLIT_DTYPE = np.dtype([
     ("right_count", np.int32), ("left_output", np.float64), ("right_output", np.float64),
     ("left_sum_gradient", np.float64), ("left_sum_hessian", np.float64), ("right_sum_gradient", np.float64),
     ("right_sum_hessian", np.float64), ("gain", np.float64), ("left_int_sum", np.int64),
-    ("right_int_sum", np.int64),
+    ("right_int_sum", np.int64), ("categorical", np.int32), ("_pad", np.int32), ("cat_bins", np.uint32, (8,)),
 ], align=True)
 
 
@@ -44,6 +63,12 @@ class Tree:
         self.internal_weight = np.zeros(n_int, np.float64)
         self.internal_count = np.zeros(n_int, np.int32)
         self.shrinkage = 1.0
+        # categorical splits (tree.rs:405-443): per node its category bitset range, and the bins
+        # that go left (for replays on stored bins)
+        self.num_cat = 0
+        self.cat_boundaries = [0]
+        self.cat_threshold = []
+        self.cat_bin_bits = {}
 
     @classmethod
     def from_records(cls, max_leaves, records, leaf_values, root_output, features, min_gain_to_split=0.0):
@@ -80,11 +105,23 @@ class Tree:
             t.leaf_count[nl] = r["right_count"]
             t.leaf_depth[nl] = t.leaf_depth[leaf] + 1
             t.leaf_depth[leaf] += 1
-            dt = 2 if r["default_left"] else 0
-            dt = (dt & 3) | (int(r["missing_type"]) << 2)
-            t.decision_type[node] = dt
-            t.threshold_in_bin[node] = r["threshold"]
-            t.threshold[node] = fi.bin_to_value(int(r["threshold"]))
+            if int(r["categorical"]):
+                # the tree keeps the categories of the left bins; the partition used the bins
+                bins = bits_to_bins(r["cat_bins"])
+                bitset = construct_bitset([int(fi.bin_to_category[b]) for b in bins])
+                t.decision_type[node] = K_CATEGORICAL_MASK | (int(r["missing_type"]) << 2)
+                t.threshold_in_bin[node] = t.num_cat
+                t.threshold[node] = float(t.num_cat)
+                t.num_cat += 1
+                t.cat_boundaries.append(t.cat_boundaries[-1] + len(bitset))
+                t.cat_threshold.extend(bitset)
+                t.cat_bin_bits[node] = np.asarray(r["cat_bins"], dtype=np.uint32).copy()
+            else:
+                dt = 2 if r["default_left"] else 0
+                dt = (dt & 3) | (int(r["missing_type"]) << 2)
+                t.decision_type[node] = dt
+                t.threshold_in_bin[node] = r["threshold"]
+                t.threshold[node] = fi.bin_to_value(int(r["threshold"]))
             t.num_leaves += 1
         # the learner's final leaf outputs (equal to the split outputs unless renewed)
         for i in range(t.num_leaves):

@@ -33,29 +33,40 @@ typedef struct {
   int32_t most_freq_bin;
   double penalty;
   int32_t real_feature;
-  int32_t _pad;
+  int32_t bin_type; /* 0 numerical, 1 categorical (meta.rs BinType) */
 } bk_feature;
 
 /* The Config fields the tree learner reads (config/auto.rs). `num_threads` is the reference's
  * thread count, used only to seed stochastic-rounding noise per block exactly as the reference
  * does (gradient_discretizer/mod.rs:87-106). `fused_madd` selects the rounding of the
- * reference's `madd` (utils/common.rs:207-216): 1 = fused, as the aarch64 build; 0 = unfused. */
+ * reference's `madd` (utils/common.rs:207-216): 1 = fused, as the aarch64 build; 0 = unfused.
+ * The last five fields are the categorical search's CatParams (treelearner/feature_histogram.rs:
+ * 1146-1163; defaults 4, 32, 10.0, 10.0, 100 in config/auto.rs:214-218). */
 typedef struct {
   int32_t num_leaves, max_depth, min_data_in_leaf, _pad0;
   double min_sum_hessian_in_leaf, lambda_l1, lambda_l2, max_delta_step, path_smooth, min_gain_to_split;
   int32_t use_quantized_grad, num_grad_quant_bins, quant_train_renew_leaf, stochastic_rounding;
   int32_t seed, num_threads, fused_madd, is_constant_hessian;
+  int32_t max_cat_to_onehot, max_cat_threshold;
+  double cat_smooth, cat_l2;
+  int32_t min_data_per_group, _pad1;
 } bk_config;
 
-/* One numerical split: the arguments of Tree::split_numerical (tree.rs:361-403) as computed by
- * SerialTreeLearner::split (serial.rs:1685-1876). Counts are the partition's actual counts. */
+/* One split: the arguments of Tree::split_numerical (tree.rs:361-403) or, for a categorical
+ * feature, Tree::split_categorical (tree.rs:405-443), as computed by SerialTreeLearner::split
+ * (serial.rs:1685-1876). Counts are the partition's actual counts. */
 typedef struct {
   int32_t leaf, right_leaf, inner_feature, real_feature;
-  uint32_t threshold; /* bin; the host maps it with BinMapper::bin_to_value */
+  uint32_t threshold; /* numerical: bin; the host maps it with BinMapper::bin_to_value */
   int32_t default_left, missing_type, left_count, right_count;
   double left_output, right_output, left_sum_gradient, left_sum_hessian, right_sum_gradient, right_sum_hessian;
   double gain; /* without min_gain_to_split; the tree stores (gain + min_gain_to_split) as f32 */
   int64_t left_int_sum, right_int_sum; /* quantized path: (grad << 32) | hess; 0 otherwise */
+  int32_t categorical; /* 1: categorical split (serial.rs:1724-1759) */
+  int32_t _pad;
+  uint32_t cat_bins[8]; /* categorical: bitset of the bins that go left (bit b = bin b, construct_bitset of
+                         * cat_threshold); the host maps the bins to categories with bin_to_value and builds
+                         * the tree's category bitset */
 } bk_split;
 
 typedef struct bk_learner bk_learner;
@@ -237,6 +248,18 @@ int32_t bk_find_bin_numerical(double* values, int64_t num_values, int64_t total_
 /* Stored group bins of one column (io/dataset.rs:633-685 with BinMapper::value_to_bin). */
 void bk_values_to_group_bins(const double* col, int64_t n, int64_t stride, const double* upper_bounds,
                              int32_t num_bin, int32_t missing_type, int32_t most_freq_bin, uint8_t* out);
+
+/* BinMapper::find_bin for a categorical feature (io/bin.rs:459-554): bin_to_category receives the
+ * category code of every bin (bin 0 = -1, "other / missing"). */
+int32_t bk_find_bin_categorical(double* values, int64_t num_values, int64_t total_sample_cnt, int32_t max_bin,
+                                int32_t min_data_in_bin, int32_t min_split_data, int32_t pre_filter,
+                                int32_t use_missing, int32_t zero_as_missing, int32_t* bin_to_category, int32_t cap,
+                                int32_t* meta_out, double* dmeta_out);
+
+/* Stored group bins of one categorical column (io/dataset.rs:633-685 with the categorical
+ * BinMapper::value_to_bin, io/bin.rs:558-589). */
+void bk_values_to_group_bins_categorical(const double* col, int64_t n, int64_t stride, const int32_t* bin_to_category,
+                                         int32_t num_bin, int32_t most_freq_bin, uint8_t* out);
 
 #ifdef __cplusplus
 }

@@ -57,6 +57,7 @@ def load():
         lib.orc_discretize.argtypes = [P, P, i64, i32, i32, i32, u32, i32, i32, i32, P, P]
         lib.orc_mt19937.argtypes = [u32, i32, u32, i64, P]
         lib.orc_route_table.argtypes = [P, u32, i32, P]
+        lib.orc_route_table_cat.argtypes = [P, P, P]
         lib.orc_find_best_threshold_int.restype = i32
         lib.orc_find_best_threshold_int.argtypes = [P, P, P, P, i64, i64, ctypes.c_double, ctypes.c_double, i32,
                                                     ctypes.c_double, P]
@@ -323,8 +324,12 @@ def replay_leaves(tree, ds, rows):
     luts = np.zeros((max(ni, 1), 256), dtype=np.uint8)
     for node in range(ni):
         f = int(tree.split_feature_inner[node])
-        lib.orc_route_table(feats[f:f + 1].ctypes.data, int(tree.threshold_in_bin[node]),
-                            int((int(tree.decision_type[node]) >> 1) & 1), luts[node].ctypes.data)
+        if node in tree.cat_bin_bits:
+            bits = np.ascontiguousarray(tree.cat_bin_bits[node], dtype=np.uint32)
+            lib.orc_route_table_cat(feats[f:f + 1].ctypes.data, bits.ctypes.data, luts[node].ctypes.data)
+        else:
+            lib.orc_route_table(feats[f:f + 1].ctypes.data, int(tree.threshold_in_bin[node]),
+                                int((int(tree.decision_type[node]) >> 1) & 1), luts[node].ctypes.data)
     rows = np.asarray(rows, dtype=np.int64)
     node = np.zeros(len(rows), dtype=np.int64)
     leaf = np.full(len(rows), -1 if ni > 0 else 0, dtype=np.int64)
@@ -435,6 +440,13 @@ def compare_tree(t: Tree, ref: dict, leaf_rtol=1e-12):
             bad.append("internal_value")
         if not np.allclose(floats("internal_weight"), t.internal_weight[:ni], rtol=1e-5):
             bad.append("internal_weight")
+    if int(ref.get("num_cat", "0")) != t.num_cat:
+        bad.append("num_cat")
+    elif t.num_cat > 0:
+        if [int(x) for x in ref["cat_boundaries"].split()] != t.cat_boundaries:
+            bad.append("cat_boundaries")
+        if [int(x) for x in ref["cat_threshold"].split()] != t.cat_threshold:
+            bad.append("cat_threshold")
     if not np.array_equal(ints("leaf_count"), t.leaf_count[:nl].astype(np.int64)):
         bad.append("leaf_count")
     if not np.allclose(floats("leaf_value"), t.leaf_value[:nl], rtol=leaf_rtol, atol=0):

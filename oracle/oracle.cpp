@@ -216,12 +216,16 @@ struct Params {
   double min_hess = 1e-3;
   double min_gain = 0;
   bool fused = false;
+  // CatParams (feature_histogram.rs:1146-1163), config/auto.rs:214-218 defaults
+  double cat_smooth = 10.0, cat_l2 = 10.0;
+  int32_t max_cat_threshold = 32, max_cat_to_onehot = 4, min_data_per_group = 100;
 };
 
 struct FeatureMeta {
   int32_t num_bin, missing, offset, default_bin, mfb;
   double penalty;
   int32_t real;
+  int32_t categorical = 0;  // BinType::Categorical
 };
 
 struct SplitInfo {
@@ -232,6 +236,7 @@ struct SplitInfo {
   double lsg = 0, lsh = 0, rsg = 0, rsh = 0;
   int64_t lint = 0, rint = 0;
   bool default_left = true;
+  std::vector<uint32_t> cat_bins;  // categorical: the bins that go left (cat_threshold)
   // split_info.rs:104-121
   bool better_than(const SplitInfo& o) const {
     double a = gain, b = o.gain;
@@ -574,6 +579,249 @@ static bool find_best_threshold_numerical_int(const int64_t* hg, const int64_t* 
   return sp;
 }
 
+// ---------------------------------------------------------------------------------------------
+// Categorical threshold search (feature_histogram.rs:1328-1886), no extra-trees draw, no
+// monotone constraints: one-hot (one category against the rest) when num_bin <= max_cat_to_onehot,
+// otherwise the categories with enough data sorted by grad / (hess + cat_smooth) and scanned from
+// both ends for at most max_cat_threshold categories, with lambda_l2 + cat_l2.
+// ---------------------------------------------------------------------------------------------
+
+// min_gain_shift of a categorical search (feature_histogram.rs:1356-1386): with path smoothing
+// the parent output is the leaf output, otherwise the unsmoothed leaf gain.
+static double cat_gain_shift(const Flags& F, const Params& p, double sum_g, double sum_h, int32_t num_data,
+                             double parent) {
+  if (F.sm) return leaf_gain_given_output(F.l1, sum_g, sum_h, p, parent);
+  Flags F0{F.l1, F.mx, false};
+  return leaf_gain(F0, sum_g, sum_h, p, num_data, 0.0);
+}
+
+// The stable ascending order of `idx` by key (Rust's stable sort_by with partial_cmp).
+static void stable_sort_by_key(std::vector<int32_t>& idx, const std::vector<double>& key) {
+  std::stable_sort(idx.begin(), idx.end(), [&](int32_t a, int32_t b) { return key[(size_t)a] < key[(size_t)b]; });
+}
+
+// Float form (feature_histogram.rs:1328-1598). hist: [g, h] per slice index.
+static bool find_best_threshold_categorical(const double* hist, const FeatureMeta& m, const Params& p, double sum_g,
+                                            double sum_h_in, int32_t num_data, double parent, SplitInfo* out) {
+  const double sum_h = sum_h_in + 2.0 * EPS;
+  out->default_left = false;
+  out->gain = K_MIN_SCORE;
+  Flags F{p.l1 > 0.0, p.max_delta > 0.0, p.smooth > EPS};
+  const double mgs = cat_gain_shift(F, p, sum_g, sum_h, num_data, parent) + p.min_gain;
+  const int32_t offset = m.offset, bin_start = 1 - offset, bin_end = m.num_bin - offset;
+  auto grad = [&](int32_t t) { return hist[2 * t]; };
+  auto hess = [&](int32_t t) { return hist[2 * t + 1]; };
+  const double cnt_factor = (double)num_data / sum_h;
+  const bool onehot = m.num_bin <= p.max_cat_to_onehot;
+  Params pl = p;
+  bool sp = false;
+  double best_gain = K_MIN_SCORE, best_lg = 0.0, best_lh = 0.0;
+  int32_t best_t = -1, best_dir = 1, best_lc = 0, used_bin = -1;
+  std::vector<int32_t> sorted;
+  if (onehot) {
+    for (int32_t t = bin_start; t < bin_end; ++t) {
+      const double g = grad(t), h = hess(t);
+      const int32_t cnt = round_int(h * cnt_factor);
+      if (cnt < p.min_data || h < p.min_hess) continue;
+      const int32_t other_cnt = num_data - cnt;
+      if (other_cnt < p.min_data) continue;
+      const double other_h = sum_h - h - EPS;
+      if (other_h < p.min_hess) continue;
+      const double other_g = sum_g - g;
+      const double gain = gains(F, pl, other_g, other_h, g, h + EPS, other_cnt, cnt, parent);
+      if (!(gain > mgs)) continue;
+      sp = true;
+      if (gain > best_gain) {
+        best_t = t;
+        best_lg = g;
+        best_lh = h + EPS;
+        best_lc = cnt;
+        best_gain = gain;
+      }
+    }
+  } else {
+    std::vector<double> key((size_t)std::max(bin_end, 0), 0.0);
+    for (int32_t i = bin_start; i < bin_end; ++i) {
+      if ((double)round_int(hess(i) * cnt_factor) >= p.cat_smooth) sorted.push_back(i);
+      key[(size_t)i] = grad(i) / (hess(i) + p.cat_smooth);
+    }
+    used_bin = (int32_t)sorted.size();
+    pl.l2 = p.l2 + p.cat_l2;
+    stable_sort_by_key(sorted, key);
+    const int32_t max_num_cat = std::min(p.max_cat_threshold, (used_bin + 1) / 2);
+    for (int dir = 1, start = 0, pass = 0; pass < 2; ++pass, dir = -1, start = used_bin - 1) {
+      int32_t pos = start, cnt_group = 0, left_cnt = 0;
+      double lg = 0.0, lh = EPS;
+      for (int32_t i = 0; i < used_bin && i < max_num_cat; ++i) {
+        const int32_t t = sorted[(size_t)pos];
+        pos += dir;
+        const double g = grad(t), h = hess(t);
+        const int32_t cnt = round_int(h * cnt_factor);
+        lg += g;
+        lh += h;
+        left_cnt += cnt;
+        cnt_group += cnt;
+        if (left_cnt < p.min_data || lh < p.min_hess) continue;
+        const int32_t right_cnt = num_data - left_cnt;
+        if (right_cnt < p.min_data || right_cnt < p.min_data_per_group) break;
+        const double rh = sum_h - lh;
+        if (rh < p.min_hess) break;
+        if (cnt_group < p.min_data_per_group) continue;
+        cnt_group = 0;
+        const double rg = sum_g - lg;
+        const double gain = gains(F, pl, lg, lh, rg, rh, left_cnt, right_cnt, parent);
+        if (gain > mgs) {
+          sp = true;
+          if (gain > best_gain) {
+            best_lc = left_cnt;
+            best_lg = lg;
+            best_lh = lh;
+            best_t = i;
+            best_gain = gain;
+            best_dir = dir;
+          }
+        }
+      }
+    }
+  }
+  if (sp) {
+    out->left_output = leaf_output(F, best_lg, best_lh, pl, best_lc, parent);
+    out->left_count = best_lc;
+    out->lsg = best_lg;
+    out->lsh = best_lh - EPS;
+    out->right_output = leaf_output(F, sum_g - best_lg, sum_h - best_lh, pl, num_data - best_lc, parent);
+    out->right_count = num_data - best_lc;
+    out->rsg = sum_g - best_lg;
+    out->rsh = sum_h - best_lh - EPS;
+    out->gain = best_gain - mgs;
+    out->cat_bins.clear();
+    if (onehot) {
+      out->cat_bins.push_back((uint32_t)(best_t + offset));
+    } else {
+      for (int32_t i = 0; i <= best_t; ++i) {
+        const int32_t pos = best_dir == 1 ? i : used_bin - 1 - i;
+        out->cat_bins.push_back((uint32_t)(sorted[(size_t)pos] + offset));
+      }
+    }
+  }
+  out->gain *= m.penalty;
+  return sp;
+}
+
+// Integer form (feature_histogram.rs:1600-1886): exact integer sums scaled once; no kEpsilon.
+static bool find_best_threshold_categorical_int(const int64_t* hg, const int64_t* hh, const FeatureMeta& m,
+                                                const Params& p, int64_t tg, int64_t th, double gs, double hs,
+                                                int32_t num_data, double parent, SplitInfo* out) {
+  const double sum_g = (double)tg * gs, sum_h = (double)th * hs;
+  out->default_left = false;
+  out->gain = K_MIN_SCORE;
+  Flags F{p.l1 > 0.0, p.max_delta > 0.0, p.smooth > EPS};
+  const double mgs = cat_gain_shift(F, p, sum_g, sum_h, num_data, parent) + p.min_gain;
+  const int32_t offset = m.offset, bin_start = 1 - offset, bin_end = m.num_bin - offset;
+  const double cnt_factor = (double)num_data / (double)th;
+  const bool onehot = m.num_bin <= p.max_cat_to_onehot;
+  Params pl = p;
+  bool sp = false;
+  double best_gain = K_MIN_SCORE;
+  int64_t best_ig = 0, best_ih = 0;
+  int32_t best_t = -1, best_dir = 1, used_bin = -1;
+  std::vector<int32_t> sorted;
+  if (onehot) {
+    for (int32_t t = bin_start; t < bin_end; ++t) {
+      const int64_t ig = hg[t], ih = hh[t];
+      const double h = (double)ih * hs;
+      const int32_t cnt = round_int((double)ih * cnt_factor);
+      if (cnt < p.min_data || h < p.min_hess) continue;
+      const int32_t other_cnt = num_data - cnt;
+      if (other_cnt < p.min_data) continue;
+      const double other_h = (double)(th - ih) * hs;
+      if (other_h < p.min_hess) continue;
+      const double g = (double)ig * gs;
+      const double other_g = (double)(tg - ig) * gs;
+      const double gain = gains(F, pl, other_g, other_h, g, h, other_cnt, cnt, parent);
+      if (!(gain > mgs)) continue;
+      sp = true;
+      if (gain > best_gain) {
+        best_t = t;
+        best_ig = ig;
+        best_ih = ih;
+        best_gain = gain;
+      }
+    }
+  } else {
+    std::vector<double> key((size_t)std::max(bin_end, 0), 0.0);
+    for (int32_t i = bin_start; i < bin_end; ++i) {
+      if ((double)round_int((double)hh[i] * cnt_factor) >= p.cat_smooth) sorted.push_back(i);
+      key[(size_t)i] = ((double)hg[i] * gs) / ((double)hh[i] * hs + p.cat_smooth);
+    }
+    used_bin = (int32_t)sorted.size();
+    pl.l2 = p.l2 + p.cat_l2;
+    stable_sort_by_key(sorted, key);
+    const int32_t max_num_cat = std::min(p.max_cat_threshold, (used_bin + 1) / 2);
+    for (int dir = 1, start = 0, pass = 0; pass < 2; ++pass, dir = -1, start = used_bin - 1) {
+      int32_t pos = start, cnt_group = 0, left_cnt = 0;
+      int64_t lig = 0, lih = 0;
+      for (int32_t i = 0; i < used_bin && i < max_num_cat; ++i) {
+        const int32_t t = sorted[(size_t)pos];
+        pos += dir;
+        const int32_t cnt = round_int((double)hh[t] * cnt_factor);
+        lig += hg[t];
+        lih += hh[t];
+        left_cnt += cnt;
+        cnt_group += cnt;
+        const double lh = (double)lih * hs;
+        if (left_cnt < p.min_data || lh < p.min_hess) continue;
+        const int32_t right_cnt = num_data - left_cnt;
+        if (right_cnt < p.min_data || right_cnt < p.min_data_per_group) break;
+        const double rh = (double)(th - lih) * hs;
+        if (rh < p.min_hess) break;
+        if (cnt_group < p.min_data_per_group) continue;
+        cnt_group = 0;
+        const double lg = (double)lig * gs, rg = (double)(tg - lig) * gs;
+        const double gain = gains(F, pl, lg, lh, rg, rh, left_cnt, right_cnt, parent);
+        if (gain > mgs) {
+          sp = true;
+          if (gain > best_gain) {
+            best_ig = lig;
+            best_ih = lih;
+            best_t = i;
+            best_gain = gain;
+            best_dir = dir;
+          }
+        }
+      }
+    }
+  }
+  if (sp) {
+    const double lg = (double)best_ig * gs, lh = (double)best_ih * hs;
+    const int64_t rig = tg - best_ig, rih = th - best_ih;
+    const double rg = (double)rig * gs, rh = (double)rih * hs;
+    const int32_t lc = round_int((double)best_ih * cnt_factor), rc = round_int((double)rih * cnt_factor);
+    out->left_output = leaf_output(F, lg, lh, pl, lc, parent);
+    out->left_count = lc;
+    out->lsg = lg;
+    out->lsh = lh;
+    out->right_output = leaf_output(F, rg, rh, pl, rc, parent);
+    out->right_count = rc;
+    out->rsg = rg;
+    out->rsh = rh;
+    out->lint = (int64_t)(((uint64_t)best_ig << 32) | ((uint64_t)best_ih & 0xffffffffULL));
+    out->rint = (int64_t)(((uint64_t)rig << 32) | ((uint64_t)rih & 0xffffffffULL));
+    out->gain = best_gain - mgs;
+    out->cat_bins.clear();
+    if (onehot) {
+      out->cat_bins.push_back((uint32_t)(best_t + offset));
+    } else {
+      for (int32_t i = 0; i <= best_t; ++i) {
+        const int32_t pos = best_dir == 1 ? i : used_bin - 1 - i;
+        out->cat_bins.push_back((uint32_t)(sorted[(size_t)pos] + offset));
+      }
+    }
+  }
+  out->gain *= m.penalty;
+  return sp;
+}
+
 // feature_histogram.rs:114-125 — leaf_output_root.
 static double leaf_output_root(const Params& p, double sg, double sh, int32_t n) {
   Flags F{true, true, false};
@@ -633,6 +881,22 @@ static void route_table(const FeatureMeta& m, uint32_t threshold, bool default_l
     }
     lut[b] = left ? 1 : 0;
   }
+}
+
+// Categorical routing (data_partition.rs:264-300, route_bin :367-377): group bin 0 (the most
+// frequent bin's rows) takes the default route — left when the most frequent bin is in the bitset
+// and not 0 —, any other stored bin b looks up bit b - 1 + offset of the bin bitset.
+static void route_table_cat(const FeatureMeta& m, const uint32_t* bits, int32_t group_bins, uint8_t* lut) {
+  const uint32_t mfb = (uint32_t)m.mfb, offset = m.mfb == 0 ? 1u : 0u;
+  auto in_bits = [&](uint32_t pos) { return pos < 256 && ((bits[pos / 32] >> (pos % 32)) & 1u) != 0; };
+  const bool default_left = mfb > 0 && in_bits(mfb);
+  for (int32_t b = 0; b < group_bins; ++b) lut[b] = b == 0 ? (default_left ? 1 : 0) : (in_bits((uint32_t)b - 1 + offset) ? 1 : 0);
+}
+
+static void bitset_of(const std::vector<uint32_t>& vals, uint32_t* bits) {
+  for (int i = 0; i < 8; ++i) bits[i] = 0;
+  for (uint32_t v : vals)
+    if (v < 256) bits[v / 32] |= 1u << (v % 32);
 }
 
 // ---------------------------------------------------------------------------------------------
@@ -707,13 +971,15 @@ struct Pool {
 // ---------------------------------------------------------------------------------------------
 // Learner (treelearner/serial.rs)
 // ---------------------------------------------------------------------------------------------
-struct SplitRecord {  // one numerical split, the arguments of tree.split_numerical
+struct SplitRecord {  // one split: the arguments of tree.split_numerical / split_categorical
   int32_t leaf, right_leaf, inner_feature, real_feature;
   uint32_t threshold;
   int32_t default_left, missing_type, left_count, right_count;
   double left_output, right_output, left_sum_gradient, left_sum_hessian, right_sum_gradient, right_sum_hessian,
       gain;
   int64_t left_int_sum, right_int_sum;
+  int32_t categorical, _pad;
+  uint32_t cat_bins[8];  // categorical: bitset of the bins that go left (construct_bitset, utils/common.rs:221)
 };
 
 struct LeafSplits {  // serial.rs:53-76
@@ -917,13 +1183,15 @@ struct Learner {
             fix_slice_int(lg_, lh_, m.mfb, m.num_bin, larger.int_sum >> 32, larger.int_sum & 0xffffffffLL);
           }
         }
-        ss = find_best_threshold_numerical_int(sg_, sh_, m, p, smaller.int_sum >> 32, smaller.int_sum & 0xffffffffLL,
-                                               gscale, hscale, smaller.num_data, sp_out, &cs);
+        // serial.rs:2381-2433 — categorical features take the categorical search
+        auto search_int = m.categorical ? find_best_threshold_categorical_int : find_best_threshold_numerical_int;
+        ss = search_int(sg_, sh_, m, p, smaller.int_sum >> 32, smaller.int_sum & 0xffffffffLL, gscale, hscale,
+                        smaller.num_data, sp_out, &cs);
         if (lslot >= 0) {
           int64_t* lg_ = islots_g[lslot].data() + start;
           int64_t* lh_ = islots_h[lslot].data() + start;
-          sl = find_best_threshold_numerical_int(lg_, lh_, m, p, larger.int_sum >> 32, larger.int_sum & 0xffffffffLL,
-                                                 gscale, hscale, larger.num_data, lp_out, &cl);
+          sl = search_int(lg_, lh_, m, p, larger.int_sum >> 32, larger.int_sum & 0xffffffffLL, gscale, hscale,
+                          larger.num_data, lp_out, &cl);
         }
       } else {
         double* sd = slots[smaller_slot].data() + 2 * start;
@@ -936,10 +1204,12 @@ struct Learner {
             fix_slice(ld, m.mfb, m.num_bin, larger.sg, larger.sh);
           }
         }
-        ss = find_best_threshold_numerical(sd, m, p, smaller.sg, smaller.sh, smaller.num_data, sp_out, &cs);
+        // serial.rs:2335-2379
+        auto search = m.categorical ? find_best_threshold_categorical : find_best_threshold_numerical;
+        ss = search(sd, m, p, smaller.sg, smaller.sh, smaller.num_data, sp_out, &cs);
         if (lslot >= 0) {
           double* ld = slots[lslot].data() + 2 * start;
-          sl = find_best_threshold_numerical(ld, m, p, larger.sg, larger.sh, larger.num_data, lp_out, &cl);
+          sl = search(ld, m, p, larger.sg, larger.sh, larger.num_data, lp_out, &cl);
         }
       }
       cs.feature = m.real;
@@ -1026,9 +1296,11 @@ struct Learner {
   }
 
   // data_partition.rs:124-174 — stable split of `leaf` into itself (left) and `right_leaf`.
-  void partition_split(int32_t leaf, int32_t right_leaf, int32_t f, uint32_t threshold, bool default_left) {
+  void partition_split(int32_t leaf, int32_t right_leaf, int32_t f, uint32_t threshold, bool default_left,
+                       const uint32_t* cat_bits) {
     uint8_t lut[65536];
-    route_table(metas[f], threshold, default_left, gbins[f], lut);
+    if (cat_bits) route_table_cat(metas[f], cat_bits, gbins[f], lut);
+    else route_table(metas[f], threshold, default_left, gbins[f], lut);
     int64_t b = leaf_begin[leaf], c = leaf_count[leaf];
     std::vector<int32_t> L, R;
     L.reserve(c);
@@ -1057,15 +1329,22 @@ struct Learner {
     for (int f = 0; f < nf; ++f)
       if (metas[f].real == info.feature) inner = f;
     int32_t next_leaf = tree_leaves;
-    partition_split(best_leaf, next_leaf, inner, info.threshold, info.default_left);
+    // serial.rs:1724-1745 — a categorical split partitions by the bitset of its bins
+    const bool cat = metas[inner].categorical != 0;
+    uint32_t bits[8];
+    bitset_of(info.cat_bins, bits);
+    partition_split(best_leaf, next_leaf, inner, info.threshold, info.default_left, cat ? bits : nullptr);
     info.left_count = (int32_t)leaf_count[best_leaf];
     info.right_count = (int32_t)leaf_count[next_leaf];
     SplitRecord r;
+    std::memset(&r, 0, sizeof(r));
+    r.categorical = cat ? 1 : 0;
+    for (int i = 0; i < 8; ++i) r.cat_bins[i] = cat ? bits[i] : 0u;
     r.leaf = best_leaf;
     r.right_leaf = next_leaf;
     r.inner_feature = inner;
     r.real_feature = info.feature;
-    r.threshold = info.threshold;
+    r.threshold = cat ? 0u : info.threshold;
     r.default_left = info.default_left ? 1 : 0;
     r.missing_type = metas[inner].missing;
     r.left_count = info.left_count;
@@ -1197,7 +1476,7 @@ extern "C" {
 typedef struct {
   int32_t num_bin, missing_type, default_bin, most_freq_bin;
   double penalty;
-  int32_t real_feature, _pad;
+  int32_t real_feature, bin_type;  // bin_type: 0 numerical, 1 categorical
 } orc_feature;
 
 typedef struct {
@@ -1205,6 +1484,9 @@ typedef struct {
   double min_sum_hessian_in_leaf, lambda_l1, lambda_l2, max_delta_step, path_smooth, min_gain_to_split;
   int32_t use_quantized_grad, num_grad_quant_bins, quant_train_renew_leaf, stochastic_rounding;
   int32_t seed, num_threads, fused_madd, is_constant_hessian;
+  int32_t max_cat_to_onehot, max_cat_threshold;
+  double cat_smooth, cat_l2;
+  int32_t min_data_per_group, _pad1;
 } orc_config;
 
 typedef SplitRecord orc_split;
@@ -1223,6 +1505,7 @@ void* orc_learner_create(const orc_feature* feats, int32_t nf, const uint8_t* bi
     m.offset = m.mfb == 0 ? 1 : 0;
     m.penalty = feats[f].penalty;
     m.real = feats[f].real_feature;
+    m.categorical = feats[f].bin_type == 1 ? 1 : 0;
     L->metas.push_back(m);
     L->cols.push_back(bins_colmajor + (size_t)f * (size_t)n);
   }
@@ -1234,6 +1517,11 @@ void* orc_learner_create(const orc_feature* feats, int32_t nf, const uint8_t* bi
   L->p.min_hess = c->min_sum_hessian_in_leaf;
   L->p.min_gain = c->min_gain_to_split;
   L->p.fused = c->fused_madd != 0;
+  L->p.max_cat_to_onehot = c->max_cat_to_onehot;
+  L->p.max_cat_threshold = c->max_cat_threshold;
+  L->p.cat_smooth = c->cat_smooth;
+  L->p.cat_l2 = c->cat_l2;
+  L->p.min_data_per_group = c->min_data_per_group;
   L->num_leaves = c->num_leaves;
   L->max_depth = c->max_depth;
   L->const_hess = c->is_constant_hessian != 0;
@@ -1396,6 +1684,11 @@ static Params params_of(const orc_config* c) {
   p.min_hess = c->min_sum_hessian_in_leaf;
   p.min_gain = c->min_gain_to_split;
   p.fused = c->fused_madd != 0;
+  p.max_cat_to_onehot = c->max_cat_to_onehot;
+  p.max_cat_threshold = c->max_cat_threshold;
+  p.cat_smooth = c->cat_smooth;
+  p.cat_l2 = c->cat_l2;
+  p.min_data_per_group = c->min_data_per_group;
   return p;
 }
 
@@ -1408,6 +1701,7 @@ static FeatureMeta meta_of(const orc_feature* f) {
   m.offset = m.mfb == 0 ? 1 : 0;
   m.penalty = f->penalty;
   m.real = f->real_feature;
+  m.categorical = f->bin_type == 1 ? 1 : 0;
   return m;
 }
 
@@ -1458,6 +1752,12 @@ int32_t orc_find_best_threshold(const double* hist, const orc_feature* f, const 
   out->right_sum_hessian = si.rsh;
   out->gain = si.gain;
   return sp ? 1 : 0;
+}
+
+// Route table of one categorical split (bits: the bin bitset of the split, 8 words).
+void orc_route_table_cat(const orc_feature* f, const uint32_t* bits, uint8_t* lut) {
+  FeatureMeta m = meta_of(f);
+  route_table_cat(m, bits, 1 + m.num_bin - m.offset, lut);
 }
 
 }  // extern "C"

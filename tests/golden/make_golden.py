@@ -9,8 +9,9 @@ It copies, unchanged, the reference's own golden data for the tree-learner path:
 * ``train/<case>/{x.npy,y.npy,params.json,model.txt}`` — upstream-LightGBM 4.7.0 models that the
   reference reproduces byte for byte (tests/fixtures/train, generated on darwin/arm64 with
   ``deterministic, num_threads=1, force_col_wise, seed=7``), for the cases inside this learner's
-  scope (dense numerical features, L2 / binary / multiclass objectives; plain bagging and the
-  by-tree feature fraction, which reach the learner as its `rows` and feature-mask inputs);
+  scope (dense numerical and categorical features, L2 / binary / multiclass objectives; plain
+  bagging and the by-tree feature fraction, which reach the learner as its `rows` and
+  feature-mask inputs);
 * ``quantized_gradients.json`` — 16 upstream stumps for the gradient discretizer
   (tests/fixtures/quantized_gradients.json);
 
@@ -32,7 +33,8 @@ import sys
 HERE = os.path.dirname(os.path.abspath(__file__))
 CASES = ["binary", "l2_default", "l2_nan", "l2_zero", "l2_zero_as_missing", "l2_small", "l2_regularized",
          "l2_max_delta_smooth", "l2_max_depth", "l2_no_boost_from_average", "multiclass", "bagging",
-         "bagging_no_freq", "bagging_feature_fraction", "feature_fraction"]
+         "bagging_no_freq", "bagging_feature_fraction", "feature_fraction", "cat_default", "cat_binary", "cat_nan",
+         "cat_onehot", "cat_regularized", "cat_bagging"]
 
 
 def _ints(text):

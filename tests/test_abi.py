@@ -20,8 +20,8 @@ def test_header_symbols_are_exported(bklib):
 def test_record_layouts():
     from lgbm_gb300 import CONFIG_DTYPE, FEATURE_DTYPE, SPLIT_DTYPE
     assert FEATURE_DTYPE.itemsize == 32
-    assert CONFIG_DTYPE.itemsize == 96
-    assert SPLIT_DTYPE.itemsize == 112
+    assert CONFIG_DTYPE.itemsize == 128
+    assert SPLIT_DTYPE.itemsize == 152
 
 
 def test_binning_matches_reference_layout(bklib):

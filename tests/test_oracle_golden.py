@@ -29,10 +29,10 @@ def _load_case(case):
     return P, X, y, model
 
 
-def _dataset(p, X):
+def _dataset(p, X, categorical=()):
     from lgbm_gb300 import BinnedDataset
     return BinnedDataset.from_dense(X, max_bin=p.get("max_bin", 255), min_data_in_leaf=p.get("min_data_in_leaf", 20),
-                                    zero_as_missing=p.get("zero_as_missing", False))
+                                    zero_as_missing=p.get("zero_as_missing", False), categorical=categorical)
 
 
 @pytest.mark.parametrize("fused", [1, 0])
@@ -41,7 +41,7 @@ def test_oracle_reproduces_reference_models(oracle, bklib, case, fused):
     from lgbm_gb300 import LearnerConfig
     P, X, y, model = _load_case(case)
     p = P["params"]
-    ds = _dataset(p, X)
+    ds = _dataset(p, X, P.get("categorical", []))
     obj = oracle.make_objective(p, y)
     cfg = LearnerConfig(**p, fused_madd=fused, is_constant_hessian=int(obj.constant_hessian))
     learner = oracle.OracleLearner(ds, cfg)
