@@ -213,6 +213,10 @@ extern "C" int bk_bin_dense_device(const void* values, int32_t value_type, int64
   for (int f = 0; f < num_features; ++f) {
     const bk_feature& x = features[f];
     const int32_t nb = x.num_bin, off = x.most_freq_bin == 0 ? 1 : 0;
+    if (x.bin_type != 0) {
+      bin_error("bk_bin_dense_device: feature %d is categorical; device binning takes numerical features", f);
+      return -1;
+    }
     if (x.real_feature < 0 || x.real_feature >= num_columns || nb < 1 || 1 + nb - off > 256 ||
         x.missing_type < 0 || x.missing_type > 2 || x.most_freq_bin < 0 || x.most_freq_bin >= nb ||
         bound_offsets[f] < 0 || bound_offsets[f + 1] - bound_offsets[f] != nb) {

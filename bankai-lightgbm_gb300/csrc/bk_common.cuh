@@ -40,6 +40,8 @@ struct DevFeature {
   int32_t real;    // real (original) column index
   int32_t len;     // searched slice length: num_bin - offset
   double penalty;
+  int32_t cat;     // 1: categorical (BinType::Categorical)
+  int32_t _pad;
 };
 
 // A split candidate of one (leaf, feature): SplitInfo (split_info.rs:9-31) plus its
@@ -50,6 +52,7 @@ struct Cand {
   int32_t feature, inner;
   uint32_t threshold;
   int32_t left_count, right_count, default_left, splittable, missing;  // missing: the feature's missing type
+  uint32_t cat[8];  // categorical: bitset of the bins that go left (bit b = bin b)
 };
 
 // LeafSplits (serial.rs:53-76).
@@ -67,6 +70,9 @@ struct Params {
   int32_t renew, part_grid, pdl;  // pdl: launch the grow-loop kernels with programmatic dependence
   int32_t hist_min_rows;          // fewest rows a histogram CTA takes (launch shape, autotuned)
   int64_t n;
+  // CatParams of the categorical search (feature_histogram.rs:1146-1163)
+  double cat_smooth, cat_l2;
+  int32_t max_cat_threshold, max_cat_to_onehot, min_data_per_group, _p2;
 };
 
 // Per-leaf constants of one searched leaf (FindBestThreshold's preamble, feature_histogram.rs:

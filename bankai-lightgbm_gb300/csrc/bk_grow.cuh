@@ -162,6 +162,16 @@ __device__ __forceinline__ void post_split_writes(const Job& J, const Params& p,
     r.gain = info.gain;
     r.left_int_sum = info.lint;
     r.right_int_sum = info.rint;
+    // a categorical split (serial.rs:1724-1759) carries the bitset of its left bins; a numerical
+    // candidate's bitset is empty
+    uint32_t any = 0u;
+#pragma unroll
+    for (int w = 0; w < 8; ++w) {
+      r.cat_bins[w] = info.cat[w];
+      any |= info.cat[w];
+    }
+    r.categorical = any != 0u ? 1 : 0;
+    r._pad = 0;
     J.leaf_value[bl] = isnan(info.left_output) ? 0.0 : info.left_output;
     J.leaf_value[nl] = isnan(info.right_output) ? 0.0 : info.right_output;
     J.leaf_depth[nl] = o.depth;

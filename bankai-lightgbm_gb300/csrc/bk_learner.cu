@@ -353,6 +353,11 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
     p.stochastic = c->stochastic_rounding ? 1 : 0;
     p.renew = c->quant_train_renew_leaf ? 1 : 0;
     p.n = num_data;
+    p.cat_smooth = c->cat_smooth;
+    p.cat_l2 = c->cat_l2;
+    p.max_cat_threshold = c->max_cat_threshold;
+    p.max_cat_to_onehot = c->max_cat_to_onehot;
+    p.min_data_per_group = c->min_data_per_group;
     L->K = num_jobs;
     int maxb = 0;
     for (int f = 0; f < num_features; ++f) {
@@ -366,11 +371,7 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
       d.real = features[f].real_feature;
       d.len = d.num_bin - d.offset;
       d.penalty = features[f].penalty;
-      if (features[f].bin_type != 0) {
-        set_error("feature %d: categorical features are not supported by this learner yet", f);
-        delete L;
-        return -1;
-      }
+      d.cat = features[f].bin_type == 1 ? 1 : 0;
       if (d.num_bin < 1 || d.gbins > 256 || d.missing < 0 || d.missing > 2 || d.mfb < 0 || d.mfb >= d.num_bin ||
           d.default_bin < 0 || d.default_bin >= d.num_bin) {
         set_error("feature %d: unsupported bin mapper (num_bin %d, missing %d, mfb %d, default %d)", f, d.num_bin,
@@ -1057,6 +1058,11 @@ int bk_learner_predict_add(bk_learner* L, int32_t num_leaves, const int32_t* lef
         set_error("bk_learner_predict_add: node %d has child %d outside the tree", i, ch);
         return -1;
       }
+    }
+    if (decision_type[i] & 1) {
+      set_error("bk_learner_predict_add: node %d is a categorical split; the device replay takes numerical "
+                "splits only", i);
+      return -1;
     }
     if (split_feature_inner[i] < 0 || split_feature_inner[i] >= L->p.F ||
         threshold_in_bin[i] >= (uint32_t)L->h_feat[split_feature_inner[i]].num_bin) {

@@ -104,10 +104,22 @@ __device__ __forceinline__ T block_excl_scan(T v, T* total, T* sh) {
 }
 
 // The route of every stored bin of the chosen split (data_partition.rs:299-410), one per thread.
-__device__ __forceinline__ void build_route(const Decision& d, const DevFeature* feats, uint8_t* lut) {
+// A categorical split routes by the bitset of its left bins, kept in the chosen leaf's candidate
+// (data_partition.rs:264-300 and route_bin :367-377): group bin 0 (the most frequent bin's rows)
+// goes left when the most frequent bin is not 0 and is in the bitset; stored bin b looks up bit
+// b - 1 + offset.
+__device__ __forceinline__ void build_route(const Job& J, const Params& p, const Decision& d,
+                                            const DevFeature* feats, uint8_t* lut) {
   const DevFeature m = feats[d.inner];
-  const uint32_t th = d.thr;
   const uint32_t b = threadIdx.x;
+  if (m.cat) {
+    const uint32_t* bits = J.cand[(size_t)d.leaf * p.F + d.inner].cat;
+    const uint32_t pos = b == 0 ? (uint32_t)m.mfb : b - 1 + (uint32_t)m.offset;
+    const bool set = pos < 256u && ((__ldcg(bits + (pos >> 5)) >> (pos & 31)) & 1u) != 0u;
+    lut[b] = ((int)b < m.gbins && set && (b != 0 || m.mfb > 0)) ? 1 : 0;
+    return;
+  }
+  const uint32_t th = d.thr;
   lut[b] = (int)b < m.gbins ? route_bin(m, th & 0x7fffffffu, (th >> 31) != 0, b) : 0;
 }
 
@@ -122,7 +134,7 @@ __global__ void __launch_bounds__(kThreads) k_part_count(const JobTable jobs, Pa
   const Decision dec = recorded_decision(J.st);
   PartRange R;
   part_range(J, p, bins_cm, dec, &R);  // its loads are in flight with the route table's
-  build_route(dec, feats, lut);
+  build_route(J, p, dec, feats, lut);
   __syncthreads();
   if ((int)blockIdx.x >= R.active) {  // no rows: the scatter reads only active CTAs' counts
     griddep_launch();
@@ -159,7 +171,7 @@ __global__ void __launch_bounds__(kThreads) k_part_scatter(const JobTable jobs, 
   const Decision dec = recorded_decision(J.st);
   PartRange R;
   part_range(J, p, bins_cm, dec, &R);  // its loads are in flight with the route table's
-  build_route(dec, feats, lut);
+  build_route(J, p, dec, feats, lut);
   __syncthreads();
   // left rows before this chunk, and in total
   int64_t before = 0, all = 0;
@@ -255,7 +267,7 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
     griddep_launch();
     return;
   }
-  build_route(dec, feats, lut);
+  build_route(J, p, dec, feats, lut);
   __syncthreads();
   unsigned long long* cnt_left = reinterpret_cast<unsigned long long*>(&st->pcnt[par][0]);
   unsigned long long* cnt_right = reinterpret_cast<unsigned long long*>(&st->pcnt[par][1]);

@@ -26,6 +26,8 @@
 // bookkeeping (bk_grow.cuh) runs in the last CTA of the partition scatter.
 #include <math_constants.h>
 
+#include <type_traits>
+
 #include "bk_decide.cuh"
 #include "bk_grow.cuh"
 #include "bk_launch.cuh"
@@ -145,6 +147,8 @@ __device__ void cand_reset(Cand* c, int32_t real, int32_t inner) {
   c->left_count = c->right_count = 0;
   c->default_left = 1;
   c->splittable = 0;
+#pragma unroll
+  for (int w = 0; w < 8; ++w) c->cat[w] = 0u;
 }
 
 // Direction geometry of FindBestThreshold[Int] (feature_histogram.rs:219-357, :673-830): direction
@@ -942,6 +946,367 @@ __device__ void search_float(const Job& J, const Params& p, const JobState* st, 
   });
 }
 
+// ---- categorical features (feature_histogram.rs:1328-1886) ----
+// One CTA per (leaf side, feature) as for numerical features; thread t holds slice index t. The
+// histogram slice is loaded, fixed and (larger side) derived by subtraction exactly as the
+// numerical searches do, so the pool holds the same values afterwards. Then:
+//   one-hot (num_bin <= max_cat_to_onehot): every category's split against the rest is evaluated
+//     by its own thread; the first best in category order wins;
+//   sorted: the categories with enough data are ranked by grad / (hess + cat_smooth) (a stable
+//     rank over order-preserving integer keys, ties by category), one thread per direction walks
+//     the reference's sequential scan (its sums, counts, skips and breaks do not depend on the
+//     gains) and queues the positions that need a gain, which the CTA then evaluates in parallel;
+//     the first best in scan order (ascending direction first) wins.
+// Gains and outputs use lambda_l2 + cat_l2 in the sorted form, as the reference does.
+constexpr int kCatQueue = kSearchThreads / 2;  // queued positions per direction: max_num_cat <= 128
+
+// The categorical search's shared memory, overlaid on the numerical search's (a CTA runs one or
+// the other). V: int64_t (quantized, integer sums) or double (float path).
+template <typename V>
+struct CatSmem {
+  V a[kSearchThreads], b[kSearchThreads];  // per-bin gradient / hessian sums
+  int32_t cnt[kSearchThreads];
+  long long key[kSearchThreads];
+  int16_t sorted[kSearchThreads];
+  V qa[2][kCatQueue], qb[2][kCatQueue];    // queued positions: the accumulated left side's sums
+  int32_t qlc[2][kCatQueue], qi[2][kCatQueue];
+  int32_t qn[2];
+  long long wk[kSearchWarps];
+  int32_t wo[kSearchWarps], wsp[kSearchWarps];
+  int64_t wi[kSearchWarps];
+  double wd[2][kSearchWarps];
+  double best_gain;
+};
+
+__device__ __forceinline__ long long cat_block_max(long long v, long long* w, int lane, int warp) {
+  v = warp_max64(v);
+  if (lane == 0) w[warp] = v;
+  __syncthreads();
+  long long r = w[0];
+#pragma unroll
+  for (int i = 1; i < kSearchWarps; ++i) r = w[i] > r ? w[i] : r;
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ int32_t cat_block_min(int32_t v, int32_t* w, int lane, int warp) {
+  v = __reduce_min_sync(FULL, v);
+  if (lane == 0) w[warp] = v;
+  __syncthreads();
+  int32_t r = w[0];
+#pragma unroll
+  for (int i = 1; i < kSearchWarps; ++i) r = w[i] < r ? w[i] : r;
+  __syncthreads();
+  return r;
+}
+
+__device__ __forceinline__ int32_t cat_block_or(int32_t v, int32_t* w, int lane, int warp) {
+  v = (int32_t)__reduce_or_sync(FULL, (unsigned)v);
+  if (lane == 0) w[warp] = v;
+  __syncthreads();
+  int32_t r = 0;
+#pragma unroll
+  for (int i = 0; i < kSearchWarps; ++i) r |= w[i];
+  __syncthreads();
+  return r;
+}
+
+template <bool QUANT>
+__device__ void search_cat(const Job& J, const Params& p, const JobState* st, const DevFeature& m, int side,
+                           int32_t f, int32_t leaf, SearchSmem& sm) {
+  using V = typename std::conditional<QUANT, int64_t, double>::type;
+  static_assert(sizeof(CatSmem<V>) <= sizeof(SearchSmem), "the categorical search fits the search's shared memory");
+  CatSmem<V>& cs = *reinterpret_cast<CatSmem<V>*>(&sm);
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const LeafConst C = J.lconst[side];
+  const LeafSum S0 = J.leaf_sum[st->smaller_leaf];
+  const LeafSum SL = J.leaf_sum[leaf];
+  const int32_t num_data = SL.num_data;
+  const size_t slot_stride = (size_t)p.T * p.B * TILE;
+  const size_t feat_off = (size_t)(f / TILE) * p.B * TILE + (f % TILE);
+  const bool fix = m.mfb > 0;
+  const bool in = t < m.len;
+  // -- the slice: FixHistogram of the smaller leaf, the larger as parent minus smaller (serial.rs:
+  //    1407-1437, 2205-2238), written back exactly as the numerical searches write it --
+  if (QUANT) {
+    int64_t* pool = reinterpret_cast<int64_t*>(J.pool);
+    int64_t* hs = pool + (size_t)st->smaller_slot * slot_stride + feat_off;
+    int64_t* hl = pool + (size_t)(side ? st->larger_slot : st->smaller_slot) * slot_stride + feat_off;
+    const int64_t sv = (in && !(fix && t == m.mfb)) ? hs[(size_t)(t + 1) * TILE] : 0;
+    const int64_t lv = (side && in) ? hl[(size_t)(t + 1) * TILE] : 0;
+    int64_t v = side ? lv - sv : sv;
+    if (fix) {
+      const int64_t a = warp_sum(sv);
+      if (lane == 0) cs.wi[warp] = a;
+      __syncthreads();
+      int64_t aux = 0;
+#pragma unroll
+      for (int i = 0; i < kSearchWarps; ++i) aux += cs.wi[i];
+      const int64_t fixed = S0.int_sum - aux;  // the leaf total minus every other bin
+      if (t == m.mfb) {
+        v += side ? -fixed : fixed;
+        if (side == 0) hs[(size_t)(t + 1) * TILE] = fixed;
+      }
+    }
+    if (side && in) hl[(size_t)(t + 1) * TILE] = v;
+    cs.a[t] = in ? unpack_g(v) : 0;
+    cs.b[t] = in ? unpack_h(v) : 0;
+    cs.cnt[t] = in ? round_int((double)unpack_h(v) * C.cnt_factor) : 0;
+  } else {
+    double2* pool = reinterpret_cast<double2*>(J.pool);
+    double2* hs = pool + (size_t)st->smaller_slot * slot_stride + feat_off;
+    double2* hl = pool + (size_t)(side ? st->larger_slot : st->smaller_slot) * slot_stride + feat_off;
+    const double2 zero = make_double2(0.0, 0.0);
+    double2 sv = (in && !(fix && t == m.mfb)) ? hs[(size_t)(t + 1) * TILE] : zero;
+    const double2 lv = (side && in) ? hl[(size_t)(t + 1) * TILE] : zero;
+    if (fix) {
+      const double ag = warp_sum(sv.x), ah = warp_sum(sv.y);
+      if (lane == 0) {
+        cs.wd[0][warp] = ag;
+        cs.wd[1][warp] = ah;
+      }
+      __syncthreads();
+      double tg = 0.0, th = 0.0;
+#pragma unroll
+      for (int i = 0; i < kSearchWarps; ++i) {
+        tg += cs.wd[0][i];
+        th += cs.wd[1][i];
+      }
+      if (t == m.mfb) {
+        sv = make_double2(S0.sg - tg, S0.sh - th);
+        if (side == 0) hs[(size_t)(t + 1) * TILE] = sv;
+      }
+    }
+    const double2 v = side ? make_double2(lv.x - sv.x, lv.y - sv.y) : sv;
+    if (side && in) hl[(size_t)(t + 1) * TILE] = v;
+    cs.a[t] = in ? v.x : 0.0;
+    cs.b[t] = in ? v.y : 0.0;
+    cs.cnt[t] = in ? round_int(v.y * C.cnt_factor) : 0;
+  }
+  if (t < 2) cs.qn[t] = 0;
+  __syncthreads();
+  // -- the leaf's totals and min_gain_shift (feature_histogram.rs:1347-1386, :1614-1665) --
+  const int64_t l_int = side ? SL.int_sum : S0.int_sum;
+  const int64_t tgi = unpack_g(l_int), thi = unpack_h(l_int);
+  const double gs = C.gs, hsc = C.hs;
+  const double sum_g = C.sum_g, sum_h = C.sum_h;  // float path: sum_h includes 2 kEpsilon
+  const double mgs =
+      p.use_smooth ? leaf_gain_given_output(p.use_l1, sum_g, sum_h, p, C.parent) + p.min_gain : C.mgs;
+  const int32_t bin_start = 1 - m.offset, bin_end = m.num_bin - m.offset;
+  const bool onehot = m.num_bin <= p.max_cat_to_onehot;
+  Params pl = p;
+  int32_t best_dir = 0, best_i = -1, used_bin = 0, sp = 0;
+  double best_gain = -CUDART_INF;
+  // the chosen position's left side
+  double blg = 0.0, blh = 0.0;
+  int64_t big = 0, bih = 0;
+  int32_t blc = 0;
+  if (onehot) {
+    // -- one category against the rest, thread t = category t --
+    bool pass = false;
+    double gain = -CUDART_INF;
+    if (t >= bin_start && t < bin_end) {
+      const int32_t cnt = cs.cnt[t];
+      if (QUANT) {
+        const int64_t ig = (int64_t)cs.a[t], ih = (int64_t)cs.b[t];
+        const double h = (double)ih * hsc;
+        const int32_t other_cnt = num_data - cnt;
+        const double other_h = (double)(thi - ih) * hsc;
+        if (!(cnt < p.min_data || h < p.min_hess) && other_cnt >= p.min_data && !(other_h < p.min_hess)) {
+          const double g = (double)ig * gs, other_g = (double)(tgi - ig) * gs;
+          gain = split_gains(pl, other_g, other_h, g, h, other_cnt, cnt, C.parent);
+          pass = gain > mgs;
+        }
+      } else {
+        const double g = (double)cs.a[t], h = (double)cs.b[t];
+        const int32_t other_cnt = num_data - cnt;
+        const double other_h = sum_h - h - BK_EPS;
+        if (!(cnt < p.min_data || h < p.min_hess) && other_cnt >= p.min_data && !(other_h < p.min_hess)) {
+          const double other_g = sum_g - g;
+          gain = split_gains(pl, other_g, other_h, g, h + BK_EPS, other_cnt, cnt, C.parent);
+          pass = gain > mgs;
+        }
+      }
+    }
+    sp = cat_block_or(pass ? 1 : 0, cs.wsp, lane, warp);
+    const long long k = cat_block_max(pass ? dkey(gain) : kNoKey, cs.wk, lane, warp);
+    if (k != kNoKey) {
+      // the first category (in order) with the best gain
+      const int32_t first = cat_block_min(pass && dkey(gain) == k ? t : 0x7fffffff, cs.wo, lane, warp);
+      if (t == first) cs.best_gain = gain;
+      __syncthreads();
+      best_gain = cs.best_gain;
+      best_i = first;
+      blc = cs.cnt[first];
+      if (QUANT) {
+        big = (int64_t)cs.a[first];
+        bih = (int64_t)cs.b[first];
+      } else {
+        blg = (double)cs.a[first];
+        blh = (double)cs.b[first] + BK_EPS;
+      }
+    }
+    if (warp != 0) return;
+  } else {
+    // -- the categories with enough data, ranked by grad / (hess + cat_smooth) --
+    const bool elig = t >= bin_start && t < bin_end && (double)cs.cnt[t] >= p.cat_smooth;
+    double ctr = 0.0;
+    if (elig) {
+      if (QUANT) ctr = ((double)cs.a[t] * gs) / ((double)cs.b[t] * hsc + p.cat_smooth);
+      else ctr = (double)cs.a[t] / ((double)cs.b[t] + p.cat_smooth);
+    }
+    cs.key[t] = elig ? dkey(ctr) : kNoKey;
+    const int32_t ne = __popc(__ballot_sync(FULL, elig));
+    if (lane == 0) cs.wo[warp] = ne;
+    __syncthreads();
+    used_bin = 0;
+#pragma unroll
+    for (int i = 0; i < kSearchWarps; ++i) used_bin += cs.wo[i];
+    if (elig) {
+      const long long kt = cs.key[t];
+      int32_t rank = 0;
+      for (int u = 0; u < kSearchThreads; ++u) {
+        const long long ku = cs.key[u];
+        rank += (ku != kNoKey && (ku < kt || (ku == kt && u < t))) ? 1 : 0;
+      }
+      cs.sorted[rank] = (int16_t)t;
+    }
+    pl.l2 = p.l2 + p.cat_l2;
+    __syncthreads();
+    const int32_t max_num_cat = min(p.max_cat_threshold, (used_bin + 1) / 2);
+    // -- the sequential scans, one thread per direction (warp 0 ascending, warp 1 descending) --
+    if ((t == 0 || t == 32) && used_bin > 0) {
+      const int d = t == 0 ? 0 : 1;
+      const int dir = d == 0 ? 1 : -1;
+      int32_t pos = d == 0 ? 0 : used_bin - 1, cnt_group = 0, left_cnt = 0, q = 0;
+      double lg = 0.0, lh = BK_EPS;
+      int64_t lig = 0, lih = 0;
+      for (int32_t i = 0; i < used_bin && i < max_num_cat; ++i) {
+        const int32_t c = cs.sorted[pos];
+        pos += dir;
+        const int32_t cnt = cs.cnt[c];
+        left_cnt += cnt;
+        cnt_group += cnt;
+        double lhv;
+        if (QUANT) {
+          lig += (int64_t)cs.a[c];
+          lih += (int64_t)cs.b[c];
+          lhv = (double)lih * hsc;
+        } else {
+          lg += (double)cs.a[c];
+          lh += (double)cs.b[c];
+          lhv = lh;
+        }
+        if (left_cnt < p.min_data || lhv < p.min_hess) continue;
+        const int32_t right_cnt = num_data - left_cnt;
+        if (right_cnt < p.min_data || right_cnt < p.min_data_per_group) break;
+        const double rhv = QUANT ? (double)(thi - lih) * hsc : sum_h - lh;
+        if (rhv < p.min_hess) break;
+        if (cnt_group < p.min_data_per_group) continue;
+        cnt_group = 0;
+        if (q < kCatQueue) {
+          cs.qa[d][q] = QUANT ? (V)lig : (V)lg;
+          cs.qb[d][q] = QUANT ? (V)lih : (V)lh;
+          cs.qlc[d][q] = left_cnt;
+          cs.qi[d][q] = i;
+          ++q;
+        }
+      }
+      cs.qn[d] = q;
+    }
+    __syncthreads();
+    // -- the queued gains, one thread each: direction 0 on threads 0..127, direction 1 on 128..255 --
+    const int d = t >> 7, j = t & 127;
+    bool pass = false;
+    double gain = -CUDART_INF;
+    if (j < cs.qn[d]) {
+      const int32_t lc = cs.qlc[d][j], rc = num_data - lc;
+      if (QUANT) {
+        const int64_t lig = (int64_t)cs.qa[d][j], lih = (int64_t)cs.qb[d][j];
+        const double lg = (double)lig * gs, lh = (double)lih * hsc;
+        const double rg = (double)(tgi - lig) * gs, rh = (double)(thi - lih) * hsc;
+        gain = split_gains(pl, lg, lh, rg, rh, lc, rc, C.parent);
+      } else {
+        const double lg = (double)cs.qa[d][j], lh = (double)cs.qb[d][j];
+        gain = split_gains(pl, lg, lh, sum_g - lg, sum_h - lh, lc, rc, C.parent);
+      }
+      pass = gain > mgs;
+    }
+    sp = cat_block_or(pass ? 1 : 0, cs.wsp, lane, warp);
+    const long long k = cat_block_max(pass ? dkey(gain) : kNoKey, cs.wk, lane, warp);
+    if (k != kNoKey) {
+      // scan order: direction 0 before direction 1, then the position
+      const int32_t first = cat_block_min(pass && dkey(gain) == k ? t : 0x7fffffff, cs.wo, lane, warp);
+      best_dir = first >> 7;
+      const int32_t bj = first & 127;
+      best_i = cs.qi[best_dir][bj];
+      if (QUANT) {
+        big = (int64_t)cs.qa[best_dir][bj];
+        bih = (int64_t)cs.qb[best_dir][bj];
+      } else {
+        blg = (double)cs.qa[best_dir][bj];
+        blh = (double)cs.qb[best_dir][bj];
+      }
+      blc = cs.qlc[best_dir][bj];
+      if (t == first) cs.best_gain = gain;
+      __syncthreads();
+      best_gain = cs.best_gain;
+    }
+    if (warp != 0) return;
+  }
+  // -- warp 0: the SplitInfo of the chosen position (feature_histogram.rs:1537-1598, :1828-1886) --
+  Cand c;
+  cand_reset(&c, m.real, f);
+  c.default_left = 0;
+  if (sp && best_i >= 0) {
+    if (QUANT) {
+      const double lg = (double)big * gs, lh = (double)bih * hsc;
+      const int64_t rig = tgi - big, rih = thi - bih;
+      const double rg = (double)rig * gs, rh = (double)rih * hsc;
+      const int32_t lc = round_int((double)bih * C.cnt_factor), rc = round_int((double)rih * C.cnt_factor);
+      c.left_output = split_output(pl, lg, lh, lc, C.parent);
+      c.right_output = split_output(pl, rg, rh, rc, C.parent);
+      c.left_count = lc;
+      c.right_count = rc;
+      c.lsg = lg;
+      c.lsh = lh;
+      c.rsg = rg;
+      c.rsh = rh;
+      c.lint = (int64_t)(((uint64_t)big << 32) | ((uint64_t)bih & 0xffffffffULL));
+      c.rint = (int64_t)(((uint64_t)rig << 32) | ((uint64_t)rih & 0xffffffffULL));
+    } else {
+      c.left_output = split_output(pl, blg, blh, blc, C.parent);
+      c.right_output = split_output(pl, sum_g - blg, sum_h - blh, num_data - blc, C.parent);
+      c.left_count = blc;
+      c.right_count = num_data - blc;
+      c.lsg = blg;
+      c.lsh = blh - BK_EPS;
+      c.rsg = sum_g - blg;
+      c.rsh = sum_h - blh - BK_EPS;
+    }
+    c.gain = best_gain - mgs;
+    // the bins that go left: the category itself (one-hot) or the first best_i + 1 categories of
+    // the chosen scan direction; lane w collects word w of the bitset
+    uint32_t word = 0u;
+    if (onehot) {
+      const uint32_t b = (uint32_t)(best_i + m.offset);
+      if ((int)(b >> 5) == lane) word |= 1u << (b & 31);
+    } else {
+      for (int32_t i = 0; i <= best_i; ++i) {
+        const int32_t pos = best_dir == 0 ? i : used_bin - 1 - i;
+        const uint32_t b = (uint32_t)(cs.sorted[pos] + m.offset);
+        if ((int)(b >> 5) == lane) word |= 1u << (b & 31);
+      }
+    }
+#pragma unroll
+    for (int w = 0; w < 8; ++w) c.cat[w] = __shfl_sync(FULL, word, w);
+  }
+  c.gain *= m.penalty;
+  c.splittable = sp;
+  c.missing = m.missing;
+  if (lane == 0) store_cand(J, p, side, leaf, f, c);
+}
+
 // One CTA per (feature, side): blockIdx.x = 2 * feature + side (0 = smaller leaf). With `decide`,
 // the last CTA to finish runs the fold / arg-max and records the split; otherwise the single-pass
 // partition that follows decides it.
@@ -966,7 +1331,9 @@ __global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, 
   if (st->stop) return;  // uniform over the grid
   const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
   if (st->do_search && J.used[f] && leaf >= 0) {  // uniform over the CTA
-    if (QUANT)
+    if (m.cat)
+      search_cat<QUANT>(J, p, st, m, side, f, leaf, sm);
+    else if (QUANT)
       search_int<PLAIN>(J, p, st, m, side, f, leaf, sm);
     else
       search_float<PLAIN>(J, p, st, m, side, f, leaf, sm);

@@ -72,7 +72,9 @@ def _assert_records_equal(a, b):
     for i, (x, y) in enumerate(zip(a, b)):
         for name in a.dtype.names:
             xv, yv = x[name], y[name]
-            if isinstance(xv, (np.floating, float)):
+            if isinstance(xv, np.ndarray):  # the categorical bin bitset
+                same = np.array_equal(xv, yv)
+            elif isinstance(xv, (np.floating, float)):
                 same = (xv == yv) or (np.isnan(xv) and np.isnan(yv))
             else:
                 same = xv == yv
@@ -250,7 +252,8 @@ def test_gpu_reproduces_reference_models(oracle, case):
     X = np.load(os.path.join(d, "x.npy"))
     y = np.load(os.path.join(d, "y.npy"))
     ds = BinnedDataset.from_dense(X, max_bin=p.get("max_bin", 255), min_data_in_leaf=p.get("min_data_in_leaf", 20),
-                                  zero_as_missing=p.get("zero_as_missing", False))
+                                  zero_as_missing=p.get("zero_as_missing", False),
+                                  categorical=P.get("categorical", []))
     obj = oracle.make_objective(p, y)
     cfg = LearnerConfig(**p, fused_madd=1, is_constant_hessian=int(obj.constant_hessian))
     learner = GpuTreeLearner(ds, cfg)
@@ -339,3 +342,60 @@ def test_autotune_keeps_parity_and_caches_by_shape():
     assert other.autotune(g, h, trials=1) == shape
     gpu.close()
     other.close()
+
+
+def _cat_dataset(n, seed, nan_frac=0.05):
+    """Two categorical columns with 3 and 40 categories (one-hot and sorted searches), one with
+    200 categories, plus numerical columns; the target depends on category groups."""
+    from lgbm_gb300 import BinnedDataset
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((n, 8))
+    X[:, 0] = rng.integers(0, 3, n)
+    X[:, 3] = rng.integers(0, 40, n)
+    X[:, 6] = rng.integers(0, 200, n)
+    X[rng.random((n, 8)) < nan_frac] = np.nan
+    eff = rng.standard_normal(200)
+    c3 = np.nan_to_num(X[:, 3], nan=0).astype(int)
+    c6 = np.nan_to_num(X[:, 6], nan=0).astype(int)
+    z = eff[c3 % 40] + 0.5 * eff[c6] + np.nan_to_num(X[:, 1]) + (np.nan_to_num(X[:, 0]) == 1)
+    ds = BinnedDataset.from_dense(X, categorical=[0, 3, 6])
+    assert sum(f.categorical for f in ds.features) == 3
+    return ds, z
+
+
+CAT_CASES = [dict(), dict(max_cat_to_onehot=64, min_data_per_group=20),
+             dict(cat_smooth=2.0, cat_l2=1.0, max_cat_threshold=8, min_data_per_group=30, lambda_l2=0.5),
+             dict(lambda_l1=0.2, max_delta_step=0.8, path_smooth=1.5, min_data_per_group=10)]
+
+
+@pytest.mark.parametrize("case", range(len(CAT_CASES)))
+def test_categorical_trees(case):
+    """Categorical features (one-hot and sorted searches, bitset partitions): quantized trees
+    bit-exact with the oracle's, float trees within the float tolerance."""
+    ds, z = _cat_dataset(30000, seed=40 + case)
+    for quant in (1, 0):
+        for kind in ("binary", "l2"):
+            g, h, const = _grads(z, kind, seed=50 + case)
+            cfg = dict(CAT_CASES[case], num_leaves=31, use_quantized_grad=quant, stochastic_rounding=1, seed=3,
+                       num_threads=2)
+            orc, gpu, _ = _learners(ds, const, **cfg)
+            divergences = []
+            ncat = 0
+            for it in range(2):
+                ro, rg = orc.train(g, h), gpu.train(g, h)
+                ncat += int(np.sum(rg[0]["categorical"]))
+                if quant:
+                    _assert_records_equal(ro[0], rg[0])
+                    assert np.array_equal(ro[1], rg[1])
+                    assert np.array_equal(orc.row_leaf(), gpu.row_leaf())
+                else:
+                    d = _float_compare(ro, rg)
+                    if d >= 0:
+                        divergences.append((it, d))
+                    else:
+                        assert all(np.array_equal(a["cat_bins"], b["cat_bins"]) for a, b in zip(ro[0], rg[0]))
+                g = (g * 0.9).astype(np.float32)
+            assert ncat > 0, "no categorical split was chosen"
+            print("float near-tie divergences:", divergences)
+            assert len(divergences) <= 1
+            gpu.close()
