@@ -52,7 +52,7 @@ struct Cand {
   int32_t feature, inner;
   uint32_t threshold;
   int32_t left_count, right_count, default_left, splittable, missing;  // missing: the feature's missing type
-  uint32_t cat[8];  // categorical: bitset of the bins that go left (bit b = bin b)
+  int32_t categorical;  // 1: a categorical split, its left bins in cand_cat_bits()
 };
 
 // LeafSplits (serial.rs:53-76).
@@ -164,6 +164,15 @@ inline void for_job_groups(const Job* h_jobs, int num_jobs, F f) {
     for (int i = 0; i < nz; ++i) t.job[i] = h_jobs[z0 + i];
     f(t, nz);
   }
+}
+
+// The bin bitsets of categorical candidates, stored after the [L][F] candidates in the same
+// allocation (8 words per (leaf, feature); written only by categorical searches).
+__host__ __device__ __forceinline__ size_t cand_cat_words(int num_leaves, int F) {
+  return (size_t)num_leaves * (size_t)F * 8;
+}
+__device__ __forceinline__ uint32_t* cand_cat_bits(const Job& J, const Params& p, int32_t leaf, int32_t f) {
+  return reinterpret_cast<uint32_t*>(J.cand + (size_t)p.num_leaves * p.F) + ((size_t)leaf * p.F + f) * 8;
 }
 
 __device__ __forceinline__ const int32_t* leaf_idx(const Job& J, int32_t buf) { return buf ? J.idx1 : J.idx0; }

@@ -137,6 +137,10 @@ __device__ __forceinline__ void post_split_writes(const Job& J, const Params& p,
   info.left_count = (int32_t)o.L;
   info.right_count = (int32_t)o.R;
   const int32_t bl = o.bl, nl = o.nl;
+  // lanes 0-7: word `lane` of a categorical split's left-bin bitset (serial.rs:1724-1759)
+  if (lane < 8)
+    J.records[o.tl - 1].cat_bins[lane] =
+        info.categorical ? __ldcg(cand_cat_bits(J, p, o.bl, info.inner) + lane) : 0u;
   if (lane == 0) {
     J.leaf_count[bl] = o.L;
     J.leaf_begin[nl] = o.b + o.L;
@@ -162,15 +166,7 @@ __device__ __forceinline__ void post_split_writes(const Job& J, const Params& p,
     r.gain = info.gain;
     r.left_int_sum = info.lint;
     r.right_int_sum = info.rint;
-    // a categorical split (serial.rs:1724-1759) carries the bitset of its left bins; a numerical
-    // candidate's bitset is empty
-    uint32_t any = 0u;
-#pragma unroll
-    for (int w = 0; w < 8; ++w) {
-      r.cat_bins[w] = info.cat[w];
-      any |= info.cat[w];
-    }
-    r.categorical = any != 0u ? 1 : 0;
+    r.categorical = info.categorical;
     r._pad = 0;
     J.leaf_value[bl] = isnan(info.left_output) ? 0.0 : info.left_output;
     J.leaf_value[nl] = isnan(info.right_output) ? 0.0 : info.right_output;

@@ -490,7 +490,9 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
       J.leaf_sum = L->dalloc<LeafSum>(Lv);
       J.bgain = L->dalloc<double>(Lv);
       J.bfeat = L->dalloc<int32_t>(Lv);
-      J.cand = L->dalloc<Cand>((size_t)Lv * F);
+      // the candidates, then the categorical candidates' bin bitsets
+      J.cand = L->dalloc<Cand>((size_t)Lv * F + (cand_cat_words(Lv, F) * sizeof(uint32_t) + sizeof(Cand) - 1) /
+                                                     sizeof(Cand));
       J.cgain = L->dalloc<double>(2 * (size_t)F);
       J.csplit = L->dalloc<uint8_t>(2 * (size_t)F);
       J.cthr = L->dalloc<uint32_t>(2 * (size_t)F);

@@ -113,7 +113,7 @@ __device__ __forceinline__ void build_route(const Job& J, const Params& p, const
   const DevFeature m = feats[d.inner];
   const uint32_t b = threadIdx.x;
   if (m.cat) {
-    const uint32_t* bits = J.cand[(size_t)d.leaf * p.F + d.inner].cat;
+    const uint32_t* bits = cand_cat_bits(J, p, d.leaf, d.inner);
     const uint32_t pos = b == 0 ? (uint32_t)m.mfb : b - 1 + (uint32_t)m.offset;
     const bool set = pos < 256u && ((__ldcg(bits + (pos >> 5)) >> (pos & 31)) & 1u) != 0u;
     lut[b] = ((int)b < m.gbins && set && (b != 0 || m.mfb > 0)) ? 1 : 0;

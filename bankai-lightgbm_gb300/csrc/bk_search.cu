@@ -147,8 +147,7 @@ __device__ void cand_reset(Cand* c, int32_t real, int32_t inner) {
   c->left_count = c->right_count = 0;
   c->default_left = 1;
   c->splittable = 0;
-#pragma unroll
-  for (int w = 0; w < 8; ++w) c->cat[w] = 0u;
+  c->categorical = 0;
 }
 
 // Direction geometry of FindBestThreshold[Int] (feature_histogram.rs:219-357, :673-830): direction
@@ -1258,6 +1257,8 @@ __device__ void search_cat(const Job& J, const Params& p, const JobState* st, co
   Cand c;
   cand_reset(&c, m.real, f);
   c.default_left = 0;
+  c.categorical = 1;
+  uint32_t word = 0u;  // lane w: word w of the left bins' bitset
   if (sp && best_i >= 0) {
     if (QUANT) {
       const double lg = (double)big * gs, lh = (double)bih * hsc;
@@ -1287,7 +1288,6 @@ __device__ void search_cat(const Job& J, const Params& p, const JobState* st, co
     c.gain = best_gain - mgs;
     // the bins that go left: the category itself (one-hot) or the first best_i + 1 categories of
     // the chosen scan direction; lane w collects word w of the bitset
-    uint32_t word = 0u;
     if (onehot) {
       const uint32_t b = (uint32_t)(best_i + m.offset);
       if ((int)(b >> 5) == lane) word |= 1u << (b & 31);
@@ -1298,13 +1298,12 @@ __device__ void search_cat(const Job& J, const Params& p, const JobState* st, co
         if ((int)(b >> 5) == lane) word |= 1u << (b & 31);
       }
     }
-#pragma unroll
-    for (int w = 0; w < 8; ++w) c.cat[w] = __shfl_sync(FULL, word, w);
   }
   c.gain *= m.penalty;
   c.splittable = sp;
   c.missing = m.missing;
   if (lane == 0) store_cand(J, p, side, leaf, f, c);
+  if (lane < 8) cand_cat_bits(J, p, leaf, f)[lane] = word;
 }
 
 // One CTA per (feature, side): blockIdx.x = 2 * feature + side (0 = smaller leaf). With `decide`,
