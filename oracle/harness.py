@@ -16,6 +16,7 @@ import ctypes
 import math
 import os
 import sys
+from fractions import Fraction
 
 import numpy as np
 
@@ -136,34 +137,55 @@ class OracleLearner:
 # ------------------------------------------------------------------------------------------
 # objectives (host, f64 score -> f32 gradients), written in the reference's operation order
 # ------------------------------------------------------------------------------------------
+def _madd(a, b, c, fused):
+    """utils/common.rs:207-216: a * b + c, rounded once when fused (exact rational arithmetic, one
+    correctly rounded conversion), twice otherwise."""
+    if fused:
+        return float(Fraction(a) * Fraction(b) + Fraction(c))
+    return a * b + c
+
+
 class L2Objective:
-    """objective/regression.rs:240-248 and :127-142."""
-    constant_hessian = True
+    """objective/regression.rs:240-248, :321-330 (weighted) and :127-142."""
     num_class = 1
 
-    def __init__(self, label):
+    def __init__(self, label, weights=None, fused=True):
         self.label = np.asarray(label, dtype=np.float32)
+        self.w = None if weights is None else np.asarray(weights, dtype=np.float32)
+        self.fused = fused
+        self.constant_hessian = self.w is None
 
     def gradients(self, score):
         g = (score - self.label.astype(np.float64)).astype(np.float32)
-        h = np.ones_like(g)
+        if self.w is None:
+            h = np.ones_like(g)
+        else:
+            g = (g * self.w).astype(np.float32)  # f32 product
+            h = self.w.copy()
         return g[None, :], h[None, :]
 
     def boost_from_score(self, k):
-        suml = 0.0
-        for v in self.label.astype(np.float64):
-            suml += v
-        return suml / len(self.label)
+        if self.w is None:
+            suml = 0.0
+            for v in self.label.astype(np.float64):
+                suml += v
+            return suml / len(self.label)
+        suml = sumw = 0.0
+        for lab, wt in zip(self.label.astype(np.float64), self.w.astype(np.float64)):
+            suml = _madd(float(lab), float(wt), suml, self.fused)
+            sumw += float(wt)
+        return suml / sumw
 
 
 class BinaryObjective:
-    """objective/binary.rs:71-115 (sigmoid 1, no weights)."""
+    """objective/binary.rs:71-115 (sigmoid, optional weights)."""
     constant_hessian = False
     num_class = 1
 
-    def __init__(self, label, sigmoid=1.0):
+    def __init__(self, label, sigmoid=1.0, weights=None):
         self.is_pos = np.asarray(label, dtype=np.float32) > 0
         self.s = float(sigmoid)
+        self.w = None if weights is None else np.asarray(weights, dtype=np.float32)
 
     def gradients(self, score):
         n = len(score)
@@ -174,32 +196,50 @@ class BinaryObjective:
             label = 1.0 if self.is_pos[i] else -1.0
             response = -label * s / (1.0 + math.exp(label * s * float(score[i])))
             ar = abs(response)
-            g[i] = np.float32(response * 1.0)
-            h[i] = np.float32(ar * (s - ar) * 1.0)
+            if self.w is None:
+                g[i] = np.float32(response * 1.0)
+                h[i] = np.float32(ar * (s - ar) * 1.0)
+            else:
+                w = float(self.w[i])
+                g[i] = np.float32(response * 1.0 * w)
+                h[i] = np.float32(ar * (s - ar) * 1.0 * w)
         return g[None, :], h[None, :]
 
     def boost_from_score(self, k):
         suml = 0.0
-        for p in self.is_pos:
-            suml += 1.0 if p else 0.0
-        sumw = float(len(self.is_pos))
-        pavg = min(max(suml / sumw, EPS), 1.0 - EPS)
+        if self.w is None:
+            for p in self.is_pos:
+                suml += 1.0 if p else 0.0
+            sumw = float(len(self.is_pos))
+        else:
+            sumw = 0.0
+            for p, w in zip(self.is_pos, self.w):
+                suml += float(np.float32(1.0 if p else 0.0) * w)  # an f32 product, widened
+                sumw += float(w)
         pavg = max(min(suml / sumw, 1.0 - EPS), EPS)
         return math.log(pavg / (1.0 - pavg)) / self.s
 
 
 class SoftmaxObjective:
-    """objective/multiclass.rs:20-110 (no weights)."""
+    """objective/multiclass.rs:20-110 (optional weights)."""
     constant_hessian = False
 
-    def __init__(self, label, num_class):
+    def __init__(self, label, num_class, weights=None):
         self.num_class = num_class
         self.label_int = np.asarray(label, dtype=np.float32).astype(np.int64)
         self.factor = num_class / (num_class - 1.0)
-        probs = np.zeros(num_class)
-        for v in self.label_int:
-            probs[v] += 1.0
-        self.init_probs = probs / float(len(self.label_int))
+        self.w = None if weights is None else np.asarray(weights, dtype=np.float32)
+        probs = [0.0] * num_class
+        if self.w is None:
+            for v in self.label_int:
+                probs[v] += 1.0
+            sum_weight = float(len(self.label_int))
+        else:
+            sum_weight = 0.0
+            for v, w in zip(self.label_int, self.w):
+                probs[v] += float(w)
+                sum_weight += float(w)
+        self.init_probs = np.array([pr / sum_weight for pr in probs])
 
     def gradients(self, score):
         K = self.num_class
@@ -221,6 +261,9 @@ class SoftmaxObjective:
                 p = rec[k]
                 gi = p - 1.0 if self.label_int[i] == k else p
                 hi = self.factor * p * (1.0 - p)
+                if self.w is not None:
+                    w = float(self.w[i])
+                    gi, hi = gi * w, hi * w
                 g[k, i] = np.float32(gi)
                 h[k, i] = np.float32(hi)
         return g, h
@@ -233,14 +276,14 @@ class SoftmaxObjective:
         return not (p <= EPS or p >= 1.0 - EPS)
 
 
-def make_objective(params, y):
+def make_objective(params, y, weights=None, fused=True):
     obj = params.get("objective", "regression")
     if obj in ("regression", "l2", "regression_l2", "mse"):
-        return L2Objective(y)
+        return L2Objective(y, weights, fused)
     if obj == "binary":
-        return BinaryObjective(y, params.get("sigmoid", 1.0))
+        return BinaryObjective(y, params.get("sigmoid", 1.0), weights)
     if obj in ("multiclass", "softmax"):
-        return SoftmaxObjective(y, int(params["num_class"]))
+        return SoftmaxObjective(y, int(params["num_class"]), weights)
     raise ValueError("objective %r is outside the learner's scope" % obj)
 
 

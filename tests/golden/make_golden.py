@@ -6,7 +6,7 @@ Run in a container that has the reference at REFERENCE (default /root/reference)
 
 It copies, unchanged, the reference's own golden data for the tree-learner path:
 
-* ``train/<case>/{x.npy,y.npy,params.json,model.txt}`` — upstream-LightGBM 4.7.0 models that the
+* ``train/<case>/{x.npy,y.npy[,w.npy],params.json,model.txt}`` — upstream-LightGBM 4.7.0 models that the
   reference reproduces byte for byte (tests/fixtures/train, generated on darwin/arm64 with
   ``deterministic, num_threads=1, force_col_wise, seed=7``), for the cases inside this learner's
   scope (dense numerical and categorical features, L2 / binary / multiclass objectives; plain
@@ -34,7 +34,8 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 CASES = ["binary", "l2_default", "l2_nan", "l2_zero", "l2_zero_as_missing", "l2_small", "l2_regularized",
          "l2_max_delta_smooth", "l2_max_depth", "l2_no_boost_from_average", "multiclass", "bagging",
          "bagging_no_freq", "bagging_feature_fraction", "feature_fraction", "cat_default", "cat_binary", "cat_nan",
-         "cat_onehot", "cat_regularized", "cat_bagging"]
+         "cat_onehot", "cat_regularized", "cat_bagging", "l2_default_weighted", "binary_weighted",
+         "multiclass_weighted", "bagging_weighted", "cat_default_weighted"]
 
 
 def _ints(text):
@@ -47,7 +48,9 @@ def main(ref):
         src = os.path.join(fx, "train", case)
         dst = os.path.join(HERE, "train", case)
         os.makedirs(dst, exist_ok=True)
-        for name in ("x.npy", "y.npy", "params.json", "model.txt"):
+        for name in ("x.npy", "y.npy", "w.npy", "params.json", "model.txt"):
+            if name == "w.npy" and not os.path.exists(os.path.join(src, name)):
+                continue  # sample weights only where the case has them
             shutil.copyfile(os.path.join(src, name), os.path.join(dst, name))
     shutil.copyfile(os.path.join(fx, "quantized_gradients.json"), os.path.join(HERE, "quantized_gradients.json"))
 

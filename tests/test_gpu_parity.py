@@ -251,10 +251,12 @@ def test_gpu_reproduces_reference_models(oracle, case):
     p = P["params"]
     X = np.load(os.path.join(d, "x.npy"))
     y = np.load(os.path.join(d, "y.npy"))
+    wp = os.path.join(d, "w.npy")
+    weights = np.load(wp) if os.path.exists(wp) else None
     ds = BinnedDataset.from_dense(X, max_bin=p.get("max_bin", 255), min_data_in_leaf=p.get("min_data_in_leaf", 20),
                                   zero_as_missing=p.get("zero_as_missing", False),
                                   categorical=P.get("categorical", []))
-    obj = oracle.make_objective(p, y)
+    obj = oracle.make_objective(p, y, weights, fused=True)
     cfg = LearnerConfig(**p, fused_madd=1, is_constant_hessian=int(obj.constant_hessian))
     learner = GpuTreeLearner(ds, cfg)
     model = open(os.path.join(d, "model.txt")).read()

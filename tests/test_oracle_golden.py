@@ -25,6 +25,8 @@ def _load_case(case):
     P = json.load(open(os.path.join(d, "params.json")))
     X = np.load(os.path.join(d, "x.npy"))
     y = np.load(os.path.join(d, "y.npy"))
+    wp = os.path.join(d, "w.npy")
+    P["weights"] = np.load(wp) if os.path.exists(wp) else None
     model = open(os.path.join(d, "model.txt")).read()
     return P, X, y, model
 
@@ -42,7 +44,7 @@ def test_oracle_reproduces_reference_models(oracle, bklib, case, fused):
     P, X, y, model = _load_case(case)
     p = P["params"]
     ds = _dataset(p, X, P.get("categorical", []))
-    obj = oracle.make_objective(p, y)
+    obj = oracle.make_objective(p, y, P["weights"], fused=bool(fused))
     cfg = LearnerConfig(**p, fused_madd=fused, is_constant_hessian=int(obj.constant_hessian))
     learner = oracle.OracleLearner(ds, cfg)
     cols, bag = oracle.samplers_from_params(oracle.resolved_params(model), ds)
