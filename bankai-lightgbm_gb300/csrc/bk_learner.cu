@@ -748,8 +748,10 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
         best = c;
       }
     };
-    for (int mr : {64, 128, 512, 1024}) consider({mr, best[1], best[2]});
-    consider({best[0], 2 * sms / T, best[2]});
+    // rows per histogram CTA: small values spread small leaves over more SMs; large ones give
+    // mid-size leaves fewer CTAs, so fewer shared histograms to flush into the pool slot
+    for (int mr : {64, 128, 512, 1024, 2048, 4096, 8192, 16384}) consider({mr, best[1], best[2]});
+    for (int ct : {2 * sms / T, sms / (2 * T)}) consider({best[0], ct, best[2]});
     for (int pg : {sms, 4 * sms}) consider({best[0], best[1], pg});
     CK(cudaMemcpyAsync(L->jobs[0].st, saved, state_bytes, cudaMemcpyDeviceToDevice, L->stream));
     CK(cudaFreeAsync(saved, L->stream));
