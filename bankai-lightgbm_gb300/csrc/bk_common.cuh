@@ -72,7 +72,8 @@ struct Params {
   int64_t n;
   // CatParams of the categorical search (feature_histogram.rs:1146-1163)
   double cat_smooth, cat_l2;
-  int32_t max_cat_threshold, max_cat_to_onehot, min_data_per_group, _p2;
+  int32_t max_cat_threshold, max_cat_to_onehot, min_data_per_group;
+  int32_t bynode;  // 1: every searched leaf draws a by-node feature sample (Job::used[F..3F))
 };
 
 // Per-leaf constants of one searched leaf (FindBestThreshold's preamble, feature_histogram.rs:
@@ -105,6 +106,11 @@ struct JobState {
   int32_t mt_idx, _p1;
   int64_t hist_rows_direct, hist_rows_gather, hist_builds;  // work done by the histogram kernels
   uint32_t search_done, part_done;  // CTAs finished in the current search / scatter launch
+  // by-node column sample (col_sampler.rs:109-177): the sampler's LCG state, whether a by-tree
+  // sample is active, the by-node fraction
+  uint32_t col_rng;
+  int32_t bytree_on;
+  double bynode_fraction;
   uint32_t mt[624];
 };
 
@@ -134,7 +140,8 @@ struct Job {
   int64_t* bsplit;     // [L]   inner feature << 32 | threshold | default_left << 31 of each leaf's best split
   LeafConst* lconst;   // [2]   constants of the smaller / larger leaf of the current search
   uint8_t* splittable; // [L][F]
-  uint8_t* used;       // [F]   features searched in the current step
+  uint8_t* used;       // [4][F] features searched in the current step; the by-node samples of the
+                       //        smaller / larger leaf; the sample's scratch
   uint8_t* tree_mask;  // [F]   features the tree may split on (by-tree column sample), 1 by default
   bk_split* records;   // [L-1]
   double* leaf_value;  // [L]

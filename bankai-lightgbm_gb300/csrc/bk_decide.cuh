@@ -159,9 +159,11 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
       const double g = __ldcg(&J.cgain[side * p.F + f]);
       const uint32_t th = __ldcg(&J.cthr[side * p.F + f]);
       const int real = feats[f].real;
+      // serial.rs:1538-1554: the by-node sample gates only the fold, not the splittable flags
+      const uint8_t nm = p.bynode ? __ldcg(&J.used[(size_t)(1 + side) * p.F + f]) : (uint8_t)1;
       if (!searched || leaf < 0 || !u) continue;
       if (record) J.splittable[(size_t)slot * p.F + f] = cs;
-      pick(a, make_pick(f, g, real, th));
+      if (nm) pick(a, make_pick(f, g, real, th));
     }
   }
   // split_info.rs:125-133 — first arg-max leaf under better_than; the searched leaves' new bests

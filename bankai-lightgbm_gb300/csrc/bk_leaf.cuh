@@ -111,6 +111,62 @@ __device__ __forceinline__ void compute_leaf_const(const Job& J, const Params& p
   compute_leaf_const_ls(J, p, st, side, J.leaf_sum[leaf], st->tree_leaves == 1, lane);
 }
 
+// ColSampler::get_by_node (col_sampler.rs:109-177, no interaction constraints) for side `side` of
+// the coming search, on one thread: Random::sample (utils/random.rs:53-80) of get_cnt(n, fraction)
+// positions among the n candidates — the tree's by-tree sample (ascending inner features) when one
+// is active, else every feature — continuing the sampler's LCG stream kept in the job state.
+__device__ __forceinline__ uint32_t lcg_step(uint32_t x) { return x * 214013u + 2531011u; }
+
+__device__ __forceinline__ void draw_node_sample(const Job& J, const Params& p, JobState* st, int side) {
+  uint8_t* out = J.used + (size_t)(1 + side) * p.F;
+  uint8_t* sel = J.used + (size_t)3 * p.F;
+  const bool bytree = st->bytree_on != 0;
+  int32_t n = 0;
+  for (int f = 0; f < p.F; ++f) {
+    out[f] = 0;
+    sel[f] = 0;
+    n += (!bytree || J.tree_mask[f]) ? 1 : 0;
+  }
+  const int32_t used = (int32_t)((double)n * st->bynode_fraction + 0.5);
+  const int32_t k = used > (n < 1 ? n : 1) ? used : (n < 1 ? n : 1);
+  uint32_t x = st->col_rng;
+  if (k > n || k <= 0) {
+    // no position is drawn
+  } else if (k == n) {
+    for (int32_t q = 0; q < n; ++q) sel[q] = 1;
+  } else if (k > 1 && (double)k > (double)n / ((k & (k - 1)) == 0 ? (double)(31 - __clz(k)) : log2((double)k))) {
+    int32_t got = 0;
+    for (int32_t i = 0; i < n; ++i) {
+      x = lcg_step(x);
+      const float r = (float)((x >> 16) & 0x7fffu) / 32768.0f;
+      const double prob = (double)(k - got) / (double)(n - i);
+      if ((double)r < prob) {
+        sel[i] = 1;
+        ++got;
+      }
+    }
+  } else {
+    for (int32_t r = n - k; r < n; ++r) {
+      x = lcg_step(x);
+      const int32_t v = (int32_t)(x & 0x7fffffffu) % (r + 1);
+      if (sel[v]) sel[r] = 1;
+      else sel[v] = 1;
+    }
+  }
+  st->col_rng = x;
+  for (int32_t f = 0, q = 0; f < p.F; ++f) {
+    if (bytree && !J.tree_mask[f]) continue;
+    out[f] = sel[q++];
+  }
+}
+
+// The by-node samples of a search: the smaller leaf's, then the larger leaf's (serial.rs:1328-1336).
+__device__ __forceinline__ void draw_node_samples(const Job& J, const Params& p, bool larger) {
+  JobState* st = J.st;
+  draw_node_sample(J, p, st, 0);
+  if (larger) draw_node_sample(J, p, st, 1);
+}
+
 // The histogram CTA that does the serial side work of its launch: the last CTA of tile 0, idle for
 // leaves that do not need the whole grid.
 __device__ __forceinline__ bool hist_side_cta() { return blockIdx.x == gridDim.x - 1 && blockIdx.y == 0; }
@@ -118,9 +174,13 @@ __device__ __forceinline__ bool hist_side_cta() { return blockIdx.x == gridDim.x
 // Called by every thread of a histogram CTA before its row loop: the side CTA computes both sides'
 // constants with its first two warps, from the leaf records.
 __device__ __forceinline__ void hist_leaf_constants(const Job& J, const Params& p) {
-  if (!hist_side_cta() || threadIdx.x >= 64) return;
+  if (!hist_side_cta() || threadIdx.x >= 128) return;
   const JobState* st = J.st;
   if (st->stop || !st->do_search) return;
+  if (threadIdx.x >= 64) {
+    if (p.bynode && threadIdx.x == 96) draw_node_samples(J, p, st->larger_leaf >= 0);
+    return;
+  }
   compute_leaf_const(J, p, st, (int)(threadIdx.x >> 5), (int)(threadIdx.x & 31));
 }
 
@@ -128,13 +188,17 @@ __device__ __forceinline__ void hist_leaf_constants(const Job& J, const Params& 
 // to the histogram launch): the side CTA's warps 0 / 1 compute the constants from the split's
 // candidate record and row counts, warp 2 writes the split's bookkeeping.
 __device__ __forceinline__ void hist_apply_split(const Job& J, const Params& p, const SplitOutcome& o) {
-  if (!hist_side_cta() || threadIdx.x >= 96) return;
+  if (!hist_side_cta() || threadIdx.x >= 128) return;
   const int warp = (int)(threadIdx.x >> 5), lane = (int)(threadIdx.x & 31);
   if (warp == 2) {
     post_split_writes(J, p, o, lane);
     return;
   }
   if (!o.go) return;
+  if (warp == 3) {
+    if (p.bynode && lane == 0) draw_node_samples(J, p, true);
+    return;
+  }
   const JobState* st = J.st;
   const Cand& info = J.cand[(size_t)o.bl * p.F + st->split_inner];
   LeafSum small, large;

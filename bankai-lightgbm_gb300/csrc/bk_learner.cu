@@ -499,7 +499,8 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
       J.bsplit = L->dalloc<int64_t>(Lv);
       J.lconst = L->dalloc<LeafConst>(2);
       J.splittable = L->dalloc<uint8_t>((size_t)Lv * F);
-      J.used = L->dalloc<uint8_t>(F);
+      J.used = L->dalloc<uint8_t>(4 * (size_t)F);
+      CK(cudaMemset(J.used, 1, 4 * (size_t)F));
       J.tree_mask = L->dalloc<uint8_t>(F);
       CK(cudaMemset(J.tree_mask, 1, F));
       J.records = L->dalloc<bk_split>(Lv);
@@ -975,6 +976,50 @@ int bk_learner_set_feature_mask(bk_learner* L, const uint8_t* mask) {
   } catch (const CudaError& e) {
     return fail_cuda(e);
   }
+  return 0;
+}
+
+int bk_learner_set_bynode(bk_learner* L, double fraction, int32_t bytree_active, uint32_t rng_state) {
+  if (!L) {
+    set_error("bk_learner_set_bynode: null learner");
+    return -1;
+  }
+  const bool on = fraction < 1.0;
+  if (on && L->K != 1) {
+    set_error("bk_learner_set_bynode: by-node sampling continues one sampler's stream across trees, which "
+              "needs one tree per train call (num_jobs 1)");
+    return -1;
+  }
+  if (on && !(fraction > 0.0)) {
+    set_error("bk_learner_set_bynode: fraction must be in (0, 1]");
+    return -1;
+  }
+  try {
+    JobState* st = L->jobs[0].st;
+    L->h_state[0].col_rng = rng_state;
+    L->h_state[0].bytree_on = bytree_active ? 1 : 0;
+    L->h_state[0].bynode_fraction = fraction;
+    CK(cudaMemcpyAsync(&st->col_rng, &L->h_state[0].col_rng,
+                       offsetof(JobState, bynode_fraction) + sizeof(double) - offsetof(JobState, col_rng),
+                       cudaMemcpyHostToDevice, L->stream));
+    CK(cudaStreamSynchronize(L->stream));
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
+  }
+  if ((on ? 1 : 0) != L->p.bynode && L->graph_exec) {
+    cudaGraphExecDestroy(L->graph_exec);
+    L->graph_exec = nullptr;
+  }
+  L->p.bynode = on ? 1 : 0;
+  return 0;
+}
+
+int bk_learner_bynode_state(bk_learner* L, uint32_t* rng_state) {
+  if (!L || !rng_state) {
+    set_error("bk_learner_bynode_state: invalid arguments");
+    return -1;
+  }
+  *rng_state = L->h_state[0].col_rng;  // copied back with the job state at the end of each train call
   return 0;
 }
 

@@ -67,6 +67,18 @@ class GpuTreeLearner:
                                  dtype=np.uint8)
         _lib.check(self.lib.bk_learner_set_feature_mask(self.h, m.ctypes.data), "bk_learner_set_feature_mask")
 
+    def set_bynode(self, fraction, bytree_active, rng_state):
+        """The by-node column sample of the following trees (ColSampler::get_by_node,
+        treelearner/col_sampler.rs:109-177) drawn on the device, continuing the sampler's LCG
+        state ``rng_state`` (after the host's by-tree draw)."""
+        _lib.check(self.lib.bk_learner_set_bynode(self.h, float(fraction), int(bool(bytree_active)),
+                                                  int(rng_state) & 0xFFFFFFFF), "bk_learner_set_bynode")
+
+    def bynode_state(self):
+        out = ctypes.c_uint32()
+        _lib.check(self.lib.bk_learner_bynode_state(self.h, ctypes.byref(out)), "bk_learner_bynode_state")
+        return int(out.value)
+
     def autotune(self, gradients, hessians, on_device=False, trials=2):
         """Picks the grow-loop launch shape by timing whole trees grown from these gradients
         (bk_learner_autotune; cached per dataset shape class). Returns the chosen shape

@@ -147,6 +147,21 @@ int bk_learner_set_launch_overlap(bk_learner* learner, int32_t on);
  * tree, as the reference draws one per train call), or NULL for "every feature". */
 int bk_learner_set_feature_mask(bk_learner* learner, const uint8_t* mask);
 
+/* The by-node column sample (ColSampler::get_by_node, treelearner/col_sampler.rs:109-177, without
+ * interaction constraints) of the following train calls: every searched leaf — the smaller one,
+ * then the larger one, at every split — draws Random::sample(n, get_cnt(n, fraction)) of its
+ * candidate features on the device, the candidates being the tree's by-tree sample (the
+ * bk_learner_set_feature_mask mask) when bytree_active, else every feature; a leaf's best split
+ * comes only from its sample (serial.rs:1328-1336, :1538-1554). rng_state is the sampler's LCG
+ * state after the host's by-tree draw for the coming tree; the state after the tree's by-node
+ * draws is read back with bk_learner_bynode_state, so the host's next by-tree draw continues the
+ * same stream. fraction >= 1 turns it off. Needs num_jobs == 1 (the reference draws the K class
+ * trees' samples from one stream, one tree after the other). */
+int bk_learner_set_bynode(bk_learner* learner, double fraction, int32_t bytree_active, uint32_t rng_state);
+
+/* The by-node sampler's LCG state after the last train call. */
+int bk_learner_bynode_state(bk_learner* learner, uint32_t* rng_state);
+
 /* Launch-shape autotuner (GB300-only, no reference counterpart; results never depend on it).
  * Times whole trees (graph form, median of `trials` after one untimed tree per shape) grown from
  * the given gradients (as bk_learner_train takes them, all rows) over a coordinate descent of

@@ -45,6 +45,9 @@ def load():
         lib.orc_learner_create.argtypes = [P, i32, P, i64, P]
         lib.orc_learner_destroy.argtypes = [P]
         lib.orc_learner_set_feature_mask.argtypes = [P, P]
+        lib.orc_learner_set_bynode.argtypes = [P, ctypes.c_double, i32, u32]
+        lib.orc_learner_bynode_state.restype = u32
+        lib.orc_learner_bynode_state.argtypes = [P]
         lib.orc_learner_train.restype = i32
         lib.orc_learner_train.argtypes = [P, P, P, P, i64, P, P]
         lib.orc_learner_root_output.restype = ctypes.c_double
@@ -114,6 +117,12 @@ class OracleLearner:
             self._mask = np.ascontiguousarray(np.asarray(mask, dtype=bool).reshape(-1), dtype=np.uint8)
             assert len(self._mask) == self.ds.num_features
         self.lib.orc_learner_set_feature_mask(self.h, _ptr(self._mask))
+
+    def set_bynode(self, fraction, bytree_active, rng_state):
+        self.lib.orc_learner_set_bynode(self.h, float(fraction), int(bool(bytree_active)), int(rng_state))
+
+    def bynode_state(self):
+        return int(self.lib.orc_learner_bynode_state(self.h))
 
     def row_leaf(self):
         out = np.zeros(self.ds.num_data, dtype=np.int32)
@@ -291,17 +300,31 @@ def make_objective(params, y, weights=None, fused=True):
 # row and column sampling (the Trainer's side of the learner's `rows` / feature-mask inputs)
 # ------------------------------------------------------------------------------------------
 class TreeColumnSampler:
-    """The by-tree part of ColSampler (treelearner/col_sampler.rs:9-108): one draw when the learner
-    is built, then one per tree (serial.rs:678). Features are the learner's inner features, which
-    follow the real-index order of the used features."""
+    """ColSampler (treelearner/col_sampler.rs:9-177, no interaction constraints): the by-tree draw
+    once when the learner is built and once per tree (serial.rs:678) on the host; the by-node draws
+    of a tree (one per searched leaf) by the learner, continuing the same LCG stream. Features are
+    the learner's inner features, which follow the real-index order of the used features."""
 
-    def __init__(self, num_features, fraction, seed):
+    def __init__(self, num_features, fraction, seed, fraction_bynode=1.0):
         self.nf = num_features
         self.rand = LcgRandom(seed)
         self.active = fraction < 1.0
+        self.bynode = float(fraction_bynode)
         self.cnt = max(min(1, num_features), int(num_features * fraction + 0.5)) if self.active else num_features
         self.mask = np.ones(num_features, dtype=bool)
         self.reset_by_tree()
+
+    def before_tree(self, learner):
+        """reset_by_tree on the host, then the learner draws the by-node samples of the tree from the
+        same LCG stream; after the tree the host continues from the learner's state."""
+        mask = self.reset_by_tree()
+        learner.set_feature_mask(mask)
+        if self.bynode < 1.0:
+            learner.set_bynode(self.bynode, self.active, self.rand.x)
+
+    def after_tree(self, learner):
+        if self.bynode < 1.0:
+            self.rand.x = learner.bynode_state()
 
     def reset_by_tree(self):
         if self.active:
@@ -347,12 +370,11 @@ def resolved_params(model_text):
 
 
 def samplers_from_params(resolved, ds):
-    """(TreeColumnSampler or None, RowBagging or None) for a resolved config; by-node sampling is
-    outside the learner's interface."""
-    if float(resolved.get("feature_fraction_bynode", 1)) < 1.0:
-        raise NotImplementedError("feature_fraction_bynode draws per node inside the grow loop")
+    """(TreeColumnSampler or None, RowBagging or None) for a resolved config."""
     ff = float(resolved.get("feature_fraction", 1))
-    cols = TreeColumnSampler(ds.num_features, ff, int(resolved.get("feature_fraction_seed", 2))) if ff < 1 else None
+    fn = float(resolved.get("feature_fraction_bynode", 1))
+    cols = (TreeColumnSampler(ds.num_features, ff, int(resolved.get("feature_fraction_seed", 2)), fn)
+            if ff < 1 or fn < 1 else None)
     bag = RowBagging(ds.num_data, float(resolved.get("bagging_fraction", 1)), int(resolved.get("bagging_freq", 0)),
                      int(resolved.get("bagging_seed", 3)))
     return cols, (bag if bag.active else None)
@@ -414,8 +436,10 @@ def train_gbdt(learner, ds, objective, rounds, learning_rate=0.1, boost_from_ave
             if not need:
                 raise NotImplementedError("constant class trees are outside the learner's scope")
             if col_sampler is not None:
-                learner.set_feature_mask(col_sampler.reset_by_tree())
+                col_sampler.before_tree(learner)
             recs, leaf_values, root = learner.train(g[k], h[k], rows)
+            if col_sampler is not None:
+                col_sampler.after_tree(learner)
             t = Tree.from_records(learner.num_leaves, recs, leaf_values, root, ds.features, min_gain_to_split)
             if t.num_leaves > 1:
                 cont = True

@@ -893,6 +893,48 @@ static void route_table_cat(const FeatureMeta& m, const uint32_t* bits, int32_t 
   for (int32_t b = 0; b < group_bins; ++b) lut[b] = b == 0 ? (default_left ? 1 : 0) : (in_bits((uint32_t)b - 1 + offset) ? 1 : 0);
 }
 
+// utils/random.rs:6-80 — LightGBM's LCG and its k-of-n sample, for the by-node column sample.
+struct Lcg {
+  uint32_t x = 0;
+  uint32_t step() {
+    x = x * 214013u + 2531011u;
+    return x;
+  }
+  int32_t next_int(int32_t lo, int32_t hi) { return (int32_t)(step() & 0x7fffffffu) % (hi - lo) + lo; }
+  float next_float() { return (float)((step() >> 16) & 0x7fffu) / 32768.0f; }
+  std::vector<int32_t> sample(int32_t n, int32_t k) {
+    std::vector<int32_t> ret;
+    if (k > n || k <= 0) return ret;
+    if (k == n) {
+      for (int32_t i = 0; i < n; ++i) ret.push_back(i);
+      return ret;
+    }
+    if (k > 1 && (double)k > (double)n / std::log2((double)k)) {
+      for (int32_t i = 0; i < n; ++i) {
+        const double prob = (double)(k - (int32_t)ret.size()) / (double)(n - i);
+        if ((double)next_float() < prob) ret.push_back(i);
+      }
+      return ret;
+    }
+    std::vector<uint8_t> in((size_t)n, 0);
+    for (int32_t r = n - k; r < n; ++r) {
+      const int32_t v = next_int(0, r + 1);
+      if (in[(size_t)v]) in[(size_t)r] = 1;
+      else in[(size_t)v] = 1;
+    }
+    for (int32_t i = 0; i < n; ++i)
+      if (in[(size_t)i]) ret.push_back(i);
+    return ret;
+  }
+};
+
+// col_sampler.rs:14-20 — GetCnt.
+static int32_t col_get_cnt(int32_t total, double fraction) {
+  const int32_t mn = std::min(1, total);
+  const int32_t used = (int32_t)((double)total * fraction + 0.5);
+  return std::max(used, mn);
+}
+
 static void bitset_of(const std::vector<uint32_t>& vals, uint32_t* bits) {
   for (int i = 0; i < 8; ++i) bits[i] = 0;
   for (uint32_t v : vals)
@@ -1022,6 +1064,30 @@ struct Learner {
   double root_output = 0.0;
   std::vector<float> og, oh;
   std::vector<uint8_t> tree_mask;  // empty: every feature is used by the tree
+  // by-node column sample (col_sampler.rs:109-177 without interaction constraints)
+  double bynode_fraction = 1.0;
+  bool bytree_active = false;
+  Lcg node_rng;
+
+  // ColSampler::get_by_node: the features a searched leaf may split on
+  std::vector<uint8_t> node_mask() {
+    std::vector<uint8_t> ret((size_t)nf, 0);
+    if (bynode_fraction >= 1.0) {
+      std::fill(ret.begin(), ret.end(), 1);
+      return ret;
+    }
+    if (bytree_active) {
+      std::vector<int32_t> used_list;  // the by-tree sample, ascending
+      for (int32_t f = 0; f < nf; ++f)
+        if (tree_mask.empty() || tree_mask[(size_t)f]) used_list.push_back(f);
+      const int32_t cnt = col_get_cnt((int32_t)used_list.size(), bynode_fraction);
+      for (int32_t q : node_rng.sample((int32_t)used_list.size(), cnt)) ret[(size_t)used_list[(size_t)q]] = 1;
+    } else {
+      const int32_t cnt = col_get_cnt(nf, bynode_fraction);
+      for (int32_t q : node_rng.sample(nf, cnt)) ret[(size_t)q] = 1;
+    }
+    return ret;
+  }
   Pool* workers = nullptr;
   ~Learner() { delete workers; }
 
@@ -1158,6 +1224,9 @@ struct Learner {
   void find_best_splits_from_histograms(const std::vector<uint8_t>& used, bool use_subtract, double sp_out,
                                         double lp_out) {
     int32_t lslot = larger.leaf >= 0 ? larger_slot : -1;
+    // serial.rs:1328-1336 — the by-node samples of the smaller leaf, then the larger one
+    const std::vector<uint8_t> smask = node_mask();
+    const std::vector<uint8_t> lmask = larger.leaf >= 0 ? node_mask() : std::vector<uint8_t>((size_t)nf, 1);
     std::vector<SplitInfo> cs_all(nf), cl_all(nf);
     std::vector<uint8_t> ss_all(nf, 0), sl_all(nf, 0);
     workers->run(nf, [&](int f) {
@@ -1224,10 +1293,10 @@ struct Learner {
     for (int f = 0; f < nf; ++f) {
       if (!used[f]) continue;
       splittable[smaller_slot][f] = ss_all[f];
-      if (cs_all[f].better_than(sbest)) sbest = cs_all[f];
+      if (smask[(size_t)f] && cs_all[f].better_than(sbest)) sbest = cs_all[f];
       if (lslot >= 0) {
         splittable[lslot][f] = sl_all[f];
-        if (cl_all[f].better_than(lbest)) lbest = cl_all[f];
+        if (lmask[(size_t)f] && cl_all[f].better_than(lbest)) lbest = cl_all[f];
       }
     }
     best[smaller.leaf] = sbest;
@@ -1539,6 +1608,19 @@ void* orc_learner_create(const orc_feature* feats, int32_t nf, const uint8_t* bi
 }
 
 void orc_learner_destroy(void* h) { delete (Learner*)h; }
+
+// The by-node column sample of the following trees: fraction_bynode (>= 1: off), whether a by-tree
+// sample is active (the by-node draw then picks among its features) and the sampler's LCG state
+// after the host's by-tree draw.
+void orc_learner_set_bynode(void* h, double fraction, int32_t bytree_active, uint32_t rng_state) {
+  Learner* L = (Learner*)h;
+  L->bynode_fraction = fraction;
+  L->bytree_active = bytree_active != 0;
+  L->node_rng.x = rng_state;
+}
+
+// The LCG state after the last tree's by-node draws.
+uint32_t orc_learner_bynode_state(void* h) { return ((Learner*)h)->node_rng.x; }
 
 // The features the following trees may split on (ColSampler::reset_by_tree, col_sampler.rs:87-103):
 // mask[f] != 0 for every used inner feature f; NULL restores "all features".

@@ -35,7 +35,8 @@ CASES = ["binary", "l2_default", "l2_nan", "l2_zero", "l2_zero_as_missing", "l2_
          "l2_max_delta_smooth", "l2_max_depth", "l2_no_boost_from_average", "multiclass", "bagging",
          "bagging_no_freq", "bagging_feature_fraction", "feature_fraction", "cat_default", "cat_binary", "cat_nan",
          "cat_onehot", "cat_regularized", "cat_bagging", "l2_default_weighted", "binary_weighted",
-         "multiclass_weighted", "bagging_weighted", "cat_default_weighted"]
+         "multiclass_weighted", "bagging_weighted", "cat_default_weighted", "feature_fraction_bynode",
+         "feature_fraction_both"]
 
 
 def _ints(text):

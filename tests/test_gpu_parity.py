@@ -401,3 +401,29 @@ def test_categorical_trees(case):
             print("float near-tie divergences:", divergences)
             assert len(divergences) <= 1
             gpu.close()
+
+
+@pytest.mark.parametrize("bytree", [False, True])
+def test_bynode_column_sample(bytree):
+    """bk_learner_set_bynode: every searched leaf draws its feature sample on the device from the
+    sampler's LCG stream; trees (quantized, bit-exact) and the stream's state after each tree
+    equal the oracle's, with and without a by-tree sample."""
+    import harness
+    ds, z = _dataset(20000, 60, seed=31)
+    g, h, const = _grads(z, "binary", seed=32)
+    cfg = dict(num_leaves=31, use_quantized_grad=1, stochastic_rounding=1, seed=5, num_threads=2)
+    orc, gpu, _ = _learners(ds, const, **cfg)
+    cols_o = harness.TreeColumnSampler(ds.num_features, 0.7 if bytree else 1.0, 9, 0.35)
+    cols_g = harness.TreeColumnSampler(ds.num_features, 0.7 if bytree else 1.0, 9, 0.35)
+    for it in range(3):
+        cols_o.before_tree(orc)
+        cols_g.before_tree(gpu)
+        ro, rg = orc.train(g, h), gpu.train(g, h)
+        cols_o.after_tree(orc)
+        cols_g.after_tree(gpu)
+        _assert_records_equal(ro[0], rg[0])
+        assert np.array_equal(ro[1], rg[1])
+        assert cols_o.rand.x == cols_g.rand.x, "sampler state after tree %d" % it
+        g = (g * 0.9).astype(np.float32)
+    gpu.set_bynode(1.0, False, 0)
+    gpu.close()
