@@ -358,6 +358,46 @@ class RowBagging:
         return self.bag if len(self.bag) < self.n else None
 
 
+class Goss:
+    """GOSS row sampling (boosting/sample.rs Goss::draw, one tree per iteration): no sampling for
+    the first int(1 / learning_rate) iterations; then the rows whose |g * h| (f32) reaches the
+    top_rate-th largest value, plus a draw of the rest (one LCG per 1024-row block) whose
+    gradients and hessians are scaled by (n - top_k) / other_k in f32."""
+    BLOCK = 1024
+
+    def __init__(self, n, top_rate, other_rate, learning_rate, seed):
+        self.n = n
+        self.top_rate, self.other_rate = float(top_rate), float(other_rate)
+        self.warmup = int(1.0 / float(learning_rate))
+        self.rands = [LcgRandom((int(seed) + b) & 0xFFFFFFFF) for b in range((n + self.BLOCK - 1) // self.BLOCK)]
+
+    def sample(self, it, g, h):
+        """Returns the rows (or None) and rescales g / h ([1, n] float32) in place."""
+        if it < self.warmup:
+            return None
+        n = self.n
+        tmp = np.abs((g[0] * h[0]).astype(np.float32))
+        top_k = max(int(n * self.top_rate), 1)
+        other_k = int(n * self.other_rate)
+        threshold = np.sort(tmp)[::-1][top_k - 1]
+        multiply = np.float32(np.float32(n - top_k) / np.float32(other_k))
+        bag, big = [], 0
+        for i in range(n):
+            if tmp[i] >= threshold:
+                bag.append(i)
+                big += 1
+            else:
+                rest_need = other_k - (len(bag) - big)
+                rest_all = (n - i) - (top_k - big)
+                prob = rest_need / float(rest_all)
+                if float(self.rands[i // self.BLOCK].next_float()) < prob:
+                    bag.append(i)
+                    g[0, i] = np.float32(g[0, i] * multiply)
+                    h[0, i] = np.float32(h[0, i] * multiply)
+        bag = np.array(bag, dtype=np.int32)
+        return bag if len(bag) < n else None
+
+
 def resolved_params(model_text):
     """The resolved config a model file records in its parameters section (`[name: value]`
     lines), e.g. the seeds upstream derives from `seed`."""
@@ -375,6 +415,9 @@ def samplers_from_params(resolved, ds):
     fn = float(resolved.get("feature_fraction_bynode", 1))
     cols = (TreeColumnSampler(ds.num_features, ff, int(resolved.get("feature_fraction_seed", 2)), fn)
             if ff < 1 or fn < 1 else None)
+    if resolved.get("data_sample_strategy", "bagging") == "goss":
+        return cols, Goss(ds.num_data, float(resolved["top_rate"]), float(resolved["other_rate"]),
+                          float(resolved["learning_rate"]), int(resolved.get("bagging_seed", 3)))
     bag = RowBagging(ds.num_data, float(resolved.get("bagging_fraction", 1)), int(resolved.get("bagging_freq", 0)),
                      int(resolved.get("bagging_seed", 3)))
     return cols, (bag if bag.active else None)
@@ -428,7 +471,10 @@ def train_gbdt(learner, ds, objective, rounds, learning_rate=0.1, boost_from_ave
                     init[k] = v
                     score[k] += v
         g, h = objective.gradients(score[0] if K == 1 else score)
-        rows = bagging.sample(it) if bagging is not None else None
+        if isinstance(bagging, Goss):
+            rows = bagging.sample(it, g, h)
+        else:
+            rows = bagging.sample(it) if bagging is not None else None
         oob = None if rows is None else np.setdiff1d(np.arange(n, dtype=np.int32), rows)
         cont = False
         for k in range(K):

@@ -257,7 +257,8 @@ def test_gpu_reproduces_reference_models(oracle, case):
                                   zero_as_missing=p.get("zero_as_missing", False),
                                   categorical=P.get("categorical", []))
     obj = oracle.make_objective(p, y, weights, fused=True)
-    cfg = LearnerConfig(**p, fused_madd=1, is_constant_hessian=int(obj.constant_hessian))
+    cfg = LearnerConfig(**p, fused_madd=1, is_constant_hessian=int(obj.constant_hessian and
+                                                                       p.get("data_sample_strategy") != "goss"))
     learner = GpuTreeLearner(ds, cfg)
     model = open(os.path.join(d, "model.txt")).read()
     cols, bag = oracle.samplers_from_params(oracle.resolved_params(model), ds)

@@ -45,7 +45,8 @@ def test_oracle_reproduces_reference_models(oracle, bklib, case, fused):
     p = P["params"]
     ds = _dataset(p, X, P.get("categorical", []))
     obj = oracle.make_objective(p, y, P["weights"], fused=bool(fused))
-    cfg = LearnerConfig(**p, fused_madd=fused, is_constant_hessian=int(obj.constant_hessian))
+    cfg = LearnerConfig(**p, fused_madd=fused, is_constant_hessian=int(obj.constant_hessian and
+                                                                       p.get("data_sample_strategy") != "goss"))
     learner = oracle.OracleLearner(ds, cfg)
     cols, bag = oracle.samplers_from_params(oracle.resolved_params(model), ds)
     trees, _ = oracle.train_gbdt(learner, ds, obj, P["num_boost_round"], learning_rate=p.get("learning_rate", 0.1),
