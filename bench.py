@@ -279,8 +279,9 @@ def run_gpu(args, rank, world):
     roof = form(True, 1, args.steps, 1, timing=True)
     plain = form(False, 0, args.steps, args.warmup)
     e2e = form(True, 1, args.steps, 1, e2e=True)
-    multiclass = run_multiclass(args) if args.multiclass_rows > 0 else None
-    batched_jobs = run_batched_jobs(args) if args.batch_jobs > 0 else None
+    multiclass = _side(run_multiclass, args) if args.multiclass_rows > 0 else None
+    batched_jobs = _side(run_batched_jobs, args) if args.batch_jobs > 0 else None
+    binary = _side(run_binary, args) if args.binary_rows > 0 else None
     ms, value = aggregate_ranks(main["ms_per_step"], world)
     hist_gbs = roof["hist_bytes"] / (roof["hist_ms"] * 1e6) if roof["hist_ms"] > 0 else None
     hist_launches = (args.leaves - 1) * args.steps  # one histogram launch per split step of a tree
@@ -307,7 +308,7 @@ def run_gpu(args, rank, world):
                                            "iterations": plain["iterations"],
                                            "launch_shape": _shape_dict(shapes.get((False, 0)), args.autotune)},
                   "heldout_l2_delta": main["heldout_l2"] - plain["heldout_l2"], "heldout_rows": m_ho,
-                  "multiclass_k10": multiclass, "batched_jobs": batched_jobs},
+                  "multiclass_k10": multiclass, "batched_jobs": batched_jobs, "binary_quantized_200": binary},
         "e2e": {"value": round(world * 1000.0 / e2e["ms_per_step"], 4), "unit": "iters/s",
                 "h2d_bytes_per_step": 2 * 4 * ds.num_data,
                 "d2h_bytes_per_step": 112 * (args.leaves - 1) + 8 * args.leaves + 8 + 8},
@@ -490,6 +491,114 @@ def run_batched_jobs(args):
             "learner_setup_s": round(setup_s, 2), "autotuned": bool(args.autotune)}
 
 
+def _auc(score, label):
+    """Area under the ROC curve with average ranks for tied scores (metric/binary.rs AUC)."""
+    import torch
+    order = torch.argsort(score)
+    s = score[order]
+    y = label[order].double()
+    _, inverse, counts = torch.unique_consecutive(s, return_inverse=True, return_counts=True)
+    ends = torch.cumsum(counts, 0).double()
+    avg_rank = ends - (counts.double() - 1.0) / 2.0  # 1-based average rank of each tie group
+    ranks = avg_rank[inverse]
+    pos = float(y.sum().item())
+    neg = float(len(y)) - pos
+    return float(((ranks * y).sum().item() - pos * (pos + 1.0) / 2.0) / (pos * neg))
+
+
+def run_binary(args):
+    """Binary classification with quantized gradients: rows x 200 float32 features (100 N(0,1) and
+    100 uniform(-1, 1), 5% NaN), labels from a logistic model on a random sparse linear term
+    (20 nonzero weights), 255 leaves; the quantized form (4 gradient bins, stochastic rounding,
+    graph) against the plain float form (one host round trip per split). The values are generated
+    on the device (seeded) and binned there (host bin mappers from the row sample); iterations/s
+    and the AUC of a 20% held-out split from the same generator."""
+    import torch
+    from lgbm_gb300 import BinnedDataset, GpuTreeLearner, LearnerConfig
+    from lgbm_gb300.tree import Tree
+    rows, F, leaves, lr = args.binary_rows, 200, 255, 0.1
+    n_all = rows + rows // 4
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(3)
+    X = torch.empty((n_all, F), dtype=torch.float32, device="cuda")
+    X[:, :F // 2].normal_(generator=gen)
+    X[:, F // 2:].uniform_(-1.0, 1.0, generator=gen)
+    w = torch.zeros(F, dtype=torch.float32, device="cuda")
+    nz = torch.randperm(F, generator=gen, device="cuda")[:F // 10]
+    w[nz] = torch.randn(F // 10, generator=gen, device="cuda")
+    y = (torch.rand(n_all, generator=gen, device="cuda") < torch.sigmoid(X @ w)).float()
+    for c0 in range(0, F, 25):  # NaNs in column blocks (bounded temporary memory)
+        blk = X[:, c0:c0 + 25]
+        blk[torch.rand(blk.shape, generator=gen, device="cuda") < 0.05] = float("nan")
+    torch.cuda.synchronize()
+    threads = min(32, os.cpu_count() or 8)
+    t0 = time.time()
+    ds = BinnedDataset.from_dense_device(X[:rows], max_bin=255, min_data_in_leaf=20, threads=threads)
+    ho_bins = ds.bin_like_device(X[rows:])
+    torch.cuda.synchronize()
+    prep_s = time.time() - t0
+    del X
+    torch.cuda.empty_cache()
+    n, m = ds.num_data, ho_bins.shape[1]
+    label, ho_y = y[:rows].contiguous(), y[rows:].contiguous()
+    pavg = min(max(float(label.mean().item()), 1e-15), 1.0 - 1e-15)
+    init = float(np.log(pavg / (1.0 - pavg)))
+
+    def form(quant, loop_mode, steps, warmup):
+        cfg = LearnerConfig(num_leaves=leaves, min_data_in_leaf=20, use_quantized_grad=int(quant),
+                            num_grad_quant_bins=4, stochastic_rounding=1, seed=0, num_threads=16, fused_madd=1)
+        learner = GpuTreeLearner(ds, cfg, loop_mode=loop_mode)
+        stream = torch.cuda.ExternalStream(learner.stream())
+        score = torch.full((n,), init, dtype=torch.float64, device="cuda")
+        gbuf, hbuf = learner.gradient_buffers()
+        torch.cuda.synchronize()
+        if args.autotune:
+            learner.objective_gradients(1, score.data_ptr(), label.data_ptr())
+            learner.autotune(gbuf, hbuf, on_device=True, trials=2)
+        trees, total_ms = [], 0.0
+        for it in range(warmup + steps):
+            ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            ev0.record(stream)
+            learner.objective_gradients(1, score.data_ptr(), label.data_ptr())
+            splits, lv, roots, nls = learner.train_raw(gbuf, hbuf, on_device=True)
+            vals = lv * lr
+            vals[np.abs(vals) <= K_ZERO_THRESHOLD] = 0.0
+            learner.add_prediction_to_score(vals, score.data_ptr(), on_device=True)
+            ev1.record(stream)
+            ev1.synchronize()
+            if it >= warmup:
+                total_ms += ev0.elapsed_time(ev1)
+            trees.append((splits[0, :nls[0] - 1].copy(), lv[0, :nls[0]].copy(), float(roots[0])))
+        train_loss = learner.objective_loss(1, score.data_ptr(), label.data_ptr())
+        ho = torch.full((m,), init, dtype=torch.float64, device="cuda")
+        torch.cuda.synchronize()
+        for sp, lvals, root in trees:
+            t = Tree.from_records(leaves, sp, lvals, root, ds.features)
+            t.apply_shrinkage(lr)
+            learner.predict_add(t, ho_bins.data_ptr(), m, ho.data_ptr())
+        torch.cuda.synchronize()
+        out = {"iters_per_s": round(1000.0 * steps / total_ms, 3), "ms_per_iter": round(total_ms / steps, 3),
+               "train_logloss": round(train_loss, 6), "heldout_auc": round(_auc(ho, ho_y), 6),
+               "iterations": len(trees), "launch_shape": _shape_dict(learner.launch_shape(), args.autotune)}
+        learner.close()
+        return out
+
+    q = form(True, 1, args.steps, args.warmup)
+    p = form(False, 0, args.steps, args.warmup)
+    return {"workload": "binary, %d x %d (N(0,1) / uniform halves, 5%% NaN), sparse logistic labels, 255 leaves; "
+                        "step = device gradients + 1 tree + score update" % (n, ds.num_features),
+            "quantized_graph": q, "plain_float_stepwise": p,
+            "heldout_auc_delta": round(q["heldout_auc"] - p["heldout_auc"], 6), "prep_s": round(prep_s, 1)}
+
+
+def _side(fn, args):
+    """A side form's result, or its error (a side form never takes the headline line down)."""
+    try:
+        return fn(args)
+    except Exception as e:  # noqa: BLE001
+        return {"error": "%s: %s" % (type(e).__name__, e)}
+
+
 def run_hist_traffic(args):
     """One quantized tree (graph form) on the synthetic workload, for a DRAM-traffic capture of the
     histogram kernel: prints its algorithmic bytes and launch count, the denominator of
@@ -605,13 +714,16 @@ def main():
     ap.add_argument("--hist-traffic", action="store_true",
                     help="train one tree and print the histogram kernel's algorithmic bytes (for an ncu capture)")
     ap.add_argument("--autotune", type=int, default=1, help="1: autotune each form's launch shape first")
-    ap.add_argument("--only", choices=["multiclass", "batched"],
+    ap.add_argument("--binary-rows", type=int, default=10_000_000,
+                    help="rows of the 200-feature binary quantized form (0: skip it)")
+    ap.add_argument("--only", choices=["multiclass", "batched", "binary"],
                     help="run only that side form and print its result (not a bench line)")
     args = ap.parse_args()
     if args.only:
         import torch
         torch.cuda.set_device(0)
-        print(json.dumps(run_multiclass(args) if args.only == "multiclass" else run_batched_jobs(args)))
+        fn = {"multiclass": run_multiclass, "batched": run_batched_jobs, "binary": run_binary}[args.only]
+        print(json.dumps(fn(args)))
         return
     if args.hist_traffic:
         print(json.dumps(run_hist_traffic(args)))
