@@ -673,15 +673,15 @@ int bk_learner_train(bk_learner* L, const float* gradients, const float* hessian
 
 namespace {
 
-// Autotuned launch shapes by dataset shape class: (log2 rows, feature tiles, bins per feature
-// slot, quantized, num_leaves) -> (hist_min_rows, hist CTAs per tile, partition CTAs).
+// Autotuned launch shapes by shape class: (device, log2 rows, feature tiles, bins per feature
+// slot, quantized, num_leaves, jobs) -> (hist_min_rows, hist CTAs per tile, partition CTAs).
 std::mutex g_tune_mutex;
-std::map<std::array<int, 5>, std::array<int, 3>> g_tune_cache;
+std::map<std::array<int, 7>, std::array<int, 3>> g_tune_cache;
 
-std::array<int, 5> tune_key(const bk_learner* L) {
+std::array<int, 7> tune_key(const bk_learner* L) {
   int lg = 0;
   while ((int64_t(1) << (lg + 1)) <= L->p.n) ++lg;
-  return {lg, L->p.T, L->p.B, L->p.quant, L->p.num_leaves};
+  return {L->device, lg, L->p.T, L->p.B, L->p.quant, L->p.num_leaves, L->K};
 }
 
 }  // namespace

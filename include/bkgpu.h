@@ -166,9 +166,9 @@ int bk_learner_bynode_state(bk_learner* learner, uint32_t* rng_state);
  * Times whole trees (graph form, median of `trials` after one untimed tree per shape) grown from
  * the given gradients (as bk_learner_train takes them, all rows) over a coordinate descent of
  * three launch parameters — the fewest rows a histogram CTA takes, histogram CTAs per 32-feature
- * tile, partition CTAs — and keeps the fastest. Choices are cached per dataset shape class
- * (log2 rows, feature tiles, bins per feature, quantized, num_leaves): a later learner of the same
- * class takes the cached shape without timing. The learner's state across trees (the
+ * tile, partition CTAs — and keeps the fastest. Choices are cached per shape class (device,
+ * log2 rows, feature tiles, bins per feature, quantized, num_leaves, num_jobs): a later learner of
+ * the same class takes the cached shape without timing. The learner's state across trees (the
  * stochastic-rounding engine) is restored afterwards; the trial trees replace the "last tree"
  * outputs (bk_learner_row_leaf), so call it before the first bk_learner_train. shape_out (host,
  * 3 ints, may be NULL) receives the chosen shape. */
