@@ -128,13 +128,18 @@ class BinnedDataset:
     @classmethod
     def from_dense(cls, X, max_bin=255, min_data_in_bin=3, min_data_in_leaf=20, bin_construct_sample_cnt=200000,
                    data_random_seed=1, use_missing=True, zero_as_missing=False, feature_pre_filter=True,
-                   threads=8, categorical=()):
+                   threads=8, categorical=(), max_bin_by_feature=None):
         """``categorical``: the column indices binned as categories (io/dataset.rs from_dense's
-        categorical list); the others are numerical."""
-        if max_bin > 255:
-            raise ValueError("max_bin above 255 needs 16-bit stored bins, which this learner does not take")
+        categorical list); the others are numerical. ``max_bin_by_feature``: one max_bin per
+        column (io/sample.rs:136-175), or None for ``max_bin`` everywhere."""
         X = np.asarray(X)
         n, ncol = X.shape
+        if max_bin_by_feature is not None:
+            max_bin = [int(b) for b in max_bin_by_feature]
+            if len(max_bin) != ncol or min(max_bin) <= 1:
+                raise ValueError("max_bin_by_feature needs one value > 1 per column")
+        if max(max_bin if isinstance(max_bin, list) else [max_bin]) > 255:
+            raise ValueError("max_bin above 255 needs 16-bit stored bins, which this learner does not take")
         rows = _Random(data_random_seed).sample(n, min(n, bin_construct_sample_cnt))
         features = _find_mappers(lambda col: np.asarray(X[rows, col], dtype=np.float64), ncol, n, len(rows),
                                  max_bin, min_data_in_bin, min_data_in_leaf, use_missing, zero_as_missing,
@@ -229,8 +234,10 @@ def _find_mappers(sample_col, ncol, n, sample_cnt, max_bin, min_data_in_bin, min
     filter_cnt = int((float(min_data_in_leaf) * sample_cnt) / float(n))
     cap = 1024
     cat_cols = set(int(c) for c in categorical)
+    max_bins = max_bin if isinstance(max_bin, list) else [max_bin] * ncol
 
     def find(col):
+        max_bin = max_bins[col]
         vals = np.asarray(sample_col(col), dtype=np.float64)
         keep = (np.abs(vals) > K_ZERO_THRESHOLD) | np.isnan(vals)
         vals = np.ascontiguousarray(vals[keep])

@@ -14,6 +14,9 @@ It copies, unchanged, the reference's own golden data for the tree-learner path:
   feature-mask inputs);
 * ``quantized_gradients.json`` — 16 upstream stumps for the gradient discretizer
   (tests/fixtures/quantized_gradients.json);
+* ``datasets/<case>.json`` + ``datasets/x_*.npz`` — the 20 upstream dataset cases of
+  tests/fixtures/datasets: the value matrix and the bin mappers upstream's ``save_binary`` wrote
+  for it (read from its dataset.bin as the reference's io/binary.rs reads it);
 
 and extracts the known-answer vectors that the reference keeps inside its Rust tests:
 
@@ -24,11 +27,15 @@ and extracts the known-answer vectors that the reference keeps inside its Rust t
 
 Nothing at test time reads the reference; the tests read only this folder.
 """
+import hashlib
 import json
 import os
 import re
 import shutil
+import struct
 import sys
+
+import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 CASES = ["binary", "l2_default", "l2_nan", "l2_zero", "l2_zero_as_missing", "l2_small", "l2_regularized",
@@ -37,6 +44,122 @@ CASES = ["binary", "l2_default", "l2_nan", "l2_zero", "l2_zero_as_missing", "l2_
          "cat_onehot", "cat_regularized", "cat_bagging", "l2_default_weighted", "binary_weighted",
          "multiclass_weighted", "bagging_weighted", "cat_default_weighted", "feature_fraction_bynode",
          "feature_fraction_both", "goss", "goss_dense_sample", "goss_weighted"]
+
+
+# ---- upstream binary dataset files (the reference's io/binary.rs reader, restated) ----
+_TOKEN = b"______LightGBM_Binary_File_Token______\n"
+
+
+class _Reader:
+    """Little-endian reader of upstream's 8-byte aligned layout (io/binary.rs:13-89)."""
+
+    def __init__(self, buf):
+        self.buf, self.pos = buf, 0
+
+    def take(self, n):
+        s = self.buf[self.pos:self.pos + n]
+        assert len(s) == n, "binary dataset truncated"
+        self.pos += n
+        return s
+
+    def i32(self):
+        return struct.unpack("<i", self.take(4))[0]
+
+    def f64(self):
+        return struct.unpack("<d", self.take(8))[0]
+
+    def u64(self):
+        return struct.unpack("<Q", self.take(8))[0]
+
+    def aligned_i32(self):
+        v = self.i32()
+        self.take(4)
+        return v
+
+    def aligned_bool(self):
+        return self.take(8)[0] != 0
+
+    def aligned_i32_vec(self, n):
+        start = self.pos
+        v = [self.i32() for _ in range(n)]
+        used = self.pos - start
+        self.take((used + 7) // 8 * 8 - used)
+        return v
+
+    def aligned_bytes(self, n):
+        s = self.take(n)
+        self.take((n + 7) // 8 * 8 - n)
+        return s
+
+
+def _bin_mapper(r):
+    """BinMapper::from_bytes (io/bin.rs:666-703)."""
+    m = {"num_bin": r.aligned_i32(), "missing_type": r.aligned_i32(), "is_trivial": r.aligned_bool(),
+         "sparse_rate": r.f64(), "bin_type": r.aligned_i32(), "min_val": r.f64(), "max_val": r.f64(),
+         "default_bin": r.aligned_i32(), "most_freq_bin": r.aligned_i32()}
+    if m["bin_type"] == 0:
+        m["bin_upper_bound"] = [r.f64() for _ in range(m["num_bin"])]
+    else:
+        m["bin_2_categorical"] = [r.i32() for _ in range(m["num_bin"])]
+    return m
+
+
+def read_bin_mappers(path):
+    """The used-feature map and every used feature's BinMapper of an upstream binary dataset file
+    (io/binary.rs:146-295: token, header, metadata, feature groups)."""
+    r = _Reader(open(path, "rb").read())
+    assert r.aligned_bytes(len(_TOKEN)) == _TOKEN
+    header_size = r.u64()
+    h0 = r.pos
+    num_data, num_features, ntf = r.aligned_i32(), r.aligned_i32(), r.aligned_i32()
+    for _ in range(4):  # label_idx, max_bin, bin_construct_sample_cnt, min_data_in_bin
+        r.aligned_i32()
+    for _ in range(3):  # use_missing, zero_as_missing, has_raw
+        r.aligned_bool()
+    used_feature_map = r.aligned_i32_vec(ntf)
+    num_groups = r.aligned_i32()
+    r.aligned_i32_vec(num_features)  # real_feature_idx
+    feature2group = r.aligned_i32_vec(num_features)
+    feature2subfeature = r.aligned_i32_vec(num_features)
+    r.pos = h0 + header_size  # the rest of the header (bin boundaries, names, forced bins)
+    meta_size = r.u64()
+    r.pos += meta_size
+    groups = []
+    for _ in range(num_groups):
+        size = r.u64()
+        start = r.pos
+        for _ in range(3):  # is_multi_val, is_dense_multi_val, is_sparse
+            r.aligned_bool()
+        nfeat = r.aligned_i32()
+        groups.append([_bin_mapper(r) for _ in range(nfeat)])
+        r.pos = start + size
+    mappers = []
+    for real in range(ntf):
+        inner = used_feature_map[real]
+        if inner < 0:
+            mappers.append(None)
+        else:
+            mappers.append(groups[feature2group[inner]][feature2subfeature[inner]])
+    return {"num_data": num_data, "mappers": mappers}
+
+
+def copy_datasets(fx):
+    """tests/fixtures/datasets: the value matrix of each case (deduplicated, compressed) and the
+    bin mappers upstream wrote into its dataset.bin, as JSON."""
+    src_root = os.path.join(fx, "datasets")
+    dst_root = os.path.join(HERE, "datasets")
+    os.makedirs(dst_root, exist_ok=True)
+    for case in sorted(os.listdir(src_root)):
+        src = os.path.join(src_root, case)
+        x = np.load(os.path.join(src, "x.npy"))
+        xname = "x_%s.npz" % hashlib.sha256(x.tobytes()).hexdigest()[:12]
+        if not os.path.exists(os.path.join(dst_root, xname)):
+            np.savez_compressed(os.path.join(dst_root, xname), x=x)
+        P = json.load(open(os.path.join(src, "params.json")))
+        P["x"] = xname
+        P.update(read_bin_mappers(os.path.join(src, "dataset.bin")))
+        with open(os.path.join(dst_root, case + ".json"), "w") as f:
+            json.dump(P, f)
 
 
 def _ints(text):
@@ -54,6 +177,7 @@ def main(ref):
                 continue  # sample weights only where the case has them
             shutil.copyfile(os.path.join(src, name), os.path.join(dst, name))
     shutil.copyfile(os.path.join(fx, "quantized_gradients.json"), os.path.join(HERE, "quantized_gradients.json"))
+    copy_datasets(fx)
 
     tests = os.path.join(ref, "crates", "lgbm-core", "tests")
     mt = open(os.path.join(tests, "mt19937.rs")).read()
