@@ -1689,7 +1689,7 @@ void orc_hist_float(const uint8_t* bins_colmajor, int64_t n, int32_t nf, const i
       o[ti] += (double)g[r];
       o[ti + 1] += const_hess ? 1.0 : (double)h[r];
     }
-    if (const_hess)
+    if (const_hess && n > 0)  // hessians[0] exists only for a non-empty dataset
       for (int b = 0; b < group_bins[f]; ++b) o[2 * b + 1] *= (double)h[0];
     cur += group_bins[f];
   }
