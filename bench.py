@@ -325,7 +325,7 @@ def run_gpu(args, rank, world):
         "binning": binning,
     }
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(ds, y, sample_rows=args.cpu_rows)
+        line["cpu_baseline"] = cpu_baseline(ds, y, sample_rows=args.cpu_rows, leaves=args.leaves)
     return line
 
 
@@ -651,17 +651,17 @@ def _device_view(ptr, count):
     return torch.as_tensor(_CAI(), device="cuda")
 
 
-def cpu_baseline(ds, y, sample_rows, threads=None):
+def cpu_baseline(ds, y, sample_rows, threads=None, leaves=255):
     """The oracle (the C++ port of the reference's tree learner) on the first `sample_rows` rows
-    of the same binned data: one float-path iteration (L2 gradients, one 255-leaf tree),
-    scaled to the full row count (linear in rows)."""
+    of the same binned data: one float-path iteration (L2 gradients, one tree of `leaves`
+    leaves), scaled to the full row count (linear in rows)."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import harness
     from lgbm_gb300 import BinnedDataset
     threads = threads or 1
     m = min(sample_rows, ds.num_data)
     sub = BinnedDataset(np.ascontiguousarray(ds.bins[:, :m]), ds.features, ds.num_total_features)
-    cfg = make_cfg(False)
+    cfg = make_cfg(False, leaves)
     cfg.values["num_threads"] = threads
     orc = harness.OracleLearner(sub, cfg)
     score = np.full(m, float(np.mean(y[:m], dtype=np.float64)))
@@ -681,14 +681,17 @@ def run_reference(args):
     ds, y, _ = build_dataset(args.rows)
     steps = []
     for _ in range(args.warmup):
-        cpu_baseline(ds, y, args.cpu_rows, threads)
+        cpu_baseline(ds, y, args.cpu_rows, threads, args.leaves)
     for _ in range(args.steps):
-        steps.append(cpu_baseline(ds, y, args.cpu_rows, threads))
+        steps.append(cpu_baseline(ds, y, args.cpu_rows, threads, args.leaves))
     v = float(np.median([s["value"] for s in steps]))
     return {"metric": METRIC, "impl": "reference", "value": v, "unit": "iters/s", "n_gpus": args.gpus,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 / v, 1) if v else None,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 grad/hess, f64 histograms",
-            "data": "synthetic (seeded)", "config": {"workload": WORKLOAD, "rows": ds.num_data},
+            "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "rows": ds.num_data, "features": ds.num_features,
+                       "num_leaves": args.leaves, "parallelism": "%d host threads" % threads,
+                       "l2_flush": "not applicable (CPU)"},
             "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
                              "sample": steps[-1]["sample"]},
             "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
