@@ -73,7 +73,11 @@ struct Params {
   // CatParams of the categorical search (feature_histogram.rs:1146-1163)
   double cat_smooth, cat_l2;
   int32_t max_cat_threshold, max_cat_to_onehot, min_data_per_group;
-  int32_t bynode;  // 1: every searched leaf draws a by-node feature sample (Job::used[F..3F))
+  int32_t bynode;  // 1: every searched leaf gets a by-node feature mask (Job::used[F..3F)): a sample
+                   //    and / or its interaction constraints
+  int32_t n_icons;     // interaction constraints: how many feature sets, of `path_words` words each
+  int32_t path_words;  // words of a feature bitset: ceil(F / 32)
+  const uint32_t* icons;  // [n_icons][path_words] inner-feature bitsets
 };
 
 // Per-leaf constants of one searched leaf (FindBestThreshold's preamble, feature_histogram.rs:
@@ -140,8 +144,9 @@ struct Job {
   int64_t* bsplit;     // [L]   inner feature << 32 | threshold | default_left << 31 of each leaf's best split
   LeafConst* lconst;   // [2]   constants of the smaller / larger leaf of the current search
   uint8_t* splittable; // [L][F]
-  uint8_t* used;       // [4][F] features searched in the current step; the by-node samples of the
-                       //        smaller / larger leaf; the sample's scratch
+  uint8_t* used;       // [4][F] features searched in the current step; the by-node masks of the
+                       //        smaller / larger leaf; the sample's scratch; then [L][path_words]
+                       //        uint32 bitsets of the features on the path to each leaf
   uint8_t* tree_mask;  // [F]   features the tree may split on (by-tree column sample), 1 by default
   bk_split* records;   // [L-1]
   double* leaf_value;  // [L]
@@ -180,6 +185,12 @@ __host__ __device__ __forceinline__ size_t cand_cat_words(int num_leaves, int F)
 }
 __device__ __forceinline__ uint32_t* cand_cat_bits(const Job& J, const Params& p, int32_t leaf, int32_t f) {
   return reinterpret_cast<uint32_t*>(J.cand + (size_t)p.num_leaves * p.F) + ((size_t)leaf * p.F + f) * 8;
+}
+
+// The features on the path to `leaf` (SerialTreeLearner::branch_features, serial.rs:233-234) as a
+// bitset over inner features, kept only with interaction constraints.
+__device__ __forceinline__ uint32_t* leaf_path_bits(const Job& J, const Params& p, int32_t leaf) {
+  return reinterpret_cast<uint32_t*>(J.used + 4 * (size_t)p.F) + (size_t)leaf * p.path_words;
 }
 
 __device__ __forceinline__ const int32_t* leaf_idx(const Job& J, int32_t buf) { return buf ? J.idx1 : J.idx0; }

@@ -137,6 +137,17 @@ __device__ __forceinline__ void post_split_writes(const Job& J, const Params& p,
   info.left_count = (int32_t)o.L;
   info.right_count = (int32_t)o.R;
   const int32_t bl = o.bl, nl = o.nl;
+  // serial.rs:1719-1722 — with interaction constraints, both children's paths gain the feature
+  if (p.n_icons > 0) {
+    uint32_t* pb = leaf_path_bits(J, p, bl);
+    uint32_t* pn = leaf_path_bits(J, p, nl);
+    const int32_t inner = info.inner;
+    for (int w = lane; w < p.path_words; w += 32) {
+      const uint32_t v = pb[w] | (w == (inner >> 5) ? (1u << (inner & 31)) : 0u);
+      pn[w] = v;
+      pb[w] = v;
+    }
+  }
   // lanes 0-7: word `lane` of a categorical split's left-bin bitset (serial.rs:1724-1759)
   if (lane < 8)
     J.records[o.tl - 1].cat_bins[lane] =

@@ -111,24 +111,56 @@ __device__ __forceinline__ void compute_leaf_const(const Job& J, const Params& p
   compute_leaf_const_ls(J, p, st, side, J.leaf_sum[leaf], st->tree_leaves == 1, lane);
 }
 
-// ColSampler::get_by_node (col_sampler.rs:109-177, no interaction constraints) for side `side` of
-// the coming search, on one thread: Random::sample (utils/random.rs:53-80) of get_cnt(n, fraction)
-// positions among the n candidates — the tree's by-tree sample (ascending inner features) when one
-// is active, else every feature — continuing the sampler's LCG stream kept in the job state.
+// ColSampler::get_by_node (col_sampler.rs:109-177) for side `side` of the coming search, on one
+// thread. With interaction constraints the allowed features are the leaf's path features plus
+// every constraint set that holds the whole path (every set at the root); `extra` is a feature
+// the path gains with the split being applied (-1: none). Without sampling the mask is the
+// allowed set; with sampling it is Random::sample (utils/random.rs:53-80) of get_cnt(n, fraction)
+// positions (at most the allowed candidates) among the candidates — the tree's by-tree sample
+// (ascending inner features) when one is active, else every feature — filtered by the allowed
+// set, continuing the sampler's LCG stream kept in the job state.
 __device__ __forceinline__ uint32_t lcg_step(uint32_t x) { return x * 214013u + 2531011u; }
 
-__device__ __forceinline__ void draw_node_sample(const Job& J, const Params& p, JobState* st, int side) {
+__device__ __forceinline__ bool path_has(const uint32_t* path, int f, int extra) {
+  return f == extra || ((path[f >> 5] >> (f & 31)) & 1u) != 0u;
+}
+
+__device__ __forceinline__ void draw_node_sample(const Job& J, const Params& p, JobState* st, int side, int32_t leaf,
+                                                 int extra) {
   uint8_t* out = J.used + (size_t)(1 + side) * p.F;
   uint8_t* sel = J.used + (size_t)3 * p.F;
   const bool bytree = st->bytree_on != 0;
-  int32_t n = 0;
-  for (int f = 0; f < p.F; ++f) {
-    out[f] = 0;
-    sel[f] = 0;
-    n += (!bytree || J.tree_mask[f]) ? 1 : 0;
+  const bool constrained = p.n_icons > 0;
+  const bool sampled = st->bynode_fraction < 1.0;
+  // the allowed features
+  if (!constrained) {
+    for (int f = 0; f < p.F; ++f) out[f] = 1;
+  } else {
+    const uint32_t* path = leaf_path_bits(J, p, leaf);
+    bool empty = extra < 0;
+    for (int w = 0; w < p.path_words && empty; ++w) empty = path[w] == 0u;
+    for (int f = 0; f < p.F; ++f) out[f] = path_has(path, f, extra) ? 1 : 0;
+    for (int c = 0; c < p.n_icons; ++c) {
+      const uint32_t* set = p.icons + (size_t)c * p.path_words;
+      bool holds = true;  // every path feature is in the set
+      for (int f = 0; f < p.F && holds && !empty; ++f)
+        if (path_has(path, f, extra) && ((set[f >> 5] >> (f & 31)) & 1u) == 0u) holds = false;
+      if (empty || holds)
+        for (int f = 0; f < p.F; ++f) out[f] |= (uint8_t)((set[f >> 5] >> (f & 31)) & 1u);
+    }
   }
-  const int32_t used = (int32_t)((double)n * st->bynode_fraction + 0.5);
-  const int32_t k = used > (n < 1 ? n : 1) ? used : (n < 1 ? n : 1);
+  if (!sampled) return;
+  int32_t n_all = 0, n = 0;
+  for (int f = 0; f < p.F; ++f) {
+    const bool cand = !bytree || J.tree_mask[f];
+    n_all += cand ? 1 : 0;
+    n += (cand && out[f]) ? 1 : 0;
+    sel[f] = 0;
+  }
+  const int32_t used = (int32_t)((double)n_all * st->bynode_fraction + 0.5);
+  const int32_t mn = n_all < 1 ? n_all : 1;
+  int32_t k = used > mn ? used : mn;
+  if (constrained && n < k) k = n;
   uint32_t x = st->col_rng;
   if (k > n || k <= 0) {
     // no position is drawn
@@ -155,16 +187,18 @@ __device__ __forceinline__ void draw_node_sample(const Job& J, const Params& p, 
   }
   st->col_rng = x;
   for (int32_t f = 0, q = 0; f < p.F; ++f) {
-    if (bytree && !J.tree_mask[f]) continue;
-    out[f] = sel[q++];
+    const bool cand = (!bytree || J.tree_mask[f]) && out[f];
+    out[f] = cand ? sel[q++] : 0;
   }
 }
 
-// The by-node samples of a search: the smaller leaf's, then the larger leaf's (serial.rs:1328-1336).
-__device__ __forceinline__ void draw_node_samples(const Job& J, const Params& p, bool larger) {
+// The by-node masks of a search: the smaller leaf's, then the larger leaf's, if any
+// (serial.rs:1328-1336). `small` / `large` name the leaves whose paths the masks use.
+__device__ __forceinline__ void draw_node_samples(const Job& J, const Params& p, int32_t small, int32_t large,
+                                                  int extra) {
   JobState* st = J.st;
-  draw_node_sample(J, p, st, 0);
-  if (larger) draw_node_sample(J, p, st, 1);
+  draw_node_sample(J, p, st, 0, small, extra);
+  if (large >= 0) draw_node_sample(J, p, st, 1, large, extra);
 }
 
 // The histogram CTA that does the serial side work of its launch: the last CTA of tile 0, idle for
@@ -178,7 +212,7 @@ __device__ __forceinline__ void hist_leaf_constants(const Job& J, const Params& 
   const JobState* st = J.st;
   if (st->stop || !st->do_search) return;
   if (threadIdx.x >= 64) {
-    if (p.bynode && threadIdx.x == 96) draw_node_samples(J, p, st->larger_leaf >= 0);
+    if (p.bynode && threadIdx.x == 96) draw_node_samples(J, p, st->smaller_leaf, st->larger_leaf, -1);
     return;
   }
   compute_leaf_const(J, p, st, (int)(threadIdx.x >> 5), (int)(threadIdx.x & 31));
@@ -196,7 +230,9 @@ __device__ __forceinline__ void hist_apply_split(const Job& J, const Params& p, 
   }
   if (!o.go) return;
   if (warp == 3) {
-    if (p.bynode && lane == 0) draw_node_samples(J, p, true);
+    // both children's paths are the split leaf's plus the split feature (warp 2 is writing them
+    // now; either value of the split leaf's path, with that feature added, is the children's)
+    if (p.bynode && lane == 0) draw_node_samples(J, p, o.bl, o.bl, J.st->split_inner);
     return;
   }
   const JobState* st = J.st;

@@ -126,6 +126,7 @@ struct bk_learner {
   int K = 1;
   int loop_mode = 1;
   bool timing = false;
+  bool bynode_sampling = false;  // bk_learner_set_bynode with a fraction below 1
   int exact_quant_root = 1;
   HistLaunch hl{};
   // dataset
@@ -358,6 +359,10 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
     p.max_cat_threshold = c->max_cat_threshold;
     p.max_cat_to_onehot = c->max_cat_to_onehot;
     p.min_data_per_group = c->min_data_per_group;
+    p.bynode = 0;
+    p.n_icons = 0;
+    p.path_words = (num_features + 31) / 32;
+    p.icons = nullptr;
     L->K = num_jobs;
     int maxb = 0;
     for (int f = 0; f < num_features; ++f) {
@@ -471,6 +476,10 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
     L->d_pool = L->dalloc<uint8_t>(L->pool_bytes_per_job * K);
     JobState* d_states = L->dalloc<JobState>(K);
     CK(cudaMemset(d_states, 0, sizeof(JobState) * K));
+    for (int j = 0; j < K; ++j) {  // no by-node sampling until bk_learner_set_bynode
+      const double one = 1.0;
+      CK(cudaMemcpy(&d_states[j].bynode_fraction, &one, sizeof(double), cudaMemcpyHostToDevice));
+    }
     L->jobs.resize(K);
     for (int j = 0; j < K; ++j) {
       Job& J = L->jobs[j];
@@ -499,8 +508,10 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
       J.bsplit = L->dalloc<int64_t>(Lv);
       J.lconst = L->dalloc<LeafConst>(2);
       J.splittable = L->dalloc<uint8_t>((size_t)Lv * F);
-      J.used = L->dalloc<uint8_t>(4 * (size_t)F);
+      // used, the two by-node masks, the sample scratch, then every leaf's path bitset
+      J.used = L->dalloc<uint8_t>(4 * (size_t)F + sizeof(uint32_t) * (size_t)Lv * p.path_words);
       CK(cudaMemset(J.used, 1, 4 * (size_t)F));
+      CK(cudaMemset(J.used + 4 * (size_t)F, 0, sizeof(uint32_t) * (size_t)Lv * p.path_words));
       J.tree_mask = L->dalloc<uint8_t>(F);
       CK(cudaMemset(J.tree_mask, 1, F));
       J.records = L->dalloc<bk_split>(Lv);
@@ -1006,11 +1017,50 @@ int bk_learner_set_bynode(bk_learner* L, double fraction, int32_t bytree_active,
   } catch (const CudaError& e) {
     return fail_cuda(e);
   }
-  if ((on ? 1 : 0) != L->p.bynode && L->graph_exec) {
+  L->bynode_sampling = on;
+  const int32_t masks = (on || L->p.n_icons > 0) ? 1 : 0;
+  if (masks != L->p.bynode && L->graph_exec) {
     cudaGraphExecDestroy(L->graph_exec);
     L->graph_exec = nullptr;
   }
-  L->p.bynode = on ? 1 : 0;
+  L->p.bynode = masks;
+  return 0;
+}
+
+int bk_learner_set_interaction_constraints(bk_learner* L, const int32_t* features, const int32_t* offsets,
+                                           int32_t num_sets) {
+  if (!L || num_sets < 0 || (num_sets > 0 && (!features || !offsets))) {
+    set_error("bk_learner_set_interaction_constraints: invalid arguments");
+    return -1;
+  }
+  const int W = L->p.path_words, F = L->p.F;
+  std::vector<uint32_t> bits((size_t)num_sets * W, 0u);
+  for (int32_t k = 0; k < num_sets; ++k) {
+    if (offsets[k + 1] < offsets[k]) {
+      set_error("bk_learner_set_interaction_constraints: offsets must not decrease");
+      return -1;
+    }
+    for (int32_t i = offsets[k]; i < offsets[k + 1]; ++i)
+      for (int f = 0; f < F; ++f)  // real feature -> inner feature; unused features drop out
+        if (L->h_feat[f].real == features[i]) bits[(size_t)k * W + (f >> 5)] |= 1u << (f & 31);
+  }
+  try {
+    const uint32_t* d = nullptr;
+    if (num_sets > 0) {
+      uint32_t* buf = L->dalloc<uint32_t>(bits.size());
+      CK(cudaMemcpy(buf, bits.data(), sizeof(uint32_t) * bits.size(), cudaMemcpyHostToDevice));
+      d = buf;
+    }
+    L->p.icons = d;
+    L->p.n_icons = num_sets;
+    L->p.bynode = (L->bynode_sampling || num_sets > 0) ? 1 : 0;
+    if (L->graph_exec) {  // the kernels take the constraints through their parameters
+      cudaGraphExecDestroy(L->graph_exec);
+      L->graph_exec = nullptr;
+    }
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
+  }
   return 0;
 }
 

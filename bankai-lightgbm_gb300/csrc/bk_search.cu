@@ -1378,6 +1378,10 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
     J.bfeat[i] = -1;
     J.bsplit[i] = (int64_t)-1 * 4294967296LL;
   }
+  if (p.n_icons > 0) {  // serial.rs:660-662: every leaf's path starts empty
+    uint32_t* paths = leaf_path_bits(J, p, 0);
+    for (int i = threadIdx.x; i < p.num_leaves * p.path_words; i += blockDim.x) paths[i] = 0u;
+  }
   __syncthreads();
   if (threadIdx.x < 32) {
     const int lane = threadIdx.x;

@@ -70,6 +70,7 @@ _GPU_SIGNATURES = [
     ("bk_learner_set_feature_mask", _i32, [_P, _P]),
     ("bk_learner_set_bynode", _i32, [_P, _f64, _i32, _u32]),
     ("bk_learner_bynode_state", _i32, [_P, _P]),
+    ("bk_learner_set_interaction_constraints", _i32, [_P, _P, _P, _i32]),
     ("bk_learner_autotune", _i32, [_P, _P, _P, _i32, _i32, _P]),
     ("bk_learner_launch_shape", _i32, [_P, _P]),
     ("bk_learner_set_launch_shape", _i32, [_P, _P]),

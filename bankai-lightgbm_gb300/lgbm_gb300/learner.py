@@ -74,6 +74,17 @@ class GpuTreeLearner:
         _lib.check(self.lib.bk_learner_set_bynode(self.h, float(fraction), int(bool(bytree_active)),
                                                   int(rng_state) & 0xFFFFFFFF), "bk_learner_set_bynode")
 
+    def set_interaction_constraints(self, sets):
+        """Interaction constraints of the following trees: a list of sets of real feature indices
+        (treelearner/col_sampler.rs:148-177); [] removes them."""
+        offs = np.zeros(len(sets) + 1, dtype=np.int32)
+        for k, c in enumerate(sets):
+            offs[k + 1] = offs[k] + len(c)
+        feats = np.array([int(f) for c in sets for f in c] or [0], dtype=np.int32)
+        _lib.check(self.lib.bk_learner_set_interaction_constraints(self.h, feats.ctypes.data, offs.ctypes.data,
+                                                                   len(sets)),
+                   "bk_learner_set_interaction_constraints")
+
     def bynode_state(self):
         out = ctypes.c_uint32()
         _lib.check(self.lib.bk_learner_bynode_state(self.h, ctypes.byref(out)), "bk_learner_bynode_state")

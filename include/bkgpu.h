@@ -162,6 +162,15 @@ int bk_learner_set_bynode(bk_learner* learner, double fraction, int32_t bytree_a
 /* The by-node sampler's LCG state after the last train call. */
 int bk_learner_bynode_state(bk_learner* learner, uint32_t* rng_state);
 
+/* Interaction constraints (config interaction_constraints; ColSampler::get_by_node's allowed
+ * features, treelearner/col_sampler.rs:148-177): a searched leaf may split only on the features
+ * on its path (serial.rs:1719-1722) and on those of every set that holds the whole path (every
+ * set at the root); with by-node sampling the sample is drawn among the allowed features. Set k
+ * holds the real feature indices features[offsets[k] .. offsets[k + 1]); num_sets 0 removes the
+ * constraints. Applies to the following train calls. */
+int bk_learner_set_interaction_constraints(bk_learner* learner, const int32_t* features, const int32_t* offsets,
+                                           int32_t num_sets);
+
 /* Launch-shape autotuner (GB300-only, no reference counterpart; results never depend on it).
  * Times whole trees (graph form, median of `trials` after one untimed tree per shape) grown from
  * the given gradients (as bk_learner_train takes them, all rows) over a coordinate descent of

@@ -48,6 +48,7 @@ def load():
         lib.orc_learner_set_bynode.argtypes = [P, ctypes.c_double, i32, u32]
         lib.orc_learner_bynode_state.restype = u32
         lib.orc_learner_bynode_state.argtypes = [P]
+        lib.orc_learner_set_interaction_constraints.argtypes = [P, P, P, i32]
         lib.orc_learner_train.restype = i32
         lib.orc_learner_train.argtypes = [P, P, P, P, i64, P, P]
         lib.orc_learner_root_output.restype = ctypes.c_double
@@ -75,6 +76,14 @@ def load():
 
 def _ptr(a):
     return None if a is None else a.ctypes.data
+
+
+def _flatten_sets(sets):
+    offs = np.zeros(len(sets) + 1, dtype=np.int32)
+    for k, c in enumerate(sets):
+        offs[k + 1] = offs[k] + len(c)
+    feats = np.array([int(f) for c in sets for f in c] or [0], dtype=np.int32)
+    return feats, offs
 
 
 class OracleLearner:
@@ -123,6 +132,10 @@ class OracleLearner:
 
     def bynode_state(self):
         return int(self.lib.orc_learner_bynode_state(self.h))
+
+    def set_interaction_constraints(self, sets):
+        feats, offs = _flatten_sets(sets)
+        self.lib.orc_learner_set_interaction_constraints(self.h, feats.ctypes.data, offs.ctypes.data, len(sets))
 
     def row_leaf(self):
         out = np.zeros(self.ds.num_data, dtype=np.int32)
@@ -305,9 +318,11 @@ class TreeColumnSampler:
     of a tree (one per searched leaf) by the learner, continuing the same LCG stream. Features are
     the learner's inner features, which follow the real-index order of the used features."""
 
-    def __init__(self, num_features, fraction, seed, fraction_bynode=1.0):
+    def __init__(self, num_features, fraction, seed, fraction_bynode=1.0, interaction_constraints=None):
         self.nf = num_features
         self.rand = LcgRandom(seed)
+        self.icons = interaction_constraints or []
+        self._set_on = set()
         self.active = fraction < 1.0
         self.bynode = float(fraction_bynode)
         self.cnt = max(min(1, num_features), int(num_features * fraction + 0.5)) if self.active else num_features
@@ -319,6 +334,9 @@ class TreeColumnSampler:
         same LCG stream; after the tree the host continues from the learner's state."""
         mask = self.reset_by_tree()
         learner.set_feature_mask(mask)
+        if self.icons and id(learner) not in self._set_on:
+            learner.set_interaction_constraints(self.icons)
+            self._set_on.add(id(learner))
         if self.bynode < 1.0:
             learner.set_bynode(self.bynode, self.active, self.rand.x)
 
@@ -409,12 +427,19 @@ def resolved_params(model_text):
     return out
 
 
+def parse_interaction_constraints(text):
+    """`[0,1,2],[3,4,5]` (the model file's parameter line) -> [[0, 1, 2], [3, 4, 5]]."""
+    import re
+    return [[int(v) for v in grp.split(",") if v.strip()] for grp in re.findall(r"\[([^\]]*)\]", text or "")]
+
+
 def samplers_from_params(resolved, ds):
     """(TreeColumnSampler or None, RowBagging or None) for a resolved config."""
     ff = float(resolved.get("feature_fraction", 1))
     fn = float(resolved.get("feature_fraction_bynode", 1))
-    cols = (TreeColumnSampler(ds.num_features, ff, int(resolved.get("feature_fraction_seed", 2)), fn)
-            if ff < 1 or fn < 1 else None)
+    icons = parse_interaction_constraints(resolved.get("interaction_constraints", ""))
+    cols = (TreeColumnSampler(ds.num_features, ff, int(resolved.get("feature_fraction_seed", 2)), fn, icons)
+            if ff < 1 or fn < 1 or icons else None)
     if resolved.get("data_sample_strategy", "bagging") == "goss":
         return cols, Goss(ds.num_data, float(resolved["top_rate"]), float(resolved["other_rate"]),
                           float(resolved["learning_rate"]), int(resolved.get("bagging_seed", 3)))

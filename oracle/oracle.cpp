@@ -1069,23 +1069,51 @@ struct Learner {
   bool bytree_active = false;
   Lcg node_rng;
 
+  // interaction constraints (config interaction_constraints, col_sampler.rs:148-177): sets of inner
+  // features; the features on the path to each leaf (serial.rs:233-234, :1719-1722)
+  std::vector<std::vector<uint8_t>> icons;
+  std::vector<std::vector<uint8_t>> branch;
+
+  // ColSampler::allowed_features: the path's features, plus every constraint that contains the
+  // whole path (every constraint at the root)
+  std::vector<uint8_t> allowed_features(int32_t leaf) {
+    const std::vector<uint8_t>& b = branch[(size_t)leaf];
+    std::vector<uint8_t> allowed = b;
+    bool empty = true;
+    for (uint8_t x : b) empty = empty && !x;
+    for (const auto& c : icons) {
+      bool all = true;
+      for (int32_t f = 0; f < nf; ++f) all = all && (!b[(size_t)f] || c[(size_t)f]);
+      if (empty || all)
+        for (int32_t f = 0; f < nf; ++f) allowed[(size_t)f] |= c[(size_t)f];
+    }
+    return allowed;
+  }
+
   // ColSampler::get_by_node: the features a searched leaf may split on
-  std::vector<uint8_t> node_mask() {
+  std::vector<uint8_t> node_mask(int32_t leaf) {
     std::vector<uint8_t> ret((size_t)nf, 0);
+    const bool constrained = !icons.empty();
+    const std::vector<uint8_t> allowed = constrained ? allowed_features(leaf) : std::vector<uint8_t>();
     if (bynode_fraction >= 1.0) {
-      std::fill(ret.begin(), ret.end(), 1);
-      return ret;
+      if (!constrained) {
+        std::fill(ret.begin(), ret.end(), 1);
+        return ret;
+      }
+      return allowed;
     }
-    if (bytree_active) {
-      std::vector<int32_t> used_list;  // the by-tree sample, ascending
-      for (int32_t f = 0; f < nf; ++f)
-        if (tree_mask.empty() || tree_mask[(size_t)f]) used_list.push_back(f);
-      const int32_t cnt = col_get_cnt((int32_t)used_list.size(), bynode_fraction);
-      for (int32_t q : node_rng.sample((int32_t)used_list.size(), cnt)) ret[(size_t)used_list[(size_t)q]] = 1;
-    } else {
-      const int32_t cnt = col_get_cnt(nf, bynode_fraction);
-      for (int32_t q : node_rng.sample(nf, cnt)) ret[(size_t)q] = 1;
+    std::vector<int32_t> cand;  // the by-tree sample or every feature, ascending
+    for (int32_t f = 0; f < nf; ++f)
+      if (!bytree_active || tree_mask.empty() || tree_mask[(size_t)f]) cand.push_back(f);
+    int32_t cnt = col_get_cnt((int32_t)cand.size(), bynode_fraction);
+    if (constrained) {
+      std::vector<int32_t> filtered;
+      for (int32_t f : cand)
+        if (allowed[(size_t)f]) filtered.push_back(f);
+      cand.swap(filtered);
+      cnt = std::min(cnt, (int32_t)cand.size());
     }
+    for (int32_t q : node_rng.sample((int32_t)cand.size(), cnt)) ret[(size_t)cand[(size_t)q]] = 1;
     return ret;
   }
   Pool* workers = nullptr;
@@ -1225,8 +1253,9 @@ struct Learner {
                                         double lp_out) {
     int32_t lslot = larger.leaf >= 0 ? larger_slot : -1;
     // serial.rs:1328-1336 — the by-node samples of the smaller leaf, then the larger one
-    const std::vector<uint8_t> smask = node_mask();
-    const std::vector<uint8_t> lmask = larger.leaf >= 0 ? node_mask() : std::vector<uint8_t>((size_t)nf, 1);
+    const std::vector<uint8_t> smask = node_mask(smaller.leaf);
+    const std::vector<uint8_t> lmask =
+        larger.leaf >= 0 ? node_mask(larger.leaf) : std::vector<uint8_t>((size_t)nf, 1);
     std::vector<SplitInfo> cs_all(nf), cl_all(nf);
     std::vector<uint8_t> ss_all(nf, 0), sl_all(nf, 0);
     workers->run(nf, [&](int f) {
@@ -1399,6 +1428,10 @@ struct Learner {
       if (metas[f].real == info.feature) inner = f;
     int32_t next_leaf = tree_leaves;
     // serial.rs:1724-1745 — a categorical split partitions by the bitset of its bins
+    // serial.rs:1719-1722 — both children's paths gain the split feature
+    branch[(size_t)next_leaf] = branch[(size_t)best_leaf];
+    branch[(size_t)next_leaf][(size_t)inner] = 1;
+    branch[(size_t)best_leaf][(size_t)inner] = 1;
     const bool cat = metas[inner].categorical != 0;
     uint32_t bits[8];
     bitset_of(info.cat_bins, bits);
@@ -1513,6 +1546,7 @@ struct Learner {
 
   // serial.rs:578-628
   void train(const float* g, const float* h, const int32_t* rows, int64_t nrows) {
+    branch.assign((size_t)num_leaves, std::vector<uint8_t>((size_t)nf, 0));  // serial.rs:660-662
     before_train(g, h, rows, nrows);
     records.clear();
     std::fill(leaf_value.begin(), leaf_value.end(), 0.0);
@@ -1621,6 +1655,21 @@ void orc_learner_set_bynode(void* h, double fraction, int32_t bytree_active, uin
 
 // The LCG state after the last tree's by-node draws.
 uint32_t orc_learner_bynode_state(void* h) { return ((Learner*)h)->node_rng.x; }
+
+// Interaction constraints: `num_sets` sets of real feature indices, set k at
+// features[offsets[k] .. offsets[k + 1]); features the learner does not use are dropped.
+void orc_learner_set_interaction_constraints(void* h, const int32_t* features, const int32_t* offsets,
+                                             int32_t num_sets) {
+  Learner* L = (Learner*)h;
+  L->icons.clear();
+  for (int32_t k = 0; k < num_sets; ++k) {
+    std::vector<uint8_t> c((size_t)L->nf, 0);
+    for (int32_t i = offsets[k]; i < offsets[k + 1]; ++i)
+      for (int32_t f = 0; f < L->nf; ++f)
+        if (L->metas[(size_t)f].real == features[i]) c[(size_t)f] = 1;
+    L->icons.push_back(c);
+  }
+}
 
 // The features the following trees may split on (ColSampler::reset_by_tree, col_sampler.rs:87-103):
 // mask[f] != 0 for every used inner feature f; NULL restores "all features".

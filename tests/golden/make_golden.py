@@ -43,7 +43,8 @@ CASES = ["binary", "l2_default", "l2_nan", "l2_zero", "l2_zero_as_missing", "l2_
          "bagging_no_freq", "bagging_feature_fraction", "feature_fraction", "cat_default", "cat_binary", "cat_nan",
          "cat_onehot", "cat_regularized", "cat_bagging", "l2_default_weighted", "binary_weighted",
          "multiclass_weighted", "bagging_weighted", "cat_default_weighted", "feature_fraction_bynode",
-         "feature_fraction_both", "goss", "goss_dense_sample", "goss_weighted"]
+         "feature_fraction_both", "goss", "goss_dense_sample", "goss_weighted", "interaction", "interaction_bynode",
+         "interaction_sampled"]
 
 
 # ---- upstream binary dataset files (the reference's io/binary.rs reader, restated) ----

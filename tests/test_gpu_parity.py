@@ -404,18 +404,21 @@ def test_categorical_trees(case):
             gpu.close()
 
 
-@pytest.mark.parametrize("bytree", [False, True])
-def test_bynode_column_sample(bytree):
-    """bk_learner_set_bynode: every searched leaf draws its feature sample on the device from the
-    sampler's LCG stream; trees (quantized, bit-exact) and the stream's state after each tree
-    equal the oracle's, with and without a by-tree sample."""
+@pytest.mark.parametrize("bytree,bynode,constrained", [(False, 0.35, False), (True, 0.35, False),
+                                                       (False, 1.0, True), (True, 0.5, True)])
+def test_bynode_column_sample(bytree, bynode, constrained):
+    """bk_learner_set_bynode / bk_learner_set_interaction_constraints: every searched leaf gets its
+    feature mask on the device (a sample from the sampler's LCG stream, the features its path's
+    interaction constraints allow, or both); trees (quantized, bit-exact) and the stream's state
+    after each tree equal the oracle's."""
     import harness
     ds, z = _dataset(20000, 60, seed=31)
     g, h, const = _grads(z, "binary", seed=32)
     cfg = dict(num_leaves=31, use_quantized_grad=1, stochastic_rounding=1, seed=5, num_threads=2)
     orc, gpu, _ = _learners(ds, const, **cfg)
-    cols_o = harness.TreeColumnSampler(ds.num_features, 0.7 if bytree else 1.0, 9, 0.35)
-    cols_g = harness.TreeColumnSampler(ds.num_features, 0.7 if bytree else 1.0, 9, 0.35)
+    icons = [list(range(0, 20)), list(range(10, 35)), [40, 41, 42, 43, 59]] if constrained else None
+    cols_o = harness.TreeColumnSampler(ds.num_features, 0.7 if bytree else 1.0, 9, bynode, icons)
+    cols_g = harness.TreeColumnSampler(ds.num_features, 0.7 if bytree else 1.0, 9, bynode, icons)
     for it in range(3):
         cols_o.before_tree(orc)
         cols_g.before_tree(gpu)
