@@ -18,8 +18,8 @@ the training loss back.
 `--impl reference` times the CPU learner (the oracle port of the reference's tree learner, with
 all host threads) on a bounded row sample of the same workload and scales to the full workload.
 
-Multi-GPU (`--gpus N`, torchrun): independent replicas, one per GPU (the path has no exchange
-step in this build); value = iterations of all ranks / max time over ranks.
+Multi-GPU (`--gpus N`, torchrun): independent replicas, one per GPU (the learner adds no
+cross-GPU exchange step); value = iterations of all ranks / max time over ranks.
 """
 import argparse
 import json

@@ -1,7 +1,7 @@
 // ORACLE — test infrastructure only.
 //
 // A plain C++ CPU restatement of bankai-lightgbm's tree-learner hot path, used as the parity
-// checker for the GB300 learner and as the timed CPU baseline ("port"). Nothing in the product
+// oracle of the GB300 learner and as the timed CPU baseline ("port"). Nothing in the product
 // library links, loads or calls this file; only tests, the smoke check and the CPU-baseline leg
 // of bench.py do.
 //

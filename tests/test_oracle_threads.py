@@ -2,7 +2,7 @@
 the oracle grows identical trees (15 iterations, 31 leaves) with 1, 2 and 3 worker threads, on
 the reference's own splitmix64 data generators (8,000 rows here instead of 40,000), for the
 full-precision path and for the quantized path with nearest rounding (8 gradient bins). The GPU learner's trees are compared with the oracle's elsewhere, so this
-pins that the checker itself is thread-invariant, as the reference is.
+pins that the oracle itself is thread-invariant, as the reference is.
 """
 import numpy as np
 import pytest
