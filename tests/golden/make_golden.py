@@ -14,6 +14,9 @@ It copies, unchanged, the reference's own golden data for the tree-learner path:
   feature-mask inputs);
 * ``quantized_gradients.json`` — 16 upstream stumps for the gradient discretizer
   (tests/fixtures/quantized_gradients.json);
+* ``predict/<case>/`` — six upstream models with their training / test rows and the leaf index of
+  every test row in every tree (tests/fixtures/{binary, missing, zero_as_missing, regression_l2,
+  categorical, multiclass});
 * ``datasets/<case>.json`` + ``datasets/x_*.npz`` — the 20 upstream dataset cases of
   tests/fixtures/datasets: the value matrix and the bin mappers upstream's ``save_binary`` wrote
   for it (read from its dataset.bin as the reference's io/binary.rs reads it);
@@ -163,6 +166,20 @@ def copy_datasets(fx):
             json.dump(P, f)
 
 
+PREDICT_CASES = ["binary", "missing", "zero_as_missing", "regression_l2", "categorical", "multiclass"]
+
+
+def copy_predict_cases(fx):
+    """tests/fixtures/<case>: an upstream model, its training and test rows and the leaf every test
+    row reaches in every tree (pred_leaf.npy), for the routing of held-out rows."""
+    for case in PREDICT_CASES:
+        src = os.path.join(fx, case)
+        dst = os.path.join(HERE, "predict", case)
+        os.makedirs(dst, exist_ok=True)
+        for name in ("train.npy", "test.npy", "pred_leaf.npy", "model.txt", "params.json"):
+            shutil.copyfile(os.path.join(src, name), os.path.join(dst, name))
+
+
 def _ints(text):
     return [int(x) for x in re.findall(r"-?\d+", text)]
 
@@ -179,6 +196,7 @@ def main(ref):
             shutil.copyfile(os.path.join(src, name), os.path.join(dst, name))
     shutil.copyfile(os.path.join(fx, "quantized_gradients.json"), os.path.join(HERE, "quantized_gradients.json"))
     copy_datasets(fx)
+    copy_predict_cases(fx)
 
     tests = os.path.join(ref, "crates", "lgbm-core", "tests")
     mt = open(os.path.join(tests, "mt19937.rs")).read()
