@@ -14,8 +14,8 @@ It copies, unchanged, the reference's own golden data for the tree-learner path:
   feature-mask inputs);
 * ``quantized_gradients.json`` — 16 upstream stumps for the gradient discretizer
   (tests/fixtures/quantized_gradients.json);
-* ``predict/<case>/`` — six upstream models with their training / test rows and the leaf index of
-  every test row in every tree (tests/fixtures/{binary, missing, zero_as_missing, regression_l2,
+* ``predict/<case>/`` — six upstream models with their training / test rows, the leaf index of
+  every test row in every tree and the raw scores (tests/fixtures/{binary, missing, zero_as_missing, regression_l2,
   categorical, multiclass});
 * ``datasets/<case>.json`` + ``datasets/x_*.npz`` — the 20 upstream dataset cases of
   tests/fixtures/datasets: the value matrix and the bin mappers upstream's ``save_binary`` wrote
@@ -176,7 +176,7 @@ def copy_predict_cases(fx):
         src = os.path.join(fx, case)
         dst = os.path.join(HERE, "predict", case)
         os.makedirs(dst, exist_ok=True)
-        for name in ("train.npy", "test.npy", "pred_leaf.npy", "model.txt", "params.json"):
+        for name in ("train.npy", "test.npy", "pred_leaf.npy", "pred_raw.npy", "model.txt", "params.json"):
             shutil.copyfile(os.path.join(src, name), os.path.join(dst, name))
 
 

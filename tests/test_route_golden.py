@@ -9,7 +9,9 @@ become bin thresholds (a numerical threshold is one of its feature's bin upper b
 categorical split's category bitset becomes a bin bitset), and the rows are routed on their
 stored bins through the route tables of the learner's partition (data_partition.rs:264-410):
 every test row must reach upstream's leaf, NaN and zero-as-missing rows and unseen categories
-included. This is the routing that bk_learner_predict_add and the out-of-bag replay use.
+included; and the raw scores, the leaf values summed in tree order, equal upstream's bit for
+bit. This is the routing and the score update that bk_learner_predict_add and the out-of-bag
+replay use.
 """
 import json
 import os
@@ -71,7 +73,14 @@ def test_held_out_rows_reach_upstreams_leaves(oracle, bklib, case):
     trees = oracle.parse_model_trees(open(os.path.join(d, "model.txt")).read())
     assert want.shape == (len(test), len(trees))
     rows = np.arange(len(test))
+    raw_want = np.load(os.path.join(d, "pred_raw.npy")).reshape(len(test), -1)
+    K = raw_want.shape[1]
+    raw = np.zeros((len(test), K))
     for k, rec in enumerate(trees):
         got = oracle.replay_leaves(_Tree(rec, ds), held, rows)
         assert np.array_equal(got, want[:, k]), "tree %d: %d of %d rows differ" % (k, int(np.sum(got != want[:, k])),
                                                                                      len(rows))
+        # the score update: every tree's leaf value added in tree order (class k % K)
+        leaf_value = np.array([float(v) for v in rec["leaf_value"].split()])
+        raw[:, k % K] += leaf_value[got]
+    assert np.array_equal(raw, raw_want), "raw scores differ"
