@@ -250,7 +250,7 @@ def run_gpu(args, rank, world):
             t = Tree.from_records(args.leaves, sp, lvals, root, ds.features)
             t.apply_shrinkage(lr)
             learner.predict_add(t, ho_bins.data_ptr(), m_ho, ho_score.data_ptr())
-        stats["heldout_l2"] = float(((ho_score - ho_label) ** 2).mean().item())
+        stats["heldout_l2"] = _l2(ho_score, ho_label)
         stats["iterations"] = len(trees)
         learner.close()
         return stats
@@ -386,7 +386,7 @@ def run_multiclass(args):
                 t.apply_shrinkage(lr)
                 learner.predict_add(t, ho_bins.data_ptr(), m, ho[k].data_ptr())
         torch.cuda.synchronize()
-        ho_loss = float((torch.logsumexp(ho, 0) - ho.gather(0, ho_y[None, :])[0]).mean().item())
+        ho_loss = _multi_logloss(ho, ho_y)
         learner.close()
         return {"iters_per_s": round(1000.0 * steps / total_ms, 3), "ms_per_iter": round(total_ms / steps, 3),
                 "train_logloss": round(train_loss, 6), "heldout_logloss": round(ho_loss, 6),
@@ -489,6 +489,18 @@ def run_batched_jobs(args):
                         "mean_train_logloss": round(bat_loss, 6)},
             "speedup": round(seq_s / bat_s, 3), "prep_s": round(prep_s, 1),
             "learner_setup_s": round(setup_s, 2), "autotuned": bool(args.autotune)}
+
+
+def _l2(score, label):
+    """Mean squared error (metric/regression.rs `l2`)."""
+    return float(((score - label.to(score.dtype)) ** 2).mean().item())
+
+
+def _multi_logloss(score, label):
+    """Mean multi-class log loss of raw scores [K, n] (metric/multiclass.rs `multi_logloss`:
+    -log of the softmax probability of the label class)."""
+    import torch
+    return float((torch.logsumexp(score, 0) - score.gather(0, label.long()[None, :])[0]).mean().item())
 
 
 def _auc(score, label):

@@ -17,6 +17,8 @@ It copies, unchanged, the reference's own golden data for the tree-learner path:
 * ``predict/<case>/`` — six upstream models with their training / test rows, the leaf index of
   every test row in every tree and the raw scores (tests/fixtures/{binary, missing, zero_as_missing, regression_l2,
   categorical, multiclass});
+* ``metrics/{binary, reg, multiclass}/`` — scores, labels and upstream's metric values
+  (tests/fixtures/metrics), for the benchmark's held-out metrics;
 * ``datasets/<case>.json`` + ``datasets/x_*.npz`` — the 20 upstream dataset cases of
   tests/fixtures/datasets: the value matrix and the bin mappers upstream's ``save_binary`` wrote
   for it (read from its dataset.bin as the reference's io/binary.rs reads it);
@@ -169,6 +171,20 @@ def copy_datasets(fx):
 PREDICT_CASES = ["binary", "missing", "zero_as_missing", "regression_l2", "categorical", "multiclass"]
 
 
+METRIC_CASES = ["binary", "reg", "multiclass"]
+
+
+def copy_metric_cases(fx):
+    """tests/fixtures/metrics/{binary, reg, multiclass}: scores, labels and upstream's metric
+    values at those scores."""
+    for case in METRIC_CASES:
+        src = os.path.join(fx, "metrics", case)
+        dst = os.path.join(HERE, "metrics", case)
+        os.makedirs(dst, exist_ok=True)
+        for name in ("score.npy", "label.npy", "params.json", "expected.json"):
+            shutil.copyfile(os.path.join(src, name), os.path.join(dst, name))
+
+
 def copy_predict_cases(fx):
     """tests/fixtures/<case>: an upstream model, its training and test rows and the leaf every test
     row reaches in every tree (pred_leaf.npy), for the routing of held-out rows."""
@@ -197,6 +213,7 @@ def main(ref):
     shutil.copyfile(os.path.join(fx, "quantized_gradients.json"), os.path.join(HERE, "quantized_gradients.json"))
     copy_datasets(fx)
     copy_predict_cases(fx)
+    copy_metric_cases(fx)
 
     tests = os.path.join(ref, "crates", "lgbm-core", "tests")
     mt = open(os.path.join(tests, "mt19937.rs")).read()
