@@ -17,7 +17,6 @@ data so the learner can be driven without the Rust host:
 Numerical and categorical features (``categorical=`` column list) are supported.
 """
 from concurrent.futures import ThreadPoolExecutor
-import ctypes
 import math
 
 import numpy as np

@@ -24,8 +24,7 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 ROOT = os.path.dirname(HERE)
 sys.path.insert(0, os.path.join(ROOT, "bankai-lightgbm_gb300"))
 
-from lgbm_gb300.config import CONFIG_DTYPE, LearnerConfig  # noqa: E402
-from lgbm_gb300.dataset import FEATURE_DTYPE  # noqa: E402
+from lgbm_gb300.config import LearnerConfig  # noqa: E402
 from lgbm_gb300.dataset import _Random as LcgRandom  # noqa: E402  (utils/random.rs, the bin sampler's LCG)
 from lgbm_gb300.tree import SPLIT_DTYPE, Tree  # noqa: E402
 
