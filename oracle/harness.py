@@ -199,14 +199,25 @@ class L2Objective:
 
 
 class BinaryObjective:
-    """objective/binary.rs:71-115 (sigmoid, optional weights)."""
+    """objective/binary.rs:13-115 (sigmoid, is_unbalance / scale_pos_weight, optional weights)."""
     constant_hessian = False
     num_class = 1
 
-    def __init__(self, label, sigmoid=1.0, weights=None):
+    def __init__(self, label, sigmoid=1.0, weights=None, is_unbalance=False, scale_pos_weight=1.0):
         self.is_pos = np.asarray(label, dtype=np.float32) > 0
         self.s = float(sigmoid)
         self.w = None if weights is None else np.asarray(weights, dtype=np.float32)
+        # per-class label weights (binary.rs:33-41): is_unbalance up-weights the rarer class by the
+        # count ratio, then the positive class is scaled by scale_pos_weight
+        pos = int(np.sum(self.is_pos))
+        neg = len(self.is_pos) - pos
+        self.label_weights = [1.0, 1.0]
+        if is_unbalance and pos > 0 and neg > 0:
+            if pos > neg:
+                self.label_weights[0] = float(pos) / float(neg)
+            else:
+                self.label_weights[1] = float(neg) / float(pos)
+        self.label_weights[1] *= float(scale_pos_weight)
 
     def gradients(self, score):
         n = len(score)
@@ -215,15 +226,16 @@ class BinaryObjective:
         s = self.s
         for i in range(n):
             label = 1.0 if self.is_pos[i] else -1.0
+            lw = self.label_weights[1 if self.is_pos[i] else 0]
             response = -label * s / (1.0 + math.exp(label * s * float(score[i])))
             ar = abs(response)
             if self.w is None:
-                g[i] = np.float32(response * 1.0)
-                h[i] = np.float32(ar * (s - ar) * 1.0)
+                g[i] = np.float32(response * lw)
+                h[i] = np.float32(ar * (s - ar) * lw)
             else:
                 w = float(self.w[i])
-                g[i] = np.float32(response * 1.0 * w)
-                h[i] = np.float32(ar * (s - ar) * 1.0 * w)
+                g[i] = np.float32(response * lw * w)
+                h[i] = np.float32(ar * (s - ar) * lw * w)
         return g[None, :], h[None, :]
 
     def boost_from_score(self, k):
@@ -302,7 +314,8 @@ def make_objective(params, y, weights=None, fused=True):
     if obj in ("regression", "l2", "regression_l2", "mse"):
         return L2Objective(y, weights, fused)
     if obj == "binary":
-        return BinaryObjective(y, params.get("sigmoid", 1.0), weights)
+        return BinaryObjective(y, params.get("sigmoid", 1.0), weights, bool(params.get("is_unbalance", False)),
+                               float(params.get("scale_pos_weight", 1.0)))
     if obj in ("multiclass", "softmax"):
         return SoftmaxObjective(y, int(params["num_class"]), weights)
     raise ValueError("objective %r is outside the learner's scope" % obj)
@@ -351,16 +364,24 @@ class TreeColumnSampler:
 
 
 class RowBagging:
-    """Plain bagging (boosting/sample.rs:16-240 without the balanced / by-query / GOSS forms): one
-    LCG per 1024-row block seeded bagging_seed + block, one draw per row in row order, redrawn
-    every bagging_freq iterations. sample(iter) returns the ascending bag or None (all rows)."""
+    """Bagging (boosting/sample.rs:16-240 without the by-query / GOSS forms): one LCG per 1024-row
+    block seeded bagging_seed + block, one draw per row in row order, redrawn every bagging_freq
+    iterations; a row is kept when its draw is below bagging_fraction, or, balanced by label
+    (sample.rs:95-104,224-236; binary objective with positives only), below pos_bagging_fraction
+    for label > 0 and neg_bagging_fraction otherwise. sample(iter) returns the ascending bag or
+    None (all rows)."""
     BLOCK = 1024
 
-    def __init__(self, n, fraction, freq, seed):
+    def __init__(self, n, fraction, freq, seed, pos_fraction=1.0, neg_fraction=1.0, positive=None):
         self.n = n
         self.fraction = float(fraction)
         self.freq = int(freq)
-        self.active = self.fraction < 1.0 and self.freq > 0
+        self.positive = None if positive is None else np.asarray(positive, dtype=bool)
+        self.balanced = ((float(pos_fraction) < 1.0 or float(neg_fraction) < 1.0)
+                         and self.positive is not None and bool(self.positive.any()))
+        self.threshold = (np.where(self.positive, float(pos_fraction), float(neg_fraction)) if self.balanced
+                          else np.full(n, self.fraction))
+        self.active = (self.fraction < 1.0 or self.balanced) and self.freq > 0
         self.rands = [LcgRandom((int(seed) + b) & 0xFFFFFFFF) for b in range((n + self.BLOCK - 1) // self.BLOCK)]
         self.bag = None
         self.need = True
@@ -371,7 +392,8 @@ class RowBagging:
         if self.need or (len(self.bag) < self.n and it % self.freq == 0):
             self.need = False
             self.bag = np.array([i for i in range(self.n)
-                                 if float(self.rands[i // self.BLOCK].next_float()) < self.fraction], dtype=np.int32)
+                                 if float(self.rands[i // self.BLOCK].next_float()) < self.threshold[i]],
+                                dtype=np.int32)
         return self.bag if len(self.bag) < self.n else None
 
 
@@ -432,8 +454,9 @@ def parse_interaction_constraints(text):
     return [[int(v) for v in grp.split(",") if v.strip()] for grp in re.findall(r"\[([^\]]*)\]", text or "")]
 
 
-def samplers_from_params(resolved, ds):
-    """(TreeColumnSampler or None, RowBagging or None) for a resolved config."""
+def samplers_from_params(resolved, ds, label=None):
+    """(TreeColumnSampler or None, RowBagging or None) for a resolved config; ``label`` enables
+    bagging balanced by label for the binary objective."""
     ff = float(resolved.get("feature_fraction", 1))
     fn = float(resolved.get("feature_fraction_bynode", 1))
     icons = parse_interaction_constraints(resolved.get("interaction_constraints", ""))
@@ -442,8 +465,11 @@ def samplers_from_params(resolved, ds):
     if resolved.get("data_sample_strategy", "bagging") == "goss":
         return cols, Goss(ds.num_data, float(resolved["top_rate"]), float(resolved["other_rate"]),
                           float(resolved["learning_rate"]), int(resolved.get("bagging_seed", 3)))
+    positive = (np.asarray(label, dtype=np.float32) > 0
+                if label is not None and resolved.get("objective") == "binary" else None)
     bag = RowBagging(ds.num_data, float(resolved.get("bagging_fraction", 1)), int(resolved.get("bagging_freq", 0)),
-                     int(resolved.get("bagging_seed", 3)))
+                     int(resolved.get("bagging_seed", 3)), float(resolved.get("pos_bagging_fraction", 1)),
+                     float(resolved.get("neg_bagging_fraction", 1)), positive)
     return cols, (bag if bag.active else None)
 
 

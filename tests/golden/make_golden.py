@@ -12,6 +12,9 @@ It copies, unchanged, the reference's own golden data for the tree-learner path:
   scope (dense numerical and categorical features, L2 / binary / multiclass objectives; plain
   bagging and the by-tree feature fraction, which reach the learner as its `rows` and
   feature-mask inputs);
+* ``train_oracle/<case>/`` — the same files for three cases that differ from those only on the
+  Trainer's side of the learner (binary sigmoid 0.7 with scale_pos_weight 2.5, is_unbalance,
+  bagging balanced by label), pinned on the oracle;
 * ``quantized_gradients.json`` — 16 upstream stumps for the gradient discretizer
   (tests/fixtures/quantized_gradients.json);
 * ``predict/<case>/`` — six upstream models with their training / test rows, the leaf index of
@@ -50,6 +53,10 @@ CASES = ["binary", "l2_default", "l2_nan", "l2_zero", "l2_zero_as_missing", "l2_
          "multiclass_weighted", "bagging_weighted", "cat_default_weighted", "feature_fraction_bynode",
          "feature_fraction_both", "goss", "goss_dense_sample", "goss_weighted", "interaction", "interaction_bynode",
          "interaction_sampled"]
+# Cases whose differences lie on the Trainer's side of the learner only (the binary objective's
+# sigmoid and label weights, bagging balanced by label): copied to train_oracle/ and pinned on the
+# oracle; the learner receives the same kind of gradients and row lists as in the cases above.
+ORACLE_CASES = ["binary_sigmoid", "binary_unbalance", "bagging_balanced"]
 
 
 # ---- upstream binary dataset files (the reference's io/binary.rs reader, restated) ----
@@ -202,9 +209,9 @@ def _ints(text):
 
 def main(ref):
     fx = os.path.join(ref, "tests", "fixtures")
-    for case in CASES:
+    for case, sub in [(c, "train") for c in CASES] + [(c, "train_oracle") for c in ORACLE_CASES]:
         src = os.path.join(fx, "train", case)
-        dst = os.path.join(HERE, "train", case)
+        dst = os.path.join(HERE, sub, case)
         os.makedirs(dst, exist_ok=True)
         for name in ("x.npy", "y.npy", "w.npy", "params.json", "model.txt"):
             if name == "w.npy" and not os.path.exists(os.path.join(src, name)):

@@ -1,6 +1,6 @@
 """Pins the oracle to the reference's own golden data (no GPU).
 
-* the upstream-LightGBM models that bankai-lightgbm reproduces (tests/golden/train/*), rebuilt
+* the upstream-LightGBM models that bankai-lightgbm reproduces (tests/golden/train*/*), rebuilt
   tree by tree through the oracle learner, with both ``madd`` rounding modes (bagged cases pass
   their rows, feature-fraction cases a by-tree feature mask, drawn as the reference's Trainer
   draws them);
@@ -17,11 +17,14 @@ import pytest
 
 from conftest import GOLDEN
 
-CASES = sorted(os.listdir(os.path.join(GOLDEN, "train")))
+# train/: the cases the GPU learner is also checked on; train_oracle/: cases that differ only on
+# the Trainer's side of the learner (binary objective options, bagging balanced by label)
+CASES = ([("train", c) for c in sorted(os.listdir(os.path.join(GOLDEN, "train")))]
+         + [("train_oracle", c) for c in sorted(os.listdir(os.path.join(GOLDEN, "train_oracle")))])
 
 
 def _load_case(case):
-    d = os.path.join(GOLDEN, "train", case)
+    d = os.path.join(GOLDEN, *case)
     P = json.load(open(os.path.join(d, "params.json")))
     X = np.load(os.path.join(d, "x.npy"))
     y = np.load(os.path.join(d, "y.npy"))
@@ -38,7 +41,7 @@ def _dataset(p, X, categorical=()):
 
 
 @pytest.mark.parametrize("fused", [1, 0])
-@pytest.mark.parametrize("case", CASES)
+@pytest.mark.parametrize("case", CASES, ids=["/".join(c) for c in CASES])
 def test_oracle_reproduces_reference_models(oracle, bklib, case, fused):
     from lgbm_gb300 import LearnerConfig
     P, X, y, model = _load_case(case)
@@ -48,7 +51,7 @@ def test_oracle_reproduces_reference_models(oracle, bklib, case, fused):
     cfg = LearnerConfig(**p, fused_madd=fused, is_constant_hessian=int(obj.constant_hessian and
                                                                        p.get("data_sample_strategy") != "goss"))
     learner = oracle.OracleLearner(ds, cfg)
-    cols, bag = oracle.samplers_from_params(oracle.resolved_params(model), ds)
+    cols, bag = oracle.samplers_from_params(oracle.resolved_params(model), ds, y)
     trees, _ = oracle.train_gbdt(learner, ds, obj, P["num_boost_round"], learning_rate=p.get("learning_rate", 0.1),
                                  boost_from_average=p.get("boost_from_average", True),
                                  min_gain_to_split=p.get("min_gain_to_split", 0.0), col_sampler=cols, bagging=bag)
