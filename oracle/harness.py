@@ -198,6 +198,129 @@ class L2Objective:
         return suml / sumw
 
 
+class PointwiseRegression:
+    """The gradient-only regression objectives of objective/regression.rs:240-318 (unweighted)
+    and :349-407 (weighted): huber, fair, poisson, gamma and tweedie, with their initial scores
+    (:176-184: the label mean, weighted by madd, and its log for poisson, gamma and tweedie). The
+    leaf-renewing forms (l1, quantile, mape) are not restated."""
+    num_class = 1
+
+    def __init__(self, kind, label, params, weights=None, fused=True):
+        self.kind = kind
+        self.label = np.asarray(label, dtype=np.float32)
+        self.w = None if weights is None else np.asarray(weights, dtype=np.float32)
+        self.fused = fused
+        self.alpha = float(params.get("alpha", 0.9))
+        self.fair_c = float(params.get("fair_c", 1.0))
+        self.max_delta_step = float(params.get("poisson_max_delta_step", 0.7))
+        self.rho = float(params.get("tweedie_variance_power", 1.5))
+        self.constant_hessian = kind == "huber" and self.w is None
+
+    def gradients(self, score):
+        n = len(score)
+        g = np.empty(n, np.float32)
+        h = np.empty(n, np.float32)
+        emds = math.exp(self.max_delta_step)
+        rho = self.rho
+        for i in range(n):
+            sc, lab = float(score[i]), float(self.label[i])
+            if self.kind == "huber":
+                diff = sc - lab
+                sgn = 1.0 if diff > 0 else (-1.0 if diff < 0 else 0.0)
+                if self.w is None:
+                    g[i] = np.float32(diff if abs(diff) <= self.alpha else sgn * self.alpha)
+                    h[i] = 1.0
+                else:
+                    wi = self.w[i]
+                    # the clipped form is an f32 product sign * w, widened, times alpha
+                    g[i] = np.float32(diff * float(wi) if abs(diff) <= self.alpha
+                                      else float(np.float32(sgn) * wi) * self.alpha)
+                    h[i] = wi
+                continue
+            wi = 1.0 if self.w is None else float(self.w[i])
+            if self.kind == "fair":
+                x, c = sc - lab, self.fair_c
+                gv, hv = c * x / (abs(x) + c), c * c / ((abs(x) + c) * (abs(x) + c))
+            elif self.kind == "poisson":
+                e = math.exp(sc)
+                gv, hv = e - lab, e * emds
+            elif self.kind == "gamma":
+                e = math.exp(-sc)
+                gv, hv = _madd(-lab, e, 1.0, self.fused), lab * e
+            else:  # tweedie
+                e1 = math.exp((1.0 - rho) * sc)
+                e2 = math.exp((2.0 - rho) * sc)
+                gv = _madd(-lab, e1, e2, self.fused)
+                hv = _madd(-lab * (1.0 - rho), e1, (2.0 - rho) * e2, self.fused)
+            if self.w is None:
+                g[i], h[i] = np.float32(gv), np.float32(hv)
+            else:
+                g[i], h[i] = np.float32(gv * wi), np.float32(hv * wi)
+        return g[None, :], h[None, :]
+
+    def boost_from_score(self, k):
+        mean = L2Objective(self.label, self.w, self.fused).boost_from_score(k)
+        if self.kind in ("huber", "fair"):
+            return mean
+        return math.log(mean) if mean > 0.0 else -math.inf
+
+
+class CrossEntropyObjective:
+    """objective/xentropy.rs: cross_entropy (:62-91) and cross_entropy_lambda (:127-155), labels in
+    [0, 1], optional weights; initial scores from the (madd-weighted) label mean (:36-51)."""
+    num_class = 1
+    constant_hessian = False
+
+    def __init__(self, label, weights=None, fused=True, lam=False):
+        self.label = np.asarray(label, dtype=np.float32)
+        self.w = None if weights is None else np.asarray(weights, dtype=np.float32)
+        self.fused = fused
+        self.lam = lam
+
+    def gradients(self, score):
+        n = len(score)
+        g = np.empty(n, np.float32)
+        h = np.empty(n, np.float32)
+        for i in range(n):
+            sc, lab = float(score[i]), float(self.label[i])
+            if self.lam:
+                if self.w is None:
+                    z = 1.0 / (1.0 + math.exp(-sc))
+                    g[i], h[i] = np.float32(z - lab), np.float32(z * (1.0 - z))
+                    continue
+                w = float(self.w[i])
+                epf = math.exp(sc)
+                z = 1.0 - math.exp(-w * math.log1p(epf))
+                g[i] = np.float32((1.0 - lab / z) * w / (1.0 + 1.0 / epf))
+                c = 1.0 / (1.0 - z)
+                d = 1.0 + epf
+                a = w * epf / (d * d)
+                d = c - 1.0
+                b = (c / (d * d)) * (_madd(w, epf, 1.0, self.fused) - c)
+                h[i] = np.float32(a * _madd(lab, b, 1.0, self.fused))
+                continue
+            if sc > -37.0:
+                e = math.exp(-sc)
+                gi = _madd(-lab, e, float(np.float32(1.0) - self.label[i]), self.fused) / (1.0 + e)
+                hi = e / ((1.0 + e) * (1.0 + e))
+            else:
+                e = math.exp(sc)
+                gi, hi = e - lab, e
+            if self.w is None:
+                g[i], h[i] = np.float32(gi), np.float32(hi)
+            else:
+                w = float(self.w[i])
+                g[i], h[i] = np.float32(gi * w), np.float32(hi * w)
+        return g[None, :], h[None, :]
+
+    def boost_from_score(self, k):
+        mean = L2Objective(self.label, self.w, self.fused).boost_from_score(k)
+        if self.lam:
+            return math.log(math.expm1(mean))
+        pavg = max(min(mean, 1.0 - EPS), EPS)
+        return math.log(pavg / (1.0 - pavg))
+
+
 class BinaryObjective:
     """objective/binary.rs:13-115 (sigmoid, is_unbalance / scale_pos_weight, optional weights)."""
     constant_hessian = False
@@ -312,7 +435,14 @@ class SoftmaxObjective:
 def make_objective(params, y, weights=None, fused=True):
     obj = params.get("objective", "regression")
     if obj in ("regression", "l2", "regression_l2", "mse"):
+        if params.get("reg_sqrt", False):
+            # regression.rs:50-71: the model is fitted to sign(y) * sqrt(|y|), an f32 label
+            y = np.sign(np.asarray(y, np.float32)) * np.sqrt(np.abs(np.asarray(y, np.float32)))
         return L2Objective(y, weights, fused)
+    if obj in ("cross_entropy", "xentropy", "cross_entropy_lambda", "xentlambda"):
+        return CrossEntropyObjective(y, weights, fused, lam=obj in ("cross_entropy_lambda", "xentlambda"))
+    if obj in ("huber", "fair", "poisson", "gamma", "tweedie"):
+        return PointwiseRegression(obj, y, params, weights, fused)
     if obj == "binary":
         return BinaryObjective(y, params.get("sigmoid", 1.0), weights, bool(params.get("is_unbalance", False)),
                                float(params.get("scale_pos_weight", 1.0)))

@@ -12,9 +12,11 @@ It copies, unchanged, the reference's own golden data for the tree-learner path:
   scope (dense numerical and categorical features, L2 / binary / multiclass objectives; plain
   bagging and the by-tree feature fraction, which reach the learner as its `rows` and
   feature-mask inputs);
-* ``train_oracle/<case>/`` — the same files for three cases that differ from those only on the
+* ``train_oracle/<case>/`` — the same files for 18 cases that differ from those only on the
   Trainer's side of the learner (binary sigmoid 0.7 with scale_pos_weight 2.5, is_unbalance,
-  bagging balanced by label), pinned on the oracle;
+  bagging balanced by label, reg_sqrt, huber, fair, poisson, gamma, tweedie, cross_entropy and
+  cross_entropy_lambda, weighted and not), pinned on the oracle; where upstream's libm gives a
+  different model on linux-x86_64 the reference's ``model.linux-x86_64.txt`` comes too;
 * ``quantized_gradients.json`` — 16 upstream stumps for the gradient discretizer
   (tests/fixtures/quantized_gradients.json);
 * ``predict/<case>/`` — six upstream models with their training / test rows, the leaf index of
@@ -54,9 +56,12 @@ CASES = ["binary", "l2_default", "l2_nan", "l2_zero", "l2_zero_as_missing", "l2_
          "feature_fraction_both", "goss", "goss_dense_sample", "goss_weighted", "interaction", "interaction_bynode",
          "interaction_sampled"]
 # Cases whose differences lie on the Trainer's side of the learner only (the binary objective's
-# sigmoid and label weights, bagging balanced by label): copied to train_oracle/ and pinned on the
-# oracle; the learner receives the same kind of gradients and row lists as in the cases above.
-ORACLE_CASES = ["binary_sigmoid", "binary_unbalance", "bagging_balanced"]
+# sigmoid and label weights, bagging balanced by label, the gradient-only regression and
+# cross-entropy objectives): copied to train_oracle/ and pinned on the oracle; the learner receives
+# the same kind of gradients and row lists as in the cases above.
+ORACLE_CASES = ["binary_sigmoid", "binary_unbalance", "bagging_balanced", "l2_sqrt", "huber", "huber_weighted",
+                "fair", "fair_weighted", "poisson", "poisson_weighted", "gamma", "gamma_weighted", "tweedie",
+                "tweedie_weighted", "xentropy", "xentropy_weighted", "xentlambda", "xentlambda_weighted"]
 
 
 # ---- upstream binary dataset files (the reference's io/binary.rs reader, restated) ----
@@ -213,9 +218,9 @@ def main(ref):
         src = os.path.join(fx, "train", case)
         dst = os.path.join(HERE, sub, case)
         os.makedirs(dst, exist_ok=True)
-        for name in ("x.npy", "y.npy", "w.npy", "params.json", "model.txt"):
-            if name == "w.npy" and not os.path.exists(os.path.join(src, name)):
-                continue  # sample weights only where the case has them
+        for name in ("x.npy", "y.npy", "w.npy", "params.json", "model.txt", "model.linux-x86_64.txt"):
+            if name in ("w.npy", "model.linux-x86_64.txt") and not os.path.exists(os.path.join(src, name)):
+                continue  # sample weights, and the linux-x86_64 libm variant, only where the case has them
             shutil.copyfile(os.path.join(src, name), os.path.join(dst, name))
     shutil.copyfile(os.path.join(fx, "quantized_gradients.json"), os.path.join(HERE, "quantized_gradients.json"))
     copy_datasets(fx)
