@@ -26,7 +26,7 @@ sys.path.insert(0, os.path.join(ROOT, "bankai-lightgbm_gb300"))
 
 from lgbm_gb300.config import LearnerConfig  # noqa: E402
 from lgbm_gb300.dataset import _Random as LcgRandom  # noqa: E402  (utils/random.rs, the bin sampler's LCG)
-from lgbm_gb300.tree import SPLIT_DTYPE, Tree  # noqa: E402
+from lgbm_gb300.tree import SPLIT_DTYPE, Tree, _round_to_zero  # noqa: E402
 
 EPS = float(np.float32(1e-15))
 _olib = None
@@ -265,6 +265,105 @@ class PointwiseRegression:
         return math.log(mean) if mean > 0.0 else -math.inf
 
 
+def _percentile(vals, alpha, f32, fused):
+    """regression.rs:413-437 (upstream's PercentileFun): interpolate between the order statistics
+    around (n - 1) * (1 - alpha) counted from the largest, v1 - (v1 - v2) * bias as one madd;
+    ``f32`` values take their difference in f32."""
+    n = len(vals)
+    if n <= 1:
+        return vals[0]
+    float_pos = (n - 1) * (1.0 - alpha)
+    pos = int(float_pos) + 1
+    if pos < 1:
+        return max(vals)
+    if pos >= n:
+        return min(vals)
+    bias = float_pos - (pos - 1)
+    desc = sorted(vals, reverse=True)
+    v1, v2 = desc[pos - 1], desc[pos]
+    diff = float(np.float32(v1) - np.float32(v2)) if f32 else v1 - v2
+    out = _madd(-diff, bias, float(v1), fused)
+    return float(np.float32(out)) if f32 else out
+
+
+def _weighted_percentile(vals, weights, alpha, f32, fused):
+    """regression.rs:439-478 (upstream's WeightedPercentileFun): a stable ascending sort, the f64
+    cumulative weights, the first position above alpha of the total, and a linear interpolation
+    when that step carries a weight of at least 1."""
+    n = len(vals)
+    if n <= 1:
+        return vals[0]
+    idx = sorted(range(n), key=lambda i: vals[i])
+    cdf = []
+    acc = 0.0
+    for j, i in enumerate(idx):
+        acc = float(weights[i]) if j == 0 else acc + float(weights[i])
+        cdf.append(acc)
+    threshold = cdf[n - 1] * alpha
+    pos = min(int(np.searchsorted(np.asarray(cdf), threshold, side="right")), n - 1)
+    if pos == 0 or pos == n - 1:
+        return vals[idx[pos]]
+    v1, v2 = vals[idx[pos - 1]], vals[idx[pos]]
+    if cdf[pos] - cdf[pos - 1] >= 1.0:
+        t = (threshold - cdf[pos - 1]) / (cdf[pos] - cdf[pos - 1])
+        diff = float(np.float32(v2) - np.float32(v1)) if f32 else v2 - v1
+        out = _madd(t, diff, float(v1), fused)
+        return float(np.float32(out)) if f32 else out
+    return v1
+
+
+class RenewingRegression:
+    """The leaf-renewing regression objectives of objective/regression.rs: l1, quantile and mape
+    (gradients :215-255 and :331-384; initial scores :185-195 from the label's (weighted)
+    percentile; after each tree, every leaf's output becomes the (weighted) percentile of its
+    rows' residuals label - score, :209-238, called per leaf by boosting/train.rs:1198-1211 before
+    shrinkage, on the leaf's rows in partition order)."""
+    num_class = 1
+
+    def __init__(self, kind, label, params, weights=None, fused=True):
+        self.kind = kind
+        self.label = np.asarray(label, dtype=np.float32)
+        self.w = None if weights is None else np.asarray(weights, dtype=np.float32)
+        self.fused = fused
+        self.alpha_f32 = np.float32(params.get("alpha", 0.9))
+        self.alpha = 0.5 if kind in ("l1", "mape") else float(self.alpha_f32)
+        self.constant_hessian = kind == "mape" or self.w is None
+        if kind == "mape":
+            lw = np.float32(1.0) / np.maximum(np.abs(self.label), np.float32(1.0))
+            self.label_weight = (lw if self.w is None else lw * self.w).astype(np.float32)
+
+    def gradients(self, score):
+        n = len(score)
+        g = np.empty(n, np.float32)
+        h = np.ones(n, np.float32) if self.w is None else self.w.copy()
+        for i in range(n):
+            diff = float(score[i]) - float(self.label[i])
+            sgn = np.float32(1.0 if diff > 0 else (-1.0 if diff < 0 else 0.0))
+            if self.kind == "l1":
+                g[i] = sgn if self.w is None else sgn * self.w[i]
+            elif self.kind == "quantile":
+                v = np.float32(1.0) - self.alpha_f32 if np.float32(diff) >= 0 else -self.alpha_f32
+                g[i] = v if self.w is None else v * self.w[i]
+            else:  # mape
+                g[i] = sgn * self.label_weight[i]
+        return g[None, :], h[None, :]
+
+    def _pct(self, vals, weights, f32):
+        if weights is None:
+            return _percentile(vals, self.alpha, f32, self.fused)
+        return _weighted_percentile(vals, weights, self.alpha, f32, self.fused)
+
+    def boost_from_score(self, k):
+        vals = [float(v) for v in self.label]
+        weights = self.label_weight if self.kind == "mape" else self.w
+        return self._pct(vals, weights, True)
+
+    def renew_tree_output(self, score, rows):
+        vals = [float(self.label[r]) - float(score[r]) for r in rows]
+        weights = self.label_weight if self.kind == "mape" else self.w
+        return self._pct(vals, None if weights is None else weights[rows], False)
+
+
 class CrossEntropyObjective:
     """objective/xentropy.rs: cross_entropy (:62-91) and cross_entropy_lambda (:127-155), labels in
     [0, 1], optional weights; initial scores from the (madd-weighted) label mean (:36-51)."""
@@ -441,6 +540,8 @@ def make_objective(params, y, weights=None, fused=True):
         return L2Objective(y, weights, fused)
     if obj in ("cross_entropy", "xentropy", "cross_entropy_lambda", "xentlambda"):
         return CrossEntropyObjective(y, weights, fused, lam=obj in ("cross_entropy_lambda", "xentlambda"))
+    if obj in ("regression_l1", "l1", "mae", "quantile", "mape"):
+        return RenewingRegression("l1" if obj in ("regression_l1", "l1", "mae") else obj, y, params, weights, fused)
     if obj in ("huber", "fair", "poisson", "gamma", "tweedie"):
         return PointwiseRegression(obj, y, params, weights, fused)
     if obj == "binary":
@@ -635,9 +736,10 @@ def replay_leaves(tree, ds, rows):
 
 def train_gbdt(learner, ds, objective, rounds, learning_rate=0.1, boost_from_average=True,
                min_gain_to_split=0.0, col_sampler=None, bagging=None):
-    """train.rs:723-839 with optional plain bagging (rows passed to the learner, out-of-bag rows
-    scored by replaying the tree, serial.rs:1995-2000) and a by-tree column sample (a mask set
-    before each tree); no DART / RF / GOSS. Returns (trees, score)."""
+    """train.rs:723-839 with optional bagging or GOSS (rows passed to the learner, out-of-bag rows
+    scored by replaying the tree, serial.rs:1995-2000), a column sampler (a mask set before each
+    tree) and the objective's leaf renewal before shrinkage (train.rs:780-783); no DART / RF.
+    Returns (trees, score)."""
     K = getattr(objective, "num_class", 1)
     n = ds.num_data
     score = np.zeros((K, n), dtype=np.float64)
@@ -669,8 +771,13 @@ def train_gbdt(learner, ds, objective, rounds, learning_rate=0.1, boost_from_ave
             t = Tree.from_records(learner.num_leaves, recs, leaf_values, root, ds.features, min_gain_to_split)
             if t.num_leaves > 1:
                 cont = True
-                t.apply_shrinkage(learning_rate)
                 leaf = learner.row_leaf()
+                if hasattr(objective, "renew_tree_output"):
+                    for lf in range(t.num_leaves):
+                        rows_lf = np.nonzero(leaf == lf)[0]  # ascending: the stable partition's order
+                        if len(rows_lf):
+                            t.leaf_value[lf] = _round_to_zero(objective.renew_tree_output(score[k], rows_lf))
+                t.apply_shrinkage(learning_rate)
                 inbag = leaf >= 0
                 score[k][inbag] += t.leaf_value[leaf[inbag]]
                 if oob is not None and len(oob):
