@@ -475,6 +475,29 @@ class BinaryObjective:
         return math.log(pavg / (1.0 - pavg)) / self.s
 
 
+class OvaObjective:
+    """objective/multiclass.rs:114-170: one binary objective per class, class k's positives being
+    the rows whose label truncates to k."""
+    constant_hessian = False
+
+    def __init__(self, label, num_class, sigmoid=1.0, weights=None, is_unbalance=False, scale_pos_weight=1.0):
+        self.num_class = num_class
+        lab = np.asarray(label, dtype=np.float32).astype(np.int32)
+        self.binary = [BinaryObjective((lab == k).astype(np.float32), sigmoid, weights, is_unbalance,
+                                       scale_pos_weight) for k in range(num_class)]
+
+    def gradients(self, score):
+        gh = [b.gradients(score[k]) for k, b in enumerate(self.binary)]
+        return np.concatenate([g for g, _ in gh]), np.concatenate([h for _, h in gh])
+
+    def boost_from_score(self, k):
+        return self.binary[k].boost_from_score(0)
+
+    def class_need_train(self, k):
+        pos = self.binary[k].is_pos
+        return bool(pos.any()) and not bool(pos.all())
+
+
 class SoftmaxObjective:
     """objective/multiclass.rs:20-110 (optional weights)."""
     constant_hessian = False
@@ -547,6 +570,9 @@ def make_objective(params, y, weights=None, fused=True):
     if obj == "binary":
         return BinaryObjective(y, params.get("sigmoid", 1.0), weights, bool(params.get("is_unbalance", False)),
                                float(params.get("scale_pos_weight", 1.0)))
+    if obj in ("multiclassova", "multiclass_ova", "ova", "ovr"):
+        return OvaObjective(y, int(params["num_class"]), params.get("sigmoid", 1.0), weights,
+                            bool(params.get("is_unbalance", False)), float(params.get("scale_pos_weight", 1.0)))
     if obj in ("multiclass", "softmax"):
         return SoftmaxObjective(y, int(params["num_class"]), weights)
     raise ValueError("objective %r is outside the learner's scope" % obj)
