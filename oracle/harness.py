@@ -760,6 +760,42 @@ def replay_leaves(tree, ds, rows):
     return leaf
 
 
+def train_rf(learner, ds, objective, rounds, min_gain_to_split=0.0, col_sampler=None, bagging=None):
+    """Random forest boosting (boosting/train.rs:600-608,637-700): the gradients are taken once at
+    the initial score; each iteration's trees are grown on a fresh row sample of those same
+    gradients, renewed against the initial score, carry the initial score as a bias and are not
+    shrunk. Returns the trees."""
+    K = getattr(objective, "num_class", 1)
+    n = ds.num_data
+    init = [0.0] * K
+    for k in range(K):
+        v = objective.boost_from_score(k)
+        init[k] = v if abs(v) > EPS else 0.0
+    pred = np.repeat(np.asarray(init, dtype=np.float64)[:, None], n, axis=1)
+    g, h = objective.gradients(pred[0] if K == 1 else pred)
+    trees = []
+    for it in range(rounds):
+        rows = bagging.sample(it) if bagging is not None else None
+        for k in range(K):
+            if col_sampler is not None:
+                col_sampler.before_tree(learner)
+            recs, leaf_values, root = learner.train(g[k], h[k], rows)
+            if col_sampler is not None:
+                col_sampler.after_tree(learner)
+            t = Tree.from_records(learner.num_leaves, recs, leaf_values, root, ds.features, min_gain_to_split)
+            if t.num_leaves > 1:
+                if hasattr(objective, "renew_tree_output"):
+                    leaf = learner.row_leaf()
+                    for lf in range(t.num_leaves):
+                        rows_lf = np.nonzero(leaf == lf)[0]
+                        if len(rows_lf):
+                            t.leaf_value[lf] = _round_to_zero(objective.renew_tree_output(pred[k], rows_lf))
+                if abs(init[k]) > EPS:
+                    t.add_bias(init[k])
+            trees.append(t)
+    return trees
+
+
 def train_gbdt(learner, ds, objective, rounds, learning_rate=0.1, boost_from_average=True,
                min_gain_to_split=0.0, col_sampler=None, bagging=None):
     """train.rs:723-839 with optional bagging or GOSS (rows passed to the learner, out-of-bag rows

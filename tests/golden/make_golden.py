@@ -12,11 +12,11 @@ It copies, unchanged, the reference's own golden data for the tree-learner path:
   scope (dense numerical and categorical features, L2 / binary / multiclass objectives; plain
   bagging and the by-tree feature fraction, which reach the learner as its `rows` and
   feature-mask inputs);
-* ``train_oracle/<case>/`` — the same files for 28 cases that differ from those only on the
+* ``train_oracle/<case>/`` — the same files for 31 cases that differ from those only on the
   Trainer's side of the learner (binary sigmoid 0.7 with scale_pos_weight 2.5, is_unbalance,
   bagging balanced by label, reg_sqrt, huber, fair, poisson, gamma, tweedie, cross_entropy,
   cross_entropy_lambda, one-vs-all multiclass, and the leaf-renewing l1, quantile and mape,
-  weighted and not), pinned on
+  weighted and not; random-forest boosting), pinned on
   the oracle; where the reference keeps the model its linux-x86_64 build gives (unfused madd,
   glibc's libm) as ``model.linux-x86_64.txt``, that file comes too;
 * ``quantized_gradients.json`` — 16 upstream stumps for the gradient discretizer
@@ -65,7 +65,7 @@ ORACLE_CASES = ["binary_sigmoid", "binary_unbalance", "bagging_balanced", "l2_sq
                 "fair", "fair_weighted", "poisson", "poisson_weighted", "gamma", "gamma_weighted", "tweedie",
                 "tweedie_weighted", "xentropy", "xentropy_weighted", "xentlambda", "xentlambda_weighted", "l1",
                 "l1_weighted", "l1_no_boost_from_average", "quantile", "quantile_high", "quantile_weighted", "mape",
-                "mape_weighted", "multiclassova", "multiclassova_weighted"]
+                "mape_weighted", "multiclassova", "multiclassova_weighted", "rf", "rf_binary", "rf_feature_fraction"]
 
 
 # ---- upstream binary dataset files (the reference's io/binary.rs reader, restated) ----

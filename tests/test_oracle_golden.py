@@ -80,9 +80,13 @@ def test_oracle_reproduces_reference_models(oracle, bklib, case, fused):
                                                                        p.get("data_sample_strategy") != "goss"))
     learner = oracle.OracleLearner(ds, cfg)
     cols, bag = oracle.samplers_from_params(oracle.resolved_params(model), ds, y)
-    trees, _ = oracle.train_gbdt(learner, ds, obj, P["num_boost_round"], learning_rate=p.get("learning_rate", 0.1),
-                                 boost_from_average=p.get("boost_from_average", True),
-                                 min_gain_to_split=p.get("min_gain_to_split", 0.0), col_sampler=cols, bagging=bag)
+    if p.get("boosting") in ("rf", "random_forest"):
+        trees = oracle.train_rf(learner, ds, obj, P["num_boost_round"], min_gain_to_split=p.get("min_gain_to_split", 0.0),
+                                col_sampler=cols, bagging=bag)
+    else:
+        trees, _ = oracle.train_gbdt(learner, ds, obj, P["num_boost_round"], learning_rate=p.get("learning_rate", 0.1),
+                                     boost_from_average=p.get("boost_from_average", True),
+                                     min_gain_to_split=p.get("min_gain_to_split", 0.0), col_sampler=cols, bagging=bag)
     ref = oracle.parse_model_trees(model)
     assert len(trees) == len(ref)
     exact = total = 0
