@@ -245,3 +245,23 @@ def test_int_split_search_brute_force(oracle):
             assert abs(o["gain"] - want["gain"]) <= 1e-12 * max(abs(want["gain"]), 1.0)
             assert abs(o["left_output"] - want["left_output"]) <= 1e-12
             assert abs(o["right_output"] - want["right_output"]) <= 1e-12
+
+
+@pytest.mark.parametrize("fused", [True, False])
+def test_percentile_matches_order_statistics(oracle, fused):
+    """The reference's unit check of its percentile (objective/regression.rs:487-503): between the
+    order statistics around (n - 1) * (1 - alpha) counted from the largest, to 1e-12."""
+    data = [5.0, 1.0, 4.0, 4.0, 2.0, 9.0, 7.0, 3.0]
+    desc = sorted(data, reverse=True)
+    for alpha in (0.1, 0.3, 0.5, 0.7, 0.9):
+        got = oracle._percentile(data, alpha, False, fused)
+        fp = (len(data) - 1) * (1.0 - alpha)
+        pos = int(fp) + 1
+        bias = fp - (pos - 1)
+        v1, v2 = desc[pos - 1], desc[pos]
+        assert abs(got - (v1 - (v1 - v2) * bias)) < 1e-12, alpha
+    # with unit weights every step of the cumulative weight is 1, so the weighted form
+    # interpolates between neighbouring order statistics too
+    for alpha in (0.25, 0.5, 0.75):
+        got = oracle._weighted_percentile(data, [1.0] * len(data), alpha, False, fused)
+        assert min(data) <= got <= max(data)
