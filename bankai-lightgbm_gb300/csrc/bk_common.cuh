@@ -252,10 +252,11 @@ cudaError_t predict_tree(const DevFeature* feats, int32_t num_leaves, const int3
                          const uint8_t* bins, int64_t m, double* score, cudaStream_t s);
 
 // bk_objective.cu
+// bad_label: device counter of multiclass labels outside [0, K) (kind 2 only)
 cudaError_t objective_gradients(int kind, const double* score, const float* label, int64_t n, int K, double sigmoid,
-                                float* g, float* h, cudaStream_t s);
+                                float* g, float* h, int32_t* bad_label, cudaStream_t s);
 cudaError_t objective_loss(int kind, const double* score, const float* label, int64_t n, int K, double* partial,
-                           int grid, cudaStream_t s);
+                           int grid, int32_t* bad_label, cudaStream_t s);
 void launch_tree_begin(const Job* d_jobs, int num_jobs, const Params& p, cudaStream_t s);
 
 }  // namespace bk

@@ -23,6 +23,8 @@
 //
 // The last CTA of tile 0 also computes the per-leaf constants of the search that follows
 // (bk_leaf.cuh) before its own rows.
+#include <mutex>
+
 #include "bk_launch.cuh"
 #include "bk_leaf.cuh"
 
@@ -388,17 +390,23 @@ void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t
 }
 
 cudaError_t hist_set_smem_attrs(size_t smem) {
-  // The attribute is per kernel and process-wide: only ever raise it, so learners created
-  // earlier with larger tiles keep working.
-  static size_t current = 0;
-  if (smem <= current) return cudaSuccess;
-  cudaError_t e = cudaSuccess;
+  // The attribute belongs to the kernel on the current device: remember the largest value set on
+  // each device and only ever raise it, so learners created earlier with larger tiles keep working.
+  constexpr int kMaxDevices = 64;
+  static std::mutex m;
+  static size_t current[kMaxDevices] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= kMaxDevices) return cudaErrorInvalidDevice;
+  std::lock_guard<std::mutex> g(m);
+  if (smem <= current[dev]) return cudaSuccess;
   int v = (int)smem;
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hist_int<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hist_int<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hist_float<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
   if (e == cudaSuccess) e = cudaFuncSetAttribute(k_hist_float<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, v);
-  if (e == cudaSuccess) current = smem;
+  if (e == cudaSuccess) current[dev] = smem;
   return e;
 }
 

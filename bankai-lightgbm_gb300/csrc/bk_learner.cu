@@ -150,6 +150,8 @@ struct bk_learner {
   bk_split* h_records = nullptr;
   double* h_leaf_values = nullptr;
   JobState* h_state = nullptr;
+  int32_t* d_bad_label = nullptr;  // multiclass labels outside [0, K) seen by the objective kernels
+  int32_t* h_bad_label = nullptr;  // pinned copy, read by the train call that follows the gradients
   double* d_leaf_vals_in = nullptr;
   int32_t* d_tree = nullptr;     // one tree's node arrays for prediction (5 x (num_leaves - 1))
   double* d_tree_values = nullptr;
@@ -175,6 +177,7 @@ struct bk_learner {
     if (h_records) cudaFreeHost(h_records);
     if (h_leaf_values) cudaFreeHost(h_leaf_values);
     if (h_state) cudaFreeHost(h_state);
+    if (h_bad_label) cudaFreeHost(h_bad_label);
     for (cudaEvent_t e : hist_events) cudaEventDestroy(e);
     if (ev_start) cudaEventDestroy(ev_start);
     if (ev_end) cudaEventDestroy(ev_end);
@@ -528,6 +531,10 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
     CK(cudaMallocHost(&L->h_records, sizeof(bk_split) * (size_t)Lv * K));
     CK(cudaMallocHost(&L->h_leaf_values, sizeof(double) * (size_t)Lv * K));
     CK(cudaMallocHost(&L->h_state, sizeof(JobState) * K));
+    CK(cudaMallocHost(&L->h_bad_label, sizeof(int32_t)));
+    *L->h_bad_label = 0;
+    L->d_bad_label = L->dalloc<int32_t>(1);
+    CK(cudaMemset(L->d_bad_label, 0, sizeof(int32_t)));
     L->d_leaf_vals_in = L->dalloc<double>((size_t)Lv * K);
     L->d_tree = L->dalloc<int32_t>(5 * (size_t)Lv);
     L->d_tree_values = L->dalloc<double>(Lv);
@@ -613,8 +620,20 @@ bool train_enqueue(bk_learner* L, const float* gradients, const float* hessians,
                        L->stream));
     CK(cudaMemcpyAsync(&L->h_state[j], J.st, offsetof(JobState, mt), cudaMemcpyDeviceToHost, L->stream));
   }
+  // labels the objective kernels rejected since the previous train call
+  CK(cudaMemcpyAsync(L->h_bad_label, L->d_bad_label, sizeof(int32_t), cudaMemcpyDeviceToHost, L->stream));
+  CK(cudaMemsetAsync(L->d_bad_label, 0, sizeof(int32_t), L->stream));
   CK(cudaEventRecord(L->ev_end, L->stream));
   return true;
+}
+
+// After train_finish: a multiclass label outside [0, K) met by bk_learner_objective_gradients
+// before this train call fails the call (the trees were grown on those gradients).
+bool labels_ok(bk_learner* L) {
+  if (*L->h_bad_label == 0) return true;
+  set_error("bk_learner_objective_gradients: %d multiclass labels outside [0, %d) before this train call",
+            *L->h_bad_label, L->K);
+  return false;
 }
 
 // The synchronous half: waits for the learner's stream, reads the timings and fills the outputs.
@@ -676,6 +695,7 @@ int bk_learner_train(bk_learner* L, const float* gradients, const float* hessian
   try {
     if (!train_enqueue(L, gradients, hessians, on_device, rows, num_rows, 0.0, nullptr)) return -1;
     train_finish(L, splits, leaf_values, root_outputs, num_leaves_out);
+    if (!labels_ok(L)) return -1;
   } catch (const CudaError& e) {
     return fail_cuda(e);
   }
@@ -847,6 +867,12 @@ int bk_learners_train_batch(bk_learner* const* learners, int32_t count, const fl
     for (i = 0; i < count; ++i)
       train_finish(learners[i], splits ? splits[i] : nullptr, leaf_values ? leaf_values[i] : nullptr,
                    root_outputs ? root_outputs[i] : nullptr, num_leaves_out ? num_leaves_out[i] : nullptr);
+    for (i = 0; i < count; ++i)
+      if (!labels_ok(learners[i])) {
+        std::string msg = g_last_error;
+        set_error("bk_learners_train_batch: learner %d: %s", i, msg.c_str());
+        return -1;
+      }
   } catch (const CudaError& e) {
     for (int32_t k = 0; k < count; ++k) cudaStreamSynchronize(learners[k]->stream);
     set_error("bk_learners_train_batch: learner %d: CUDA error: %s", i, e.msg.c_str());
@@ -1111,7 +1137,7 @@ int bk_learner_objective_gradients(bk_learner* L, int32_t kind, const double* sc
     return -1;
   }
   try {
-    CK(objective_gradients(kind, score, label, L->p.n, L->K, sigmoid, L->d_g, L->d_h, L->stream));
+    CK(objective_gradients(kind, score, label, L->p.n, L->K, sigmoid, L->d_g, L->d_h, L->d_bad_label, L->stream));
   } catch (const CudaError& e) {
     return fail_cuda(e);
   }
@@ -1119,17 +1145,27 @@ int bk_learner_objective_gradients(bk_learner* L, int32_t kind, const double* sc
 }
 
 int bk_learner_objective_loss(bk_learner* L, int32_t kind, const double* score, const float* label, double* out) {
-  if (!L || !score || !label || !out || kind < 0 || kind > 2) {
-    set_error("bk_learner_objective_loss: invalid arguments");
+  if (!L || !score || !label || !out || kind < 0 || kind > 2 || (kind == 2) != (L->K > 1) || L->K > 32) {
+    set_error("bk_learner_objective_loss: invalid arguments (kind %d, num_jobs %d)", kind, L ? L->K : 0);
     return -1;
   }
   try {
     const int grid = 512;
     double* d_part = L->jobs[0].red;  // 2 * kRootGrid >= grid doubles of scratch
-    CK(objective_loss(kind, score, label, L->p.n, L->K, d_part, grid, L->stream));
+    int32_t* d_bad = L->d_bad_label + 0;
+    // the loss counts its own rejected labels: the gradients' count is kept for the next train call
+    int32_t bad_before = 0, bad_after = 0;
+    CK(cudaMemcpyAsync(&bad_before, d_bad, sizeof(int32_t), cudaMemcpyDeviceToHost, L->stream));
+    CK(objective_loss(kind, score, label, L->p.n, L->K, d_part, grid, d_bad, L->stream));
     std::vector<double> part(grid);
     CK(cudaMemcpyAsync(part.data(), d_part, sizeof(double) * grid, cudaMemcpyDeviceToHost, L->stream));
+    CK(cudaMemcpyAsync(&bad_after, d_bad, sizeof(int32_t), cudaMemcpyDeviceToHost, L->stream));
     CK(cudaStreamSynchronize(L->stream));
+    if (bad_after != bad_before) {
+      CK(cudaMemcpy(d_bad, &bad_before, sizeof(int32_t), cudaMemcpyHostToDevice));
+      set_error("bk_learner_objective_loss: %d multiclass labels outside [0, %d)", bad_after - bad_before, L->K);
+      return -1;
+    }
     double s = 0.0;
     for (double v : part) s += v;
     *out = s / (double)L->p.n;

@@ -148,6 +148,8 @@ extern "C" int bk_partition_split_noalloc(const int32_t* rows_in, int64_t num_ro
                       "(1024 chunks of at most 2^20 rows)");
     return -1;
   }
+  // an error left on this thread by earlier, unrelated work must not fail this call
+  (void)cudaGetLastError();
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
@@ -187,11 +189,15 @@ extern "C" int bk_partition_split_noalloc(const int32_t* rows_in, int64_t num_ro
     return -1;
   }
   k_na_count<<<blocks, kThreads, 0, s>>>(rows_in, num_rows, chunk, bins, bins_len, rt, scratch);
-  k_na_scatter<<<blocks, kThreads, 0, s>>>(rows_in, num_rows, chunk, bins, bins_len, rt, rows_out, scratch);
+  e = cudaGetLastError();
+  if (e == cudaSuccess) {
+    k_na_scatter<<<blocks, kThreads, 0, s>>>(rows_in, num_rows, chunk, bins, bins_len, rt, rows_out, scratch);
+    e = cudaGetLastError();
+  }
   int64_t result[2] = {0, 0};
-  e = cudaMemcpyAsync(result, scratch + kMaxBlocks, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(result, scratch + kMaxBlocks, 2 * sizeof(int64_t), cudaMemcpyDeviceToHost, s);
   if (e == cudaSuccess) e = cudaStreamSynchronize(s);
-  if (e == cudaSuccess) e = cudaGetLastError();
   if (e != cudaSuccess) {
     bk_set_last_error(cudaGetErrorString(e));
     return -1;

@@ -6,6 +6,10 @@
 // Operation order follows the reference. `exp` is CUDA's double-precision exp, which can differ
 // from the host libm's in the last bit, so binary / multiclass gradients may differ from a host
 // computation by one f32 ulp; the learner's parity is checked on given gradients.
+//
+// A multiclass label outside [0, K) (or NaN) is not a class: the softmax gradient treats the row
+// as belonging to no class and the loss skips the row, and both count it in `bad_label`, which the
+// host turns into an error (a label is never used as an index without this check).
 #include <math_constants.h>
 
 #include "bk_common.cuh"
@@ -36,8 +40,15 @@ __global__ void k_grad_binary(const double* __restrict__ score, const float* __r
   }
 }
 
+// The class of a multiclass label, or -1 (counted in *bad_label) when it is not in [0, K).
+__device__ __forceinline__ int class_of(float lf, int K, int32_t* bad_label) {
+  if (lf >= 0.0f && lf < (float)K) return (int)lf;
+  atomicAdd(bad_label, 1);
+  return -1;
+}
+
 __global__ void k_grad_softmax(const double* __restrict__ score, const float* __restrict__ label, int64_t n, int K,
-                               float* __restrict__ g, float* __restrict__ h) {
+                               float* __restrict__ g, float* __restrict__ h, int32_t* __restrict__ bad_label) {
   const double factor = (double)K / ((double)K - 1.0);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double rec[32];
@@ -48,7 +59,7 @@ __global__ void k_grad_softmax(const double* __restrict__ score, const float* __
       rec[k] = exp(score[(size_t)k * n + i] - wmax);
       wsum += rec[k];
     }
-    int lab = (int)label[i];
+    const int lab = class_of(label[i], K, bad_label);
     for (int k = 0; k < K; ++k) {
       double p = rec[k] / wsum;
       double gi = lab == k ? p - 1.0 : p;
@@ -62,7 +73,7 @@ __global__ void k_grad_softmax(const double* __restrict__ score, const float* __
 
 // Per-CTA partial losses (mean squared error / log loss / multiclass log loss).
 __global__ void k_loss(int kind, const double* __restrict__ score, const float* __restrict__ label, int64_t n, int K,
-                       double* __restrict__ partial) {
+                       double* __restrict__ partial, int32_t* __restrict__ bad_label) {
   double acc = 0.0;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     if (kind == 0) {
@@ -77,8 +88,8 @@ __global__ void k_loss(int kind, const double* __restrict__ score, const float* 
       for (int k = 1; k < K; ++k) wmax = fmax(score[(size_t)k * n + i], wmax);
       double wsum = 0.0;
       for (int k = 0; k < K; ++k) wsum += exp(score[(size_t)k * n + i] - wmax);
-      int lab = (int)label[i];
-      acc += -(score[(size_t)lab * n + i] - wmax - log(wsum));
+      const int lab = class_of(label[i], K, bad_label);
+      if (lab >= 0) acc += -(score[(size_t)lab * n + i] - wmax - log(wsum));
     }
   }
   for (int o = 16; o > 0; o >>= 1) acc += __shfl_xor_sync(0xffffffffu, acc, o);
@@ -95,17 +106,17 @@ __global__ void k_loss(int kind, const double* __restrict__ score, const float* 
 }  // namespace
 
 cudaError_t objective_gradients(int kind, const double* score, const float* label, int64_t n, int K, double sigmoid,
-                                float* g, float* h, cudaStream_t s) {
+                                float* g, float* h, int32_t* bad_label, cudaStream_t s) {
   const int grid = 1024, threads = 256;
   if (kind == 0) k_grad_l2<<<grid, threads, 0, s>>>(score, label, n, g, h);
   else if (kind == 1) k_grad_binary<<<grid, threads, 0, s>>>(score, label, n, sigmoid, g, h);
-  else k_grad_softmax<<<grid, threads, 0, s>>>(score, label, n, K, g, h);
+  else k_grad_softmax<<<grid, threads, 0, s>>>(score, label, n, K, g, h, bad_label);
   return cudaGetLastError();
 }
 
 cudaError_t objective_loss(int kind, const double* score, const float* label, int64_t n, int K, double* partial,
-                           int grid, cudaStream_t s) {
-  k_loss<<<grid, 256, 0, s>>>(kind, score, label, n, K, partial);
+                           int grid, int32_t* bad_label, cudaStream_t s) {
+  k_loss<<<grid, 256, 0, s>>>(kind, score, label, n, K, partial, bad_label);
   return cudaGetLastError();
 }
 

@@ -16,7 +16,8 @@ gradients / hessians from pinned host memory to the device inside the timed regi
 the training loss back.
 
 `--impl reference` times the CPU learner (the oracle port of the reference's tree learner, with
-all host threads) on a bounded row sample of the same workload and scales to the full workload.
+all host threads) on the same workload: all rows, the quantized config of `value`, every step a
+full boosting iteration; its rows are binned by the oracle's own restatement of the bin mappers.
 
 Multi-GPU (`--gpus N`, torchrun): independent replicas, one per GPU (the learner adds no
 cross-GPU exchange step); value = iterations of all ranks / max time over ranks.
@@ -278,6 +279,8 @@ def run_gpu(args, rank, world):
     # separate run so that they do not perturb the headline number
     roof = form(True, 1, args.steps, 1, timing=True)
     plain = form(False, 0, args.steps, args.warmup)
+    # the float learner in the same graph form as `value`: the quantization gain on its own
+    float_graph = form(False, 1, args.steps, args.warmup)
     e2e = form(True, 1, args.steps, 1, e2e=True)
     multiclass = _side(run_multiclass, args) if args.multiclass_rows > 0 else None
     batched_jobs = _side(run_batched_jobs, args) if args.batch_jobs > 0 else None
@@ -292,9 +295,7 @@ def run_gpu(args, rank, world):
         "metric": METRIC, "value": round(value, 4), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "int8 grad/hess, int64 histograms, f64 gains", "data": "synthetic (seeded)",
-        "config": {"workload": WORKLOAD, "rows": ds.num_data, "features": ds.num_features, "num_leaves": args.leaves,
-                   "parallelism": "replicas" if world > 1 else "single GPU",
-                   "l2_flush": "inputs larger than L2 (bins %.2f GB)" % (ds.num_data * ds.num_features / 1e9)},
+        "config": _config(ds, args, world),
         "forms": {"quantized_graph": {"iters_per_s": round(1000.0 / main["ms_per_step"], 4),
                                       "train_call_ms": round(main["train_ms_per_step"], 3),
                                       "hist_ms": round(roof["hist_ms_per_step"], 3),
@@ -307,6 +308,10 @@ def run_gpu(args, rank, world):
                                            "train_l2": plain["loss_final"], "heldout_l2": plain["heldout_l2"],
                                            "iterations": plain["iterations"],
                                            "launch_shape": _shape_dict(shapes.get((False, 0)), args.autotune)},
+                  "float_graph": {"iters_per_s": round(1000.0 / float_graph["ms_per_step"], 4),
+                                  "train_l2": float_graph["loss_final"], "heldout_l2": float_graph["heldout_l2"],
+                                  "iterations": float_graph["iterations"],
+                                  "launch_shape": _shape_dict(shapes.get((False, 1)), args.autotune)},
                   "heldout_l2_delta": main["heldout_l2"] - plain["heldout_l2"], "heldout_rows": m_ho,
                   "multiclass_k10": multiclass, "batched_jobs": batched_jobs, "binary_quantized_200": binary},
         "e2e": {"value": round(world * 1000.0 / e2e["ms_per_step"], 4), "unit": "iters/s",
@@ -325,8 +330,36 @@ def run_gpu(args, rank, world):
         "binning": binning,
     }
     if rank == 0:
-        line["cpu_baseline"] = cpu_baseline(ds, y, sample_rows=args.cpu_rows, leaves=args.leaves)
+        line["cpu_baseline"] = cpu_baseline(ds, y, leaves=args.leaves)
+    line["summary"] = _summary(line)
     return line
+
+
+def _summary(line):
+    """The line's key figures once more, compactly, at its end (a log that keeps only the tail of
+    the output still shows them)."""
+    f = line["forms"]
+
+    def get(d, *keys):
+        for k in keys:
+            if not isinstance(d, dict) or k not in d:
+                return None
+            d = d[k]
+        return d
+    return {"iters_per_s": {"quantized_graph": line["value"], "float_graph": get(f, "float_graph", "iters_per_s"),
+                            "plain_float_stepwise": get(f, "plain_float_stepwise", "iters_per_s"),
+                            "e2e": line["e2e"]["value"], "cpu_oracle": get(line, "cpu_baseline", "value")},
+            "heldout_l2": {"quantized": get(f, "quantized_graph", "heldout_l2"),
+                           "float_graph": get(f, "float_graph", "heldout_l2"),
+                           "delta_vs_float": f.get("heldout_l2_delta")},
+            "multiclass_k10_iters_per_s": [get(f, "multiclass_k10", "quantized_graph", "iters_per_s"),
+                                           get(f, "multiclass_k10", "plain_float_stepwise", "iters_per_s")],
+            "binary_200_iters_per_s": [get(f, "binary_quantized_200", "quantized_graph", "iters_per_s"),
+                                       get(f, "binary_quantized_200", "plain_float_stepwise", "iters_per_s")],
+            "binary_200_heldout_auc_delta": get(f, "binary_quantized_200", "heldout_auc_delta"),
+            "batched_job_iters_per_s": [get(f, "batched_jobs", "batched", "job_iters_per_s"),
+                                        get(f, "batched_jobs", "one_by_one", "job_iters_per_s")],
+            "hist_roofline_frac": line["roofline"]["frac"]}
 
 
 def run_multiclass(args):
@@ -663,50 +696,85 @@ def _device_view(ptr, count):
     return torch.as_tensor(_CAI(), device="cuda")
 
 
-def cpu_baseline(ds, y, sample_rows, threads=None, leaves=255):
-    """The oracle (the C++ port of the reference's tree learner) on the first `sample_rows` rows
-    of the same binned data: one float-path iteration (L2 gradients, one tree of `leaves`
-    leaves), scaled to the full row count (linear in rows)."""
+def _config(ds, args, world):
+    """The workload both arms time (the same dict for the GPU arm and the CPU reference arm)."""
+    return {"workload": WORKLOAD, "rows": ds.num_data, "features": ds.num_features, "num_leaves": args.leaves,
+            "quantized": {"num_grad_quant_bins": 4, "stochastic_rounding": True},
+            "parallelism": "replicas" if world > 1 else "one learner",
+            "l2_flush": "inputs larger than L2 (stored bins %.2f GB)" % (ds.num_data * ds.num_features / 1e9)}
+
+
+def _oracle_iterations(ds, y, quant, iters, warmup, threads, leaves=255, lr=0.1):
+    """Boosting iterations of the oracle (the C++ port of the reference's tree learner) on all rows
+    of a binned dataset, each timed whole: L2 gradients (objective/regression.rs:240-248), one
+    tree (serial.rs:569-628, quantized or float path), shrinkage and the score update
+    (serial.rs:1974-1990). `threads` host threads run the per-feature tasks and the block
+    partition; the config's num_threads stays 16, the value that seeds the stochastic-rounding
+    noise blocks of the GPU run (gradient_discretizer/mod.rs:87-106). Returns seconds per timed
+    iteration and the final training L2."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import harness
-    from lgbm_gb300 import BinnedDataset
-    threads = threads or 1
-    m = min(sample_rows, ds.num_data)
-    sub = BinnedDataset(np.ascontiguousarray(ds.bins[:, :m]), ds.features, ds.num_total_features)
-    cfg = make_cfg(False, leaves)
-    cfg.values["num_threads"] = threads
-    orc = harness.OracleLearner(sub, cfg)
-    score = np.full(m, float(np.mean(y[:m], dtype=np.float64)))
-    g = (score - y[:m].astype(np.float64)).astype(np.float32)
-    h = np.ones(m, np.float32)
-    t0 = time.time()
-    orc.train(g, h)
-    dt = time.time() - t0
-    return {"value": round((1.0 / dt) * (m / ds.num_data), 6), "unit": "iters/s", "cores": threads, "kind": "port",
-            "sample": "oracle float path, one 255-leaf tree on the first %d of %d rows (%.1f s), scaled by rows"
-                      % (m, ds.num_data, dt)}
+    cfg = make_cfg(quant, leaves)
+    orc = harness.OracleLearner(ds, cfg)
+    orc.set_threads(threads)
+    label = y.astype(np.float64)
+    score = np.full(ds.num_data, float(np.mean(label)))
+    h = np.ones(ds.num_data, np.float32)
+    times = []
+    for it in range(warmup + iters):
+        t0 = time.perf_counter()
+        g = (score - label).astype(np.float32)
+        _, lv, _ = orc.train(g, h)
+        if len(lv) > 1:
+            vals = lv * lr
+            vals[np.abs(vals) <= K_ZERO_THRESHOLD] = 0.0
+            orc.add_score(vals, score)
+        if it >= warmup:
+            times.append(time.perf_counter() - t0)
+    return times, float(np.mean((score - label) ** 2))
+
+
+def cpu_baseline(ds, y, leaves=255):
+    """The oracle on the GB300 machine's host cores: one quantized boosting iteration of the same
+    workload (all rows), with every host thread."""
+    threads = os.cpu_count() or 1
+    times, _ = _oracle_iterations(ds, y, True, 1, 0, threads, leaves)
+    return {"value": round(1.0 / times[0], 6), "unit": "iters/s", "cores": threads, "kind": "port",
+            "sample": "one boosting iteration (L2 gradients + one quantized %d-leaf tree + score update) on all %d "
+                      "rows of the workload, %.1f s" % (leaves, ds.num_data, times[0])}
 
 
 def run_reference(args):
-    """CPU arm: the oracle port with all host threads, same workload, bounded sample per step."""
+    """CPU arm: the oracle port of the reference's tree learner, with every host thread, on the
+    whole workload — the same rows (binned by the oracle's own restatement of the reference's bin
+    mappers, without the product library), the same quantized config as the GPU arm's `value`,
+    every step a full boosting iteration. The float path of the oracle is timed beside it."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import harness
+    from lgbm_gb300 import synthetic
     threads = os.cpu_count() or 1
-    ds, y, _ = build_dataset(args.rows)
-    steps = []
-    for _ in range(args.warmup):
-        cpu_baseline(ds, y, args.cpu_rows, threads, args.leaves)
-    for _ in range(args.steps):
-        steps.append(cpu_baseline(ds, y, args.cpu_rows, threads, args.leaves))
-    v = float(np.median([s["value"] for s in steps]))
-    return {"metric": METRIC, "impl": "reference", "value": v, "unit": "iters/s", "n_gpus": args.gpus,
-            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(1000.0 / v, 1) if v else None,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32 grad/hess, f64 histograms",
-            "data": "synthetic (seeded)",
-            "config": {"workload": WORKLOAD, "rows": ds.num_data, "features": ds.num_features,
-                       "num_leaves": args.leaves, "parallelism": "%d host threads" % threads,
-                       "l2_flush": "not applicable (CPU)"},
-            "cpu_baseline": {"value": v, "unit": "iters/s", "cores": threads, "kind": "port",
-                             "sample": steps[-1]["sample"]},
-            "e2e": {"value": v, "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    t0 = time.time()
+    X, y = synthetic.l2_steps(n=args.rows, seed=0)
+    ds = harness.bin_dense(X, max_bin=255, min_data_in_leaf=20, threads=threads)
+    del X
+    prep_s = time.time() - t0
+    times, loss = _oracle_iterations(ds, y, True, args.steps, args.warmup, threads, args.leaves)
+    ms = 1000.0 * float(np.mean(times))
+    v = 1000.0 / ms
+    ftimes, floss = _oracle_iterations(ds, y, False, min(args.steps, 2), 0, threads, args.leaves)
+    return {"metric": METRIC, "impl": "reference", "value": round(v, 6), "unit": "iters/s", "n_gpus": args.gpus,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": round(ms, 1),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "int8 grad/hess, int64 histograms, f64 gains", "data": "synthetic (seeded)",
+            "config": _config(ds, args, 1), "host_threads": threads,
+            "cpu_baseline": {"value": round(v, 6), "unit": "iters/s", "cores": threads, "kind": "port",
+                             "sample": "%d full boosting iterations (after %d untimed), all %d rows, quantized "
+                                       "(the reference's quantized CPU path)" % (args.steps, args.warmup, ds.num_data)},
+            "e2e": {"value": round(v, 6), "unit": "iters/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+            "forms": {"quantized": {"iters_per_s": round(v, 6), "train_l2": loss},
+                      "plain_float": {"iters_per_s": round(len(ftimes) / sum(ftimes), 6), "iterations": len(ftimes),
+                                      "train_l2": floss}},
+            "prep_s": round(prep_s, 1), "wall_s_timed": round(sum(times), 1)}
 
 
 def main():
@@ -720,7 +788,6 @@ def main():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--rows", type=int, default=10_000_000)
     ap.add_argument("--leaves", type=int, default=255)
-    ap.add_argument("--cpu-rows", type=int, default=1_000_000)
     ap.add_argument("--batch-jobs", type=int, default=32,
                     help="independent jobs of the batched-jobs form (256 for the full set; 0: skip it)")
     ap.add_argument("--batch-iters", type=int, default=10, help="iterations per job of the batched-jobs form")

@@ -3,7 +3,7 @@
  * The reference has no trait for its tree learner: `Trainer` calls the concrete method set of
  * `SerialTreeLearner` (crates/lgbm-core/src/treelearner/serial.rs:183-2044). Each entry point
  * below replaces one of those methods (cited per function) and takes plain pointers and sizes,
- * so a Rust `extern "C"` block can bind it directly (see INTEGRATION.md).
+ * so a Rust `extern "C"` block can bind it directly.
  *
  * Conventions (mirroring the reference's c_api, crates/lgbm-capi/src/lib.rs:1-8,78):
  *   - every function returns 0 on success and -1 on failure; bk_last_error() then holds a

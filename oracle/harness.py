@@ -68,6 +68,14 @@ def load():
         lib.orc_find_best_threshold.restype = i32
         lib.orc_find_best_threshold.argtypes = [P, P, P, ctypes.c_double, ctypes.c_double, i32, ctypes.c_double, P]
         lib.orc_sizeof_split.restype = i32
+        lib.orc_learner_set_threads.argtypes = [P, i32]
+        lib.orc_learner_add_score.argtypes = [P, P, P]
+        lib.orc_bin_dense_f32.restype = i32
+        lib.orc_bin_dense_f32.argtypes = [P, i64, i32, i32, i32, i32, i64, i32, i32, i32, P, P, P, P]
+        lib.orc_find_bin.restype = i32
+        lib.orc_find_bin.argtypes = [P, i64, i64, i32, i32, i32, i32, i32, i32, P, i32, P, P]
+        lib.orc_sample_rows.restype = i64
+        lib.orc_sample_rows.argtypes = [i64, i64, i32, P]
         assert lib.orc_sizeof_split() == SPLIT_DTYPE.itemsize
         _olib = lib
     return _olib
@@ -117,6 +125,18 @@ class OracleLearner:
         root = self.lib.orc_learner_root_output(self.h)
         return splits[:nl - 1].copy(), leaf_values[:nl].copy(), root
 
+    def set_threads(self, threads):
+        """Worker threads of the per-feature tasks and the block partition (the rayon pool); the
+        config's num_threads keeps seeding the stochastic-rounding noise blocks."""
+        self.lib.orc_learner_set_threads(self.h, int(threads))
+
+    def add_score(self, leaf_values, score):
+        """serial.rs:1974-1990 — score[row] += leaf_values[leaf of row] over the last tree's
+        partition; ``score`` (float64, C-contiguous) is updated in place."""
+        lv = np.ascontiguousarray(leaf_values, dtype=np.float64)
+        assert score.dtype == np.float64 and score.flags.c_contiguous and len(score) == self.ds.num_data
+        self.lib.orc_learner_add_score(self.h, lv.ctypes.data, score.ctypes.data)
+
     def set_feature_mask(self, mask=None):
         """By-tree column sample of the following trees (None = every feature)."""
         if mask is None:
@@ -158,6 +178,43 @@ class OracleLearner:
 # ------------------------------------------------------------------------------------------
 # objectives (host, f64 score -> f32 gradients), written in the reference's operation order
 # ------------------------------------------------------------------------------------------
+def bin_dense(X, max_bin=255, min_data_in_bin=3, min_data_in_leaf=20, bin_construct_sample_cnt=200000,
+              data_random_seed=1, threads=8):
+    """The oracle's own binned dataset of a dense float32 matrix (oracle/binning.cpp: the LCG row
+    sample of io/sample.rs, BinMapper::find_bin of io/bin.rs, the stored bins of
+    io/dataset.rs:633-685), numerical features, trivial columns dropped (io/dataset.rs:389-393).
+    Returns a ``BinnedDataset`` built without the product library."""
+    from lgbm_gb300.dataset import BinnedDataset, FeatureInfo
+    lib = load()
+    X = np.ascontiguousarray(X, dtype=np.float32)
+    n, ncol = X.shape
+    cap = 1024
+    meta = np.zeros((ncol, 4), np.int32)
+    nbin = np.zeros(ncol, np.int32)
+    bounds = np.zeros((ncol, cap), np.float64)
+    bins = np.zeros((ncol, n), np.uint8)
+    rc = lib.orc_bin_dense_f32(X.ctypes.data, n, ncol, int(max_bin), int(min_data_in_bin), int(min_data_in_leaf),
+                               int(bin_construct_sample_cnt), int(data_random_seed), int(threads), cap,
+                               meta.ctypes.data, nbin.ctypes.data, bounds.ctypes.data, bins.ctypes.data)
+    if rc != 0:
+        raise RuntimeError("orc_bin_dense_f32: bin mapper capacity exceeded")
+    feats, keep = [], []
+    for c in range(ncol):
+        if meta[c, 1]:
+            continue
+        fi = FeatureInfo()
+        fi.real = c
+        fi.num_bin = int(nbin[c])
+        fi.missing_type = int(meta[c, 0])
+        fi.default_bin = int(meta[c, 2])
+        fi.most_freq_bin = int(meta[c, 3])
+        fi.upper_bounds = bounds[c, :nbin[c]].copy()
+        fi.penalty = 1.0
+        feats.append(fi)
+        keep.append(c)
+    return BinnedDataset(bins[keep] if len(keep) < ncol else bins, feats, ncol)
+
+
 def _madd(a, b, c, fused):
     """utils/common.rs:207-216: a * b + c, rounded once when fused (exact rational arithmetic, one
     correctly rounded conversion), twice otherwise."""

@@ -1400,20 +1400,39 @@ struct Learner {
     if (cat_bits) route_table_cat(metas[f], cat_bits, gbins[f], lut);
     else route_table(metas[f], threshold, default_left, gbins[f], lut);
     int64_t b = leaf_begin[leaf], c = leaf_count[leaf];
-    std::vector<int32_t> L, R;
-    L.reserve(c);
-    R.reserve(c);
     const uint8_t* col = cols[f];
-    for (int64_t i = 0; i < c; ++i) {
-      int32_t r = indices[b + i];
-      if (lut[col[r]]) L.push_back(r);
-      else R.push_back(r);
+    // data_partition.rs:137-159 — a leaf of at least 2048 rows is routed in one contiguous block
+    // of rows per thread; each block keeps its rows' order and the blocks are concatenated in
+    // order, which is the sequential stable partition
+    const int64_t threads = workers ? (int64_t)workers->workers.size() + 1 : 1;
+    const int64_t block_len = (threads > 1 && c >= 2048) ? (c + threads - 1) / threads : std::max<int64_t>(c, 1);
+    const int64_t blocks = (c + block_len - 1) / block_len;
+    std::vector<std::vector<int32_t>> L((size_t)std::max<int64_t>(blocks, 1)), R(L.size());
+    auto route_block = [&](int k) {
+      const int64_t lo = (int64_t)k * block_len, hi = std::min(c, lo + block_len);
+      L[(size_t)k].reserve((size_t)(hi - lo));
+      R[(size_t)k].reserve((size_t)(hi - lo));
+      for (int64_t i = lo; i < hi; ++i) {
+        int32_t r = indices[b + i];
+        if (lut[col[r]]) L[(size_t)k].push_back(r);
+        else R[(size_t)k].push_back(r);
+      }
+    };
+    if (blocks > 1) workers->run((int)blocks, route_block);
+    else if (blocks == 1) route_block(0);
+    int64_t pos = b;
+    for (const auto& v : L) {
+      std::copy(v.begin(), v.end(), indices.begin() + pos);
+      pos += (int64_t)v.size();
     }
-    std::copy(L.begin(), L.end(), indices.begin() + b);
-    std::copy(R.begin(), R.end(), indices.begin() + b + (int64_t)L.size());
-    leaf_count[leaf] = (int64_t)L.size();
-    leaf_begin[right_leaf] = b + (int64_t)L.size();
-    leaf_count[right_leaf] = c - (int64_t)L.size();
+    const int64_t left = pos - b;
+    for (const auto& v : R) {
+      std::copy(v.begin(), v.end(), indices.begin() + pos);
+      pos += (int64_t)v.size();
+    }
+    leaf_count[leaf] = left;
+    leaf_begin[right_leaf] = b + left;
+    leaf_count[right_leaf] = c - left;
   }
 
   static double round_to_zero(double v) {  // tree.rs:66-68,299-301
@@ -1700,6 +1719,27 @@ void orc_learner_row_leaf(void* h, int32_t* out) {
   for (int32_t leaf = 0; leaf < L->tree_leaves; ++leaf) {
     const int32_t* ix = L->leaf_rows(leaf);
     for (int64_t k = 0; k < L->leaf_count[leaf]; ++k) out[ix[k]] = leaf;
+  }
+}
+
+// The worker threads of the per-feature tasks and the block partition (the reference's rayon
+// pool size). Independent of config num_threads, which also seeds the stochastic-rounding noise
+// blocks (gradient_discretizer/mod.rs:87-106) and so stays what the reference run used.
+void orc_learner_set_threads(void* h, int32_t threads) {
+  Learner* L = (Learner*)h;
+  delete L->workers;
+  L->workers = new Pool(threads > 0 ? threads : 1);
+}
+
+// serial.rs:1974-1990 — SerialTreeLearner::add_prediction_to_score: every row of leaf l of the
+// last tree gets score[row] += leaf_values[l] (leaf_values: the tree's values after shrinkage).
+void orc_learner_add_score(void* h, const double* leaf_values, double* score) {
+  Learner* L = (Learner*)h;
+  if (L->tree_leaves <= 1) return;
+  for (int32_t leaf = 0; leaf < L->tree_leaves; ++leaf) {
+    const int32_t* ix = L->leaf_rows(leaf);
+    const double out = leaf_values[leaf];
+    for (int64_t k = 0; k < L->leaf_count[leaf]; ++k) score[ix[k]] += out;
   }
 }
 
