@@ -1120,6 +1120,26 @@ int bk_learner_last_phase_timing(bk_learner* L, double* search_ms, double* parti
   return 0;
 }
 
+int bk_learner_last_step_timing(bk_learner* L, float* out) {
+  if (!L || !out) {
+    set_error("bk_learner_last_step_timing: invalid arguments");
+    return -1;
+  }
+  if (!L->timing || L->hist_events.size() != (size_t)(4 * (L->p.num_leaves - 1))) {
+    set_error("bk_learner_last_step_timing: timing is off (bk_learner_set_timing)");
+    return -1;
+  }
+  for (int it = 0; it < L->p.num_leaves - 1; ++it)
+    for (int k = 0; k < 3; ++k) {
+      float t = -1.f;
+      if (cudaEventElapsedTime(&t, L->hist_events[4 * it + k], L->hist_events[4 * it + k + 1]) != cudaSuccess)
+        t = -1.f;
+      out[3 * it + k] = t;
+    }
+  cudaGetLastError();  // an unrecorded event of a stepwise loop that stopped early is not an error
+  return 0;
+}
+
 int bk_learner_gradient_buffers(bk_learner* L, float** gradients, float** hessians) {
   if (!L) {
     set_error("bk_learner_gradient_buffers: null learner");
@@ -1220,6 +1240,54 @@ int bk_learner_predict_add(bk_learner* L, int32_t num_leaves, const int32_t* lef
     if (num_rows > 0)
       CK(predict_tree(L->d_feat, num_leaves, L->d_tree, L->d_tree_values, bins, num_rows, score, L->stream));
     CK(cudaStreamSynchronize(L->stream));
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
+  }
+  return 0;
+}
+
+int bk_learner_leaf_histogram(bk_learner* L, int32_t job, int32_t leaf, void* out, int32_t* slot_out) {
+  if (!L || !out || job < 0 || job >= L->K || leaf < 0 || leaf >= L->p.num_leaves) {
+    set_error("bk_learner_leaf_histogram: invalid arguments");
+    return -1;
+  }
+  const Params& p = L->p;
+  const Job& J = L->jobs[job];
+  try {
+    int32_t slot = -1;
+    CK(cudaMemcpyAsync(&slot, J.leaf_slot + leaf, sizeof(int32_t), cudaMemcpyDeviceToHost, L->stream));
+    CK(cudaStreamSynchronize(L->stream));
+    if (slot_out) *slot_out = slot;
+    if (slot < 0) {
+      set_error("bk_learner_leaf_histogram: leaf %d of the last tree has no histogram", leaf);
+      return -1;
+    }
+    // the slot [T][B][32]: tile f / 32, group bin b, lane f % 32
+    const size_t cells = (size_t)p.T * p.B * TILE;
+    const size_t elem = p.quant ? sizeof(int64_t) : sizeof(double2);
+    std::vector<unsigned char> raw(cells * elem);
+    CK(cudaMemcpyAsync(raw.data(), reinterpret_cast<const unsigned char*>(J.pool) + (size_t)slot * cells * elem,
+                       cells * elem, cudaMemcpyDeviceToHost, L->stream));
+    CK(cudaStreamSynchronize(L->stream));
+    size_t o = 0;
+    for (int f = 0; f < p.F; ++f) {
+      const DevFeature& d = L->h_feat[f];
+      for (int b = 0; b < d.gbins; ++b, ++o) {
+        const size_t c = ((size_t)(f / TILE) * p.B + b) * TILE + (f % TILE);
+        if (p.quant) {
+          int64_t pk;
+          std::memcpy(&pk, raw.data() + c * elem, sizeof(pk));
+          const int64_t h = pk & 0xffffffffLL;
+          reinterpret_cast<int64_t*>(out)[2 * o] = (pk - h) / 4294967296LL;
+          reinterpret_cast<int64_t*>(out)[2 * o + 1] = h;
+        } else {
+          double2 v;
+          std::memcpy(&v, raw.data() + c * elem, sizeof(v));
+          reinterpret_cast<double*>(out)[2 * o] = v.x;
+          reinterpret_cast<double*>(out)[2 * o + 1] = v.y;
+        }
+      }
+    }
   } catch (const CudaError& e) {
     return fail_cuda(e);
   }

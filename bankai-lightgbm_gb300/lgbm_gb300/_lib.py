@@ -77,10 +77,12 @@ _GPU_SIGNATURES = [
     ("bk_learner_last_timing", _i32, [_P, _P, _P, _P]),
     ("bk_learner_set_timing", _i32, [_P, _i32]),
     ("bk_learner_last_phase_timing", _i32, [_P, _P, _P]),
+    ("bk_learner_last_step_timing", _i32, [_P, _P]),
     ("bk_learner_gradient_buffers", _i32, [_P, _P, _P]),
     ("bk_learner_objective_gradients", _i32, [_P, _i32, _P, _P, _f64]),
     ("bk_learner_objective_loss", _i32, [_P, _i32, _P, _P, _P]),
     ("bk_learner_predict_add", _i32, [_P, _i32, _P, _P, _P, _P, _P, _P, _P, _i64, _P]),
+    ("bk_learner_leaf_histogram", _i32, [_P, _i32, _i32, _P, _P]),
     ("bk_learner_stream", _i32, [_P, _P]),
     ("bk_learner_destroy", _i32, [_P]),
     ("bk_partition_split_noalloc", _i32, [_P, _i64, _P, _i64, _P, _P, _P, _P]),

@@ -129,6 +129,13 @@ class GpuTreeLearner:
                    "bk_learner_last_phase_timing")
         return {"total_ms": t[0], "hist_ms": t[1], "hist_bytes": t[2], "search_ms": ph[0], "partition_ms": ph[1]}
 
+    def last_step_timing(self):
+        """With timing on: [num_leaves - 1, 3] ms of (histogram, search, partition) per grow-loop
+        step of the last train call (-1 where a step did not run)."""
+        out = np.zeros((self.num_leaves - 1, 3), dtype=np.float32)
+        _lib.check(self.lib.bk_learner_last_step_timing(self.h, out.ctypes.data), "bk_learner_last_step_timing")
+        return out
+
     def stream(self):
         s = ctypes.c_void_p()
         _lib.check(self.lib.bk_learner_stream(self.h, ctypes.byref(s)), "bk_learner_stream")
@@ -205,6 +212,20 @@ class GpuTreeLearner:
         out = np.zeros((self.num_jobs, self.ds.num_data), dtype=np.int32)
         _lib.check(self.lib.bk_learner_row_leaf(self.h, out.ctypes.data), "bk_learner_row_leaf")
         return out[0] if self.num_jobs == 1 else out
+
+    def leaf_histogram(self, leaf, job=0):
+        """The histogram pool slot of `leaf` after the last tree (bk_learner_leaf_histogram):
+        [total group bins, 2] (gradient, hessian) sums, float64 or (quantized) int64; None when
+        the leaf has no slot."""
+        total = sum(fi.group_bins for fi in self.ds.features)
+        out = np.zeros((total, 2), dtype=np.int64 if self.cfg.use_quantized_grad else np.float64)
+        slot = ctypes.c_int32(-1)
+        rc = self.lib.bk_learner_leaf_histogram(self.h, int(job), int(leaf), out.ctypes.data, ctypes.byref(slot))
+        if rc != 0:
+            if slot.value < 0:
+                return None
+            _lib.check(rc, "bk_learner_leaf_histogram")
+        return out
 
     def add_prediction_to_score(self, leaf_values, score, on_device=False):
         lv = np.ascontiguousarray(leaf_values, dtype=np.float64).reshape(self.num_jobs, self.num_leaves)

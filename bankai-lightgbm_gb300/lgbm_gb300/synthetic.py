@@ -77,3 +77,22 @@ def gaussian_mixture(n=2_000_000, F=64, K=10, spread=2.0, seed=0):
     y = rng.integers(0, K, size=n)
     X = rng.standard_normal((n, F), dtype=np.float32) + means[y]
     return X, y.astype(np.float32)
+
+
+def batched_jobs(count=256, seed=7):
+    """The independent binary jobs of the batched workload, one at a time: rows log-uniform in
+    [5,000, 500,000], features uniform in [20, 300] (N(0,1), 1% NaN), logistic labels from a per-job
+    random linear model (20% of the weights non-zero), max_bin drawn from {15, 63, 255}. Yields
+    (X float32 [rows, F], y float32 [rows], max_bin); one generator draws every job in order, so
+    job i is the same however many jobs are taken."""
+    rng = np.random.default_rng(seed)
+    for _ in range(count):
+        n = int(round(np.exp(rng.uniform(np.log(5_000), np.log(500_000)))))
+        F = int(rng.integers(20, 301))
+        mb = int(rng.choice([15, 63, 255]))
+        X = rng.standard_normal((n, F), dtype=np.float32)
+        w = (rng.standard_normal(F) * (rng.random(F) < 0.2)).astype(np.float32)
+        z = X @ w
+        X[rng.random((n, F), dtype=np.float32) < 0.01] = np.nan
+        y = (rng.random(n) < 1.0 / (1.0 + np.exp(-z))).astype(np.float32)
+        yield X, y, mb

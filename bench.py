@@ -442,20 +442,11 @@ def run_batched_jobs(args):
     all jobs in one bk_learners_train_batch call per iteration. Host wall clock around each
     iteration loop, bracketed by device synchronization (the work spans many streams)."""
     import torch
-    from lgbm_gb300 import BinnedDataset, GpuTreeLearner, LearnerConfig, train_batch
-    rng = np.random.default_rng(7)
+    from lgbm_gb300 import BinnedDataset, GpuTreeLearner, LearnerConfig, synthetic, train_batch
     threads = min(32, os.cpu_count() or 8)
     jobs = []
     t0 = time.time()
-    for i in range(args.batch_jobs):
-        n = int(round(np.exp(rng.uniform(np.log(5_000), np.log(500_000)))))
-        F = int(rng.integers(20, 301))
-        mb = int(rng.choice([15, 63, 255]))
-        X = rng.standard_normal((n, F), dtype=np.float32)
-        w = (rng.standard_normal(F) * (rng.random(F) < 0.2)).astype(np.float32)
-        z = X @ w
-        X[rng.random((n, F), dtype=np.float32) < 0.01] = np.nan
-        y = (rng.random(n) < 1.0 / (1.0 + np.exp(-z))).astype(np.float32)
+    for X, y, mb in synthetic.batched_jobs(args.batch_jobs, seed=7):
         ds = BinnedDataset.from_dense(X, max_bin=mb, min_data_in_leaf=20, threads=threads)
         jobs.append((ds, torch.from_numpy(y).cuda(), mb))
         del X

@@ -203,6 +203,12 @@ int bk_learner_last_timing(bk_learner* learner, double* total_ms, double* hist_m
 /* With timing on: the split-search and partition phases of the last train call (ms). */
 int bk_learner_last_phase_timing(bk_learner* learner, double* search_ms, double* partition_ms);
 
+/* With timing on: the phases of every grow-loop step of the last train call, out[3 * i + k] (ms)
+ * for step i = 0 .. num_leaves - 2 and k = histogram, split search, partition (-1 where a step
+ * did not run). Step i builds the histogram of the smaller child of split i - 1 (the root's at
+ * i = 0), searches both children and partitions split i. */
+int bk_learner_last_step_timing(bk_learner* learner, float* out);
+
 /* Enables (1) or disables (0) CUDA-event timing of every grow-loop phase of a train call
  * (histogram, split search, partition), reported by bk_learner_last_timing and
  * bk_learner_last_phase_timing. */
@@ -237,6 +243,17 @@ int bk_learner_predict_add(bk_learner* learner, int32_t num_leaves, const int32_
                            const int32_t* right_child, const int32_t* split_feature_inner,
                            const uint32_t* threshold_in_bin, const int8_t* decision_type, const double* leaf_value,
                            const uint8_t* bins, int64_t num_rows, double* score);
+
+/* The histogram of one leaf of the last tree, as the learner's histogram pool holds it after the
+ * tree (serial.rs:80-162 HistogramPool, with FixHistogram and the parent-minus-child subtraction of
+ * serial.rs:1407-1437 applied): the leaf's slot, group bins of every inner feature in feature
+ * order (io/dataset.rs:35-76, one dense group per feature: 1 + num_bin - (most_freq_bin == 0)
+ * bins each). out: host [total group bins][2] (gradient, hessian) sums — double on the float
+ * path, int64 on the quantized path (integer gradient / hessian units, unscaled). slot_out (may be
+ * NULL): the pool slot, -1 when the leaf has none (it was never searched: -1 is returned). The
+ * reference has no such call (its pool is private); it exists so a host can report the device
+ * histograms' error against an f64 CPU learner. */
+int bk_learner_leaf_histogram(bk_learner* learner, int32_t job, int32_t leaf, void* out, int32_t* slot_out);
 
 /* The CUDA stream (cudaStream_t) every call of this learner is ordered on, for callers that
  * time or order their own work against the learner's. */

@@ -69,6 +69,8 @@ def load():
         lib.orc_find_best_threshold.argtypes = [P, P, P, ctypes.c_double, ctypes.c_double, i32, ctypes.c_double, P]
         lib.orc_sizeof_split.restype = i32
         lib.orc_learner_set_threads.argtypes = [P, i32]
+        lib.orc_learner_leaf_histogram.restype = i32
+        lib.orc_learner_leaf_histogram.argtypes = [P, i32, P]
         lib.orc_learner_add_score.argtypes = [P, P, P]
         lib.orc_bin_dense_f32.restype = i32
         lib.orc_bin_dense_f32.argtypes = [P, i64, i32, i32, i32, i32, i64, i32, i32, i32, P, P, P, P]
@@ -136,6 +138,14 @@ class OracleLearner:
         lv = np.ascontiguousarray(leaf_values, dtype=np.float64)
         assert score.dtype == np.float64 and score.flags.c_contiguous and len(score) == self.ds.num_data
         self.lib.orc_learner_add_score(self.h, lv.ctypes.data, score.ctypes.data)
+
+    def leaf_histogram(self, leaf):
+        """The leaf's histogram pool slot after the last tree: [total group bins, 2] (gradient,
+        hessian), float64 or (quantized) int64; None when the leaf has no slot."""
+        total = sum(fi.group_bins for fi in self.ds.features)
+        out = np.zeros((total, 2), dtype=np.int64 if self.cfg.use_quantized_grad else np.float64)
+        slot = self.lib.orc_learner_leaf_histogram(self.h, int(leaf), out.ctypes.data)
+        return None if slot < 0 else out
 
     def set_feature_mask(self, mask=None):
         """By-tree column sample of the following trees (None = every feature)."""
@@ -973,3 +983,82 @@ def compare_tree(t: Tree, ref: dict, leaf_rtol=1e-12):
     if ni > 0 and not np.allclose(floats("leaf_weight"), t.leaf_weight[:nl], rtol=1e-12):
         bad.append("leaf_weight")
     return bad
+
+
+# ---------------------------------------------------------------------------------------------
+# Error report of a GPU tree against the oracle's f64 learner (the checker, not the thing timed).
+# ---------------------------------------------------------------------------------------------
+def current_leaves(records, min_data_in_leaf, max_depth=-1):
+    """Leaves whose histogram pool slot holds their own final histogram after the tree: every leaf
+    searched after the split that made it (serial.rs:779-825 BeforeFindBestSplit let it through),
+    except the last split's two children, which no search follows. records: the split records in
+    order (SPLIT_DTYPE)."""
+    n = len(records)
+    if n == 0:
+        return [0]
+    depth = {0: 0}
+    last = {}
+    for i, r in enumerate(records):
+        bl, nl = int(r["leaf"]), int(r["right_leaf"])
+        d = depth.get(bl, 0) + 1
+        depth[bl] = depth[nl] = d
+        lc, rc = int(r["left_count"]), int(r["right_count"])
+        go = not (max_depth > 0 and d >= max_depth) and not (lc < 2 * min_data_in_leaf and rc < 2 * min_data_in_leaf)
+        last[bl] = last[nl] = (i, go)
+    return sorted(leaf for leaf, (i, go) in last.items() if go and i < n - 1)
+
+
+def histogram_errors(ds, row_leaf, g, h, leaves, gpu_hist, orc_hist):
+    """Error of the device float histograms against the oracle's f64 sums over the searched slice
+    of every feature (group bins 1 .. num_bin - offset; group bin 0 is the elided most-frequent
+    bin, outside every search). gpu_hist / orc_hist: leaf -> [total group bins, 2]. Each entry's
+    error is |gpu - oracle| divided by the entry's absolute mass (the sum of |gradient| or of the
+    hessians of the rows behind it: serial.rs:1167-1207 FixHistogram gives the most frequent bin
+    the leaf total minus the other bins); entries whose mass is below 1e-9 of the feature's mass in
+    the leaf are reported only relative to that feature mass. Returns max / mean relative errors
+    and the count."""
+    gstart = np.cumsum([0] + [fi.group_bins for fi in ds.features])
+    rel, rel_leaf = [], []
+    ag, hh = np.abs(np.asarray(g, np.float64)), np.asarray(h, np.float64)
+    for leaf in leaves:
+        rows = np.flatnonzero(row_leaf == leaf)
+        a, b = gpu_hist[leaf], orc_hist[leaf]
+        for j, fi in enumerate(ds.features):
+            gb = fi.group_bins
+            col = np.asarray(ds.bins[j][rows], dtype=np.int64)
+            mass = np.stack([np.bincount(col, weights=ag[rows], minlength=gb),
+                             np.bincount(col, weights=hh[rows], minlength=gb)], axis=1)
+            if fi.most_freq_bin > 0:  # the fixed entry holds the stored-bin-0 rows
+                mass[fi.most_freq_bin + 1] = mass[0]
+            sl = slice(gstart[j] + 1, gstart[j] + gb)
+            d = np.abs(a[sl] - b[sl])
+            m = mass[1:]
+            fm = m.sum(axis=0, keepdims=True)
+            ok = m > 1e-9 * fm
+            rel.append(d[ok] / m[ok])
+            rel_leaf.append((d / np.maximum(fm, 1e-300)).ravel())
+    rel = np.concatenate(rel) if rel else np.zeros(0)
+    rel_leaf = np.concatenate(rel_leaf) if rel_leaf else np.zeros(0)
+    return {"leaves": len(leaves), "entries": int(rel_leaf.size),
+            "max_rel": float(rel.max()) if rel.size else 0.0, "mean_rel": float(rel.mean()) if rel.size else 0.0,
+            "max_rel_to_feature_mass": float(rel_leaf.max()) if rel_leaf.size else 0.0}
+
+
+def gain_errors(rec_gpu, rec_orc):
+    """Split-by-split comparison of two float trees grown from the same gradients: relative gain
+    error of every split while the two trees agree, and the near-tie divergences (the first split
+    whose leaf, feature or threshold differs, with both gains)."""
+    rel, near_ties = [], []
+    for i, (a, b) in enumerate(zip(rec_gpu, rec_orc)):
+        same = (int(a["leaf"]) == int(b["leaf"]) and int(a["real_feature"]) == int(b["real_feature"])
+                and int(a["threshold"]) == int(b["threshold"]) and int(a["default_left"]) == int(b["default_left"]))
+        ga, gb = float(a["gain"]), float(b["gain"])
+        if not same:
+            near_ties.append({"split": i, "gpu": [int(a["leaf"]), int(a["real_feature"]), int(a["threshold"]), ga],
+                              "oracle": [int(b["leaf"]), int(b["real_feature"]), int(b["threshold"]), gb],
+                              "gain_rel_diff": abs(ga - gb) / max(abs(gb), 1e-300)})
+            break
+        rel.append(abs(ga - gb) / max(abs(gb), 1e-300))
+    rel = np.asarray(rel)
+    return {"splits_compared": int(rel.size), "max_rel": float(rel.max()) if rel.size else 0.0,
+            "mean_rel": float(rel.mean()) if rel.size else 0.0, "near_ties": near_ties}

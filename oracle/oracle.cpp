@@ -1743,6 +1743,25 @@ void orc_learner_add_score(void* h, const double* leaf_values, double* score) {
   }
 }
 
+// The histogram pool slot of one leaf after the last tree ([total group bins][2] (gradient,
+// hessian): double on the float path, int64 on the quantized path), or -1 when the leaf has no slot.
+int32_t orc_learner_leaf_histogram(void* h, int32_t leaf, void* out) {
+  Learner* L = (Learner*)h;
+  if (leaf < 0 || leaf >= L->num_leaves) return -1;
+  const int32_t slot = L->leaf_slot[(size_t)leaf];
+  if (slot < 0) return -1;
+  for (int64_t b = 0; b < L->total_bins; ++b) {
+    if (L->quant) {
+      reinterpret_cast<int64_t*>(out)[2 * b] = L->islots_g[(size_t)slot][(size_t)b];
+      reinterpret_cast<int64_t*>(out)[2 * b + 1] = L->islots_h[(size_t)slot][(size_t)b];
+    } else {
+      reinterpret_cast<double*>(out)[2 * b] = L->slots[(size_t)slot][(size_t)(2 * b)];
+      reinterpret_cast<double*>(out)[2 * b + 1] = L->slots[(size_t)slot][(size_t)(2 * b + 1)];
+    }
+  }
+  return slot;
+}
+
 // Partition order (indices) and per-leaf ranges after the last tree.
 void orc_learner_partition(void* h, int32_t* indices, int64_t* begin, int64_t* count) {
   Learner* L = (Learner*)h;

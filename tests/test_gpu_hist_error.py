@@ -1,0 +1,89 @@
+"""Histogram and gain error of the GPU learner against the oracle's FP64 learner.
+
+The float path accumulates each bin as an fp32 (hi, lo) compensated pair per CTA and flushes
+(double)hi + (double)lo with f64 atomics; the reference sums f64 in leaf row order
+(treelearner/histogram.rs:117-245, serial.rs:891-1065). Both learners grow the same tree from the
+same gradients here; every searched leaf's histogram is read back from the device pool
+(bk_learner_leaf_histogram) and compared entry by entry with the oracle's pool, each entry's error
+relative to its absolute mass (sum of |g| or of h of its rows). Split gains are compared split by
+split (the 1e-6 relative bound of the float path), near-tie divergences listed. On the quantized
+path the integer histograms must be identical.
+"""
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+# fp32 compensated accumulation carries about 2^-48 of each bin's absolute mass, the f64 flush and
+# the oracle's sequential f64 sum about n * 2^-53: both far below this bound
+HIST_REL_BOUND = 1e-10
+GAIN_REL_BOUND = 1e-6
+
+
+def _data(n, F, seed):
+    rng = np.random.default_rng(seed)
+    X = rng.standard_normal((n, F)).astype(np.float32)
+    X[:, : F // 4] = rng.integers(0, 12, size=(n, F // 4))
+    X[rng.random((n, F)) < 0.05] = np.nan
+    z = np.nan_to_num(X[:, 1]) - 0.5 * np.nan_to_num(X[:, 3]) + 0.3 * np.nan_to_num(X[:, 0])
+    y = (rng.random(n) < 1.0 / (1.0 + np.exp(-z))).astype(np.float64)
+    p = np.full(n, y.mean())
+    g = (p - y).astype(np.float32)
+    h = (p * (1.0 - p) * (1.0 + 0.5 * rng.random(n))).astype(np.float32)  # a varying hessian
+    return X, g, h
+
+
+@pytest.mark.parametrize("quant", [0, 1])
+def test_leaf_histograms_and_gains_against_the_fp64_oracle(oracle, quant):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from lgbm_gb300 import BinnedDataset, GpuTreeLearner, LearnerConfig
+    X, g, h = _data(200_000, 24, 5)
+    ds = BinnedDataset.from_dense(X)
+    cfg = LearnerConfig(num_leaves=31, min_data_in_leaf=20, use_quantized_grad=quant, stochastic_rounding=1,
+                        seed=2, num_threads=4, fused_madd=1)
+    gpu = GpuTreeLearner(ds, cfg)
+    orc = oracle.OracleLearner(ds, cfg)
+    rg, ro = gpu.train(g, h), orc.train(g, h)
+    rec_g, rec_o = rg[0], ro[0]
+    gains = oracle.gain_errors(rec_g, rec_o)
+    print("gain error vs FP64 oracle:", gains)
+    assert gains["max_rel"] <= GAIN_REL_BOUND
+    agree = gains["splits_compared"]
+    assert agree >= 1
+    # histograms of the leaves both learners searched; when the trees diverge at a near tie, the
+    # leaves of the splits before it
+    recs = rec_o[:agree] if agree < len(rec_o) else rec_o
+    leaves = oracle.current_leaves(recs, 20) if agree == len(rec_o) else []
+    if agree < len(rec_o):
+        pytest.skip("float trees diverge at a near tie: %s" % gains["near_ties"])
+    row_leaf = orc.row_leaf()
+    assert np.array_equal(gpu.row_leaf(), row_leaf)
+    hg = {leaf: gpu.leaf_histogram(leaf) for leaf in leaves}
+    ho = {leaf: orc.leaf_histogram(leaf) for leaf in leaves}
+    assert leaves and all(hg[l] is not None and ho[l] is not None for l in leaves)
+    if quant:
+        for leaf in leaves:
+            assert np.array_equal(hg[leaf], ho[leaf]), "leaf %d" % leaf
+        return
+    err = oracle.histogram_errors(ds, row_leaf, g, h, leaves, hg, ho)
+    print("histogram error vs FP64 oracle:", err)
+    assert err["entries"] > 1000
+    assert err["max_rel"] <= HIST_REL_BOUND
+    gpu.close()
+
+
+def test_leaf_histogram_argument_checks(bklib):
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from lgbm_gb300 import BinnedDataset, GpuTreeLearner, LearnerConfig
+    X, g, h = _data(5000, 6, 1)
+    ds = BinnedDataset.from_dense(X)
+    gpu = GpuTreeLearner(ds, LearnerConfig(num_leaves=7))
+    gpu.train(g, h)
+    assert gpu.leaf_histogram(0) is not None
+    with pytest.raises(RuntimeError):
+        gpu.leaf_histogram(99)
+    gpu.close()
