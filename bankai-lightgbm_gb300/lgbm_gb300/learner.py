@@ -219,10 +219,10 @@ class GpuTreeLearner:
         the leaf has no slot."""
         total = sum(fi.group_bins for fi in self.ds.features)
         out = np.zeros((total, 2), dtype=np.int64 if self.cfg.use_quantized_grad else np.float64)
-        slot = ctypes.c_int32(-1)
+        slot = ctypes.c_int32(-2)  # the library writes -1 only for a leaf without a slot
         rc = self.lib.bk_learner_leaf_histogram(self.h, int(job), int(leaf), out.ctypes.data, ctypes.byref(slot))
         if rc != 0:
-            if slot.value < 0:
+            if slot.value == -1:
                 return None
             _lib.check(rc, "bk_learner_leaf_histogram")
         return out

@@ -70,7 +70,7 @@ def load():
         lib.orc_sizeof_split.restype = i32
         lib.orc_learner_set_threads.argtypes = [P, i32]
         lib.orc_learner_leaf_histogram.restype = i32
-        lib.orc_learner_leaf_histogram.argtypes = [P, i32, P]
+        lib.orc_learner_leaf_histogram.argtypes = [P, i32, P, P]
         lib.orc_learner_add_score.argtypes = [P, P, P]
         lib.orc_bin_dense_f32.restype = i32
         lib.orc_bin_dense_f32.argtypes = [P, i64, i32, i32, i32, i32, i64, i32, i32, i32, P, P, P, P]
@@ -140,12 +140,15 @@ class OracleLearner:
         self.lib.orc_learner_add_score(self.h, lv.ctypes.data, score.ctypes.data)
 
     def leaf_histogram(self, leaf):
-        """The leaf's histogram pool slot after the last tree: [total group bins, 2] (gradient,
-        hessian), float64 or (quantized) int64; None when the leaf has no slot."""
+        """The leaf's histogram pool slot after the last tree: ([total group bins, 2] (gradient,
+        hessian) float64 or (quantized) int64, the [num_features] mask of the features its last
+        search covered — the slot's other entries are left from earlier use); None when the leaf
+        has no slot."""
         total = sum(fi.group_bins for fi in self.ds.features)
         out = np.zeros((total, 2), dtype=np.int64 if self.cfg.use_quantized_grad else np.float64)
-        slot = self.lib.orc_learner_leaf_histogram(self.h, int(leaf), out.ctypes.data)
-        return None if slot < 0 else out
+        used = np.zeros(self.ds.num_features, np.uint8)
+        slot = self.lib.orc_learner_leaf_histogram(self.h, int(leaf), out.ctypes.data, used.ctypes.data)
+        return None if slot < 0 else (out, used.astype(bool))
 
     def set_feature_mask(self, mask=None):
         """By-tree column sample of the following trees (None = every feature)."""
@@ -1008,10 +1011,22 @@ def current_leaves(records, min_data_in_leaf, max_depth=-1):
     return sorted(leaf for leaf, (i, go) in last.items() if go and i < n - 1)
 
 
+def searched_entries(ds, used):
+    """Mask over the group bins of a slot: the searched slice (group bins 1 .. num_bin - offset;
+    group bin 0 is the elided most-frequent bin, outside every search) of the features in `used`."""
+    mask = []
+    for fi, u in zip(ds.features, used):
+        m = np.zeros(fi.group_bins, bool)
+        m[1:] = bool(u)
+        mask.append(m)
+    return np.concatenate(mask)
+
+
 def histogram_errors(ds, row_leaf, g, h, leaves, gpu_hist, orc_hist):
     """Error of the device float histograms against the oracle's f64 sums over the searched slice
-    of every feature (group bins 1 .. num_bin - offset; group bin 0 is the elided most-frequent
-    bin, outside every search). gpu_hist / orc_hist: leaf -> [total group bins, 2]. Each entry's
+    of every feature the leaf's last search covered (group bins 1 .. num_bin - offset; group bin 0
+    is the elided most-frequent bin, outside every search). gpu_hist: leaf -> [total group bins,
+    2]; orc_hist: leaf -> (that, the searched-feature mask). Each entry's
     error is |gpu - oracle| divided by the entry's absolute mass (the sum of |gradient| or of the
     hessians of the rows behind it: serial.rs:1167-1207 FixHistogram gives the most frequent bin
     the leaf total minus the other bins); entries whose mass is below 1e-9 of the feature's mass in
@@ -1022,8 +1037,10 @@ def histogram_errors(ds, row_leaf, g, h, leaves, gpu_hist, orc_hist):
     ag, hh = np.abs(np.asarray(g, np.float64)), np.asarray(h, np.float64)
     for leaf in leaves:
         rows = np.flatnonzero(row_leaf == leaf)
-        a, b = gpu_hist[leaf], orc_hist[leaf]
+        a, (b, used) = gpu_hist[leaf], orc_hist[leaf]
         for j, fi in enumerate(ds.features):
+            if not used[j]:
+                continue
             gb = fi.group_bins
             col = np.asarray(ds.bins[j][rows], dtype=np.int64)
             mass = np.stack([np.bincount(col, weights=ag[rows], minlength=gb),

@@ -1060,6 +1060,9 @@ struct Learner {
   int32_t smaller_slot = 0, larger_slot = -1, parent_slot = -1;
   std::vector<SplitRecord> records;
   std::vector<double> leaf_value;
+  // the features of each leaf's last search (its histogram slot holds their histograms; the
+  // slot's other features are left from earlier use)
+  std::vector<std::vector<uint8_t>> leaf_used;
   int32_t tree_leaves = 1;
   double root_output = 0.0;
   std::vector<float> og, oh;
@@ -1160,6 +1163,7 @@ struct Learner {
     best.assign(num_leaves, SplitInfo());
     leaf_depth.assign(num_leaves, 0);
     leaf_value.assign(num_leaves, 0.0);
+    leaf_used.assign(num_leaves, std::vector<uint8_t>(nf, 0));
   }
 
   const int32_t* leaf_rows(int32_t leaf) const { return indices.data() + leaf_begin[leaf]; }
@@ -1330,6 +1334,8 @@ struct Learner {
     }
     best[smaller.leaf] = sbest;
     if (larger.leaf >= 0) best[larger.leaf] = lbest;
+    leaf_used[(size_t)smaller.leaf] = used;
+    if (larger.leaf >= 0) leaf_used[(size_t)larger.leaf] = used;
   }
 
   // serial.rs:779-825
@@ -1502,6 +1508,7 @@ struct Learner {
 
   // serial.rs:658-776 (no bagging / column sampling / constraints)
   void before_train(const float* g, const float* h, const int32_t* rows, int64_t nrows) {
+    for (auto& u : leaf_used) std::fill(u.begin(), u.end(), 0);
     std::fill(leaf_slot.begin(), leaf_slot.end(), -1);
     next_free = 0;
     std::fill(leaf_depth.begin(), leaf_depth.end(), 0);
@@ -1745,11 +1752,13 @@ void orc_learner_add_score(void* h, const double* leaf_values, double* score) {
 
 // The histogram pool slot of one leaf after the last tree ([total group bins][2] (gradient,
 // hessian): double on the float path, int64 on the quantized path), or -1 when the leaf has no slot.
-int32_t orc_learner_leaf_histogram(void* h, int32_t leaf, void* out) {
+// used_out [nf]: 1 for the features of the leaf's last search, whose entries the slot holds.
+int32_t orc_learner_leaf_histogram(void* h, int32_t leaf, void* out, uint8_t* used_out) {
   Learner* L = (Learner*)h;
   if (leaf < 0 || leaf >= L->num_leaves) return -1;
   const int32_t slot = L->leaf_slot[(size_t)leaf];
   if (slot < 0) return -1;
+  std::copy(L->leaf_used[(size_t)leaf].begin(), L->leaf_used[(size_t)leaf].end(), used_out);
   for (int64_t b = 0; b < L->total_bins; ++b) {
     if (L->quant) {
       reinterpret_cast<int64_t*>(out)[2 * b] = L->islots_g[(size_t)slot][(size_t)b];
