@@ -2,11 +2,13 @@
 //
 // Layout in HBM (one learner, `n` rows, `F` inner features, `T = ceil(F / 32)` feature tiles,
 // `B` = the largest stored-bin count of any feature, rounded up to a multiple of 8):
-//   bins_rt   uint8 [n][T][32]   row-tiled stored bins: one 32-byte sector per (row, tile), so a
-//                                gathered row of a sparse leaf is one sector read per tile, and
-//                                the T histogram CTAs of a row chunk, which run side by side,
-//                                read neighbouring sectors of the same lines;
-//   bins_tm   uint8 [T][n][32]   the same sectors tile-major: the root and dense leaves (a
+//   bins_rt   uint8 [n][Σ w_t]   row-tiled stored bins: one w_t-byte run per (row, tile) — 32 bytes
+//                                for a tile of 8-bit bins, 16 for a tile of 4-bit bins (every
+//                                feature of the tile has at most 16 group bins) — so a gathered
+//                                row of a sparse leaf is one sector read per tile, and the T
+//                                histogram CTAs of a row chunk, which run side by side, read
+//                                neighbouring sectors of the same lines;
+//   bins_tm   [T] x uint8 [n][w_t]   the same runs tile-major: the root and dense leaves (a
 //                                quarter of the rows or more) stream each tile contiguously;
 //   bins_cm   uint8 [F][n]       column-major stored bins, read by the partition (one byte/row);
 //   pool      [L][T][B][32]      histogram pool, one slot per leaf (serial.rs:80-162 with a full
@@ -55,6 +57,22 @@ struct Cand {
   int32_t categorical;  // 1: a categorical split, its left bins in cand_cat_bits()
 };
 
+// The stored-bin layout of one 32-feature tile in the two row-tiled copies (static per learner):
+// a tile whose features all have at most 16 group bins holds 4-bit bins (16 bytes per row: byte k
+// = feature 2k in the low nibble, feature 2k + 1 in the high one, as io/bin_data.rs:20-30 stores
+// groups of <= 16 bins two to a byte); any other tile one byte per bin, 32 bytes per row, or 16
+// when it holds at most 16 features (the last tile of a feature count that is not a multiple of 32).
+struct TileGeom {
+  int32_t bins;    // group bins the tile's shared histogram holds: its largest feature's, rounded up to 8
+  int32_t nibble;  // 1: 4-bit stored bins
+  int32_t width;   // bytes per row: 16 or 32
+  int32_t _pad;
+  int64_t rt_off;  // byte offset of the tile in a row of bins_rt
+  int64_t tm_off;  // byte offset of the tile's [n][width] block in bins_tm
+};
+
+__host__ __device__ __forceinline__ int tile_width(const TileGeom& g) { return g.width; }
+
 // LeafSplits (serial.rs:53-76).
 struct LeafSum {
   double sg, sh, weight;
@@ -69,6 +87,8 @@ struct Params {
   int32_t T, B, quant_bins, stochastic;
   int32_t renew, part_grid, pdl;  // pdl: launch the grow-loop kernels with programmatic dependence
   int32_t hist_min_rows;          // fewest rows a histogram CTA takes (launch shape, autotuned)
+  int32_t rt_stride;              // bytes per row of bins_rt: the widths of all tiles
+  const TileGeom* tiles;          // [T] the tiles' layouts
   int64_t n;
   // CatParams of the categorical search (feature_histogram.rs:1146-1163)
   double cat_smooth, cat_l2;
@@ -207,6 +227,8 @@ struct HistLaunch {
   int threads;
   size_t smem;
   int flush_rounds;  // quantized: rounds of 32*warps rows between 16-bit -> 32-bit flushes (0: wide)
+  int direct_rows;   // quantized: a CTA with at most this many rows adds each (row, feature) to the
+                     // pool slot with a global atomic instead of through a shared histogram
 };
 // BinsCheck over device columns: the smallest flat index (feature * n + row) of a stored bin
 // outside its feature's range, or INT64_MAX (bk_binning.cu). Synchronizes `s`.

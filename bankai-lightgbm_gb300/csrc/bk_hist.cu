@@ -1,12 +1,19 @@
 // ConstructHistograms for the smaller leaf (serial.rs:891-1164), GB300 form.
 //
 // Grid: (blocks_per_tile, T, jobs). Each CTA owns one 32-feature tile and one contiguous chunk
-// of the leaf's rows. A warp takes 32 rows at a time: every lane fetches its row's 32-byte
-// tile sector with two 128-bit loads and stages it in shared memory; then, row by row, lane f
-// adds that row's statistics to bin[row][f] of a CTA-private shared histogram laid out
-// [bin][feature] — lane f always hits bank f, so the shared-memory atomics of a warp never
-// conflict and never collide. At the end the CTA adds its non-zero bins to the leaf's slot in
-// the histogram pool with global atomics (the pool slot is zeroed when the tree starts).
+// of the leaf's rows. A warp takes 32 rows at a time: every lane fetches its row's run of the
+// tile (32 bytes of 8-bit bins, or 16 bytes of 4-bit bins) with 128-bit loads and stages it in
+// shared memory; then, row by row, lane f adds that row's statistics to bin[row][f] of a
+// CTA-private shared histogram laid out [bin][feature] — lane f always hits bank f, so the
+// shared-memory atomics of a warp never conflict and never collide. At the end the CTA adds its
+// non-zero bins to the leaf's slot in the histogram pool with global atomics (the pool slot is
+// zeroed when the tree starts). Only the tile's own bins (its largest feature's group bins) are
+// zeroed and flushed.
+//
+// A quantized CTA with few rows (at most `direct_rows`) skips the shared histogram: each
+// (row, feature) is added to the pool slot with one global 64-bit atomic as it is read, which
+// saves the CTA's zeroing, barrier and flush pass (with so few rows nearly every bin would be
+// flushed anyway). Integer sums do not depend on the order, so both forms give the same slot.
 //
 // Quantized path: the packed int8 gradient / uint8 hessian of a row is added as one 32-bit
 // value (grad << 16) + hess into a 16:16 "hot" histogram, which is folded into 32-bit
@@ -105,7 +112,7 @@ struct RoundLoad {
 };
 
 __device__ __forceinline__ RoundLoad load_round_int(const uint8_t* tb, size_t rs, const Range& R, int64_t i, int32_t row,
-                                                    bool wide) {
+                                                    bool wide, bool half) {
   RoundLoad L;
   L.a = make_uint4(0, 0, 0, 0);
   L.b = make_uint4(0, 0, 0, 0);
@@ -113,7 +120,7 @@ __device__ __forceinline__ RoundLoad load_round_int(const uint8_t* tb, size_t rs
   if (row >= 0) {
     const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * rs);
     L.a = __ldg(src);
-    L.b = __ldg(src + 1);
+    if (!half) L.b = __ldg(src + 1);
     int32_t pk = R.pk_row ? R.pk[row] : R.pk[i];
     int32_t gi = (int32_t)(int8_t)(pk >> 8);
     int32_t hi = pk & 0xff;
@@ -124,6 +131,22 @@ __device__ __forceinline__ RoundLoad load_round_int(const uint8_t* tb, size_t rs
 
 // The gradient half of a 16:16 hot counter (grad * 65536 + hess, hess in [0, 65536)).
 __device__ __forceinline__ int32_t hot_g(uint32_t s) { return ((int32_t)s - (int32_t)(s & 0xffffu)) >> 16; }
+
+// Lane f's stored bin of staged row j: byte f of the row's 32-byte run, or the nibble f of its
+// 16-byte run (low nibble for even f).
+template <bool NIBBLE>
+__device__ __forceinline__ uint32_t staged_bin(const uint8_t* sb, int j, int lane) {
+  if (!NIBBLE) return sb[j * 32 + lane];
+  return (sb[j * 32 + (lane >> 1)] >> ((lane & 1) << 2)) & 15u;
+}
+
+// The (grad << 32) + hess pool value of a row's packed statistics as the kernel carries them.
+template <bool WIDE>
+__device__ __forceinline__ unsigned long long pool_value(int32_t v) {
+  const int32_t g = WIDE ? (int32_t)(int16_t)(v & 0xffff) : hot_g((uint32_t)v);
+  const int32_t h = WIDE ? (v >> 16) : (v & 0xffff);
+  return (unsigned long long)((int64_t)g * 4294967296LL + (int64_t)h);
+}
 
 template <bool WIDE>
 __device__ __forceinline__ void add_row(uint32_t* hot, int32_t* cold_g, int32_t* cold_h, uint32_t bin, int32_t v,
@@ -136,64 +159,65 @@ __device__ __forceinline__ void add_row(uint32_t* hot, int32_t* cold_g, int32_t*
   }
 }
 
-template <bool WIDE>
-__global__ void __launch_bounds__(1024, 1)
-    k_hist_int(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
-               int blocks_per_tile, int flush_rounds, int post, int par) {
-  extern __shared__ __align__(16) unsigned char smem[];
-  const int B = p.B;
-  // the shared histogram is zeroed while the previous kernel of the grow loop finishes
-  {
-    uint4* z = reinterpret_cast<uint4*>(smem);
-    const int n16 = (WIDE ? 2 : 3) * B * TILE / 4;
-    for (int e = threadIdx.x; e < n16; e += blockDim.x) z[e] = make_uint4(0, 0, 0, 0);
-  }
-  griddep_wait();
-  const Job& J = jobs.job[blockIdx.z];
-  Range R;
-  if (!cta_range(J, p, blocks_per_tile, post, par, &R)) return;
+// The rows and flush of one integer-histogram CTA, its range known (NIBBLE: the tile holds
+// 4-bit bins).
+template <bool WIDE, bool NIBBLE>
+__device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, const Range& R, const TileGeom& geo,
+                                              const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
+                                              int flush_rounds, int direct_rows, unsigned char* smem) {
   const int tile = blockIdx.y;
+  const int Bt = geo.bins;
+  const bool half = geo.width == 16;  // one 16-byte run per row
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
-  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + (WIDE ? 0 : B * TILE));
-  int32_t* cold_h = cold_g + B * TILE;
-  uint4* stage = reinterpret_cast<uint4*>(cold_h + B * TILE);
+  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + (WIDE ? 0 : Bt * TILE));
+  int32_t* cold_h = cold_g + Bt * TILE;
+  uint4* stage = reinterpret_cast<uint4*>(cold_h + Bt * TILE);
   int32_t* stage_v = reinterpret_cast<int32_t*>(stage + nwarps * 64);
+  unsigned long long* slot = reinterpret_cast<unsigned long long*>(J.pool) +
+                             ((size_t)R.slot * p.T + tile) * (size_t)p.B * TILE;
+  const bool direct = R.r1 - R.r0 <= (int64_t)direct_rows;  // uniform over the CTA
   __syncthreads();
-  // the tile's sector of row 0 and the row stride, in the copy that suits the leaf's density
+  // the tile's run of row 0 and the row stride, in the copy that suits the leaf's density
   const bool dense = R.count * 4 >= p.n;
-  const uint8_t* tb = dense ? bins_tm + (size_t)tile * (size_t)p.n * TILE : bins_rt + (size_t)tile * TILE;
-  const size_t rs = dense ? (size_t)TILE : (size_t)p.T * TILE;
-  // lanes past the last feature of the last tile (padding bytes) add nothing
+  const uint8_t* tb = dense ? bins_tm + geo.tm_off : bins_rt + geo.rt_off;
+  const size_t rs = dense ? (size_t)tile_width(geo) : (size_t)p.rt_stride;
+  // lanes past the last feature of the last tile (padding) add nothing
   const bool feat_lane = tile * TILE + lane < p.F;
   const int64_t per_round = (int64_t)TILE * nwarps;
   const int64_t rounds = ceil_div64(R.r1 - R.r0, per_round);
   uint4* my_stage = stage + warp * 64;
   const uint8_t* sb = reinterpret_cast<const uint8_t*>(my_stage);
   int32_t* my_v = stage_v + warp * 32;
-  // software pipeline: the next round's sectors and the round after's row indices are in flight
+  // software pipeline: the next round's runs and the round after's row indices are in flight
   // while this round is added up
   const int64_t first = R.r0 + (int64_t)warp * TILE + lane;
-  RoundLoad cur = load_round_int(tb, rs, R, first, round_row(R, first), WIDE);
+  RoundLoad cur = load_round_int(tb, rs, R, first, round_row(R, first), WIDE, half);
   int32_t row_nxt = round_row(R, first + per_round);
   int until_flush = flush_rounds;
   for (int64_t rd = 0; rd < rounds; ++rd) {
     const int64_t base = R.r0 + rd * per_round + (int64_t)warp * TILE;
     const int32_t row_nn = round_row(R, base + 2 * per_round + lane);
-    RoundLoad nxt = load_round_int(tb, rs, R, base + per_round + lane, row_nxt, WIDE);
+    RoundLoad nxt = load_round_int(tb, rs, R, base + per_round + lane, row_nxt, WIDE, half);
     row_nxt = row_nn;
     if (base < R.r1) {
       my_stage[lane * 2] = cur.a;
-      my_stage[lane * 2 + 1] = cur.b;
+      if (!half) my_stage[lane * 2 + 1] = cur.b;
       my_v[lane] = cur.v;
       __syncwarp();
       const int jn = (int)min((int64_t)32, R.r1 - base);  // warp-uniform
-      if (jn == 32) {
+      if (direct) {
+        for (int j = 0; j < jn; ++j) {
+          const uint32_t b0 = staged_bin<NIBBLE>(sb, j, lane);
+          const int32_t v0 = my_v[j];
+          if (feat_lane) atomicAdd(slot + b0 * TILE + lane, pool_value<WIDE>(v0));
+        }
+      } else if (jn == 32) {
 #pragma unroll 2
         for (int j = 0; j < 32; j += 4) {
           const int4 v4 = *reinterpret_cast<const int4*>(my_v + j);
-          const uint32_t b0 = sb[(j + 0) * 32 + lane], b1 = sb[(j + 1) * 32 + lane];
-          const uint32_t b2 = sb[(j + 2) * 32 + lane], b3 = sb[(j + 3) * 32 + lane];
+          const uint32_t b0 = staged_bin<NIBBLE>(sb, j + 0, lane), b1 = staged_bin<NIBBLE>(sb, j + 1, lane);
+          const uint32_t b2 = staged_bin<NIBBLE>(sb, j + 2, lane), b3 = staged_bin<NIBBLE>(sb, j + 3, lane);
           if (feat_lane) {
             add_row<WIDE>(hot, cold_g, cold_h, b0, v4.x, lane);
             add_row<WIDE>(hot, cold_g, cold_h, b1, v4.y, lane);
@@ -203,7 +227,7 @@ __global__ void __launch_bounds__(1024, 1)
         }
       } else {
         for (int j = 0; j < jn; ++j) {
-          const uint32_t b0 = sb[j * 32 + lane];
+          const uint32_t b0 = staged_bin<NIBBLE>(sb, j, lane);
           const int32_t v0 = my_v[j];
           if (feat_lane) add_row<WIDE>(hot, cold_g, cold_h, b0, v0, lane);
         }
@@ -213,13 +237,13 @@ __global__ void __launch_bounds__(1024, 1)
     cur = nxt;
     // fold the 16:16 counters into the 32-bit ones before either half can overflow (the last
     // round's counters are folded by the final flush below)
-    if (!WIDE && --until_flush == 0 && rd + 1 < rounds) {
+    if (!WIDE && !direct && --until_flush == 0 && rd + 1 < rounds) {
       until_flush = flush_rounds;
       __syncthreads();
       uint4* hot4 = reinterpret_cast<uint4*>(hot);
       int4* g4 = reinterpret_cast<int4*>(cold_g);
       int4* h4 = reinterpret_cast<int4*>(cold_h);
-      for (int e = threadIdx.x; e < B * TILE / 4; e += blockDim.x) {
+      for (int e = threadIdx.x; e < Bt * TILE / 4; e += blockDim.x) {
         const uint4 s = hot4[e];
         if (s.x | s.y | s.z | s.w) {
           int4 g = g4[e], h = h4[e];
@@ -240,10 +264,9 @@ __global__ void __launch_bounds__(1024, 1)
     }
   }
   griddep_launch();  // only the flush is left: the next kernel may be scheduled
+  if (direct) return;
   __syncthreads();
-  unsigned long long* slot = reinterpret_cast<unsigned long long*>(J.pool) +
-                             ((size_t)R.slot * p.T + tile) * (size_t)B * TILE;
-  for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
+  for (int e = threadIdx.x; e < Bt * TILE; e += blockDim.x) {
     int32_t gg = cold_g[e], hh = cold_h[e];
     if (!WIDE) {
       const uint32_t s = hot[e];
@@ -257,22 +280,37 @@ __global__ void __launch_bounds__(1024, 1)
   }
 }
 
-template <bool CONST_HESS>
+template <bool WIDE>
 __global__ void __launch_bounds__(1024, 1)
-    k_hist_float(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
-                 int blocks_per_tile, int post, int par) {
+    k_hist_int(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
+               int blocks_per_tile, int flush_rounds, int direct_rows, int post, int par) {
   extern __shared__ __align__(16) unsigned char smem[];
-  const int B = p.B;
+  const TileGeom geo = p.tiles[blockIdx.y];  // static: loaded while the previous kernel finishes
+  // the shared histogram is zeroed while the previous kernel of the grow loop finishes
   {
     uint4* z = reinterpret_cast<uint4*>(smem);
-    const int n16 = (CONST_HESS ? 3 : 4) * B * TILE / 4;
+    const int n16 = (WIDE ? 2 : 3) * geo.bins * TILE / 4;
     for (int e = threadIdx.x; e < n16; e += blockDim.x) z[e] = make_uint4(0, 0, 0, 0);
   }
   griddep_wait();
   const Job& J = jobs.job[blockIdx.z];
   Range R;
   if (!cta_range(J, p, blocks_per_tile, post, par, &R)) return;
+  if (geo.nibble)
+    hist_int_rows<WIDE, true>(J, p, R, geo, bins_rt, bins_tm, flush_rounds, direct_rows, smem);
+  else
+    hist_int_rows<WIDE, false>(J, p, R, geo, bins_rt, bins_tm, flush_rounds, direct_rows, smem);
+}
+
+// The rows and flush of one float-histogram CTA, its range known (NIBBLE: the tile holds 4-bit
+// bins).
+template <bool CONST_HESS, bool NIBBLE>
+__device__ __forceinline__ void hist_float_rows(const Job& J, const Params& p, const Range& R, const TileGeom& geo,
+                                                const uint8_t* __restrict__ bins_rt,
+                                                const uint8_t* __restrict__ bins_tm, unsigned char* smem) {
   const int tile = blockIdx.y;
+  const int B = geo.bins;
+  const bool half = geo.width == 16;  // one 16-byte run per row
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   float* ghi = reinterpret_cast<float*>(smem);
   float* glo = ghi + B * TILE;
@@ -282,10 +320,10 @@ __global__ void __launch_bounds__(1024, 1)
   float2* stage_v = reinterpret_cast<float2*>(stage + nwarps * 64);
   uint32_t* hcnt = reinterpret_cast<uint32_t*>(hhi);
   __syncthreads();
-  // the tile's sector of row 0 and the row stride, in the copy that suits the leaf's density
+  // the tile's run of row 0 and the row stride, in the copy that suits the leaf's density
   const bool dense = R.count * 4 >= p.n;
-  const uint8_t* tb = dense ? bins_tm + (size_t)tile * (size_t)p.n * TILE : bins_rt + (size_t)tile * TILE;
-  const size_t rs = dense ? (size_t)TILE : (size_t)p.T * TILE;
+  const uint8_t* tb = dense ? bins_tm + geo.tm_off : bins_rt + geo.rt_off;
+  const size_t rs = dense ? (size_t)tile_width(geo) : (size_t)p.rt_stride;
   const bool feat_lane = tile * TILE + lane < p.F;
   const float* G = J.g;
   const float* H = J.h;
@@ -298,7 +336,7 @@ __global__ void __launch_bounds__(1024, 1)
     if (row >= 0) {
       const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * rs);
       a = __ldg(src);
-      b = __ldg(src + 1);
+      if (!half) b = __ldg(src + 1);
       v.x = G[row];
       if (!CONST_HESS) v.y = H[row];
     }
@@ -325,7 +363,7 @@ __global__ void __launch_bounds__(1024, 1)
     const int jn = (int)min((int64_t)32, R.r1 - base);  // warp-uniform; padding lanes add nothing
 #pragma unroll 4
     for (int j = 0; j < jn; ++j) {
-      uint32_t e = (uint32_t)sb[j * 32 + lane] * TILE + lane;
+      uint32_t e = staged_bin<NIBBLE>(sb, j, lane) * TILE + lane;
       float2 vv = stage_v[warp * 32 + j];
       if (feat_lane) {
         float old = atomicAdd(&ghi[e], vv.x);
@@ -344,7 +382,7 @@ __global__ void __launch_bounds__(1024, 1)
   }
   griddep_launch();
   __syncthreads();
-  double2* slot = reinterpret_cast<double2*>(J.pool) + ((size_t)R.slot * p.T + tile) * (size_t)B * TILE;
+  double2* slot = reinterpret_cast<double2*>(J.pool) + ((size_t)R.slot * p.T + tile) * (size_t)p.B * TILE;
   const double h0 = CONST_HESS ? (double)H[0] : 0.0;
   for (int e = threadIdx.x; e < B * TILE; e += blockDim.x) {
     double gs = (double)ghi[e] + (double)glo[e];
@@ -355,6 +393,27 @@ __global__ void __launch_bounds__(1024, 1)
       atomicAdd(&slot[e].y, hs);
     }
   }
+}
+
+template <bool CONST_HESS>
+__global__ void __launch_bounds__(1024, 1)
+    k_hist_float(const JobTable jobs, Params p, const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
+                 int blocks_per_tile, int post, int par) {
+  extern __shared__ __align__(16) unsigned char smem[];
+  const TileGeom geo = p.tiles[blockIdx.y];  // static: loaded while the previous kernel finishes
+  {
+    uint4* z = reinterpret_cast<uint4*>(smem);
+    const int n16 = (CONST_HESS ? 3 : 4) * geo.bins * TILE / 4;
+    for (int e = threadIdx.x; e < n16; e += blockDim.x) z[e] = make_uint4(0, 0, 0, 0);
+  }
+  griddep_wait();
+  const Job& J = jobs.job[blockIdx.z];
+  Range R;
+  if (!cta_range(J, p, blocks_per_tile, post, par, &R)) return;
+  if (geo.nibble)
+    hist_float_rows<CONST_HESS, true>(J, p, R, geo, bins_rt, bins_tm, smem);
+  else
+    hist_float_rows<CONST_HESS, false>(J, p, R, geo, bins_rt, bins_tm, smem);
 }
 
 }  // namespace
@@ -375,10 +434,10 @@ void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t
     if (p.quant) {
       if (hl.flush_rounds > 0)
         (void)launch_kernel(k_hist_int<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
-                            hl.blocks_per_tile, hl.flush_rounds, post, par);
+                            hl.blocks_per_tile, hl.flush_rounds, hl.direct_rows, post, par);
       else
         (void)launch_kernel(k_hist_int<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
-                            hl.blocks_per_tile, 1, post, par);
+                            hl.blocks_per_tile, 1, hl.direct_rows, post, par);
     } else if (p.const_hess) {
       (void)launch_kernel(k_hist_float<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
                           hl.blocks_per_tile, post, par);

@@ -89,30 +89,42 @@ struct HostMt {
   }
 };
 
-// The two row-tiled copies of the column-major bins: rt [n][T][32] and tm [T][n][32].
+// The two row-tiled copies of the column-major bins: rt [n][rt_stride] and tm, tile t's block
+// [n][width_t] at tiles[t].tm_off; a 4-bit tile packs feature 2k into the low nibble of byte k
+// and feature 2k + 1 into its high nibble; a 16-byte 8-bit tile holds the tile's first 16 features.
 __global__ void k_pack_rowtile(const uint8_t* __restrict__ cm, uint8_t* __restrict__ rt, uint8_t* __restrict__ tm,
-                               int64_t n, int F, int T) {
+                               int64_t n, int F, int T, const TileGeom* __restrict__ tiles, int rt_stride) {
   int64_t total = n * T;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < total; k += (int64_t)gridDim.x * blockDim.x) {
     int64_t tile = k / n, row = k % n;
+    const TileGeom g = tiles[tile];
     uint32_t w[8];
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
       uint32_t v = 0;
 #pragma unroll
       for (int b = 0; b < 4; ++b) {
-        int f = (int)tile * TILE + q * 4 + b;
-        uint32_t x = f < F ? cm[(size_t)f * n + row] : 0u;
-        v |= x << (8 * b);
+        if (g.nibble) {  // byte q * 4 + b of the 16-byte run holds features 2 (q * 4 + b) and + 1
+          const int f0 = (int)tile * TILE + 2 * (q * 4 + b);
+          uint32_t lo = (q < 4 && f0 < F) ? cm[(size_t)f0 * n + row] : 0u;
+          uint32_t hi = (q < 4 && f0 + 1 < F) ? cm[(size_t)(f0 + 1) * n + row] : 0u;
+          v |= ((lo & 15u) | ((hi & 15u) << 4)) << (8 * b);
+        } else {
+          int f = (int)tile * TILE + q * 4 + b;
+          uint32_t x = f < F ? cm[(size_t)f * n + row] : 0u;
+          v |= x << (8 * b);
+        }
       }
       w[q] = v;
     }
-    uint4* dst = reinterpret_cast<uint4*>(rt + ((size_t)row * T + tile) * TILE);
+    uint4* dst = reinterpret_cast<uint4*>(rt + (size_t)row * rt_stride + g.rt_off);
+    uint4* dtm = reinterpret_cast<uint4*>(tm + g.tm_off + (size_t)row * tile_width(g));
     dst[0] = make_uint4(w[0], w[1], w[2], w[3]);
-    dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
-    uint4* dtm = reinterpret_cast<uint4*>(tm + ((size_t)tile * n + row) * TILE);
     dtm[0] = make_uint4(w[0], w[1], w[2], w[3]);
-    dtm[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    if (g.width == 32) {
+      dst[1] = make_uint4(w[4], w[5], w[6], w[7]);
+      dtm[1] = make_uint4(w[4], w[5], w[6], w[7]);
+    }
   }
 }
 
@@ -133,8 +145,9 @@ struct bk_learner {
   DevFeature* d_feat = nullptr;
   std::vector<DevFeature> h_feat;
   uint8_t* d_bins_cm = nullptr;
-  uint8_t* d_bins_rt = nullptr;  // [n][T][32]: gathered leaves
-  uint8_t* d_bins_tm = nullptr;  // [T][n][32]: the root and dense leaves
+  uint8_t* d_bins_rt = nullptr;  // [n][rt_stride]: gathered leaves
+  uint8_t* d_bins_tm = nullptr;  // per tile [n][width]: the root and dense leaves
+  std::vector<TileGeom> h_tiles;
   double* d_noise_g = nullptr;
   double* d_noise_h = nullptr;
   // jobs
@@ -188,8 +201,9 @@ struct bk_learner {
   // leaf never has more rows than the dataset, so CTAs past n / min_rows would never get rows.
   // Results do not depend on it (integer histograms are exact; the float path changes only its
   // rounding order; the partitions it feeds are the same). The graph is captured anew.
-  void set_launch_shape(int hist_min_rows, int hist_ctas_per_tile, int part_grid) {
+  void set_launch_shape(int hist_min_rows, int hist_ctas_per_tile, int part_grid, int direct_rows) {
     const int64_t n = p.n;
+    hl.direct_rows = std::max(0, direct_rows);
     p.hist_min_rows = std::max(32, hist_min_rows / 32 * 32);
     hl.blocks_per_tile = (int)std::max<int64_t>(
         1, std::min<int64_t>(hist_ctas_per_tile, (n + p.hist_min_rows - 1) / p.hist_min_rows));
@@ -198,6 +212,13 @@ struct bk_learner {
       cudaGraphExecDestroy(graph_exec);
       graph_exec = nullptr;
     }
+  }
+
+  void shape_of(int32_t* out) const {
+    out[0] = p.hist_min_rows;
+    out[1] = hl.blocks_per_tile;
+    out[2] = p.part_grid;
+    out[3] = hl.direct_rows;
   }
 
   bool capturing = false;
@@ -403,11 +424,31 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
         }
     }
     p.B = (maxb + 7) / 8 * 8;
+    // the feature tiles' stored-bin layouts: 16-byte runs of 4-bit bins for tiles whose features
+    // all have at most 16 group bins, 8-bit runs otherwise (16 bytes for a last tile of at most
+    // 16 features, else 32); each tile's shared histogram holds its largest feature's group bins
+    {
+      int64_t off = 0;
+      for (int t = 0; t < p.T; ++t) {
+        TileGeom g{};
+        int tb = 0;
+        const int nf_tile = std::min(num_features, (t + 1) * TILE) - t * TILE;
+        for (int f = t * TILE; f < t * TILE + nf_tile; ++f) tb = std::max(tb, L->h_feat[f].gbins);
+        g.bins = (tb + 7) / 8 * 8;
+        g.nibble = tb <= 16 ? 1 : 0;
+        g.width = (g.nibble || nf_tile <= 16) ? 16 : 32;
+        g.rt_off = off;
+        g.tm_off = off * num_data;
+        off += tile_width(g);
+        L->h_tiles.push_back(g);
+      }
+      p.rt_stride = (int32_t)off;
+    }
     // launch shapes: histogram CTAs of 1024 threads, one per SM, split evenly over the feature
     // tiles, each taking at least 256 rows; two partition CTAs per SM; no more CTAs than the
-    // dataset's rows can fill (bk_learner_autotune may change all three)
+    // dataset's rows can fill; no direct-atomic CTAs (bk_learner_autotune may change all four)
     L->hl.threads = 1024;
-    L->set_launch_shape(256, L->num_sms / p.T, 2 * L->num_sms);
+    L->set_launch_shape(256, L->num_sms / p.T, 2 * L->num_sms, 0);
     bool wide = false;
     if (quant) {
       int max_h = p.const_hess ? 1 : p.quant_bins;
@@ -446,10 +487,13 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
         return -1;
       }
     }
-    L->d_bins_rt = L->dalloc<uint8_t>(n * p.T * TILE);
-    L->d_bins_tm = L->dalloc<uint8_t>(n * p.T * TILE);
+    TileGeom* d_tiles = L->dalloc<TileGeom>(p.T);
+    CK(cudaMemcpy(d_tiles, L->h_tiles.data(), sizeof(TileGeom) * p.T, cudaMemcpyHostToDevice));
+    p.tiles = d_tiles;
+    L->d_bins_rt = L->dalloc<uint8_t>(n * (size_t)p.rt_stride);
+    L->d_bins_tm = L->dalloc<uint8_t>(n * (size_t)p.rt_stride);
     k_pack_rowtile<<<4 * L->num_sms, 256, 0, L->stream>>>(L->d_bins_cm, L->d_bins_rt, L->d_bins_tm, num_data,
-                                                          num_features, p.T);
+                                                          num_features, p.T, d_tiles, p.rt_stride);
     CK(cudaGetLastError());
     if (quant && p.stochastic) {
       // GradientDiscretizer::init_stochastic (gradient_discretizer/mod.rs:87-106)
@@ -666,7 +710,9 @@ void train_finish(bk_learner* L, bk_split* splits, double* leaf_values, double* 
   double bytes = 0.0;
   for (size_t j = 0; j < K; ++j) {
     const JobState& s = L->h_state[j];
-    double per_row = (double)p.F + (p.quant ? 2.0 : (p.const_hess ? 4.0 : 8.0));
+    double bin_bytes = 0.0;  // a 4-bit tile's features take half a byte each
+    for (int f = 0; f < p.F; ++f) bin_bytes += L->h_tiles[f / TILE].nibble ? 0.5 : 1.0;
+    double per_row = bin_bytes + (p.quant ? 2.0 : (p.const_hess ? 4.0 : 8.0));
     bytes += (double)s.hist_rows_direct * per_row + (double)s.hist_rows_gather * (per_row + 4.0);
     double slot_bytes = 0.0;
     for (const DevFeature& f : L->h_feat) slot_bytes += (double)f.gbins * (p.quant ? 8.0 : 16.0);
@@ -707,7 +753,7 @@ namespace {
 // Autotuned launch shapes by shape class: (device, log2 rows, feature tiles, bins per feature
 // slot, quantized, num_leaves, jobs) -> (hist_min_rows, hist CTAs per tile, partition CTAs).
 std::mutex g_tune_mutex;
-std::map<std::array<int, 7>, std::array<int, 3>> g_tune_cache;
+std::map<std::array<int, 7>, std::array<int, 4>> g_tune_cache;
 
 std::array<int, 7> tune_key(const bk_learner* L) {
   int lg = 0;
@@ -728,12 +774,8 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
     std::lock_guard<std::mutex> g(g_tune_mutex);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
-      L->set_launch_shape(it->second[0], it->second[1], it->second[2]);
-      if (shape_out) {
-        shape_out[0] = L->p.hist_min_rows;
-        shape_out[1] = L->hl.blocks_per_tile;
-        shape_out[2] = L->p.part_grid;
-      }
+      L->set_launch_shape(it->second[0], it->second[1], it->second[2], it->second[3]);
+      if (shape_out) L->shape_of(shape_out);
       return 0;
     }
   }
@@ -751,11 +793,11 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
     if (gradients != L->d_g) CK(cudaMemcpyAsync(L->d_g, gradients, n * sizeof(float), kind, L->stream));
     if (hessians != L->d_h) CK(cudaMemcpyAsync(L->d_h, hessians, n * sizeof(float), kind, L->stream));
     L->loop_mode = 1;
-    std::map<std::array<int, 3>, double> seen;
+    std::map<std::array<int, 4>, double> seen;
     // one tree per trial (graph form) after one untimed tree of each shape; the median device time
-    auto measure = [&](int min_rows, int ctas, int grid) -> std::pair<std::array<int, 3>, double> {
-      L->set_launch_shape(min_rows, ctas, grid);
-      std::array<int, 3> s = {L->p.hist_min_rows, L->hl.blocks_per_tile, L->p.part_grid};
+    auto measure = [&](const std::array<int, 4>& c) -> std::pair<std::array<int, 4>, double> {
+      L->set_launch_shape(c[0], c[1], c[2], c[3]);
+      std::array<int, 4> s = {L->p.hist_min_rows, L->hl.blocks_per_tile, L->p.part_grid, L->hl.direct_rows};
       auto f = seen.find(s);
       if (f != seen.end()) return {s, f->second};
       std::vector<double> t;
@@ -771,10 +813,10 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
     };
     // coordinate descent from the default shape: rows per histogram CTA, histogram CTAs per
     // feature tile, partition CTAs
-    std::array<int, 3> best = {256, sms / T, 2 * sms};
-    double best_ms = measure(best[0], best[1], best[2]).second;
-    auto consider = [&](std::array<int, 3> c) {
-      auto r = measure(c[0], c[1], c[2]);
+    std::array<int, 4> best = {256, sms / T, 2 * sms, 0};
+    double best_ms = measure(best).second;
+    auto consider = [&](std::array<int, 4> c) {
+      auto r = measure(c);
       if (r.second < best_ms) {
         best_ms = r.second;
         best = c;
@@ -782,24 +824,23 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
     };
     // rows per histogram CTA: small values spread small leaves over more SMs; large ones give
     // mid-size leaves fewer CTAs, so fewer shared histograms to flush into the pool slot
-    for (int mr : {64, 128, 512, 1024, 2048, 4096, 8192, 16384}) consider({mr, best[1], best[2]});
-    for (int ct : {2 * sms / T, sms / (2 * T)}) consider({best[0], ct, best[2]});
-    for (int pg : {sms, 4 * sms}) consider({best[0], best[1], pg});
+    for (int mr : {64, 128, 512, 1024, 2048, 4096, 8192, 16384}) consider({mr, best[1], best[2], best[3]});
+    for (int ct : {2 * sms / T, sms / (2 * T)}) consider({best[0], ct, best[2], best[3]});
+    for (int pg : {sms, 4 * sms}) consider({best[0], best[1], pg, best[3]});
+    // the global-atomic variant of the quantized histogram for CTAs with few rows
+    if (L->p.quant)
+      for (int dr : {128, 256, 512, 1024, 2048}) consider({best[0], best[1], best[2], dr});
     CK(cudaMemcpyAsync(L->jobs[0].st, saved, state_bytes, cudaMemcpyDeviceToDevice, L->stream));
     CK(cudaFreeAsync(saved, L->stream));
     saved = nullptr;
     CK(cudaStreamSynchronize(L->stream));
     L->loop_mode = saved_mode;
-    L->set_launch_shape(best[0], best[1], best[2]);
+    L->set_launch_shape(best[0], best[1], best[2], best[3]);
     {
       std::lock_guard<std::mutex> g(g_tune_mutex);
       g_tune_cache[key] = best;
     }
-    if (shape_out) {
-      shape_out[0] = L->p.hist_min_rows;
-      shape_out[1] = L->hl.blocks_per_tile;
-      shape_out[2] = L->p.part_grid;
-    }
+    if (shape_out) L->shape_of(shape_out);
   } catch (const CudaError& e) {
     if (saved) {
       cudaMemcpyAsync(L->jobs[0].st, saved, state_bytes, cudaMemcpyDeviceToDevice, L->stream);
@@ -814,11 +855,11 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
 }
 
 int bk_learner_set_launch_shape(bk_learner* L, const int32_t* shape) {
-  if (!L || !shape || shape[0] < 32 || shape[1] < 1 || shape[2] < 1) {
+  if (!L || !shape || shape[0] < 32 || shape[1] < 1 || shape[2] < 1 || shape[3] < 0) {
     set_error("bk_learner_set_launch_shape: invalid arguments");
     return -1;
   }
-  L->set_launch_shape(shape[0], shape[1], shape[2]);
+  L->set_launch_shape(shape[0], shape[1], shape[2], shape[3]);
   return 0;
 }
 
@@ -827,9 +868,7 @@ int bk_learner_launch_shape(bk_learner* L, int32_t* shape_out) {
     set_error("bk_learner_launch_shape: invalid arguments");
     return -1;
   }
-  shape_out[0] = L->p.hist_min_rows;
-  shape_out[1] = L->hl.blocks_per_tile;
-  shape_out[2] = L->p.part_grid;
+  L->shape_of(shape_out);
   return 0;
 }
 

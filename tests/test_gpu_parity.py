@@ -304,9 +304,11 @@ def test_device_prediction_replays_the_partition():
         gpu.close()
 
 
-@pytest.mark.parametrize("shape", [(32, 1, 1), (64, 3, 7), (1024, 200, 1024), (256, 38, 304)])
+@pytest.mark.parametrize("shape", [(32, 1, 1, 0), (64, 3, 7, 0), (1024, 200, 1024, 0), (256, 38, 304, 0),
+                                   (64, 3, 7, 1 << 30), (256, 38, 304, 512), (32, 64, 64, 96)])
 def test_launch_shapes_do_not_change_results(shape):
-    """Every launch shape grows the oracle's trees: quantized bit-exact, both partition forms."""
+    """Every launch shape grows the oracle's trees: quantized bit-exact, both partition forms,
+    with the shared-histogram CTAs, the global-atomic CTAs (every CTA at 1 << 30) or a mix."""
     cfg = dict(num_leaves=31, use_quantized_grad=1, stochastic_rounding=1, seed=2, num_threads=2)
     ds, z = _dataset(25000, 40, seed=21)
     g, h, const = _grads(z, "binary", seed=22)
@@ -315,6 +317,7 @@ def test_launch_shapes_do_not_change_results(shape):
         gpu.set_launch_shape(shape)
         got = gpu.launch_shape()
         assert got[0] == max(32, shape[0] // 32 * 32) and 1 <= got[1] <= shape[1] and 1 <= got[2] <= shape[2]
+        assert got[3] == shape[3]
         for it in range(2):
             ro, rg = orc.train(g, h), gpu.train(g, h)
             _assert_records_equal(ro[0], rg[0])
@@ -431,3 +434,42 @@ def test_bynode_column_sample(bytree, bynode, constrained):
         g = (g * 0.9).astype(np.float32)
     gpu.set_bynode(1.0, False, 0)
     gpu.close()
+
+
+@pytest.mark.parametrize("quant", [1, 0])
+def test_packed_bin_tiles(quant):
+    """Stored-bin tiles of every layout in one dataset: 32 features of at most 16 group bins (a
+    4-bit tile, two bins per byte as io/bin_data.rs:20-30 stores them), 32 features of 8-bit bins
+    and a last tile of 8 features (a 16-byte 8-bit run): the quantized trees equal the oracle's bit
+    for bit, with shared-histogram and global-atomic histogram CTAs; the float trees agree within
+    the float tolerance."""
+    from lgbm_gb300 import BinnedDataset
+    rng = np.random.default_rng(31)
+    n, F = 40000, 72
+    X = rng.standard_normal((n, F))
+    X[:, 40:50] = rng.integers(0, 6, size=(n, 10))
+    X[rng.random((n, F)) < 0.03] = np.nan
+    z = np.nan_to_num(X) @ rng.standard_normal(F) * 0.3
+    ds = BinnedDataset.from_dense(X, max_bin_by_feature=[15] * 32 + [255] * 40)
+    gb = [fi.group_bins for fi in ds.features]
+    assert len(gb) == F and max(gb[:32]) <= 16 and max(gb[32:64]) > 16
+    g, h, const = _grads(z, "binary", seed=32)
+    cfg = dict(num_leaves=31, use_quantized_grad=quant, stochastic_rounding=1, seed=3, num_threads=2)
+    shapes = [(256, 38, 304, 0), (64, 20, 64, 1 << 30)] if quant else [(256, 38, 304, 0)]
+    for shape in shapes:
+        for loop_mode in (1, 0):
+            orc, gpu, _ = _learners(ds, const, loop_mode=loop_mode, **cfg)
+            gpu.set_launch_shape(shape)
+            gg = g
+            for it in range(2):
+                ro, rg = orc.train(gg, h), gpu.train(gg, h)
+                if quant:
+                    _assert_records_equal(ro[0], rg[0])
+                    assert np.array_equal(ro[1], rg[1])
+                    assert np.array_equal(orc.row_leaf(), gpu.row_leaf())
+                else:
+                    import harness
+                    e = harness.gain_errors(rg[0], ro[0])
+                    assert e["max_rel"] <= 1e-6, e
+                gg = (gg * 0.9).astype(np.float32)
+            gpu.close()
