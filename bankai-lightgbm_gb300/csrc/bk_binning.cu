@@ -192,10 +192,12 @@ using namespace bk;
 
 namespace {
 
-template <typename... A>
-void bin_error(const char* fmt, A... a) {
+void bin_error(const char* msg) { bk_set_last_error(msg); }
+
+template <typename A0, typename... A>
+void bin_error(const char* fmt, A0 a0, A... a) {
   char buf[256];
-  snprintf(buf, sizeof(buf), fmt, a...);
+  snprintf(buf, sizeof(buf), fmt, a0, a...);
   bk_set_last_error(buf);
 }
 

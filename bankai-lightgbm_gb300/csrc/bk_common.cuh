@@ -109,6 +109,7 @@ struct LeafConst {
   float gsf, hsf, l2f;     // fp32 copies of the gradient / hessian scales and lambda_l2
   float _pad;
   double gs, hs;           // quantized path: the gradient / hessian scales
+  LeafSum ls;              // the leaf's sums (its LeafSplits), as leaf_sum[leaf] holds them
 };
 
 // Per-job control block, written and read only by kernels (the device-resident grow loop).
@@ -274,9 +275,15 @@ cudaError_t predict_tree(const DevFeature* feats, int32_t num_leaves, const int3
                          const uint8_t* bins, int64_t m, double* score, cudaStream_t s);
 
 // bk_objective.cu
+// Row weights (device f32 [n] or null: Metadata::weights) and the binary objective's label
+// weights of the negative and positive class (BinaryLogloss::label_weights, binary.rs:33-52).
+struct ObjectiveWeights {
+  const float* row = nullptr;
+  double label_neg = 1.0, label_pos = 1.0;
+};
 // bad_label: device counter of multiclass labels outside [0, K) (kind 2 only)
 cudaError_t objective_gradients(int kind, const double* score, const float* label, int64_t n, int K, double sigmoid,
-                                float* g, float* h, int32_t* bad_label, cudaStream_t s);
+                                const ObjectiveWeights& ow, float* g, float* h, int32_t* bad_label, cudaStream_t s);
 cudaError_t objective_loss(int kind, const double* score, const float* label, int64_t n, int K, double* partial,
                            int grid, int32_t* bad_label, cudaStream_t s);
 void launch_tree_begin(const Job* d_jobs, int num_jobs, const Params& p, cudaStream_t s);

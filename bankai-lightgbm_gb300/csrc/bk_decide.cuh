@@ -131,7 +131,8 @@ struct Decision {
 // is issued up front (the candidates of both searched leaves and every other leaf's best), then
 // one barrier; warp 0 finishes. Candidates written by other CTAs are read through L2 (__ldcg). A
 // leaf's best split stays in cand[leaf][feature]; the partition builds the route table of the
-// chosen split from (inner, thr).
+// chosen split from (inner, thr). A stopped tree (the stop flag is loaded with everything else, so
+// the caller need not test it first) gives out->stop = 1 and writes nothing.
 __device__ void decide_split(const Job& J, const Params& p, const DevFeature* feats, bool record, Decision* out) {
   __shared__ Pick s_f[kDecideWarps], s_l[kDecideWarps];
   // the row range of the first kDecideThreads leaves, so the chosen leaf's is at hand for the
@@ -141,6 +142,7 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
   JobState* st = J.st;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   constexpr int kHalf = kDecideThreads / 2;
+  const bool stopped = st->stop != 0;
   const bool searched = st->do_search != 0;
   const int32_t leaf0 = st->smaller_leaf, leaf1 = st->larger_leaf;
   const Pick none{-1, 0x7fffffff, 0, false, 0.0, 0};
@@ -162,7 +164,7 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
       // serial.rs:1538-1554: the by-node sample gates only the fold, not the splittable flags
       const uint8_t nm = p.bynode ? __ldcg(&J.used[(size_t)(1 + side) * p.F + f]) : (uint8_t)1;
       if (!searched || leaf < 0 || !u) continue;
-      if (record) J.splittable[(size_t)slot * p.F + f] = cs;
+      if (record && !stopped) J.splittable[(size_t)slot * p.F + f] = cs;
       if (nm) pick(a, make_pick(f, g, real, th));
     }
   }
@@ -197,6 +199,10 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
   }
   __syncthreads();
   if (warp != 0) return;
+  if (stopped) {
+    if (lane == 0) out->stop = 1;
+    return;
+  }
   // lanes 0 / 1: the new best of the smaller / larger leaf
   Pick nb = none;
   const int32_t my_leaf = lane == 0 ? leaf0 : leaf1;

@@ -61,11 +61,13 @@ struct Range {
 __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blocks_per_tile, int post, int par,
                                           Range* r) {
   const JobState* st = J.st;
-  if (st->stop) return false;
+  // the stop flag is loaded with the rest of the state (one round of independent loads)
+  const int32_t stop = st->stop;
   int64_t begin, count;
   int32_t buf;
   if (post) {
     const SplitOutcome o = split_outcome(p, st, __ldcg(&st->pcnt[par][0]));
+    if (stop) return false;
     hist_apply_split(J, p, o);
     if (!o.go) return false;
     begin = o.hist_begin();
@@ -74,18 +76,22 @@ __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blo
     r->slot = o.sslot;
     r->pk_row = false;
   } else {
-    hist_leaf_constants(J, p);
-    if (!st->do_search) return false;
+    const int32_t do_search = st->do_search, slot = st->smaller_slot, leaves = st->tree_leaves;
     begin = st->hist_begin;
     count = st->hist_count;
     buf = st->hist_buf;
-    r->slot = st->smaller_slot;
-    r->pk_row = st->tree_leaves == 1;  // the root: no leaf-ordered copy yet
+    if (stop) return false;
+    hist_leaf_constants(J, p);
+    if (!do_search) return false;
+    r->slot = slot;
+    r->pk_row = leaves == 1;  // the root: no leaf-ordered copy yet
   }
   // at least p.hist_min_rows rows per CTA (256 by default, eight warps' worth): small leaves spread
   // over as many SMs as they can fill, since a CTA's rows cost its SM's load and shared-atomic
-  // pipes, not a DRAM share
-  int64_t chunk = ceil_div64(count, blocks_per_tile);
+  // pipes, not a DRAM share. Tile 0 leaves its last CTA, the side CTA, without rows (when it has
+  // others), so the side work (bookkeeping, leaf constants) runs beside the rows, not before them.
+  const int row_ctas = (blockIdx.y == 0 && blocks_per_tile > 1) ? blocks_per_tile - 1 : blocks_per_tile;
+  int64_t chunk = ceil_div64(count, row_ctas);
   if (chunk < p.hist_min_rows) chunk = p.hist_min_rows;
   chunk = (chunk + 31) / 32 * 32;
   r->r0 = (int64_t)blockIdx.x * chunk;
@@ -263,7 +269,6 @@ __device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, con
       __syncthreads();
     }
   }
-  griddep_launch();  // only the flush is left: the next kernel may be scheduled
   if (direct) return;
   __syncthreads();
   for (int e = threadIdx.x; e < Bt * TILE; e += blockDim.x) {
@@ -293,6 +298,9 @@ __global__ void __launch_bounds__(1024, 1)
     for (int e = threadIdx.x; e < n16; e += blockDim.x) z[e] = make_uint4(0, 0, 0, 0);
   }
   griddep_wait();
+  // the search may be scheduled now: its CTAs read their static data while this launch runs, and
+  // wait for its completion before reading anything it writes
+  griddep_launch();
   const Job& J = jobs.job[blockIdx.z];
   Range R;
   if (!cta_range(J, p, blocks_per_tile, post, par, &R)) return;
@@ -380,7 +388,6 @@ __device__ __forceinline__ void hist_float_rows(const Job& J, const Params& p, c
     }
     __syncwarp();
   }
-  griddep_launch();
   __syncthreads();
   double2* slot = reinterpret_cast<double2*>(J.pool) + ((size_t)R.slot * p.T + tile) * (size_t)p.B * TILE;
   const double h0 = CONST_HESS ? (double)H[0] : 0.0;
@@ -407,6 +414,9 @@ __global__ void __launch_bounds__(1024, 1)
     for (int e = threadIdx.x; e < n16; e += blockDim.x) z[e] = make_uint4(0, 0, 0, 0);
   }
   griddep_wait();
+  // the search may be scheduled now: its CTAs read their static data while this launch runs, and
+  // wait for its completion before reading anything it writes
+  griddep_launch();
   const Job& J = jobs.job[blockIdx.z];
   Range R;
   if (!cta_range(J, p, blocks_per_tile, post, par, &R)) return;

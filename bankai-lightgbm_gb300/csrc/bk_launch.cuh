@@ -1,10 +1,12 @@
 // Kernel launches of the grow loop with programmatic dependent launch: each grow-loop kernel is
 // launched with programmatic stream serialization, so it is scheduled while the kernel before it
-// finishes. It runs its independent prologue (shared-memory setup), then waits in griddep_wait()
-// until the previous grid has completed and its writes are visible. Each kernel calls
-// griddep_launch() when only its serial tail is left (the histogram's flush, the search's and the
-// scatter's last-CTA bookkeeping), which lets the next kernel be scheduled then. Without the
-// launch attribute (or when the previous stream operation is not a kernel) both are no-ops.
+// finishes. It runs its independent prologue (shared-memory setup, static metadata), then waits in
+// griddep_wait() until the previous grid has completed and its writes are visible. The histogram,
+// search and single-pass partition kernels call griddep_launch() right after that wait, so the
+// next kernel's CTAs are resident and through their own prologue by the time this one completes
+// (every grid of the chain is small enough to be resident beside the one before it); the stable
+// partition's kernels call it when only their last-CTA bookkeeping is left. Without the launch
+// attribute (or when the previous stream operation is not a kernel) both are no-ops.
 #pragma once
 #include <cuda_runtime.h>
 

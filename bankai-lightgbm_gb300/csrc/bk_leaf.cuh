@@ -101,6 +101,7 @@ __device__ __forceinline__ void compute_leaf_const_ls(const Job& J, const Params
   c._pad = 0.f;
   c.gs = st->gscale;
   c.hs = st->hscale;
+  c.ls = ls;
   if (lane == 0) J.lconst[side] = c;
 }
 

@@ -12,6 +12,7 @@
 
 #include <algorithm>
 #include <array>
+#include <cmath>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
@@ -164,6 +165,7 @@ struct bk_learner {
   double* h_leaf_values = nullptr;
   JobState* h_state = nullptr;
   int32_t* d_bad_label = nullptr;  // multiclass labels outside [0, K) seen by the objective kernels
+  ObjectiveWeights obj_w;          // row / label weights of the device objectives (caller-owned rows)
   int32_t* h_bad_label = nullptr;  // pinned copy, read by the train call that follows the gradients
   double* d_leaf_vals_in = nullptr;
   int32_t* d_tree = nullptr;     // one tree's node arrays for prediction (5 x (num_leaves - 1))
@@ -1006,6 +1008,23 @@ int bk_learner_set_timing(bk_learner* L, int32_t on) {
   return 0;
 }
 
+int bk_learner_histogram_cache_capacity(bk_learner* L, int64_t* capacity) {
+  if (!L || !capacity) {
+    set_error("bk_learner_histogram_cache_capacity: invalid arguments");
+    return -1;
+  }
+  *capacity = L->p.num_leaves;  // a full pool: one slot per leaf
+  return 0;
+}
+
+int bk_learner_reset_histogram_pool_config(bk_learner* L) {
+  if (!L) {
+    set_error("bk_learner_reset_histogram_pool_config: null learner");
+    return -1;
+  }
+  return 0;
+}
+
 int bk_learner_reset_constant_hessian(bk_learner* L, int32_t value) {
   if (!L) {
     set_error("bk_learner_reset_constant_hessian: null learner");
@@ -1196,10 +1215,24 @@ int bk_learner_objective_gradients(bk_learner* L, int32_t kind, const double* sc
     return -1;
   }
   try {
-    CK(objective_gradients(kind, score, label, L->p.n, L->K, sigmoid, L->d_g, L->d_h, L->d_bad_label, L->stream));
+    CK(objective_gradients(kind, score, label, L->p.n, L->K, sigmoid, L->obj_w, L->d_g, L->d_h, L->d_bad_label,
+                           L->stream));
   } catch (const CudaError& e) {
     return fail_cuda(e);
   }
+  return 0;
+}
+
+int bk_learner_set_objective_weights(bk_learner* L, const float* weights, double neg_label_weight,
+                                     double pos_label_weight) {
+  if (!L || !(neg_label_weight > 0.0) || !(pos_label_weight > 0.0) || std::isinf(neg_label_weight) ||
+      std::isinf(pos_label_weight)) {
+    set_error("bk_learner_set_objective_weights: invalid arguments");
+    return -1;
+  }
+  L->obj_w.row = weights;
+  L->obj_w.label_neg = neg_label_weight;
+  L->obj_w.label_pos = pos_label_weight;
   return 0;
 }
 

@@ -1,9 +1,14 @@
 // Built-in objective gradients on the device, written into the learner's gradient buffers, and
 // the training loss, so one boosting iteration (gradients, K trees, score update) stays in HBM:
 //   L2         objective/regression.rs:240-248   g = (score - label) as f32, h = 1
-//   binary     objective/binary.rs:71-90         response = -label*s / (1 + exp(label*s*score))
-//   multiclass objective/multiclass.rs:68-90     softmax over the K class scores of a row
-// Operation order follows the reference. `exp` is CUDA's double-precision exp, which can differ
+//              weighted, regression.rs:321-329   g = ((score - label) as f32) * w, h = w
+//   binary     objective/binary.rs:71-90         response = -label*s / (1 + exp(label*s*score)),
+//                                                times the label weight of the row's class
+//                                                (binary.rs:33-52) and the row weight
+//   multiclass objective/multiclass.rs:68-90     softmax over the K class scores of a row, times
+//                                                the row weight
+// Operation order follows the reference. Row weights (`w`, device f32 [n], or null) and the
+// binary label weights are set on the learner (bk_learner_set_objective_weights). `exp` is CUDA's double-precision exp, which can differ
 // from the host libm's in the last bit, so binary / multiclass gradients may differ from a host
 // computation by one f32 ulp; the learner's parity is checked on given gradients.
 //
@@ -19,24 +24,40 @@ namespace bk {
 namespace {
 
 __global__ void k_grad_l2(const double* __restrict__ score, const float* __restrict__ label, int64_t n,
-                          float* __restrict__ g, float* __restrict__ h) {
+                          const float* __restrict__ w, float* __restrict__ g, float* __restrict__ h) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    g[i] = (float)(score[i] - (double)label[i]);
-    h[i] = 1.0f;
+    const float d = (float)(score[i] - (double)label[i]);
+    if (w) {
+      const float wi = w[i];
+      g[i] = __fmul_rn(d, wi);
+      h[i] = wi;
+    } else {
+      g[i] = d;
+      h[i] = 1.0f;
+    }
   }
 }
 
 __global__ void k_grad_binary(const double* __restrict__ score, const float* __restrict__ label, int64_t n,
-                              double sigmoid, float* __restrict__ g, float* __restrict__ h) {
+                              double sigmoid, const float* __restrict__ w, double lw_neg, double lw_pos,
+                              float* __restrict__ g, float* __restrict__ h) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
-    double lab = label[i] > 0.0f ? 1.0 : -1.0;
+    const bool pos = label[i] > 0.0f;
+    double lab = pos ? 1.0 : -1.0;
+    const double lw = pos ? lw_pos : lw_neg;
     double t = -lab * sigmoid;
     double e = exp(lab * sigmoid * score[i]);
     double response = t / (1.0 + e);
     double ar = fabs(response);
-    g[i] = (float)(response * 1.0);
     double q = ar * (sigmoid - ar);
-    h[i] = (float)(q * 1.0);
+    if (w) {
+      const double wi = (double)w[i];
+      g[i] = (float)(response * lw * wi);
+      h[i] = (float)(q * lw * wi);
+    } else {
+      g[i] = (float)(response * lw);
+      h[i] = (float)(q * lw);
+    }
   }
 }
 
@@ -48,7 +69,8 @@ __device__ __forceinline__ int class_of(float lf, int K, int32_t* bad_label) {
 }
 
 __global__ void k_grad_softmax(const double* __restrict__ score, const float* __restrict__ label, int64_t n, int K,
-                               float* __restrict__ g, float* __restrict__ h, int32_t* __restrict__ bad_label) {
+                               const float* __restrict__ w, float* __restrict__ g, float* __restrict__ h,
+                               int32_t* __restrict__ bad_label) {
   const double factor = (double)K / ((double)K - 1.0);
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     double rec[32];
@@ -60,13 +82,14 @@ __global__ void k_grad_softmax(const double* __restrict__ score, const float* __
       wsum += rec[k];
     }
     const int lab = class_of(label[i], K, bad_label);
+    const double wi = w ? (double)w[i] : 1.0;
     for (int k = 0; k < K; ++k) {
       double p = rec[k] / wsum;
       double gi = lab == k ? p - 1.0 : p;
       double hi = factor * p;
       hi = hi * (1.0 - p);
-      g[(size_t)k * n + i] = (float)gi;
-      h[(size_t)k * n + i] = (float)hi;
+      g[(size_t)k * n + i] = (float)(w ? gi * wi : gi);
+      h[(size_t)k * n + i] = (float)(w ? hi * wi : hi);
     }
   }
 }
@@ -106,11 +129,12 @@ __global__ void k_loss(int kind, const double* __restrict__ score, const float* 
 }  // namespace
 
 cudaError_t objective_gradients(int kind, const double* score, const float* label, int64_t n, int K, double sigmoid,
-                                float* g, float* h, int32_t* bad_label, cudaStream_t s) {
+                                const ObjectiveWeights& ow, float* g, float* h, int32_t* bad_label, cudaStream_t s) {
   const int grid = 1024, threads = 256;
-  if (kind == 0) k_grad_l2<<<grid, threads, 0, s>>>(score, label, n, g, h);
-  else if (kind == 1) k_grad_binary<<<grid, threads, 0, s>>>(score, label, n, sigmoid, g, h);
-  else k_grad_softmax<<<grid, threads, 0, s>>>(score, label, n, K, g, h, bad_label);
+  if (kind == 0) k_grad_l2<<<grid, threads, 0, s>>>(score, label, n, ow.row, g, h);
+  else if (kind == 1)
+    k_grad_binary<<<grid, threads, 0, s>>>(score, label, n, sigmoid, ow.row, ow.label_neg, ow.label_pos, g, h);
+  else k_grad_softmax<<<grid, threads, 0, s>>>(score, label, n, K, ow.row, g, h, bad_label);
   return cudaGetLastError();
 }
 

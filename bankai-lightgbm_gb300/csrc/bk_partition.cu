@@ -55,14 +55,13 @@ __device__ __forceinline__ Decision recorded_decision(const JobState* st) {
 
 __device__ __forceinline__ void part_range(const Job& J, const Params& p, const uint8_t* bins_cm, const Decision& d,
                                            PartRange* r) {
-  const JobState* st = J.st;
   r->begin = d.begin;
   r->count = d.count;
   const int32_t buf = d.buf;
   r->src = leaf_idx(J, buf) + r->begin;
   r->dst = leaf_idx_w(J, 1 - buf) + r->begin;
   r->col = bins_cm + (size_t)d.inner * (size_t)p.n;
-  r->pk_row = st->tree_leaves == 1;  // the root: no leaf-ordered copy yet
+  r->pk_row = d.new_leaf == 1;  // the root (one leaf when decided): no leaf-ordered copy yet
   r->pk_src = p.quant ? (r->pk_row ? J.packed : leaf_pk(J, buf) + r->begin) : nullptr;
   r->pk_dst = p.quant ? leaf_pk(J, 1 - buf) + r->begin : nullptr;
   // rows per CTA in multiples of one row per thread: a small leaf spreads over as many CTAs as
@@ -103,14 +102,14 @@ __device__ __forceinline__ T block_excl_scan(T v, T* total, T* sh) {
   return excl;
 }
 
-// The route of every stored bin of the chosen split (data_partition.rs:299-410), one per thread.
+// The route of every stored bin of the chosen split (data_partition.rs:299-410), one per thread,
+// from the split feature's metadata `m` (gbins, default_bin, mfb, missing, cat, offset).
 // A categorical split routes by the bitset of its left bins, kept in the chosen leaf's candidate
 // (data_partition.rs:264-300 and route_bin :367-377): group bin 0 (the most frequent bin's rows)
 // goes left when the most frequent bin is not 0 and is in the bitset; stored bin b looks up bit
 // b - 1 + offset.
-__device__ __forceinline__ void build_route(const Job& J, const Params& p, const Decision& d,
-                                            const DevFeature* feats, uint8_t* lut) {
-  const DevFeature m = feats[d.inner];
+__device__ __forceinline__ void build_route_of(const Job& J, const Params& p, const Decision& d, const DevFeature m,
+                                               uint8_t* lut) {
   const uint32_t b = threadIdx.x;
   if (m.cat) {
     const uint32_t* bits = cand_cat_bits(J, p, d.leaf, d.inner);
@@ -121,6 +120,33 @@ __device__ __forceinline__ void build_route(const Job& J, const Params& p, const
   }
   const uint32_t th = d.thr;
   lut[b] = (int)b < m.gbins ? route_bin(m, th & 0x7fffffffu, (th >> 31) != 0, b) : 0;
+}
+
+__device__ __forceinline__ void build_route(const Job& J, const Params& p, const Decision& d,
+                                            const DevFeature* feats, uint8_t* lut) {
+  build_route_of(J, p, d, feats[d.inner], lut);
+}
+
+// What build_route needs of a feature, packed in 8 bytes so a CTA can hold every feature's in
+// shared memory before the split is known: x = gbins | default_bin << 16, y = mfb | missing << 16 |
+// cat << 20 | offset << 21.
+constexpr int kRoutePrefetch = 1024;  // features whose descriptors a partition CTA keeps
+
+__device__ __forceinline__ uint2 route_desc(const DevFeature& m) {
+  return make_uint2((uint32_t)m.gbins | ((uint32_t)m.default_bin << 16),
+                    (uint32_t)m.mfb | ((uint32_t)m.missing << 16) | ((uint32_t)(m.cat != 0) << 20) |
+                        ((uint32_t)m.offset << 21));
+}
+
+__device__ __forceinline__ DevFeature route_feature(uint2 q) {
+  DevFeature m{};
+  m.gbins = (int32_t)(q.x & 0xffffu);
+  m.default_bin = (int32_t)(q.x >> 16);
+  m.mfb = (int32_t)(q.y & 0xffffu);
+  m.missing = (int32_t)((q.y >> 16) & 15u);
+  m.cat = (int32_t)((q.y >> 20) & 1u);
+  m.offset = (int32_t)((q.y >> 21) & 1u);
+  return m;
 }
 
 __global__ void __launch_bounds__(kThreads) k_part_count(const JobTable jobs, Params p,
@@ -246,15 +272,22 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
                                                            int decide) {
   static_assert(kThreads == kDecideThreads, "the partition CTA runs the split decision");
   __shared__ uint8_t lut[256];
-  __shared__ int32_t sh[32];
   __shared__ int64_t s_off[2];
   __shared__ Decision dec;
+  __shared__ uint2 s_route[kRoutePrefetch];
+  // static: every feature's route descriptor, read while the search finishes
+  const bool prefetched = p.F <= kRoutePrefetch;
+  if (prefetched)
+    for (int f = threadIdx.x; f < p.F; f += kThreads) s_route[f] = route_desc(feats[f]);
   griddep_wait();
+  // the next histogram launch may be scheduled now: its CTAs zero their shared histograms while
+  // this partition runs, and wait for its completion before reading anything it writes
+  griddep_launch();
   const Job& J = jobs.job[blockIdx.z];
   JobState* st = J.st;
-  if (st->stop) return;
   if (decide) {
-    // every CTA decides the split from the search's records; CTA 0 records it
+    // every CTA decides the split from the search's records (a stopped tree included: the stop
+    // flag comes with the records' loads); CTA 0 records it
     decide_split(J, p, feats, blockIdx.x == 0, &dec);
   } else if (threadIdx.x == 0) {
     dec = recorded_decision(st);
@@ -263,11 +296,9 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
   if (dec.stop) return;
   PartRange R;
   part_range(J, p, bins_cm, dec, &R);
-  if ((int)blockIdx.x >= R.active) {  // CTAs past the leaf's rows leave at once
-    griddep_launch();
-    return;
-  }
-  build_route(J, p, dec, feats, lut);
+  if ((int)blockIdx.x >= R.active) return;  // CTAs past the leaf's rows leave at once
+  if (prefetched) build_route_of(J, p, dec, route_feature(s_route[dec.inner]), lut);
+  else build_route(J, p, dec, feats, lut);
   __syncthreads();
   unsigned long long* cnt_left = reinterpret_cast<unsigned long long*>(&st->pcnt[par][0]);
   unsigned long long* cnt_right = reinterpret_cast<unsigned long long*>(&st->pcnt[par][1]);
@@ -345,7 +376,6 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
     }
     __syncthreads();  // s_pre and s_off are rewritten by the next tile
   }
-  griddep_launch();
 }
 
 }  // namespace

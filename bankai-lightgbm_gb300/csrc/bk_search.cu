@@ -136,6 +136,15 @@ __device__ __forceinline__ double int_split_gain(const Params& p, int64_t lg, in
                      parent);
 }
 
+// What one search CTA needs of the job state, loaded in one round of independent loads: the
+// searched leaf's constants and sums (computed by the histogram launch), the smaller leaf's sums
+// (for FixHistogram), and the pool slots of the smaller and larger leaf.
+struct SearchIn {
+  LeafConst C;
+  LeafSum S0;
+  int32_t sslot, lslot;
+};
+
 __device__ void cand_reset(Cand* c, int32_t real, int32_t inner) {
   c->gain = -CUDART_INF;
   c->left_output = c->right_output = 0.0;
@@ -241,6 +250,57 @@ __device__ __forceinline__ Eval eval_float(const Params& p, int d, double ag, do
   return v;
 }
 
+// One side of a queued position, as one lane evaluates it: the side's share of the split gain
+// (GetLeafGain of that side, feature_histogram.rs:148-176 / simd.rs:6-8), and the side's sums,
+// count and output for the SplitInfo (feature_histogram.rs:240-357, :700-830).
+struct SidePart {
+  double gain;   // the side's leaf gain (left + right = the split gain, in that order)
+  double sg, sh;  // the side's sums as the SplitInfo stores them
+  double out;     // the side's output
+  int32_t n;      // the side's count
+};
+
+// Side s (0: left, 1: right) of an integer threshold with left sums (lg, lh): its share of
+// GetSplitGains (feature_histogram.rs:878-925: the hessian gets kEpsilon added) and its SplitInfo
+// sums, count and output exactly as int_split_gain and eval_int compute them.
+__device__ __forceinline__ SidePart int_side(const Params& p, int64_t lg, int64_t lh, int64_t tg, int64_t th,
+                                             double gs, double hs, double cnt_factor, double parent, int s) {
+  const int64_t sg = s == 0 ? lg : tg - lg, sh = s == 0 ? lh : th - lh;
+  const double dg = (double)(int32_t)sg * gs, dh = (double)(uint32_t)sh * hs;
+  const int32_t n = round_int((double)(uint32_t)sh * cnt_factor);
+  SidePart r;
+  r.gain = leaf_gain(p, dg, dh + BK_EPS, n, parent);
+  r.sg = dg;
+  r.sh = dh;
+  r.n = n;
+  r.out = split_output(p, dg, dh, n, parent);
+  return r;
+}
+
+// Side s of a float threshold of direction d with accumulated sums (ag, ah, c): its share of the
+// split gain with the sums split_gains gets (the reverse scan's right side is the accumulated one)
+// and its SplitInfo sums, count and output as eval_float computes them (the right side from the
+// left sums).
+__device__ __forceinline__ SidePart float_side(const Params& p, int d, double ag, double ah, int32_t c, double sum_g,
+                                               double sum_h, int32_t num_data, double parent, int s) {
+  const double slg = d == 0 ? sum_g - ag : ag, slh = d == 0 ? sum_h - ah : ah;
+  const int32_t lc = d == 0 ? num_data - c : c;
+  // the gain's sums: the accumulated side as accumulated, the other as total minus it
+  const double gg = s == 0 ? slg : (d == 0 ? ag : sum_g - ag);
+  const double gh = s == 0 ? slh : (d == 0 ? ah : sum_h - ah);
+  const int32_t gn = s == 0 ? lc : (d == 0 ? c : num_data - c);
+  // the SplitInfo's sums: the right side from the left sums
+  const double og = s == 0 ? slg : sum_g - slg, oh = s == 0 ? slh : sum_h - slh;
+  const int32_t on = s == 0 ? lc : num_data - lc;
+  SidePart r;
+  r.gain = leaf_gain(p, gg, gh, gn, parent);
+  r.sg = og;
+  r.sh = oh - BK_EPS;
+  r.n = on;
+  r.out = split_output(p, og, oh, on, parent);
+  return r;
+}
+
 // One direction's stop / prefilter summary of a warp (published before one barrier).
 struct WarpFilt {
   int32_t lb;      // the warp's first `break` position in scan order (kNoneLo / kNoneHi: none)
@@ -261,7 +321,6 @@ struct SearchSmem {
   int32_t qn[2];
   DirBest pres[2][4];         // per direction and batch lane (below): the arg-max of its batches
   int32_t psplit[2][4];
-  Eval pev[2];                // per direction: the outputs of its only queued position
   int64_t wi[2][kSearchWarps];
   double wd[10][kSearchWarps];
   int32_t wc[3][kSearchWarps];
@@ -426,13 +485,17 @@ __device__ __forceinline__ void queue_push(SearchSmem& sm, int d, bool push, con
   if (push) sm.q[d][base + __popc(bal & ((1u << lane) - 1u))] = e;
 }
 
-// Queue batches of 32 positions: batch k of direction d runs on warp d + 2 (k mod 4), so the
-// first batches of the two directions run on two schedulers and longer queues spread over all
-// four (f64 issue throughput is the bottleneck of this part). One warp: the f64 gains of its
-// batches k0, k0 + 4, ...; their arg-max (highest gain, ties to the earliest position in scan
-// order) and whether any passed, into sm.pres[d][k0] / sm.psplit[d][k0].
-template <typename Gain>
-__device__ __forceinline__ void eval_batches(SearchSmem& sm, int d, int k0, int lane, double mgs, Gain gain_of) {
+// Queue batches of 16 positions, two lanes per position: lane 2k evaluates the left side of
+// position k, lane 2k + 1 its right side. An f64 instruction costs a scheduler the same whether
+// one lane or 32 run it, so splitting a gain's two leaf gains over two lanes halves its
+// instruction chain, and evaluating every queued position's outputs with its gain (in the same
+// instructions) leaves none to evaluate after the arg-max. Batch k of direction d runs on warp
+// d + 2 (k mod 4), so the first batches of the two directions run on two schedulers and longer
+// queues spread over all four. One warp: its batches k0, k0 + 4, ...; their arg-max (highest gain,
+// ties to the earliest position in scan order) with its SplitInfo, and whether any passed, into
+// sm.pres[d][k0] / sm.psplit[d][k0].
+template <typename SideOf>
+__device__ __forceinline__ void eval_batches(SearchSmem& sm, int d, int k0, int lane, double mgs, SideOf side_of) {
   DirBest r;
   r.key = kNoKey;
   r.ev.gain = -CUDART_INF;
@@ -441,36 +504,53 @@ __device__ __forceinline__ void eval_batches(SearchSmem& sm, int d, int k0, int 
   r.c = 0;
   int split = 0;
   const int n = sm.qn[d];
+  const int k = lane >> 1, side = lane & 1;
   auto batch = [&](int b0) {
-    // lanes past the queue's end evaluate its last entry and discard the result: an all-zero
+    // pairs past the queue's end evaluate its last entry and discard the result: an all-zero
     // entry would send the whole warp through the f64 division's slow path (zero dividend, tiny
     // divisor), which costs more than the gain itself on this part
-    const bool have = b0 + lane < n;
-    const QEnt e = sm.q[d][have ? b0 + lane : n - 1];
-    double g = gain_of(e);
+    const bool have = b0 + k < n;
+    const QEnt e = sm.q[d][have ? b0 + k : n - 1];
+    const SidePart sp = side_of(e, side);
+    const double gl = __shfl_sync(FULL, sp.gain, lane & ~1);
+    const double gr = __shfl_sync(FULL, sp.gain, lane | 1);
+    double g = gl + gr;
     if (!have) g = -CUDART_INF;
     const bool passed = have && gain_passes(g, mgs);
     if (__any_sync(FULL, passed)) split = 1;
     const bool elig = passed && !dnan(g) && !is_neg_inf(g);  // NaN never wins
-    const long long k = warp_max64(elig ? dkey(g) : kNoKey);
-    if (k == kNoKey) return;
-    const bool at = elig && dkey(g) == k;
+    const long long key = warp_max64(elig ? dkey(g) : kNoKey);
+    if (key == kNoKey) return;
+    const bool at = elig && dkey(g) == key;
     const int tb = d == 0 ? __reduce_max_sync(FULL, at ? (int)e.t : kNoneLo)
                           : __reduce_min_sync(FULL, at ? (int)e.t : kNoneHi);
-    const int wl = __ffs(__ballot_sync(FULL, at && (int)e.t == tb)) - 1;
-    if (k > r.key || (k == r.key && earlier(d, tb, r.t))) {
-      r.key = k;
+    const int wl = __ffs(__ballot_sync(FULL, at && (int)e.t == tb)) - 1 & ~1;  // the pair's left lane
+    Eval v;
+    v.gain = __shfl_sync(FULL, g, wl);
+    v.lsg = __shfl_sync(FULL, sp.sg, wl);
+    v.lsh = __shfl_sync(FULL, sp.sh, wl);
+    v.lo = __shfl_sync(FULL, sp.out, wl);
+    v.lc = __shfl_sync(FULL, sp.n, wl);
+    v.rsg = __shfl_sync(FULL, sp.sg, wl + 1);
+    v.rsh = __shfl_sync(FULL, sp.sh, wl + 1);
+    v.ro = __shfl_sync(FULL, sp.out, wl + 1);
+    v.rc = __shfl_sync(FULL, sp.n, wl + 1);
+    v.lint = v.rint = 0;
+    const int64_t wa = __shfl_sync(FULL, e.a, wl), wb = __shfl_sync(FULL, e.b, wl);
+    const int32_t wc = __shfl_sync(FULL, e.c, wl);
+    if (key > r.key || (key == r.key && earlier(d, tb, r.t))) {
+      r.key = key;
       r.t = tb;
-      r.ev.gain = __shfl_sync(FULL, g, wl);
-      r.a = __shfl_sync(FULL, e.a, wl);
-      r.b = __shfl_sync(FULL, e.b, wl);
-      r.c = __shfl_sync(FULL, e.c, wl);
+      r.ev = v;
+      r.a = wa;
+      r.b = wb;
+      r.c = wc;
     }
   };
   // the first batch outside the loop: the f64 gain evaluated inside a loop measured about twice
   // as slow as the same code in straight-line form
-  if (32 * k0 < n) batch(32 * k0);
-  for (int b0 = 32 * k0 + 128; b0 < n; b0 += 128) batch(b0);
+  if (16 * k0 < n) batch(16 * k0);
+  for (int b0 = 16 * k0 + 64; b0 < n; b0 += 64) batch(b0);
   if (lane == 0) {
     sm.pres[d][k0] = r;
     sm.psplit[d][k0] = split;
@@ -478,19 +558,13 @@ __device__ __forceinline__ void eval_batches(SearchSmem& sm, int d, int k0, int 
 }
 
 // After the queues are filled (barrier 3): warps 0-7 evaluate the queue batches (warp w takes
-// direction w & 1, batches w >> 1, (w >> 1) + 4, ...); warps 2 / 3, whose direction has a
-// single queued position (so no batch of theirs), evaluate that position's outputs (it is the
-// direction's only possible choice). Barrier 4; then warp 0 combines the batch results of each
-// direction into r / rs.
-template <typename Gain, typename Side>
-__device__ __forceinline__ void eval_queues(SearchSmem& sm, int warp, int lane, double mgs, Gain gain_of,
-                                            Side side_of, DirBest (&r)[2], int (&rs)[2]) {
+// direction w & 1, batches w >> 1, (w >> 1) + 4, ...). Barrier 4; then warp 0 combines the batch
+// results of each direction into r / rs, the winner's SplitInfo included.
+template <typename SideOf>
+__device__ __forceinline__ void eval_queues(SearchSmem& sm, int warp, int lane, double mgs, SideOf side_of,
+                                            DirBest (&r)[2], int (&rs)[2]) {
   const int d = warp & 1, k0 = warp >> 1;
-  if (k0 < 4) eval_batches(sm, d, k0, lane, mgs, gain_of);
-  if ((warp == 2 || warp == 3) && sm.qn[d] == 1) {
-    const Eval v = side_of(sm.q[d][0]);
-    if (lane == 0) sm.pev[d] = v;
-  }
+  if (k0 < 4) eval_batches(sm, d, k0, lane, mgs, side_of);
   __syncthreads();
   if (warp != 0) return;
 #pragma unroll
@@ -542,7 +616,7 @@ __device__ __forceinline__ void finish_cand(const Job& J, const Params& p, const
     b.b = ch == 0 ? r[0].b : r[1].b;
     b.c = ch == 0 ? r[0].c : r[1].c;
     b.t = ch == 0 ? r[0].t : r[1].t;
-    b.ev.gain = ch == 0 ? r[0].ev.gain : r[1].ev.gain;
+    b.ev = ch == 0 ? r[0].ev : r[1].ev;
     const Eval e = eval_of(b, ch);
     const int32_t t = b.t;
     c.threshold = (uint32_t)(ch == 0 ? t - 1 + G.off : t + G.off);
@@ -570,17 +644,17 @@ __device__ __forceinline__ void finish_cand(const Job& J, const Params& p, const
 // Three barriers: the prefix scan (with the most-frequent-bin fix and the forward scan's start
 // folded in), the stop / prefilter summaries, and the arg-max.
 template <bool PLAIN>
-__device__ void search_int(const Job& J, const Params& p, const JobState* st, const DevFeature& m, int side,
+__device__ void search_int(const Job& J, const Params& p, const SearchIn& si, const DevFeature& m, int side,
                            int32_t f, int32_t leaf, SearchSmem& sm) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const LeafConst C = J.lconst[side];
-  const int64_t s_int = J.leaf_sum[st->smaller_leaf].int_sum;
-  const int64_t l_int = side ? J.leaf_sum[leaf].int_sum : s_int;
+  const LeafConst& C = si.C;
+  const int64_t s_int = si.S0.int_sum;
+  const int64_t l_int = side ? C.ls.int_sum : s_int;
   const size_t slot_stride = (size_t)p.T * p.B * TILE;
   const size_t feat_off = (size_t)(f / TILE) * p.B * TILE + (f % TILE);
   int64_t* pool = reinterpret_cast<int64_t*>(J.pool);
-  int64_t* hs = pool + (size_t)st->smaller_slot * slot_stride + feat_off;  // group bin 0 of the feature
-  int64_t* hl = pool + (size_t)(side ? st->larger_slot : st->smaller_slot) * slot_stride + feat_off;
+  int64_t* hs = pool + (size_t)si.sslot * slot_stride + feat_off;  // group bin 0 of the feature
+  int64_t* hl = pool + (size_t)(side ? si.lslot : si.sslot) * slot_stride + feat_off;
   const bool fix = m.mfb > 0;  // offset 0: the slice holds every bin and the most frequent one is empty
   const bool in = t < m.len;
   // the smaller leaf's most-frequent entry is rewritten by its side-0 CTA; side 1 never reads it
@@ -682,8 +756,7 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
     const double gs = C.gs, hsc = C.hs;
     eval_queues(
         sm, warp, lane, C.mgs,
-        [&](const QEnt& e) { return int_split_gain(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, true); },
-        [&](const QEnt& e) { return eval_int(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, 0.0, lane); }, r,
+        [&](const QEnt& e, int s) { return int_side(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, s); }, r,
         rs);
     if (warp != 0) return;
   } else {
@@ -712,9 +785,11 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
   }
   // FindBestThresholdInt's combination of the directions (feature_histogram.rs:700-830)
   finish_cand(J, p, m, side, leaf, f, G, C.mgs, r, rs, lane, [&](const DirBest& b, int d) {
-    if (PLAIN && sm.qn[d] == 1) {  // evaluated by warp 2 + d
-      Eval v = sm.pev[d];
-      v.gain = b.ev.gain;
+    (void)d;
+    if (PLAIN) {  // evaluated with the gain
+      Eval v = b.ev;
+      v.lint = (int64_t)(((uint64_t)b.a << 32) | ((uint64_t)b.b & 0xffffffffull));
+      v.rint = (int64_t)(((uint64_t)(tg - b.a) << 32) | ((uint64_t)(th - b.b) & 0xffffffffull));
       return v;
     }
     return eval_int(p, b.a, b.b, tg, th, C.gs, C.hs, C.cnt_factor, C.parent, b.ev.gain, lane);
@@ -726,17 +801,17 @@ __device__ void search_int(const Job& J, const Params& p, const JobState* st, co
 // cnt_factor); the forward scan uses prefix sums, the reverse scan suffix sums (accumulated from
 // the top bin down, not derived by subtraction).
 template <bool PLAIN>
-__device__ void search_float(const Job& J, const Params& p, const JobState* st, const DevFeature& m, int side,
+__device__ void search_float(const Job& J, const Params& p, const SearchIn& si, const DevFeature& m, int side,
                              int32_t f, int32_t leaf, SearchSmem& sm) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const LeafConst C = J.lconst[side];
-  const LeafSum S0 = J.leaf_sum[st->smaller_leaf];
-  const int32_t num_data = side ? J.leaf_sum[leaf].num_data : S0.num_data;
+  const LeafConst& C = si.C;
+  const LeafSum& S0 = si.S0;
+  const int32_t num_data = side ? C.ls.num_data : S0.num_data;
   const size_t slot_stride = (size_t)p.T * p.B * TILE;
   const size_t feat_off = (size_t)(f / TILE) * p.B * TILE + (f % TILE);
   double2* pool = reinterpret_cast<double2*>(J.pool);
-  double2* hs = pool + (size_t)st->smaller_slot * slot_stride + feat_off;
-  double2* hl = pool + (size_t)(side ? st->larger_slot : st->smaller_slot) * slot_stride + feat_off;
+  double2* hs = pool + (size_t)si.sslot * slot_stride + feat_off;
+  double2* hl = pool + (size_t)(side ? si.lslot : si.sslot) * slot_stride + feat_off;
   const double2 zero = make_double2(0.0, 0.0);
   const bool fix = m.mfb > 0;
   const bool in = t < m.len;
@@ -904,10 +979,10 @@ __device__ void search_float(const Job& J, const Params& p, const JobState* st, 
     }
     __syncthreads();
     eval_queues(
-        sm, warp, lane, C.mgs, gain_of,
-        [&](const QEnt& e) {
-          return eval_float(p, e.d, __longlong_as_double(e.a), __longlong_as_double(e.b), e.c, sum_g, sum_h,
-                            num_data, C.parent, 0.0, lane);
+        sm, warp, lane, C.mgs,
+        [&](const QEnt& e, int s) {
+          return float_side(p, e.d, __longlong_as_double(e.a), __longlong_as_double(e.b), e.c, sum_g, sum_h,
+                            num_data, C.parent, s);
         },
         r, rs);
     if (warp != 0) return;
@@ -935,11 +1010,7 @@ __device__ void search_float(const Job& J, const Params& p, const JobState* st, 
   }
   // FindBestThreshold's combination of the directions (feature_histogram.rs:240-357)
   finish_cand(J, p, m, side, leaf, f, G, C.mgs, r, rs, lane, [&](const DirBest& b, int d) {
-    if (PLAIN && sm.qn[d] == 1) {  // evaluated by warp 2 + d
-      Eval v = sm.pev[d];
-      v.gain = b.ev.gain;
-      return v;
-    }
+    if (PLAIN) return b.ev;  // evaluated with the gain
     return eval_float(p, d, __longlong_as_double(b.a), __longlong_as_double(b.b), b.c, sum_g, sum_h, num_data,
                       C.parent, b.ev.gain, lane);
   });
@@ -1011,15 +1082,15 @@ __device__ __forceinline__ int32_t cat_block_or(int32_t v, int32_t* w, int lane,
 }
 
 template <bool QUANT>
-__device__ void search_cat(const Job& J, const Params& p, const JobState* st, const DevFeature& m, int side,
+__device__ void search_cat(const Job& J, const Params& p, const SearchIn& si, const DevFeature& m, int side,
                            int32_t f, int32_t leaf, SearchSmem& sm) {
   using V = typename std::conditional<QUANT, int64_t, double>::type;
   static_assert(sizeof(CatSmem<V>) <= sizeof(SearchSmem), "the categorical search fits the search's shared memory");
   CatSmem<V>& cs = *reinterpret_cast<CatSmem<V>*>(&sm);
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
-  const LeafConst C = J.lconst[side];
-  const LeafSum S0 = J.leaf_sum[st->smaller_leaf];
-  const LeafSum SL = J.leaf_sum[leaf];
+  const LeafConst& C = si.C;
+  const LeafSum& S0 = si.S0;
+  const LeafSum& SL = C.ls;
   const int32_t num_data = SL.num_data;
   const size_t slot_stride = (size_t)p.T * p.B * TILE;
   const size_t feat_off = (size_t)(f / TILE) * p.B * TILE + (f % TILE);
@@ -1029,8 +1100,8 @@ __device__ void search_cat(const Job& J, const Params& p, const JobState* st, co
   //    1407-1437, 2205-2238), written back exactly as the numerical searches write it --
   if (QUANT) {
     int64_t* pool = reinterpret_cast<int64_t*>(J.pool);
-    int64_t* hs = pool + (size_t)st->smaller_slot * slot_stride + feat_off;
-    int64_t* hl = pool + (size_t)(side ? st->larger_slot : st->smaller_slot) * slot_stride + feat_off;
+    int64_t* hs = pool + (size_t)si.sslot * slot_stride + feat_off;
+    int64_t* hl = pool + (size_t)(side ? si.lslot : si.sslot) * slot_stride + feat_off;
     const int64_t sv = (in && !(fix && t == m.mfb)) ? hs[(size_t)(t + 1) * TILE] : 0;
     const int64_t lv = (side && in) ? hl[(size_t)(t + 1) * TILE] : 0;
     int64_t v = side ? lv - sv : sv;
@@ -1053,8 +1124,8 @@ __device__ void search_cat(const Job& J, const Params& p, const JobState* st, co
     cs.cnt[t] = in ? round_int((double)unpack_h(v) * C.cnt_factor) : 0;
   } else {
     double2* pool = reinterpret_cast<double2*>(J.pool);
-    double2* hs = pool + (size_t)st->smaller_slot * slot_stride + feat_off;
-    double2* hl = pool + (size_t)(side ? st->larger_slot : st->smaller_slot) * slot_stride + feat_off;
+    double2* hs = pool + (size_t)si.sslot * slot_stride + feat_off;
+    double2* hl = pool + (size_t)(side ? si.lslot : si.sslot) * slot_stride + feat_off;
     const double2 zero = make_double2(0.0, 0.0);
     double2 sv = (in && !(fix && t == m.mfb)) ? hs[(size_t)(t + 1) * TILE] : zero;
     const double2 lv = (side && in) ? hl[(size_t)(t + 1) * TILE] : zero;
@@ -1320,6 +1391,9 @@ __global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, 
   const int f = (int)(blockIdx.x >> 1);
   const DevFeature m = feats[f];  // static: loaded while the histogram launch finishes
   griddep_wait();
+  // the partition may be scheduled now: its CTAs read their static data while this search runs,
+  // and wait for its completion before reading anything it writes
+  griddep_launch();
   const Job& J = jobs.job[blockIdx.z];
   JobState* st = J.st;
   if (clear_par >= 0 && blockIdx.x == 0 && threadIdx.x < 2) {
@@ -1327,17 +1401,24 @@ __global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, 
     // histogram launch before this one, has finished
     st->pcnt[clear_par][threadIdx.x] = 0;
   }
-  if (st->stop) return;  // uniform over the grid
+  // one round of independent loads: the state, the feature's flag and both leaves' constants
+  const int32_t stop = st->stop, do_search = st->do_search;
   const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
-  if (st->do_search && J.used[f] && leaf >= 0) {  // uniform over the CTA
+  const uint8_t used = J.used[f];
+  SearchIn si;
+  si.sslot = st->smaller_slot;
+  si.lslot = st->larger_slot;
+  si.C = J.lconst[side];
+  si.S0 = side ? J.lconst[0].ls : si.C.ls;
+  if (stop) return;  // uniform over the grid
+  if (do_search && used && leaf >= 0) {  // uniform over the CTA
     if (m.cat)
-      search_cat<QUANT>(J, p, st, m, side, f, leaf, sm);
+      search_cat<QUANT>(J, p, si, m, side, f, leaf, sm);
     else if (QUANT)
-      search_int<PLAIN>(J, p, st, m, side, f, leaf, sm);
+      search_int<PLAIN>(J, p, si, m, side, f, leaf, sm);
     else
-      search_float<PLAIN>(J, p, st, m, side, f, leaf, sm);
+      search_float<PLAIN>(J, p, si, m, side, f, leaf, sm);
   }
-  griddep_launch();  // only the last CTA's fold (if any) is left: the partition may be scheduled
   if (!decide) return;
   __syncthreads();
   if (threadIdx.x == 0) {

@@ -67,6 +67,8 @@ _GPU_SIGNATURES = [
     ("bk_learner_set_loop_mode", _i32, [_P, _i32]),
     ("bk_learner_set_launch_overlap", _i32, [_P, _i32]),
     ("bk_learner_reset_constant_hessian", _i32, [_P, _i32]),
+    ("bk_learner_histogram_cache_capacity", _i32, [_P, _P]),
+    ("bk_learner_reset_histogram_pool_config", _i32, [_P]),
     ("bk_learner_set_feature_mask", _i32, [_P, _P]),
     ("bk_learner_set_bynode", _i32, [_P, _f64, _i32, _u32]),
     ("bk_learner_bynode_state", _i32, [_P, _P]),
@@ -81,6 +83,7 @@ _GPU_SIGNATURES = [
     ("bk_learner_gradient_buffers", _i32, [_P, _P, _P]),
     ("bk_learner_objective_gradients", _i32, [_P, _i32, _P, _P, _f64]),
     ("bk_learner_objective_loss", _i32, [_P, _i32, _P, _P, _P]),
+    ("bk_learner_set_objective_weights", _i32, [_P, _P, _f64, _f64]),
     ("bk_learner_predict_add", _i32, [_P, _i32, _P, _P, _P, _P, _P, _P, _P, _i64, _P]),
     ("bk_learner_leaf_histogram", _i32, [_P, _i32, _i32, _P, _P]),
     ("bk_learner_stream", _i32, [_P, _P]),

@@ -146,6 +146,24 @@ class GpuTreeLearner:
         _lib.check(self.lib.bk_learner_objective_gradients(self.h, int(kind), int(score_ptr), int(label_ptr),
                                                            float(sigmoid)), "bk_learner_objective_gradients")
 
+    def histogram_cache_capacity(self):
+        """Histogram slots the learner keeps (a full pool: num_leaves)."""
+        out = ctypes.c_int64()
+        _lib.check(self.lib.bk_learner_histogram_cache_capacity(self.h, ctypes.byref(out)),
+                   "bk_learner_histogram_cache_capacity")
+        return out.value
+
+    def reset_histogram_pool_config(self):
+        """The budget-only reset of SerialTreeLearner::reset_histogram_pool_config: nothing changes."""
+        _lib.check(self.lib.bk_learner_reset_histogram_pool_config(self.h), "bk_learner_reset_histogram_pool_config")
+
+    def set_objective_weights(self, weights_ptr=0, neg_label_weight=1.0, pos_label_weight=1.0):
+        """Row weights (a device f32 [num_data] pointer, 0 for none) and the binary label weights
+        used by objective_gradients from now on (bk_learner_set_objective_weights)."""
+        _lib.check(self.lib.bk_learner_set_objective_weights(self.h, int(weights_ptr) or None, float(neg_label_weight),
+                                                             float(pos_label_weight)),
+                   "bk_learner_set_objective_weights")
+
     def objective_loss(self, kind, score_ptr, label_ptr):
         out = ctypes.c_double()
         _lib.check(self.lib.bk_learner_objective_loss(self.h, int(kind), int(score_ptr), int(label_ptr),

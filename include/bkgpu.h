@@ -197,6 +197,18 @@ int bk_learner_set_launch_shape(bk_learner* learner, const int32_t* shape);
 /* Replaces SerialTreeLearner::reset_constant_hessian (serial.rs:279). */
 int bk_learner_reset_constant_hessian(bk_learner* learner, int32_t value);
 
+/* Replaces SerialTreeLearner::histogram_cache_capacity (serial.rs:250-252): the histogram slots
+ * the learner keeps, into *capacity (host). This learner always keeps a full pool, one slot per
+ * leaf (num_leaves), whatever histogram_pool_size says; the pool size never changes a result. */
+int bk_learner_histogram_cache_capacity(bk_learner* learner, int64_t* capacity);
+
+/* Replaces SerialTreeLearner::reset_histogram_pool_config (serial.rs:254-264), the Trainer's
+ * budget-only reset (boosting/train.rs:997-1003): the learner keeps its rows, its by-node
+ * sampler's state and its pool (always full here), so the call changes nothing and only checks the
+ * handle. The by-tree sample that the reference redraws there is the host's (it passes the mask
+ * with bk_learner_set_feature_mask). */
+int bk_learner_reset_histogram_pool_config(bk_learner* learner);
+
 /* Timing of the last train call, from CUDA events on the learner's stream: total device time
  * and the histogram kernels' time (ms), plus the algorithmic bytes the histogram kernels moved. */
 int bk_learner_last_timing(bk_learner* learner, double* total_ms, double* hist_ms, double* hist_bytes);
@@ -227,6 +239,17 @@ int bk_learner_gradient_buffers(bk_learner* learner, float** gradients, float** 
  * Enqueued on the learner's stream, ordered before its next call. */
 int bk_learner_objective_gradients(bk_learner* learner, int32_t kind, const double* score, const float* label,
                                    double sigmoid);
+
+/* Weights of the device objectives (bk_learner_objective_gradients), kept until changed:
+ * weights: device f32 [num_data] row weights (Metadata::weights), or NULL for none; read by every
+ * later gradient call, so it must stay valid while the learner uses it (the caller owns it).
+ * neg_label_weight / pos_label_weight: the binary objective's label weights of the negative and
+ * positive class (BinaryLogloss::label_weights, objective/binary.rs:33-52, which the host derives
+ * from is_unbalance or scale_pos_weight); 1 and 1 for neither. Operation order of the weighted
+ * gradients: objective/regression.rs:321-329 (L2), binary.rs:71-90, multiclass.rs:68-90. The loss
+ * of bk_learner_objective_loss stays unweighted. */
+int bk_learner_set_objective_weights(bk_learner* learner, const float* weights, double neg_label_weight,
+                                     double pos_label_weight);
 
 /* Mean training loss (L2: squared error; binary / multiclass: log loss) of a device score,
  * returned in *out (host). */

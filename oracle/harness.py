@@ -1079,3 +1079,36 @@ def gain_errors(rec_gpu, rec_orc):
     rel = np.asarray(rel)
     return {"splits_compared": int(rel.size), "max_rel": float(rel.max()) if rel.size else 0.0,
             "mean_rel": float(rel.mean()) if rel.size else 0.0, "near_ties": near_ties}
+
+
+def split_match(rec_gpu, rec_orc):
+    """Whole-tree comparison of two float trees grown from the same gradients, past near-tie
+    divergences: every split node is keyed by its path from the root (the (feature, threshold,
+    default_left, side) of each ancestor split), which fixes the node's rows. Nodes whose key and
+    split agree in both trees are matched (their gains compared); the rest are divergences, listed
+    with both trees' choices. A near tie changes the subtree under the node where it happens (and,
+    through the leaf budget, which leaves get split at all), not the splits elsewhere."""
+    def nodes(rec):
+        path = {0: ()}
+        out = {}
+        for i, r in enumerate(rec):
+            leaf, right = int(r["leaf"]), int(r["right_leaf"])
+            key = path[leaf]
+            sp = (int(r["real_feature"]), int(r["threshold"]), int(r["default_left"]))
+            out[key] = (sp, float(r["gain"]), i)
+            path[leaf] = key + (sp + (0,),)
+            path[right] = key + (sp + (1,),)
+        return out
+    a, b = nodes(rec_gpu), nodes(rec_orc)
+    rel, diverged = [], []
+    for key in sorted(set(a) | set(b), key=lambda k: (len(k), k)):
+        x, y = a.get(key), b.get(key)
+        if x is not None and y is not None and x[0] == y[0]:
+            rel.append(abs(x[1] - y[1]) / max(abs(y[1]), 1e-300))
+        else:
+            diverged.append({"depth": len(key), "gpu": None if x is None else [*x[0], x[1], x[2]],
+                             "oracle": None if y is None else [*y[0], y[1], y[2]]})
+    rel = np.asarray(rel)
+    return {"matched": int(rel.size), "diverged": len(diverged), "splits": (len(rec_gpu), len(rec_orc)),
+            "max_rel": float(rel.max()) if rel.size else 0.0, "mean_rel": float(rel.mean()) if rel.size else 0.0,
+            "divergences": diverged[:20]}

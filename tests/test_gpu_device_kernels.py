@@ -3,8 +3,10 @@
 * objective gradients (bk_learner_objective_gradients): L2 (objective/regression.rs:240-248)
   bit for bit; binary (objective/binary.rs:71-90) and softmax (objective/multiclass.rs:68-90)
   within one f32 ulp (CUDA's exp against the host's, in the last f64 bit), in the reference's
-  operation order; a multiclass label outside [0, K) fails the next train call and the loss call
-  instead of indexing the scores;
+  operation order; with row weights (regression.rs:321-329 for L2, bit for bit) and the binary
+  label weights of is_unbalance / scale_pos_weight (binary.rs:33-52) against the oracle harness's
+  weighted objectives; a multiclass label outside [0, K) fails the next train call and the loss
+  call instead of indexing the scores;
 * held-out prediction (bk_learner_predict_add, the replay of serial.rs:2009-2041) on upstream's own
   models and test rows (tests/fixtures/predict: binary, NaN, zero as missing, L2, 3-class): every
   row reaches upstream's leaf in every tree (pred_leaf.npy) and the raw scores, the leaf values
@@ -123,6 +125,66 @@ def test_objective_gradients_on_device(oracle, kind):
         go = (score[:m] - label[:m].astype(np.float64)).astype(np.float32)[None, :]
         ho = np.ones((1, m), np.float32)
     assert int(_ulps(go, gw[:, :m]).max()) <= 1 and int(_ulps(ho, hw[:, :m]).max()) <= 1
+    gpu.close()
+
+
+@pytest.mark.parametrize("kind,weighted,is_unbalance,scale_pos", [
+    (0, True, False, 1.0), (1, True, False, 1.0), (1, False, True, 1.0), (1, False, False, 2.5),
+    (1, True, True, 1.0), (2, True, False, 1.0)])
+def test_weighted_objective_gradients_on_device(oracle, kind, weighted, is_unbalance, scale_pos):
+    """Row weights and binary label weights (bk_learner_set_objective_weights) against the oracle
+    harness's weighted objectives: L2 bit for bit, binary / softmax within one f32 ulp."""
+    import torch
+    from lgbm_gb300 import BinnedDataset, GpuTreeLearner, LearnerConfig
+    n = 4000
+    K = 4 if kind == 2 else 1
+    rng = np.random.default_rng(40 + kind)
+    score = rng.normal(0.0, 1.5, (K, n))
+    if kind == 0:
+        label = rng.normal(0.0, 2.0, n).astype(np.float32)
+    elif kind == 1:
+        label = (rng.random(n) < 0.3).astype(np.float32)
+    else:
+        label = rng.integers(0, K, n).astype(np.float32)
+    w = rng.uniform(0.2, 3.0, n).astype(np.float32) if weighted else None
+    if kind == 0:
+        obj = oracle.L2Objective(label, weights=w)
+    elif kind == 1:
+        obj = oracle.BinaryObjective(label, weights=w, is_unbalance=is_unbalance, scale_pos_weight=scale_pos)
+    else:
+        obj = oracle.SoftmaxObjective(label, K, weights=w)
+    go, ho = obj.gradients(score if kind == 2 else score[0])
+    go, ho = np.asarray(go).reshape(K, n), np.asarray(ho).reshape(K, n)
+    ds = BinnedDataset.from_dense(rng.standard_normal((n, 3)))
+    gpu = GpuTreeLearner(ds, LearnerConfig(num_leaves=4), num_jobs=K)
+    sc = torch.from_numpy(np.ascontiguousarray(score.reshape(-1))).cuda()
+    lab = torch.from_numpy(label).cuda()
+    wd = torch.from_numpy(w).cuda() if weighted else None
+    lw = obj.label_weights if kind == 1 else [1.0, 1.0]
+    torch.cuda.synchronize()
+    gpu.set_objective_weights(wd.data_ptr() if weighted else 0, lw[0], lw[1])
+    gpu.objective_gradients(kind, sc.data_ptr(), lab.data_ptr())
+    gp, hp = gpu.gradient_buffers()
+    stream = torch.cuda.ExternalStream(gpu.stream())
+    with torch.cuda.stream(stream):
+        g = _view(gp, K * n).clone()
+        h = _view(hp, K * n).clone()
+    stream.synchronize()
+    g, h = g.cpu().numpy().reshape(K, n), h.cpu().numpy().reshape(K, n)
+    if kind == 0:
+        assert np.array_equal(g, go) and np.array_equal(h, ho)
+    else:
+        assert int(_ulps(g, go).max()) <= 1 and int(_ulps(h, ho).max()) <= 1
+    # weights off again: the unweighted formulas
+    gpu.set_objective_weights(0, 1.0, 1.0)
+    gpu.objective_gradients(kind, sc.data_ptr(), lab.data_ptr())
+    with torch.cuda.stream(stream):
+        g2 = _view(gp, K * n).clone()
+    stream.synchronize()
+    gu, _ = _grads_host(kind, score.reshape(-1), label, K)
+    assert int(_ulps(g2.cpu().numpy().reshape(K, n), gu.reshape(K, n)).max()) <= 1
+    with pytest.raises(RuntimeError):
+        gpu.set_objective_weights(0, 0.0, 1.0)
     gpu.close()
 
 

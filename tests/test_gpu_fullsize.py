@@ -61,16 +61,14 @@ def test_float_tree_matches_at_full_size(workload):
     h = np.ones_like(g)
     orc, gpu = _learners(ds, 0, threads)
     ro, rg = orc.train(g, h), gpu.train(g, h)
-    a, b = ro[0], rg[0]
-    diverged = -1
-    for i in range(min(len(a), len(b))):
-        if any(a[i][k] != b[i][k] for k in ("leaf", "real_feature", "threshold", "default_left", "left_count",
-                                             "right_count")):
-            diverged = i
-            break
-        ga, gb = float(a[i]["gain"]), float(b[i]["gain"])
-        assert abs(ga - gb) <= 1e-6 * max(abs(ga), 1e-300), "split %d gain %r vs %r" % (i, ga, gb)
-    print("float near-tie divergence at split:", diverged)
-    if diverged < 0:
-        assert len(a) == len(b)
+    # the whole tree, past any near tie: nodes keyed by their root path, gains of matched nodes
+    # within 1e-6 relative, divergences counted, listed and bounded
+    import harness
+    m = harness.split_match(rg[0], ro[0])
+    print("float tree vs oracle: %d matched, %d diverged, max rel gain error %.3g, mean %.3g"
+          % (m["matched"], m["diverged"], m["max_rel"], m["mean_rel"]))
+    for d in m["divergences"]:
+        print("  divergence:", d)
+    assert m["max_rel"] <= 1e-6, m
+    assert m["matched"] >= 0.8 * max(len(ro[0]), len(rg[0])), m
     gpu.close()

@@ -473,3 +473,22 @@ def test_packed_bin_tiles(quant):
                     assert e["max_rel"] <= 1e-6, e
                 gg = (gg * 0.9).astype(np.float32)
             gpu.close()
+
+
+def test_pool_capacity_and_budget_reset():
+    """histogram_cache_capacity reports the full pool (one slot per leaf); the budget-only reset of
+    reset_histogram_pool_config (serial.rs:250-264) changes nothing: the next trees still equal
+    the oracle's bit for bit."""
+    cfg = dict(num_leaves=23, use_quantized_grad=1, stochastic_rounding=1, seed=4, num_threads=2)
+    ds, z = _dataset(12000, 18, seed=51)
+    g, h, const = _grads(z, "binary", seed=52)
+    orc, gpu, _ = _learners(ds, const, **cfg)
+    assert gpu.histogram_cache_capacity() == 23
+    for it in range(2):
+        ro, rg = orc.train(g, h), gpu.train(g, h)
+        _assert_records_equal(ro[0], rg[0])
+        assert np.array_equal(ro[1], rg[1])
+        gpu.reset_histogram_pool_config()
+        assert gpu.histogram_cache_capacity() == 23
+        g = (g * 0.9).astype(np.float32)
+    gpu.close()
