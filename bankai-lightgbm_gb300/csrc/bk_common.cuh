@@ -2,7 +2,8 @@
 //
 // Layout in HBM (one learner, `n` rows, `F` inner features, `T = ceil(F / 32)` feature tiles,
 // `B` = the largest stored-bin count of any feature, rounded up to a multiple of 8):
-//   bins_rt   uint8 [n][Σ w_t]   row-tiled stored bins: one w_t-byte run per (row, tile) — 32 bytes
+//   bins_rt   uint8 [n][S]       (S = Σ w_t rounded up to a multiple of 64: rows on 64-byte bursts)
+//                                row-tiled stored bins: one w_t-byte run per (row, tile) — 32 bytes
 //                                for a tile of 8-bit bins, 16 for a tile of 4-bit bins (every
 //                                feature of the tile has at most 16 group bins) — so a gathered
 //                                row of a sparse leaf is one sector read per tile, and the T
@@ -88,6 +89,8 @@ struct Params {
   int32_t renew, part_grid, pdl;  // pdl: launch the grow-loop kernels with programmatic dependence
   int32_t hist_min_rows;          // fewest rows a histogram CTA takes (launch shape, autotuned)
   int32_t rt_stride;              // bytes per row of bins_rt: the widths of all tiles
+  int32_t search_narrow;          // 1: every feature is numerical with at most 63 searched bins (the
+                                  //    plain single-pass search runs in 64-thread CTAs)
   const TileGeom* tiles;          // [T] the tiles' layouts
   int64_t n;
   // CatParams of the categorical search (feature_histogram.rs:1146-1163)

@@ -17,6 +17,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <memory>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -168,11 +169,20 @@ struct bk_learner {
   ObjectiveWeights obj_w;          // row / label weights of the device objectives (caller-owned rows)
   int32_t* h_bad_label = nullptr;  // pinned copy, read by the train call that follows the gradients
   double* d_leaf_vals_in = nullptr;
-  int32_t* d_tree = nullptr;     // one tree's node arrays for prediction (5 x (num_leaves - 1))
+  int32_t* d_tree = nullptr;     // one tree's node arrays for prediction (13 x (num_leaves - 1))
   double* d_tree_values = nullptr;
   std::vector<int32_t> h_tree;
   // graph
   cudaGraphExec_t graph_exec = nullptr;
+  uint64_t graph_gen = 0;  // bumped whenever the captured kernels' parameters change
+
+  // The captured grow loop no longer matches the learner's parameters: captured anew when next
+  // needed (here and in every learner group that holds this learner).
+  void drop_graph() {
+    if (graph_exec) cudaGraphExecDestroy(graph_exec);
+    graph_exec = nullptr;
+    ++graph_gen;
+  }
   // timing
   cudaEvent_t ev_start = nullptr, ev_end = nullptr;
   std::vector<cudaEvent_t> hist_events;
@@ -210,10 +220,7 @@ struct bk_learner {
     hl.blocks_per_tile = (int)std::max<int64_t>(
         1, std::min<int64_t>(hist_ctas_per_tile, (n + p.hist_min_rows - 1) / p.hist_min_rows));
     p.part_grid = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(part_grid, kMaxPartGrid), (n + 255) / 256));
-    if (graph_exec) {
-      cudaGraphExecDestroy(graph_exec);
-      graph_exec = nullptr;
-    }
+    drop_graph();
   }
 
   void shape_of(int32_t* out) const {
@@ -426,6 +433,11 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
         }
     }
     p.B = (maxb + 7) / 8 * 8;
+    // the plain single-pass search runs in 64-thread CTAs when every feature is numerical and its
+    // searched slice has at most 63 bins (thread 63 holds the forward scan's position -1)
+    p.search_narrow = 1;
+    for (const DevFeature& d : L->h_feat)
+      if (d.cat || d.len > 63) p.search_narrow = 0;
     // the feature tiles' stored-bin layouts: 16-byte runs of 4-bit bins for tiles whose features
     // all have at most 16 group bins, 8-bit runs otherwise (16 bytes for a last tile of at most
     // 16 features, else 32); each tile's shared histogram holds its largest feature's group bins
@@ -444,7 +456,10 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
         off += tile_width(g);
         L->h_tiles.push_back(g);
       }
-      p.rt_stride = (int32_t)off;
+      // a row of bins_rt starts on a 64-byte boundary: a gathered row then costs the fewest 64-byte
+      // DRAM bursts (112 bytes at a 112-byte stride touch three bursts in three rows of four, two
+      // at a 128-byte stride)
+      p.rt_stride = (int32_t)((off + 63) / 64 * 64);
     }
     // launch shapes: histogram CTAs of 1024 threads, one per SM, split evenly over the feature
     // tiles, each taking at least 256 rows; two partition CTAs per SM; no more CTAs than the
@@ -582,7 +597,7 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
     L->d_bad_label = L->dalloc<int32_t>(1);
     CK(cudaMemset(L->d_bad_label, 0, sizeof(int32_t)));
     L->d_leaf_vals_in = L->dalloc<double>((size_t)Lv * K);
-    L->d_tree = L->dalloc<int32_t>(5 * (size_t)Lv);
+    L->d_tree = L->dalloc<int32_t>(13 * (size_t)Lv);
     L->d_tree_values = L->dalloc<double>(Lv);
     CK(cudaEventCreate(&L->ev_start));
     CK(cudaEventCreate(&L->ev_end));
@@ -647,10 +662,7 @@ bool train_enqueue(bk_learner* L, const float* gradients, const float* hessians,
     for (cudaEvent_t e : L->hist_events) cudaEventDestroy(e);
     L->hist_events.assign(4 * (Lv - 1), nullptr);
     for (auto& e : L->hist_events) CK(cudaEventCreate(&e));
-    if (L->graph_exec) {
-      cudaGraphExecDestroy(L->graph_exec);
-      L->graph_exec = nullptr;
-    }
+    L->drop_graph();
   }
   if (L->loop_mode == 1) L->run_graph();
   else L->run_stepwise();
@@ -684,17 +696,19 @@ bool labels_ok(bk_learner* L) {
 
 // The synchronous half: waits for the learner's stream, reads the timings and fills the outputs.
 void train_finish(bk_learner* L, bk_split* splits, double* leaf_values, double* root_outputs,
-                  int32_t* num_leaves_out) {
+                  int32_t* num_leaves_out, bool timed = true) {
   const Params& p = L->p;
   const size_t K = (size_t)L->K;
   const int Lv = p.num_leaves;
-  CK(cudaStreamSynchronize(L->stream));
-  CK(cudaGetLastError());
+  if (timed) {
+    CK(cudaStreamSynchronize(L->stream));
+    CK(cudaGetLastError());
+  }
   float ms = 0.f;
-  CK(cudaEventElapsedTime(&ms, L->ev_start, L->ev_end));
+  if (timed) CK(cudaEventElapsedTime(&ms, L->ev_start, L->ev_end));
   L->last_total_ms = ms;
   L->last_hist_ms = L->last_search_ms = L->last_part_ms = 0.0;
-  if (L->timing) {
+  if (L->timing && timed) {
     // the phases of the steps that ran (a finished tree's remaining steps return early but are
     // still timed: they are part of the replayed graph); a stepwise loop that stopped early
     // leaves later events unrecorded, which the elapsed-time calls report and skip
@@ -922,6 +936,343 @@ int bk_learners_train_batch(bk_learner* const* learners, int32_t count, const fl
   return 0;
 }
 
+
+// ---- learner groups: many learners' iterations captured into one CUDA graph ----
+
+namespace {
+
+// One learner's share of a group iteration, issued into the group's capture on the learner's own
+// stream: what train_enqueue issues for an iteration on device gradients (no bagging), the grow
+// loop issued directly (it cannot launch its own graph inside another capture), and the score
+// update and result readback.
+void group_enqueue(bk_learner* L, const float* gradients, const float* hessians, double shrinkage, double* score) {
+  const Params& p = L->p;
+  const size_t n = (size_t)p.n, K = (size_t)L->K;
+  const int Lv = p.num_leaves;
+  if (gradients != L->d_g)
+    CK(cudaMemcpyAsync(L->d_g, gradients, n * K * sizeof(float), cudaMemcpyDeviceToDevice, L->stream));
+  if (hessians != L->d_h)
+    CK(cudaMemcpyAsync(L->d_h, hessians, n * K * sizeof(float), cudaMemcpyDeviceToDevice, L->stream));
+  for (size_t j = 0; j < K; ++j) {
+    JobState* st = L->jobs[j].st;
+    CK(cudaMemcpyAsync(&st->use_rows, &L->h_state[j].use_rows, sizeof(int32_t), cudaMemcpyHostToDevice, L->stream));
+    CK(cudaMemcpyAsync(&st->root_count, &L->h_state[j].root_count, sizeof(int64_t), cudaMemcpyHostToDevice,
+                       L->stream));
+    CK(cudaMemcpyAsync(&st->hist_rows_direct, &L->h_state[j].hist_rows_direct, 3 * sizeof(int64_t),
+                       cudaMemcpyHostToDevice, L->stream));
+  }
+  L->capturing = true;
+  L->tree_prologue();
+  for (int it = 0; it < Lv - 1; ++it) {
+    L->step_a(it);
+    L->step_b(it);
+  }
+  L->tree_epilogue();
+  L->capturing = false;
+  if (score) {
+    launch_add_score_own(L->d_jobs, L->K, p, shrinkage, score, L->stream);
+    CK(cudaGetLastError());
+  }
+  for (size_t j = 0; j < K; ++j) {
+    const Job& J = L->jobs[j];
+    CK(cudaMemcpyAsync(L->h_records + j * Lv, J.records, sizeof(bk_split) * (Lv - 1), cudaMemcpyDeviceToHost,
+                       L->stream));
+    CK(cudaMemcpyAsync(L->h_leaf_values + j * Lv, J.leaf_value, sizeof(double) * Lv, cudaMemcpyDeviceToHost,
+                       L->stream));
+    CK(cudaMemcpyAsync(&L->h_state[j], J.st, offsetof(JobState, mt), cudaMemcpyDeviceToHost, L->stream));
+  }
+  CK(cudaMemcpyAsync(L->h_bad_label, L->d_bad_label, sizeof(int32_t), cudaMemcpyDeviceToHost, L->stream));
+  CK(cudaMemsetAsync(L->d_bad_label, 0, sizeof(int32_t), L->stream));
+}
+
+}  // namespace
+
+struct bk_learner_group {
+  std::vector<bk_learner*> learners;
+  std::vector<uint64_t> gens;     // each learner's graph generation when captured
+  std::vector<const float*> g, h;  // the captured inputs
+  std::vector<double*> scores;
+  double shrinkage = 0.0;
+  int device = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t fork = nullptr;
+  std::vector<cudaEvent_t> joins;
+  cudaGraphExec_t exec = nullptr;
+
+  ~bk_learner_group() {
+    if (exec) cudaGraphExecDestroy(exec);
+    for (cudaEvent_t e : joins) cudaEventDestroy(e);
+    if (fork) cudaEventDestroy(fork);
+    if (stream) cudaStreamDestroy(stream);
+  }
+
+  bool current(const float* const* gg, const float* const* hh, double shr, double* const* sc) const {
+    if (!exec || shr != shrinkage) return false;
+    for (size_t i = 0; i < learners.size(); ++i)
+      if (gens[i] != learners[i]->graph_gen || g[i] != gg[i] || h[i] != hh[i] || scores[i] != (sc ? sc[i] : nullptr))
+        return false;
+    return true;
+  }
+
+  // Captures one iteration of every learner: a fork event on the group's stream, each learner's
+  // stream joining the capture behind it, every learner's work on its own stream (independent
+  // branches of one graph), and a join of every branch back into the group's stream.
+  void capture(const float* const* gg, const float* const* hh, double shr, double* const* sc) {
+    if (exec) {
+      cudaGraphExecDestroy(exec);
+      exec = nullptr;
+    }
+    cudaGraph_t graph = nullptr;
+    CK(cudaStreamBeginCapture(stream, cudaStreamCaptureModeThreadLocal));
+    try {
+      CK(cudaEventRecord(fork, stream));
+      for (size_t i = 0; i < learners.size(); ++i) {
+        bk_learner* L = learners[i];
+        CK(cudaStreamWaitEvent(L->stream, fork, 0));
+        group_enqueue(L, gg[i], hh[i], shr, sc ? sc[i] : nullptr);
+        CK(cudaEventRecord(joins[i], L->stream));
+        CK(cudaStreamWaitEvent(stream, joins[i], 0));
+      }
+    } catch (...) {
+      for (bk_learner* L : learners) L->capturing = false;
+      cudaStreamEndCapture(stream, &graph);
+      if (graph) cudaGraphDestroy(graph);
+      throw;
+    }
+    CK(cudaStreamEndCapture(stream, &graph));
+    cudaError_t e = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    CK(e);
+    for (size_t i = 0; i < learners.size(); ++i) {
+      gens[i] = learners[i]->graph_gen;
+      g[i] = gg[i];
+      h[i] = hh[i];
+      scores[i] = sc ? sc[i] : nullptr;
+    }
+    shrinkage = shr;
+  }
+};
+
+int bk_learner_group_create(bk_learner* const* learners, int32_t count, bk_learner_group** out) {
+  if (!learners || count <= 0 || !out) {
+    set_error("bk_learner_group_create: invalid arguments");
+    return -1;
+  }
+  *out = nullptr;
+  for (int32_t i = 0; i < count; ++i) {
+    if (!learners[i]) {
+      set_error("bk_learner_group_create: learner %d is null", i);
+      return -1;
+    }
+    if (learners[i]->device != learners[0]->device) {
+      set_error("bk_learner_group_create: learner %d is on device %d, learner 0 on device %d", i,
+                learners[i]->device, learners[0]->device);
+      return -1;
+    }
+    for (int32_t k = 0; k < i; ++k)
+      if (learners[k] == learners[i]) {
+        set_error("bk_learner_group_create: learner %d appears twice", i);
+        return -1;
+      }
+  }
+  auto G = std::make_unique<bk_learner_group>();
+  try {
+    G->device = learners[0]->device;
+    CK(cudaSetDevice(G->device));
+    G->learners.assign(learners, learners + count);
+    G->gens.assign(count, 0);
+    G->g.assign(count, nullptr);
+    G->h.assign(count, nullptr);
+    G->scores.assign(count, nullptr);
+    CK(cudaStreamCreateWithFlags(&G->stream, cudaStreamNonBlocking));
+    CK(cudaEventCreateWithFlags(&G->fork, cudaEventDisableTiming));
+    G->joins.assign(count, nullptr);
+    for (auto& e : G->joins) CK(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+  } catch (const CudaError& e) {
+    return fail_cuda(e);
+  }
+  *out = G.release();
+  return 0;
+}
+
+int bk_learner_group_train(bk_learner_group* G, const float* const* gradients, const float* const* hessians,
+                           double shrinkage, double* const* scores, bk_split* const* splits,
+                           double* const* leaf_values, double* const* root_outputs, int32_t* const* num_leaves_out) {
+  if (!G || !gradients || !hessians) {
+    set_error("bk_learner_group_train: invalid arguments");
+    return -1;
+  }
+  const size_t count = G->learners.size();
+  for (size_t i = 0; i < count; ++i) {
+    const bk_learner* L = G->learners[i];
+    if (!gradients[i] || !hessians[i]) {
+      set_error("bk_learner_group_train: learner %d: null gradients", (int)i);
+      return -1;
+    }
+    if (L->loop_mode != 1 || L->timing) {
+      set_error("bk_learner_group_train: learner %d: a group runs the graph form without phase timing", (int)i);
+      return -1;
+    }
+  }
+  size_t i = 0;
+  try {
+    CK(cudaSetDevice(G->device));
+    for (bk_learner* L : G->learners)
+      for (int j = 0; j < L->K; ++j) {
+        L->h_state[j].use_rows = 0;
+        L->h_state[j].root_count = L->p.n;
+        L->h_state[j].hist_rows_direct = L->h_state[j].hist_rows_gather = L->h_state[j].hist_builds = 0;
+      }
+    if (!G->current(gradients, hessians, shrinkage, scores)) G->capture(gradients, hessians, shrinkage, scores);
+    // the iteration comes after the work already queued on every member's stream (the gradients
+    // of bk_learner_objective_gradients, an earlier call)
+    for (size_t k = 0; k < count; ++k) {
+      CK(cudaEventRecord(G->joins[k], G->learners[k]->stream));
+      CK(cudaStreamWaitEvent(G->stream, G->joins[k], 0));
+    }
+    CK(cudaGraphLaunch(G->exec, G->stream));
+    CK(cudaStreamSynchronize(G->stream));
+    CK(cudaGetLastError());
+    for (i = 0; i < count; ++i)
+      train_finish(G->learners[i], splits ? splits[i] : nullptr, leaf_values ? leaf_values[i] : nullptr,
+                   root_outputs ? root_outputs[i] : nullptr, num_leaves_out ? num_leaves_out[i] : nullptr, false);
+    for (i = 0; i < count; ++i)
+      if (!labels_ok(G->learners[i])) {
+        std::string msg = g_last_error;
+        set_error("bk_learner_group_train: learner %d: %s", (int)i, msg.c_str());
+        return -1;
+      }
+  } catch (const CudaError& e) {
+    cudaStreamSynchronize(G->stream);
+    set_error("bk_learner_group_train: CUDA error: %s", e.msg.c_str());
+    return -1;
+  }
+  return 0;
+}
+
+int bk_learner_group_autotune(bk_learner_group* G, const float* const* gradients, const float* const* hessians,
+                              int32_t trials, int32_t* policy_out) {
+  if (!G || !gradients || !hessians || trials < 1) {
+    set_error("bk_learner_group_autotune: invalid arguments");
+    return -1;
+  }
+  const size_t count = G->learners.size();
+  for (size_t i = 0; i < count; ++i)
+    if (!gradients[i] || !hessians[i] || G->learners[i]->loop_mode != 1 || G->learners[i]->timing) {
+      set_error("bk_learner_group_autotune: learner %d: null gradients, or not the graph form without timing", (int)i);
+      return -1;
+    }
+  // (rows per histogram CTA at least, histogram CTAs per learner over all its tiles, partition CTAs):
+  // from a quarter of the device per learner down to a thirtieth, so more learners' kernels run
+  // side by side; each with and without programmatic dependent launch (whose early-resident CTAs
+  // hold SM room that other learners' kernels could use)
+  static const int kCand[4][3] = {{1024, 38, 64}, {2048, 19, 32}, {4096, 10, 16}, {8192, 5, 8}};
+  std::vector<JobState*> saved(count, nullptr);
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  std::vector<uint8_t> pdl0(count);
+  std::vector<std::array<int, 4>> shape0(count);
+  for (size_t i = 0; i < count; ++i) {
+    pdl0[i] = (uint8_t)G->learners[i]->p.pdl;
+    G->learners[i]->shape_of(shape0[i].data());
+  }
+  auto apply = [&](int pdl, int c) {
+    for (bk_learner* L : G->learners) {
+      if ((pdl != 0) != (L->p.pdl != 0)) {
+        L->p.pdl = pdl;
+        L->drop_graph();
+      }
+      L->set_launch_shape(kCand[c][0], std::max(1, kCand[c][1] / L->p.T), kCand[c][2], 0);
+    }
+  };
+  try {
+    CK(cudaSetDevice(G->device));
+    CK(cudaEventCreate(&e0));
+    CK(cudaEventCreate(&e1));
+    // the trial iterations must not advance the learners' state across trees (the stochastic-
+    // rounding engines): every job state is saved here and put back before each trial and after
+    for (size_t i = 0; i < count; ++i) {
+      bk_learner* L = G->learners[i];
+      CK(cudaMalloc((void**)&saved[i], sizeof(JobState) * (size_t)L->K));
+      CK(cudaMemcpyAsync(saved[i], L->jobs[0].st, sizeof(JobState) * (size_t)L->K, cudaMemcpyDeviceToDevice,
+                         L->stream));
+    }
+    for (bk_learner* L : G->learners) CK(cudaStreamSynchronize(L->stream));
+    auto restore = [&]() {
+      for (size_t i = 0; i < count; ++i)
+        CK(cudaMemcpyAsync(G->learners[i]->jobs[0].st, saved[i], sizeof(JobState) * (size_t)G->learners[i]->K,
+                           cudaMemcpyDeviceToDevice, G->stream));
+    };
+    double best_ms = 1e300;
+    int best_pdl = 1, best_c = 0;
+    for (int pdl = 1; pdl >= 0; --pdl)
+      for (int c = 0; c < 4; ++c) {
+        apply(pdl, c);
+        for (bk_learner* L : G->learners)
+          for (int j = 0; j < L->K; ++j) {
+            L->h_state[j].use_rows = 0;
+            L->h_state[j].root_count = L->p.n;
+            L->h_state[j].hist_rows_direct = L->h_state[j].hist_rows_gather = L->h_state[j].hist_builds = 0;
+          }
+        G->capture(gradients, hessians, 0.0, nullptr);
+        std::vector<float> t;
+        for (int r = 0; r <= trials; ++r) {  // one untimed iteration, then `trials` timed ones
+          restore();
+          CK(cudaEventRecord(e0, G->stream));
+          CK(cudaGraphLaunch(G->exec, G->stream));
+          CK(cudaEventRecord(e1, G->stream));
+          CK(cudaEventSynchronize(e1));
+          float ms = 0.f;
+          CK(cudaEventElapsedTime(&ms, e0, e1));
+          if (r > 0) t.push_back(ms);
+        }
+        std::sort(t.begin(), t.end());
+        const double med = t[t.size() / 2];
+        if (med < best_ms) {
+          best_ms = med;
+          best_pdl = pdl;
+          best_c = c;
+        }
+      }
+    restore();
+    CK(cudaStreamSynchronize(G->stream));
+    apply(best_pdl, best_c);
+    if (policy_out) {
+      policy_out[0] = best_pdl;
+      policy_out[1] = kCand[best_c][0];
+      policy_out[2] = kCand[best_c][1];
+      policy_out[3] = kCand[best_c][2];
+    }
+  } catch (const CudaError& e) {
+    cudaStreamSynchronize(G->stream);
+    for (size_t i = 0; i < count; ++i) {
+      bk_learner* L = G->learners[i];
+      if (saved[i]) cudaMemcpy(L->jobs[0].st, saved[i], sizeof(JobState) * (size_t)L->K, cudaMemcpyDeviceToDevice);
+      if ((pdl0[i] != 0) != (L->p.pdl != 0)) {
+        L->p.pdl = pdl0[i];
+        L->drop_graph();
+      }
+      L->set_launch_shape(shape0[i][0], shape0[i][1], shape0[i][2], shape0[i][3]);
+    }
+    for (JobState* x : saved) cudaFree(x);
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    set_error("bk_learner_group_autotune: CUDA error: %s", e.msg.c_str());
+    return -1;
+  }
+  for (JobState* x : saved) cudaFree(x);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  return 0;
+}
+
+int bk_learner_group_destroy(bk_learner_group* G) {
+  if (!G) return 0;
+  cudaSetDevice(G->device);
+  cudaStreamSynchronize(G->stream);
+  delete G;
+  return 0;
+}
+
 int bk_learner_add_prediction_to_score(bk_learner* L, const double* leaf_values, double* score, int32_t on_device) {
   if (!L || !leaf_values || !score) {
     set_error("bk_learner_add_prediction_to_score: invalid arguments");
@@ -987,10 +1338,7 @@ int bk_learner_set_launch_overlap(bk_learner* L, int32_t on) {
     set_error("bk_learner_set_launch_overlap: null learner");
     return -1;
   }
-  if ((on != 0) != (L->p.pdl != 0) && L->graph_exec) {
-    cudaGraphExecDestroy(L->graph_exec);
-    L->graph_exec = nullptr;
-  }
+  if ((on != 0) != (L->p.pdl != 0)) L->drop_graph();
   L->p.pdl = on != 0;
   return 0;
 }
@@ -1000,11 +1348,18 @@ int bk_learner_set_timing(bk_learner* L, int32_t on) {
     set_error("bk_learner_set_timing: null learner");
     return -1;
   }
-  if ((on != 0) != L->timing && L->graph_exec) {
-    cudaGraphExecDestroy(L->graph_exec);
-    L->graph_exec = nullptr;
-  }
+  if ((on != 0) != L->timing) L->drop_graph();
   L->timing = on != 0;
+  return 0;
+}
+
+int bk_learner_search_threads(bk_learner* L, int32_t* threads) {
+  if (!L || !threads) {
+    set_error("bk_learner_search_threads: invalid arguments");
+    return -1;
+  }
+  const bool plain = !L->p.use_l1 && !L->p.use_max && !L->p.use_smooth;
+  *threads = (plain && L->p.search_narrow && !L->stable_partition()) ? 64 : 256;
   return 0;
 }
 
@@ -1044,10 +1399,7 @@ int bk_learner_reset_constant_hessian(bk_learner* L, int32_t value) {
       set_error("CUDA error: %s", cudaGetErrorString(e));
       return -1;
     }
-    if (L->graph_exec) {
-      cudaGraphExecDestroy(L->graph_exec);
-      L->graph_exec = nullptr;
-    }
+    L->drop_graph();
   }
   return 0;
 }
@@ -1103,10 +1455,7 @@ int bk_learner_set_bynode(bk_learner* L, double fraction, int32_t bytree_active,
   }
   L->bynode_sampling = on;
   const int32_t masks = (on || L->p.n_icons > 0) ? 1 : 0;
-  if (masks != L->p.bynode && L->graph_exec) {
-    cudaGraphExecDestroy(L->graph_exec);
-    L->graph_exec = nullptr;
-  }
+  if (masks != L->p.bynode) L->drop_graph();
   L->p.bynode = masks;
   return 0;
 }
@@ -1138,10 +1487,7 @@ int bk_learner_set_interaction_constraints(bk_learner* L, const int32_t* feature
     L->p.icons = d;
     L->p.n_icons = num_sets;
     L->p.bynode = (L->bynode_sampling || num_sets > 0) ? 1 : 0;
-    if (L->graph_exec) {  // the kernels take the constraints through their parameters
-      cudaGraphExecDestroy(L->graph_exec);
-      L->graph_exec = nullptr;
-    }
+    L->drop_graph();  // the kernels take the constraints through their parameters
   } catch (const CudaError& e) {
     return fail_cuda(e);
   }
@@ -1269,8 +1615,8 @@ int bk_learner_objective_loss(bk_learner* L, int32_t kind, const double* score, 
 
 int bk_learner_predict_add(bk_learner* L, int32_t num_leaves, const int32_t* left_child, const int32_t* right_child,
                            const int32_t* split_feature_inner, const uint32_t* threshold_in_bin,
-                           const int8_t* decision_type, const double* leaf_value, const uint8_t* bins,
-                           int64_t num_rows, double* score) {
+                           const int8_t* decision_type, const uint32_t* cat_bins, const double* leaf_value,
+                           const uint8_t* bins, int64_t num_rows, double* score) {
   if (!L || !leaf_value || !bins || !score || num_rows < 0 || num_leaves < 1 || num_leaves > L->p.num_leaves ||
       (num_leaves > 1 && (!left_child || !right_child || !split_feature_inner || !threshold_in_bin ||
                           !decision_type))) {
@@ -1286,24 +1632,30 @@ int bk_learner_predict_add(bk_learner* L, int32_t num_leaves, const int32_t* lef
         return -1;
       }
     }
-    if (decision_type[i] & 1) {
-      set_error("bk_learner_predict_add: node %d is a categorical split; the device replay takes numerical "
-                "splits only", i);
+    if (split_feature_inner[i] < 0 || split_feature_inner[i] >= L->p.F) {
+      set_error("bk_learner_predict_add: node %d splits an unknown feature", i);
       return -1;
     }
-    if (split_feature_inner[i] < 0 || split_feature_inner[i] >= L->p.F ||
-        threshold_in_bin[i] >= (uint32_t)L->h_feat[split_feature_inner[i]].num_bin) {
+    const bool cat = (decision_type[i] & 1) != 0;
+    if (cat && (!cat_bins || !L->h_feat[split_feature_inner[i]].cat)) {
+      set_error("bk_learner_predict_add: node %d is a categorical split without a bin bitset, or on a numerical "
+                "feature", i);
+      return -1;
+    }
+    if (!cat && threshold_in_bin[i] >= (uint32_t)L->h_feat[split_feature_inner[i]].num_bin) {
       set_error("bk_learner_predict_add: node %d splits an unknown feature or bin", i);
       return -1;
     }
   }
-  L->h_tree.assign(5 * (size_t)std::max(ni, 1), 0);
+  L->h_tree.assign(13 * (size_t)std::max(ni, 1), 0);
   for (int i = 0; i < ni; ++i) {
     L->h_tree[i] = left_child[i];
     L->h_tree[ni + i] = right_child[i];
     L->h_tree[2 * ni + i] = split_feature_inner[i];
     L->h_tree[3 * ni + i] = (int32_t)threshold_in_bin[i];
     L->h_tree[4 * ni + i] = decision_type[i];
+    if (decision_type[i] & 1)
+      for (int w = 0; w < 8; ++w) L->h_tree[5 * ni + 8 * i + w] = (int32_t)cat_bins[8 * (size_t)i + w];
   }
   try {
     CK(cudaMemcpyAsync(L->d_tree, L->h_tree.data(), sizeof(int32_t) * L->h_tree.size(), cudaMemcpyHostToDevice,

@@ -316,19 +316,22 @@ struct QEnt {
   int16_t t, d;  // position, direction
 };
 
-struct SearchSmem {
-  QEnt q[2][kSearchThreads];  // per direction: every position at most once
+// The shared memory of a numerical search CTA of NW warps (32 * NW threads, one per local bin).
+template <int NW>
+struct SearchSmemT {
+  QEnt q[2][32 * NW];  // per direction: every position at most once
   int32_t qn[2];
-  DirBest pres[2][4];         // per direction and batch lane (below): the arg-max of its batches
+  DirBest pres[2][4];  // per direction and batch lane (below): the arg-max of its batches
   int32_t psplit[2][4];
-  int64_t wi[2][kSearchWarps];
-  double wd[10][kSearchWarps];
-  int32_t wc[3][kSearchWarps];
-  WarpFilt wf[2][kSearchWarps];
+  int64_t wi[2][NW];
+  double wd[10][NW];
+  int32_t wc[3][NW];
+  WarpFilt wf[2][NW];
   WarpFilt xf;  // the forward scan's position -1 (last thread)
-  int32_t spl[2][kSearchWarps];
-  DirBest wb[2][kSearchWarps];
+  int32_t spl[2][NW];
+  DirBest wb[2][NW];
 };
+using SearchSmem = SearchSmemT<kSearchWarps>;
 
 // This warp's arg-max of direction d (highest key, then the earliest position in scan order) into w.
 __device__ __forceinline__ void warp_best(int d, bool elig, double gain, int t, int64_t a, int64_t b, int32_t c,
@@ -357,14 +360,15 @@ __device__ __forceinline__ void warp_best(int d, bool elig, double gain, int t, 
 
 // Warp 0 after the barrier: the CTA's best of each direction (lane 0: direction 0, lane 8:
 // direction 1), broadcast to every lane of the warp.
-__device__ __forceinline__ void combine_best(const SearchSmem& sm, int lane, DirBest (&r)[2], int (&split)[2]) {
+template <int NW>
+__device__ __forceinline__ void combine_best(const SearchSmemT<NW>& sm, int lane, DirBest (&r)[2], int (&split)[2]) {
   const int d = (lane >> 3) & 1;
   long long key = kNoKey;
   double gain = -CUDART_INF;
   int64_t a = 0, b = 0;
   int32_t t = 0, c = 0;
   int sp = 0;
-  if (lane < 16) {
+  if (lane < 16 && (lane & 7) < NW) {
     const DirBest& e = sm.wb[d][lane & 7];
     key = e.key;
     if (key != kNoKey) {
@@ -422,8 +426,8 @@ __device__ __forceinline__ Filt filt_of(bool cand, const Approx& a, const LeafCo
 }
 
 // Before the barrier: the warp's summary of direction d for positions `pos` (thread order = t).
-template <bool PLAIN>
-__device__ __forceinline__ void publish_dir(SearchSmem& sm, int d, bool brk, int pos, const Filt& f, int lane,
+template <bool PLAIN, int NW>
+__device__ __forceinline__ void publish_dir(SearchSmemT<NW>& sm, int d, bool brk, int pos, const Filt& f, int lane,
                                             int warp) {
   const int lb = d == 0 ? __reduce_max_sync(FULL, brk ? pos : kNoneLo) : __reduce_min_sync(FULL, brk ? pos : kNoneHi);
   WarpFilt w;
@@ -443,11 +447,11 @@ __device__ __forceinline__ void publish_dir(SearchSmem& sm, int d, bool brk, int
 // positions 32w .. 32w + 31; the forward scan's position -1 (when `has_x`) comes first in its
 // scan order. The maximal gain G* of the direction is at least M, so only positions whose upper
 // bound reaches M can hold it; and any position passes min_gain_shift exactly when G* does.
-template <bool PLAIN>
-__device__ __forceinline__ void resolve_dir(const SearchSmem& sm, int d, bool has_x, int* S, int32_t* M) {
+template <bool PLAIN, int NW>
+__device__ __forceinline__ void resolve_dir(const SearchSmemT<NW>& sm, int d, bool has_x, int* S, int32_t* M) {
   int s = d == 0 ? kNoneLo : kNoneHi;
 #pragma unroll
-  for (int w = 0; w < kSearchWarps; ++w) s = d == 0 ? max(s, sm.wf[d][w].lb) : min(s, sm.wf[d][w].lb);
+  for (int w = 0; w < NW; ++w) s = d == 0 ? max(s, sm.wf[d][w].lb) : min(s, sm.wf[d][w].lb);
   if (d == 1 && has_x && sm.xf.lb == -1) s = -1;
   *S = s;
   int32_t m = float_key(-CUDART_INF_F);
@@ -455,7 +459,7 @@ __device__ __forceinline__ void resolve_dir(const SearchSmem& sm, int d, bool ha
     const bool none = d == 0 ? s == kNoneLo : s == kNoneHi;
     if (d == 1 && has_x && s != -1) m = sm.xf.ma;
 #pragma unroll
-    for (int w = 0; w < kSearchWarps; ++w) {
+    for (int w = 0; w < NW; ++w) {
       const WarpFilt& f = sm.wf[d][w];
       const bool contains = !none && f.lb == s;
       const bool all_before = none || (d == 0 ? 32 * w > s : 32 * w + 31 < s);
@@ -477,7 +481,8 @@ __device__ __forceinline__ bool is_neg_inf(double x) {
 }
 
 // Appends this thread's entry (when `push`) to direction d's queue, one shared atomic per warp.
-__device__ __forceinline__ void queue_push(SearchSmem& sm, int d, bool push, const QEnt& e, int lane) {
+template <int NW>
+__device__ __forceinline__ void queue_push(SearchSmemT<NW>& sm, int d, bool push, const QEnt& e, int lane) {
   const unsigned bal = __ballot_sync(FULL, push);
   int base = 0;
   if (lane == 0 && bal) base = atomicAdd(&sm.qn[d], __popc(bal));
@@ -493,9 +498,9 @@ __device__ __forceinline__ void queue_push(SearchSmem& sm, int d, bool push, con
 // d + 2 (k mod 4), so the first batches of the two directions run on two schedulers and longer
 // queues spread over all four. One warp: its batches k0, k0 + 4, ...; their arg-max (highest gain,
 // ties to the earliest position in scan order) with its SplitInfo, and whether any passed, into
-// sm.pres[d][k0] / sm.psplit[d][k0].
-template <typename SideOf>
-__device__ __forceinline__ void eval_batches(SearchSmem& sm, int d, int k0, int lane, double mgs, SideOf side_of) {
+// sm.pres[d][k0] / sm.psplit[d][k0]. (With NW warps, batch k runs on warp d + 2 (k mod NW / 2).)
+template <int NW, typename SideOf>
+__device__ __forceinline__ void eval_batches(SearchSmemT<NW>& sm, int d, int k0, int lane, double mgs, SideOf side_of) {
   DirBest r;
   r.key = kNoKey;
   r.ev.gain = -CUDART_INF;
@@ -549,22 +554,24 @@ __device__ __forceinline__ void eval_batches(SearchSmem& sm, int d, int k0, int 
   };
   // the first batch outside the loop: the f64 gain evaluated inside a loop measured about twice
   // as slow as the same code in straight-line form
+  constexpr int kLanes = NW / 2;  // batch lanes per direction
   if (16 * k0 < n) batch(16 * k0);
-  for (int b0 = 16 * k0 + 64; b0 < n; b0 += 64) batch(b0);
+  for (int b0 = 16 * (k0 + kLanes); b0 < n; b0 += 16 * kLanes) batch(b0);
   if (lane == 0) {
     sm.pres[d][k0] = r;
     sm.psplit[d][k0] = split;
   }
 }
 
-// After the queues are filled (barrier 3): warps 0-7 evaluate the queue batches (warp w takes
-// direction w & 1, batches w >> 1, (w >> 1) + 4, ...). Barrier 4; then warp 0 combines the batch
-// results of each direction into r / rs, the winner's SplitInfo included.
-template <typename SideOf>
-__device__ __forceinline__ void eval_queues(SearchSmem& sm, int warp, int lane, double mgs, SideOf side_of,
+// After the queues are filled (barrier 3): the NW warps evaluate the queue batches (warp w takes
+// direction w & 1, batches w >> 1, (w >> 1) + NW / 2, ...). Barrier 4; then warp 0 combines the
+// batch results of each direction into r / rs, the winner's SplitInfo included.
+template <int NW, typename SideOf>
+__device__ __forceinline__ void eval_queues(SearchSmemT<NW>& sm, int warp, int lane, double mgs, SideOf side_of,
                                             DirBest (&r)[2], int (&rs)[2]) {
+  static_assert(NW >= 2 && NW <= 8 && NW % 2 == 0, "one batch lane of each direction per pair of warps");
   const int d = warp & 1, k0 = warp >> 1;
-  if (k0 < 4) eval_batches(sm, d, k0, lane, mgs, side_of);
+  if (k0 < NW / 2) eval_batches<NW>(sm, d, k0, lane, mgs, side_of);
   __syncthreads();
   if (warp != 0) return;
 #pragma unroll
@@ -572,7 +579,7 @@ __device__ __forceinline__ void eval_queues(SearchSmem& sm, int warp, int lane, 
     r[dd] = sm.pres[dd][0];
     rs[dd] = sm.psplit[dd][0];
 #pragma unroll
-    for (int k = 1; k < 4; ++k) {
+    for (int k = 1; k < NW / 2; ++k) {
       const DirBest& x = sm.pres[dd][k];
       rs[dd] |= sm.psplit[dd][k];
       if (x.key != kNoKey && (x.key > r[dd].key || (x.key == r[dd].key && earlier(dd, x.t, r[dd].t)))) r[dd] = x;
@@ -643,9 +650,9 @@ __device__ __forceinline__ void finish_cand(const Job& J, const Params& p, const
 // FindBestThresholdInt for one (leaf, feature): feature_histogram.rs:673-830, scans :839-1142.
 // Three barriers: the prefix scan (with the most-frequent-bin fix and the forward scan's start
 // folded in), the stop / prefilter summaries, and the arg-max.
-template <bool PLAIN>
+template <bool PLAIN, int NW>
 __device__ void search_int(const Job& J, const Params& p, const SearchIn& si, const DevFeature& m, int side,
-                           int32_t f, int32_t leaf, SearchSmem& sm) {
+                           int32_t f, int32_t leaf, SearchSmemT<NW>& sm) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const LeafConst& C = si.C;
   const int64_t s_int = si.S0.int_sum;
@@ -676,7 +683,7 @@ __device__ void search_int(const Job& J, const Params& p, const SearchIn& si, co
   __syncthreads();
   int64_t T = 0, AUX = 0;
 #pragma unroll
-  for (int i = 0; i < kSearchWarps; ++i) {
+  for (int i = 0; i < NW; ++i) {
     const int64_t y = sm.wi[0][i];
     if (i < warp) P += y;
     T += y;
@@ -703,7 +710,7 @@ __device__ void search_int(const Job& J, const Params& p, const SearchIn& si, co
   // bins 0 .. t; the last thread also holds forward position -1 (left side = base_f)
   const int64_t right = T - (P - w);
   const int64_t left = base_f + P;
-  const bool xpos = G.fwd_rest && t == kSearchThreads - 1;
+  const bool xpos = G.fwd_rest && t == 32 * NW - 1;
   const bool first0 = t >= 1 - G.off && acc_t && unpack_h(right) >= C.first_x;
   const bool brk0 = first0 && unpack_h(right) >= C.brk_x;
   const bool first1 = G.two && t <= G.t_end && !skip_t && unpack_h(left) >= C.first_x;
@@ -721,11 +728,11 @@ __device__ void search_int(const Job& J, const Params& p, const SearchIn& si, co
     if (PLAIN && cand) a = approx_int(lg[d], lh[d], tg, th, C.gsf, C.hsf, C.l2f);
     fl[d] = filt_of(cand, a, C);
   }
-  publish_dir<PLAIN>(sm, 0, brk0, t, fl[0], lane, warp);
+  publish_dir<PLAIN, NW>(sm, 0, brk0, t, fl[0], lane, warp);
   {
     Filt nat = fl[1];
     if (xpos) nat.lo = float_key(-CUDART_INF_F);  // the natural position 255 is never a candidate
-    publish_dir<PLAIN>(sm, 1, brk1, t, nat, lane, warp);
+    publish_dir<PLAIN, NW>(sm, 1, brk1, t, nat, lane, warp);
   }
   if (xpos) {
     WarpFilt x;
@@ -736,8 +743,8 @@ __device__ void search_int(const Job& J, const Params& p, const SearchIn& si, co
   __syncthreads();
   int S[2];
   int32_t M[2];
-  resolve_dir<PLAIN>(sm, 0, false, &S[0], &M[0]);
-  resolve_dir<PLAIN>(sm, 1, G.fwd_rest, &S[1], &M[1]);
+  resolve_dir<PLAIN, NW>(sm, 0, false, &S[0], &M[0]);
+  resolve_dir<PLAIN, NW>(sm, 1, G.fwd_rest, &S[1], &M[1]);
   const bool valid[2] = {first0 && t > S[0], xpos ? (firstx && S[1] != -1) : (first1 && t < S[1])};
   DirBest r[2];
   int rs[2] = {0, 0};
@@ -800,9 +807,9 @@ __device__ void search_int(const Job& J, const Params& p, const SearchIn& si, co
 // :363-663. f64 (grad, hess) sums and row counts estimated per bin as round_int(hess *
 // cnt_factor); the forward scan uses prefix sums, the reverse scan suffix sums (accumulated from
 // the top bin down, not derived by subtraction).
-template <bool PLAIN>
+template <bool PLAIN, int NW>
 __device__ void search_float(const Job& J, const Params& p, const SearchIn& si, const DevFeature& m, int side,
-                             int32_t f, int32_t leaf, SearchSmem& sm) {
+                             int32_t f, int32_t leaf, SearchSmemT<NW>& sm) {
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   const LeafConst& C = si.C;
   const LeafSum& S0 = si.S0;
@@ -829,7 +836,7 @@ __device__ void search_float(const Job& J, const Params& p, const SearchIn& si, 
     __syncthreads();
     double tg = 0.0, th = 0.0;
 #pragma unroll
-    for (int i = 0; i < kSearchWarps; ++i) {
+    for (int i = 0; i < NW; ++i) {
       tg += sm.wd[0][i];
       th += sm.wd[1][i];
     }
@@ -878,7 +885,7 @@ __device__ void search_float(const Job& J, const Params& p, const SearchIn& si, 
     double og = 0.0, oh = 0.0, sg_ = 0.0, sh_ = 0.0, ug = 0.0, uh = 0.0;
     int32_t oc = 0, sc = 0, uc = 0;
 #pragma unroll
-    for (int i = 0; i < kSearchWarps; ++i) {
+    for (int i = 0; i < NW; ++i) {
       if (i < warp) {
         og += sm.wd[2][i];
         oh += sm.wd[3][i];
@@ -886,7 +893,7 @@ __device__ void search_float(const Job& J, const Params& p, const SearchIn& si, 
       }
     }
 #pragma unroll
-    for (int i = kSearchWarps - 1; i >= 0; --i) {
+    for (int i = NW - 1; i >= 0; --i) {
       if (i > warp) {
         sg_ += sm.wd[4][i];
         sh_ += sm.wd[5][i];
@@ -895,7 +902,7 @@ __device__ void search_float(const Job& J, const Params& p, const SearchIn& si, 
     }
     if (G.fwd_rest) {
 #pragma unroll
-      for (int i = 0; i < kSearchWarps; ++i) {
+      for (int i = 0; i < NW; ++i) {
         ug += sm.wd[6][i];
         uh += sm.wd[7][i];
         uc += sm.wc[2][i];
@@ -913,7 +920,7 @@ __device__ void search_float(const Job& J, const Params& p, const SearchIn& si, 
   }
   // reverse position t: right side (rg, rh, rc); forward position t: left side (pg, ph, pc); the
   // last thread holds forward position -1 when the scan starts outside the slice
-  const bool xpos = G.fwd_rest && t == kSearchThreads - 1;
+  const bool xpos = G.fwd_rest && t == 32 * NW - 1;
   const bool first0 = t >= 1 - G.off && rin && !skip_t && !(rc < p.min_data || rh < p.min_hess);
   const bool brk0 = first0 && (num_data - rc < p.min_data || sum_h - rh < p.min_hess);
   const bool first1 = G.two && t <= G.t_end && !skip_t && !(pc < p.min_data || ph < p.min_hess);
@@ -935,11 +942,11 @@ __device__ void search_float(const Job& J, const Params& p, const SearchIn& si, 
       a = approx_from((float)slg[d], __fadd_rn((float)slh[d], C.l2f), (float)srg[d], __fadd_rn((float)srh[d], C.l2f));
     fl[d] = filt_of(cand, a, C);
   }
-  publish_dir<PLAIN>(sm, 0, brk0, t, fl[0], lane, warp);
+  publish_dir<PLAIN, NW>(sm, 0, brk0, t, fl[0], lane, warp);
   {
     Filt nat = fl[1];
     if (xpos) nat.lo = float_key(-CUDART_INF_F);
-    publish_dir<PLAIN>(sm, 1, brk1, t, nat, lane, warp);
+    publish_dir<PLAIN, NW>(sm, 1, brk1, t, nat, lane, warp);
   }
   if (xpos) {
     WarpFilt x;
@@ -950,8 +957,8 @@ __device__ void search_float(const Job& J, const Params& p, const SearchIn& si, 
   __syncthreads();
   int S[2];
   int32_t M[2];
-  resolve_dir<PLAIN>(sm, 0, false, &S[0], &M[0]);
-  resolve_dir<PLAIN>(sm, 1, G.fwd_rest, &S[1], &M[1]);
+  resolve_dir<PLAIN, NW>(sm, 0, false, &S[0], &M[0]);
+  resolve_dir<PLAIN, NW>(sm, 1, G.fwd_rest, &S[1], &M[1]);
   const bool valid[2] = {first0 && t > S[0], xpos ? (firstx && S[1] != -1) : (first1 && t < S[1])};
   DirBest r[2];
   int rs[2] = {0, 0};
@@ -1380,11 +1387,15 @@ __device__ void search_cat(const Job& J, const Params& p, const SearchIn& si, co
 // One CTA per (feature, side): blockIdx.x = 2 * feature + side (0 = smaller leaf). With `decide`,
 // the last CTA to finish runs the fold / arg-max and records the split; otherwise the single-pass
 // partition that follows decides it.
-template <bool PLAIN, bool QUANT>
-__global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, Params p,
-                                                           const DevFeature* __restrict__ feats, int clear_par,
-                                                           int decide) {
-  __shared__ SearchSmem sm;
+// NW warps per CTA: 8 for features of up to 256 group bins; 2 (64 threads) when every feature
+// has at most 64, so a CTA holds what a small-bin feature needs and four times as many CTAs fit
+// on an SM. Only NW = 8 takes categorical features and the stable path's last-CTA decision
+// (both use 256 threads); the host picks NW accordingly.
+template <bool PLAIN, bool QUANT, int NW>
+__global__ void __launch_bounds__(32 * NW) k_search(const JobTable jobs, Params p,
+                                                    const DevFeature* __restrict__ feats, int clear_par,
+                                                    int decide) {
+  __shared__ SearchSmemT<NW> sm;
   __shared__ int last;
   __shared__ Decision dec;
   const int side = (int)(blockIdx.x & 1u);
@@ -1412,13 +1423,20 @@ __global__ void __launch_bounds__(kSearchThreads) k_search(const JobTable jobs, 
   si.S0 = side ? J.lconst[0].ls : si.C.ls;
   if (stop) return;  // uniform over the grid
   if (do_search && used && leaf >= 0) {  // uniform over the CTA
-    if (m.cat)
-      search_cat<QUANT>(J, p, si, m, side, f, leaf, sm);
-    else if (QUANT)
-      search_int<PLAIN>(J, p, si, m, side, f, leaf, sm);
-    else
-      search_float<PLAIN>(J, p, si, m, side, f, leaf, sm);
+    if constexpr (NW == kSearchWarps) {
+      if (m.cat) {
+        search_cat<QUANT>(J, p, si, m, side, f, leaf, sm);
+      } else if (QUANT) {
+        search_int<PLAIN>(J, p, si, m, side, f, leaf, sm);
+      } else {
+        search_float<PLAIN>(J, p, si, m, side, f, leaf, sm);
+      }
+    } else {
+      if (QUANT) search_int<PLAIN>(J, p, si, m, side, f, leaf, sm);
+      else search_float<PLAIN>(J, p, si, m, side, f, leaf, sm);
+    }
   }
+  if constexpr (NW != kSearchWarps) return;  // the host gives the decision to a 256-thread launch
   if (!decide) return;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -1486,15 +1504,25 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
 void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, int clear_par,
                    bool decide, cudaStream_t s) {
   const bool plain = !p.use_l1 && !p.use_max && !p.use_smooth;
-  const dim3 block(kSearchThreads);
+  // 64-thread CTAs when every feature's slice fits in 63 bins (thread 63 holds the forward scan's
+  // position -1), no feature is categorical and no CTA has to run the 256-thread decision
+  const bool narrow = plain && p.search_narrow && !decide;
+  const int dec = decide ? 1 : 0;
   for_job_groups(h_jobs, num_jobs, [&](const JobTable& t, int nz) {
     dim3 grid((unsigned)(2 * p.F), 1, nz);
+    if (narrow) {
+      const dim3 block(64);
+      if (p.quant) (void)launch_kernel(k_search<true, true, 2>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
+      else (void)launch_kernel(k_search<true, false, 2>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
+      return;
+    }
+    const dim3 block(kSearchThreads);
     if (p.quant) {
-      if (plain) (void)launch_kernel(k_search<true, true>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, decide ? 1 : 0);
-      else (void)launch_kernel(k_search<false, true>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, decide ? 1 : 0);
+      if (plain) (void)launch_kernel(k_search<true, true, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
+      else (void)launch_kernel(k_search<false, true, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
     } else {
-      if (plain) (void)launch_kernel(k_search<true, false>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, decide ? 1 : 0);
-      else (void)launch_kernel(k_search<false, false>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, decide ? 1 : 0);
+      if (plain) (void)launch_kernel(k_search<true, false, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
+      else (void)launch_kernel(k_search<false, false, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
     }
   });
 }

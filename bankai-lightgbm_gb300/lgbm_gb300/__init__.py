@@ -6,4 +6,4 @@ serial.rs) over the C-ABI library ``lib/libbkgpu.so`` (declared in ``include/bkg
 from .dataset import BinnedDataset, FeatureInfo, FEATURE_DTYPE  # noqa: F401
 from .tree import Tree, SPLIT_DTYPE  # noqa: F401
 from .config import LearnerConfig, CONFIG_DTYPE  # noqa: F401
-from .learner import GpuTreeLearner, train_batch  # noqa: F401
+from .learner import GpuTreeLearner, LearnerGroup, train_batch  # noqa: F401

@@ -62,12 +62,17 @@ _GPU_SIGNATURES = [
     ("bk_bin_dense_device", _i32, [_P, _i32, _i64, _i32, _P, _i32, _P, _P, _P, _P]),
     ("bk_learner_train", _i32, [_P, _P, _P, _i32, _P, _i64, _P, _P, _P, _P]),
     ("bk_learners_train_batch", _i32, [_P, _i32, _P, _P, _i32, _f64, _P, _P, _P, _P, _P]),
+    ("bk_learner_group_create", _i32, [_P, _i32, _P]),
+    ("bk_learner_group_train", _i32, [_P, _P, _P, _f64, _P, _P, _P, _P, _P]),
+    ("bk_learner_group_destroy", _i32, [_P]),
+    ("bk_learner_group_autotune", _i32, [_P, _P, _P, _i32, _P]),
     ("bk_learner_add_prediction_to_score", _i32, [_P, _P, _P, _i32]),
     ("bk_learner_row_leaf", _i32, [_P, _P]),
     ("bk_learner_set_loop_mode", _i32, [_P, _i32]),
     ("bk_learner_set_launch_overlap", _i32, [_P, _i32]),
     ("bk_learner_reset_constant_hessian", _i32, [_P, _i32]),
     ("bk_learner_histogram_cache_capacity", _i32, [_P, _P]),
+    ("bk_learner_search_threads", _i32, [_P, _P]),
     ("bk_learner_reset_histogram_pool_config", _i32, [_P]),
     ("bk_learner_set_feature_mask", _i32, [_P, _P]),
     ("bk_learner_set_bynode", _i32, [_P, _f64, _i32, _u32]),
@@ -84,7 +89,7 @@ _GPU_SIGNATURES = [
     ("bk_learner_objective_gradients", _i32, [_P, _i32, _P, _P, _f64]),
     ("bk_learner_objective_loss", _i32, [_P, _i32, _P, _P, _P]),
     ("bk_learner_set_objective_weights", _i32, [_P, _P, _f64, _f64]),
-    ("bk_learner_predict_add", _i32, [_P, _i32, _P, _P, _P, _P, _P, _P, _P, _i64, _P]),
+    ("bk_learner_predict_add", _i32, [_P, _i32, _P, _P, _P, _P, _P, _P, _P, _P, _i64, _P]),
     ("bk_learner_leaf_histogram", _i32, [_P, _i32, _i32, _P, _P]),
     ("bk_learner_stream", _i32, [_P, _P]),
     ("bk_learner_destroy", _i32, [_P]),

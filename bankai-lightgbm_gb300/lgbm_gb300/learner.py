@@ -153,6 +153,12 @@ class GpuTreeLearner:
                    "bk_learner_histogram_cache_capacity")
         return out.value
 
+    def search_threads(self):
+        """Threads per split-search CTA of the next train call (64 or 256)."""
+        out = ctypes.c_int32()
+        _lib.check(self.lib.bk_learner_search_threads(self.h, ctypes.byref(out)), "bk_learner_search_threads")
+        return out.value
+
     def reset_histogram_pool_config(self):
         """The budget-only reset of SerialTreeLearner::reset_histogram_pool_config: nothing changes."""
         _lib.check(self.lib.bk_learner_reset_histogram_pool_config(self.h), "bk_learner_reset_histogram_pool_config")
@@ -181,9 +187,16 @@ class GpuTreeLearner:
         th = np.ascontiguousarray(tree.threshold_in_bin[:ni], np.uint32)
         dt = np.ascontiguousarray(tree.decision_type[:ni], np.int8)
         lv = np.ascontiguousarray(tree.leaf_value[:tree.num_leaves], np.float64)
+        # categorical nodes: the left-bin bitsets (a dict node -> 8 words, or a [ni, 8] array)
+        cb = np.zeros((max(ni, 1), 8), np.uint32)
+        bits = getattr(tree, "cat_bin_bits", None)
+        if bits is not None:
+            for node in (bits.keys() if isinstance(bits, dict) else range(ni)):
+                cb[node] = np.asarray(bits[node], np.uint32)
         _lib.check(self.lib.bk_learner_predict_add(self.h, tree.num_leaves, lc.ctypes.data, rc.ctypes.data,
-                                                   sf.ctypes.data, th.ctypes.data, dt.ctypes.data, lv.ctypes.data,
-                                                   int(bins_ptr), int(num_rows), int(score_ptr)),
+                                                   sf.ctypes.data, th.ctypes.data, dt.ctypes.data,
+                                                   cb.ctypes.data if bits is not None else None,
+                                                   lv.ctypes.data, int(bins_ptr), int(num_rows), int(score_ptr)),
                    "bk_learner_predict_add")
 
     def gradient_buffers(self):
@@ -301,3 +314,62 @@ def train_batch(learners, gradients, hessians, on_device=False, shrinkage=None, 
                                            float(shrinkage if shrinkage is not None else 0.0), sc, sp, lp, rp, np_),
                "bk_learners_train_batch")
     return outs
+
+
+class LearnerGroup:
+    """A fixed set of learners whose iterations run as one CUDA graph (``bk_learner_group_*``):
+    every learner's grow loop, score update and result readback is one branch of the graph, so one
+    launch runs all of them with no host work between their kernels."""
+
+    def __init__(self, learners):
+        self.learners = list(learners)
+        assert self.learners
+        self.lib = self.learners[0].lib
+        count = len(self.learners)
+        hs = (ctypes.c_void_p * count)(*[L.h.value for L in self.learners])
+        h = ctypes.c_void_p()
+        _lib.check(self.lib.bk_learner_group_create(hs, count, ctypes.byref(h)), "bk_learner_group_create")
+        self.h = h
+        self._outs = []
+        for L in self.learners:
+            K, Lv = L.num_jobs, L.num_leaves
+            self._outs.append((np.zeros((K, max(Lv - 1, 1)), dtype=SPLIT_DTYPE), np.zeros((K, Lv), dtype=np.float64),
+                               np.zeros(K, dtype=np.float64), np.zeros(K, dtype=np.int32)))
+        arr = lambda k: (ctypes.c_void_p * count)(*[o[k].ctypes.data for o in self._outs])
+        self._sp, self._lp, self._rp, self._np = arr(0), arr(1), arr(2), arr(3)
+
+    def train(self, gradients, hessians, shrinkage=0.0, scores=None):
+        """One iteration of every learner: gradients / hessians are per learner device pointers
+        ([num_jobs, num_data] f32); scores None or per learner a device f64 score pointer, which
+        receives the new trees' leaf outputs times ``shrinkage``. Returns per learner (splits,
+        leaf_values, root_outputs, num_leaves), arrays the next call overwrites."""
+        count = len(self.learners)
+        gp = (ctypes.c_void_p * count)(*[int(g) for g in gradients])
+        hp = (ctypes.c_void_p * count)(*[int(x) for x in hessians])
+        sc = None if scores is None else (ctypes.c_void_p * count)(*[int(s) for s in scores])
+        _lib.check(self.lib.bk_learner_group_train(self.h, gp, hp, float(shrinkage), sc, self._sp, self._lp, self._rp,
+                                                   self._np), "bk_learner_group_train")
+        return self._outs
+
+    def autotune(self, gradients, hessians, trials=2):
+        """Picks the group's launch policy by timing whole group iterations
+        (bk_learner_group_autotune); returns (launch overlap, rows per histogram CTA, histogram
+        CTAs per member, partition CTAs)."""
+        count = len(self.learners)
+        gp = (ctypes.c_void_p * count)(*[int(g) for g in gradients])
+        hp = (ctypes.c_void_p * count)(*[int(x) for x in hessians])
+        out = np.zeros(4, np.int32)
+        _lib.check(self.lib.bk_learner_group_autotune(self.h, gp, hp, int(trials), out.ctypes.data),
+                   "bk_learner_group_autotune")
+        return tuple(int(x) for x in out)
+
+    def close(self):
+        if self.h:
+            self.lib.bk_learner_group_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

@@ -42,12 +42,13 @@ WORKLOAD = ("L2 regression 10M x 100 (70 N(0,1) + 30 int 0..15, 10% NaN), max_bi
 
 
 # DRAM bytes (read + write) per algorithmic byte of the quantized histogram kernel, from one ncu
-# capture of every k_hist_int launch of one 255-leaf tree on this workload (10M rows):
-#   python bench.py --hist-traffic --rows 10000000 &&
+# capture of every k_hist_int launch of one 255-leaf tree on this workload at 2M rows (the bins,
+# 2M x 128 bytes, are larger than L2; the capture's metrics take one pass):
+#   python bench.py --hist-traffic --rows 2000000 &&
 #   ncu --metrics dram__bytes_read.sum,dram__bytes_write.sum,gpu__time_duration.sum --clock-control none \
-#       -k regex:k_hist_int --csv --log-file ht10.csv python bench.py --hist-traffic --rows 10000000
-# 6.353 GB of DRAM traffic for 4.078 GB of algorithmic bytes over the 254 launches.
-HIST_TRAFFIC_PER_BYTE = 6.353 / 4.078
+#       -k regex:k_hist_int --csv --log-file ht2m.csv python bench.py --hist-traffic --rows 2000000
+# 1.148 GB read + 3.1 MB written for 0.841 GB of algorithmic bytes over the 254 launches.
+HIST_TRAFFIC_PER_BYTE = (1.148e9 + 3.1e6) / 0.841278208e9
 
 
 def _peaks():
@@ -321,8 +322,9 @@ def run_gpu(args, rank, world):
                      "unit": "GB/s", "frac": round(hist_gbs / peak, 4) if hist_gbs else None,
                      "traffic": round(HIST_TRAFFIC_PER_BYTE * roof["hist_bytes"] / hist_launches, 0),
                      "algorithmic_bytes_per_launch": round(roof["hist_bytes"] / hist_launches, 0),
-                     "traffic_source": "ncu capture of one tree's launches (DRAM bytes per algorithmic byte x this "
-                                       "run's algorithmic bytes per launch)",
+                     "traffic_source": "ncu capture of one tree's 254 launches at 2M rows (DRAM bytes per "
+                                       "algorithmic byte, %.3f) x this run's algorithmic bytes per launch"
+                                       % HIST_TRAFFIC_PER_BYTE,
                      "kernel": "k_hist_int (quantized histogram)", "peak_kind": peak_kind},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk,
@@ -357,7 +359,8 @@ def _summary(line):
             "binary_200_iters_per_s": [get(f, "binary_quantized_200", "quantized_graph", "iters_per_s"),
                                        get(f, "binary_quantized_200", "plain_float_stepwise", "iters_per_s")],
             "binary_200_heldout_auc_delta": get(f, "binary_quantized_200", "heldout_auc_delta"),
-            "batched_job_iters_per_s": [get(f, "batched_jobs", "batched", "job_iters_per_s"),
+            "batched_job_iters_per_s": [get(f, "batched_jobs", "group_graph", "job_iters_per_s"),
+                                        get(f, "batched_jobs", "batched", "job_iters_per_s"),
                                         get(f, "batched_jobs", "one_by_one", "job_iters_per_s")],
             "hist_roofline_frac": line["roofline"]["frac"]}
 
@@ -438,11 +441,13 @@ def run_batched_jobs(args):
     uniform in [20, 300] (N(0,1), 1% NaN), logistic labels from per-job random linear models,
     max_bin drawn from {15, 63, 255}, 31 leaves, quantized gradients. Every job has its own
     learner, dataset and stream. One iteration = device binary gradients + one tree + device score
-    update for every job; timed for the jobs one after another (bk_learner_train per job) and for
-    all jobs in one bk_learners_train_batch call per iteration. Host wall clock around each
-    iteration loop, bracketed by device synchronization (the work spans many streams)."""
+    update for every job; timed three ways: the jobs one after another (bk_learner_train per job),
+    all jobs in one bk_learners_train_batch call per iteration (one stream per job), and all jobs
+    as one CUDA graph per iteration (bk_learner_group_train) with the launch policy the group's
+    autotuner picks (bk_learner_group_autotune). Host wall clock around each iteration loop,
+    bracketed by device synchronization (the work spans many streams)."""
     import torch
-    from lgbm_gb300 import BinnedDataset, GpuTreeLearner, LearnerConfig, synthetic, train_batch
+    from lgbm_gb300 import BinnedDataset, GpuTreeLearner, LearnerConfig, LearnerGroup, synthetic, train_batch
     threads = min(32, os.cpu_count() or 8)
     jobs = []
     t0 = time.time()
@@ -470,13 +475,18 @@ def run_batched_jobs(args):
         torch.cuda.synchronize()
         return out
 
-    def run(learners, batched, iters):
+    def run(learners, batched, iters, group=None):
         for L, score, label, _ in learners:
             score.zero_()
         torch.cuda.synchronize()
         t = time.perf_counter()
         for _ in range(iters):
-            if batched:
+            if group is not None:
+                for L, score, label, _ in learners:
+                    L.objective_gradients(1, score.data_ptr(), label.data_ptr())
+                group.train([x[3][0] for x in learners], [x[3][1] for x in learners], shrinkage=0.1,
+                            scores=[x[1].data_ptr() for x in learners])
+            elif batched:
                 for L, score, label, _ in learners:
                     L.objective_gradients(1, score.data_ptr(), label.data_ptr())
                 train_batch([x[0] for x in learners], [x[3][0] for x in learners], [x[3][1] for x in learners],
@@ -501,6 +511,18 @@ def run_batched_jobs(args):
     run(learners, False, 1)
     seq_s, seq_loss = run(learners, False, args.batch_iters)
     bat_s, bat_loss = run(learners, True, args.batch_iters)
+    # one CUDA graph per iteration for all jobs, with the group's autotuned launch policy
+    group = LearnerGroup([x[0] for x in learners])
+    t0 = time.time()
+    for L, score, label, _ in learners:
+        score.zero_()
+        L.objective_gradients(1, score.data_ptr(), label.data_ptr())
+    torch.cuda.synchronize()
+    policy = group.autotune([x[3][0] for x in learners], [x[3][1] for x in learners], trials=2)
+    tune_s = time.time() - t0
+    run(learners, True, 1, group)  # warm-up: the group graph's capture
+    grp_s, grp_loss = run(learners, True, args.batch_iters, group)
+    group.close()
     for L, _, _, _ in learners:
         L.close()
     J, it = len(jobs), args.batch_iters
@@ -511,7 +533,12 @@ def run_batched_jobs(args):
                            "mean_train_logloss": round(seq_loss, 6)},
             "batched": {"job_iters_per_s": round(J * it / bat_s, 2), "s": round(bat_s, 3),
                         "mean_train_logloss": round(bat_loss, 6)},
-            "speedup": round(seq_s / bat_s, 3), "prep_s": round(prep_s, 1),
+            "group_graph": {"job_iters_per_s": round(J * it / grp_s, 2), "s": round(grp_s, 3),
+                            "mean_train_logloss": round(grp_loss, 6),
+                            "policy": {"launch_overlap": policy[0], "hist_min_rows_per_cta": policy[1],
+                                       "hist_ctas_per_job": policy[2], "partition_ctas": policy[3]},
+                            "autotune_s": round(tune_s, 2)},
+            "speedup": round(seq_s / bat_s, 3), "speedup_group": round(seq_s / grp_s, 3), "prep_s": round(prep_s, 1),
             "learner_setup_s": round(setup_s, 2), "autotuned": bool(args.autotune)}
 
 

@@ -70,6 +70,7 @@ typedef struct {
 } bk_split;
 
 typedef struct bk_learner bk_learner;
+typedef struct bk_learner_group bk_learner_group;
 
 /* Replaces SerialTreeLearner::new (serial.rs:284-565). `bins` is column-major uint8
  * [num_features][num_data] of stored bins. `num_jobs` trees are grown per train call over the
@@ -121,6 +122,44 @@ int bk_learners_train_batch(bk_learner* const* learners, int32_t count, const fl
                             const float* const* hessians, int32_t on_device, double shrinkage, double* const* scores,
                             bk_split* const* splits, double* const* leaf_values, double* const* root_outputs,
                             int32_t* const* num_leaves_out);
+
+/* A fixed set of learners whose iterations run as one CUDA graph (GB300-only; the reference's
+ * counterpart is the same as bk_learners_train_batch's: one SerialTreeLearner::train +
+ * add_prediction_to_score per Booster, serial.rs:569-628, :1974-1990). Every learner's iteration
+ * — the grow loop of its trees, the score update, the readback of its results — is one branch of
+ * the graph, issued on the learner's own stream; one graph launch runs all of them with no host
+ * work between their kernels. The learners keep their own datasets, shapes and configs; they must
+ * share one device, appear once, use the graph form (loop mode 1) and have phase timing off when
+ * trained. The graph is captured on the first bk_learner_group_train call and again whenever a
+ * member's launch parameters change (launch shape, overlap, constraints, by-node sampling) or the
+ * call's input pointers or shrinkage differ from the captured ones. A learner of a group may also
+ * be used on its own, but never while a group call that holds it is running. */
+int bk_learner_group_create(bk_learner* const* learners, int32_t count, bk_learner_group** out);
+
+/* One iteration of every learner of the group, as bk_learners_train_batch does it with
+ * on_device = 1: gradients[i] / hessians[i] device f32 [num_jobs][num_data] of learner i,
+ * scores[i] device f64 [num_jobs][num_data] (the array may be NULL: no score update), outputs as in
+ * bk_learners_train_batch. It runs after the work already queued on each member's stream (such as
+ * bk_learner_objective_gradients). Synchronous. */
+int bk_learner_group_train(bk_learner_group* group, const float* const* gradients, const float* const* hessians,
+                           double shrinkage, double* const* scores, bk_split* const* splits,
+                           double* const* leaf_values, double* const* root_outputs, int32_t* const* num_leaves_out);
+
+/* Launch policy of a group, chosen by timing whole group iterations (GB300-only, no reference
+ * counterpart; results never depend on it): for every member the same budget of histogram CTAs
+ * (38, 19, 10 or 5 over all its feature tiles, with at least 1024, 2048, 4096 or 8192 rows each)
+ * and partition CTAs (64, 32, 16 or 8), each with and without programmatic dependent launch — a
+ * smaller budget lets more members' kernels run side by side. Every candidate runs one untimed and
+ * `trials` timed iterations (median) on the given device gradients, without score updates; the
+ * members' job states (their stochastic-rounding engines) are put back afterwards, so call it
+ * before the first bk_learner_group_train. The fastest candidate is applied to every member
+ * (bk_learner_set_launch_shape, bk_learner_set_launch_overlap) and written to policy_out (host,
+ * 4 ints, may be NULL): {launch overlap on, rows per histogram CTA, histogram CTAs per member,
+ * partition CTAs}. */
+int bk_learner_group_autotune(bk_learner_group* group, const float* const* gradients, const float* const* hessians,
+                              int32_t trials, int32_t* policy_out);
+
+int bk_learner_group_destroy(bk_learner_group* group);
 
 /* Replaces SerialTreeLearner::add_prediction_to_score (serial.rs:1974-1990): for every job j
  * and every row r of leaf l of the last tree, score[j][r] += leaf_values[j][l].
@@ -197,6 +236,11 @@ int bk_learner_set_launch_shape(bk_learner* learner, const int32_t* shape);
 /* Replaces SerialTreeLearner::reset_constant_hessian (serial.rs:279). */
 int bk_learner_reset_constant_hessian(bk_learner* learner, int32_t value);
 
+/* Threads per split-search CTA (one CTA per leaf side and feature) of the learner's next train call
+ * (GB300-only): 64 when every feature is numerical with at most 63 searched bins and the grow
+ * loop runs the single-pass form without L1 / max_delta_step / path_smooth, else 256. */
+int bk_learner_search_threads(bk_learner* learner, int32_t* threads);
+
 /* Replaces SerialTreeLearner::histogram_cache_capacity (serial.rs:250-252): the histogram slots
  * the learner keeps, into *capacity (host). This learner always keeps a full pool, one slot per
  * leaf (num_leaves), whatever histogram_pool_size says; the pool size never changes a result. */
@@ -260,13 +304,16 @@ int bk_learner_objective_loss(bk_learner* learner, int32_t kind, const double* s
  * SerialTreeLearner::add_prediction_for_rows (serial.rs:2009-2041) for rows outside the training
  * partition (held-out / out-of-bag rows). The tree is given as the node arrays of
  * tree.rs:310-403 (left_child / right_child with ~leaf for leaves, split_feature_inner,
- * threshold_in_bin, decision_type with the default-left bit 2) plus leaf_value [num_leaves],
- * all host. bins: device uint8 [num_features][num_rows] stored bins of the rows, made with this
- * learner's bin mappers; score: device f64 [num_rows]. */
+ * threshold_in_bin, decision_type with the categorical bit 1 and the default-left bit 2) plus
+ * leaf_value [num_leaves], all host. cat_bins: host [num_leaves - 1][8] uint32, for each
+ * categorical node the bitset of the bin-mapper bins that go left (bk_split.cat_bins; the
+ * categories of Tree::split_categorical mapped to bins), may be NULL when no node is categorical.
+ * bins: device uint8 [num_features][num_rows] stored bins of the rows, made with this learner's
+ * bin mappers; score: device f64 [num_rows]. */
 int bk_learner_predict_add(bk_learner* learner, int32_t num_leaves, const int32_t* left_child,
                            const int32_t* right_child, const int32_t* split_feature_inner,
-                           const uint32_t* threshold_in_bin, const int8_t* decision_type, const double* leaf_value,
-                           const uint8_t* bins, int64_t num_rows, double* score);
+                           const uint32_t* threshold_in_bin, const int8_t* decision_type, const uint32_t* cat_bins,
+                           const double* leaf_value, const uint8_t* bins, int64_t num_rows, double* score);
 
 /* The histogram of one leaf of the last tree, as the learner's histogram pool holds it after the
  * tree (serial.rs:80-162 HistogramPool, with FixHistogram and the parent-minus-child subtraction of

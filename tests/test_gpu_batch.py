@@ -95,3 +95,66 @@ def test_batch_rejects_a_learner_twice():
     with pytest.raises(RuntimeError, match="appears twice"):
         train_batch([gpu, gpu], [g, g], [h, h])
     gpu.close()
+
+
+def test_learner_group_matches_oracle():
+    """The same jobs as one CUDA graph (bk_learner_group_*), after the group's launch-policy
+    autotuner: every quantized tree equals the oracle's bit for bit, the float job's within the
+    float tolerance, the device score update the host's; changing one member's launch shape
+    recaptures the graph and changes no result."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import harness
+    from lgbm_gb300 import GpuTreeLearner, LearnerConfig, LearnerGroup
+    jobs = []
+    for i, (n, F, mb, quant) in enumerate(JOBS):
+        ds, y = _job(i, n, F, mb)
+        cfg = LearnerConfig(num_leaves=31, use_quantized_grad=quant, stochastic_rounding=1, seed=i, num_threads=2)
+        jobs.append(dict(ds=ds, y=y, gpu=GpuTreeLearner(ds, cfg), orc=harness.OracleLearner(ds, cfg),
+                         score=np.zeros(n), dscore=torch.zeros(n, dtype=torch.float64, device="cuda"),
+                         dg=torch.zeros(n, dtype=torch.float32, device="cuda"),
+                         dh=torch.zeros(n, dtype=torch.float32, device="cuda"), quant=quant))
+    group = LearnerGroup([j["gpu"] for j in jobs])
+    # the launch-policy autotuner first: its trial iterations must leave every learner's state
+    # (the stochastic-rounding engines) as it found it, so the trees below still equal the oracle's
+    for j in jobs:
+        g0, h0 = _binary_grads(j["score"], j["y"])
+        j["dg"].copy_(torch.from_numpy(g0))
+        j["dh"].copy_(torch.from_numpy(h0))
+    torch.cuda.synchronize()
+    policy = group.autotune([j["dg"].data_ptr() for j in jobs], [j["dh"].data_ptr() for j in jobs], trials=1)
+    assert policy[0] in (0, 1) and policy[2] in (38, 19, 10, 5), policy
+    float_divergences = []
+    for it in range(4):
+        if it == 2:
+            jobs[2]["gpu"].set_launch_shape((64, 7, 40, 0))  # the group graph is captured anew
+        grads = [_binary_grads(j["score"], j["y"]) for j in jobs]
+        for j, (g, h) in zip(jobs, grads):
+            j["dg"].copy_(torch.from_numpy(g))
+            j["dh"].copy_(torch.from_numpy(h))
+        torch.cuda.synchronize()
+        outs = group.train([j["dg"].data_ptr() for j in jobs], [j["dh"].data_ptr() for j in jobs], shrinkage=0.1,
+                           scores=[j["dscore"].data_ptr() for j in jobs])
+        for j, (g, h), (splits, lv, roots, nls) in zip(jobs, grads, outs):
+            nl = int(nls[0])
+            ro = j["orc"].train(g, h)
+            if j["quant"]:
+                assert len(ro[0]) == nl - 1
+                for name in ro[0].dtype.names:
+                    assert np.array_equal(ro[0][name], splits[0, :nl - 1][name]), (it, name)
+                assert np.array_equal(ro[1], lv[0, :nl])
+                assert np.array_equal(j["orc"].row_leaf(), j["gpu"].row_leaf())
+            else:
+                m = harness.split_match(splits[0, :nl - 1], ro[0])
+                assert m["max_rel"] <= 1e-6, m
+                if m["diverged"]:
+                    float_divergences.append(it)
+            if nl > 1:
+                j["score"] += _round0(lv[0, :nl] * 0.1)[j["gpu"].row_leaf()]
+            assert np.array_equal(j["dscore"].cpu().numpy(), j["score"]), "device score update, iteration %d" % it
+    print("float near-tie divergences (iterations):", float_divergences)
+    assert len(float_divergences) <= 1
+    group.close()
+    for j in jobs:
+        j["gpu"].close()

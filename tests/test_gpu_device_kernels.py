@@ -8,7 +8,8 @@
   weighted objectives; a multiclass label outside [0, K) fails the next train call and the loss
   call instead of indexing the scores;
 * held-out prediction (bk_learner_predict_add, the replay of serial.rs:2009-2041) on upstream's own
-  models and test rows (tests/fixtures/predict: binary, NaN, zero as missing, L2, 3-class): every
+  models and test rows (tests/fixtures/predict: binary, NaN, zero as missing, L2, a categorical
+  feature (bin bitsets), 3-class): every
   row reaches upstream's leaf in every tree (pred_leaf.npy) and the raw scores, the leaf values
   added in tree order on the device, equal upstream's bit for bit (pred_raw.npy).
 """
@@ -23,7 +24,7 @@ from conftest import GOLDEN
 pytestmark = pytest.mark.gpu
 
 PREDICT = os.path.join(GOLDEN, "predict")
-NUMERICAL_CASES = ["binary", "missing", "multiclass", "regression_l2", "zero_as_missing"]
+PREDICT_CASES = ["binary", "categorical", "missing", "multiclass", "regression_l2", "zero_as_missing"]
 
 
 @pytest.fixture(scope="module", autouse=True)
@@ -212,7 +213,7 @@ def test_bad_multiclass_label_is_an_error():
     gpu.close()
 
 
-@pytest.mark.parametrize("case", NUMERICAL_CASES)
+@pytest.mark.parametrize("case", PREDICT_CASES)
 def test_device_prediction_matches_upstream(oracle, bklib, case):
     import torch
     from test_route_golden import _Tree
@@ -223,7 +224,8 @@ def test_device_prediction_matches_upstream(oracle, bklib, case):
     test = np.load(os.path.join(d, "test.npy"))
     want_leaf = np.load(os.path.join(d, "pred_leaf.npy"))
     raw_want = np.load(os.path.join(d, "pred_raw.npy")).reshape(len(test), -1)
-    ds = BinnedDataset.from_dense(train[:, 1:], zero_as_missing=P["params"].get("zero_as_missing", False))
+    ds = BinnedDataset.from_dense(train[:, 1:], zero_as_missing=P["params"].get("zero_as_missing", False),
+                                  categorical=P["dataset"].get("categorical_feature", []))
     held = torch.from_numpy(np.ascontiguousarray(ds.bin_like(test[:, 1:]))).cuda()
     trees = oracle.parse_model_trees(open(os.path.join(d, "model.txt")).read())
     max_leaves = max(int(rec["num_leaves"]) for rec in trees)

@@ -492,3 +492,33 @@ def test_pool_capacity_and_budget_reset():
         assert gpu.histogram_cache_capacity() == 23
         g = (g * 0.9).astype(np.float32)
     gpu.close()
+
+
+@pytest.mark.parametrize("max_bin,nan_frac", [(15, 0.1), (31, 0.0), (63, 0.0)])
+@pytest.mark.parametrize("quant", [1, 0])
+def test_narrow_search_ctas(max_bin, nan_frac, quant):
+    """Learners whose every feature has at most 63 searched bins run the single-pass search in
+    64-thread CTAs (two warps per (leaf side, feature)): the quantized trees equal the oracle's bit
+    for bit and the float trees agree within the float tolerance, as in the 256-thread form (the
+    stepwise form, which keeps 256-thread CTAs, is checked beside it)."""
+    import harness
+    cfg = dict(num_leaves=31, use_quantized_grad=quant, stochastic_rounding=1, seed=6, num_threads=2)
+    ds, z = _dataset(30000, 40, seed=61, max_bin=max_bin, nan_frac=nan_frac)
+    assert max(fi.num_bin for fi in ds.features) <= 64
+    g, h, const = _grads(z, "binary", seed=62)
+    for loop_mode in (1, 0):
+        orc, gpu, _ = _learners(ds, const, loop_mode=loop_mode, **cfg)
+        assert gpu.search_threads() == (64 if loop_mode == 1 else 256)
+        gg = g
+        for it in range(3):
+            ro, rg = orc.train(gg, h), gpu.train(gg, h)
+            if quant:
+                _assert_records_equal(ro[0], rg[0])
+                assert np.array_equal(ro[1], rg[1])
+                assert np.array_equal(orc.row_leaf(), gpu.row_leaf())
+            else:
+                m = harness.split_match(rg[0], ro[0])
+                assert m["max_rel"] <= 1e-6, m
+                assert m["matched"] >= 0.8 * max(len(ro[0]), len(rg[0])), m
+            gg = (gg * 0.9).astype(np.float32)
+        gpu.close()
