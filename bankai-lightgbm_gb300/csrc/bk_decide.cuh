@@ -122,34 +122,76 @@ struct Decision {
   int64_t begin, count;
 };
 
-// The fold of the searched leaves' candidates and the leaf arg-max on one CTA of kDecideThreads
-// threads. Every thread gets the chosen split through `out` (written by thread 0: the caller
+// Shared memory of a split decision.
+struct DecideSmem {
+  Pick f[kDecideWarps], l[kDecideWarps];  // per warp: the fold's and the leaf arg-max's partials
+  // the row range of the first kDecideThreads leaves, so the chosen leaf's is at hand for the
+  // partition that follows
+  int64_t lb[kDecideThreads], lc[kDecideThreads];
+  int32_t lbuf[kDecideThreads], ld[kDecideThreads];
+  int32_t stopped, searched, leaf0, leaf1;
+};
+
+// Part one of a split decision (split_info.rs:125-133): the arg-max over every leaf but the two
+// the current search covers, whose records the histogram launch of this step and earlier steps
+// wrote. A launch that follows the search can run it before its griddep_wait: the search triggers
+// its dependents only after its own wait, so by then the histogram launch has completed; the
+// loads go through L2 (__ldcg). Every thread of the CTA calls it; no barrier.
+__device__ __forceinline__ void decide_leaves(const Job& J, const Params& p, DecideSmem& ds) {
+  const JobState* st = J.st;
+  const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
+  const bool stopped = __ldcg(&st->stop) != 0;
+  const bool searched = __ldcg(&st->do_search) != 0;
+  const int32_t leaf0 = __ldcg(&st->smaller_leaf), leaf1 = __ldcg(&st->larger_leaf);
+  if (t == 0) {
+    ds.stopped = stopped;
+    ds.searched = searched;
+    ds.leaf0 = leaf0;
+    ds.leaf1 = leaf1;
+  }
+  Pick b{-1, 0, 0, false, 0.0, 0};
+  for (int i = t; i < p.num_leaves; i += kDecideThreads) {
+    if (i < kDecideThreads) {
+      ds.lb[i] = __ldcg(&J.leaf_begin[i]);
+      ds.lc[i] = __ldcg(&J.leaf_count[i]);
+      ds.lbuf[i] = __ldcg(&J.leaf_buf[i]);
+      ds.ld[i] = __ldcg(&J.leaf_depth[i]);
+    }
+    const double bg = __ldcg(&J.bgain[i]);
+    const int32_t bf = __ldcg(&J.bfeat[i]);
+    const int64_t bs = __ldcg(&J.bsplit[i]);
+    if (searched && (i == leaf0 || i == leaf1)) continue;
+    leaf_pick(b, make_pick(i, bg, bf, bs));
+  }
+  if (__any_sync(FULL, b.i >= 0 && b.nan)) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) leaf_pick(b, shfl_pick(b, o, true));
+  } else {
+    b = warp_argmax(b, b.i >= 0, lane);
+  }
+  if (lane == 0) ds.l[warp] = b;
+}
+
+// Part two (serial.rs:1523-1558, split_info.rs:125-133, serial.rs:611): the fold of the searched
+// leaves' candidates in feature order (the first half of the CTA folds the smaller leaf, the second
+// half the larger one), then the leaf arg-max over part one's partials and the searched leaves'
+// new bests. Every thread gets the chosen split through `out` (written by thread 0: the caller
 // synchronizes before reading it). With `record`, the decision's effects are written to the job:
 // the searched leaves' new bests and splittable flags, the chosen split (the row range, depth and
 // new pool slot the partition and the next histogram launch use) or the stop flag; without it
-// nothing is written, so several CTAs can decide the same split from the same records. Every load
-// is issued up front (the candidates of both searched leaves and every other leaf's best), then
-// one barrier; warp 0 finishes. Candidates written by other CTAs are read through L2 (__ldcg). A
-// leaf's best split stays in cand[leaf][feature]; the partition builds the route table of the
-// chosen split from (inner, thr). A stopped tree (the stop flag is loaded with everything else, so
-// the caller need not test it first) gives out->stop = 1 and writes nothing.
-__device__ void decide_split(const Job& J, const Params& p, const DevFeature* feats, bool record, Decision* out) {
-  __shared__ Pick s_f[kDecideWarps], s_l[kDecideWarps];
-  // the row range of the first kDecideThreads leaves, so the chosen leaf's is at hand for the
-  // partition that follows
-  __shared__ int64_t s_lb[kDecideThreads], s_lc[kDecideThreads];
-  __shared__ int32_t s_lbuf[kDecideThreads], s_ld[kDecideThreads];
+// nothing is written, so several CTAs can decide the same split from the same records. Candidates
+// written by other CTAs are read through L2 (__ldcg). A leaf's best split stays in
+// cand[leaf][feature]; the partition builds the route table of the chosen split from (inner,
+// thr). A stopped tree gives out->stop = 1 and writes nothing. Call after decide_leaves and a
+// barrier.
+__device__ void decide_finish(const Job& J, const Params& p, const DevFeature* feats, bool record, Decision* out,
+                              DecideSmem& ds) {
   JobState* st = J.st;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
   constexpr int kHalf = kDecideThreads / 2;
-  const bool stopped = st->stop != 0;
-  const bool searched = st->do_search != 0;
-  const int32_t leaf0 = st->smaller_leaf, leaf1 = st->larger_leaf;
+  const bool stopped = ds.stopped != 0, searched = ds.searched != 0;
+  const int32_t leaf0 = ds.leaf0, leaf1 = ds.leaf1;
   const Pick none{-1, 0x7fffffff, 0, false, 0.0, 0};
-  // serial.rs:1523-1558 — fold the candidates of each searched leaf in feature order: the first
-  // half of the CTA folds the smaller leaf, the second half the larger one
-  // the candidate and leaf loads do not depend on the state: issued together with its loads, so
-  // the fold and the arg-max wait for one memory round trip
   Pick a = none;
   {
     const int side = t / kHalf;
@@ -168,35 +210,9 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
       if (nm) pick(a, make_pick(f, g, real, th));
     }
   }
-  // split_info.rs:125-133 — first arg-max leaf under better_than; the searched leaves' new bests
-  // join from the fold
-  Pick b = none;
-  b.f = 0;
-  for (int i = t; i < p.num_leaves; i += kDecideThreads) {
-    if (i < kDecideThreads) {
-      s_lb[i] = J.leaf_begin[i];
-      s_lc[i] = J.leaf_count[i];
-      s_lbuf[i] = J.leaf_buf[i];
-      s_ld[i] = J.leaf_depth[i];
-    }
-    const double bg = J.bgain[i];
-    const int32_t bf = J.bfeat[i];
-    const int64_t bs = J.bsplit[i];
-    if (searched && (i == leaf0 || i == leaf1)) continue;
-    leaf_pick(b, make_pick(i, bg, bf, bs));
-  }
   // the fold never adopts a NaN gain, so its order is total
   if (searched) a = warp_argmax(a, a.i >= 0, lane);
-  if (__any_sync(FULL, b.i >= 0 && b.nan)) {
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) leaf_pick(b, shfl_pick(b, o, true));
-  } else {
-    b = warp_argmax(b, b.i >= 0, lane);
-  }
-  if (lane == 0) {
-    s_f[warp] = a;
-    s_l[warp] = b;
-  }
+  if (lane == 0) ds.f[warp] = a;
   __syncthreads();
   if (warp != 0) return;
   if (stopped) {
@@ -208,7 +224,7 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
   const int32_t my_leaf = lane == 0 ? leaf0 : leaf1;
   if (searched && lane < 2 && my_leaf >= 0) {
     Pick fa = none;
-    for (int w = lane * (kDecideWarps / 2); w < (lane + 1) * (kDecideWarps / 2); ++w) pick(fa, s_f[w]);
+    for (int w = lane * (kDecideWarps / 2); w < (lane + 1) * (kDecideWarps / 2); ++w) pick(fa, ds.f[w]);
     // the fold starts from SplitInfo::default (gain -inf, feature -1) and replaces it only with a
     // better candidate
     const bool take = fa.i >= 0 && better_k(fa.k, fa.nan, fa.f, dkey(-CUDART_INF), false, -1);
@@ -224,7 +240,7 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
   }
   // the leaf arg-max over the 8 warp partials (lanes 0..7) and the searched leaves (lanes 8, 9)
   const Pick moved = shfl_pick(nb, lane & 1, false);
-  Pick w = lane < kDecideWarps ? s_l[lane] : ((lane == 8 || lane == 9) ? moved : none);
+  Pick w = lane < kDecideWarps ? ds.l[lane] : ((lane == 8 || lane == 9) ? moved : none);
   if (__any_sync(FULL, w.i >= 0 && w.nan)) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) leaf_pick(w, shfl_pick(w, o, true));
@@ -247,10 +263,10 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
     d.leaf = w.i;
     d.inner = inner;
     d.thr = (uint32_t)(w.pay & 0xffffffffLL);
-    d.begin = near ? s_lb[w.i] : J.leaf_begin[w.i];
-    d.count = near ? s_lc[w.i] : J.leaf_count[w.i];
-    d.buf = near ? s_lbuf[w.i] : J.leaf_buf[w.i];
-    d.depth = near ? s_ld[w.i] : J.leaf_depth[w.i];
+    d.begin = near ? ds.lb[w.i] : __ldcg(&J.leaf_begin[w.i]);
+    d.count = near ? ds.lc[w.i] : __ldcg(&J.leaf_count[w.i]);
+    d.buf = near ? ds.lbuf[w.i] : __ldcg(&J.leaf_buf[w.i]);
+    d.depth = near ? ds.ld[w.i] : __ldcg(&J.leaf_depth[w.i]);
     d.sslot = st->next_free;
     d.new_leaf = st->tree_leaves;
     *out = d;
@@ -268,6 +284,13 @@ __device__ void decide_split(const Job& J, const Params& p, const DevFeature* fe
   }
 }
 
+// The whole decision on one CTA of kDecideThreads threads (the stable path's last search CTA).
+__device__ void decide_split(const Job& J, const Params& p, const DevFeature* feats, bool record, Decision* out) {
+  __shared__ DecideSmem ds;
+  decide_leaves(J, p, ds);
+  __syncthreads();
+  decide_finish(J, p, feats, record, out, ds);
+}
 
 }  // namespace
 

@@ -275,10 +275,16 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
   __shared__ int64_t s_off[2];
   __shared__ Decision dec;
   __shared__ uint2 s_route[kRoutePrefetch];
+  __shared__ DecideSmem ds;
   // static: every feature's route descriptor, read while the search finishes
   const bool prefetched = p.F <= kRoutePrefetch;
   if (prefetched)
     for (int f = threadIdx.x; f < p.F; f += kThreads) s_route[f] = route_desc(feats[f]);
+  // the leaf arg-max over the leaves the search does not cover, while the search runs (their
+  // records come from the histogram launch of this step and earlier, complete by the time the
+  // search lets this launch start)
+  const Job& Jpre = jobs.job[blockIdx.z];
+  if (decide) decide_leaves(Jpre, p, ds);
   griddep_wait();
   // the next histogram launch may be scheduled now: its CTAs zero their shared histograms while
   // this partition runs, and wait for its completion before reading anything it writes
@@ -287,8 +293,9 @@ __global__ void __launch_bounds__(kThreads) k_part_onepass(const JobTable jobs, 
   JobState* st = J.st;
   if (decide) {
     // every CTA decides the split from the search's records (a stopped tree included: the stop
-    // flag comes with the records' loads); CTA 0 records it
-    decide_split(J, p, feats, blockIdx.x == 0, &dec);
+    // flag comes with part one's loads); CTA 0 records it
+    __syncthreads();
+    decide_finish(J, p, feats, blockIdx.x == 0, &dec, ds);
   } else if (threadIdx.x == 0) {
     dec = recorded_decision(st);
   }
