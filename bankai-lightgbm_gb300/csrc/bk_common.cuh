@@ -233,6 +233,8 @@ struct HistLaunch {
   int flush_rounds;  // quantized: rounds of 32*warps rows between 16-bit -> 32-bit flushes (0: wide)
   int direct_rows;   // quantized: a CTA with at most this many rows adds each (row, feature) to the
                      // pool slot with a global atomic instead of through a shared histogram
+  int cluster = 1;   // quantized: CTAs of a tile per thread-block cluster, which add up their shared
+                     // histograms through distributed shared memory before one flush (1: none)
 };
 // BinsCheck over device columns: the smallest flat index (feature * n + row) of a stored bin
 // outside its feature's range, or INT64_MAX (bk_binning.cu). Synchronizes `s`.

@@ -54,12 +54,14 @@ struct Range {
   bool direct, pk_row;
 };
 
-// The smaller leaf's rows for this CTA (false: none). With `post`, the previous split's
-// single-pass partition left its bookkeeping to this launch: the range comes from the split's
-// outcome (bk_grow.cuh), and the side CTA writes the bookkeeping and the leaf constants.
-// Otherwise it comes from the job state and the side CTA computes the constants.
-__device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blocks_per_tile, int post, int par,
-                                          Range* r) {
+// The smaller leaf's rows for this CTA: 1 with rows, 2 without rows for this CTA (r->slot set),
+// 0 when the job builds no histogram in this launch (the same for every CTA of the job). With
+// `post`, the previous split's single-pass partition left its bookkeeping to this launch: the
+// range comes from the split's outcome (bk_grow.cuh), and the side CTA writes the bookkeeping and
+// the leaf constants. Otherwise it comes from the job state and the side CTA computes the
+// constants.
+__device__ __forceinline__ int cta_range(const Job& J, const Params& p, int blocks_per_tile, int post, int par,
+                                         Range* r) {
   const JobState* st = J.st;
   // the stop flag is loaded with the rest of the state (one round of independent loads)
   const int32_t stop = st->stop;
@@ -67,9 +69,9 @@ __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blo
   int32_t buf;
   if (post) {
     const SplitOutcome o = split_outcome(p, st, __ldcg(&st->pcnt[par][0]));
-    if (stop) return false;
+    if (stop) return 0;
     hist_apply_split(J, p, o);
-    if (!o.go) return false;
+    if (!o.go) return 0;
     begin = o.hist_begin();
     count = o.hist_count();
     buf = o.nbuf;
@@ -80,9 +82,9 @@ __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blo
     begin = st->hist_begin;
     count = st->hist_count;
     buf = st->hist_buf;
-    if (stop) return false;
+    if (stop) return 0;
     hist_leaf_constants(J, p);
-    if (!do_search) return false;
+    if (!do_search) return 0;
     r->slot = slot;
     r->pk_row = leaves == 1;  // the root: no leaf-ordered copy yet
   }
@@ -95,13 +97,13 @@ __device__ __forceinline__ bool cta_range(const Job& J, const Params& p, int blo
   if (chunk < p.hist_min_rows) chunk = p.hist_min_rows;
   chunk = (chunk + 31) / 32 * 32;
   r->r0 = (int64_t)blockIdx.x * chunk;
-  if (r->r0 >= count) return false;
+  if (r->r0 >= count) return 2;
   r->r1 = min(count, r->r0 + chunk);
   r->count = count;
   r->idx = leaf_idx(J, buf) + begin;
   r->direct = (count == p.n);  // all rows in order: the index buffer is the identity
   r->pk = r->pk_row ? J.packed : (J.pk0 ? leaf_pk(J, buf) + begin : nullptr);
-  return true;
+  return 1;
 }
 
 // The rows of a warp's round are fetched in two stages, each one round ahead of its use: the row
@@ -170,7 +172,7 @@ __device__ __forceinline__ void add_row(uint32_t* hot, int32_t* cold_g, int32_t*
 template <bool WIDE, bool NIBBLE>
 __device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, const Range& R, const TileGeom& geo,
                                               const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
-                                              int flush_rounds, int direct_rows, unsigned char* smem) {
+                                              int flush_rounds, int direct_rows, bool in_cluster, unsigned char* smem) {
   const int tile = blockIdx.y;
   const int Bt = geo.bins;
   const bool half = geo.width == 16;  // one 16-byte run per row
@@ -182,7 +184,8 @@ __device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, con
   int32_t* stage_v = reinterpret_cast<int32_t*>(stage + nwarps * 64);
   unsigned long long* slot = reinterpret_cast<unsigned long long*>(J.pool) +
                              ((size_t)R.slot * p.T + tile) * (size_t)p.B * TILE;
-  const bool direct = R.r1 - R.r0 <= (int64_t)direct_rows;  // uniform over the CTA
+  // uniform over the CTA; a CTA of a cluster always adds through its shared histogram
+  const bool direct = !in_cluster && R.r1 - R.r0 <= (int64_t)direct_rows;
   __syncthreads();
   // the tile's run of row 0 and the row stride, in the copy that suits the leaf's density
   const bool dense = R.count * 4 >= p.n;
@@ -269,7 +272,7 @@ __device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, con
       __syncthreads();
     }
   }
-  if (direct) return;
+  if (direct || in_cluster) return;  // a cluster flushes its CTAs' histograms together
   __syncthreads();
   for (int e = threadIdx.x; e < Bt * TILE; e += blockDim.x) {
     int32_t gg = cold_g[e], hh = cold_h[e];
@@ -283,6 +286,68 @@ __device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, con
       atomicAdd(slot + e, (unsigned long long)pk);
     }
   }
+}
+
+// The flush of a thread-block cluster of `ncta` CTAs of one feature tile: every CTA folds its
+// 16:16 counters into its 32-bit ones, then (after a cluster barrier) CTA `rank` adds up its
+// 1/ncta share of the tile's bins over every CTA's shared histogram through distributed shared
+// memory and adds the non-zero sums to the pool slot — ncta times fewer global atomics than a
+// flush per CTA. A second cluster barrier keeps every CTA's shared memory alive until the others
+// have read it. Every CTA of the cluster calls it, with or without rows of its own (a CTA without
+// rows contributes its zeroed histogram). Integer sums: the slot gets the same values.
+template <bool WIDE>
+__device__ __forceinline__ void hist_cluster_flush(const Params& p, const TileGeom& geo, unsigned long long* slot,
+                                                   uint32_t ncta, unsigned char* smem) {
+  const int Bt = geo.bins;
+  uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
+  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + (WIDE ? 0 : Bt * TILE));
+  int32_t* cold_h = cold_g + Bt * TILE;
+  const int n4 = Bt * TILE / 4;  // int4 groups of the tile's bins: a multiple of 64 (Bt a multiple of 8)
+  __syncthreads();
+  if (!WIDE) {
+    const uint4* hot4 = reinterpret_cast<const uint4*>(hot);
+    int4* g4 = reinterpret_cast<int4*>(cold_g);
+    int4* h4 = reinterpret_cast<int4*>(cold_h);
+    for (int e = threadIdx.x; e < n4; e += blockDim.x) {
+      const uint4 s = hot4[e];
+      if (s.x | s.y | s.z | s.w) {
+        int4 g = g4[e], h = h4[e];
+        g.x += hot_g(s.x);
+        g.y += hot_g(s.y);
+        g.z += hot_g(s.z);
+        g.w += hot_g(s.w);
+        h.x += (int32_t)(s.x & 0xffffu);
+        h.y += (int32_t)(s.y & 0xffffu);
+        h.z += (int32_t)(s.z & 0xffffu);
+        h.w += (int32_t)(s.w & 0xffffu);
+        g4[e] = g;
+        h4[e] = h;
+      }
+    }
+  }
+  cluster_sync_all();
+  const uint32_t rank = cluster_ctarank();
+  const int per = n4 / (int)ncta;
+  for (int e = (int)rank * per + threadIdx.x; e < ((int)rank + 1) * per; e += blockDim.x) {
+    int4 g = make_int4(0, 0, 0, 0), h = make_int4(0, 0, 0, 0);
+    for (uint32_t q = 0; q < ncta; ++q) {
+      const int4 a = ld_dsmem_v4(cold_g + 4 * e, q), b = ld_dsmem_v4(cold_h + 4 * e, q);
+      g.x += a.x;
+      g.y += a.y;
+      g.z += a.z;
+      g.w += a.w;
+      h.x += b.x;
+      h.y += b.y;
+      h.z += b.z;
+      h.w += b.w;
+    }
+    const int32_t gg[4] = {g.x, g.y, g.z, g.w}, hh[4] = {h.x, h.y, h.z, h.w};
+#pragma unroll
+    for (int k = 0; k < 4; ++k)
+      if (gg[k] | hh[k])
+        atomicAdd(slot + 4 * e + k, (unsigned long long)((int64_t)gg[k] * 4294967296LL + (int64_t)hh[k]));
+  }
+  cluster_sync_all();
 }
 
 template <bool WIDE>
@@ -303,11 +368,22 @@ __global__ void __launch_bounds__(1024, 1)
   griddep_launch();
   const Job& J = jobs.job[blockIdx.z];
   Range R;
-  if (!cta_range(J, p, blocks_per_tile, post, par, &R)) return;
-  if (geo.nibble)
-    hist_int_rows<WIDE, true>(J, p, R, geo, bins_rt, bins_tm, flush_rounds, direct_rows, smem);
-  else
-    hist_int_rows<WIDE, false>(J, p, R, geo, bins_rt, bins_tm, flush_rounds, direct_rows, smem);
+  // a cluster's CTAs belong to one job and tile, so code 0 is the same for all of them; every
+  // other CTA of a cluster reaches both cluster barriers of the flush
+  const uint32_t ncta = cluster_nctarank();
+  const int rc = cta_range(J, p, blocks_per_tile, post, par, &R);
+  if (rc == 0 || (rc == 2 && ncta == 1)) return;
+  if (rc == 1) {
+    if (geo.nibble)
+      hist_int_rows<WIDE, true>(J, p, R, geo, bins_rt, bins_tm, flush_rounds, direct_rows, ncta > 1, smem);
+    else
+      hist_int_rows<WIDE, false>(J, p, R, geo, bins_rt, bins_tm, flush_rounds, direct_rows, ncta > 1, smem);
+  }
+  if (ncta > 1) {
+    unsigned long long* slot = reinterpret_cast<unsigned long long*>(J.pool) +
+                               ((size_t)R.slot * p.T + blockIdx.y) * (size_t)p.B * TILE;
+    hist_cluster_flush<WIDE>(p, geo, slot, ncta, smem);
+  }
 }
 
 // The rows and flush of one float-histogram CTA, its range known (NIBBLE: the tile holds 4-bit
@@ -419,7 +495,7 @@ __global__ void __launch_bounds__(1024, 1)
   griddep_launch();
   const Job& J = jobs.job[blockIdx.z];
   Range R;
-  if (!cta_range(J, p, blocks_per_tile, post, par, &R)) return;
+  if (cta_range(J, p, blocks_per_tile, post, par, &R) != 1) return;
   if (geo.nibble)
     hist_float_rows<CONST_HESS, true>(J, p, R, geo, bins_rt, bins_tm, smem);
   else
@@ -443,11 +519,11 @@ void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t
     dim3 grid(hl.blocks_per_tile, p.T, nz);
     if (p.quant) {
       if (hl.flush_rounds > 0)
-        (void)launch_kernel(k_hist_int<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
-                            hl.blocks_per_tile, hl.flush_rounds, hl.direct_rows, post, par);
+        (void)launch_kernel_cluster(k_hist_int<false>, grid, dim3(hl.threads), hl.smem, s, p.pdl, hl.cluster, t, p,
+                                    bins_rt, bins_tm, hl.blocks_per_tile, hl.flush_rounds, hl.direct_rows, post, par);
       else
-        (void)launch_kernel(k_hist_int<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
-                            hl.blocks_per_tile, 1, hl.direct_rows, post, par);
+        (void)launch_kernel_cluster(k_hist_int<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, hl.cluster, t, p,
+                                    bins_rt, bins_tm, hl.blocks_per_tile, 1, hl.direct_rows, post, par);
     } else if (p.const_hess) {
       (void)launch_kernel(k_hist_float<true>, grid, dim3(hl.threads), hl.smem, s, p.pdl, t, p, bins_rt, bins_tm,
                           hl.blocks_per_tile, post, par);

@@ -213,12 +213,18 @@ struct bk_learner {
   // leaf never has more rows than the dataset, so CTAs past n / min_rows would never get rows.
   // Results do not depend on it (integer histograms are exact; the float path changes only its
   // rounding order; the partitions it feeds are the same). The graph is captured anew.
-  void set_launch_shape(int hist_min_rows, int hist_ctas_per_tile, int part_grid, int direct_rows) {
+  void set_launch_shape(int hist_min_rows, int hist_ctas_per_tile, int part_grid, int direct_rows, int cluster) {
     const int64_t n = p.n;
     hl.direct_rows = std::max(0, direct_rows);
     p.hist_min_rows = std::max(32, hist_min_rows / 32 * 32);
     hl.blocks_per_tile = (int)std::max<int64_t>(
         1, std::min<int64_t>(hist_ctas_per_tile, (n + p.hist_min_rows - 1) / p.hist_min_rows));
+    // a cluster of 2, 4 or 8 CTAs of one tile (quantized path): the tile's CTAs a multiple of it
+    hl.cluster = 1;
+    if (p.quant && cluster >= 2) {
+      hl.cluster = cluster >= 8 ? 8 : (cluster >= 4 ? 4 : 2);
+      hl.blocks_per_tile = std::max(hl.cluster, hl.blocks_per_tile / hl.cluster * hl.cluster);
+    }
     p.part_grid = (int)std::max<int64_t>(1, std::min<int64_t>(std::min(part_grid, kMaxPartGrid), (n + 255) / 256));
     drop_graph();
   }
@@ -228,6 +234,7 @@ struct bk_learner {
     out[1] = hl.blocks_per_tile;
     out[2] = p.part_grid;
     out[3] = hl.direct_rows;
+    out[4] = hl.cluster;
   }
 
   bool capturing = false;
@@ -465,7 +472,7 @@ int learner_create(const bk_feature* features, int32_t num_features, const uint8
     // tiles, each taking at least 256 rows; two partition CTAs per SM; no more CTAs than the
     // dataset's rows can fill; no direct-atomic CTAs (bk_learner_autotune may change all four)
     L->hl.threads = 1024;
-    L->set_launch_shape(256, L->num_sms / p.T, 2 * L->num_sms, 0);
+    L->set_launch_shape(256, L->num_sms / p.T, 2 * L->num_sms, 0, 1);
     bool wide = false;
     if (quant) {
       int max_h = p.const_hess ? 1 : p.quant_bins;
@@ -769,7 +776,7 @@ namespace {
 // Autotuned launch shapes by shape class: (device, log2 rows, feature tiles, bins per feature
 // slot, quantized, num_leaves, jobs) -> (hist_min_rows, hist CTAs per tile, partition CTAs).
 std::mutex g_tune_mutex;
-std::map<std::array<int, 7>, std::array<int, 4>> g_tune_cache;
+std::map<std::array<int, 7>, std::array<int, 5>> g_tune_cache;
 
 std::array<int, 7> tune_key(const bk_learner* L) {
   int lg = 0;
@@ -790,7 +797,7 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
     std::lock_guard<std::mutex> g(g_tune_mutex);
     auto it = g_tune_cache.find(key);
     if (it != g_tune_cache.end()) {
-      L->set_launch_shape(it->second[0], it->second[1], it->second[2], it->second[3]);
+      L->set_launch_shape(it->second[0], it->second[1], it->second[2], it->second[3], it->second[4]);
       if (shape_out) L->shape_of(shape_out);
       return 0;
     }
@@ -809,11 +816,12 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
     if (gradients != L->d_g) CK(cudaMemcpyAsync(L->d_g, gradients, n * sizeof(float), kind, L->stream));
     if (hessians != L->d_h) CK(cudaMemcpyAsync(L->d_h, hessians, n * sizeof(float), kind, L->stream));
     L->loop_mode = 1;
-    std::map<std::array<int, 4>, double> seen;
+    std::map<std::array<int, 5>, double> seen;
     // one tree per trial (graph form) after one untimed tree of each shape; the median device time
-    auto measure = [&](const std::array<int, 4>& c) -> std::pair<std::array<int, 4>, double> {
-      L->set_launch_shape(c[0], c[1], c[2], c[3]);
-      std::array<int, 4> s = {L->p.hist_min_rows, L->hl.blocks_per_tile, L->p.part_grid, L->hl.direct_rows};
+    auto measure = [&](const std::array<int, 5>& c) -> std::pair<std::array<int, 5>, double> {
+      L->set_launch_shape(c[0], c[1], c[2], c[3], c[4]);
+      std::array<int, 5> s = {L->p.hist_min_rows, L->hl.blocks_per_tile, L->p.part_grid, L->hl.direct_rows,
+                              L->hl.cluster};
       auto f = seen.find(s);
       if (f != seen.end()) return {s, f->second};
       std::vector<double> t;
@@ -829,9 +837,9 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
     };
     // coordinate descent from the default shape: rows per histogram CTA, histogram CTAs per
     // feature tile, partition CTAs
-    std::array<int, 4> best = {256, sms / T, 2 * sms, 0};
+    std::array<int, 5> best = {256, sms / T, 2 * sms, 0, 1};
     double best_ms = measure(best).second;
-    auto consider = [&](std::array<int, 4> c) {
+    auto consider = [&](std::array<int, 5> c) {
       auto r = measure(c);
       if (r.second < best_ms) {
         best_ms = r.second;
@@ -840,18 +848,21 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
     };
     // rows per histogram CTA: small values spread small leaves over more SMs; large ones give
     // mid-size leaves fewer CTAs, so fewer shared histograms to flush into the pool slot
-    for (int mr : {64, 128, 512, 1024, 2048, 4096, 8192, 16384}) consider({mr, best[1], best[2], best[3]});
-    for (int ct : {2 * sms / T, sms / (2 * T)}) consider({best[0], ct, best[2], best[3]});
-    for (int pg : {sms, 4 * sms}) consider({best[0], best[1], pg, best[3]});
-    // the global-atomic variant of the quantized histogram for CTAs with few rows
-    if (L->p.quant)
-      for (int dr : {128, 256, 512, 1024, 2048}) consider({best[0], best[1], best[2], dr});
+    for (int mr : {64, 128, 512, 1024, 2048, 4096, 8192, 16384}) consider({mr, best[1], best[2], best[3], best[4]});
+    for (int ct : {2 * sms / T, sms / (2 * T)}) consider({best[0], ct, best[2], best[3], best[4]});
+    for (int pg : {sms, 4 * sms}) consider({best[0], best[1], pg, best[3], best[4]});
+    if (L->p.quant) {
+      // the global-atomic variant of the quantized histogram for CTAs with few rows
+      for (int dr : {128, 256, 512, 1024, 2048}) consider({best[0], best[1], best[2], dr, best[4]});
+      // clusters of a tile's CTAs that add up their histograms in distributed shared memory
+      for (int cl : {2, 4}) consider({best[0], best[1], best[2], best[3], cl});
+    }
     CK(cudaMemcpyAsync(L->jobs[0].st, saved, state_bytes, cudaMemcpyDeviceToDevice, L->stream));
     CK(cudaFreeAsync(saved, L->stream));
     saved = nullptr;
     CK(cudaStreamSynchronize(L->stream));
     L->loop_mode = saved_mode;
-    L->set_launch_shape(best[0], best[1], best[2], best[3]);
+    L->set_launch_shape(best[0], best[1], best[2], best[3], best[4]);
     {
       std::lock_guard<std::mutex> g(g_tune_mutex);
       g_tune_cache[key] = best;
@@ -871,11 +882,12 @@ int bk_learner_autotune(bk_learner* L, const float* gradients, const float* hess
 }
 
 int bk_learner_set_launch_shape(bk_learner* L, const int32_t* shape) {
-  if (!L || !shape || shape[0] < 32 || shape[1] < 1 || shape[2] < 1 || shape[3] < 0) {
+  if (!L || !shape || shape[0] < 32 || shape[1] < 1 || shape[2] < 1 || shape[3] < 0 || shape[4] < 0 ||
+      shape[4] > 8) {
     set_error("bk_learner_set_launch_shape: invalid arguments");
     return -1;
   }
-  L->set_launch_shape(shape[0], shape[1], shape[2], shape[3]);
+  L->set_launch_shape(shape[0], shape[1], shape[2], shape[3], shape[4]);
   return 0;
 }
 
@@ -1170,7 +1182,7 @@ int bk_learner_group_autotune(bk_learner_group* G, const float* const* gradients
   std::vector<JobState*> saved(count, nullptr);
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   std::vector<uint8_t> pdl0(count);
-  std::vector<std::array<int, 4>> shape0(count);
+  std::vector<std::array<int, 5>> shape0(count);
   for (size_t i = 0; i < count; ++i) {
     pdl0[i] = (uint8_t)G->learners[i]->p.pdl;
     G->learners[i]->shape_of(shape0[i].data());
@@ -1181,7 +1193,7 @@ int bk_learner_group_autotune(bk_learner_group* G, const float* const* gradients
         L->p.pdl = pdl;
         L->drop_graph();
       }
-      L->set_launch_shape(kCand[c][0], std::max(1, kCand[c][1] / L->p.T), kCand[c][2], 0);
+      L->set_launch_shape(kCand[c][0], std::max(1, kCand[c][1] / L->p.T), kCand[c][2], 0, 1);
     }
   };
   try {
@@ -1251,7 +1263,7 @@ int bk_learner_group_autotune(bk_learner_group* G, const float* const* gradients
         L->p.pdl = pdl0[i];
         L->drop_graph();
       }
-      L->set_launch_shape(shape0[i][0], shape0[i][1], shape0[i][2], shape0[i][3]);
+      L->set_launch_shape(shape0[i][0], shape0[i][1], shape0[i][2], shape0[i][3], shape0[i][4]);
     }
     for (JobState* x : saved) cudaFree(x);
     if (e0) cudaEventDestroy(e0);

@@ -250,54 +250,59 @@ __device__ __forceinline__ Eval eval_float(const Params& p, int d, double ag, do
   return v;
 }
 
-// One side of a queued position, as one lane evaluates it: the side's share of the split gain
-// (GetLeafGain of that side, feature_histogram.rs:148-176 / simd.rs:6-8), and the side's sums,
-// count and output for the SplitInfo (feature_histogram.rs:240-357, :700-830).
+// One quarter of a queued position's evaluation, as one lane computes it (plain gains: no L1,
+// max_delta_step or path_smooth). Role 0 / 1: the left / right leaf gain (simd.rs:6-8,
+// feature_histogram.rs:148-176: left + right = the split gain, in that order); role 2 / 3: the
+// left / right output (feature_histogram.rs:79-104) with the side's SplitInfo sums and count
+// (feature_histogram.rs:240-357, :700-830). Both are one division, num / (den + lambda_l2), so all
+// four lanes run the same instructions: gain = g^2 / (h + l2), output = -g / (h + l2).
 struct SidePart {
-  double gain;   // the side's leaf gain (left + right = the split gain, in that order)
-  double sg, sh;  // the side's sums as the SplitInfo stores them
-  double out;     // the side's output
-  int32_t n;      // the side's count
+  double val;     // the leaf gain (roles 0, 1) or the output (roles 2, 3)
+  double sg, sh;  // the side's sums as the SplitInfo stores them (roles 2, 3)
+  int32_t n;      // the side's count (roles 2, 3)
 };
 
-// Side s (0: left, 1: right) of an integer threshold with left sums (lg, lh): its share of
-// GetSplitGains (feature_histogram.rs:878-925: the hessian gets kEpsilon added) and its SplitInfo
-// sums, count and output exactly as int_split_gain and eval_int compute them.
+// Role `role` of an integer threshold with left sums (lg, lh): the hessian gets kEpsilon added for
+// the gain (feature_histogram.rs:878-925), the output and the SplitInfo use the plain sums, the
+// counts are round_int(hess * cnt_factor) — exactly as int_split_gain and eval_int compute them.
 __device__ __forceinline__ SidePart int_side(const Params& p, int64_t lg, int64_t lh, int64_t tg, int64_t th,
-                                             double gs, double hs, double cnt_factor, double parent, int s) {
-  const int64_t sg = s == 0 ? lg : tg - lg, sh = s == 0 ? lh : th - lh;
+                                             double gs, double hs, double cnt_factor, int role) {
+  const bool right = (role & 1) != 0, gain = role < 2;
+  const int64_t sg = right ? tg - lg : lg, sh = right ? th - lh : lh;
   const double dg = (double)(int32_t)sg * gs, dh = (double)(uint32_t)sh * hs;
-  const int32_t n = round_int((double)(uint32_t)sh * cnt_factor);
   SidePart r;
-  r.gain = leaf_gain(p, dg, dh + BK_EPS, n, parent);
+  r.n = round_int((double)(uint32_t)sh * cnt_factor);
+  const double sq = dg * dg;
+  const double he = dh + BK_EPS;
+  const double num = gain ? sq : -dg;
+  const double den = (gain ? he : dh) + p.l2;
+  r.val = num / den;
   r.sg = dg;
   r.sh = dh;
-  r.n = n;
-  r.out = split_output(p, dg, dh, n, parent);
   return r;
 }
 
-// Side s of a float threshold of direction d with accumulated sums (ag, ah, c): its share of the
-// split gain with the sums split_gains gets (the reverse scan's right side is the accumulated one)
-// and its SplitInfo sums, count and output as eval_float computes them (the right side from the
-// left sums).
+// Role `role` of a float threshold of direction d with accumulated sums (ag, ah, c): the gain
+// takes the sums split_gains gets (the reverse scan's right side is the accumulated one), the
+// output and the SplitInfo the right side from the left sums, as eval_float computes them.
 __device__ __forceinline__ SidePart float_side(const Params& p, int d, double ag, double ah, int32_t c, double sum_g,
-                                               double sum_h, int32_t num_data, double parent, int s) {
+                                               double sum_h, int32_t num_data, int role) {
+  const bool right = (role & 1) != 0, gain = role < 2;
   const double slg = d == 0 ? sum_g - ag : ag, slh = d == 0 ? sum_h - ah : ah;
   const int32_t lc = d == 0 ? num_data - c : c;
   // the gain's sums: the accumulated side as accumulated, the other as total minus it
-  const double gg = s == 0 ? slg : (d == 0 ? ag : sum_g - ag);
-  const double gh = s == 0 ? slh : (d == 0 ? ah : sum_h - ah);
-  const int32_t gn = s == 0 ? lc : (d == 0 ? c : num_data - c);
+  const double gg = !right ? slg : (d == 0 ? ag : sum_g - ag);
+  const double gh = !right ? slh : (d == 0 ? ah : sum_h - ah);
   // the SplitInfo's sums: the right side from the left sums
-  const double og = s == 0 ? slg : sum_g - slg, oh = s == 0 ? slh : sum_h - slh;
-  const int32_t on = s == 0 ? lc : num_data - lc;
+  const double og = !right ? slg : sum_g - slg, oh = !right ? slh : sum_h - slh;
   SidePart r;
-  r.gain = leaf_gain(p, gg, gh, gn, parent);
+  r.n = !right ? lc : num_data - lc;
+  const double sq = gg * gg;
+  const double num = gain ? sq : -og;
+  const double den = (gain ? gh : oh) + p.l2;
+  r.val = num / den;
   r.sg = og;
   r.sh = oh - BK_EPS;
-  r.n = on;
-  r.out = split_output(p, og, oh, on, parent);
   return r;
 }
 
@@ -490,11 +495,12 @@ __device__ __forceinline__ void queue_push(SearchSmemT<NW>& sm, int d, bool push
   if (push) sm.q[d][base + __popc(bal & ((1u << lane) - 1u))] = e;
 }
 
-// Queue batches of 16 positions, two lanes per position: lane 2k evaluates the left side of
-// position k, lane 2k + 1 its right side. An f64 instruction costs a scheduler the same whether
-// one lane or 32 run it, so splitting a gain's two leaf gains over two lanes halves its
-// instruction chain, and evaluating every queued position's outputs with its gain (in the same
-// instructions) leaves none to evaluate after the arg-max. Batch k of direction d runs on warp
+// Queue batches of 8 positions, four lanes per position: lanes 4k, 4k + 1 evaluate the left and
+// right leaf gains of position k, lanes 4k + 2, 4k + 3 its left and right outputs (SidePart). An
+// f64 instruction costs a scheduler the same whether one lane or 32 run it, so spreading a
+// position's two gains and two outputs over four lanes (one division each, in the same
+// instructions) shortens its instruction chain to a quarter of the work, and evaluating every
+// queued position's outputs with its gain leaves none to evaluate after the arg-max. Batch k of direction d runs on warp
 // d + 2 (k mod 4), so the first batches of the two directions run on two schedulers and longer
 // queues spread over all four. One warp: its batches k0, k0 + 4, ...; their arg-max (highest gain,
 // ties to the earliest position in scan order) with its SplitInfo, and whether any passed, into
@@ -509,16 +515,17 @@ __device__ __forceinline__ void eval_batches(SearchSmemT<NW>& sm, int d, int k0,
   r.c = 0;
   int split = 0;
   const int n = sm.qn[d];
-  const int k = lane >> 1, side = lane & 1;
+  const int k = lane >> 2, role = lane & 3;
   auto batch = [&](int b0) {
-    // pairs past the queue's end evaluate its last entry and discard the result: an all-zero
+    // quads past the queue's end evaluate its last entry and discard the result: an all-zero
     // entry would send the whole warp through the f64 division's slow path (zero dividend, tiny
     // divisor), which costs more than the gain itself on this part
     const bool have = b0 + k < n;
     const QEnt e = sm.q[d][have ? b0 + k : n - 1];
-    const SidePart sp = side_of(e, side);
-    const double gl = __shfl_sync(FULL, sp.gain, lane & ~1);
-    const double gr = __shfl_sync(FULL, sp.gain, lane | 1);
+    const SidePart sp = side_of(e, role);
+    const int q0 = lane & ~3;
+    const double gl = __shfl_sync(FULL, sp.val, q0);
+    const double gr = __shfl_sync(FULL, sp.val, q0 | 1);
     double g = gl + gr;
     if (!have) g = -CUDART_INF;
     const bool passed = have && gain_passes(g, mgs);
@@ -529,17 +536,17 @@ __device__ __forceinline__ void eval_batches(SearchSmemT<NW>& sm, int d, int k0,
     const bool at = elig && dkey(g) == key;
     const int tb = d == 0 ? __reduce_max_sync(FULL, at ? (int)e.t : kNoneLo)
                           : __reduce_min_sync(FULL, at ? (int)e.t : kNoneHi);
-    const int wl = __ffs(__ballot_sync(FULL, at && (int)e.t == tb)) - 1 & ~1;  // the pair's left lane
+    const int wl = __ffs(__ballot_sync(FULL, at && (int)e.t == tb)) - 1 & ~3;  // the quad's first lane
     Eval v;
     v.gain = __shfl_sync(FULL, g, wl);
-    v.lsg = __shfl_sync(FULL, sp.sg, wl);
-    v.lsh = __shfl_sync(FULL, sp.sh, wl);
-    v.lo = __shfl_sync(FULL, sp.out, wl);
-    v.lc = __shfl_sync(FULL, sp.n, wl);
-    v.rsg = __shfl_sync(FULL, sp.sg, wl + 1);
-    v.rsh = __shfl_sync(FULL, sp.sh, wl + 1);
-    v.ro = __shfl_sync(FULL, sp.out, wl + 1);
-    v.rc = __shfl_sync(FULL, sp.n, wl + 1);
+    v.lsg = __shfl_sync(FULL, sp.sg, wl + 2);
+    v.lsh = __shfl_sync(FULL, sp.sh, wl + 2);
+    v.lo = __shfl_sync(FULL, sp.val, wl + 2);
+    v.lc = __shfl_sync(FULL, sp.n, wl + 2);
+    v.rsg = __shfl_sync(FULL, sp.sg, wl + 3);
+    v.rsh = __shfl_sync(FULL, sp.sh, wl + 3);
+    v.ro = __shfl_sync(FULL, sp.val, wl + 3);
+    v.rc = __shfl_sync(FULL, sp.n, wl + 3);
     v.lint = v.rint = 0;
     const int64_t wa = __shfl_sync(FULL, e.a, wl), wb = __shfl_sync(FULL, e.b, wl);
     const int32_t wc = __shfl_sync(FULL, e.c, wl);
@@ -555,8 +562,8 @@ __device__ __forceinline__ void eval_batches(SearchSmemT<NW>& sm, int d, int k0,
   // the first batch outside the loop: the f64 gain evaluated inside a loop measured about twice
   // as slow as the same code in straight-line form
   constexpr int kLanes = NW / 2;  // batch lanes per direction
-  if (16 * k0 < n) batch(16 * k0);
-  for (int b0 = 16 * (k0 + kLanes); b0 < n; b0 += 16 * kLanes) batch(b0);
+  if (8 * k0 < n) batch(8 * k0);
+  for (int b0 = 8 * (k0 + kLanes); b0 < n; b0 += 8 * kLanes) batch(b0);
   if (lane == 0) {
     sm.pres[d][k0] = r;
     sm.psplit[d][k0] = split;
@@ -763,8 +770,7 @@ __device__ void search_int(const Job& J, const Params& p, const SearchIn& si, co
     const double gs = C.gs, hsc = C.hs;
     eval_queues(
         sm, warp, lane, C.mgs,
-        [&](const QEnt& e, int s) { return int_side(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, C.parent, s); }, r,
-        rs);
+        [&](const QEnt& e, int role) { return int_side(p, e.a, e.b, tg, th, gs, hsc, C.cnt_factor, role); }, r, rs);
     if (warp != 0) return;
   } else {
     // every valid position evaluates its own f64 gain; barrier 3: the arg-max
@@ -987,9 +993,9 @@ __device__ void search_float(const Job& J, const Params& p, const SearchIn& si, 
     __syncthreads();
     eval_queues(
         sm, warp, lane, C.mgs,
-        [&](const QEnt& e, int s) {
+        [&](const QEnt& e, int role) {
           return float_side(p, e.d, __longlong_as_double(e.a), __longlong_as_double(e.b), e.c, sum_g, sum_h,
-                            num_data, C.parent, s);
+                            num_data, role);
         },
         r, rs);
     if (warp != 0) return;

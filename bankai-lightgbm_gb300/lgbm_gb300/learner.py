@@ -94,7 +94,7 @@ class GpuTreeLearner:
         """Picks the grow-loop launch shape by timing whole trees grown from these gradients
         (bk_learner_autotune; cached per dataset shape class). Returns the chosen shape
         (rows per histogram CTA, histogram CTAs per feature tile, partition CTAs, rows per histogram
-        CTA up to which it adds to the pool with global atomics)."""
+        CTA up to which it adds to the pool with global atomics, histogram CTAs per cluster)."""
         K = self.num_jobs
         if on_device:
             gp, hp = int(gradients), int(hessians)
@@ -103,19 +103,19 @@ class GpuTreeLearner:
             hh = np.ascontiguousarray(hessians, dtype=np.float32).reshape(K, -1)
             assert g.shape[1] == self.ds.num_data and hh.shape == g.shape
             gp, hp = g.ctypes.data, hh.ctypes.data
-        out = np.zeros(4, np.int32)
+        out = np.zeros(5, np.int32)
         _lib.check(self.lib.bk_learner_autotune(self.h, gp, hp, int(bool(on_device)), int(trials), out.ctypes.data),
                    "bk_learner_autotune")
         return tuple(int(x) for x in out)
 
     def launch_shape(self):
-        out = np.zeros(4, np.int32)
+        out = np.zeros(5, np.int32)
         _lib.check(self.lib.bk_learner_launch_shape(self.h, out.ctypes.data), "bk_learner_launch_shape")
         return tuple(int(x) for x in out)
 
     def set_launch_shape(self, shape):
-        arr = np.ascontiguousarray(tuple(shape) + (0,) * (4 - len(shape)), dtype=np.int32)
-        assert arr.shape == (4,)
+        arr = np.ascontiguousarray(tuple(shape) + (0,) * (5 - len(shape)), dtype=np.int32)
+        assert arr.shape == (5,)
         _lib.check(self.lib.bk_learner_set_launch_shape(self.h, arr.ctypes.data), "bk_learner_set_launch_shape")
 
     def set_timing(self, on: bool):

@@ -688,7 +688,8 @@ def _shape_dict(shape, tuned):
     if shape is None:
         return None
     return {"hist_min_rows_per_cta": shape[0], "hist_ctas_per_feature_tile": shape[1], "partition_ctas": shape[2],
-            "hist_direct_atomic_rows_per_cta": shape[3], "source": "bk_learner_autotune" if tuned else "default"}
+            "hist_direct_atomic_rows_per_cta": shape[3], "hist_ctas_per_cluster": shape[4],
+            "source": "bk_learner_autotune" if tuned else "default"}
 
 
 def aggregate_ranks(ms_per_step, world):

@@ -213,24 +213,29 @@ int bk_learner_set_interaction_constraints(bk_learner* learner, const int32_t* f
 /* Launch-shape autotuner (GB300-only, no reference counterpart; results never depend on it).
  * Times whole trees (graph form, median of `trials` after one untimed tree per shape) grown from
  * the given gradients (as bk_learner_train takes them, all rows) over a coordinate descent of
- * four launch parameters — the fewest rows a histogram CTA takes, histogram CTAs per 32-feature
+ * five launch parameters — the fewest rows a histogram CTA takes, histogram CTAs per 32-feature
  * tile, partition CTAs, and (quantized) the most rows a histogram CTA adds straight to the pool
- * slot with global atomics instead of through a shared histogram — and keeps the fastest. Choices are cached per shape class (device,
+ * slot with global atomics instead of through a shared histogram, and the histogram CTAs of a tile
+ * per thread-block cluster (1, 2 or 4; a cluster adds up its CTAs' shared histograms in distributed
+ * shared memory before one flush) — and keeps the fastest. Choices are cached per shape class (device,
  * log2 rows, feature tiles, bins per feature, quantized, num_leaves, num_jobs): a later learner of
  * the same class takes the cached shape without timing. The learner's state across trees (the
  * stochastic-rounding engine) is restored afterwards; the trial trees replace the "last tree"
  * outputs (bk_learner_row_leaf), so call it before the first bk_learner_train. shape_out (host,
- * 4 ints, may be NULL) receives the chosen shape. */
+ * 5 ints, may be NULL) receives the chosen shape. */
 int bk_learner_autotune(bk_learner* learner, const float* gradients, const float* hessians, int32_t on_device,
                         int32_t trials, int32_t* shape_out);
 
-/* The current launch shape: {rows per histogram CTA (minimum), histogram CTAs per feature tile,
- * partition CTAs, rows per histogram CTA up to which it uses global atomics (0: never)}. */
+/* The current launch shape (5 ints): {rows per histogram CTA (minimum), histogram CTAs per
+ * feature tile, partition CTAs, rows per histogram CTA up to which it uses global atomics (0:
+ * never), histogram CTAs per cluster (1: none)}. */
 int bk_learner_launch_shape(bk_learner* learner, int32_t* shape_out);
 
 /* Sets the launch shape (e.g. one found by bk_learner_autotune earlier), clamped to what the
  * dataset's rows can fill: shape[0] >= 32 rows (rounded down to a multiple of 32), shape[1] >= 1,
- * shape[2] >= 1 (at most 1024), shape[3] >= 0 (used on the quantized path only). */
+ * shape[2] >= 1 (at most 1024), shape[3] >= 0 (used on the quantized path only), shape[4] in
+ * 0 .. 8 (0 or 1: no cluster; 2, 3 -> 2; 4 .. 7 -> 4; 8; quantized path only; the histogram CTAs
+ * per tile become a multiple of it). 5 ints. */
 int bk_learner_set_launch_shape(bk_learner* learner, const int32_t* shape);
 
 /* Replaces SerialTreeLearner::reset_constant_hessian (serial.rs:279). */

@@ -305,10 +305,14 @@ def test_device_prediction_replays_the_partition():
 
 
 @pytest.mark.parametrize("shape", [(32, 1, 1, 0), (64, 3, 7, 0), (1024, 200, 1024, 0), (256, 38, 304, 0),
-                                   (64, 3, 7, 1 << 30), (256, 38, 304, 512), (32, 64, 64, 96)])
+                                   (64, 3, 7, 1 << 30), (256, 38, 304, 512), (32, 64, 64, 96),
+                                   (256, 38, 304, 0, 2), (256, 38, 304, 0, 4), (64, 9, 33, 0, 4),
+                                   (32, 2, 8, 0, 8), (256, 38, 304, 512, 4)])
 def test_launch_shapes_do_not_change_results(shape):
     """Every launch shape grows the oracle's trees: quantized bit-exact, both partition forms,
-    with the shared-histogram CTAs, the global-atomic CTAs (every CTA at 1 << 30) or a mix."""
+    with the shared-histogram CTAs, the global-atomic CTAs (every CTA at 1 << 30) or a mix, and
+    with clusters of 2, 4 or 8 histogram CTAs adding up their histograms in distributed shared
+    memory (leaves smaller than a cluster included: its CTAs without rows add zeros)."""
     cfg = dict(num_leaves=31, use_quantized_grad=1, stochastic_rounding=1, seed=2, num_threads=2)
     ds, z = _dataset(25000, 40, seed=21)
     g, h, const = _grads(z, "binary", seed=22)
@@ -316,8 +320,11 @@ def test_launch_shapes_do_not_change_results(shape):
         orc, gpu, _ = _learners(ds, const, loop_mode=loop_mode, **cfg)
         gpu.set_launch_shape(shape)
         got = gpu.launch_shape()
-        assert got[0] == max(32, shape[0] // 32 * 32) and 1 <= got[1] <= shape[1] and 1 <= got[2] <= shape[2]
-        assert got[3] == shape[3]
+        cl = shape[4] if len(shape) > 4 else 0
+        assert got[4] == (1 if cl < 2 else cl) and got[1] % got[4] == 0
+        # the tile's CTAs: at most the asked number, rounded to whole clusters (at least one)
+        assert got[0] == max(32, shape[0] // 32 * 32) and 1 <= got[1] <= max(shape[1], got[4])
+        assert 1 <= got[2] <= shape[2] and got[3] == shape[3]
         for it in range(2):
             ro, rg = orc.train(g, h), gpu.train(g, h)
             _assert_records_equal(ro[0], rg[0])
@@ -455,7 +462,7 @@ def test_packed_bin_tiles(quant):
     assert len(gb) == F and max(gb[:32]) <= 16 and max(gb[32:64]) > 16
     g, h, const = _grads(z, "binary", seed=32)
     cfg = dict(num_leaves=31, use_quantized_grad=quant, stochastic_rounding=1, seed=3, num_threads=2)
-    shapes = [(256, 38, 304, 0), (64, 20, 64, 1 << 30)] if quant else [(256, 38, 304, 0)]
+    shapes = [(256, 38, 304, 0), (64, 20, 64, 1 << 30), (128, 38, 64, 0, 4)] if quant else [(256, 38, 304, 0)]
     for shape in shapes:
         for loop_mode in (1, 0):
             orc, gpu, _ = _learners(ds, const, loop_mode=loop_mode, **cfg)
