@@ -65,6 +65,14 @@ def test_invalid_arguments_fail_with_a_message(bklib):
         (lambda: bklib.bk_learner_autotune(None, None, None, 0, 1, None), "invalid arguments"),
         (lambda: bklib.bk_learner_set_launch_shape(None, None), "invalid arguments"),
         (lambda: bklib.bk_partition_split_noalloc(None, 0, None, 0, None, None, None, None), "invalid arguments"),
+        (lambda: bklib.bk_learner_group_create(None, 0, ctypes.byref(out)), "invalid arguments"),
+        (lambda: bklib.bk_learner_group_train(None, None, None, 0.0, None, None, None, None, None),
+         "invalid arguments"),
+        (lambda: bklib.bk_learner_group_autotune(None, None, None, 1, None), "invalid arguments"),
+        (lambda: bklib.bk_learner_search_threads(None, None), "invalid arguments"),
+        (lambda: bklib.bk_learner_histogram_cache_capacity(None, None), "invalid arguments"),
+        (lambda: bklib.bk_learner_reset_histogram_pool_config(None), "null learner"),
+        (lambda: bklib.bk_learner_set_objective_weights(None, None, 1.0, 1.0), "invalid arguments"),
     ]
     for call, words in cases:
         assert call() == -1
