@@ -290,8 +290,8 @@ def run_gpu(args, rank, world):
     hist_gbs = roof["hist_bytes"] / (roof["hist_ms"] * 1e6) if roof["hist_ms"] > 0 else None
     hist_launches = (args.leaves - 1) * args.steps  # one histogram launch per split step of a tree
     # per step: objective gradients, row init, discretization (4), root sums (2), tree begin, three
-    # kernels per split (histogram, search, partition), score update
-    launches_per_step = 1 + 1 + 4 + 2 + 1 + 3 * (args.leaves - 1) + 1
+    # kernels per split (histogram, search, partition), the last split's bookkeeping, score update
+    launches_per_step = 1 + 1 + 4 + 2 + 1 + 3 * (args.leaves - 1) + 1 + 1
     line = {
         "metric": METRIC, "value": round(value, 4), "unit": "iters/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(ms, 3), "higher_is_better": True, "scaling": "weak",
