@@ -131,7 +131,8 @@ struct JobState {
   double gscale, hscale, inv_g, inv_h;
   double root_output;
   uint32_t start_pos, red_maxg, red_maxh, red_flags;
-  int32_t mt_idx, _p1;
+  int32_t mt_idx;
+  int32_t split_pslot;  // the chosen leaf's pool slot, which its larger child keeps
   int64_t hist_rows_direct, hist_rows_gather, hist_builds;  // work done by the histogram kernels
   uint32_t search_done, part_done;  // CTAs finished in the current search / scatter launch
   // by-node column sample (col_sampler.rs:109-177): the sampler's LCG state, whether a by-tree
@@ -251,7 +252,7 @@ void launch_apply_split(const Job* h_jobs, int num_jobs, const Params& p, int pa
 // clear_par >= 0: the launch zeroes that single-pass partition counter pair first. decide: its
 // last CTA decides and records the split (else the single-pass partition decides it).
 void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, int clear_par,
-                   bool decide, cudaStream_t s);
+                   bool decide, int post, cudaStream_t s);
 // stable: the two-kernel compaction whose last CTA applies the split's bookkeeping; otherwise the
 // single-pass partition, counting into the counter pair `par` (the split index's parity), whose
 // bookkeeping the next histogram launch applies.

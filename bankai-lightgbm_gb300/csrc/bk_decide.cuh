@@ -117,7 +117,7 @@ __device__ __forceinline__ Pick make_pick(int i, double g, int f, long long pay)
 
 // The chosen split, as every CTA that decides it sees it.
 struct Decision {
-  int32_t stop, leaf, inner, buf, depth, sslot, new_leaf;
+  int32_t stop, leaf, inner, buf, depth, sslot, new_leaf, pslot;
   uint32_t thr;  // threshold | default_left << 31
   int64_t begin, count;
 };
@@ -128,15 +128,20 @@ struct DecideSmem {
   // the row range of the first kDecideThreads leaves, so the chosen leaf's is at hand for the
   // partition that follows
   int64_t lb[kDecideThreads], lc[kDecideThreads];
-  int32_t lbuf[kDecideThreads], ld[kDecideThreads];
+  int32_t lbuf[kDecideThreads], ld[kDecideThreads], lslot[kDecideThreads];
   int32_t stopped, searched, leaf0, leaf1;
+  // the pool slots of the searched leaves, the next free slot and the leaf count (the histogram
+  // launch's bookkeeping wrote them)
+  int32_t slot0, slot1, next_free, tree_leaves;
 };
 
 // Part one of a split decision (split_info.rs:125-133): the arg-max over every leaf but the two
 // the current search covers, whose records the histogram launch of this step and earlier steps
-// wrote. A launch that follows the search can run it before its griddep_wait: the search triggers
-// its dependents only after its own wait, so by then the histogram launch has completed; the
-// loads go through L2 (__ldcg). Every thread of the CTA calls it; no barrier.
+// wrote, and the loads of the job-state fields part two needs (the searched leaves' pool slots,
+// the next free slot, the leaf count: the histogram launch's bookkeeping wrote them). A launch
+// that follows the search can run it before its griddep_wait: the search triggers its dependents
+// only after its own wait, so by then the histogram launch has completed; the loads go through L2
+// (__ldcg). Every thread of the CTA calls it; no barrier.
 __device__ __forceinline__ void decide_leaves(const Job& J, const Params& p, DecideSmem& ds) {
   const JobState* st = J.st;
   const int t = threadIdx.x, lane = t & 31, warp = t >> 5;
@@ -148,6 +153,10 @@ __device__ __forceinline__ void decide_leaves(const Job& J, const Params& p, Dec
     ds.searched = searched;
     ds.leaf0 = leaf0;
     ds.leaf1 = leaf1;
+    ds.slot0 = __ldcg(&st->smaller_slot);
+    ds.slot1 = __ldcg(&st->larger_slot);
+    ds.next_free = __ldcg(&st->next_free);
+    ds.tree_leaves = __ldcg(&st->tree_leaves);
   }
   Pick b{-1, 0, 0, false, 0.0, 0};
   for (int i = t; i < p.num_leaves; i += kDecideThreads) {
@@ -156,6 +165,7 @@ __device__ __forceinline__ void decide_leaves(const Job& J, const Params& p, Dec
       ds.lc[i] = __ldcg(&J.leaf_count[i]);
       ds.lbuf[i] = __ldcg(&J.leaf_buf[i]);
       ds.ld[i] = __ldcg(&J.leaf_depth[i]);
+      ds.lslot[i] = __ldcg(&J.leaf_slot[i]);
     }
     const double bg = __ldcg(&J.bgain[i]);
     const int32_t bf = __ldcg(&J.bfeat[i]);
@@ -196,7 +206,7 @@ __device__ void decide_finish(const Job& J, const Params& p, const DevFeature* f
   {
     const int side = t / kHalf;
     const int32_t leaf = side ? leaf1 : leaf0;
-    const int32_t slot = side ? st->larger_slot : st->smaller_slot;
+    const int32_t slot = side ? ds.slot1 : ds.slot0;
     for (int f = t % kHalf; f < p.F; f += kHalf) {
       const uint8_t u = J.used[f];
       const uint8_t cs = __ldcg(&J.csplit[side * p.F + f]);
@@ -267,8 +277,9 @@ __device__ void decide_finish(const Job& J, const Params& p, const DevFeature* f
     d.count = near ? ds.lc[w.i] : __ldcg(&J.leaf_count[w.i]);
     d.buf = near ? ds.lbuf[w.i] : __ldcg(&J.leaf_buf[w.i]);
     d.depth = near ? ds.ld[w.i] : __ldcg(&J.leaf_depth[w.i]);
-    d.sslot = st->next_free;
-    d.new_leaf = st->tree_leaves;
+    d.pslot = near ? ds.lslot[w.i] : __ldcg(&J.leaf_slot[w.i]);
+    d.sslot = ds.next_free;
+    d.new_leaf = ds.tree_leaves;
     *out = d;
     if (record) {
       st->split_begin = d.begin;
@@ -276,6 +287,7 @@ __device__ void decide_finish(const Job& J, const Params& p, const DevFeature* f
       st->split_buf = d.buf;
       st->split_depth = d.depth;
       st->split_sslot = d.sslot;
+      st->split_pslot = d.pslot;
       st->split_leaf = d.leaf;
       st->split_inner = d.inner;
       st->split_thr = d.thr;

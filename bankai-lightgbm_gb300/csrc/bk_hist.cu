@@ -2,10 +2,13 @@
 //
 // Grid: (blocks_per_tile, T, jobs). Each CTA owns one 32-feature tile and one contiguous chunk
 // of the leaf's rows. A warp takes 32 rows at a time: every lane fetches its row's run of the
-// tile (32 bytes of 8-bit bins, or 16 bytes of 4-bit bins) with 128-bit loads and stages it in
-// shared memory; then, row by row, lane f adds that row's statistics to bin[row][f] of a
-// CTA-private shared histogram laid out [bin][feature] — lane f always hits bank f, so the
-// shared-memory atomics of a warp never conflict and never collide. At the end the CTA adds its
+// tile (32 bytes of 8-bit bins, or 16 bytes of 4-bit bins) with 128-bit loads. The CTA-private
+// shared histogram is laid out [bin][feature], so feature f's counters all sit in bank f. The
+// integer kernel adds every lane's own row feature by feature, lane l taking feature k ^ l at
+// step k: the 32 lanes of each shared atomic hit 32 different features, 32 different banks, and
+// no row passes through shared memory. The float kernel stages the runs in shared memory and
+// then, row by row, lane f adds that row's statistics to bin[row][f]. Either way the atomics of
+// a warp never conflict and never collide. At the end the CTA adds its
 // non-zero bins to the leaf's slot in the histogram pool with global atomics (the pool slot is
 // zeroed when the tree starts). Only the tile's own bins (its largest feature's group bins) are
 // zeroed and flushed.
@@ -30,6 +33,7 @@
 //
 // The last CTA of tile 0 also computes the per-leaf constants of the search that follows
 // (bk_leaf.cuh) before its own rows.
+#include <algorithm>
 #include <mutex>
 
 #include "bk_launch.cuh"
@@ -156,48 +160,141 @@ __device__ __forceinline__ unsigned long long pool_value(int32_t v) {
   return (unsigned long long)((int64_t)g * 4294967296LL + (int64_t)h);
 }
 
+// Adds a row's packed value to the (bin, feature) counter of the tile's shared histogram: the
+// 16:16 hot counter, or (WIDE) the 32-bit gradient and hessian counters.
 template <bool WIDE>
 __device__ __forceinline__ void add_row(uint32_t* hot, int32_t* cold_g, int32_t* cold_h, uint32_t bin, int32_t v,
-                                        int lane) {
+                                        uint32_t f) {
   if (WIDE) {
-    atomicAdd(&cold_g[bin * TILE + lane], (int32_t)(int16_t)(v & 0xffff));
-    atomicAdd(&cold_h[bin * TILE + lane], v >> 16);
+    atomicAdd(&cold_g[bin * TILE + f], (int32_t)(int16_t)(v & 0xffff));
+    atomicAdd(&cold_h[bin * TILE + f], v >> 16);
   } else {
-    atomicAdd(&hot[bin * TILE + lane], (uint32_t)v);
+    atomicAdd(&hot[bin * TILE + f], (uint32_t)v);
   }
 }
 
-// The rows and flush of one integer-histogram CTA, its range known (NIBBLE: the tile holds
-// 4-bit bins).
+// w[i] <- w[i ^ q] for q < N (N a power of two): one select per word and bit of q.
+template <int N>
+__device__ __forceinline__ void xor_permute(uint32_t (&w)[N], uint32_t q) {
+#pragma unroll
+  for (int bit = N / 2; bit >= 1; bit >>= 1) {
+    const bool s = (q & (uint32_t)bit) != 0u;
+    uint32_t t[N];
+#pragma unroll
+    for (int i = 0; i < N; ++i) t[i] = s ? w[i ^ bit] : w[i];
+#pragma unroll
+    for (int i = 0; i < N; ++i) w[i] = t[i];
+  }
+}
+
+// Every lane adds its own row (its run and packed value as loaded) to the shared histogram, one
+// feature per step: at step k lane l takes feature k ^ l, so the 32 lanes of each atomic hit 32
+// different features — 32 different banks, whatever their bins — and no row is staged through
+// shared memory or broadcast. The run's words are first permuted by the lane's high feature bits
+// (a word index that varies by lane cannot be a register index), leaving a per-lane byte or
+// nibble choice at each step. A 16-byte run of 8-bit bins (at most 16 features) takes feature
+// (k ^ l) & 15 at step k < 16 (lanes l and l ^ 16 share a column). Features at or past nf, the
+// tile's feature count, get nothing. A lane without a row carries zeros.
 template <bool WIDE, bool NIBBLE>
-__device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, const Range& R, const TileGeom& geo,
-                                              const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
-                                              int flush_rounds, int direct_rows, bool in_cluster, unsigned char* smem) {
+__device__ __forceinline__ void add_own_row(uint32_t* hot, int32_t* cold_g, int32_t* cold_h, const RoundLoad& L,
+                                            uint32_t lane, bool half, uint32_t nf) {
+  const int32_t v = L.v;
+  if (NIBBLE) {
+    // 32 features in four words, feature f at bits 4 (f & 7) of word f >> 3
+    uint32_t w[4] = {L.a.x, L.a.y, L.a.z, L.a.w};
+    xor_permute<4>(w, (lane >> 3) & 3u);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      const uint32_t f = (uint32_t)k ^ lane;
+      const uint32_t bin = (w[k >> 3] >> ((((uint32_t)k & 7u) ^ (lane & 7u)) << 2)) & 15u;
+      if (f < nf) add_row<WIDE>(hot, cold_g, cold_h, bin, v, f);
+    }
+  } else if (half) {
+    // at most 16 features in four words, feature f in byte f & 3 of word f >> 2
+    uint32_t w[4] = {L.a.x, L.a.y, L.a.z, L.a.w};
+    xor_permute<4>(w, (lane >> 2) & 3u);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const uint32_t f = ((uint32_t)k ^ lane) & 15u;
+      const uint32_t bin = __byte_perm(w[k >> 2], 0u, 0x4440u | (((uint32_t)k & 3u) ^ (lane & 3u)));
+      if (f < nf) add_row<WIDE>(hot, cold_g, cold_h, bin, v, f);
+    }
+  } else {
+    // 32 features in eight words, feature f in byte f & 3 of word f >> 2
+    uint32_t w[8] = {L.a.x, L.a.y, L.a.z, L.a.w, L.b.x, L.b.y, L.b.z, L.b.w};
+    xor_permute<8>(w, lane >> 2);
+    if (nf >= 32u) {
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const uint32_t f = (uint32_t)k ^ lane;
+        const uint32_t bin = __byte_perm(w[k >> 2], 0u, 0x4440u | (((uint32_t)k & 3u) ^ (lane & 3u)));
+        add_row<WIDE>(hot, cold_g, cold_h, bin, v, f);
+      }
+    } else {
+#pragma unroll
+      for (int k = 0; k < 32; ++k) {
+        const uint32_t f = (uint32_t)k ^ lane;
+        const uint32_t bin = __byte_perm(w[k >> 2], 0u, 0x4440u | (((uint32_t)k & 3u) ^ (lane & 3u)));
+        if (f < nf) add_row<WIDE>(hot, cold_g, cold_h, bin, v, f);
+      }
+    }
+  }
+}
+
+// Folds the hot counters into the cold ones and clears them. Every thread of the CTA calls it
+// between barriers.
+__device__ __forceinline__ void fold_hot(uint32_t* hot, int32_t* cold_g, int32_t* cold_h, int Bt) {
+  uint4* hot4 = reinterpret_cast<uint4*>(hot);
+  int4* g4 = reinterpret_cast<int4*>(cold_g);
+  int4* h4 = reinterpret_cast<int4*>(cold_h);
+  for (int e = threadIdx.x; e < Bt * TILE / 4; e += blockDim.x) {
+    const uint4 s = hot4[e];
+    if (s.x | s.y | s.z | s.w) {
+      int4 g = g4[e], h = h4[e];
+      g.x += hot_g(s.x);
+      g.y += hot_g(s.y);
+      g.z += hot_g(s.z);
+      g.w += hot_g(s.w);
+      h.x += (int32_t)(s.x & 0xffffu);
+      h.y += (int32_t)(s.y & 0xffffu);
+      h.z += (int32_t)(s.z & 0xffffu);
+      h.w += (int32_t)(s.w & 0xffffu);
+      g4[e] = g;
+      h4[e] = h;
+      hot4[e] = make_uint4(0, 0, 0, 0);
+    }
+  }
+}
+
+// Shared memory of the integer kernel: the hot counters [bin][32] (none when WIDE), then the
+// 32-bit gradient and hessian counters [bin][32] each. A CTA that adds straight to the pool slot
+// (direct) uses none of them, and stages its rows over the same bytes instead: 64 uint4 per warp,
+// then 32 packed values per warp.
+__device__ __forceinline__ size_t hist_int_hot_words(int Bt, bool wide) { return wide ? 0 : (size_t)Bt * TILE; }
+
+// The row loop of one integer-histogram CTA: with DIRECT every (row, feature) goes to the pool
+// slot by a global atomic, otherwise to the CTA's shared histogram (the hot counters folded into
+// the cold ones every `flush_rounds` rounds, before either half can overflow; the last round's
+// are folded by the flush).
+template <bool WIDE, bool NIBBLE, bool DIRECT>
+__device__ __forceinline__ void hist_int_loop(const Params& p, const Range& R, const TileGeom& geo, const uint8_t* tb,
+                                              size_t rs, int flush_rounds, unsigned long long* slot,
+                                              unsigned char* smem) {
   const int tile = blockIdx.y;
   const int Bt = geo.bins;
   const bool half = geo.width == 16;  // one 16-byte run per row
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
   uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
-  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + (WIDE ? 0 : Bt * TILE));
+  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + hist_int_hot_words(Bt, WIDE));
   int32_t* cold_h = cold_g + Bt * TILE;
-  uint4* stage = reinterpret_cast<uint4*>(cold_h + Bt * TILE);
-  int32_t* stage_v = reinterpret_cast<int32_t*>(stage + nwarps * 64);
-  unsigned long long* slot = reinterpret_cast<unsigned long long*>(J.pool) +
-                             ((size_t)R.slot * p.T + tile) * (size_t)p.B * TILE;
-  // uniform over the CTA; a CTA of a cluster always adds through its shared histogram
-  const bool direct = !in_cluster && R.r1 - R.r0 <= (int64_t)direct_rows;
-  __syncthreads();
-  // the tile's run of row 0 and the row stride, in the copy that suits the leaf's density
-  const bool dense = R.count * 4 >= p.n;
-  const uint8_t* tb = dense ? bins_tm + geo.tm_off : bins_rt + geo.rt_off;
-  const size_t rs = dense ? (size_t)tile_width(geo) : (size_t)p.rt_stride;
-  // lanes past the last feature of the last tile (padding) add nothing
-  const bool feat_lane = tile * TILE + lane < p.F;
+  uint4* my_stage = reinterpret_cast<uint4*>(smem) + warp * 64;
+  int32_t* my_v = reinterpret_cast<int32_t*>(reinterpret_cast<uint4*>(smem) + nwarps * 64) + warp * 32;
+  const uint8_t* sb = reinterpret_cast<const uint8_t*>(my_stage);
+  // lanes / features past the last feature of the last tile (padding) add nothing
+  const uint32_t tile_feats = (uint32_t)min(TILE, p.F - tile * TILE);
+  const bool feat_lane = (uint32_t)lane < tile_feats;
   const int64_t per_round = (int64_t)TILE * nwarps;
   const int64_t rounds = ceil_div64(R.r1 - R.r0, per_round);
-  uint4* my_stage = stage + warp * 64;
-  const uint8_t* sb = reinterpret_cast<const uint8_t*>(my_stage);
-  int32_t* my_v = stage_v + warp * 32;
   // software pipeline: the next round's runs and the round after's row indices are in flight
   // while this round is added up
   const int64_t first = R.r0 + (int64_t)warp * TILE + lane;
@@ -210,69 +307,60 @@ __device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, con
     RoundLoad nxt = load_round_int(tb, rs, R, base + per_round + lane, row_nxt, WIDE, half);
     row_nxt = row_nn;
     if (base < R.r1) {
-      my_stage[lane * 2] = cur.a;
-      if (!half) my_stage[lane * 2 + 1] = cur.b;
-      my_v[lane] = cur.v;
-      __syncwarp();
-      const int jn = (int)min((int64_t)32, R.r1 - base);  // warp-uniform
-      if (direct) {
+      if (DIRECT) {
+        // global atomics: the round's rows are staged so that each atomic covers one row's 32
+        // features, 32 consecutive pool entries
+        my_stage[lane * 2] = cur.a;
+        if (!half) my_stage[lane * 2 + 1] = cur.b;
+        my_v[lane] = cur.v;
+        __syncwarp();
+        const int jn = (int)min((int64_t)32, R.r1 - base);  // warp-uniform
         for (int j = 0; j < jn; ++j) {
           const uint32_t b0 = staged_bin<NIBBLE>(sb, j, lane);
           const int32_t v0 = my_v[j];
           if (feat_lane) atomicAdd(slot + b0 * TILE + lane, pool_value<WIDE>(v0));
         }
-      } else if (jn == 32) {
-#pragma unroll 2
-        for (int j = 0; j < 32; j += 4) {
-          const int4 v4 = *reinterpret_cast<const int4*>(my_v + j);
-          const uint32_t b0 = staged_bin<NIBBLE>(sb, j + 0, lane), b1 = staged_bin<NIBBLE>(sb, j + 1, lane);
-          const uint32_t b2 = staged_bin<NIBBLE>(sb, j + 2, lane), b3 = staged_bin<NIBBLE>(sb, j + 3, lane);
-          if (feat_lane) {
-            add_row<WIDE>(hot, cold_g, cold_h, b0, v4.x, lane);
-            add_row<WIDE>(hot, cold_g, cold_h, b1, v4.y, lane);
-            add_row<WIDE>(hot, cold_g, cold_h, b2, v4.z, lane);
-            add_row<WIDE>(hot, cold_g, cold_h, b3, v4.w, lane);
-          }
-        }
+        __syncwarp();
       } else {
-        for (int j = 0; j < jn; ++j) {
-          const uint32_t b0 = staged_bin<NIBBLE>(sb, j, lane);
-          const int32_t v0 = my_v[j];
-          if (feat_lane) add_row<WIDE>(hot, cold_g, cold_h, b0, v0, lane);
-        }
+        add_own_row<WIDE, NIBBLE>(hot, cold_g, cold_h, cur, (uint32_t)lane, half, tile_feats);
       }
-      __syncwarp();
     }
     cur = nxt;
-    // fold the 16:16 counters into the 32-bit ones before either half can overflow (the last
-    // round's counters are folded by the final flush below)
-    if (!WIDE && !direct && --until_flush == 0 && rd + 1 < rounds) {
+    if (!WIDE && !DIRECT && --until_flush == 0 && rd + 1 < rounds) {
       until_flush = flush_rounds;
       __syncthreads();
-      uint4* hot4 = reinterpret_cast<uint4*>(hot);
-      int4* g4 = reinterpret_cast<int4*>(cold_g);
-      int4* h4 = reinterpret_cast<int4*>(cold_h);
-      for (int e = threadIdx.x; e < Bt * TILE / 4; e += blockDim.x) {
-        const uint4 s = hot4[e];
-        if (s.x | s.y | s.z | s.w) {
-          int4 g = g4[e], h = h4[e];
-          g.x += hot_g(s.x);
-          g.y += hot_g(s.y);
-          g.z += hot_g(s.z);
-          g.w += hot_g(s.w);
-          h.x += (int32_t)(s.x & 0xffffu);
-          h.y += (int32_t)(s.y & 0xffffu);
-          h.z += (int32_t)(s.z & 0xffffu);
-          h.w += (int32_t)(s.w & 0xffffu);
-          g4[e] = g;
-          h4[e] = h;
-          hot4[e] = make_uint4(0, 0, 0, 0);
-        }
-      }
+      fold_hot(hot, cold_g, cold_h, Bt);
       __syncthreads();
     }
   }
-  if (direct || in_cluster) return;  // a cluster flushes its CTAs' histograms together
+}
+
+// The rows and flush of one integer-histogram CTA, its range known (NIBBLE: the tile holds
+// 4-bit bins).
+template <bool WIDE, bool NIBBLE>
+__device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, const Range& R, const TileGeom& geo,
+                                              const uint8_t* __restrict__ bins_rt, const uint8_t* __restrict__ bins_tm,
+                                              int flush_rounds, int direct_rows, bool in_cluster, unsigned char* smem) {
+  const int tile = blockIdx.y;
+  const int Bt = geo.bins;
+  uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
+  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + hist_int_hot_words(Bt, WIDE));
+  int32_t* cold_h = cold_g + Bt * TILE;
+  unsigned long long* slot = reinterpret_cast<unsigned long long*>(J.pool) +
+                             ((size_t)R.slot * p.T + tile) * (size_t)p.B * TILE;
+  // uniform over the CTA; a CTA of a cluster always adds through its shared histogram
+  const bool direct = !in_cluster && R.r1 - R.r0 <= (int64_t)direct_rows;
+  __syncthreads();
+  // the tile's run of row 0 and the row stride, in the copy that suits the leaf's density
+  const bool dense = R.count * 4 >= p.n;
+  const uint8_t* tb = dense ? bins_tm + geo.tm_off : bins_rt + geo.rt_off;
+  const size_t rs = dense ? (size_t)tile_width(geo) : (size_t)p.rt_stride;
+  if (direct) {
+    hist_int_loop<WIDE, NIBBLE, true>(p, R, geo, tb, rs, flush_rounds, slot, smem);
+    return;
+  }
+  hist_int_loop<WIDE, NIBBLE, false>(p, R, geo, tb, rs, flush_rounds, slot, smem);
+  if (in_cluster) return;  // a cluster flushes its CTAs' histograms together
   __syncthreads();
   for (int e = threadIdx.x; e < Bt * TILE; e += blockDim.x) {
     int32_t gg = cold_g[e], hh = cold_h[e];
@@ -300,31 +388,11 @@ __device__ __forceinline__ void hist_cluster_flush(const Params& p, const TileGe
                                                    uint32_t ncta, unsigned char* smem) {
   const int Bt = geo.bins;
   uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
-  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + (WIDE ? 0 : Bt * TILE));
+  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + hist_int_hot_words(Bt, WIDE));
   int32_t* cold_h = cold_g + Bt * TILE;
   const int n4 = Bt * TILE / 4;  // int4 groups of the tile's bins: a multiple of 64 (Bt a multiple of 8)
   __syncthreads();
-  if (!WIDE) {
-    const uint4* hot4 = reinterpret_cast<const uint4*>(hot);
-    int4* g4 = reinterpret_cast<int4*>(cold_g);
-    int4* h4 = reinterpret_cast<int4*>(cold_h);
-    for (int e = threadIdx.x; e < n4; e += blockDim.x) {
-      const uint4 s = hot4[e];
-      if (s.x | s.y | s.z | s.w) {
-        int4 g = g4[e], h = h4[e];
-        g.x += hot_g(s.x);
-        g.y += hot_g(s.y);
-        g.z += hot_g(s.z);
-        g.w += hot_g(s.w);
-        h.x += (int32_t)(s.x & 0xffffu);
-        h.y += (int32_t)(s.y & 0xffffu);
-        h.z += (int32_t)(s.z & 0xffffu);
-        h.w += (int32_t)(s.w & 0xffffu);
-        g4[e] = g;
-        h4[e] = h;
-      }
-    }
-  }
+  if (!WIDE) fold_hot(hot, cold_g, cold_h, Bt);
   cluster_sync_all();
   const uint32_t rank = cluster_ctarank();
   const int per = n4 / (int)ncta;
@@ -508,7 +576,8 @@ size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide) {
   size_t warps = (size_t)threads / 32;
   size_t stage = warps * 64 * sizeof(uint4);
   size_t bins = (size_t)p.B * TILE;
-  if (quant) return (wide ? 0 : bins * 4) + bins * 8 + stage + warps * 32 * 4;
+  // the integer kernel's direct CTAs stage their rows over the (unused) shared histogram
+  if (quant) return std::max((wide ? 0 : bins * 4) + bins * 8, stage + warps * 32 * 4);
   if (p.const_hess) return bins * 12 + stage + warps * 32 * sizeof(float2);
   return bins * 16 + stage + warps * 32 * sizeof(float2);
 }

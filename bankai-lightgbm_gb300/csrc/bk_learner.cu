@@ -258,7 +258,7 @@ struct bk_learner {
     record_hist_event(4 * it + 1);
     // it clears the counter pair that split it + 1 uses; on the stable path its last CTA also
     // decides the split, otherwise the partition does
-    launch_search(jobs.data(), K, p, d_feat, stable ? -1 : (it + 1) & 1, stable, stream);
+    launch_search(jobs.data(), K, p, d_feat, stable ? -1 : (it + 1) & 1, stable, !stable && it > 0, stream);
     record_hist_event(4 * it + 2);
   }
   void step_b(int it) {

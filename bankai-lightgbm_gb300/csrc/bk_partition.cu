@@ -50,6 +50,7 @@ __device__ __forceinline__ Decision recorded_decision(const JobState* st) {
   d.depth = st->split_depth;
   d.sslot = st->split_sslot;
   d.new_leaf = st->new_leaf;
+  d.pslot = st->split_pslot;
   return d;
 }
 

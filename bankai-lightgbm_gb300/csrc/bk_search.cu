@@ -143,7 +143,30 @@ struct SearchIn {
   LeafConst C;
   LeafSum S0;
   int32_t sslot, lslot;
+  // the integer search's two pool entries of this thread (IntPool), loaded from the slots known
+  // before the wait; valid when those slots are the state's
+  int64_t sv, lv;
+  bool pre;
 };
+
+// The pool entries thread t of an integer search scans: the smaller leaf's bin t + 1 of feature
+// f (none at the most-frequent bin, which the fix rewrites) and, on side 1, the larger leaf's.
+struct IntPool {
+  int64_t sv, lv;
+};
+__device__ __forceinline__ IntPool int_pool(const Job& J, const Params& p, const DevFeature& m, int side, int32_t f,
+                                            int32_t sslot, int32_t lslot) {
+  const int t = threadIdx.x;
+  const size_t slot_stride = (size_t)p.T * p.B * TILE;
+  const size_t feat_off = (size_t)(f / TILE) * p.B * TILE + (f % TILE) + (size_t)(t + 1) * TILE;
+  const int64_t* pool = reinterpret_cast<const int64_t*>(J.pool);
+  const bool fix = m.mfb > 0;
+  const bool in = t < m.len;
+  IntPool r;
+  r.sv = (in && !(fix && t == m.mfb)) ? pool[(size_t)sslot * slot_stride + feat_off] : 0;
+  r.lv = (side && in) ? pool[(size_t)lslot * slot_stride + feat_off] : 0;
+  return r;
+}
 
 __device__ void cand_reset(Cand* c, int32_t real, int32_t inner) {
   c->gain = -CUDART_INF;
@@ -672,8 +695,8 @@ __device__ void search_int(const Job& J, const Params& p, const SearchIn& si, co
   const bool fix = m.mfb > 0;  // offset 0: the slice holds every bin and the most frequent one is empty
   const bool in = t < m.len;
   // the smaller leaf's most-frequent entry is rewritten by its side-0 CTA; side 1 never reads it
-  const int64_t sv = (in && !(fix && t == m.mfb)) ? hs[(size_t)(t + 1) * TILE] : 0;
-  const int64_t lv = (side && in) ? hl[(size_t)(t + 1) * TILE] : 0;
+  const IntPool pv = si.pre ? IntPool{si.sv, si.lv} : int_pool(J, p, m, side, f, si.sslot, si.lslot);
+  const int64_t sv = pv.sv, lv = pv.lv;
   const ScanGeom G = scan_geom(m);
   if (t < 2) sm.qn[t] = 0;
   const bool skip_t = G.skip && t + G.off == m.default_bin;
@@ -1397,28 +1420,41 @@ __device__ void search_cat(const Job& J, const Params& p, const SearchIn& si, co
 // has at most 64, so a CTA holds what a small-bin feature needs and four times as many CTAs fit
 // on an SM. Only NW = 8 takes categorical features and the stable path's last-CTA decision
 // (both use 256 threads); the host picks NW accordingly.
+// post: the histogram launch before this one applied a single-pass split's bookkeeping.
 template <bool PLAIN, bool QUANT, int NW>
 __global__ void __launch_bounds__(32 * NW) k_search(const JobTable jobs, Params p,
                                                     const DevFeature* __restrict__ feats, int clear_par,
-                                                    int decide) {
+                                                    int decide, int post) {
   __shared__ SearchSmemT<NW> sm;
   __shared__ int last;
   __shared__ Decision dec;
   const int side = (int)(blockIdx.x & 1u);
   const int f = (int)(blockIdx.x >> 1);
   const DevFeature m = feats[f];  // static: loaded while the histogram launch finishes
+  const Job& J = jobs.job[blockIdx.z];
+  JobState* st = J.st;
+  // The two leaves' pool slots, read while the histogram launch finishes: this launch starts only
+  // after every histogram CTA has passed its own wait, so the launches before that one are
+  // complete. After a single-pass split the smaller child takes the slot the decision recorded
+  // and the larger one keeps its parent's (split_pslot); otherwise the state's slots were written
+  // before the histogram launch started. The state's own slots, read after the wait, confirm them
+  // (a mismatch reloads); clamped, an early slot only ever addresses the pool.
+  int32_t pre_s = -1, pre_l = -1;
+  if (QUANT && !m.cat) {
+    pre_s = __ldcg(post ? &st->split_sslot : &st->smaller_slot);
+    pre_l = __ldcg(post ? &st->split_pslot : &st->larger_slot);
+  }
   griddep_wait();
   // the partition may be scheduled now: its CTAs read their static data while this search runs,
   // and wait for its completion before reading anything it writes
   griddep_launch();
-  const Job& J = jobs.job[blockIdx.z];
-  JobState* st = J.st;
   if (clear_par >= 0 && blockIdx.x == 0 && threadIdx.x < 2) {
     // the single-pass partition counter pair of the split after next: its last reader, the
     // histogram launch before this one, has finished
     st->pcnt[clear_par][threadIdx.x] = 0;
   }
-  // one round of independent loads: the state, the feature's flag and both leaves' constants
+  // one round of independent loads: the state, the feature's flag, both leaves' constants and
+  // (integer search) this thread's pool entries at the early slots
   const int32_t stop = st->stop, do_search = st->do_search;
   const int32_t leaf = side ? st->larger_leaf : st->smaller_leaf;
   const uint8_t used = J.used[f];
@@ -1427,6 +1463,14 @@ __global__ void __launch_bounds__(32 * NW) k_search(const JobTable jobs, Params 
   si.lslot = st->larger_slot;
   si.C = J.lconst[side];
   si.S0 = side ? J.lconst[0].ls : si.C.ls;
+  si.pre = false;
+  if (QUANT && !m.cat) {
+    const bool ok_s = (unsigned)pre_s < (unsigned)p.num_leaves, ok_l = (unsigned)pre_l < (unsigned)p.num_leaves;
+    const IntPool pv = int_pool(J, p, m, side, f, ok_s ? pre_s : 0, ok_l ? pre_l : 0);
+    si.sv = pv.sv;
+    si.lv = pv.lv;
+    si.pre = ok_s && pre_s == si.sslot && (side == 0 || (ok_l && pre_l == si.lslot));
+  }
   if (stop) return;  // uniform over the grid
   if (do_search && used && leaf >= 0) {  // uniform over the CTA
     if constexpr (NW == kSearchWarps) {
@@ -1508,7 +1552,7 @@ __global__ void __launch_bounds__(256) k_tree_begin(const Job* __restrict__ jobs
 }  // namespace
 
 void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFeature* feats, int clear_par,
-                   bool decide, cudaStream_t s) {
+                   bool decide, int post, cudaStream_t s) {
   const bool plain = !p.use_l1 && !p.use_max && !p.use_smooth;
   // 64-thread CTAs when every feature's slice fits in 63 bins (thread 63 holds the forward scan's
   // position -1), no feature is categorical and no CTA has to run the 256-thread decision
@@ -1518,17 +1562,17 @@ void launch_search(const Job* h_jobs, int num_jobs, const Params& p, const DevFe
     dim3 grid((unsigned)(2 * p.F), 1, nz);
     if (narrow) {
       const dim3 block(64);
-      if (p.quant) (void)launch_kernel(k_search<true, true, 2>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
-      else (void)launch_kernel(k_search<true, false, 2>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
+      if (p.quant) (void)launch_kernel(k_search<true, true, 2>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec, post);
+      else (void)launch_kernel(k_search<true, false, 2>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec, post);
       return;
     }
     const dim3 block(kSearchThreads);
     if (p.quant) {
-      if (plain) (void)launch_kernel(k_search<true, true, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
-      else (void)launch_kernel(k_search<false, true, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
+      if (plain) (void)launch_kernel(k_search<true, true, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec, post);
+      else (void)launch_kernel(k_search<false, true, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec, post);
     } else {
-      if (plain) (void)launch_kernel(k_search<true, false, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
-      else (void)launch_kernel(k_search<false, false, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec);
+      if (plain) (void)launch_kernel(k_search<true, false, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec, post);
+      else (void)launch_kernel(k_search<false, false, 8>, grid, block, 0, s, p.pdl, t, p, feats, clear_par, dec, post);
     }
   });
 }

@@ -193,7 +193,8 @@ def run_gpu(args, rank, world):
         shapes[(quant, loop_mode)] = learner.launch_shape()
         pin_g = torch.empty(n, dtype=torch.float32).pin_memory() if e2e else None
         pin_h = torch.empty(n, dtype=torch.float32).pin_memory() if e2e else None
-        stats = dict(hist_ms=0.0, hist_bytes=0.0, train_ms=0.0, search_ms=0.0, part_ms=0.0, leaves=0, loss=None)
+        stats = dict(hist_ms=0.0, hist_bytes=0.0, train_ms=0.0, search_ms=0.0, part_ms=0.0, leaves=0, loss=None,
+                     launches=[])
         total_ms = 0.0
         trees = []
 
@@ -234,6 +235,11 @@ def run_gpu(args, rank, world):
                 stats["search_ms"] += tm["search_ms"]
                 stats["part_ms"] += tm["partition_ms"]
                 stats["leaves"] += int(nls[0])
+                if timing:
+                    # per histogram launch: (rows of the leaf it builds, its CUDA-event ms)
+                    st = learner.last_step_timing()
+                    rows = _hist_launch_rows(splits[0, :nls[0] - 1], n, args.leaves)
+                    stats["launches"] += [(r, float(t)) for r, t in zip(rows, st[:, 0]) if t >= 0]
 
         for _ in range(warmup):
             step(False)
@@ -325,7 +331,8 @@ def run_gpu(args, rank, world):
                      "traffic_source": "ncu capture of one tree's 254 launches at 2M rows (DRAM bytes per "
                                        "algorithmic byte, %.3f) x this run's algorithmic bytes per launch"
                                        % HIST_TRAFFIC_PER_BYTE,
-                     "kernel": "k_hist_int (quantized histogram)", "peak_kind": peak_kind},
+                     "kernel": "k_hist_int (quantized histogram)", "peak_kind": peak_kind,
+                     "by_leaf_size": _roofline_by_leaf_size(roof["launches"], ds, n, peak)},
         "gpu_launches": launches_per_step * args.steps,
         "clocks": clk,
         "prep_s": round(prep_s, 1),
@@ -690,6 +697,45 @@ def _shape_dict(shape, tuned):
     return {"hist_min_rows_per_cta": shape[0], "hist_ctas_per_feature_tile": shape[1], "partition_ctas": shape[2],
             "hist_direct_atomic_rows_per_cta": shape[3], "hist_ctas_per_cluster": shape[4],
             "source": "bk_learner_autotune" if tuned else "default"}
+
+
+def _hist_launch_rows(splits, n, leaves, min_data=20):
+    """Rows each histogram launch of one tree builds: the root's n, then the smaller child of each
+    split when the children are searched (serial.rs:779-825: not when both have fewer than
+    2 x min_data_in_leaf rows), else 0; a tree that stopped early leaves its last launches at 0."""
+    rows = [n]
+    for r in splits:
+        lc, rc = int(r["left_count"]), int(r["right_count"])
+        rows.append(0 if (lc < 2 * min_data and rc < 2 * min_data) else min(lc, rc))
+    rows = rows[:leaves - 1]
+    return rows + [0] * (leaves - 1 - len(rows))
+
+
+def _roofline_by_leaf_size(launches, ds, n, peak):
+    """The histogram launches grouped by the rows they build: algorithmic GB/s (the learner's
+    per-row bytes: stored bins, a 4-bit tile's features half a byte; 2 packed bytes; 4 index bytes
+    when gathered; the pool slot's bytes) over their CUDA-event time, and its fraction of `peak`."""
+    feats = ds.features
+    bin_bytes = 0.0
+    for t0 in range(0, len(feats), 32):
+        tile = feats[t0:t0 + 32]
+        nib = all(fi.group_bins <= 16 for fi in tile)
+        bin_bytes += len(tile) * (0.5 if nib else 1.0)
+    slot = sum(fi.group_bins for fi in feats) * 8.0
+    edges = [(n, n + 1, "root"), (1_000_000, n, "1M+"), (100_000, 1_000_000, "100k-1M"), (10_000, 100_000, "10k-100k"),
+             (1, 10_000, "<10k")]
+    out = []
+    for lo, hi, name in edges:
+        sel = [(r, t) for r, t in launches if lo <= r < hi and (r == n) == (name == "root")]
+        if not sel:
+            continue
+        byt = sum(r * (bin_bytes + 2.0 + (0.0 if r == n else 4.0)) + slot for r, _ in sel)
+        ms = sum(t for _, t in sel)
+        gbs = byt / (ms * 1e6) if ms > 0 else None
+        out.append({"leaf_rows": name, "launches": len(sel), "mean_us": round(1000.0 * ms / len(sel), 1),
+                    "achieved_gbs": round(gbs, 1) if gbs else None,
+                    "frac": round(gbs / peak, 4) if gbs else None})
+    return out
 
 
 def aggregate_ranks(ms_per_step, world):
