@@ -123,17 +123,25 @@ struct RoundLoad {
   int32_t v;
 };
 
-__device__ __forceinline__ RoundLoad load_round_int(const uint8_t* tb, size_t rs, const Range& R, int64_t i, int32_t row,
-                                                    bool wide, bool half) {
+// The integer kernel's form, in 32-bit positions (a leaf has fewer than 2^31 rows, and a
+// lookahead position past the leaf's end stays below 2^32). `swap` (0 or 1) exchanges the two
+// 16-byte halves of a 32-byte run as they are loaded.
+__device__ __forceinline__ int32_t round_row32(const Range& R, uint32_t i, uint32_t r1) {
+  if (i >= r1) return -1;
+  return R.direct ? (int32_t)i : __ldg(R.idx + i);
+}
+
+__device__ __forceinline__ RoundLoad load_round_int(const uint8_t* tb, uint32_t rs, const Range& R, uint32_t i,
+                                                    int32_t row, bool wide, bool half, uint32_t swap) {
   RoundLoad L;
   L.a = make_uint4(0, 0, 0, 0);
   L.b = make_uint4(0, 0, 0, 0);
   L.v = 0;
   if (row >= 0) {
-    const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * rs);
-    L.a = __ldg(src);
-    if (!half) L.b = __ldg(src + 1);
-    int32_t pk = R.pk_row ? R.pk[row] : R.pk[i];
+    const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)(uint32_t)row * rs);
+    L.a = __ldg(src + swap);
+    if (!half) L.b = __ldg(src + (swap ^ 1u));
+    int32_t pk = R.pk[R.pk_row ? (uint32_t)row : i];
     int32_t gi = (int32_t)(int8_t)(pk >> 8);
     int32_t hi = pk & 0xff;
     L.v = wide ? ((gi & 0xffff) | (hi << 16)) : gi * 65536 + hi;
@@ -160,24 +168,38 @@ __device__ __forceinline__ unsigned long long pool_value(int32_t v) {
   return (unsigned long long)((int64_t)g * 4294967296LL + (int64_t)h);
 }
 
-// Adds a row's packed value to the (bin, feature) counter of the tile's shared histogram: the
-// 16:16 hot counter, or (WIDE) the 32-bit gradient and hessian counters.
+// Shared memory of the integer kernel. Hot form: one 256-byte row per bin holding the tile's 32
+// 16:16 hot counters and then its 32 cold (32-bit) gradient counters, followed by the cold
+// hessian counters [bin][32]. Wide form (no hot counters): the cold gradient counters
+// [bin][32], then the cold hessian ones. Feature f's counters sit in bank f either way. A CTA
+// that adds straight to the pool slot (direct) uses none of them and stages its rows over the
+// same bytes instead: 64 uint4 per warp, then 32 packed values per warp.
 template <bool WIDE>
-__device__ __forceinline__ void add_row(uint32_t* hot, int32_t* cold_g, int32_t* cold_h, uint32_t bin, int32_t v,
-                                        uint32_t f) {
-  if (WIDE) {
-    atomicAdd(&cold_g[bin * TILE + f], (int32_t)(int16_t)(v & 0xffff));
-    atomicAdd(&cold_h[bin * TILE + f], v >> 16);
-  } else {
-    atomicAdd(&hot[bin * TILE + f], (uint32_t)v);
-  }
+struct IntHist {
+  static constexpr int GS = WIDE ? TILE : 2 * TILE;  // words from one bin's counters to the next
+  unsigned char* base;
+  int Bt;
+  __device__ uint32_t* hot() const { return reinterpret_cast<uint32_t*>(base); }
+  __device__ int32_t* cold_g() const { return reinterpret_cast<int32_t*>(base) + (WIDE ? 0 : TILE); }
+  __device__ int32_t* cold_h() const { return reinterpret_cast<int32_t*>(base) + (size_t)Bt * GS; }
+};
+
+// Adds a row's packed value to the (bin, feature) counters of the wide form.
+__device__ __forceinline__ void add_wide(const IntHist<true>& H, uint32_t bin, int32_t v, uint32_t f) {
+  atomicAdd(&H.cold_g()[bin * TILE + f], (int32_t)(int16_t)(v & 0xffff));
+  atomicAdd(&H.cold_h()[bin * TILE + f], v >> 16);
 }
 
-// w[i] <- w[i ^ q] for q < N (N a power of two): one select per word and bit of q.
-template <int N>
+// Adds a row's packed value to the hot counter at byte offset (bin << 8) | 4 f.
+__device__ __forceinline__ void add_hot(unsigned char* base, uint32_t off, int32_t v) {
+  atomicAdd(reinterpret_cast<uint32_t*>(base + off), (uint32_t)v);
+}
+
+// w[i] <- w[i ^ (q & (2 TOP - 1))] (N a power of two, TOP <= N / 2): one select per word and bit.
+template <int N, int TOP = N / 2>
 __device__ __forceinline__ void xor_permute(uint32_t (&w)[N], uint32_t q) {
 #pragma unroll
-  for (int bit = N / 2; bit >= 1; bit >>= 1) {
+  for (int bit = TOP; bit >= 1; bit >>= 1) {
     const bool s = (q & (uint32_t)bit) != 0u;
     uint32_t t[N];
 #pragma unroll
@@ -191,13 +213,16 @@ __device__ __forceinline__ void xor_permute(uint32_t (&w)[N], uint32_t q) {
 // feature per step: at step k lane l takes feature k ^ l, so the 32 lanes of each atomic hit 32
 // different features — 32 different banks, whatever their bins — and no row is staged through
 // shared memory or broadcast. The run's words are first permuted by the lane's high feature bits
-// (a word index that varies by lane cannot be a register index), leaving a per-lane byte or
-// nibble choice at each step. A 16-byte run of 8-bit bins (at most 16 features) takes feature
-// (k ^ l) & 15 at step k < 16 (lanes l and l ^ 16 share a column). Features at or past nf, the
-// tile's feature count, get nothing. A lane without a row carries zeros.
+// (a word index that varies by lane cannot be a register index) and, for 8-bit bins, the bytes of
+// each word by its low bits, so step k finds its bin at a fixed position: one byte permute gives
+// bin << 8, and one logic op adds the feature's offset 4 (k ^ l) to make the hot counter's byte
+// offset. A 16-byte run of 8-bit bins (at most 16 features) takes feature (k ^ l) & 15 at step
+// k < 16 (lanes l and l ^ 16 share a column). Features at or past nf, the tile's feature count,
+// get nothing. A lane without a row carries zeros. The full 8-bit run arrives with its halves
+// already exchanged for lanes 16-31 (bit 2 of the word permutation).
 template <bool WIDE, bool NIBBLE>
-__device__ __forceinline__ void add_own_row(uint32_t* hot, int32_t* cold_g, int32_t* cold_h, const RoundLoad& L,
-                                            uint32_t lane, bool half, uint32_t nf) {
+__device__ __forceinline__ void add_own_row(const IntHist<WIDE>& H, const RoundLoad& L, uint32_t lane, bool half,
+                                            uint32_t nf) {
   const int32_t v = L.v;
   if (NIBBLE) {
     // 32 features in four words, feature f at bits 4 (f & 7) of word f >> 3
@@ -207,35 +232,63 @@ __device__ __forceinline__ void add_own_row(uint32_t* hot, int32_t* cold_g, int3
     for (int k = 0; k < 32; ++k) {
       const uint32_t f = (uint32_t)k ^ lane;
       const uint32_t bin = (w[k >> 3] >> ((((uint32_t)k & 7u) ^ (lane & 7u)) << 2)) & 15u;
-      if (f < nf) add_row<WIDE>(hot, cold_g, cold_h, bin, v, f);
+      if (f < nf) {
+        if constexpr (WIDE) add_wide(H, bin, v, f);
+        else add_hot(H.base, (bin << 8) | (f << 2), v);
+      }
     }
-  } else if (half) {
+    return;
+  }
+  // byte i of each word <- byte i ^ (lane & 3)
+  const uint32_t bsel = 0x3210u ^ ((lane & 3u) * 0x1111u);
+  if (half) {
     // at most 16 features in four words, feature f in byte f & 3 of word f >> 2
     uint32_t w[4] = {L.a.x, L.a.y, L.a.z, L.a.w};
     xor_permute<4>(w, (lane >> 2) & 3u);
 #pragma unroll
+    for (int i = 0; i < 4; ++i) w[i] = __byte_perm(w[i], 0u, bsel);
+    const uint32_t l4 = (lane & 15u) << 2;
+#pragma unroll
     for (int k = 0; k < 16; ++k) {
       const uint32_t f = ((uint32_t)k ^ lane) & 15u;
-      const uint32_t bin = __byte_perm(w[k >> 2], 0u, 0x4440u | (((uint32_t)k & 3u) ^ (lane & 3u)));
-      if (f < nf) add_row<WIDE>(hot, cold_g, cold_h, bin, v, f);
+      if (f < nf) {
+        if constexpr (WIDE) {
+          add_wide(H, __byte_perm(w[k >> 2], 0u, 0x4440u | (uint32_t)(k & 3)), v, f);
+        } else {
+          const uint32_t b8 = __byte_perm(w[k >> 2], 0u, 0x4404u | ((uint32_t)(k & 3) << 4));
+          add_hot(H.base, b8 | (l4 ^ ((uint32_t)k << 2)), v);
+        }
+      }
+    }
+    return;
+  }
+  // 32 features in eight words, feature f in byte f & 3 of word f >> 2
+  uint32_t w[8] = {L.a.x, L.a.y, L.a.z, L.a.w, L.b.x, L.b.y, L.b.z, L.b.w};
+  xor_permute<8, 2>(w, lane >> 2);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) w[i] = __byte_perm(w[i], 0u, bsel);
+  const uint32_t l4 = lane << 2;
+  if (nf >= 32u) {
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      if constexpr (WIDE) {
+        add_wide(H, __byte_perm(w[k >> 2], 0u, 0x4440u | (uint32_t)(k & 3)), v, (uint32_t)k ^ lane);
+      } else {
+        const uint32_t b8 = __byte_perm(w[k >> 2], 0u, 0x4404u | ((uint32_t)(k & 3) << 4));
+        add_hot(H.base, b8 | (l4 ^ ((uint32_t)k << 2)), v);
+      }
     }
   } else {
-    // 32 features in eight words, feature f in byte f & 3 of word f >> 2
-    uint32_t w[8] = {L.a.x, L.a.y, L.a.z, L.a.w, L.b.x, L.b.y, L.b.z, L.b.w};
-    xor_permute<8>(w, lane >> 2);
-    if (nf >= 32u) {
 #pragma unroll
-      for (int k = 0; k < 32; ++k) {
-        const uint32_t f = (uint32_t)k ^ lane;
-        const uint32_t bin = __byte_perm(w[k >> 2], 0u, 0x4440u | (((uint32_t)k & 3u) ^ (lane & 3u)));
-        add_row<WIDE>(hot, cold_g, cold_h, bin, v, f);
-      }
-    } else {
-#pragma unroll
-      for (int k = 0; k < 32; ++k) {
-        const uint32_t f = (uint32_t)k ^ lane;
-        const uint32_t bin = __byte_perm(w[k >> 2], 0u, 0x4440u | (((uint32_t)k & 3u) ^ (lane & 3u)));
-        if (f < nf) add_row<WIDE>(hot, cold_g, cold_h, bin, v, f);
+    for (int k = 0; k < 32; ++k) {
+      const uint32_t f = (uint32_t)k ^ lane;
+      if (f < nf) {
+        if constexpr (WIDE) {
+          add_wide(H, __byte_perm(w[k >> 2], 0u, 0x4440u | (uint32_t)(k & 3)), v, f);
+        } else {
+          const uint32_t b8 = __byte_perm(w[k >> 2], 0u, 0x4404u | ((uint32_t)(k & 3) << 4));
+          add_hot(H.base, b8 | (l4 ^ ((uint32_t)k << 2)), v);
+        }
       }
     }
   }
@@ -243,14 +296,16 @@ __device__ __forceinline__ void add_own_row(uint32_t* hot, int32_t* cold_g, int3
 
 // Folds the hot counters into the cold ones and clears them. Every thread of the CTA calls it
 // between barriers.
-__device__ __forceinline__ void fold_hot(uint32_t* hot, int32_t* cold_g, int32_t* cold_h, int Bt) {
-  uint4* hot4 = reinterpret_cast<uint4*>(hot);
-  int4* g4 = reinterpret_cast<int4*>(cold_g);
-  int4* h4 = reinterpret_cast<int4*>(cold_h);
-  for (int e = threadIdx.x; e < Bt * TILE / 4; e += blockDim.x) {
-    const uint4 s = hot4[e];
+__device__ __forceinline__ void fold_hot(const IntHist<false>& H) {
+  uint4* row4 = reinterpret_cast<uint4*>(H.base);   // 16 per bin: 8 hot, then 8 cold gradient
+  int4* h4 = reinterpret_cast<int4*>(H.cold_h());  // 8 per bin
+  for (int e = threadIdx.x; e < H.Bt * (TILE / 4); e += blockDim.x) {
+    const int b = e >> 3, q = e & 7;
+    uint4* hp = row4 + b * 16 + q;
+    const uint4 s = *hp;
     if (s.x | s.y | s.z | s.w) {
-      int4 g = g4[e], h = h4[e];
+      int4* gp = reinterpret_cast<int4*>(hp + 8);
+      int4 g = *gp, h = h4[e];
       g.x += hot_g(s.x);
       g.y += hot_g(s.y);
       g.z += hot_g(s.z);
@@ -259,18 +314,12 @@ __device__ __forceinline__ void fold_hot(uint32_t* hot, int32_t* cold_g, int32_t
       h.y += (int32_t)(s.y & 0xffffu);
       h.z += (int32_t)(s.z & 0xffffu);
       h.w += (int32_t)(s.w & 0xffffu);
-      g4[e] = g;
+      *gp = g;
       h4[e] = h;
-      hot4[e] = make_uint4(0, 0, 0, 0);
+      *hp = make_uint4(0, 0, 0, 0);
     }
   }
 }
-
-// Shared memory of the integer kernel: the hot counters [bin][32] (none when WIDE), then the
-// 32-bit gradient and hessian counters [bin][32] each. A CTA that adds straight to the pool slot
-// (direct) uses none of them, and stages its rows over the same bytes instead: 64 uint4 per warp,
-// then 32 packed values per warp.
-__device__ __forceinline__ size_t hist_int_hot_words(int Bt, bool wide) { return wide ? 0 : (size_t)Bt * TILE; }
 
 // The row loop of one integer-histogram CTA: with DIRECT every (row, feature) goes to the pool
 // slot by a global atomic, otherwise to the CTA's shared histogram (the hot counters folded into
@@ -284,29 +333,31 @@ __device__ __forceinline__ void hist_int_loop(const Params& p, const Range& R, c
   const int Bt = geo.bins;
   const bool half = geo.width == 16;  // one 16-byte run per row
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nwarps = blockDim.x >> 5;
-  uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
-  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + hist_int_hot_words(Bt, WIDE));
-  int32_t* cold_h = cold_g + Bt * TILE;
+  const IntHist<WIDE> H{smem, Bt};
   uint4* my_stage = reinterpret_cast<uint4*>(smem) + warp * 64;
   int32_t* my_v = reinterpret_cast<int32_t*>(reinterpret_cast<uint4*>(smem) + nwarps * 64) + warp * 32;
   const uint8_t* sb = reinterpret_cast<const uint8_t*>(my_stage);
   // lanes / features past the last feature of the last tile (padding) add nothing
   const uint32_t tile_feats = (uint32_t)min(TILE, p.F - tile * TILE);
   const bool feat_lane = (uint32_t)lane < tile_feats;
-  const int64_t per_round = (int64_t)TILE * nwarps;
-  const int64_t rounds = ceil_div64(R.r1 - R.r0, per_round);
+  const uint32_t r0 = (uint32_t)R.r0, r1 = (uint32_t)R.r1;
+  const uint32_t per_round = (uint32_t)(TILE * nwarps);
+  const uint32_t rounds = (r1 - r0 + per_round - 1u) / per_round;
+  const uint32_t rs32 = (uint32_t)rs;
+  // the full 8-bit path loads lanes 16-31's runs with their halves exchanged
+  const uint32_t swap = (!DIRECT && !NIBBLE && !half) ? ((uint32_t)lane >> 4) & 1u : 0u;
   // software pipeline: the next round's runs and the round after's row indices are in flight
-  // while this round is added up
-  const int64_t first = R.r0 + (int64_t)warp * TILE + lane;
-  RoundLoad cur = load_round_int(tb, rs, R, first, round_row(R, first), WIDE, half);
-  int32_t row_nxt = round_row(R, first + per_round);
+  // while this round is added up; `pos` is this lane's row position in the current round
+  uint32_t pos = r0 + (uint32_t)(warp * TILE + lane);
+  RoundLoad cur = load_round_int(tb, rs32, R, pos, round_row32(R, pos, r1), WIDE, half, swap);
+  int32_t row_nxt = round_row32(R, pos + per_round, r1);
   int until_flush = flush_rounds;
-  for (int64_t rd = 0; rd < rounds; ++rd) {
-    const int64_t base = R.r0 + rd * per_round + (int64_t)warp * TILE;
-    const int32_t row_nn = round_row(R, base + 2 * per_round + lane);
-    RoundLoad nxt = load_round_int(tb, rs, R, base + per_round + lane, row_nxt, WIDE, half);
+  for (uint32_t rd = 0; rd < rounds; ++rd, pos += per_round) {
+    const int32_t row_nn = round_row32(R, pos + 2u * per_round, r1);
+    RoundLoad nxt = load_round_int(tb, rs32, R, pos + per_round, row_nxt, WIDE, half, swap);
     row_nxt = row_nn;
-    if (base < R.r1) {
+    const uint32_t base = pos - (uint32_t)lane;  // the warp's first row position of the round
+    if (base < r1) {
       if (DIRECT) {
         // global atomics: the round's rows are staged so that each atomic covers one row's 32
         // features, 32 consecutive pool entries
@@ -314,7 +365,7 @@ __device__ __forceinline__ void hist_int_loop(const Params& p, const Range& R, c
         if (!half) my_stage[lane * 2 + 1] = cur.b;
         my_v[lane] = cur.v;
         __syncwarp();
-        const int jn = (int)min((int64_t)32, R.r1 - base);  // warp-uniform
+        const int jn = (int)min(32u, r1 - base);  // warp-uniform
         for (int j = 0; j < jn; ++j) {
           const uint32_t b0 = staged_bin<NIBBLE>(sb, j, lane);
           const int32_t v0 = my_v[j];
@@ -322,15 +373,17 @@ __device__ __forceinline__ void hist_int_loop(const Params& p, const Range& R, c
         }
         __syncwarp();
       } else {
-        add_own_row<WIDE, NIBBLE>(hot, cold_g, cold_h, cur, (uint32_t)lane, half, tile_feats);
+        add_own_row<WIDE, NIBBLE>(H, cur, (uint32_t)lane, half, tile_feats);
       }
     }
     cur = nxt;
-    if (!WIDE && !DIRECT && --until_flush == 0 && rd + 1 < rounds) {
-      until_flush = flush_rounds;
-      __syncthreads();
-      fold_hot(hot, cold_g, cold_h, Bt);
-      __syncthreads();
+    if constexpr (!WIDE && !DIRECT) {
+      if (--until_flush == 0 && rd + 1 < rounds) {
+        until_flush = flush_rounds;
+        __syncthreads();
+        fold_hot(H);
+        __syncthreads();
+      }
     }
   }
 }
@@ -343,9 +396,7 @@ __device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, con
                                               int flush_rounds, int direct_rows, bool in_cluster, unsigned char* smem) {
   const int tile = blockIdx.y;
   const int Bt = geo.bins;
-  uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
-  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + hist_int_hot_words(Bt, WIDE));
-  int32_t* cold_h = cold_g + Bt * TILE;
+  const IntHist<WIDE> H{smem, Bt};
   unsigned long long* slot = reinterpret_cast<unsigned long long*>(J.pool) +
                              ((size_t)R.slot * p.T + tile) * (size_t)p.B * TILE;
   // uniform over the CTA; a CTA of a cluster always adds through its shared histogram
@@ -363,9 +414,10 @@ __device__ __forceinline__ void hist_int_rows(const Job& J, const Params& p, con
   if (in_cluster) return;  // a cluster flushes its CTAs' histograms together
   __syncthreads();
   for (int e = threadIdx.x; e < Bt * TILE; e += blockDim.x) {
-    int32_t gg = cold_g[e], hh = cold_h[e];
+    const int gi = (e >> 5) * IntHist<WIDE>::GS + (e & (TILE - 1));  // (bin, feature) in the row layout
+    int32_t gg = H.cold_g()[gi], hh = H.cold_h()[e];
     if (!WIDE) {
-      const uint32_t s = hot[e];
+      const uint32_t s = H.hot()[gi];
       gg += hot_g(s);
       hh += (int32_t)(s & 0xffffu);
     }
@@ -387,19 +439,19 @@ template <bool WIDE>
 __device__ __forceinline__ void hist_cluster_flush(const Params& p, const TileGeom& geo, unsigned long long* slot,
                                                    uint32_t ncta, unsigned char* smem) {
   const int Bt = geo.bins;
-  uint32_t* hot = reinterpret_cast<uint32_t*>(smem);
-  int32_t* cold_g = reinterpret_cast<int32_t*>(hot + hist_int_hot_words(Bt, WIDE));
-  int32_t* cold_h = cold_g + Bt * TILE;
+  const IntHist<WIDE> H{smem, Bt};
   const int n4 = Bt * TILE / 4;  // int4 groups of the tile's bins: a multiple of 64 (Bt a multiple of 8)
   __syncthreads();
-  if (!WIDE) fold_hot(hot, cold_g, cold_h, Bt);
+  if constexpr (!WIDE) fold_hot(H);
   cluster_sync_all();
   const uint32_t rank = cluster_ctarank();
   const int per = n4 / (int)ncta;
   for (int e = (int)rank * per + threadIdx.x; e < ((int)rank + 1) * per; e += blockDim.x) {
     int4 g = make_int4(0, 0, 0, 0), h = make_int4(0, 0, 0, 0);
     for (uint32_t q = 0; q < ncta; ++q) {
-      const int4 a = ld_dsmem_v4(cold_g + 4 * e, q), b = ld_dsmem_v4(cold_h + 4 * e, q);
+      // int4 group e = (bin e >> 3, features 4 (e & 7) ..)
+      const int4 a = ld_dsmem_v4(H.cold_g() + (e >> 3) * IntHist<WIDE>::GS + 4 * (e & 7), q);
+      const int4 b = ld_dsmem_v4(H.cold_h() + 4 * e, q);
       g.x += a.x;
       g.y += a.y;
       g.z += a.z;
