@@ -3,20 +3,20 @@
 // Grid: (blocks_per_tile, T, jobs). Each CTA owns one 32-feature tile and one contiguous chunk
 // of the leaf's rows. A warp takes 32 rows at a time: every lane fetches its row's run of the
 // tile (32 bytes of 8-bit bins, or 16 bytes of 4-bit bins) with 128-bit loads. The CTA-private
-// shared histogram is laid out [bin][feature], so feature f's counters all sit in bank f. The
-// integer kernel adds every lane's own row feature by feature, lane l taking feature k ^ l at
-// step k: the 32 lanes of each shared atomic hit 32 different features, 32 different banks, and
-// no row passes through shared memory. The float kernel stages the runs in shared memory and
-// then, row by row, lane f adds that row's statistics to bin[row][f]. Either way the atomics of
-// a warp never conflict and never collide. At the end the CTA adds its
-// non-zero bins to the leaf's slot in the histogram pool with global atomics (the pool slot is
-// zeroed when the tree starts). Only the tile's own bins (its largest feature's group bins) are
-// zeroed and flushed.
+// shared histogram keeps feature f's counters of every bin in bank f. Every lane adds its own
+// row feature by feature, lane l taking feature k ^ l at step k: the 32 lanes of each shared
+// atomic hit 32 different features, 32 different banks, so they never conflict and never
+// collide, and no row passes through shared memory. At the end the CTA adds its non-zero bins to
+// the leaf's slot in the histogram pool with global atomics (the pool slot is zeroed when the
+// tree starts). Only the tile's own bins (its largest feature's group bins) are zeroed and
+// flushed.
 //
-// A quantized CTA with few rows (at most `direct_rows`) skips the shared histogram: each
-// (row, feature) is added to the pool slot with one global 64-bit atomic as it is read, which
-// saves the CTA's zeroing, barrier and flush pass (with so few rows nearly every bin would be
-// flushed anyway). Integer sums do not depend on the order, so both forms give the same slot.
+// A quantized CTA with few rows (at most `direct_rows`) skips the shared histogram: it stages
+// each warp's 32 rows in shared memory and adds every (row, feature) to the pool slot with one
+// global 64-bit atomic, lane = feature, so each atomic instruction covers 32 consecutive pool
+// entries. That saves the CTA's zeroing, barrier and flush pass (with so few rows nearly every
+// bin would be flushed anyway). Integer sums do not depend on the order, so both forms give the
+// same slot.
 //
 // Quantized path: the packed int8 gradient / uint8 hessian of a row is added as one 32-bit
 // value (grad << 16) + hess into a 16:16 "hot" histogram, which is folded into 32-bit
@@ -113,19 +113,15 @@ __device__ __forceinline__ int cta_range(const Job& J, const Params& p, int bloc
 // The rows of a warp's round are fetched in two stages, each one round ahead of its use: the row
 // index (a coalesced load of the leaf's index range, two rounds ahead) and then the row's 32-byte
 // tile sector and packed value (one round ahead), so no gather waits on an index load.
-__device__ __forceinline__ int32_t round_row(const Range& R, int64_t i) {
-  if (i >= R.r1) return -1;
-  return R.direct ? (int32_t)i : __ldg(R.idx + i);
-}
 
 struct RoundLoad {
   uint4 a, b;
   int32_t v;
 };
 
-// The integer kernel's form, in 32-bit positions (a leaf has fewer than 2^31 rows, and a
-// lookahead position past the leaf's end stays below 2^32). `swap` (0 or 1) exchanges the two
-// 16-byte halves of a 32-byte run as they are loaded.
+// Positions are 32-bit: a leaf has fewer than 2^31 rows, and a lookahead position past the
+// leaf's end stays below 2^32. `swap` (0 or 1) exchanges the two 16-byte halves of a 32-byte run
+// as they are loaded.
 __device__ __forceinline__ int32_t round_row32(const Range& R, uint32_t i, uint32_t r1) {
   if (i >= r1) return -1;
   return R.direct ? (int32_t)i : __ldg(R.idx + i);
@@ -506,6 +502,67 @@ __global__ void __launch_bounds__(1024, 1)
   }
 }
 
+// Adds one row's gradient (and hessian) to the fp32 (hi, lo) pairs of bin `e`: hi takes the
+// value by atomicAdd, which returns the previous sum, and lo the exact rounding error of that
+// addition (TwoSum); with a constant hessian the hessian slot counts rows.
+template <bool CONST_HESS>
+__device__ __forceinline__ void add_float(float* ghi, float* glo, float* hhi, float* hlo, uint32_t e, float2 v) {
+  const float old = atomicAdd(&ghi[e], v.x);
+  const float err = two_sum_err(old, v.x, __fadd_rn(old, v.x));
+  if (err != 0.f) atomicAdd(&glo[e], err);
+  if (CONST_HESS) {
+    atomicAdd(reinterpret_cast<uint32_t*>(hhi) + e, 1u);
+  } else {
+    const float oh = atomicAdd(&hhi[e], v.y);
+    const float eh = two_sum_err(oh, v.y, __fadd_rn(oh, v.y));
+    if (eh != 0.f) atomicAdd(&hlo[e], eh);
+  }
+}
+
+// The float kernel's form of add_own_row: every lane with a row adds it, feature k ^ lane at
+// step k (32 different banks per atomic), from its run permuted once per row so that each step's
+// bin sits at a fixed position. The full 8-bit run arrives with its halves already exchanged for
+// lanes 16-31.
+template <bool CONST_HESS, bool NIBBLE>
+__device__ __forceinline__ void add_own_row_float(float* ghi, float* glo, float* hhi, float* hlo, const uint4& a,
+                                                  const uint4& b, float2 v, uint32_t lane, bool half, uint32_t nf) {
+  if (NIBBLE) {
+    uint32_t w[4] = {a.x, a.y, a.z, a.w};
+    xor_permute<4>(w, (lane >> 3) & 3u);
+#pragma unroll
+    for (int k = 0; k < 32; ++k) {
+      const uint32_t f = (uint32_t)k ^ lane;
+      const uint32_t bin = (w[k >> 3] >> ((((uint32_t)k & 7u) ^ (lane & 7u)) << 2)) & 15u;
+      if (f < nf) add_float<CONST_HESS>(ghi, glo, hhi, hlo, bin * TILE + f, v);
+    }
+    return;
+  }
+  const uint32_t bsel = 0x3210u ^ ((lane & 3u) * 0x1111u);  // byte i of each word <- byte i ^ (lane & 3)
+  if (half) {
+    uint32_t w[4] = {a.x, a.y, a.z, a.w};
+    xor_permute<4>(w, (lane >> 2) & 3u);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w[i] = __byte_perm(w[i], 0u, bsel);
+#pragma unroll
+    for (int k = 0; k < 16; ++k) {
+      const uint32_t f = ((uint32_t)k ^ lane) & 15u;
+      const uint32_t bin = __byte_perm(w[k >> 2], 0u, 0x4440u | (uint32_t)(k & 3));
+      if (f < nf) add_float<CONST_HESS>(ghi, glo, hhi, hlo, bin * TILE + f, v);
+    }
+    return;
+  }
+  uint32_t w[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+  xor_permute<8, 2>(w, lane >> 2);
+#pragma unroll
+  for (int i = 0; i < 8; ++i) w[i] = __byte_perm(w[i], 0u, bsel);
+#pragma unroll
+  for (int k = 0; k < 32; ++k) {
+    const uint32_t f = (uint32_t)k ^ lane;
+    const uint32_t bin = __byte_perm(w[k >> 2], 0u, 0x4440u | (uint32_t)(k & 3));
+    if (f < nf) add_float<CONST_HESS>(ghi, glo, hhi, hlo, bin * TILE + f, v);
+  }
+}
+
 // The rows and flush of one float-histogram CTA, its range known (NIBBLE: the tile holds 4-bit
 // bins).
 template <bool CONST_HESS, bool NIBBLE>
@@ -520,69 +577,47 @@ __device__ __forceinline__ void hist_float_rows(const Job& J, const Params& p, c
   float* glo = ghi + B * TILE;
   float* hhi = glo + B * TILE;  // CONST_HESS: uint32 row counts
   float* hlo = hhi + B * TILE;  // unused with CONST_HESS
-  uint4* stage = reinterpret_cast<uint4*>(CONST_HESS ? hlo : hlo + B * TILE);
-  float2* stage_v = reinterpret_cast<float2*>(stage + nwarps * 64);
   uint32_t* hcnt = reinterpret_cast<uint32_t*>(hhi);
   __syncthreads();
   // the tile's run of row 0 and the row stride, in the copy that suits the leaf's density
   const bool dense = R.count * 4 >= p.n;
   const uint8_t* tb = dense ? bins_tm + geo.tm_off : bins_rt + geo.rt_off;
-  const size_t rs = dense ? (size_t)tile_width(geo) : (size_t)p.rt_stride;
-  const bool feat_lane = tile * TILE + lane < p.F;
+  const uint32_t rs = dense ? (uint32_t)tile_width(geo) : (uint32_t)p.rt_stride;
+  const uint32_t tile_feats = (uint32_t)min(TILE, p.F - tile * TILE);
   const float* G = J.g;
   const float* H = J.h;
-  const int64_t per_round = (int64_t)TILE * nwarps;
+  const uint32_t r0 = (uint32_t)R.r0, r1 = (uint32_t)R.r1;
+  const uint32_t per_round = (uint32_t)(TILE * nwarps);
+  // the full 8-bit path loads lanes 16-31's runs with their halves exchanged
+  const uint32_t swap = (!NIBBLE && !half) ? ((uint32_t)lane >> 4) & 1u : 0u;
   // the same two-stage software pipeline as the integer kernel
   auto load = [&](int32_t row, uint4& a, uint4& b, float2& v) {
     a = make_uint4(0, 0, 0, 0);
     b = make_uint4(0, 0, 0, 0);
     v = make_float2(0.f, 0.f);
     if (row >= 0) {
-      const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)row * rs);
-      a = __ldg(src);
-      if (!half) b = __ldg(src + 1);
+      const uint4* src = reinterpret_cast<const uint4*>(tb + (size_t)(uint32_t)row * rs);
+      a = __ldg(src + swap);
+      if (!half) b = __ldg(src + (swap ^ 1u));
       v.x = G[row];
       if (!CONST_HESS) v.y = H[row];
     }
   };
-  const int64_t first = R.r0 + (int64_t)warp * TILE + lane;
+  uint32_t pos = r0 + (uint32_t)(warp * TILE + lane);
   uint4 ca, cb;
   float2 cv;
-  load(round_row(R, first), ca, cb, cv);
-  int32_t row_nxt = round_row(R, first + per_round);
-  for (int64_t base = R.r0 + (int64_t)warp * TILE; base < R.r1; base += per_round) {
-    const int32_t row_nn = round_row(R, base + 2 * per_round + lane);
+  load(round_row32(R, pos, r1), ca, cb, cv);
+  int32_t row_nxt = round_row32(R, pos + per_round, r1);
+  for (; pos - (uint32_t)lane < r1; pos += per_round) {
+    const int32_t row_nn = round_row32(R, pos + 2u * per_round, r1);
     uint4 na, nb;
     float2 nv;
     load(row_nxt, na, nb, nv);
     row_nxt = row_nn;
-    stage[(warp * 32 + lane) * 2] = ca;
-    stage[(warp * 32 + lane) * 2 + 1] = cb;
-    stage_v[warp * 32 + lane] = cv;
+    if (pos < r1) add_own_row_float<CONST_HESS, NIBBLE>(ghi, glo, hhi, hlo, ca, cb, cv, (uint32_t)lane, half, tile_feats);
     ca = na;
     cb = nb;
     cv = nv;
-    __syncwarp();
-    const uint8_t* sb = reinterpret_cast<const uint8_t*>(stage + warp * 64);
-    const int jn = (int)min((int64_t)32, R.r1 - base);  // warp-uniform; padding lanes add nothing
-#pragma unroll 4
-    for (int j = 0; j < jn; ++j) {
-      uint32_t e = staged_bin<NIBBLE>(sb, j, lane) * TILE + lane;
-      float2 vv = stage_v[warp * 32 + j];
-      if (feat_lane) {
-        float old = atomicAdd(&ghi[e], vv.x);
-        float err = two_sum_err(old, vv.x, __fadd_rn(old, vv.x));
-        if (err != 0.f) atomicAdd(&glo[e], err);
-        if (CONST_HESS) {
-          atomicAdd(&hcnt[e], 1u);
-        } else {
-          float oh = atomicAdd(&hhi[e], vv.y);
-          float eh = two_sum_err(oh, vv.y, __fadd_rn(oh, vv.y));
-          if (eh != 0.f) atomicAdd(&hlo[e], eh);
-        }
-      }
-    }
-    __syncwarp();
   }
   __syncthreads();
   double2* slot = reinterpret_cast<double2*>(J.pool) + ((size_t)R.slot * p.T + tile) * (size_t)p.B * TILE;
@@ -630,8 +665,8 @@ size_t hist_smem_bytes(const Params& p, int threads, bool quant, bool wide) {
   size_t bins = (size_t)p.B * TILE;
   // the integer kernel's direct CTAs stage their rows over the (unused) shared histogram
   if (quant) return std::max((wide ? 0 : bins * 4) + bins * 8, stage + warps * 32 * 4);
-  if (p.const_hess) return bins * 12 + stage + warps * 32 * sizeof(float2);
-  return bins * 16 + stage + warps * 32 * sizeof(float2);
+  if (p.const_hess) return bins * 12;
+  return bins * 16;
 }
 
 void launch_hist(const Job* h_jobs, int num_jobs, const Params& p, const uint8_t* bins_rt, const uint8_t* bins_tm,
