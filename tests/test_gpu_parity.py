@@ -87,6 +87,9 @@ QUANT_CASES = [
     dict(num_leaves=15, stochastic_rounding=1, num_grad_quant_bins=16, lambda_l1=0.5, min_data_in_leaf=5),
     dict(num_leaves=31, stochastic_rounding=1, num_grad_quant_bins=6, max_delta_step=0.7, path_smooth=2.0),
     dict(num_leaves=31, stochastic_rounding=1, num_grad_quant_bins=4, quant_train_renew_leaf=1, max_depth=5),
+    # 64 gradient bins: a 16:16 counter could overflow within one round of rows, so the histogram
+    # kernel takes its wide form (32-bit gradient and hessian counters, no hot counters)
+    dict(num_leaves=31, stochastic_rounding=1, num_grad_quant_bins=64),
 ]
 
 
@@ -443,13 +446,14 @@ def test_bynode_column_sample(bytree, bynode, constrained):
     gpu.close()
 
 
-@pytest.mark.parametrize("quant", [1, 0])
-def test_packed_bin_tiles(quant):
+@pytest.mark.parametrize("quant,grad_bins", [(1, 4), (1, 64), (0, 4)])
+def test_packed_bin_tiles(quant, grad_bins):
     """Stored-bin tiles of every layout in one dataset: 32 features of at most 16 group bins (a
     4-bit tile, two bins per byte as io/bin_data.rs:20-30 stores them), 32 features of 8-bit bins
     and a last tile of 8 features (a 16-byte 8-bit run): the quantized trees equal the oracle's bit
-    for bit, with shared-histogram and global-atomic histogram CTAs; the float trees agree within
-    the float tolerance."""
+    for bit, with shared-histogram and global-atomic histogram CTAs, in the histogram kernel's
+    16:16 form (4 gradient bins) and its wide form (64); the float trees agree within the float
+    tolerance."""
     from lgbm_gb300 import BinnedDataset
     rng = np.random.default_rng(31)
     n, F = 40000, 72
@@ -461,7 +465,8 @@ def test_packed_bin_tiles(quant):
     gb = [fi.group_bins for fi in ds.features]
     assert len(gb) == F and max(gb[:32]) <= 16 and max(gb[32:64]) > 16
     g, h, const = _grads(z, "binary", seed=32)
-    cfg = dict(num_leaves=31, use_quantized_grad=quant, stochastic_rounding=1, seed=3, num_threads=2)
+    cfg = dict(num_leaves=31, use_quantized_grad=quant, stochastic_rounding=1, seed=3, num_threads=2,
+               num_grad_quant_bins=grad_bins)
     shapes = [(256, 38, 304, 0), (64, 20, 64, 1 << 30), (128, 38, 64, 0, 4)] if quant else [(256, 38, 304, 0)]
     for shape in shapes:
         for loop_mode in (1, 0):
